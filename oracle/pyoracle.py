@@ -1,0 +1,303 @@
+"""ORACLE — test infrastructure only.
+
+ctypes wrapper over the two CPU implementations of the move-and-overlap path:
+
+* ``liboracle.so`` — this project's C++ restatement (oracle/rpo_*.hpp), portable;
+* ``_ref/librpref.so`` — the reference's own sources compiled in place by
+  ``make -C oracle ref`` (only where the reference checkout is present).
+
+Both export the same entry points (``rpo_*`` / ``ref_*``), so one Python class
+drives either.  Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU
+baseline import this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "librpref.so")
+REFERENCE_DIR = "/root/reference"
+
+SPHERE, SPHEROCYLINDER, POLYSPHERE = 0, 1, 2
+
+MOVE_DTYPE = np.dtype([
+    ("particle", "<i4"), ("type", "<i4"), ("domain", "<i4"), ("reserved", "<i4"),
+    ("translation", "<f8", (3,)), ("rotation", "<f8", (9,)), ("uniform", "<f8"),
+])
+assert MOVE_DTYPE.itemsize == 120
+
+
+class SimParams(C.Structure):
+    _fields_ = [("temperature", C.c_double), ("pressure", C.c_double),
+                ("translation_step", C.c_double), ("rotation_step", C.c_double),
+                ("box_kind", C.c_int32), ("adjust_steps", C.c_int32), ("box_step", C.c_double),
+                ("domains", C.c_int64 * 3), ("seed", C.c_uint64), ("threads", C.c_int64)]
+
+
+class SimStats(C.Structure):
+    _fields_ = [("moves", C.c_int64 * 2), ("accepted", C.c_int64 * 2),
+                ("scalings", C.c_int64), ("scalings_accepted", C.c_int64), ("cycles", C.c_int64),
+                ("domains", C.c_int64 * 3),
+                ("move_us", C.c_double), ("scaling_us", C.c_double), ("total_us", C.c_double),
+                ("steps", C.c_double * 2), ("box_step", C.c_double)]
+
+
+def build(reference: bool = False) -> None:
+    """Compiles liboracle.so (and the reference library when asked and possible)."""
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    if reference and os.path.isdir(os.path.join(REFERENCE_DIR, "src")):
+        subprocess.run(["make", "-s", "-j", str(os.cpu_count() or 4), "-C", HERE, "ref"], check=True)
+
+
+def reference_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+_LIBS: dict = {}
+
+_P = C.c_void_p
+_D = C.POINTER(C.c_double)
+_I64 = C.POINTER(C.c_int64)
+
+
+def _lib(which: str):
+    if which in _LIBS:
+        return _LIBS[which]
+    path, pre = (ORACLE_SO, "rpo_") if which == "oracle" else (REF_SO, "ref_")
+    if not os.path.exists(path):
+        raise FileNotFoundError(path)
+    lib = C.CDLL(path)
+    sig = {
+        "create": (_P, [C.c_int, _D, C.c_int, C.c_int64, _D, _D, _D, C.c_int]),
+        "destroy": (None, [_P]),
+        "count_overlaps": (C.c_int64, [_P, C.c_int]),
+        "set_counting": (None, [_P, C.c_int]),
+        "cached_overlaps": (C.c_int64, [_P]),
+        "replay": (C.c_int, [_P, _P, C.c_int64, _D, C.c_double, _P, _P]),
+        "try_scaling": (C.c_double, [_P, _D]),
+        "revert_scaling": (None, [_P]),
+        "get_state": (None, [_P, _D, _D, _D]),
+        "ng_divisions": (C.c_int, [_P, _I64]),
+        "pair_overlap": (C.c_int, [C.c_int, _D, C.c_int, _D, _D, C.c_int, _D, _D, C.c_int, C.c_int, _D, _D]),
+        "box_info": (None, [_D, _D, _D, _D]),
+        "rotation": (None, [_D, C.c_double, _D]),
+        "rng_create": (_P, [C.c_uint64]),
+        "rng_destroy": (None, [_P]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, pre + name)
+        f.restype, f.argtypes = res, args
+    if which == "oracle":
+        lib.rpo_draw_moves.restype = C.c_int
+        lib.rpo_draw_moves.argtypes = [_P, C.c_double, C.c_double, _D, _I64, C.c_int64, C.c_int64, C.c_int64,
+                                       C.c_int32, _P]
+        lib.rpo_sim_create.restype = _P
+        lib.rpo_sim_create.argtypes = [_P, C.POINTER(SimParams)]
+        lib.rpo_sim_run.restype = C.c_int
+        lib.rpo_sim_run.argtypes = [_P, C.c_int64, C.POINTER(SimStats)]
+        lib.rpo_sim_destroy.argtypes = [_P]
+        lib.rpo_segment_distance2.restype = C.c_double
+        lib.rpo_segment_distance2.argtypes = [_D, _D, _D, _D]
+    else:
+        lib.ref_draw_moves.restype = C.c_int
+        lib.ref_draw_moves.argtypes = [_P, _P, C.c_double, C.c_double, _I64, C.c_int64, C.c_int64, C.c_int64,
+                                       C.c_int32, _P]
+        lib.ref_sim_run.restype = C.c_int
+        lib.ref_sim_run.argtypes = [_P, C.POINTER(SimParams), C.c_int64, C.POINTER(SimStats)]
+        lib.ref_banana_centres.restype = C.c_int
+        lib.ref_banana_centres.argtypes = [C.c_double, C.c_double, C.c_int, C.c_double, _D]
+    _LIBS[which] = (lib, pre)
+    return _LIBS[which]
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(_D)
+
+
+def shape_params(kind: int, **kw) -> np.ndarray:
+    if kind == SPHERE:
+        return np.array([kw["radius"]], dtype=np.float64)
+    if kind == SPHEROCYLINDER:
+        return np.array([kw["length"], kw["radius"]], dtype=np.float64)
+    centres = np.asarray(kw["centres"], dtype=np.float64).reshape(-1, 3)
+    radii = np.asarray(kw["radii"], dtype=np.float64).reshape(-1)
+    out = [float(len(radii))]
+    for c, r in zip(centres, radii):
+        out += [c[0], c[1], c[2], r]
+    return np.array(out, dtype=np.float64)
+
+
+class CpuPacking:
+    """A Packing on the CPU: ``which`` = "oracle" (restatement) or "reference"."""
+
+    def __init__(self, which: str, kind: int, params: np.ndarray, pos: np.ndarray, rot: np.ndarray,
+                 box: np.ndarray, threads: int = 1):
+        self.lib, self.pre = _lib("oracle" if which == "oracle" else "reference")
+        self.which = which
+        self.kind = kind
+        self.params = np.ascontiguousarray(params, dtype=np.float64)
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        rot = np.ascontiguousarray(rot, dtype=np.float64).reshape(-1, 9)
+        box = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
+        self.n = pos.shape[0]
+        self.h = self._f("create")(kind, _dp(self.params), len(self.params), self.n, _dp(pos), _dp(rot), _dp(box),
+                                   threads)
+        if not self.h:
+            raise ValueError("packing construction failed")
+
+    def _f(self, name):
+        return getattr(self.lib, self.pre + name)
+
+    def close(self):
+        if self.h:
+            self._f("destroy")(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def count_overlaps(self, early_exit: bool = False) -> int:
+        return int(self._f("count_overlaps")(self.h, 1 if early_exit else 0))
+
+    def set_counting(self, on: bool) -> None:
+        self._f("set_counting")(self.h, 1 if on else 0)
+
+    def cached_overlaps(self) -> int:
+        return int(self._f("cached_overlaps")(self.h))
+
+    def replay(self, moves: np.ndarray, domains: np.ndarray | None = None, temperature: float = 1.0):
+        moves = np.ascontiguousarray(moves, dtype=MOVE_DTYPE)
+        codes = np.zeros(len(moves), dtype=np.uint8)
+        deltas = np.zeros(len(moves), dtype=np.int32)
+        dom = None if domains is None else np.ascontiguousarray(domains, dtype=np.float64)
+        rc = self._f("replay")(self.h, moves.ctypes.data_as(C.c_void_p), len(moves),
+                               None if dom is None else _dp(dom), temperature,
+                               codes.ctypes.data_as(C.c_void_p), deltas.ctypes.data_as(C.c_void_p))
+        if rc != 0:
+            raise RuntimeError("replay failed")
+        return codes, deltas
+
+    def try_scaling(self, box: np.ndarray) -> float:
+        b = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
+        return float(self._f("try_scaling")(self.h, _dp(b)))
+
+    def revert_scaling(self) -> None:
+        self._f("revert_scaling")(self.h)
+
+    def state(self):
+        pos = np.zeros((self.n, 3))
+        rot = np.zeros((self.n, 9))
+        box = np.zeros(9)
+        self._f("get_state")(self.h, _dp(pos), _dp(rot), _dp(box))
+        return pos, rot, box
+
+    def ng_divisions(self):
+        d = np.zeros(3, dtype=np.int64)
+        ok = self._f("ng_divisions")(self.h, d.ctypes.data_as(_I64))
+        return tuple(int(x) for x in d) if ok else None
+
+    def draw_moves(self, rng, trans_step: float, rot_step: float, idxs, per_type: int, n: int,
+                   domain: int = -1) -> np.ndarray:
+        idxs = np.ascontiguousarray(idxs, dtype=np.int64)
+        out = np.zeros(n, dtype=MOVE_DTYPE)
+        if self.which == "oracle":
+            _, _, box = self.state()
+            rc = self.lib.rpo_draw_moves(rng, trans_step, rot_step, _dp(box), idxs.ctypes.data_as(_I64), len(idxs),
+                                         per_type, n, domain, out.ctypes.data_as(C.c_void_p))
+        else:
+            rc = self.lib.ref_draw_moves(rng, self.h, trans_step, rot_step, idxs.ctypes.data_as(_I64), len(idxs),
+                                         per_type, n, domain, out.ctypes.data_as(C.c_void_p))
+        if rc != 0:
+            raise RuntimeError("draw_moves failed")
+        return out
+
+    def rng(self, seed: int):
+        return self._f("rng_create")(seed)
+
+    def rng_free(self, r) -> None:
+        self._f("rng_destroy")(r)
+
+
+def sim_params(**kw) -> SimParams:
+    p = SimParams()
+    p.temperature = kw.get("temperature", 1.0)
+    p.pressure = kw.get("pressure", 1.0)
+    p.translation_step = kw.get("translation_step", 0.0)
+    p.rotation_step = kw.get("rotation_step", 0.0)
+    p.box_kind = kw.get("box_kind", 0)
+    p.adjust_steps = 1 if kw.get("adjust_steps", False) else 0
+    p.box_step = kw.get("box_step", 0.0)
+    d = kw.get("domains", (1, 1, 1))
+    for i in range(3):
+        p.domains[i] = d[i]
+    p.seed = kw.get("seed", 1234)
+    p.threads = kw.get("threads", 1)
+    return p
+
+
+def run_cycles(pk: CpuPacking, cycles: int, **kw) -> SimStats:
+    """Runs the cycle loop (Simulation::integrate) on a CpuPacking."""
+    st = SimStats()
+    p = sim_params(**kw)
+    if pk.which == "oracle":
+        s = pk.lib.rpo_sim_create(pk.h, C.byref(p))
+        if not s:
+            raise ValueError("bad simulation parameters")
+        try:
+            if pk.lib.rpo_sim_run(s, cycles, C.byref(st)) != 0:
+                raise RuntimeError("cycle loop failed")
+        finally:
+            pk.lib.rpo_sim_destroy(s)
+    else:
+        if pk.lib.ref_sim_run(pk.h, C.byref(p), cycles, C.byref(st)) != 0:
+            raise RuntimeError("reference integrate failed")
+    return st
+
+
+def pair_overlap(which: str, kind: int, params, p1, r1, p2, r2, c1: int = 0, c2: int = 0,
+                 box=None, translation=None) -> bool:
+    lib, pre = _lib("oracle" if which == "oracle" else "reference")
+    prm = np.ascontiguousarray(params, dtype=np.float64)
+    a = [np.ascontiguousarray(x, dtype=np.float64).reshape(-1) for x in (p1, r1, p2, r2)]
+    bc_kind, b, t = 0, None, None
+    if box is not None:
+        bc_kind, b = 1, np.ascontiguousarray(box, dtype=np.float64).reshape(9)
+    elif translation is not None:
+        bc_kind, t = 2, np.ascontiguousarray(translation, dtype=np.float64).reshape(3)
+    r = getattr(lib, pre + "pair_overlap")(kind, _dp(prm), len(prm), _dp(a[0]), _dp(a[1]), c1, _dp(a[2]), _dp(a[3]),
+                                           c2, bc_kind, None if b is None else _dp(b), None if t is None else _dp(t))
+    if r < 0:
+        raise ValueError("bad shape")
+    return bool(r)
+
+
+def rotation(which: str, axis, angle: float) -> np.ndarray:
+    lib, pre = _lib("oracle" if which == "oracle" else "reference")
+    ax = np.ascontiguousarray(axis, dtype=np.float64)
+    out = np.zeros(9)
+    getattr(lib, pre + "rotation")(_dp(ax), angle, _dp(out))
+    return out
+
+
+def box_info(which: str, box):
+    lib, pre = _lib("oracle" if which == "oracle" else "reference")
+    b = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
+    inv, h, v = np.zeros(9), np.zeros(3), np.zeros(1)
+    getattr(lib, pre + "box_info")(_dp(b), _dp(inv), _dp(h), _dp(v))
+    return inv, h, float(v[0])
+
+
+def banana_centres(arc_radius: float, arc_angle: float, n: int, sphere_radius: float) -> np.ndarray:
+    """Body-frame centres of a bent polysphere, from the reference's own generator."""
+    lib, _ = _lib("reference")
+    out = np.zeros(4 * n)
+    k = lib.ref_banana_centres(arc_radius, arc_angle, n, sphere_radius, _dp(out))
+    return out[:4 * k].reshape(k, 4)

@@ -1,0 +1,361 @@
+// ORACLE — test infrastructure only (see rpo_geometry.hpp).
+//
+// C entry points over the reference's OWN classes (Packing, SpherocylinderTraits,
+// Simulation, ...), compiled from the reference sources in place by oracle/Makefile
+// into oracle/_ref/librpref.so.  Used only in the build container, to pin the
+// restatement in oracle/rpo_*.hpp and to generate the golden fixtures under
+// tests/golden/.  Mirrors the rpo_* entry points of rpo_capi.cpp one for one.
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <random>
+#include <sstream>
+
+#include "core/ActiveDomain.h"
+#include "core/Packing.h"
+#include "core/PeriodicBoundaryConditions.h"
+#include "core/FreeBoundaryConditions.h"
+#include "core/Simulation.h"
+#include "core/ObservablesCollector.h"
+#include "core/move_samplers/RotationSampler.h"
+#include "core/move_samplers/TranslationSampler.h"
+#include "core/shapes/PolysphereTraits.h"
+#include "core/shapes/PolysphereBananaTraits.h"
+#include "core/shapes/SphereTraits.h"
+#include "core/shapes/SpherocylinderTraits.h"
+#include "core/volume_scalers/AnisotropicVolumeScaler.h"
+#include "core/volume_scalers/LogScalingFactorSampler.h"
+#include "core/volume_scalers/TriclinicAdapter.h"
+#include "core/volume_scalers/TriclinicDeltaScaler.h"
+#include "utils/Logger.h"
+
+namespace {
+
+std::shared_ptr<ShapeTraits> make_traits(int kind, const double *prm, int np) {
+    if (kind == 0 && np >= 1) return std::make_shared<SphereTraits>(prm[0]);
+    if (kind == 1 && np >= 2) return std::make_shared<SpherocylinderTraits>(prm[0], prm[1]);
+    if (kind == 2 && np >= 1) {
+        int k = static_cast<int>(prm[0]);
+        std::vector<PolysphereTraits::SphereData> data;
+        for (int i = 0; i < k; i++)
+            data.emplace_back(Vector<3>{prm[1 + 4 * i], prm[2 + 4 * i], prm[3 + 4 * i]}, prm[4 + 4 * i]);
+        PolysphereTraits::PolysphereGeometry geom(std::move(data), std::nullopt, std::nullopt, {0, 0, 0}, 1.0);
+        return std::make_shared<PolysphereTraits>(std::move(geom));
+    }
+    return nullptr;
+}
+
+Matrix<3, 3> load_m(const double *p) {
+    Matrix<3, 3> m;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) m(i, j) = p[3 * i + j];
+    return m;
+}
+void store_m(const Matrix<3, 3> &m, double *p) {
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) p[3 * i + j] = m(i, j);
+}
+
+struct Handle {
+    std::shared_ptr<ShapeTraits> traits;
+    std::unique_ptr<Packing> pk;
+    int threads = 1;
+    bool counting = false;
+};
+
+}  // namespace
+
+extern "C" {
+
+struct ref_move {
+    int32_t particle;
+    int32_t type;
+    int32_t domain;
+    int32_t reserved;
+    double translation[3];
+    double rotation[9];
+    double uniform;
+};
+
+void *ref_create(int kind, const double *prm, int np, int64_t n, const double *pos, const double *rot,
+                 const double *box9, int threads) {
+    auto h = std::make_unique<Handle>();
+    h->traits = make_traits(kind, prm, np);
+    if (!h->traits) return nullptr;
+    h->threads = threads;
+    std::vector<Shape> shapes;
+    for (int64_t i = 0; i < n; i++)
+        shapes.emplace_back(Vector<3>{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]}, load_m(rot + 9 * i));
+    try {
+        h->pk = std::make_unique<Packing>(TriclinicBox(load_m(box9)), std::move(shapes),
+                                          std::make_unique<PeriodicBoundaryConditions>(),
+                                          h->traits->getInteraction(), threads, threads);
+    } catch (const std::exception &) {
+        return nullptr;
+    }
+    return h.release();
+}
+
+void ref_destroy(void *hp) { delete static_cast<Handle *>(hp); }
+
+int64_t ref_count_overlaps(void *hp, int early) {
+    auto *h = static_cast<Handle *>(hp);
+    return static_cast<int64_t>(h->pk->countTotalOverlaps(h->traits->getInteraction(), early != 0));
+}
+
+void ref_set_counting(void *hp, int on) {
+    auto *h = static_cast<Handle *>(hp);
+    h->pk->toggleOverlapCounting(on != 0, h->traits->getInteraction());
+    h->counting = on != 0;
+}
+
+int64_t ref_cached_overlaps(void *hp) {
+    return static_cast<int64_t>(static_cast<Handle *>(hp)->pk->getCachedNumberOfOverlaps());
+}
+
+int ref_replay(void *hp, const ref_move *mv, int64_t n, const double *domains, double temperature,
+               uint8_t *out_code, int32_t *out_delta) {
+    auto *h = static_cast<Handle *>(hp);
+    Packing &pk = *h->pk;
+    const Interaction &inter = h->traits->getInteraction();
+    try {
+        for (int64_t i = 0; i < n; i++) {
+            const ref_move &m = mv[i];
+            Vector<3> t{m.translation[0], m.translation[1], m.translation[2]};
+            Matrix<3, 3> r = load_m(m.rotation);
+            std::optional<ActiveDomain> ad;
+            if (m.domain >= 0 && domains) {
+                const double *d = domains + 6 * m.domain;
+                std::array<ActiveDomain::RegionBounds, 3> b{};
+                for (int k = 0; k < 3; k++) b[k] = {d[k], d[3 + k]};
+                ad.emplace(pk.getBox(), b);
+            }
+            std::size_t before = h->counting ? pk.getCachedNumberOfOverlaps() : 0;
+            double dE = 0;
+            bool outside = false;
+            if (m.type == 0) {
+                dE = pk.tryTranslation(m.particle, t, inter, ad);
+                if (ad.has_value() && dE == std::numeric_limits<double>::infinity()) {
+                    // distinguish the ActiveDomain rejection from an overlap
+                    Shape s = pk[m.particle];
+                    PeriodicBoundaryConditions pbc(pk.getBox());
+                    s.translate(t, pbc);
+                    outside = !ad->isInside(s.getPosition());
+                }
+            } else if (m.type == 1) {
+                dE = pk.tryRotation(m.particle, r, inter);
+            } else {
+                dE = pk.tryMove(m.particle, t, r, inter, ad);
+            }
+            uint8_t code = 0;
+            if (outside) code = 2;
+            else if (dE == std::numeric_limits<double>::infinity()) code = 1;
+            else if (dE == -std::numeric_limits<double>::infinity()) code = 3;
+            bool acc = m.uniform <= std::exp(-dE / temperature);
+            if (acc) {
+                pk.acceptMove();
+                code |= 0x80;
+            }
+            out_code[i] = code;
+            if (out_delta)
+                out_delta[i] = h->counting
+                                   ? (acc ? static_cast<int32_t>(pk.getCachedNumberOfOverlaps() - before) : 0)
+                                   : 0;
+        }
+    } catch (const std::exception &) {
+        return -1;
+    }
+    return 0;
+}
+
+double ref_try_scaling(void *hp, const double *box9) {
+    auto *h = static_cast<Handle *>(hp);
+    return h->pk->tryScaling(TriclinicBox(load_m(box9)), h->traits->getInteraction());
+}
+
+void ref_revert_scaling(void *hp) { static_cast<Handle *>(hp)->pk->revertScaling(); }
+
+void ref_get_state(void *hp, double *pos, double *rot, double *box9) {
+    auto *h = static_cast<Handle *>(hp);
+    for (std::size_t i = 0; i < h->pk->size(); i++) {
+        const Shape &s = (*h->pk)[i];
+        for (int k = 0; k < 3; k++)
+            if (pos) pos[3 * i + k] = s.getPosition()[k];
+        if (rot) store_m(s.getOrientation(), rot + 9 * i);
+    }
+    if (box9) store_m(h->pk->getBox().getDimensions(), box9);
+}
+
+int ref_ng_divisions(void *hp, int64_t *div3) {
+    auto *h = static_cast<Handle *>(hp);
+    if (h->pk->getNeighbourGridMemoryUsage() == 0) return 0;
+    auto d = h->pk->getNeighbourGridCellDivisions();
+    for (int i = 0; i < 3; i++) div3[i] = static_cast<int64_t>(d[i]);
+    return 1;
+}
+
+int ref_pair_overlap(int kind, const double *prm, int np, const double *p1, const double *r1, int c1,
+                     const double *p2, const double *r2, int c2, int bc_kind, const double *box9,
+                     const double *) {
+    auto traits = make_traits(kind, prm, np);
+    if (!traits) return -1;
+    const Interaction &in = traits->getInteraction();
+    Vector<3> v1{p1[0], p1[1], p1[2]}, v2{p2[0], p2[1], p2[2]};
+    if (bc_kind == 1) {
+        PeriodicBoundaryConditions pbc(TriclinicBox(load_m(box9)));
+        return in.overlapBetween(v1, load_m(r1), c1, v2, load_m(r2), c2, pbc) ? 1 : 0;
+    }
+    FreeBoundaryConditions fbc;
+    return in.overlapBetween(v1, load_m(r1), c1, v2, load_m(r2), c2, fbc) ? 1 : 0;
+}
+
+void ref_rotation(const double *axis3, double angle, double *out9) {
+    store_m(Matrix<3, 3>::rotation(Vector<3>{axis3[0], axis3[1], axis3[2]}, angle), out9);
+}
+
+void ref_box_info(const double *box9, double *inv9, double *heights3, double *volume) {
+    TriclinicBox b(load_m(box9));
+    Matrix<3, 3> inv = b.getDimensions().inverse();
+    if (inv9) store_m(inv, inv9);
+    auto h = b.getHeights();
+    if (heights3)
+        for (int i = 0; i < 3; i++) heights3[i] = h[i];
+    if (volume) *volume = b.getVolume();
+}
+
+// Body-frame sphere centres and radii of a bent polysphere (PolysphereBananaTraits).
+int ref_banana_centres(double arc_radius, double arc_angle, int n, double sphere_radius, double *out4) {
+    PolysphereBananaTraits traits(arc_radius, arc_angle, static_cast<std::size_t>(n), sphere_radius);
+    const auto &data = traits.getSphereData();
+    for (std::size_t i = 0; i < data.size(); i++) {
+        for (int k = 0; k < 3; k++) out4[4 * i + k] = data[i].position[k];
+        out4[4 * i + 3] = data[i].radius;
+    }
+    return static_cast<int>(data.size());
+}
+
+struct ref_rng {
+    std::mt19937 mt;
+};
+void *ref_rng_create(uint64_t seed) { return new ref_rng{std::mt19937(static_cast<unsigned long>(seed))}; }
+void ref_rng_destroy(void *r) { delete static_cast<ref_rng *>(r); }
+
+// Draws moves with the reference's own samplers (TranslationSampler, RotationSampler)
+// in Simulation::tryMove's order: move-type int, sampler draws, Metropolis uniform.
+int ref_draw_moves(void *rp, void *hp, double trans_step, double rot_step, const int64_t *idxs, int64_t nidx,
+                   int64_t per_type, int64_t n, int32_t domain, ref_move *out) {
+    auto &mt = static_cast<ref_rng *>(rp)->mt;
+    auto *h = static_cast<Handle *>(hp);
+    std::vector<std::unique_ptr<MoveSampler>> samplers;
+    if (trans_step > 0) samplers.push_back(std::make_unique<TranslationSampler>(trans_step));
+    if (rot_step > 0) samplers.push_back(std::make_unique<RotationSampler>(rot_step));
+    std::vector<std::size_t> list(idxs, idxs + nidx);
+    std::uniform_real_distribution<double> unit;
+    std::size_t total = static_cast<std::size_t>(per_type) * samplers.size();
+    for (int64_t i = 0; i < n; i++) {
+        std::uniform_int_distribution<std::size_t> md(0, total - 1);
+        std::size_t sampled = md(mt);
+        std::size_t k = sampled / static_cast<std::size_t>(per_type);
+        auto data = samplers[k]->sampleMove(*h->pk, list, mt);
+        ref_move &m = out[i];
+        std::memset(&m, 0, sizeof(m));
+        m.particle = static_cast<int32_t>(data.particleIdx);
+        m.type = data.moveType == MoveSampler::MoveType::TRANSLATION ? 0 : 1;
+        m.domain = domain;
+        for (int q = 0; q < 3; q++) m.translation[q] = data.translation[q];
+        store_m(data.rotation, m.rotation);
+        m.uniform = unit(mt);
+    }
+    return 0;
+}
+
+struct ref_sim_params {
+    double temperature, pressure, translation_step, rotation_step;
+    int32_t box_kind, adjust_steps;
+    double box_step;
+    int64_t domains[3];
+    uint64_t seed;
+    int64_t threads;
+};
+
+struct ref_sim_stats {
+    int64_t moves[2], accepted[2];
+    int64_t scalings, scalings_accepted, cycles;
+    int64_t domains[3];
+    double move_us, scaling_us, total_us;
+    double steps[2];
+    double box_step;
+};
+
+// Runs Simulation::integrate (thermalisation when adjust_steps, else averaging) for
+// `cycles` cycles on the handle's packing; the packing is moved into the Simulation and
+// its final state copied back.
+int ref_sim_run(void *hp, const ref_sim_params *p, int64_t cycles, ref_sim_stats *out) {
+    auto *h = static_cast<Handle *>(hp);
+    try {
+        std::vector<std::unique_ptr<MoveSampler>> samplers;
+        if (p->translation_step > 0) samplers.push_back(std::make_unique<TranslationSampler>(p->translation_step));
+        if (p->rotation_step > 0) samplers.push_back(std::make_unique<RotationSampler>(p->rotation_step));
+        std::unique_ptr<TriclinicBoxScaler> scaler;
+        if (p->box_kind == 1) {
+            scaler = std::make_unique<TriclinicDeltaScaler>(p->box_step, true);
+        } else if (p->box_kind == 2) {
+            auto vs = std::make_unique<AnisotropicVolumeScaler>(std::make_unique<LogScalingFactorSampler>(),
+                                                                AnisotropicVolumeScaler::X & AnisotropicVolumeScaler::Y
+                                                                    & AnisotropicVolumeScaler::Z);
+            scaler = std::make_unique<TriclinicAdapter>(std::move(vs), p->box_step);
+        }
+        std::array<std::size_t, 3> dd{static_cast<std::size_t>(p->domains[0]), static_cast<std::size_t>(p->domains[1]),
+                                      static_cast<std::size_t>(p->domains[2])};
+        Simulation sim(std::move(h->pk), std::move(samplers), static_cast<unsigned long>(p->seed), std::move(scaler),
+                       dd, false);
+        Simulation::Environment env;
+        env.setTemperature(p->temperature);
+        env.setPressure(p->pressure);
+        if (p->box_kind == 0) env.disableBoxScaling();
+        Simulation::IntegrationParameters ip;
+        if (p->adjust_steps) ip.thermalisationCycles = static_cast<std::size_t>(cycles);
+        else ip.averagingCycles = static_cast<std::size_t>(cycles);
+        ip.averagingEvery = static_cast<std::size_t>(cycles);
+        ip.snapshotEvery = static_cast<std::size_t>(cycles);
+        ip.inlineInfoEvery = static_cast<std::size_t>(cycles);
+        auto collector = std::make_shared<ObservablesCollector>();
+        std::ostringstream sink;
+        Logger logger(sink);
+        sim.integrate(env, ip, *h->traits, collector, {}, logger);
+        if (out) {
+            std::memset(out, 0, sizeof(*out));
+            auto stats = sim.getMovesStatistics();
+            int slot = 0;
+            for (const auto &st : stats) {
+                if (st.groupName == "scaling") {
+                    out->scalings = static_cast<int64_t>(st.totalMoves);
+                    out->scalings_accepted = static_cast<int64_t>(st.acceptedMoves);
+                    if (!st.stepSizeDatas.empty()) out->box_step = st.stepSizeDatas.front().stepSize;
+                    continue;
+                }
+                int k = st.groupName == "rotation" ? 1 : (st.groupName == "translation" ? 0 : slot);
+                slot++;
+                if (k > 1) continue;
+                out->moves[k] = static_cast<int64_t>(st.totalMoves);
+                out->accepted[k] = static_cast<int64_t>(st.acceptedMoves);
+                if (!st.stepSizeDatas.empty()) out->steps[k] = st.stepSizeDatas.front().stepSize;
+            }
+            out->cycles = static_cast<int64_t>(sim.getPerformedCycles());
+            out->move_us = sim.getMoveMicroseconds();
+            out->scaling_us = sim.getScalingMicroseconds();
+            out->total_us = sim.getTotalMicroseconds();
+        }
+        // take the packing back
+        const Packing &fin = sim.getPacking();
+        std::vector<Shape> shapes(fin.begin(), fin.end());
+        h->pk = std::make_unique<Packing>(fin.getBox(), std::move(shapes),
+                                          std::make_unique<PeriodicBoundaryConditions>(),
+                                          h->traits->getInteraction(), h->threads, h->threads);
+    } catch (const std::exception &) {
+        return -1;
+    }
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,342 @@
+// ORACLE — test infrastructure only (see rpo_geometry.hpp).
+//
+// C entry points over the CPU restatement, loaded with ctypes by the tests and by
+// bench.py's CPU-baseline leg.  Shape kinds: 0 sphere {r}, 1 spherocylinder {l, r},
+// 2 polysphere {k, x0, y0, z0, r0, ..., x(k-1), y(k-1), z(k-1), r(k-1)}.
+#include <cstdint>
+#include <cstring>
+#include <memory>
+
+#include "rpo_sim.hpp"
+
+using namespace rpo;
+
+namespace {
+
+struct Handle {
+    Interaction inter;
+    std::unique_ptr<Packing> pk;
+};
+
+bool make_interaction(int kind, const double *prm, int np, Interaction &out) {
+    out.kind = kind;
+    if (kind == SPHERE) {
+        if (np < 1) return false;
+        out.radius = prm[0];
+    } else if (kind == SPHEROCYLINDER) {
+        if (np < 2) return false;
+        out.length = prm[0];
+        out.radius = prm[1];
+    } else if (kind == POLYSPHERE) {
+        if (np < 1) return false;
+        int k = static_cast<int>(prm[0]);
+        if (k < 1 || np < 1 + 4 * k) return false;
+        for (int i = 0; i < k; i++) {
+            out.centres.push_back({prm[1 + 4 * i], prm[2 + 4 * i], prm[3 + 4 * i]});
+            out.radii.push_back(prm[4 + 4 * i]);
+        }
+    } else {
+        return false;
+    }
+    return true;
+}
+
+M3 load_m3(const double *p) {
+    M3 m{};
+    std::memcpy(m.data(), p, sizeof(double) * 9);
+    return m;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Same layout as rp_move in include/rampack_gb300.h (120 bytes).
+struct rpo_move {
+    int32_t particle;
+    int32_t type;
+    int32_t domain;
+    int32_t reserved;
+    double translation[3];
+    double rotation[9];
+    double uniform;
+};
+
+int rpo_move_size() { return static_cast<int>(sizeof(rpo_move)); }
+
+void *rpo_create(int kind, const double *prm, int np, int64_t n, const double *pos, const double *rot,
+                 const double *box9, int threads) {
+    auto h = std::make_unique<Handle>();
+    if (!make_interaction(kind, prm, np, h->inter)) return nullptr;
+    std::vector<Shape> shapes(static_cast<std::size_t>(n));
+    for (int64_t i = 0; i < n; i++) {
+        shapes[i].pos = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+        shapes[i].rot = load_m3(rot + 9 * i);
+    }
+    try {
+        h->pk = std::make_unique<Packing>(Box(load_m3(box9)), std::move(shapes), h->inter,
+                                          static_cast<std::size_t>(threads), static_cast<std::size_t>(threads));
+    } catch (const std::exception &) {
+        return nullptr;
+    }
+    return h.release();
+}
+
+void rpo_destroy(void *hp) { delete static_cast<Handle *>(hp); }
+
+int64_t rpo_size(void *hp) { return static_cast<int64_t>(static_cast<Handle *>(hp)->pk->size()); }
+
+int64_t rpo_count_overlaps(void *hp, int early) {
+    auto *h = static_cast<Handle *>(hp);
+    return static_cast<int64_t>(h->pk->count_total_overlaps(h->inter, early != 0));
+}
+
+void rpo_set_counting(void *hp, int on) {
+    auto *h = static_cast<Handle *>(hp);
+    h->pk->set_counting(on != 0, h->inter);
+}
+
+int64_t rpo_cached_overlaps(void *hp) { return static_cast<int64_t>(static_cast<Handle *>(hp)->pk->num_overlaps); }
+
+// Replays proposals in order through tryTranslation/tryRotation/tryMove + Metropolis +
+// acceptMove (core/Simulation.cpp:466-490).  domains: 6 doubles per record (lo[3], hi[3]),
+// indexed by rpo_move::domain; domain < 0 means no ActiveDomain.  out_code per move:
+// low two bits 0 = dE 0, 1 = overlap (+inf), 2 = outside the active domain (+inf),
+// 3 = -inf (fewer overlaps, counting mode); bit 7 = accepted.  out_delta (optional)
+// receives the overlap-count delta in counting mode.
+int rpo_replay(void *hp, const rpo_move *mv_, int64_t n, const double *domains, double temperature,
+               uint8_t *out_code, int32_t *out_delta) {
+    auto *h = static_cast<Handle *>(hp);
+    Packing &pk = *h->pk;
+    try {
+        for (int64_t i = 0; i < n; i++) {
+            const rpo_move &m = mv_[i];
+            V3 t{m.translation[0], m.translation[1], m.translation[2]};
+            M3 r = load_m3(m.rotation);
+            const double *lo = nullptr, *hi = nullptr;
+            if (m.domain >= 0 && domains) {
+                lo = domains + 6 * m.domain;
+                hi = lo + 3;
+            }
+            bool outside = false;
+            pk.last_delta[0] = 0;
+            double dE = pk.try_move(m.type, static_cast<std::size_t>(m.particle), t, r, h->inter, lo, hi, &outside);
+            uint8_t code = 0;
+            if (outside) code = 2;
+            else if (dE == Packing::INF) code = 1;
+            else if (dE == -Packing::INF) code = 3;
+            bool acc = m.uniform <= std::exp(-dE / temperature);
+            if (acc) {
+                pk.accept(2);
+                code |= 0x80;
+            }
+            out_code[i] = code;
+            if (out_delta) out_delta[i] = (pk.counting && acc) ? pk.last_delta[0] : 0;
+        }
+    } catch (const std::exception &) {
+        return -1;
+    }
+    return 0;
+}
+
+double rpo_try_scaling(void *hp, const double *box9) {
+    auto *h = static_cast<Handle *>(hp);
+    return h->pk->try_scaling(Box(load_m3(box9)), h->inter);
+}
+
+void rpo_revert_scaling(void *hp) { static_cast<Handle *>(hp)->pk->revert_scaling(); }
+
+void rpo_get_state(void *hp, double *pos, double *rot, double *box9) {
+    auto *h = static_cast<Handle *>(hp);
+    std::size_t n = h->pk->size();
+    for (std::size_t i = 0; i < n; i++) {
+        const Shape &s = h->pk->shapes[i];
+        if (pos) std::memcpy(pos + 3 * i, s.pos.data(), 3 * sizeof(double));
+        if (rot) std::memcpy(rot + 9 * i, s.rot.data(), 9 * sizeof(double));
+    }
+    if (box9) std::memcpy(box9, h->pk->box.dim.data(), 9 * sizeof(double));
+}
+
+// Real (non-halo) neighbour-grid divisions; returns 0 when the packing has no grid.
+int rpo_ng_divisions(void *hp, int64_t *div3) {
+    auto *h = static_cast<Handle *>(hp);
+    if (!h->pk->ng.has_value()) return 0;
+    auto d = h->pk->ng->real_divisions();
+    for (int i = 0; i < 3; i++) div3[i] = static_cast<int64_t>(d[i]);
+    return 1;
+}
+
+// One pair test.  bc_kind 0 free, 1 periodic in box9, 2 fixed translation t3.
+int rpo_pair_overlap(int kind, const double *prm, int np, const double *p1, const double *r1, int c1,
+                     const double *p2, const double *r2, int c2, int bc_kind, const double *box9,
+                     const double *t3) {
+    Interaction in;
+    if (!make_interaction(kind, prm, np, in)) return -1;
+    Box bx;
+    BC bc;
+    if (bc_kind == 1) {
+        bx = Box(load_m3(box9));
+        bc = BC::periodic(bx);
+    } else if (bc_kind == 2) {
+        bc = BC::fixed({t3[0], t3[1], t3[2]});
+    }
+    return in.overlap({p1[0], p1[1], p1[2]}, load_m3(r1), c1, {p2[0], p2[1], p2[2]}, load_m3(r2), c2, bc) ? 1 : 0;
+}
+
+// Geometry helpers exposed for golden checks.
+void rpo_box_info(const double *box9, double *inv9, double *heights3, double *volume) {
+    Box b(load_m3(box9));
+    if (inv9) std::memcpy(inv9, b.inv.data(), 9 * sizeof(double));
+    V3 h = b.heights();
+    if (heights3) std::memcpy(heights3, h.data(), 3 * sizeof(double));
+    if (volume) *volume = b.volume();
+}
+
+void rpo_rotation(const double *axis3, double angle, double *out9) {
+    M3 r = rotation_axis_angle({axis3[0], axis3[1], axis3[2]}, angle);
+    std::memcpy(out9, r.data(), 9 * sizeof(double));
+}
+
+void rpo_rotation_euler(double ax, double ay, double az, double *out9) {
+    M3 r = rotation_euler(ax, ay, az);
+    std::memcpy(out9, r.data(), 9 * sizeof(double));
+}
+
+double rpo_segment_distance2(const double *a, const double *b, const double *c, const double *d) {
+    return segment_distance2({a[0], a[1], a[2]}, {b[0], b[1], b[2]}, {c[0], c[1], c[2]}, {d[0], d[1], d[2]});
+}
+
+// ---- proposal streams drawn exactly as the reference's samplers draw them ----
+struct rpo_rng {
+    std::mt19937 mt;
+};
+
+void *rpo_rng_create(uint64_t seed) { return new rpo_rng{std::mt19937(static_cast<unsigned long>(seed))}; }
+void rpo_rng_destroy(void *r) { delete static_cast<rpo_rng *>(r); }
+
+// Draws n moves over the particle list idxs, as one DD domain of Simulation::tryMove
+// does (Simulation.cpp:454-483): move type from uniform_int over the per-type
+// accumulations (per_type moves each), the sampler's draws, then the Metropolis
+// uniform.  Samplers: translation (if trans_step > 0) then rotation (if rot_step > 0).
+int rpo_draw_moves(void *rp, double trans_step, double rot_step, const double *box9, const int64_t *idxs,
+                   int64_t nidx, int64_t per_type, int64_t n, int32_t domain, rpo_move *out) {
+    auto &mt = static_cast<rpo_rng *>(rp)->mt;
+    if (nidx <= 0 || per_type <= 0) return -1;
+    std::vector<int> kinds;
+    if (trans_step > 0) kinds.push_back(0);
+    if (rot_step > 0) kinds.push_back(1);
+    if (kinds.empty()) return -1;
+    Box box(load_m3(box9));
+    V3 h = box.heights();
+    double max_t = std::min({h[0], h[1], h[2]}) / 2;
+    std::uniform_real_distribution<double> unit;
+    std::size_t total = static_cast<std::size_t>(per_type) * kinds.size();
+    for (int64_t i = 0; i < n; i++) {
+        std::uniform_int_distribution<std::size_t> md(0, total - 1);
+        std::size_t sampled = md(mt);
+        std::size_t k = sampled / static_cast<std::size_t>(per_type);
+        rpo_move &m = out[i];
+        std::memset(&m, 0, sizeof(m));
+        M3 r = identity();
+        V3 t{};
+        if (kinds[k] == 0) {
+            double a = std::min(max_t, trans_step);
+            std::uniform_real_distribution<double> d(-a, a);
+            t = {d(mt), d(mt), d(mt)};
+            m.type = 0;
+        } else {
+            std::uniform_real_distribution<double> ang(-rot_step, rot_step);
+            std::uniform_real_distribution<double> pm(-1, 1);
+            V3 axis;
+            do {
+                axis = {pm(mt), pm(mt), pm(mt)};
+            } while (norm2(axis) > 1);
+            double angle = ang(mt);
+            r = rotation_axis_angle(vdiv(axis, std::sqrt(norm2(axis))), angle);
+            m.type = 1;
+        }
+        std::uniform_int_distribution<std::size_t> pd(0, static_cast<std::size_t>(nidx) - 1);
+        m.particle = static_cast<int32_t>(idxs[pd(mt)]);
+        m.domain = domain;
+        std::memcpy(m.translation, t.data(), sizeof(m.translation));
+        std::memcpy(m.rotation, r.data(), sizeof(m.rotation));
+        m.uniform = unit(mt);
+    }
+    return 0;
+}
+
+// ---- the cycle loop (CPU baseline and ensemble checks) ----
+struct rpo_sim_params {
+    double temperature, pressure, translation_step, rotation_step;
+    int32_t box_kind, adjust_steps;
+    double box_step;
+    int64_t domains[3];
+    uint64_t seed;
+    int64_t threads;
+};
+
+struct rpo_sim_stats {
+    int64_t moves[2], accepted[2];
+    int64_t scalings, scalings_accepted, cycles;
+    int64_t domains[3];
+    double move_us, scaling_us, total_us;
+    double steps[2];
+    double box_step;
+};
+
+struct SimHandle {
+    Handle *h;
+    std::unique_ptr<Simulation> sim;
+};
+
+void *rpo_sim_create(void *hp, const rpo_sim_params *p) {
+    auto *h = static_cast<Handle *>(hp);
+    SimParams sp;
+    sp.temperature = p->temperature;
+    sp.pressure = p->pressure;
+    sp.translation_step = p->translation_step;
+    sp.rotation_step = p->rotation_step;
+    sp.box_kind = p->box_kind;
+    sp.box_step = p->box_step;
+    for (int i = 0; i < 3; i++) sp.domains[i] = static_cast<std::size_t>(p->domains[i]);
+    sp.seed = static_cast<unsigned long>(p->seed);
+    sp.threads = static_cast<std::size_t>(p->threads);
+    sp.adjust_steps = p->adjust_steps != 0;
+    if (sp.domains[0] * sp.domains[1] * sp.domains[2] > h->pk->move_threads) return nullptr;
+    auto *s = new SimHandle{h, std::make_unique<Simulation>(*h->pk, h->inter, sp)};
+    return s;
+}
+
+void rpo_sim_destroy(void *sp) { delete static_cast<SimHandle *>(sp); }
+
+int rpo_sim_run(void *sp, int64_t cycles, rpo_sim_stats *out) {
+    auto *s = static_cast<SimHandle *>(sp);
+    auto &sim = *s->sim;
+    try {
+        auto t0 = std::chrono::high_resolution_clock::now();
+        for (int64_t c = 0; c < cycles; c++) sim.cycle();
+        auto t1 = std::chrono::high_resolution_clock::now();
+        sim.total_us += std::chrono::duration<double, std::micro>(t1 - t0).count();
+    } catch (const std::exception &) {
+        return -1;
+    }
+    if (out) {
+        std::memset(out, 0, sizeof(*out));
+        for (std::size_t i = 0; i < sim.samplers.size() && i < 2; i++) {
+            out->moves[sim.samplers[i]] = static_cast<int64_t>(sim.counters[i].moves);
+            out->accepted[sim.samplers[i]] = static_cast<int64_t>(sim.counters[i].accepted);
+            out->steps[sim.samplers[i]] = sim.steps[i];
+        }
+        out->scalings = static_cast<int64_t>(sim.scaling.moves);
+        out->scalings_accepted = static_cast<int64_t>(sim.scaling.accepted);
+        out->cycles = static_cast<int64_t>(sim.cycles);
+        for (int i = 0; i < 3; i++) out->domains[i] = static_cast<int64_t>(sim.p.domains[i]);
+        out->move_us = sim.move_us;
+        out->scaling_us = sim.scaling_us;
+        out->total_us = sim.total_us;
+        out->box_step = sim.p.box_step;
+    }
+    return 0;
+}
+
+}  // extern "C"
