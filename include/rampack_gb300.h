@@ -1,0 +1,200 @@
+/*
+ * rampack_gb300 — C ABI of the GB300 (sm_103a) hard-particle Monte Carlo
+ * move-and-overlap engine.
+ *
+ * The entry points replace, for one packing held in GPU memory, the calls that the
+ * reference's Simulation makes into Packing (core/Packing.h:143-466) on the hot path.
+ * Each declaration names the reference interface it stands in for (paths relative to
+ * the rampack source tree).  Plain pointers and sizes only; every call returns an int
+ * status (RP_OK or a negative RP_ERR_*); rp_last_error() describes the last failure.
+ *
+ * Ownership: the library owns all device memory; host arrays passed in are copied
+ * before the call returns.  One handle is driven by one host thread; all device work
+ * of a handle is ordered on the handle's own CUDA stream.
+ *
+ * Layouts: positions are N x 3 doubles; orientations N x 9 doubles, row-major, so that
+ * element (i, j) of Matrix<3,3> is rot[9*k + 3*i + j]; the box is 9 doubles, row-major,
+ * whose columns are the box sides (core/TriclinicBox.h).
+ */
+#ifndef RAMPACK_GB300_H
+#define RAMPACK_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RP_OK 0
+#define RP_ERR_ARG (-1)          /* invalid argument: the reference throws PreconditionException */
+#define RP_ERR_CUDA (-2)         /* a CUDA runtime call failed */
+#define RP_ERR_STATE (-3)        /* call out of order (e.g. no state uploaded) */
+#define RP_ERR_OVERLAP (-4)      /* the packing has overlaps where none are allowed */
+#define RP_ERR_UNSUPPORTED (-5)  /* a configuration this engine does not handle */
+#define RP_ERR_DEVICE (-6)       /* a device-side check failed (status word set by a kernel) */
+#define RP_ERR_CAPACITY (-7)     /* a per-cell capacity was exceeded */
+
+#define RP_SHAPE_SPHERE 0
+#define RP_SHAPE_SPHEROCYLINDER 1
+
+#define RP_MOVE_TRANSLATION 0
+#define RP_MOVE_ROTATION 1
+#define RP_MOVE_ROTOTRANSLATION 2
+
+/* Outcome code of one move (rp_run_moves, rp_sweep logs): the low two bits give the
+ * energy class returned by Packing::tryTranslation / tryRotation / tryMove
+ * (core/Packing.cpp:84-164): 0 = dE 0, 1 = overlap (+inf), 2 = outside the active
+ * domain (+inf, ActiveDomain::isInside false), 3 = -inf (overlap counting only);
+ * bit 7 is set when the Metropolis test accepted the move (core/Simulation.cpp:483). */
+#define RP_CODE_ACCEPTED 0x80
+
+/* Shape descriptor: the closed set of hard interactions the engine evaluates on the
+ * GPU; a host caller builds it from SphereTraits(r) (core/shapes/SphereTraits.h:16) or
+ * SpherocylinderTraits(l, r) (core/shapes/SpherocylinderTraits.h:16). */
+typedef struct rp_shape_desc {
+    int32_t kind;
+    int32_t reserved;
+    double radius;
+    double length;
+} rp_shape_desc;
+
+/* One proposed particle move, as MoveSampler::MoveData (core/MoveSampler.h:40-49) plus
+ * the Metropolis uniform that Simulation::tryMove draws for it (core/Simulation.cpp:483).
+ * `domain` is the linear index of the active cell of the engine's cell grid in which
+ * the move is made (rp_get_grid); it is the ActiveDomain of the move. 120 bytes. */
+typedef struct rp_move {
+    int32_t particle;
+    int32_t type;
+    int32_t domain;
+    int32_t reserved;
+    double translation[3];
+    double rotation[9];
+    double uniform;
+} rp_move;
+
+/* The engine's checkerboard cell grid (the GPU counterpart of the reference's
+ * DomainDecomposition, core/DomainDecomposition.cpp:36-117). Cells are the active
+ * domains; cell (x, y, z) has linear index x + dims[0] * (y + dims[1] * z). */
+typedef struct rp_grid_info {
+    int32_t dims[3];
+    int32_t max_occupancy;
+    double shift[3];           /* relative origin of cell (0, 0, 0) */
+    double cell_height[3];     /* absolute cell heights */
+    int64_t num_cells;
+} rp_grid_info;
+
+/* Parameters of one device-driven sweep (the GPU counterpart of one
+ * Simulation::performMovesWithDomainDivision pass, core/Simulation.cpp:396-445). */
+typedef struct rp_sweep_params {
+    double translation_step;      /* TranslationSampler step; 0 disables translations */
+    double rotation_step;         /* RotationSampler step; 0 disables rotations */
+    uint64_t seed;                /* Philox key */
+    uint64_t counter;             /* Philox counter base (e.g. the cycle number) */
+    int32_t flags;                /* RP_SWEEP_* */
+    int32_t reserved;
+} rp_sweep_params;
+
+#define RP_SWEEP_LOG 1            /* record every proposal and outcome (rp_sweep_log) */
+#define RP_SWEEP_FP64_ONLY 2      /* decide every pair in FP64 (no FP32 filter) */
+
+typedef struct rp_sweep_stats {
+    uint64_t moves;
+    uint64_t accepted;
+    uint64_t rejected_overlap;
+    uint64_t rejected_domain;
+    uint64_t pair_tests;          /* FP32-filtered pair tests */
+    uint64_t fp64_pairs;          /* pairs re-decided in FP64 (the guard band) */
+    uint64_t translations;
+    uint64_t rotations;
+} rp_sweep_stats;
+
+/* ---- lifetime ---------------------------------------------------------------------- */
+
+/* Creates an engine for n particles of one shape on CUDA device `device`.
+ * Replaces: Packing::Packing(box, shapes, bc, interaction, moveThreads, scalingThreads)
+ * (core/Packing.h:152-168) together with Packing::reset (core/Packing.cpp:67-82); the
+ * state itself arrives through rp_upload_state. */
+int rp_create(const rp_shape_desc *shape, int64_t n, int device, void **handle);
+
+/* Releases the handle and all of its device memory. */
+int rp_destroy(void *handle);
+
+/* Text of the last error on this handle (never NULL; empty when none). */
+const char *rp_last_error(void *handle);
+
+/* ---- state ------------------------------------------------------------------------- */
+
+/* Copies positions, orientations and the box to the device and builds the cell grid.
+ * Replaces: Packing::reset / Packing::restore (core/Packing.cpp:67-82, :961-964).
+ * Fails with RP_ERR_ARG when a particle lies outside the box (areShapesWithinBox,
+ * core/Packing.cpp:1069-1075). */
+int rp_upload_state(void *handle, const double *pos, const double *rot, const double *box9);
+
+/* Copies the FP64 state back (positions, orientations, box); any pointer may be NULL.
+ * Replaces: iteration over Packing (core/Packing.h:190-203) and Packing::getBox. */
+int rp_download_state(void *handle, double *pos, double *rot, double *box9);
+
+/* ---- overlap counting -------------------------------------------------------------- */
+
+/* Counts all overlapping pairs (each pair and periodic image once); with early_exit the
+ * count is 0 or 1.  Replaces: Packing::countTotalOverlaps(interaction, earlyExit)
+ * (core/Packing.cpp:519-559). */
+int rp_count_overlaps(void *handle, int early_exit, int64_t *out_count);
+
+/* ---- particle moves ---------------------------------------------------------------- */
+
+/* Rebuilds the checkerboard cell grid with the given relative shift of its origin
+ * (each component in [0, 1)) and reports its layout.  Replaces the construction of
+ * DomainDecomposition with a random origin (core/Simulation.cpp:401-411). */
+int rp_set_grid(void *handle, const double *shift3, rp_grid_info *info);
+
+/* Reports the current grid (info), the cell of every particle (linear cell index, n
+ * int32) and the ActiveDomain bounds of every cell (6 doubles per cell: lo[3] then
+ * hi[3], relative coordinates; ActiveDomain::RegionBounds, core/ActiveDomain.h:19-31).
+ * Any output pointer may be NULL. */
+int rp_get_grid(void *handle, rp_grid_info *info, int32_t *cell_of_particle, double *bounds);
+
+/* Executes a list of proposed moves, in order, with the reference's semantics for hard
+ * bodies: each move is Packing::tryTranslation / tryRotation / tryMove with the move's
+ * cell as ActiveDomain (core/Packing.cpp:84-164), then the Metropolis test with the
+ * move's uniform and Packing::acceptMove on success (core/Simulation.cpp:466-490).
+ * Consecutive moves whose cells share a checkerboard colour form one phase; the cells
+ * of a phase run concurrently, one warp each, and every move's particle must belong to
+ * its cell.  out_codes (n bytes, optional) receives the outcome codes. */
+int rp_run_moves(void *handle, const rp_move *moves, int64_t n, uint8_t *out_codes);
+
+/* One device-driven sweep: a random grid shift, then the 8 checkerboard phases in a
+ * random order; every active cell performs (number of move types) x (occupancy) moves
+ * drawn from a Philox stream.  Replaces one Simulation::performMovesWithDomainDivision
+ * (core/Simulation.cpp:396-445).  stats may be NULL. */
+int rp_sweep(void *handle, const rp_sweep_params *params, rp_sweep_stats *stats);
+
+/* Copies the proposals and outcomes logged by the last rp_sweep run with RP_SWEEP_LOG,
+ * in an order that replays serially to the same result (phase by phase, each cell's
+ * moves in order).  *count receives the number of moves; moves/codes may be NULL to
+ * query the count. */
+int rp_sweep_log(void *handle, rp_move *moves, uint8_t *codes, int64_t capacity, int64_t *count);
+
+/* ---- box moves --------------------------------------------------------------------- */
+
+/* Rescales all positions to a new box (relative coordinates kept), rebuilds the grid
+ * and recounts overlaps in one pass; *dE receives +inf on overlap and 0 otherwise.
+ * A convex shape in a box that only grew is not checked, as in the reference.
+ * Replaces: Packing::tryScaling(const TriclinicBox &, interaction)
+ * (core/Packing.cpp:172-208). */
+int rp_try_scaling(void *handle, const double *new_box9, double *dE);
+
+/* Restores the state from before the last rp_try_scaling (buffer swap, no copy).
+ * Replaces: Packing::revertScaling (core/Packing.cpp:363-371). */
+int rp_revert_scaling(void *handle);
+
+/* ---- statistics --------------------------------------------------------------------- */
+
+/* Cumulative counters of all sweeps and move lists since creation. */
+int rp_get_stats(void *handle, rp_sweep_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RAMPACK_GB300_H */

@@ -1,0 +1,104 @@
+"""ctypes binding of the C ABI declared in include/rampack_gb300.h.
+
+The shared library is built in-tree (``rampack_gb300/build.py``).  There is no
+fallback: when the library is missing or cannot be loaded, importing the engine
+raises, so no CPU path can stand in for the GPU one.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "librampack_gb300.so")
+
+RP_OK = 0
+ERRORS = {
+    -1: "RP_ERR_ARG", -2: "RP_ERR_CUDA", -3: "RP_ERR_STATE", -4: "RP_ERR_OVERLAP",
+    -5: "RP_ERR_UNSUPPORTED", -6: "RP_ERR_DEVICE", -7: "RP_ERR_CAPACITY",
+}
+SHAPE_SPHERE, SHAPE_SPHEROCYLINDER = 0, 1
+MOVE_TRANSLATION, MOVE_ROTATION, MOVE_ROTOTRANSLATION = 0, 1, 2
+CODE_ACCEPTED = 0x80
+SWEEP_LOG, SWEEP_FP64_ONLY = 1, 2
+
+MOVE_DTYPE = np.dtype([
+    ("particle", "<i4"), ("type", "<i4"), ("domain", "<i4"), ("reserved", "<i4"),
+    ("translation", "<f8", (3,)), ("rotation", "<f8", (9,)), ("uniform", "<f8"),
+])
+assert MOVE_DTYPE.itemsize == 120
+
+
+class ShapeDesc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("reserved", C.c_int32), ("radius", C.c_double), ("length", C.c_double)]
+
+
+class GridInfo(C.Structure):
+    _fields_ = [("dims", C.c_int32 * 3), ("max_occupancy", C.c_int32), ("shift", C.c_double * 3),
+                ("cell_height", C.c_double * 3), ("num_cells", C.c_int64)]
+
+
+class SweepParams(C.Structure):
+    _fields_ = [("translation_step", C.c_double), ("rotation_step", C.c_double), ("seed", C.c_uint64),
+                ("counter", C.c_uint64), ("flags", C.c_int32), ("reserved", C.c_int32)]
+
+
+class SweepStats(C.Structure):
+    _fields_ = [("moves", C.c_uint64), ("accepted", C.c_uint64), ("rejected_overlap", C.c_uint64),
+                ("rejected_domain", C.c_uint64), ("pair_tests", C.c_uint64), ("fp64_pairs", C.c_uint64),
+                ("translations", C.c_uint64), ("rotations", C.c_uint64)]
+
+    def as_dict(self) -> dict:
+        return {name: int(getattr(self, name)) for name, _ in self._fields_}
+
+
+_P = C.c_void_p
+_D = C.POINTER(C.c_double)
+
+# name -> (restype, argtypes); every function declared in include/rampack_gb300.h
+SIGNATURES = {
+    "rp_create": (C.c_int, [C.POINTER(ShapeDesc), C.c_int64, C.c_int, C.POINTER(C.c_void_p)]),
+    "rp_destroy": (C.c_int, [_P]),
+    "rp_last_error": (C.c_char_p, [_P]),
+    "rp_upload_state": (C.c_int, [_P, _D, _D, _D]),
+    "rp_download_state": (C.c_int, [_P, _D, _D, _D]),
+    "rp_count_overlaps": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int64)]),
+    "rp_set_grid": (C.c_int, [_P, _D, C.POINTER(GridInfo)]),
+    "rp_get_grid": (C.c_int, [_P, C.POINTER(GridInfo), C.POINTER(C.c_int32), _D]),
+    "rp_run_moves": (C.c_int, [_P, _P, C.c_int64, _P]),
+    "rp_sweep": (C.c_int, [_P, C.POINTER(SweepParams), C.POINTER(SweepStats)]),
+    "rp_sweep_log": (C.c_int, [_P, _P, _P, C.c_int64, C.POINTER(C.c_int64)]),
+    "rp_try_scaling": (C.c_int, [_P, _D, _D]),
+    "rp_revert_scaling": (C.c_int, [_P]),
+    "rp_get_stats": (C.c_int, [_P, C.POINTER(SweepStats)]),
+}
+
+_LIB = None
+
+
+def load(path: str | None = None):
+    """Loads the engine library (once) and declares every entry point."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise ImportError(f"rampack_gb300: CUDA library not built ({p}); run rampack_gb300/build.py")
+    lib = C.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype, f.argtypes = res, args
+    _LIB = lib
+    return lib
+
+
+class EngineError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def dptr(a: np.ndarray):
+    return a.ctypes.data_as(_D)

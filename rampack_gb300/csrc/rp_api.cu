@@ -1,0 +1,892 @@
+// C-ABI of the engine (include/rampack_gb300.h): handle lifetime, state transfer,
+// cell-grid set-up, move lists, device-driven sweeps and box moves.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "rp_internal.cuh"
+
+namespace rp {
+
+cudaError_t launch_rebuild(const DevState &s, const GridDev &g, int32_t *block_sums, cudaStream_t st);
+cudaError_t launch_rescale(const double *src, double *dst, int64_t n, const double *old_inv, const double *new_box,
+                           cudaStream_t st);
+cudaError_t launch_count(const DevState &s, const GridDev &g, int early, unsigned long long *out, int *flag,
+                         cudaStream_t st);
+cudaError_t launch_sweep(const SweepArgs &a, bool list, int nwarps, cudaStream_t st);
+size_t sweep_smem_per_warp(int kind, int cap);
+
+namespace {
+
+constexpr int OVF_WARPS = 152;          // overflow rerun: one warp per block, grid-stride over cells
+constexpr size_t OVF_SMEM = 200 * 1024; // shared memory of one overflow warp
+
+struct GridHost {
+    GridDev d{};
+    int64_t cells_alloc = 0;
+    int64_t bounds_alloc = 0;
+    int cap = 0;
+    double cellmat64[9]{};
+};
+
+struct Handle {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    rp_shape_desc shape{};
+    int64_t n = 0;
+    double range = 0;
+    bool has_state = false;
+    double box[9]{}, inv[9]{};
+    double saved_box[9]{}, saved_inv[9]{};
+    bool can_revert = false;
+    double *pos64[2] = {nullptr, nullptr};
+    int pcur = 0;
+    double *rot64 = nullptr;
+    double *trans[2] = {nullptr, nullptr};
+    GridHost grid[2];
+    int gcur = 0;
+    int32_t *block_sums = nullptr;
+    int64_t block_sums_alloc = 0;
+    uint32_t *status = nullptr;
+    unsigned long long *counters = nullptr;
+    unsigned long long *count_out = nullptr;
+    int *flag = nullptr;
+    int32_t *overflow = nullptr;
+    int32_t *overflow_count = nullptr;
+    int64_t overflow_alloc = 0;
+    ExactShape ex{};
+    std::string err;
+    // move lists
+    rp_move *d_moves = nullptr;
+    int64_t moves_alloc = 0;
+    int32_t *d_list = nullptr;  // cells, begins, move_out packed
+    int64_t list_alloc = 0;
+    uint8_t *d_codes = nullptr;
+    int64_t codes_alloc = 0;
+    // sweep log
+    rp_move *d_log = nullptr;
+    uint8_t *d_log_codes = nullptr;
+    int64_t log_alloc = 0;
+    bool log_valid = false;
+    int log_types = 0;
+    std::vector<int32_t> log_start;
+    int log_dims[3]{};
+    std::vector<int> log_phases;
+};
+
+int fail(Handle *h, int code, const std::string &msg) {
+    if (h) h->err = msg;
+    return code;
+}
+
+#define RP_CUDA(h, call)                                                                                  \
+    do {                                                                                                  \
+        cudaError_t e_ = (call);                                                                          \
+        if (e_ != cudaSuccess) return fail((h), RP_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <typename T>
+cudaError_t ensure(T *&ptr, int64_t &alloc, int64_t need) {
+    if (need <= alloc && ptr) return cudaSuccess;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    alloc = 0;
+    int64_t want = std::max<int64_t>(need, 1);
+    cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&ptr), sizeof(T) * want);
+    if (e == cudaSuccess) alloc = want;
+    return e;
+}
+
+void heights_of(const double *box, double h[3]) {
+    d3 s0{box[0], box[3], box[6]}, s1{box[1], box[4], box[7]}, s2{box[2], box[5], box[8]};
+    // core/TriclinicBox.cpp:33-51 (volume = |(s0 x s1) . s2|, h_i = V / |s_j x s_k|)
+    double vol = std::fabs(dot3(cross3(s0, s1), s2));
+    h[0] = vol / std::sqrt(norm2(cross3(s1, s2)));
+    h[1] = vol / std::sqrt(norm2(cross3(s2, s0)));
+    h[2] = vol / std::sqrt(norm2(cross3(s0, s1)));
+}
+
+double volume_of(const double *box) {
+    d3 s0{box[0], box[3], box[6]}, s1{box[1], box[4], box[7]}, s2{box[2], box[5], box[8]};
+    return std::fabs(dot3(cross3(s0, s1), s2));
+}
+
+// core/Packing.cpp:1155-1176
+bool box_upscaled(const double *ob, const double *nb) {
+    const double EPS = 100 * std::numeric_limits<double>::epsilon();
+    for (int i = 0; i < 3; i++) {
+        d3 o{ob[i], ob[3 + i], ob[6 + i]}, n{nb[i], nb[3 + i], nb[6 + i]};
+        double d = dot3(o, n), n2o = norm2(o), n2n = norm2(n);
+        if (std::fabs(d * d / n2o / n2n - 1) > EPS) return false;
+        if (d * d / n2o / n2o < 1 + EPS) return false;
+    }
+    return true;
+}
+
+// Box translations box·m, m in {-2..2}^3 (core/NeighbourGrid.cpp:203-217 for |m| <= 1).
+void translation_table(const double *box, double *out) {
+    for (int a = 0; a < 5; a++)
+        for (int b = 0; b < 5; b++)
+            for (int c = 0; c < 5; c++) {
+                d3 rel{static_cast<double>(a) - 2, static_cast<double>(b) - 2., static_cast<double>(c) - 2.};
+                d3 t = mv3(box, rel);
+                int idx = (a * 5 + b) * 5 + c;
+                out[3 * idx] = t.x;
+                out[3 * idx + 1] = t.y;
+                out[3 * idx + 2] = t.z;
+            }
+}
+
+DevState dev_state(Handle *h) {
+    DevState s{};
+    s.n = h->n;
+    s.kind = h->shape.kind;
+    std::memcpy(s.box, h->box, sizeof(s.box));
+    std::memcpy(s.inv, h->inv, sizeof(s.inv));
+    for (int i = 0; i < 9; i++) s.inv32[i] = static_cast<float>(h->inv[i]);
+    s.pos64 = h->pos64[h->pcur];
+    s.rot64 = h->rot64;
+    s.trans = h->trans[h->pcur];
+    s.ex = h->ex;
+    s.status = h->status;
+    s.counters = h->counters;
+    // ---- FP32 filter margins for the current grid ----
+    const GridHost &g = h->grid[h->gcur];
+    double lrow = 0;
+    for (int i = 0; i < 3; i++) {
+        double r = 0;
+        for (int j = 0; j < 3; j++) r += std::fabs(g.cellmat64[3 * i + j]);
+        lrow = std::max(lrow, r);
+    }
+    const double u32 = std::ldexp(1.0, -24);
+    // per-component bound of the FP32 separation error: rounded cell-local coordinates
+    // and offsets, the staging and difference roundings and a translated mover.
+    const double e_sep = 24.0 * u32 * (lrow + 1.0);
+    const double e_axis = 16.0 * u32;  // FP32 axes (a rotated mover included)
+    const double safety = 4.0;
+    FilterConsts fc{};
+    double r = h->shape.radius, l = h->shape.length;
+    auto margin = [&](double thr) {
+        double d = std::sqrt(thr);
+        return safety * (2.0 * d * std::sqrt(3.0) * e_sep + 3.0 * e_sep * e_sep + 8.0 * u32 * thr);
+    };
+    if (h->shape.kind == RP_SHAPE_SPHERE) {
+        double thr = std::pow(2 * r, 2);
+        fc.sphere_lo = static_cast<float>(thr - margin(thr));
+        fc.sphere_hi = static_cast<float>(thr + margin(thr));
+    } else {
+        double core = 4 * r * r, far = std::pow(2 * r + l, 2);
+        fc.core_lo = static_cast<float>(core - margin(far));
+        fc.core_hi = static_cast<float>(core + margin(far));
+        fc.far_lo = static_cast<float>(far - margin(far));
+        fc.far_hi = static_cast<float>(far + margin(far));
+        fc.core_thr = static_cast<float>(core);
+        // segment-distance certificate: endpoint displacement from input errors, plus
+        // FP32 evaluation of dP, f and the gap (|w| <= |d| + l, |u| = |v| = l)
+        double dend = std::sqrt(3.0) * (e_sep + l * e_axis);
+        double dmax = 2 * r + l;
+        double eval = 12.0 * u32 * (dmax + 3 * l) * (dmax + 3 * l);
+        fc.seg_err = static_cast<float>(safety * (2.0 * (2 * r) * 2.0 * dend + 4.0 * dend * dend + eval));
+        fc.d_min = static_cast<float>(2e-4 * l * l * l * l);
+        fc.len = static_cast<float>(l);
+        fc.half_len = static_cast<float>(0.5 * l);
+    }
+    fc.cell_margin = 1e-5f;
+    s.fc = fc;
+    return s;
+}
+
+// Chooses the checkerboard grid for a box: cells at least one interaction range high
+// in every direction, an even count per direction (or a single cell), so that cells of
+// one colour never interact.
+int setup_grid(Handle *h, GridHost &G, const double *box, const double *shift) {
+    double hgt[3];
+    heights_of(box, hgt);
+    const double cell_min = h->range * (1.0 + 1e-9);
+    int dims[3];
+    for (int d = 0; d < 3; d++) {
+        if (!(hgt[d] >= cell_min)) return fail(h, RP_ERR_UNSUPPORTED, "box height smaller than the interaction range");
+        double nd = std::floor(hgt[d] / cell_min);
+        if (nd > 1 << 20) return fail(h, RP_ERR_UNSUPPORTED, "too many cells");
+        int n = static_cast<int>(nd);
+        if (n >= 2) n &= ~1;
+        else n = 1;
+        dims[d] = n;
+    }
+    // The reference keeps no neighbour grid for small boxes (core/Packing.cpp:862-881)
+    // and then tests pairs through full periodic boundary conditions, an arithmetic this
+    // engine does not reproduce.
+    {
+        double ref_cell = h->range;
+        double min_cell = std::cbrt(volume_of(box) / static_cast<double>(h->n)) / 5;
+        if (h->range < min_cell) ref_cell = min_cell;
+        double mx = std::max({hgt[0], hgt[1], hgt[2]}), mn = std::min({hgt[0], hgt[1], hgt[2]});
+        if (ref_cell * 4 > mx || ref_cell * (1 + 1e-12) > mn)
+            return fail(h, RP_ERR_UNSUPPORTED, "box too small: the reference uses no neighbour grid here");
+    }
+    int64_t ncell = static_cast<int64_t>(dims[0]) * dims[1] * dims[2];
+    if (ncell > (1ll << 30)) return fail(h, RP_ERR_UNSUPPORTED, "too many cells");
+    GridDev &g = G.d;
+    for (int d = 0; d < 3; d++) {
+        g.dims[d] = dims[d];
+        g.shift[d] = shift[d];
+    }
+    g.ncell = static_cast<int>(ncell);
+    double inv_cm[9];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) G.cellmat64[3 * i + j] = box[3 * i + j] / dims[j];
+    inverse3(G.cellmat64, inv_cm);
+    for (int i = 0; i < 9; i++) {
+        g.cellmat[i] = static_cast<float>(G.cellmat64[i]);
+        g.cellinv[i] = static_cast<float>(inv_cm[i]);
+    }
+    // allocations
+    if (ncell > G.cells_alloc) {
+        cudaFree(g.count);
+        cudaFree(g.start);
+        g.count = g.start = nullptr;
+        RP_CUDA(h, cudaMalloc(&g.count, sizeof(int32_t) * ncell));
+        RP_CUDA(h, cudaMalloc(&g.start, sizeof(int32_t) * (ncell + 1)));
+        G.cells_alloc = ncell;
+    }
+    if (!g.slot_pid) {
+        int64_t n = h->n;
+        RP_CUDA(h, cudaMalloc(&g.slot_pid, sizeof(int32_t) * n));
+        RP_CUDA(h, cudaMalloc(&g.pid_slot, sizeof(int32_t) * n));
+        RP_CUDA(h, cudaMalloc(&g.pid_cell, sizeof(int32_t) * n));
+        RP_CUDA(h, cudaMalloc(&g.rank, sizeof(int32_t) * n));
+        RP_CUDA(h, cudaMalloc(&g.mpos, sizeof(float4) * n));
+        RP_CUDA(h, cudaMalloc(&g.maxis, sizeof(float4) * n));
+        RP_CUDA(h, cudaMalloc(&g.plocal, sizeof(float4) * n));
+        RP_CUDA(h, cudaMalloc(&g.max_occ, sizeof(int32_t)));
+    }
+    // ActiveDomain bounds per cell and dimension
+    int64_t nb = 2ll * (dims[0] + dims[1] + dims[2]);
+    std::vector<double> bounds(nb);
+    int off = 0;
+    for (int d = 0; d < 3; d++) {
+        g.boundsoff[d] = off;
+        for (int c = 0; c < dims[d]; c++) {
+            double lo, hi;
+            if (dims[d] == 1) {
+                lo = -std::numeric_limits<double>::infinity();
+                hi = std::numeric_limits<double>::infinity();
+            } else {
+                lo = shift[d] + static_cast<double>(c) / dims[d];
+                if (lo >= 1) lo -= 1;
+                hi = shift[d] + static_cast<double>(c + 1) / dims[d];
+                if (hi >= 1) hi -= 1;
+            }
+            bounds[off + 2 * c] = lo;
+            bounds[off + 2 * c + 1] = hi;
+        }
+        off += 2 * dims[d];
+    }
+    RP_CUDA(h, ensure(g.bounds, G.bounds_alloc, nb));
+    RP_CUDA(h, cudaMemcpyAsync(g.bounds, bounds.data(), sizeof(double) * nb, cudaMemcpyHostToDevice, h->stream));
+    // staged-candidate capacity per warp: mean neighbourhood plus six standard deviations
+    double mean = 27.0 * static_cast<double>(h->n) / static_cast<double>(ncell);
+    int cap = static_cast<int>(mean + 6.0 * std::sqrt(mean) + 32.0);
+    cap = (cap + 31) / 32 * 32;
+    int maxcap = static_cast<int>(48 * 1024 / (sweep_smem_per_warp(h->shape.kind, 32) / 32));
+    G.cap = std::min(cap, maxcap / 32 * 32);
+    int64_t nblocks = (ncell + 4095) / 4096;
+    RP_CUDA(h, ensure(h->block_sums, h->block_sums_alloc, nblocks));
+    RP_CUDA(h, ensure(h->overflow, h->overflow_alloc, ncell));
+    return RP_OK;
+}
+
+int rebuild(Handle *h, int gi, int pi) {
+    int saved_g = h->gcur, saved_p = h->pcur;
+    h->gcur = gi;
+    h->pcur = pi;
+    DevState s = dev_state(h);
+    h->gcur = saved_g;
+    h->pcur = saved_p;
+    RP_CUDA(h, launch_rebuild(s, h->grid[gi].d, h->block_sums, h->stream));
+    return RP_OK;
+}
+
+int check_status(Handle *h) {
+    uint32_t st = 0;
+    RP_CUDA(h, cudaMemcpyAsync(&st, h->status, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+    RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (st) {
+        RP_CUDA(h, cudaMemsetAsync(h->status, 0, sizeof(uint32_t), h->stream));
+        char buf[128];
+        std::snprintf(buf, sizeof(buf), "device status 0x%x%s%s", st,
+                      (st & ST_PARTICLE_NOT_IN_CELL) ? " (a move's particle is not in its cell)" : "",
+                      (st & ST_CAPACITY) ? " (a cell neighbourhood exceeds the staging capacity)" : "");
+        return fail(h, (st & ST_CAPACITY) ? RP_ERR_CAPACITY : RP_ERR_DEVICE, buf);
+    }
+    return RP_OK;
+}
+
+void phase_bits(const GridDev &g, int cell, int &ph) {
+    int cx = cell % g.dims[0], cy = (cell / g.dims[0]) % g.dims[1], cz = cell / (g.dims[0] * g.dims[1]);
+    ph = (g.dims[0] > 1 ? (cx & 1) : 0) | ((g.dims[1] > 1 ? (cy & 1) : 0) << 1) | ((g.dims[2] > 1 ? (cz & 1) : 0) << 2);
+}
+
+SweepArgs base_args(Handle *h) {
+    SweepArgs a{};
+    a.s = dev_state(h);
+    a.g = h->grid[h->gcur].d;
+    a.cap = h->grid[h->gcur].cap;
+    a.overflow = h->overflow;
+    a.overflow_count = h->overflow_count;
+    return a;
+}
+
+// Re-runs the cells of a phase whose neighbourhood did not fit the normal staging
+// capacity, with one large-capacity warp per block (device-side work count).
+int run_overflow(Handle *h, SweepArgs a, bool list) {
+    int cap = static_cast<int>(OVF_SMEM / sweep_smem_per_warp(a.s.kind, 8) * 8);
+    cap = cap / 32 * 32;
+    a.cap = cap;
+    a.work = h->overflow;
+    a.work_count = h->overflow_count;
+    a.num_work = -1;
+    a.overflow = nullptr;
+    RP_CUDA(h, launch_sweep(a, list, OVF_WARPS, h->stream));
+    RP_CUDA(h, cudaMemsetAsync(h->overflow_count, 0, sizeof(int32_t), h->stream));
+    return RP_OK;
+}
+
+}  // namespace
+}  // namespace rp
+
+using namespace rp;
+
+extern "C" {
+
+int rp_create(const rp_shape_desc *shape, int64_t n, int device, void **handle) {
+    if (!shape || !handle || n <= 0 || n > (1ll << 31) - 1) return RP_ERR_ARG;
+    if (shape->kind != RP_SHAPE_SPHERE && shape->kind != RP_SHAPE_SPHEROCYLINDER) return RP_ERR_UNSUPPORTED;
+    if (!(shape->radius > 0) || (shape->kind == RP_SHAPE_SPHEROCYLINDER && !(shape->length >= 0))) return RP_ERR_ARG;
+    Handle *h = new (std::nothrow) Handle();
+    if (!h) return RP_ERR_ARG;
+    h->device = device;
+    h->shape = *shape;
+    h->n = n;
+    double r = shape->radius, l = shape->length;
+    ExactShape ex{};
+    ex.kind = shape->kind;
+    if (shape->kind == RP_SHAPE_SPHERE) {
+        h->range = 2 * r;                      // SphereTraits.h:34
+        ex.sphere_thr = std::pow(2 * r, 2);     // SphereTraits.cpp:64
+    } else {
+        h->range = 2 * r + l;                  // SpherocylinderTraits.h:81
+        ex.core_thr = 4 * r * r;                // SpherocylinderTraits.cpp:35
+        ex.far_thr = std::pow(2 * r + l, 2);    // SpherocylinderTraits.cpp:37
+        short beg = -1, end = 1;                // SpherocylinderTraits.cpp:23-25
+        ex.neg_cap_half = 0.5 * beg * l;
+        ex.cap_half = 0.5 * end * l;
+    }
+    h->ex = ex;
+    auto bail = [&](cudaError_t e) {
+        h->err = cudaGetErrorString(e);
+        rp_destroy(h);
+        return RP_ERR_CUDA;
+    };
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return bail(e);
+    if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e);
+    for (int i = 0; i < 2; i++) {
+        if ((e = cudaMalloc(&h->pos64[i], sizeof(double) * 3 * n)) != cudaSuccess) return bail(e);
+        if ((e = cudaMalloc(&h->trans[i], sizeof(double) * 3 * 125)) != cudaSuccess) return bail(e);
+    }
+    if ((e = cudaMalloc(&h->rot64, sizeof(double) * 9 * n)) != cudaSuccess) return bail(e);
+    if ((e = cudaMalloc(&h->status, sizeof(uint32_t))) != cudaSuccess) return bail(e);
+    if ((e = cudaMalloc(&h->counters, sizeof(unsigned long long) * 8)) != cudaSuccess) return bail(e);
+    if ((e = cudaMalloc(&h->count_out, sizeof(unsigned long long))) != cudaSuccess) return bail(e);
+    if ((e = cudaMalloc(&h->flag, sizeof(int))) != cudaSuccess) return bail(e);
+    if ((e = cudaMalloc(&h->overflow_count, sizeof(int32_t))) != cudaSuccess) return bail(e);
+    cudaMemset(h->status, 0, sizeof(uint32_t));
+    cudaMemset(h->counters, 0, sizeof(unsigned long long) * 8);
+    cudaMemset(h->overflow_count, 0, sizeof(int32_t));
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return bail(e);
+    *handle = h;
+    return RP_OK;
+}
+
+int rp_destroy(void *handle) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h) return RP_ERR_ARG;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (int i = 0; i < 2; i++) {
+        cudaFree(h->pos64[i]);
+        cudaFree(h->trans[i]);
+        GridDev &g = h->grid[i].d;
+        cudaFree(g.count);
+        cudaFree(g.start);
+        cudaFree(g.slot_pid);
+        cudaFree(g.pid_slot);
+        cudaFree(g.pid_cell);
+        cudaFree(g.rank);
+        cudaFree(g.mpos);
+        cudaFree(g.maxis);
+        cudaFree(g.plocal);
+        cudaFree(g.bounds);
+        cudaFree(g.max_occ);
+    }
+    cudaFree(h->rot64);
+    cudaFree(h->block_sums);
+    cudaFree(h->status);
+    cudaFree(h->counters);
+    cudaFree(h->count_out);
+    cudaFree(h->flag);
+    cudaFree(h->overflow);
+    cudaFree(h->overflow_count);
+    cudaFree(h->d_moves);
+    cudaFree(h->d_list);
+    cudaFree(h->d_codes);
+    cudaFree(h->d_log);
+    cudaFree(h->d_log_codes);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return RP_OK;
+}
+
+const char *rp_last_error(void *handle) {
+    Handle *h = static_cast<Handle *>(handle);
+    return h ? h->err.c_str() : "null handle";
+}
+
+int rp_upload_state(void *handle, const double *pos, const double *rot, const double *box9) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !pos || !rot || !box9) return fail(h, RP_ERR_ARG, "null argument");
+    RP_CUDA(h, cudaSetDevice(h->device));
+    double inv[9];
+    if (det3(box9) == 0) return fail(h, RP_ERR_ARG, "box volume is zero");
+    inverse3(box9, inv);
+    // core/Packing.cpp:1069-1075 (areShapesWithinBox)
+    for (int64_t i = 0; i < h->n; i++) {
+        d3 r = mv3(inv, d3{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]});
+        if (r.x < 0 || r.x >= 1 || r.y < 0 || r.y >= 1 || r.z < 0 || r.z >= 1)
+            return fail(h, RP_ERR_ARG, "a particle lies outside the box");
+    }
+    std::memcpy(h->box, box9, sizeof(h->box));
+    std::memcpy(h->inv, inv, sizeof(h->inv));
+    h->pcur = 0;
+    h->gcur = 0;
+    RP_CUDA(h, cudaMemcpyAsync(h->pos64[0], pos, sizeof(double) * 3 * h->n, cudaMemcpyHostToDevice, h->stream));
+    RP_CUDA(h, cudaMemcpyAsync(h->rot64, rot, sizeof(double) * 9 * h->n, cudaMemcpyHostToDevice, h->stream));
+    double tt[375];
+    translation_table(h->box, tt);
+    RP_CUDA(h, cudaMemcpyAsync(h->trans[0], tt, sizeof(tt), cudaMemcpyHostToDevice, h->stream));
+    double shift[3] = {0, 0, 0};
+    int rc = setup_grid(h, h->grid[0], h->box, shift);
+    if (rc) return rc;
+    rc = rebuild(h, 0, 0);
+    if (rc) return rc;
+    RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->has_state = true;
+    h->can_revert = false;
+    h->log_valid = false;
+    return RP_OK;
+}
+
+int rp_download_state(void *handle, double *pos, double *rot, double *box9) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h) return RP_ERR_ARG;
+    if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
+    RP_CUDA(h, cudaSetDevice(h->device));
+    if (pos)
+        RP_CUDA(h, cudaMemcpyAsync(pos, h->pos64[h->pcur], sizeof(double) * 3 * h->n, cudaMemcpyDeviceToHost,
+                                   h->stream));
+    if (rot)
+        RP_CUDA(h, cudaMemcpyAsync(rot, h->rot64, sizeof(double) * 9 * h->n, cudaMemcpyDeviceToHost, h->stream));
+    RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (box9) std::memcpy(box9, h->box, sizeof(h->box));
+    return RP_OK;
+}
+
+int rp_count_overlaps(void *handle, int early_exit, int64_t *out_count) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !out_count) return fail(h, RP_ERR_ARG, "null argument");
+    if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
+    RP_CUDA(h, cudaSetDevice(h->device));
+    RP_CUDA(h, cudaMemsetAsync(h->count_out, 0, sizeof(unsigned long long), h->stream));
+    RP_CUDA(h, cudaMemsetAsync(h->flag, 0, sizeof(int), h->stream));
+    DevState s = dev_state(h);
+    RP_CUDA(h, launch_count(s, h->grid[h->gcur].d, early_exit ? 1 : 0, h->count_out, h->flag, h->stream));
+    unsigned long long c = 0;
+    RP_CUDA(h, cudaMemcpyAsync(&c, h->count_out, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
+    RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    *out_count = early_exit ? (c > 0 ? 1 : 0) : static_cast<int64_t>(c);
+    return check_status(h);
+}
+
+static int fill_info(Handle *h, rp_grid_info *info) {
+    const GridDev &g = h->grid[h->gcur].d;
+    int32_t mo = 0;
+    RP_CUDA(h, cudaMemcpyAsync(&mo, g.max_occ, sizeof(mo), cudaMemcpyDeviceToHost, h->stream));
+    RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    double hgt[3];
+    heights_of(h->box, hgt);
+    for (int d = 0; d < 3; d++) {
+        info->dims[d] = g.dims[d];
+        info->shift[d] = g.shift[d];
+        info->cell_height[d] = hgt[d] / g.dims[d];
+    }
+    info->max_occupancy = mo;
+    info->num_cells = g.ncell;
+    return RP_OK;
+}
+
+int rp_set_grid(void *handle, const double *shift3, rp_grid_info *info) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !shift3) return fail(h, RP_ERR_ARG, "null argument");
+    if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
+    for (int d = 0; d < 3; d++)
+        if (!(shift3[d] >= 0 && shift3[d] < 1)) return fail(h, RP_ERR_ARG, "grid shift outside [0, 1)");
+    RP_CUDA(h, cudaSetDevice(h->device));
+    int rc = setup_grid(h, h->grid[h->gcur], h->box, shift3);
+    if (rc) return rc;
+    rc = rebuild(h, h->gcur, h->pcur);
+    if (rc) return rc;
+    h->can_revert = false;
+    if (info) {
+        rc = fill_info(h, info);
+        if (rc) return rc;
+    }
+    RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    return RP_OK;
+}
+
+int rp_get_grid(void *handle, rp_grid_info *info, int32_t *cell_of_particle, double *bounds) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h) return RP_ERR_ARG;
+    if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
+    RP_CUDA(h, cudaSetDevice(h->device));
+    const GridDev &g = h->grid[h->gcur].d;
+    if (info) {
+        int rc = fill_info(h, info);
+        if (rc) return rc;
+    }
+    if (cell_of_particle)
+        RP_CUDA(h, cudaMemcpyAsync(cell_of_particle, g.pid_cell, sizeof(int32_t) * h->n, cudaMemcpyDeviceToHost,
+                                   h->stream));
+    if (bounds) {
+        int64_t nb = 2ll * (g.dims[0] + g.dims[1] + g.dims[2]);
+        std::vector<double> b(nb);
+        RP_CUDA(h, cudaMemcpyAsync(b.data(), g.bounds, sizeof(double) * nb, cudaMemcpyDeviceToHost, h->stream));
+        RP_CUDA(h, cudaStreamSynchronize(h->stream));
+        for (int64_t cell = 0; cell < g.ncell; cell++) {
+            int c[3] = {static_cast<int>(cell % g.dims[0]), static_cast<int>((cell / g.dims[0]) % g.dims[1]),
+                        static_cast<int>(cell / (static_cast<int64_t>(g.dims[0]) * g.dims[1]))};
+            for (int d = 0; d < 3; d++) {
+                bounds[6 * cell + d] = b[g.boundsoff[d] + 2 * c[d]];
+                bounds[6 * cell + 3 + d] = b[g.boundsoff[d] + 2 * c[d] + 1];
+            }
+        }
+    }
+    RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    return RP_OK;
+}
+
+int rp_run_moves(void *handle, const rp_move *moves, int64_t n, uint8_t *out_codes) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || (!moves && n > 0)) return fail(h, RP_ERR_ARG, "null argument");
+    if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
+    if (n <= 0) return RP_OK;
+    if (n > (1ll << 31) - 1) return fail(h, RP_ERR_ARG, "too many moves");
+    RP_CUDA(h, cudaSetDevice(h->device));
+    const GridDev &g = h->grid[h->gcur].d;
+    // validation and phase blocks (runs of equal checkerboard colour)
+    std::vector<int> phase(n);
+    for (int64_t i = 0; i < n; i++) {
+        const rp_move &m = moves[i];
+        if (m.domain < 0 || m.domain >= g.ncell) return fail(h, RP_ERR_ARG, "move names a cell outside the grid");
+        if (m.particle < 0 || m.particle >= h->n) return fail(h, RP_ERR_ARG, "move names an unknown particle");
+        if (m.type < 0 || m.type > 2) return fail(h, RP_ERR_ARG, "unknown move type");
+        phase_bits(g, m.domain, phase[i]);
+    }
+    RP_CUDA(h, ensure(h->d_moves, h->moves_alloc, n));
+    RP_CUDA(h, ensure(h->d_codes, h->codes_alloc, n));
+    RP_CUDA(h, cudaMemcpyAsync(h->d_moves, moves, sizeof(rp_move) * n, cudaMemcpyHostToDevice, h->stream));
+    // per block: cells, begin offsets, move order
+    std::vector<int32_t> packed;
+    struct Block {
+        int64_t cells_off, begin_off, out_off;
+        int ncells;
+    };
+    std::vector<Block> blocks;
+    std::vector<int32_t> cell_count(g.ncell, 0), cell_pos(g.ncell, -1);
+    int64_t i = 0;
+    while (i < n) {
+        int64_t j = i;
+        while (j < n && phase[j] == phase[i]) j++;
+        // stable grouping by cell, cells in order of first appearance
+        std::vector<int32_t> cells;
+        for (int64_t k = i; k < j; k++) {
+            int c = moves[k].domain;
+            if (cell_count[c]++ == 0) cells.push_back(c);
+        }
+        Block b{};
+        b.ncells = static_cast<int>(cells.size());
+        b.cells_off = static_cast<int64_t>(packed.size());
+        packed.insert(packed.end(), cells.begin(), cells.end());
+        b.begin_off = static_cast<int64_t>(packed.size());
+        int32_t run = 0;
+        for (int32_t c : cells) {
+            packed.push_back(run);
+            cell_pos[c] = run;
+            run += cell_count[c];
+        }
+        packed.push_back(run);
+        b.out_off = static_cast<int64_t>(packed.size());
+        packed.resize(packed.size() + (j - i));
+        for (int64_t k = i; k < j; k++) {
+            int c = moves[k].domain;
+            packed[b.out_off + cell_pos[c]++] = static_cast<int32_t>(k);
+        }
+        for (int32_t c : cells) {
+            cell_count[c] = 0;
+            cell_pos[c] = -1;
+        }
+        blocks.push_back(b);
+        i = j;
+    }
+    RP_CUDA(h, ensure(h->d_list, h->list_alloc, static_cast<int64_t>(packed.size())));
+    RP_CUDA(h, cudaMemcpyAsync(h->d_list, packed.data(), sizeof(int32_t) * packed.size(), cudaMemcpyHostToDevice,
+                               h->stream));
+    for (const Block &b : blocks) {
+        SweepArgs a = base_args(h);
+        a.moves = h->d_moves;
+        a.list_cells = h->d_list + b.cells_off;
+        a.list_begin = h->d_list + b.begin_off;
+        a.move_out = h->d_list + b.out_off;
+        a.num_list = b.ncells;
+        a.codes = h->d_codes;
+        a.types = 3;
+        RP_CUDA(h, launch_sweep(a, true, b.ncells, h->stream));
+        int rc = run_overflow(h, a, true);
+        if (rc) return rc;
+    }
+    if (out_codes)
+        RP_CUDA(h, cudaMemcpyAsync(out_codes, h->d_codes, n, cudaMemcpyDeviceToHost, h->stream));
+    RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->can_revert = false;
+    h->log_valid = false;
+    return check_status(h);
+}
+
+int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !p) return fail(h, RP_ERR_ARG, "null argument");
+    if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
+    int types = (p->translation_step > 0 ? 1 : 0) | (p->rotation_step > 0 ? 2 : 0);
+    if (!types) return fail(h, RP_ERR_ARG, "no move type enabled");
+    RP_CUDA(h, cudaSetDevice(h->device));
+    // random grid origin and phase order from the Philox stream of this sweep
+    u4 r = philox(u4{0x5eedu, 0x9e37u, static_cast<uint32_t>(p->counter), static_cast<uint32_t>(p->counter >> 32)},
+                  static_cast<uint32_t>(p->seed), static_cast<uint32_t>(p->seed >> 32));
+    double shift[3] = {(r.a >> 8) * (1.0 / 16777216.0), (r.b >> 8) * (1.0 / 16777216.0),
+                       (r.c >> 8) * (1.0 / 16777216.0)};
+    int rc = setup_grid(h, h->grid[h->gcur], h->box, shift);
+    if (rc) return rc;
+    rc = rebuild(h, h->gcur, h->pcur);
+    if (rc) return rc;
+    const GridDev &g = h->grid[h->gcur].d;
+    // translation step limited to half the smallest box height (TranslationSampler.cpp:39-46)
+    double hgt[3];
+    heights_of(h->box, hgt);
+    double tstep = std::min(p->translation_step, std::min({hgt[0], hgt[1], hgt[2]}) / 2);
+    std::vector<int> phases;
+    for (int ph = 0; ph < 8; ph++) {
+        bool ok = true;
+        for (int d = 0; d < 3; d++)
+            if (g.dims[d] == 1 && ((ph >> d) & 1)) ok = false;
+        if (ok) phases.push_back(ph);
+    }
+    uint32_t x = r.d;
+    for (int k = static_cast<int>(phases.size()) - 1; k > 0; k--) {
+        x = x * 1664525u + 1013904223u;
+        int j = static_cast<int>((static_cast<uint64_t>(x) * (k + 1)) >> 32);
+        std::swap(phases[k], phases[j]);
+    }
+    int ntypes = (types & 1) + ((types >> 1) & 1);
+    bool log = (p->flags & RP_SWEEP_LOG) != 0;
+    if (log) {
+        int64_t before = h->log_alloc;
+        RP_CUDA(h, ensure(h->d_log, h->log_alloc, ntypes * h->n));
+        if (!h->d_log_codes || h->log_alloc != before) {
+            cudaFree(h->d_log_codes);
+            h->d_log_codes = nullptr;
+            RP_CUDA(h, cudaMalloc(&h->d_log_codes, h->log_alloc));
+        }
+    }
+    if (stats) RP_CUDA(h, cudaMemsetAsync(h->counters, 0, sizeof(unsigned long long) * 8, h->stream));
+    for (int ph : phases) {
+        SweepArgs a = base_args(h);
+        int act[3];
+        for (int d = 0; d < 3; d++) {
+            a.phase[d] = (ph >> d) & 1;
+            act[d] = g.dims[d] == 1 ? 1 : g.dims[d] / 2;
+            a.active[d] = act[d];
+        }
+        a.num_active = act[0] * act[1] * act[2];
+        a.seed = p->seed;
+        a.counter = p->counter;
+        a.tstep = static_cast<float>(tstep);
+        a.rstep = static_cast<float>(p->rotation_step);
+        a.types = types;
+        a.fp64_only = (p->flags & RP_SWEEP_FP64_ONLY) ? 1 : 0;
+        if (log) {
+            a.log = h->d_log;
+            a.log_codes = h->d_log_codes;
+        }
+        RP_CUDA(h, launch_sweep(a, false, a.num_active, h->stream));
+        rc = run_overflow(h, a, false);
+        if (rc) return rc;
+    }
+    if (log) {
+        h->log_valid = true;
+        h->log_types = ntypes;
+        h->log_phases = phases;
+        for (int d = 0; d < 3; d++) h->log_dims[d] = g.dims[d];
+        h->log_start.resize(g.ncell + 1);
+        RP_CUDA(h, cudaMemcpyAsync(h->log_start.data(), g.start, sizeof(int32_t) * (g.ncell + 1),
+                                   cudaMemcpyDeviceToHost, h->stream));
+    }
+    if (stats) {
+        unsigned long long c[8];
+        RP_CUDA(h, cudaMemcpyAsync(c, h->counters, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
+        RP_CUDA(h, cudaStreamSynchronize(h->stream));
+        stats->moves = c[0];
+        stats->accepted = c[1];
+        stats->rejected_overlap = c[2];
+        stats->rejected_domain = c[3];
+        stats->pair_tests = c[4];
+        stats->fp64_pairs = c[5];
+        stats->translations = c[6];
+        stats->rotations = c[7];
+    }
+    h->can_revert = false;
+    if (stats || log) return check_status(h);
+    return RP_OK;
+}
+
+int rp_sweep_log(void *handle, rp_move *moves, uint8_t *codes, int64_t capacity, int64_t *count) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !count) return fail(h, RP_ERR_ARG, "null argument");
+    if (!h->log_valid) return fail(h, RP_ERR_STATE, "no logged sweep");
+    int64_t total = h->log_types * h->n;
+    *count = total;
+    if (!moves && !codes) return RP_OK;
+    if (capacity < total) return fail(h, RP_ERR_ARG, "capacity too small");
+    RP_CUDA(h, cudaSetDevice(h->device));
+    std::vector<rp_move> raw(total);
+    std::vector<uint8_t> rc(total);
+    RP_CUDA(h, cudaMemcpyAsync(raw.data(), h->d_log, sizeof(rp_move) * total, cudaMemcpyDeviceToHost, h->stream));
+    RP_CUDA(h, cudaMemcpyAsync(rc.data(), h->d_log_codes, total, cudaMemcpyDeviceToHost, h->stream));
+    RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    const int *dims = h->log_dims;
+    int64_t ncell = static_cast<int64_t>(dims[0]) * dims[1] * dims[2];
+    int64_t o = 0;
+    for (int ph : h->log_phases) {
+        for (int64_t cell = 0; cell < ncell; cell++) {
+            int cx = static_cast<int>(cell % dims[0]), cy = static_cast<int>((cell / dims[0]) % dims[1]),
+                cz = static_cast<int>(cell / (static_cast<int64_t>(dims[0]) * dims[1]));
+            int cp = (dims[0] > 1 ? (cx & 1) : 0) | ((dims[1] > 1 ? (cy & 1) : 0) << 1) |
+                     ((dims[2] > 1 ? (cz & 1) : 0) << 2);
+            if (cp != ph) continue;
+            int64_t b = static_cast<int64_t>(h->log_types) * h->log_start[cell];
+            int64_t e = static_cast<int64_t>(h->log_types) * h->log_start[cell + 1];
+            for (int64_t k = b; k < e; k++) {
+                if (moves) moves[o] = raw[k];
+                if (codes) codes[o] = rc[k];
+                o++;
+            }
+        }
+    }
+    return RP_OK;
+}
+
+int rp_try_scaling(void *handle, const double *new_box9, double *dE) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !new_box9 || !dE) return fail(h, RP_ERR_ARG, "null argument");
+    if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
+    if (det3(new_box9) == 0 || volume_of(new_box9) == 0) return fail(h, RP_ERR_ARG, "box volume is zero");
+    RP_CUDA(h, cudaSetDevice(h->device));
+    int np = 1 - h->pcur, ng = 1 - h->gcur;
+    double new_inv[9];
+    inverse3(new_box9, new_inv);
+    RP_CUDA(h, launch_rescale(h->pos64[h->pcur], h->pos64[np], h->n, h->inv, new_box9, h->stream));
+    double tt[375];
+    translation_table(new_box9, tt);
+    RP_CUDA(h, cudaMemcpyAsync(h->trans[np], tt, sizeof(tt), cudaMemcpyHostToDevice, h->stream));
+    // switch to the new state; the old one stays in the other buffers for revert
+    std::memcpy(h->saved_box, h->box, sizeof(h->box));
+    std::memcpy(h->saved_inv, h->inv, sizeof(h->inv));
+    std::memcpy(h->box, new_box9, sizeof(h->box));
+    std::memcpy(h->inv, new_inv, sizeof(h->inv));
+    int old_p = h->pcur, old_g = h->gcur;
+    h->pcur = np;
+    h->gcur = ng;
+    double shift[3] = {h->grid[old_g].d.shift[0], h->grid[old_g].d.shift[1], h->grid[old_g].d.shift[2]};
+    int rc = setup_grid(h, h->grid[ng], h->box, shift);
+    if (rc == RP_OK) rc = rebuild(h, ng, np);
+    if (rc) {
+        std::memcpy(h->box, h->saved_box, sizeof(h->box));
+        std::memcpy(h->inv, h->saved_inv, sizeof(h->inv));
+        h->pcur = old_p;
+        h->gcur = old_g;
+        return rc;
+    }
+    h->can_revert = true;
+    h->log_valid = false;
+    // A convex shape in a box that only grew cannot overlap (core/Packing.cpp:199-200).
+    if (box_upscaled(h->saved_box, h->box)) {
+        *dE = 0;
+        RP_CUDA(h, cudaStreamSynchronize(h->stream));
+        return RP_OK;
+    }
+    int64_t cnt = 0;
+    rc = rp_count_overlaps(h, 1, &cnt);
+    if (rc) return rc;
+    *dE = cnt > 0 ? std::numeric_limits<double>::infinity() : 0.0;
+    return RP_OK;
+}
+
+int rp_revert_scaling(void *handle) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h) return RP_ERR_ARG;
+    if (!h->can_revert) return fail(h, RP_ERR_STATE, "nothing to revert");
+    std::memcpy(h->box, h->saved_box, sizeof(h->box));
+    std::memcpy(h->inv, h->saved_inv, sizeof(h->inv));
+    h->pcur = 1 - h->pcur;
+    h->gcur = 1 - h->gcur;
+    h->can_revert = false;
+    h->log_valid = false;
+    return RP_OK;
+}
+
+int rp_get_stats(void *handle, rp_sweep_stats *stats) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !stats) return RP_ERR_ARG;
+    RP_CUDA(h, cudaSetDevice(h->device));
+    unsigned long long c[8];
+    RP_CUDA(h, cudaMemcpyAsync(c, h->counters, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
+    RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    stats->moves = c[0];
+    stats->accepted = c[1];
+    stats->rejected_overlap = c[2];
+    stats->rejected_domain = c[3];
+    stats->pair_tests = c[4];
+    stats->fp64_pairs = c[5];
+    stats->translations = c[6];
+    stats->rotations = c[7];
+    return RP_OK;
+}
+
+}  // extern "C"

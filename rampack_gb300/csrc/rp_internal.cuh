@@ -1,0 +1,103 @@
+// Internal layout of the engine: device structures shared by the kernels and the
+// host orchestration in rp_api.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "rp_geom.cuh"
+#include "../../include/rampack_gb300.h"
+
+namespace rp {
+
+// Status bits a kernel may raise in the handle's device status word.
+enum : uint32_t {
+    ST_PARTICLE_NOT_IN_CELL = 1u << 0,  // a listed move's particle is not in its cell
+    ST_BAD_CELL = 1u << 1,              // a listed move names a cell outside the grid
+    ST_NUMERIC = 1u << 2,               // a non-finite coordinate was produced
+    ST_CAPACITY = 1u << 3,              // a neighbourhood exceeded the largest staging capacity
+};
+
+// Constants of the FP32 filter: every comparison of the FP64 reference is decided in
+// FP32 only when it clears a margin that bounds the FP32 error; otherwise the pair is
+// re-decided in FP64 (the guard band).
+struct FilterConsts {
+    float sphere_lo, sphere_hi;   // spheres: (2r)^2 -/+ margin
+    float core_lo, core_hi;       // spherocylinders: 4 r^2 -/+ margin
+    float far_lo, far_hi;         // spherocylinders: (2r + l)^2 -/+ margin
+    float core_thr;               // 4 r^2
+    float seg_err;                // bound on |f32 - f| of the segment distance^2
+    float d_min;                  // D = |u|^2 |v|^2 - (u.v)^2 below which FP64 decides
+    float len;                    // spherocylinder cylinder length l
+    float half_len;               // l / 2
+    float cell_margin;            // relative in-cell margin of the FP32 ActiveDomain test
+};
+
+// One checkerboard cell grid with its cell list and FP32 mirror in cell order.
+struct GridDev {
+    int dims[3];
+    int ncell;
+    double shift[3];
+    float cellmat[9];     // row-major box / n (column d divided by dims[d]), FP32
+    float cellinv[9];     // inverse of cellmat (maps local coords to in-cell fractions)
+    int32_t *count;       // [ncell]
+    int32_t *start;       // [ncell + 1]
+    int32_t *slot_pid;    // [n] particle of each slot (cells contiguous, pids ascending)
+    int32_t *pid_slot;    // [n]
+    int32_t *pid_cell;    // [n]
+    int32_t *rank;        // [n] scratch: arrival rank within the cell
+    float4 *mpos;         // [n] cell-local FP32 position, .w = pid bits
+    float4 *maxis;        // [n] FP32 axis (orientation column 2)
+    float4 *plocal;       // [n] scratch: cell-local FP32 position by pid
+    double *bounds;       // ActiveDomain bounds: dim d at boundsoff[d], 2 doubles per cell
+    int boundsoff[3];
+    int32_t *max_occ;     // device scalar
+};
+
+struct DevState {
+    int64_t n;
+    int kind;
+    double box[9], inv[9];
+    double *pos64;        // [n][3]
+    double *rot64;        // [n][9]
+    double *trans;        // [125][3] box · m for m in {-2..2}^3
+    float inv32[9];
+    ExactShape ex;
+    FilterConsts fc;
+    uint32_t *status;
+    unsigned long long *counters;  // rp_sweep_stats layout
+};
+
+constexpr int SWEEP_WARPS = 4;  // warps per block of the sweep kernel
+
+struct SweepArgs {
+    DevState s;
+    GridDev g;
+    int phase[3];
+    int active[3];
+    int num_active;
+    int cap;                       // staged candidates per warp
+    // list mode
+    const rp_move *moves;
+    const int32_t *list_cells;     // cells with moves in this phase
+    const int32_t *list_begin;     // [num_list + 1] ranges into moves / move_out
+    const int32_t *move_out;       // original index of each (sorted) move
+    int num_list;
+    uint8_t *codes;
+    // rng mode
+    uint64_t seed, counter;
+    float tstep, rstep;
+    int types;                     // bit 0 translation, bit 1 rotation
+    rp_move *log;                  // [ntypes * n] indexed by ntypes * start[cell] + k
+    uint8_t *log_codes;
+    int fp64_only;
+    // overflow: cells whose neighbourhood exceeds cap are appended here and rerun
+    int32_t *overflow;             // [ncell]
+    int32_t *overflow_count;
+    const int32_t *work;           // optional explicit list of cells (overflow rerun)
+    const int32_t *work_count;     // device-side length of `work`
+    int num_work;
+};
+
+}  // namespace rp

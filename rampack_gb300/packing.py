@@ -1,0 +1,162 @@
+"""Python mirror of the reference's Packing interface (core/Packing.h:32-466) over the C ABI.
+
+``GpuPacking`` holds one packing of spheres or spherocylinders in GPU memory.  Its
+methods keep the reference's names and meaning where one exists:
+
+* ``count_total_overlaps(early_exit)``  — Packing::countTotalOverlaps (core/Packing.cpp:519-559)
+* ``try_scaling(box)`` / ``revert_scaling()`` — Packing::tryScaling / revertScaling
+  (core/Packing.cpp:172-208, :363-371); ``try_scaling`` returns +inf on overlap, else 0
+* ``run_moves(moves)`` — a list of Packing::tryTranslation / tryRotation / tryMove calls,
+  each followed by the Metropolis test and acceptMove (core/Simulation.cpp:466-490)
+* ``sweep(...)`` — one device-driven pass of domain-decomposed moves
+  (core/Simulation.cpp:396-445)
+
+Errors raise ``EngineError`` with the C status, as the reference raises
+PreconditionException / ValidationException.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib
+from ._lib import (MOVE_DTYPE, EngineError, GridInfo, ShapeDesc, SweepParams, SweepStats, dptr)
+
+
+class GpuPacking:
+    def __init__(self, kind: int, params, pos, rot, box, device: int = 0):
+        self.lib = _lib.load()
+        params = np.asarray(params, dtype=np.float64).reshape(-1)
+        desc = ShapeDesc()
+        desc.kind = kind
+        if kind == _lib.SHAPE_SPHERE:
+            desc.radius = float(params[0])
+        elif kind == _lib.SHAPE_SPHEROCYLINDER:
+            desc.length, desc.radius = float(params[0]), float(params[1])
+        else:
+            raise EngineError(-5, f"shape kind {kind} is not handled by the GPU engine")
+        self.kind = kind
+        self.params = params
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        self.n = pos.shape[0]
+        h = C.c_void_p()
+        rc = self.lib.rp_create(C.byref(desc), self.n, device, C.byref(h))
+        if rc != 0:
+            raise EngineError(rc, "rp_create failed")
+        self.h = h
+        self.upload(pos, rot, box)
+
+    # ---- plumbing ----
+    def _check(self, rc: int):
+        if rc != 0:
+            msg = self.lib.rp_last_error(self.h)
+            raise EngineError(rc, msg.decode() if msg else "")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.rp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---- state ----
+    def upload(self, pos, rot, box):
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        rot = np.ascontiguousarray(rot, dtype=np.float64).reshape(-1, 9)
+        box = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
+        if pos.shape[0] != self.n or rot.shape[0] != self.n:
+            raise EngineError(-1, "state size mismatch")
+        self._check(self.lib.rp_upload_state(self.h, dptr(pos), dptr(rot), dptr(box)))
+
+    def state(self):
+        pos = np.zeros((self.n, 3))
+        rot = np.zeros((self.n, 9))
+        box = np.zeros(9)
+        self._check(self.lib.rp_download_state(self.h, dptr(pos), dptr(rot), dptr(box)))
+        return pos, rot, box
+
+    # ---- overlaps ----
+    def count_total_overlaps(self, early_exit: bool = False) -> int:
+        out = C.c_int64()
+        self._check(self.lib.rp_count_overlaps(self.h, 1 if early_exit else 0, C.byref(out)))
+        return int(out.value)
+
+    # ---- grid and moves ----
+    @staticmethod
+    def _info(info: GridInfo) -> dict:
+        return {"dims": tuple(info.dims), "max_occupancy": info.max_occupancy, "shift": tuple(info.shift),
+                "cell_height": tuple(info.cell_height), "num_cells": int(info.num_cells)}
+
+    def set_grid(self, shift=(0.0, 0.0, 0.0)) -> dict:
+        """Rebuilds the checkerboard grid with a relative origin shift; returns its layout."""
+        s = np.ascontiguousarray(shift, dtype=np.float64)
+        info = GridInfo()
+        self._check(self.lib.rp_set_grid(self.h, dptr(s), C.byref(info)))
+        return self._info(info)
+
+    def grid(self):
+        """(layout, cell of every particle, ActiveDomain bounds lo[3] hi[3] of every cell)."""
+        info = GridInfo()
+        self._check(self.lib.rp_get_grid(self.h, C.byref(info), None, None))
+        cells = np.zeros(self.n, dtype=np.int32)
+        bounds = np.zeros((int(info.num_cells), 6))
+        self._check(self.lib.rp_get_grid(self.h, None, cells.ctypes.data_as(C.POINTER(C.c_int32)), dptr(bounds)))
+        return self._info(info), cells, bounds
+
+    def run_moves(self, moves: np.ndarray) -> np.ndarray:
+        moves = np.ascontiguousarray(moves, dtype=MOVE_DTYPE)
+        codes = np.zeros(len(moves), dtype=np.uint8)
+        self._check(self.lib.rp_run_moves(self.h, moves.ctypes.data_as(C.c_void_p), len(moves),
+                                          codes.ctypes.data_as(C.c_void_p)))
+        return codes
+
+    def sweep(self, translation_step: float, rotation_step: float, seed: int, counter: int,
+              log: bool = False, fp64_only: bool = False, stats: bool = True):
+        p = SweepParams()
+        p.translation_step = translation_step
+        p.rotation_step = rotation_step
+        p.seed = seed
+        p.counter = counter
+        p.flags = (_lib.SWEEP_LOG if log else 0) | (_lib.SWEEP_FP64_ONLY if fp64_only else 0)
+        st = SweepStats()
+        self._check(self.lib.rp_sweep(self.h, C.byref(p), C.byref(st) if stats else None))
+        return st.as_dict() if stats else None
+
+    def sweep_log(self):
+        cnt = C.c_int64()
+        self._check(self.lib.rp_sweep_log(self.h, None, None, 0, C.byref(cnt)))
+        moves = np.zeros(cnt.value, dtype=MOVE_DTYPE)
+        codes = np.zeros(cnt.value, dtype=np.uint8)
+        self._check(self.lib.rp_sweep_log(self.h, moves.ctypes.data_as(C.c_void_p),
+                                          codes.ctypes.data_as(C.c_void_p), cnt.value, C.byref(cnt)))
+        return moves, codes
+
+    def stats(self) -> dict:
+        st = SweepStats()
+        self._check(self.lib.rp_get_stats(self.h, C.byref(st)))
+        return st.as_dict()
+
+    # ---- box moves ----
+    def try_scaling(self, box) -> float:
+        b = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
+        dE = C.c_double()
+        self._check(self.lib.rp_try_scaling(self.h, dptr(b), C.byref(dE)))
+        return float(dE.value)
+
+    def revert_scaling(self):
+        self._check(self.lib.rp_revert_scaling(self.h))
+
+
+INF = math.inf

@@ -1,0 +1,68 @@
+"""Seeded test systems: lattices from rampack_gb300.workloads, thermalised by the CPU
+oracle's cycle loop (the reference's Simulation restated), optionally compressed so
+that overlaps appear."""
+from __future__ import annotations
+
+import functools
+
+import numpy as np
+
+import pyoracle as po
+from rampack_gb300 import workloads as W
+
+
+def thermalise(cfg, cycles: int, seed: int = 1234, **kw):
+    kind, prm, pos, rot, box = cfg
+    pk = po.CpuPacking("oracle", kind, prm, pos, rot, box, threads=kw.pop("threads", 1))
+    if cycles:
+        po.run_cycles(pk, cycles, seed=seed, **kw)
+    p, r, b = pk.state()
+    pk.close()
+    return kind, prm, p, r, b
+
+
+@functools.lru_cache(maxsize=None)
+def hs_small():
+    """Hard spheres d=1, N=512 at phi=0.30, 30 NpT cycles (p*=10)."""
+    return thermalise(W.hard_spheres(8, 0.30), 30, translation_step=0.1, box_kind=2, box_step=0.01 / 3,
+                      pressure=10.0)
+
+
+@functools.lru_cache(maxsize=None)
+def hs_dense():
+    """Hard spheres d=1, N=1000 at phi=0.45, 30 NVT cycles."""
+    return thermalise(W.hard_spheres(10, 0.45), 30, translation_step=0.1)
+
+
+@functools.lru_cache(maxsize=None)
+def sc_l2():
+    """Spherocylinders l=2 r=0.5, N=1000, phi=0.35, triclinic after 20 NpT cycles."""
+    return thermalise(W.spherocylinders((10, 10, 10), 0.35, 2.0, 0.5, aspect=(1, 1, 3)), 20,
+                      translation_step=0.2, rotation_step=0.2, box_kind=1, box_step=0.005, pressure=1.5)
+
+
+@functools.lru_cache(maxsize=None)
+def sc_l2_dense():
+    """Spherocylinders l=2 r=0.5, N=1728, phi=0.50, 15 NVT cycles (dense, many rejections)."""
+    return thermalise(W.spherocylinders((12, 12, 12), 0.50, 2.0, 0.5, aspect=(1, 1, 3)), 15,
+                      translation_step=0.2, rotation_step=0.2)
+
+
+@functools.lru_cache(maxsize=None)
+def sc_l5():
+    """Spherocylinders l=5 r=0.5, N=2000 (10x10x20), phi=0.35, 10 NpT cycles."""
+    return thermalise(W.spherocylinders((10, 10, 20), 0.35, 5.0, 0.5, aspect=(1, 1, 6)), 10,
+                      translation_step=0.2, rotation_step=0.2, box_kind=1, box_step=0.005, pressure=1.5)
+
+
+def compressed(cfg, factor: float):
+    """The same configuration with box and positions scaled by `factor` (overlaps for factor < 1)."""
+    kind, prm, pos, rot, box = cfg
+    b = np.array(box, dtype=np.float64).reshape(3, 3)
+    rel = np.clip(pos @ np.linalg.inv(b).T, 1e-9, 1 - 1e-9)
+    nb = b * factor
+    p = rel @ nb.T
+    return kind, prm, np.ascontiguousarray(p), rot, nb.reshape(9)
+
+
+ALL = {"hs_small": hs_small, "hs_dense": hs_dense, "sc_l2": sc_l2, "sc_l2_dense": sc_l2_dense, "sc_l5": sc_l5}

@@ -1,0 +1,152 @@
+"""GPU parity against the CPU oracle (the reference's algorithm restated; pinned to the
+reference's own outputs by tests/test_oracle_vs_reference.py and the golden fixtures).
+
+Every decision is compared bit-exactly: overlap counts, per-move outcome codes
+(accept/reject and the reason), the final FP64 positions and orientations, and box-move
+outcomes.  Move streams are drawn by the reference's sampler algorithms (restated in
+the oracle) or logged by the GPU's own device-driven sweep and replayed serially."""
+import numpy as np
+import pytest
+
+import pyoracle as po
+import systems
+from rampack_gb300 import _lib
+
+pytestmark = pytest.mark.gpu
+
+CASES = ["hs_small", "hs_dense", "sc_l2", "sc_l2_dense", "sc_l5"]
+
+
+def gpu_packing(cfg):
+    from rampack_gb300.packing import GpuPacking
+    kind, prm, pos, rot, box = cfg
+    return GpuPacking(kind, prm, pos, rot, box)
+
+
+def cpu_packing(cfg):
+    kind, prm, pos, rot, box = cfg
+    return po.CpuPacking("oracle", kind, prm, pos, rot, box, threads=1)
+
+
+def steps(cfg):
+    return (0.1, 0.0) if cfg[0] == 0 else (0.2, 0.2)
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("factor", [1.0, 0.97, 0.9])
+def test_count_overlaps(oracle, engine, name, factor):
+    cfg = systems.ALL[name]()
+    if factor != 1.0:
+        cfg = systems.compressed(cfg, factor)
+    cpu = cpu_packing(cfg)
+    expect = cpu.count_overlaps(False)
+    expect_early = cpu.count_overlaps(True)
+    with gpu_packing(cfg) as g:
+        for shift in [(0, 0, 0), (0.37, 0.81, 0.05)]:
+            g.set_grid(shift)
+            assert g.count_total_overlaps(False) == expect
+            assert g.count_total_overlaps(True) == expect_early
+    if factor == 1.0:
+        assert expect == 0
+
+
+def draw_cell_moves(cpu, g, seed, trans, rot, shift):
+    """Moves for every active cell, phase by phase, drawn with the reference samplers'
+    algorithm from each cell's particle list (DD domain = cell)."""
+    info = g.set_grid(shift)
+    _, cells, bounds = g.grid()
+    dims = info["dims"]
+    rng = cpu.rng(seed)
+    chunks = []
+    for ph in range(8):
+        par = [(ph >> d) & 1 for d in range(3)]
+        if any(dims[d] == 1 and par[d] for d in range(3)):
+            continue
+        for cell in range(info["num_cells"]):
+            c = (cell % dims[0], (cell // dims[0]) % dims[1], cell // (dims[0] * dims[1]))
+            if any(dims[d] > 1 and (c[d] & 1) != par[d] for d in range(3)):
+                continue
+            idx = np.nonzero(cells == cell)[0]
+            if len(idx) == 0:
+                continue
+            ntypes = (trans > 0) + (rot > 0)
+            chunks.append(cpu.draw_moves(rng, trans, rot, idx, len(idx), ntypes * len(idx), domain=cell))
+    cpu.rng_free(rng)
+    return np.concatenate(chunks), bounds
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_move_list_parity(oracle, engine, name):
+    cfg = systems.ALL[name]()
+    cpu = cpu_packing(cfg)
+    t, r = steps(cfg)
+    with gpu_packing(cfg) as g:
+        for rnd, shift in enumerate([(0.0, 0.0, 0.0), (0.61, 0.13, 0.77), (0.29, 0.93, 0.41)]):
+            moves, bounds = draw_cell_moves(cpu, g, 100 + rnd, t, r, shift)
+            got = g.run_moves(moves)
+            want, _ = cpu.replay(moves, bounds)
+            assert np.array_equal(got, want), f"round {rnd}: {np.count_nonzero(got != want)} codes differ"
+            gp, gr, gb = g.state()
+            cp, cr, cb = cpu.state()
+            assert np.array_equal(gp, cp) and np.array_equal(gr, cr) and np.array_equal(gb, cb)
+        acc = np.count_nonzero(got & _lib.CODE_ACCEPTED)
+        assert 0 < acc < len(got)
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("fp64_only", [False, True])
+def test_sweep_log_replays_on_oracle(oracle, engine, name, fp64_only):
+    cfg = systems.ALL[name]()
+    cpu = cpu_packing(cfg)
+    t, r = steps(cfg)
+    with gpu_packing(cfg) as g:
+        for cycle in range(3):
+            st = g.sweep(t, r, seed=2024, counter=cycle, log=True, fp64_only=fp64_only)
+            moves, codes = g.sweep_log()
+            _, _, bounds = g.grid()
+            assert st["moves"] == len(moves) == (1 + (r > 0)) * g.n
+            want, _ = cpu.replay(moves, bounds)
+            assert np.array_equal(codes, want), f"cycle {cycle}: {np.count_nonzero(codes != want)} codes differ"
+            gp, gr, _ = g.state()
+            cp, cr, _ = cpu.state()
+            assert np.array_equal(gp, cp) and np.array_equal(gr, cr)
+            assert g.count_total_overlaps(True) == 0
+
+
+def test_fp32_filter_matches_fp64_only(engine):
+    cfg = systems.sc_l2_dense()
+    t, r = steps(cfg)
+    states = []
+    for fp64_only in (False, True):
+        with gpu_packing(cfg) as g:
+            for cycle in range(4):
+                g.sweep(t, r, seed=7, counter=cycle, fp64_only=fp64_only)
+            states.append(g.state())
+    assert np.array_equal(states[0][0], states[1][0]) and np.array_equal(states[0][1], states[1][1])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_box_moves(oracle, engine, name):
+    cfg = systems.ALL[name]()
+    cpu = cpu_packing(cfg)
+    rng = np.random.default_rng(5)
+    with gpu_packing(cfg) as g:
+        for k in range(12):
+            _, _, box = cpu.state()
+            b = box.reshape(3, 3)
+            if k % 3 == 0:
+                nb = b * (1 + rng.uniform(-0.02, 0.02))
+            elif k % 3 == 1:
+                nb = b + rng.uniform(-0.05, 0.05, size=(3, 3))
+            else:
+                nb = b * 0.9
+            nb = nb.reshape(9)
+            want = cpu.try_scaling(nb)
+            got = g.try_scaling(nb)
+            assert got == want
+            if want > 0:
+                cpu.revert_scaling()
+                g.revert_scaling()
+            gp, gr, gb = g.state()
+            cp, cr, cb = cpu.state()
+            assert np.array_equal(gp, cp) and np.array_equal(gb, cb)
