@@ -1,0 +1,397 @@
+#!/usr/bin/env python3
+"""Benchmark of the hard-particle Monte Carlo move-and-overlap path.
+
+Workload (one "step" = one Monte Carlo cycle): hard spherocylinders l=2, r=0.5 (L/D=2),
+N = 100^3 = 1,000,000 started aligned on an orthorhombic lattice (cell aspect 1:1:3) at
+packing fraction 0.50 in a box that the isotension moves make triclinic; each cycle is
+2N particle moves (translation step 0.2 and rotation step 0.2, half each, in
+checkerboard domains) plus one isotension box move (every box-matrix entry perturbed
+by up to 0.005, p* = 1.5, T = 1) whose overlap check rescales, rebuilds the cell grid
+and recounts all overlaps.  Synthetic seeded input; no dataset.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W]           GPU engine (this repo)
+  python bench.py --impl reference [--steps K] [--warmup W]     CPU implementation of the path
+
+Metric: attempted particle moves per second (higher is better).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "moves/sec at N=1e6"
+UNIT = "moves/s"
+TRANS_STEP, ROT_STEP, BOX_STEP, PRESSURE, TEMPERATURE = 0.2, 0.2, 0.005, 1.5, 1.0
+WORKLOAD = ("hard spherocylinders l=2 r=0.5 (L/D=2), N={n:,}, aligned orthorhombic start at phi=0.50 "
+            "(cell aspect 1:1:3), triclinic box; per cycle 2N moves (translation 0.2, rotation 0.2) "
+            "+ 1 isotension box move (delta 0.005, p*=1.5, T=1)")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--n-side", type=int, default=100, help="particles per lattice side (default 100 -> 1e6)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--seed", type=int, default=1234)
+    return ap.parse_args()
+
+
+def workload(n_side):
+    from rampack_gb300 import workloads as W
+    return W.spherocylinders((n_side, n_side, n_side), 0.50, 2.0, 0.5, aspect=(1.0, 1.0, 3.0))
+
+
+# ----------------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ----------------------------------------------------------------------------------
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu=timestamp,{self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self, t0: float, t1: float) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 10:
+                continue
+            try:
+                ts = time.mktime(time.strptime(parts[0].split(".")[0], "%Y/%m/%d %H:%M:%S"))
+                frac = float("0." + parts[0].split(".")[1]) if "." in parts[0] else 0.0
+                rows.append((ts + frac, parts))
+            except Exception:
+                continue
+        os.unlink(self.path)
+        inside = [p for ts, p in rows if t0 - 0.15 <= ts <= t1 + 0.15]
+        if not inside and rows:  # timed region shorter than the sampling period: nearest samples
+            rows.sort(key=lambda r: abs(r[0] - 0.5 * (t0 + t1)))
+            inside = [p for _, p in rows[:3]]
+        if not inside:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(p[2]) for p in inside if p[2].replace(".", "").isdigit()]
+        mx = [float(p[3]) for p in inside if p[3].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for p in inside for k in range(4) if p[6 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(inside)}
+
+
+# ----------------------------------------------------------------------------------
+# CPU implementation (the oracle port of the reference's path; all host threads)
+# ----------------------------------------------------------------------------------
+def cpu_domains(threads: int):
+    """Domain divisions for the CPU run: the largest product <= threads, z (the long axis) first."""
+    best = (1, 1, 1)
+    for dz in range(1, threads + 1):
+        for dy in range(1, threads + 1):
+            for dx in range(1, threads + 1):
+                p = dx * dy * dz
+                if p <= threads and dx <= dy <= dz and p > best[0] * best[1] * best[2]:
+                    best = (dx, dy, dz)
+    return best
+
+
+def cpu_run(cfg, cycles: int, warmup: int, threads: int, seed: int):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    po.build()
+    kind, prm, pos, rot, box = cfg
+    pk = po.CpuPacking("oracle", kind, prm, pos, rot, box, threads=threads)
+    dom = cpu_domains(threads)
+    kw = dict(translation_step=TRANS_STEP, rotation_step=ROT_STEP, box_kind=1, box_step=BOX_STEP,
+              pressure=PRESSURE, temperature=TEMPERATURE, domains=dom, threads=threads, seed=seed)
+    if warmup:
+        po.run_cycles(pk, warmup, **kw)
+    times = []
+    for c in range(cycles):
+        t = time.perf_counter()
+        st = po.run_cycles(pk, 1, **dict(kw, seed=seed + 1000 + c))
+        times.append(time.perf_counter() - t)
+    pk.close()
+    moves = 2 * len(pos)
+    return moves, times, dom, list(st.domains)
+
+
+def main_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    cfg = workload(args.n_side)
+    moves, times, dom, dom_used = cpu_run(cfg, max(1, args.steps), max(0, args.warmup), threads, args.seed)
+    total = sum(times)
+    value = moves * len(times) / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": len(times), "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD.format(n=len(cfg[2])), "n": len(cfg[2]), "moves_per_step": moves,
+                   "parallelism": f"OpenMP domain decomposition {dom_used}"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{len(times)} full cycles of the N={len(cfg[2]):,} system after "
+                                   f"{args.warmup} warm-up cycles; oracle/ restatement of the reference's "
+                                   f"Simulation/Packing (reference sources are not present on this host)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ----------------------------------------------------------------------------------
+# GPU engine
+# ----------------------------------------------------------------------------------
+def propose_box(box, rng):
+    """Isotension proposal: every box-matrix entry + U(-0.005, 0.005) (TriclinicDeltaScaler)."""
+    return box + rng.uniform(-BOX_STEP, BOX_STEP, size=9)
+
+
+def box_volume(box):
+    return abs(np.linalg.det(box.reshape(3, 3)))
+
+
+def cycle(g, k, seed, rng, stats=False):
+    """One Monte Carlo cycle: a device sweep of 2N moves, then one box move whose Metropolis
+    pre-check runs first on the host (core/Simulation.cpp:512-530)."""
+    st = g.sweep(TRANS_STEP, ROT_STEP, seed=seed, counter=k, stats=stats)
+    box = g.box
+    nb = propose_box(box, rng)
+    v0, v1 = box_volume(box), box_volume(nb)
+    expo = g.n * math.log(v1 / v0) - PRESSURE * (v1 - v0) / TEMPERATURE
+    u = rng.uniform()
+    accepted = False
+    if u <= math.exp(min(expo, 700.0)):
+        if g.try_scaling(nb) > 0:
+            g.revert_scaling()
+        else:
+            g.box = nb
+            accepted = True
+    return st, accepted
+
+
+def read_profile_traffic():
+    """Per-launch DRAM traffic of the sweep kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "k_sweep_sc_n1e6.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def main_gpu(args):
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+
+    from rampack_gb300 import build as rb
+    rb.build()
+    from rampack_gb300.packing import GpuPacking
+
+    cfg = workload(args.n_side)
+    kind, prm, pos, rot, box = cfg
+    n = len(pos)
+    g = GpuPacking(kind, prm, pos, rot, box, device=local)
+    g.box = np.array(box, dtype=np.float64)
+    stream = torch.cuda.ExternalStream(g.stream(), device=local)
+    rng = np.random.default_rng(args.seed + rank)
+    seed = args.seed + 7919 * rank
+
+    k = 0
+    for _ in range(max(3, args.warmup)):
+        cycle(g, k, seed, rng)
+        k += 1
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+
+    s0 = g.stats()
+    g.set_timing(True)
+    clocks = Clocks(local)
+    clocks.start()
+    time.sleep(0.3)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0 = time.time()
+    ev0.record(stream)
+    box_acc = 0
+    for _ in range(args.steps):
+        _, acc = cycle(g, k, seed, rng)
+        box_acc += acc
+        k += 1
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    t1 = time.time()
+    ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop(t0, t1)
+    timing = g.timing()
+    g.set_timing(False)
+    s1 = g.stats()
+    if dist:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+
+    moves = s1["moves"] - s0["moves"]
+    value = moves * world / (ms / 1e3)
+    acc_rate = (s1["accepted"] - s0["accepted"]) / max(1, moves)
+    pairs = s1["pair_tests"] - s0["pair_tests"]
+    fp64 = s1["fp64_pairs"] - s0["fp64_pairs"]
+    launches = s1["kernel_launches"] - s0["kernel_launches"]
+
+    # ---- roofline of the dominant kernel (the checkerboard sweep, one launch per phase) ----
+    sweep_ms, sweep_launches = timing["sweep"]
+    info, _, _ = g.grid()
+    phases = 1
+    for d in info["dims"]:
+        phases *= 2 if d > 1 else 1
+    ncell = info["num_cells"]
+    moves_per_sweep = 2 * n
+    # algorithmic bytes per sweep: each phase streams every particle's FP32 record (28 B) and
+    # cell index (4 B) and the cell offsets; every move reads the mover's FP64 state (96 B)
+    # and an accepted move writes FP64 (96 B) and FP32 (28 B) state back.
+    b_sweep = phases * n * (28 + 4) + phases * (ncell + 1) * 4 + moves_per_sweep * (96 + acc_rate * (96 + 28))
+    b_launch = b_sweep / phases
+    avg_launch_ms = sweep_ms / max(1, sweep_launches)
+    achieved = b_launch / (avg_launch_ms / 1e3) / 1e9
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peak, peak_src = json.load(open(peaks_path))["hbm_gbs"], "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+    traffic = read_profile_traffic()
+
+    # ---- end to end through the C ABI with host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        hpos = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+        hrot = torch.empty((n, 9), dtype=torch.float64, pin_memory=True).numpy()
+        p0, r0, b0 = g.state()
+        hpos[:] = p0
+        hrot[:] = r0
+        hbox = b0.copy()
+        torch.cuda.synchronize()
+        e_steps = max(1, args.steps)
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        m0 = g.stats()["moves"]
+        f0.record(stream)
+        for _ in range(e_steps):
+            g.upload(hpos, hrot, hbox)   # H2D of the step's input state
+            g.box = hbox.copy()
+            cycle(g, k, seed, rng)
+            k += 1
+            p1, r1, b1 = g.state()       # D2H of the step's result
+            hpos[:] = p1
+            hrot[:] = r1
+            hbox = b1
+        f1.record(stream)
+        f1.synchronize()
+        e_ms = f0.elapsed_time(f1)
+        e_moves = g.stats()["moves"] - m0
+        if dist:
+            t = torch.tensor([e_ms], device=f"cuda:{local}")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e_ms = float(t.item())
+        e2e = {"value": e_moves * world / (e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": int(n * 12 * 8),
+               "d2h_bytes_per_step": int(n * 12 * 8),
+               "step": "rp_upload_state (pinned host -> device) + one cycle + rp_download_state"}
+
+    # ---- CPU baseline (rank 0, N=1 only) ----
+    cpu_base = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        cmoves, ctimes, dom, dom_used = cpu_run(cfg, 2, 1, threads, args.seed)
+        cpu_base = {"value": cmoves * len(ctimes) / sum(ctimes), "unit": UNIT, "cores": threads, "kind": "port",
+                    "sample": f"2 full cycles of the same N={n:,} system after 1 warm-up cycle, OpenMP domain "
+                              f"decomposition {dom_used} (oracle/ restatement of the reference's path)"}
+
+    g.close()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD.format(n=n), "n": n, "moves_per_step": 2 * n,
+                       "variant": "plain (unordered FP32 filter + FP64 guard band)",
+                       "l2": "inputs larger than L2 (FP64 state 96 MB + FP32 mirror 32 MB + cell lists)",
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "grid_dims": list(info["dims"]), "box_moves_accepted": box_acc},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "k_sweep (one launch per checkerboard phase)",
+                         "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
+                         else "fallback 6.8 TB/s",
+                         "avg_launch_ms": avg_launch_ms, "bytes_per_launch": b_launch},
+            "kernel_ms": {kname: {"ms": v[0], "groups": v[1]} for kname, v in timing.items()},
+            "acceptance": acc_rate, "guard_band": {"pair_tests": pairs, "fp64_pairs": fp64,
+                                                   "rate": fp64 / max(1, pairs)},
+            "gpu_launches": launches, "clocks": clk,
+            "e2e": e2e, "cpu_baseline": cpu_base,
+        }
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return main_reference(args)
+    return main_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -106,7 +106,16 @@ typedef struct rp_sweep_stats {
     uint64_t fp64_pairs;          /* pairs re-decided in FP64 (the guard band) */
     uint64_t translations;
     uint64_t rotations;
+    uint64_t kernel_launches;     /* kernels this library launched (all calls since creation) */
 } rp_sweep_stats;
+
+/* Kernel groups timed by rp_get_timing. */
+#define RP_KERNEL_SWEEP 0         /* checkerboard move sweep (one launch per phase) */
+#define RP_KERNEL_REBUILD 1       /* cell-grid rebuild (assign, scan, scatter, finish) */
+#define RP_KERNEL_COUNT 2         /* all-pairs overlap recount */
+#define RP_KERNEL_RESCALE 3       /* box rescale */
+#define RP_KERNEL_OVERFLOW 4      /* large-capacity rerun of oversized neighbourhoods */
+#define RP_NUM_KERNELS 5
 
 /* ---- lifetime ---------------------------------------------------------------------- */
 
@@ -192,6 +201,18 @@ int rp_revert_scaling(void *handle);
 
 /* Cumulative counters of all sweeps and move lists since creation. */
 int rp_get_stats(void *handle, rp_sweep_stats *stats);
+
+/* The cudaStream_t on which all device work of the handle runs (for the caller's own
+ * CUDA events); no reference counterpart (the reference is CPU-only). */
+int rp_get_stream(void *handle, void **stream);
+
+/* Turns per-kernel-group device timing on (CUDA events recorded around every launch
+ * group on the handle's stream) or off; turning it on clears the accumulated times. */
+int rp_set_timing(void *handle, int on);
+
+/* Accumulated device time (ms) and launch-group count per kernel group
+ * (RP_NUM_KERNELS entries each) since timing was turned on; synchronizes the stream. */
+int rp_get_timing(void *handle, double *ms, uint64_t *groups);
 
 #ifdef __cplusplus
 }

@@ -48,7 +48,7 @@ class SweepParams(C.Structure):
 class SweepStats(C.Structure):
     _fields_ = [("moves", C.c_uint64), ("accepted", C.c_uint64), ("rejected_overlap", C.c_uint64),
                 ("rejected_domain", C.c_uint64), ("pair_tests", C.c_uint64), ("fp64_pairs", C.c_uint64),
-                ("translations", C.c_uint64), ("rotations", C.c_uint64)]
+                ("translations", C.c_uint64), ("rotations", C.c_uint64), ("kernel_launches", C.c_uint64)]
 
     def as_dict(self) -> dict:
         return {name: int(getattr(self, name)) for name, _ in self._fields_}
@@ -73,7 +73,11 @@ SIGNATURES = {
     "rp_try_scaling": (C.c_int, [_P, _D, _D]),
     "rp_revert_scaling": (C.c_int, [_P]),
     "rp_get_stats": (C.c_int, [_P, C.POINTER(SweepStats)]),
+    "rp_get_stream": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
+    "rp_set_timing": (C.c_int, [_P, C.c_int]),
+    "rp_get_timing": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]),
 }
+KERNEL_GROUPS = ["sweep", "rebuild", "count", "rescale", "overflow"]
 
 _LIB = None
 

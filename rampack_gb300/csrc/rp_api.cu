@@ -79,6 +79,50 @@ struct Handle {
     std::vector<int32_t> log_start;
     int log_dims[3]{};
     std::vector<int> log_phases;
+    // launch accounting and optional per-group device timing
+    uint64_t launches = 0;
+    bool timing = false;
+    struct Mark {
+        int kid;
+        cudaEvent_t a, b;
+    };
+    std::vector<Mark> marks;
+    std::vector<cudaEvent_t> event_pool;
+    double kernel_ms[RP_NUM_KERNELS]{};
+    uint64_t kernel_groups[RP_NUM_KERNELS]{};
+    bool strict_box = false;
+};
+
+cudaEvent_t pool_event(Handle *h) {
+    if (!h->event_pool.empty()) {
+        cudaEvent_t e = h->event_pool.back();
+        h->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// One group of kernel launches: counted, and bracketed by CUDA events when timing is on.
+struct Group {
+    Handle *h;
+    int kid;
+    cudaEvent_t a = nullptr;
+    Group(Handle *h_, int kid_, int nkernels) : h{h_}, kid{kid_} {
+        h->launches += static_cast<uint64_t>(nkernels);
+        if (h->timing) {
+            a = pool_event(h);
+            cudaEventRecord(a, h->stream);
+        }
+    }
+    ~Group() {
+        if (a) {
+            cudaEvent_t b = pool_event(h);
+            cudaEventRecord(b, h->stream);
+            h->marks.push_back({kid, a, b});
+        }
+    }
 };
 
 int fail(Handle *h, int code, const std::string &msg) {
@@ -157,6 +201,7 @@ DevState dev_state(Handle *h) {
     s.ex = h->ex;
     s.status = h->status;
     s.counters = h->counters;
+    s.strict_box = h->strict_box ? 1 : 0;
     // ---- FP32 filter margins for the current grid ----
     const GridHost &g = h->grid[h->gcur];
     double lrow = 0;
@@ -310,6 +355,7 @@ int rebuild(Handle *h, int gi, int pi) {
     DevState s = dev_state(h);
     h->gcur = saved_g;
     h->pcur = saved_p;
+    Group grp(h, RP_KERNEL_REBUILD, 6);
     RP_CUDA(h, launch_rebuild(s, h->grid[gi].d, h->block_sums, h->stream));
     return RP_OK;
 }
@@ -324,6 +370,7 @@ int check_status(Handle *h) {
         std::snprintf(buf, sizeof(buf), "device status 0x%x%s%s", st,
                       (st & ST_PARTICLE_NOT_IN_CELL) ? " (a move's particle is not in its cell)" : "",
                       (st & ST_CAPACITY) ? " (a cell neighbourhood exceeds the staging capacity)" : "");
+        if (st & ST_OUTSIDE) return fail(h, RP_ERR_ARG, "a particle lies outside the box");
         return fail(h, (st & ST_CAPACITY) ? RP_ERR_CAPACITY : RP_ERR_DEVICE, buf);
     }
     return RP_OK;
@@ -354,7 +401,10 @@ int run_overflow(Handle *h, SweepArgs a, bool list) {
     a.work_count = h->overflow_count;
     a.num_work = -1;
     a.overflow = nullptr;
-    RP_CUDA(h, launch_sweep(a, list, OVF_WARPS, h->stream));
+    {
+        Group grp(h, RP_KERNEL_OVERFLOW, 1);
+        RP_CUDA(h, launch_sweep(a, list, OVF_WARPS, h->stream));
+    }
     RP_CUDA(h, cudaMemsetAsync(h->overflow_count, 0, sizeof(int32_t), h->stream));
     return RP_OK;
 }
@@ -450,6 +500,11 @@ int rp_destroy(void *handle) {
     cudaFree(h->d_codes);
     cudaFree(h->d_log);
     cudaFree(h->d_log_codes);
+    for (auto &m : h->marks) {
+        cudaEventDestroy(m.a);
+        cudaEventDestroy(m.b);
+    }
+    for (auto e : h->event_pool) cudaEventDestroy(e);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return RP_OK;
@@ -467,12 +522,6 @@ int rp_upload_state(void *handle, const double *pos, const double *rot, const do
     double inv[9];
     if (det3(box9) == 0) return fail(h, RP_ERR_ARG, "box volume is zero");
     inverse3(box9, inv);
-    // core/Packing.cpp:1069-1075 (areShapesWithinBox)
-    for (int64_t i = 0; i < h->n; i++) {
-        d3 r = mv3(inv, d3{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]});
-        if (r.x < 0 || r.x >= 1 || r.y < 0 || r.y >= 1 || r.z < 0 || r.z >= 1)
-            return fail(h, RP_ERR_ARG, "a particle lies outside the box");
-    }
     std::memcpy(h->box, box9, sizeof(h->box));
     std::memcpy(h->inv, inv, sizeof(h->inv));
     h->pcur = 0;
@@ -485,9 +534,13 @@ int rp_upload_state(void *handle, const double *pos, const double *rot, const do
     double shift[3] = {0, 0, 0};
     int rc = setup_grid(h, h->grid[0], h->box, shift);
     if (rc) return rc;
+    h->has_state = false;
+    h->strict_box = true;
     rc = rebuild(h, 0, 0);
+    h->strict_box = false;
     if (rc) return rc;
-    RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    rc = check_status(h);  // the rebuild checks that every particle lies inside the box
+    if (rc) return rc;
     h->has_state = true;
     h->can_revert = false;
     h->log_valid = false;
@@ -517,7 +570,10 @@ int rp_count_overlaps(void *handle, int early_exit, int64_t *out_count) {
     RP_CUDA(h, cudaMemsetAsync(h->count_out, 0, sizeof(unsigned long long), h->stream));
     RP_CUDA(h, cudaMemsetAsync(h->flag, 0, sizeof(int), h->stream));
     DevState s = dev_state(h);
-    RP_CUDA(h, launch_count(s, h->grid[h->gcur].d, early_exit ? 1 : 0, h->count_out, h->flag, h->stream));
+    {
+        Group grp(h, RP_KERNEL_COUNT, 1);
+        RP_CUDA(h, launch_count(s, h->grid[h->gcur].d, early_exit ? 1 : 0, h->count_out, h->flag, h->stream));
+    }
     unsigned long long c = 0;
     RP_CUDA(h, cudaMemcpyAsync(&c, h->count_out, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
     RP_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -668,7 +724,10 @@ int rp_run_moves(void *handle, const rp_move *moves, int64_t n, uint8_t *out_cod
         a.num_list = b.ncells;
         a.codes = h->d_codes;
         a.types = 3;
-        RP_CUDA(h, launch_sweep(a, true, b.ncells, h->stream));
+        {
+            Group grp(h, RP_KERNEL_SWEEP, 1);
+            RP_CUDA(h, launch_sweep(a, true, b.ncells, h->stream));
+        }
         int rc = run_overflow(h, a, true);
         if (rc) return rc;
     }
@@ -745,7 +804,10 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
             a.log = h->d_log;
             a.log_codes = h->d_log_codes;
         }
-        RP_CUDA(h, launch_sweep(a, false, a.num_active, h->stream));
+        {
+            Group grp(h, RP_KERNEL_SWEEP, 1);
+            RP_CUDA(h, launch_sweep(a, false, a.num_active, h->stream));
+        }
         rc = run_overflow(h, a, false);
         if (rc) return rc;
     }
@@ -770,6 +832,7 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
         stats->fp64_pairs = c[5];
         stats->translations = c[6];
         stats->rotations = c[7];
+        stats->kernel_launches = h->launches;
     }
     h->can_revert = false;
     if (stats || log) return check_status(h);
@@ -821,7 +884,10 @@ int rp_try_scaling(void *handle, const double *new_box9, double *dE) {
     int np = 1 - h->pcur, ng = 1 - h->gcur;
     double new_inv[9];
     inverse3(new_box9, new_inv);
-    RP_CUDA(h, launch_rescale(h->pos64[h->pcur], h->pos64[np], h->n, h->inv, new_box9, h->stream));
+    {
+        Group grp(h, RP_KERNEL_RESCALE, 1);
+        RP_CUDA(h, launch_rescale(h->pos64[h->pcur], h->pos64[np], h->n, h->inv, new_box9, h->stream));
+    }
     double tt[375];
     translation_table(new_box9, tt);
     RP_CUDA(h, cudaMemcpyAsync(h->trans[np], tt, sizeof(tt), cudaMemcpyHostToDevice, h->stream));
@@ -886,6 +952,53 @@ int rp_get_stats(void *handle, rp_sweep_stats *stats) {
     stats->fp64_pairs = c[5];
     stats->translations = c[6];
     stats->rotations = c[7];
+    stats->kernel_launches = h->launches;
+    return RP_OK;
+}
+
+int rp_get_stream(void *handle, void **stream) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !stream) return RP_ERR_ARG;
+    *stream = static_cast<void *>(h->stream);
+    return RP_OK;
+}
+
+int rp_set_timing(void *handle, int on) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h) return RP_ERR_ARG;
+    RP_CUDA(h, cudaSetDevice(h->device));
+    RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    for (auto &m : h->marks) {
+        h->event_pool.push_back(m.a);
+        h->event_pool.push_back(m.b);
+    }
+    h->marks.clear();
+    for (int k = 0; k < RP_NUM_KERNELS; k++) {
+        h->kernel_ms[k] = 0;
+        h->kernel_groups[k] = 0;
+    }
+    h->timing = on != 0;
+    return RP_OK;
+}
+
+int rp_get_timing(void *handle, double *ms, uint64_t *groups) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h) return RP_ERR_ARG;
+    RP_CUDA(h, cudaSetDevice(h->device));
+    RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    for (auto &m : h->marks) {
+        float t = 0;
+        RP_CUDA(h, cudaEventElapsedTime(&t, m.a, m.b));
+        h->kernel_ms[m.kid] += t;
+        h->kernel_groups[m.kid] += 1;
+        h->event_pool.push_back(m.a);
+        h->event_pool.push_back(m.b);
+    }
+    h->marks.clear();
+    for (int k = 0; k < RP_NUM_KERNELS; k++) {
+        if (ms) ms[k] = h->kernel_ms[k];
+        if (groups) groups[k] = h->kernel_groups[k];
+    }
     return RP_OK;
 }
 

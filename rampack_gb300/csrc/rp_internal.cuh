@@ -17,6 +17,7 @@ enum : uint32_t {
     ST_BAD_CELL = 1u << 1,              // a listed move names a cell outside the grid
     ST_NUMERIC = 1u << 2,               // a non-finite coordinate was produced
     ST_CAPACITY = 1u << 3,              // a neighbourhood exceeded the largest staging capacity
+    ST_OUTSIDE = 1u << 4,               // a particle lies outside the box
 };
 
 // Constants of the FP32 filter: every comparison of the FP64 reference is decided in
@@ -67,6 +68,7 @@ struct DevState {
     FilterConsts fc;
     uint32_t *status;
     unsigned long long *counters;  // rp_sweep_stats layout
+    int strict_box;                // rebuild: flag positions outside [0, 1) relative (uploads)
 };
 
 constexpr int SWEEP_WARPS = 4;  // warps per block of the sweep kernel

@@ -118,6 +118,13 @@ __global__ void k_assign(DevState s, GridDev g) {
     d3 p = load_d3(s.pos64 + 3 * i);
     d3 r = mv3(s.inv, p);
     double rr[3] = {r.x, r.y, r.z};
+    // core/Packing.cpp:1069-1075 (areShapesWithinBox): relative coordinates in [0, 1)
+    if (s.strict_box) {
+        if (!(rr[0] >= 0.0 && rr[0] < 1.0 && rr[1] >= 0.0 && rr[1] < 1.0 && rr[2] >= 0.0 && rr[2] < 1.0))
+            atomicOr(s.status, ST_OUTSIDE);
+    } else if (!(fabs(rr[0] - 0.5) < 0.5 + 1e-9 && fabs(rr[1] - 0.5) < 0.5 + 1e-9 && fabs(rr[2] - 0.5) < 0.5 + 1e-9)) {
+        atomicOr(s.status, ST_NUMERIC);  // rescaled positions drift at most a few ulp outside
+    }
     int c[3];
     float f[3];
     for (int d = 0; d < 3; d++) {

@@ -148,6 +148,20 @@ class GpuPacking:
         self._check(self.lib.rp_get_stats(self.h, C.byref(st)))
         return st.as_dict()
 
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._check(self.lib.rp_get_stream(self.h, C.byref(s)))
+        return int(s.value or 0)
+
+    def set_timing(self, on: bool = True):
+        self._check(self.lib.rp_set_timing(self.h, 1 if on else 0))
+
+    def timing(self) -> dict:
+        ms = (C.c_double * 5)()
+        groups = (C.c_uint64 * 5)()
+        self._check(self.lib.rp_get_timing(self.h, ms, groups))
+        return {name: (float(ms[k]), int(groups[k])) for k, name in enumerate(_lib.KERNEL_GROUPS)}
+
     # ---- box moves ----
     def try_scaling(self, box) -> float:
         b = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
