@@ -214,6 +214,31 @@ int rp_set_timing(void *handle, int on);
  * (RP_NUM_KERNELS entries each) since timing was turned on; synchronizes the stream. */
 int rp_get_timing(void *handle, double *ms, uint64_t *groups);
 
+/* ---- allocation-free overlap count ----------------------------------------------- */
+
+/* Limits of rp_count_overlaps_static and the size of the scratch array behind it. */
+#define RP_STATIC_MAX_PARTICLES 65536
+#define RP_STATIC_MAX_CELLS 65536
+#define RP_STATIC_SCRATCH_BYTES (5 * 1024 * 1024)
+
+/* Counts overlapping pairs (as rp_count_overlaps) of a packing the caller already holds in
+ * its own device memory, without allocating any memory.  This entry point has no
+ * counterpart in the reference.  It is for callers that may not allocate: a host
+ * framework that budgets or pools all device memory itself, or a stream-ordered pipeline
+ * in which cudaMalloc/cudaFree would implicitly synchronise the device and stall its other
+ * streams.  Inputs: d_pos (n x 3 doubles) and d_rot (n x 9 doubles) in device memory of the
+ * current CUDA device, box9 and shape on the host; the work is ordered on `stream` (a
+ * cudaStream_t, NULL for the default stream) and the call returns after it completes,
+ * writing the count to *out_count (host).  Working memory is one fixed array of
+ * RP_STATIC_SCRATCH_BYTES compiled into the library, which every GPU that loads the library
+ * keeps until the process exits: n above RP_STATIC_MAX_PARTICLES, or a cell grid above
+ * RP_STATIC_MAX_CELLS cells, is rejected with RP_ERR_CAPACITY.  The first call on a device
+ * looks up the array's device address (with that device current), so make the first call
+ * before any stream capture.  All calls share the array: calls whose GPU work overlaps
+ * (from several host threads or streams) race and must be serialised by the caller. */
+int rp_count_overlaps_static(const rp_shape_desc *shape, int64_t n, const double *d_pos, const double *d_rot,
+                             const double *box9, int early_exit, void *stream, int64_t *out_count);
+
 #ifdef __cplusplus
 }
 #endif

@@ -76,6 +76,8 @@ SIGNATURES = {
     "rp_get_stream": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
     "rp_set_timing": (C.c_int, [_P, C.c_int]),
     "rp_get_timing": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]),
+    "rp_count_overlaps_static": (C.c_int, [C.POINTER(ShapeDesc), C.c_int64, _P, _P, _D, C.c_int, _P,
+                                           C.POINTER(C.c_int64)]),
 }
 KERNEL_GROUPS = ["sweep", "rebuild", "count", "rescale", "overflow"]
 
