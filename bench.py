@@ -222,6 +222,16 @@ def read_profile_traffic():
     return None
 
 
+def reduce_max(value: float, dist=None, device=None) -> float:
+    """Maximum of a per-rank value over all ranks (the job's time is its slowest rank's)."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device or "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def main_gpu(args):
     import torch
 
@@ -279,9 +289,7 @@ def main_gpu(args):
     g.set_timing(False)
     s1 = g.stats()
     if dist:
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = reduce_max(ms, dist, device=f"cuda:{local}")
         dist.barrier()
 
     moves = s1["moves"] - s0["moves"]
@@ -341,9 +349,7 @@ def main_gpu(args):
         e_ms = f0.elapsed_time(f1)
         e_moves = g.stats()["moves"] - m0
         if dist:
-            t = torch.tensor([e_ms], device=f"cuda:{local}")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e_ms = float(t.item())
+            e_ms = reduce_max(e_ms, dist, device=f"cuda:{local}")
         e2e = {"value": e_moves * world / (e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": int(n * 12 * 8),
                "d2h_bytes_per_step": int(n * 12 * 8),
                "step": "rp_upload_state (pinned host -> device) + one cycle + rp_download_state"}

@@ -56,6 +56,24 @@ void store_m(const Matrix<3, 3> &m, double *p) {
         for (int j = 0; j < 3; j++) p[3 * i + j] = m(i, j);
 }
 
+// A fixed-translation boundary condition, with the semantics of the reference's
+// Packing-internal HardcodedTranslation (core/Packing.cpp:22-43): the neighbour-grid path
+// of the pair tests.
+class FixedTranslationBC : public BoundaryConditions {
+    Vector<3> t;
+
+public:
+    explicit FixedTranslationBC(const Vector<3> &t_) : t{t_} {}
+    void setBox(const TriclinicBox &) override {}
+    [[nodiscard]] Vector<3> getCorrection(const Vector<3> &) const override {
+        throw std::runtime_error("FixedTranslationBC::getCorrection");
+    }
+    [[nodiscard]] Vector<3> getTranslation(const Vector<3> &, const Vector<3> &) const override { return t; }
+    [[nodiscard]] double getDistance2(const Vector<3> &p1, const Vector<3> &p2) const override {
+        return (p2 + this->t - p1).norm2();
+    }
+};
+
 struct Handle {
     std::shared_ptr<ShapeTraits> traits;
     std::unique_ptr<Packing> pk;
@@ -196,7 +214,7 @@ int ref_ng_divisions(void *hp, int64_t *div3) {
 
 int ref_pair_overlap(int kind, const double *prm, int np, const double *p1, const double *r1, int c1,
                      const double *p2, const double *r2, int c2, int bc_kind, const double *box9,
-                     const double *) {
+                     const double *t3) {
     auto traits = make_traits(kind, prm, np);
     if (!traits) return -1;
     const Interaction &in = traits->getInteraction();
@@ -204,6 +222,10 @@ int ref_pair_overlap(int kind, const double *prm, int np, const double *p1, cons
     if (bc_kind == 1) {
         PeriodicBoundaryConditions pbc(TriclinicBox(load_m(box9)));
         return in.overlapBetween(v1, load_m(r1), c1, v2, load_m(r2), c2, pbc) ? 1 : 0;
+    }
+    if (bc_kind == 2) {
+        FixedTranslationBC fixed(Vector<3>{t3[0], t3[1], t3[2]});
+        return in.overlapBetween(v1, load_m(r1), c1, v2, load_m(r2), c2, fixed) ? 1 : 0;
     }
     FreeBoundaryConditions fbc;
     return in.overlapBetween(v1, load_m(r1), c1, v2, load_m(r2), c2, fbc) ? 1 : 0;

@@ -237,7 +237,7 @@ int rpo_draw_moves(void *rp, double trans_step, double rot_step, const double *b
         std::size_t k = sampled / static_cast<std::size_t>(per_type);
         rpo_move &m = out[i];
         std::memset(&m, 0, sizeof(m));
-        M3 r = identity();
+        M3 r{};  // MoveData's default-constructed (zero) matrix for translations (core/MoveSampler.h:40-49)
         V3 t{};
         if (kinds[k] == 0) {
             double a = std::min(max_t, trans_step);

@@ -1,0 +1,247 @@
+"""Generates the golden fixtures in this directory from the REFERENCE'S OWN CODE.
+
+Run in a checkout where the reference sources are present:
+
+    make -C oracle ref            # compiles the reference's hot-path sources in place
+    python tests/golden/make_golden.py
+
+Every expected value below is produced by the reference library (oracle/_ref/librpref.so:
+rampack's Packing, NeighbourGrid, SpherocylinderTraits, samplers and Simulation compiled
+from its sources with -ffp-contract=off).  Inputs are seeded synthetic configurations.
+The fixtures pin the oracle restatement (tests/test_oracle_golden.py) and the GPU engine
+(tests/test_gpu_golden.py) to the reference bit for bit.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+import pyoracle as po  # noqa: E402
+from rampack_gb300 import workloads as W  # noqa: E402
+
+
+def rand_rot(rng, n):
+    """Random rotation matrices via the reference's Rodrigues formula (host libm)."""
+    out = np.zeros((n, 9))
+    for i in range(n):
+        ax = rng.normal(size=3)
+        ax /= np.linalg.norm(ax)
+        out[i] = po.rotation("reference", ax, rng.uniform(-np.pi, np.pi))
+    return out
+
+
+def gen_pairs(rng):
+    """Pair overlap decisions near contact for spheres and spherocylinders."""
+    recs = []
+    shapes = [(po.SPHERE, [0.5]), (po.SPHEROCYLINDER, [2.0, 0.5]), (po.SPHEROCYLINDER, [5.0, 0.5]),
+              (po.SPHEROCYLINDER, [0.0, 0.5]), (po.SPHEROCYLINDER, [3.0, 2.0])]
+    for kind, prm in shapes:
+        prm = np.array(prm)
+        rng_len = 2 * prm[-1] + (prm[0] if kind == po.SPHEROCYLINDER else 0)
+        for k in range(1500):
+            r1 = rand_rot(rng, 1)[0]
+            if k % 5 == 0:   # near-parallel partner
+                r2 = po.rotation("reference", [1, 0, 0], rng.normal() * 1e-3).reshape(3, 3) @ r1.reshape(3, 3)
+                r2 = r2.reshape(9)
+            else:
+                r2 = rand_rot(rng, 1)[0]
+            p1 = rng.uniform(0, 10, size=3)
+            d = rng.normal(size=3)
+            d /= np.linalg.norm(d)
+            p2 = p1 + d * rng.uniform(0.0, 1.1) * rng_len
+            t = rng.normal(size=3) * 3 if k % 3 == 0 else np.zeros(3)
+            ov = po.pair_overlap("reference", kind, prm, p1, r1, p2 - t, r2, translation=t)
+            recs.append((kind, prm[0], prm[-1], p1, r1, p2 - t, r2, t, ov))
+    kinds = np.array([r[0] for r in recs], dtype=np.int32)
+    prm = np.array([[r[1], r[2]] for r in recs])
+    p1 = np.array([r[3] for r in recs])
+    r1 = np.array([r[4] for r in recs])
+    p2 = np.array([r[5] for r in recs])
+    r2 = np.array([r[6] for r in recs])
+    t = np.array([r[7] for r in recs])
+    ov = np.array([r[8] for r in recs], dtype=np.int8)
+    np.savez_compressed(os.path.join(HERE, "pairs.npz"), kind=kinds, params=prm, p1=p1, r1=r1, p2=p2, r2=r2,
+                        translation=t, overlap=ov)
+    print("pairs:", len(ov), "overlapping", int(ov.sum()))
+
+
+def gen_geometry(rng):
+    boxes = []
+    for _ in range(40):
+        b = np.diag(rng.uniform(5, 50, size=3)) + rng.uniform(-3, 3, size=(3, 3)) * (rng.uniform() < 0.7)
+        boxes.append(b.reshape(9))
+    boxes = np.array(boxes)
+    inv, hts, vol = [], [], []
+    for b in boxes:
+        i, h, v = po.box_info("reference", b)
+        inv.append(i)
+        hts.append(h)
+        vol.append(v)
+    axes = rng.normal(size=(40, 3))
+    angles = rng.uniform(-3, 3, size=40)
+    rots = np.array([po.rotation("reference", a, ang) for a, ang in zip(axes, angles)])
+    np.savez_compressed(os.path.join(HERE, "geometry.npz"), boxes=boxes, inv=np.array(inv), heights=np.array(hts),
+                        volume=np.array(vol), axes=axes, angles=angles, rotations=rots)
+    print("geometry:", len(boxes), "boxes")
+
+
+def grid_cells(pos, box, range_, shift):
+    """Checkerboard cells of the GPU engine's grid rule (even counts, cells >= range),
+    restated in numpy to pick each cell's particles; particles within 1e-9 (relative) of a
+    cell face are left out of the per-cell lists so the membership never hinges on rounding."""
+    b = box.reshape(3, 3)
+    s = [b[:, 0], b[:, 1], b[:, 2]]
+    vol = abs(np.dot(np.cross(s[0], s[1]), s[2]))
+    h = [vol / np.linalg.norm(np.cross(s[1], s[2])), vol / np.linalg.norm(np.cross(s[2], s[0])),
+         vol / np.linalg.norm(np.cross(s[0], s[1]))]
+    dims = []
+    for d in range(3):
+        n = int(np.floor(h[d] / (range_ * (1 + 1e-9))))
+        dims.append(n & ~1 if n >= 2 else 1)
+    rel = pos @ np.linalg.inv(b).T
+    u = (rel - np.array(shift)) % 1.0
+    un = u * np.array(dims)
+    c = np.minimum(un.astype(int), np.array(dims) - 1)
+    frac = un - c
+    safe = np.all((frac > 1e-9) & (frac < 1 - 1e-9), axis=1)
+    cell = c[:, 0] + dims[0] * (c[:, 1] + dims[1] * c[:, 2])
+    bounds = np.zeros((dims[0] * dims[1] * dims[2], 6))
+    for idx in range(len(bounds)):
+        cc = (idx % dims[0], (idx // dims[0]) % dims[1], idx // (dims[0] * dims[1]))
+        for d in range(3):
+            if dims[d] == 1:
+                lo, hi = -np.inf, np.inf
+            else:
+                lo = shift[d] + cc[d] / dims[d]
+                lo = lo - 1 if lo >= 1 else lo
+                hi = shift[d] + (cc[d] + 1) / dims[d]
+                hi = hi - 1 if hi >= 1 else hi
+            bounds[idx, d], bounds[idx, 3 + d] = lo, hi
+    return dims, cell, safe, bounds
+
+
+def gen_system(name, cfg, trans, rot, rng, nshift=2, seed=77):
+    """Snapshot, overlap counts, a replayed move stream and box moves, all from the reference."""
+    import systems
+    kind, prm, pos, rotm, box = cfg
+    out = {"kind": kind, "params": prm, "pos": pos, "rot": rotm, "box": box}
+    ref = po.CpuPacking("reference", kind, prm, pos, rotm, box)
+    out["count"] = ref.count_overlaps(False)
+    out["count_early"] = ref.count_overlaps(True)
+    comp = systems.compressed(cfg, 0.96)
+    rc = po.CpuPacking("reference", *comp)
+    out["comp_pos"], out["comp_box"] = comp[2], comp[4]
+    out["comp_count"] = rc.count_overlaps(False)
+    out["comp_count_early"] = rc.count_overlaps(True)
+    rc.close()
+    # move stream: per phase, per active cell, moves drawn by the reference's samplers
+    rng_h = ref.rng(seed)
+    range_ = 2 * prm[-1] + (prm[0] if kind == po.SPHEROCYLINDER else 0)
+    all_moves, all_bounds, off = [], [], 0
+    for sh in range(nshift):
+        shift = rng.uniform(0, 1, size=3) if sh else np.zeros(3)
+        cur_pos, _, cur_box = ref.state()
+        dims, cell, safe, bounds = grid_cells(cur_pos, cur_box, range_, shift)
+        chunk = []
+        for ph in range(8):
+            par = [(ph >> d) & 1 for d in range(3)]
+            if any(dims[d] == 1 and par[d] for d in range(3)):
+                continue
+            for ci in range(len(bounds)):
+                cc = (ci % dims[0], (ci // dims[0]) % dims[1], ci // (dims[0] * dims[1]))
+                if any(dims[d] > 1 and (cc[d] & 1) != par[d] for d in range(3)):
+                    continue
+                idx = np.nonzero((cell == ci) & safe)[0]
+                if len(idx) == 0:
+                    continue
+                nt = (trans > 0) + (rot > 0)
+                mv = ref.draw_moves(rng_h, trans, rot, idx, len(idx), nt * len(idx), domain=off + ci)
+                chunk.append(mv)
+        mv = np.concatenate(chunk)
+        codes, _ = ref.replay(mv, np.concatenate(all_bounds + [bounds]) if all_bounds else bounds)
+        all_moves.append((mv, codes, shift))
+        all_bounds.append(bounds)
+        off += len(bounds)
+    ref.rng_free(rng_h)
+    out["moves"] = np.concatenate([m[0] for m in all_moves])
+    out["codes"] = np.concatenate([m[1] for m in all_moves])
+    out["shifts"] = np.array([m[2] for m in all_moves])
+    out["bounds"] = np.concatenate(all_bounds)
+    out["chunk_moves"] = np.array([len(m[0]) for m in all_moves])
+    out["chunk_cells"] = np.array([len(b) for b in all_bounds])
+    out["move_pos"], out["move_rot"], out["move_box"] = ref.state()
+    # box moves from the post-move state
+    boxes, dEs = [], []
+    for k in range(10):
+        _, _, b = ref.state()
+        bb = b.reshape(3, 3)
+        nb = (bb * (1 + rng.uniform(-0.03, 0.01)) if k % 2 else bb + rng.uniform(-0.04, 0.04, size=(3, 3)))
+        nb = nb.reshape(9)
+        dE = ref.try_scaling(nb)
+        if dE > 0:
+            ref.revert_scaling()
+        boxes.append(nb)
+        dEs.append(dE)
+    out["scale_boxes"] = np.array(boxes)
+    out["scale_dE"] = np.array(dEs)
+    out["final_pos"], out["final_rot"], out["final_box"] = ref.state()
+    ref.close()
+    np.savez_compressed(os.path.join(HERE, f"system_{name}.npz"), **out)
+    acc = int(np.count_nonzero(out["codes"] & 0x80))
+    print(f"system {name}: N={len(pos)} count={out['count']} comp={out['comp_count']} moves={len(out['moves'])} "
+          f"accepted={acc} box dE={list(out['scale_dE'])}")
+
+
+def gen_sim(name, cfg, cycles, **kw):
+    """A short NpT run of the reference's Simulation::integrate from a lattice."""
+    kind, prm, pos, rotm, box = cfg
+    ref = po.CpuPacking("reference", kind, prm, pos, rotm, box, threads=kw.get("threads", 1))
+    st = po.run_cycles(ref, cycles, **kw)
+    p, r, b = ref.state()
+    np.savez_compressed(os.path.join(HERE, f"sim_{name}.npz"), kind=kind, params=prm, pos=pos, rot=rotm, box=box,
+                        final_pos=p, final_rot=r, final_box=b, cycles=cycles,
+                        moves=np.array(list(st.moves)), accepted=np.array(list(st.accepted)),
+                        params_json=repr(kw))
+    print(f"sim {name}: moves {list(st.moves)} accepted {list(st.accepted)}")
+
+
+def gen_proposals():
+    """Proposal streams drawn by the reference's TranslationSampler / RotationSampler."""
+    kind, prm, pos, rotm, box = W.spherocylinders((6, 6, 6), 0.3, 2.0, 0.5, aspect=(1, 1, 3))
+    ref = po.CpuPacking("reference", kind, prm, pos, rotm, box)
+    r = ref.rng(4242)
+    idx = np.arange(0, len(pos), 3)
+    mv = ref.draw_moves(r, 0.2, 0.3, idx, 50, 500, domain=5)
+    ref.rng_free(r)
+    np.savez_compressed(os.path.join(HERE, "proposals.npz"), moves=mv, idx=idx, box=box, seed=4242,
+                        trans=0.2, rot=0.3, per_type=50)
+    print("proposals:", len(mv))
+
+
+def main():
+    if not po.reference_available():
+        po.build(reference=True)
+    rng = np.random.default_rng(20241203)
+    gen_pairs(rng)
+    gen_geometry(rng)
+    gen_proposals()
+    import systems
+    gen_system("hs", systems.hs_small(), 0.1, 0.0, rng)
+    gen_system("sc_l2", systems.sc_l2(), 0.2, 0.2, rng)
+    gen_system("sc_l5", systems.sc_l5(), 0.2, 0.2, rng, nshift=1)
+    gen_sim("hs1000", W.config_hs_1000(), 60, translation_step=0.1, box_kind=2, box_step=0.01 / 3, pressure=10.0,
+            adjust_steps=True)
+    gen_sim("sc_dd", W.spherocylinders((12, 12, 12), 0.35, 2.0, 0.5, aspect=(1, 1, 3)), 8, translation_step=0.2,
+            rotation_step=0.2, box_kind=1, box_step=0.005, pressure=1.5, domains=(2, 2, 2), threads=8)
+
+
+if __name__ == "__main__":
+    main()
