@@ -22,6 +22,8 @@ cudaError_t launch_count(const DevState &s, const GridDev &g, int early, unsigne
                          cudaStream_t st);
 cudaError_t launch_sweep(const SweepArgs &a, bool list, int nwarps, cudaStream_t st);
 size_t sweep_smem_per_warp(int kind, int cap);
+cudaError_t launch_rot_table(double *out64, float *out32, uint32_t count, uint64_t seed, uint64_t counter, float step,
+                             cudaStream_t st);
 
 namespace {
 
@@ -56,6 +58,8 @@ struct Handle {
     int64_t block_sums_alloc = 0;
     uint32_t *status = nullptr;
     unsigned long long *counters = nullptr;
+    double *rtab64 = nullptr;   // per-sweep rotation table
+    float *rtab32 = nullptr;
     unsigned long long *count_out = nullptr;
     int *flag = nullptr;
     int32_t *overflow = nullptr;
@@ -213,7 +217,7 @@ DevState dev_state(Handle *h) {
     const double u32 = std::ldexp(1.0, -24);
     // per-component bound of the FP32 separation error: rounded cell-local coordinates
     // and offsets, the staging and difference roundings and a translated mover.
-    const double e_sep = 24.0 * u32 * (lrow + 1.0);
+    const double e_sep = 32.0 * u32 * (lrow + 1.0);
     const double e_axis = 16.0 * u32;  // FP32 axes (a rotated mover included)
     const double safety = 4.0;
     FilterConsts fc{};
@@ -238,8 +242,18 @@ DevState dev_state(Handle *h) {
         double dend = std::sqrt(3.0) * (e_sep + l * e_axis);
         double dmax = 2 * r + l;
         double eval = 12.0 * u32 * (dmax + 3 * l) * (dmax + 3 * l);
-        fc.seg_err = static_cast<float>(safety * (2.0 * (2 * r) * 2.0 * dend + 4.0 * dend * dend + eval));
-        fc.d_min = static_cast<float>(2e-4 * l * l * l * l);
+        // FP64's own closest-point parameters err by about its input noise over D (the
+        // coordinates reach |x| ~ pmax, so every FP64 difference carries ~ulp(pmax)):
+        // nearly parallel pairs with D < d_min are re-decided in FP64, and the remaining
+        // FP64 suboptimality (<= g64) is added to the certificate's margin
+        double pmax = 0;
+        for (int i = 0; i < 3; i++)
+            pmax = std::max(pmax, std::fabs(h->box[3 * i]) + std::fabs(h->box[3 * i + 1]) + std::fabs(h->box[3 * i + 2]));
+        const double u64 = std::ldexp(1.0, -52);
+        const double noise = 8.0 * u64 * (pmax + l) * l * l * (dmax + 2 * l);
+        const double g64 = 2e-6;
+        fc.d_min = static_cast<float>(std::max(64.0 * noise * l * (2 * r) / g64, 1e-7 * l * l * l * l));
+        fc.seg_err = static_cast<float>(safety * (2.0 * (2 * r) * 2.0 * dend + 4.0 * dend * dend + eval) + g64);
         fc.len = static_cast<float>(l);
         fc.half_len = static_cast<float>(0.5 * l);
     }
@@ -282,6 +296,8 @@ int setup_grid(Handle *h, GridHost &G, const double *box, const double *shift) {
     for (int d = 0; d < 3; d++) {
         g.dims[d] = dims[d];
         g.shift[d] = shift[d];
+        g.fshift[d] = static_cast<float>(shift[d]);
+        g.finv_dims[d] = 1.0f / static_cast<float>(dims[d]);
     }
     g.ncell = static_cast<int>(ncell);
     double inv_cm[9];
@@ -453,6 +469,8 @@ int rp_create(const rp_shape_desc *shape, int64_t n, int device, void **handle) 
         if ((e = cudaMalloc(&h->trans[i], sizeof(double) * 3 * 125)) != cudaSuccess) return bail(e);
     }
     if ((e = cudaMalloc(&h->rot64, sizeof(double) * 9 * n)) != cudaSuccess) return bail(e);
+    if ((e = cudaMalloc(&h->rtab64, sizeof(double) * 9 * ROT_TABLE)) != cudaSuccess) return bail(e);
+    if ((e = cudaMalloc(&h->rtab32, sizeof(float) * 9 * ROT_TABLE)) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc(&h->status, sizeof(uint32_t))) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc(&h->counters, sizeof(unsigned long long) * 8)) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc(&h->count_out, sizeof(unsigned long long))) != cudaSuccess) return bail(e);
@@ -488,6 +506,8 @@ int rp_destroy(void *handle) {
         cudaFree(g.max_occ);
     }
     cudaFree(h->rot64);
+    cudaFree(h->rtab64);
+    cudaFree(h->rtab32);
     cudaFree(h->block_sums);
     cudaFree(h->status);
     cudaFree(h->counters);
@@ -785,6 +805,11 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
         }
     }
     if (stats) RP_CUDA(h, cudaMemsetAsync(h->counters, 0, sizeof(unsigned long long) * 8, h->stream));
+    if (types & 2) {
+        Group grp(h, RP_KERNEL_REBUILD, 1);
+        RP_CUDA(h, launch_rot_table(h->rtab64, h->rtab32, ROT_TABLE, p->seed, p->counter,
+                                    static_cast<float>(p->rotation_step), h->stream));
+    }
     for (int ph : phases) {
         SweepArgs a = base_args(h);
         int act[3];
@@ -799,6 +824,9 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
         a.tstep = static_cast<float>(tstep);
         a.rstep = static_cast<float>(p->rotation_step);
         a.types = types;
+        a.rtab64 = h->rtab64;
+        a.rtab32 = h->rtab32;
+        a.rtab_mask = ROT_TABLE - 1;
         a.fp64_only = (p->flags & RP_SWEEP_FP64_ONLY) ? 1 : 0;
         if (log) {
             a.log = h->d_log;

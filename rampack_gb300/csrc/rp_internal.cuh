@@ -40,6 +40,8 @@ struct GridDev {
     int dims[3];
     int ncell;
     double shift[3];
+    float fshift[3];      // shift and 1/dims in FP32 (the FP32 box-wrap test)
+    float finv_dims[3];
     float cellmat[9];     // row-major box / n (column d divided by dims[d]), FP32
     float cellinv[9];     // inverse of cellmat (maps local coords to in-cell fractions)
     int32_t *count;       // [ncell]
@@ -71,7 +73,10 @@ struct DevState {
     int strict_box;                // rebuild: flag positions outside [0, 1) relative (uploads)
 };
 
-constexpr int SWEEP_WARPS = 4;  // warps per block of the sweep kernel
+constexpr int SWEEP_WARPS = 4;       // warps per block of the sweep kernel
+constexpr int SWEEP_MIN_BLOCKS = 4;  // resident blocks per SM the register budget allows
+constexpr int MIRROR_ROUNDINGS = 4;  // FP32 mirror updates per particle and sweep before an exact refresh
+constexpr uint32_t ROT_TABLE = 65536;  // rotations drawn per sweep (plus their inverses)
 
 struct SweepArgs {
     DevState s;
@@ -91,6 +96,9 @@ struct SweepArgs {
     uint64_t seed, counter;
     float tstep, rstep;
     int types;                     // bit 0 translation, bit 1 rotation
+    const double *rtab64;          // rotation table of this sweep: [rtab_mask + 1][9] exact FP64
+    const float *rtab32;           // the same rotations rounded to FP32
+    uint32_t rtab_mask;
     rp_move *log;                  // [ntypes * n] indexed by ntypes * start[cell] + k
     uint8_t *log_codes;
     int fp64_only;

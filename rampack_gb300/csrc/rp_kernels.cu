@@ -32,9 +32,10 @@ __device__ __forceinline__ float dot3f(float3 a, float3 b) { return fmaf(a.x, b.
 // FP32 classification of one pair.  0: no overlap, 1: overlap, 2: undecided in FP32
 // (re-decided in FP64).  d = p_j - p_i (candidate minus mover), a_i/a_j unit axes.
 // ---------------------------------------------------------------------------------
+// Centre-distance stage: 0 no overlap, 1 overlap, 2 undecided (FP64), 3 needs the
+// segment stage (spherocylinders).
 template <int KIND>
-__device__ __forceinline__ int classify(const FilterConsts &fc, float3 d, float3 ai, float3 aj) {
-    float d2 = dot3f(d, d);
+__device__ __forceinline__ int d2_stage(const FilterConsts &fc, float d2) {
     if (KIND == 0) {
         if (d2 < fc.sphere_lo) return 1;
         if (d2 > fc.sphere_hi) return 0;
@@ -43,44 +44,60 @@ __device__ __forceinline__ int classify(const FilterConsts &fc, float3 d, float3
         if (d2 > fc.far_hi) return 0;
         if (d2 < fc.core_lo) return 1;
         if (d2 < fc.core_hi || d2 > fc.far_lo) return 2;
-        // Segment-segment distance of the two cylinder axes (same branch structure as
-        // the FP64 reference), then a convexity certificate: for any feasible (s, t),
-        // f* >= f(s, t) - G with G the Frank-Wolfe gap of the box-constrained problem.
-        const float l = fc.len, h = fc.half_len;
-        float3 u = make_float3(l * ai.x, l * ai.y, l * ai.z);
-        float3 v = make_float3(l * aj.x, l * aj.y, l * aj.z);
-        float3 w = make_float3(-d.x - h * (ai.x - aj.x), -d.y - h * (ai.y - aj.y), -d.z - h * (ai.z - aj.z));
-        float a = dot3f(u, u), b = dot3f(u, v), c = dot3f(v, v), dd = dot3f(u, w), e = dot3f(v, w);
-        float D = fmaf(a, c, -b * b);
-        if (D < fc.d_min) return 2;
-        float sN = fmaf(b, e, -c * dd), tN = fmaf(a, e, -b * dd), sD = D, tD = D;
-        if (sN < 0.f) {
-            sN = 0.f; tN = e; tD = c;
-        } else if (sN > sD) {
-            sN = sD; tN = e + b; tD = c;
-        }
-        if (tN < 0.f) {
-            tN = 0.f;
-            if (-dd < 0.f) sN = 0.f;
-            else if (-dd > a) sN = sD;
-            else { sN = -dd; sD = a; }
-        } else if (tN > tD) {
-            tN = tD;
-            if (b - dd < 0.f) sN = 0.f;
-            else if (b - dd > a) sN = sD;
-            else { sN = b - dd; sD = a; }
-        }
-        float sc = fminf(fmaxf(__fdividef(sN, sD), 0.f), 1.f);
-        float tc = fminf(fmaxf(__fdividef(tN, tD), 0.f), 1.f);
-        float3 dP = make_float3(fmaf(sc, u.x, fmaf(-tc, v.x, w.x)), fmaf(sc, u.y, fmaf(-tc, v.y, w.y)),
-                                fmaf(sc, u.z, fmaf(-tc, v.z, w.z)));
-        float f = dot3f(dP, dP);
-        float gs = dot3f(dP, u), gt = -dot3f(dP, v);
-        float G = 2.f * (gs * sc - fminf(gs, 0.f) + gt * tc - fminf(gt, 0.f));
-        if (f + fc.seg_err < fc.core_thr) return 1;
-        if (f - G - fc.seg_err >= fc.core_thr) return 0;
-        return 2;
+        return 3;
     }
+}
+
+// Segment stage of a spherocylinder pair: the closest points of the two axes (same
+// branch structure as the FP64 reference), then a convexity certificate: for any feasible
+// (s, t), f* >= f(s, t) - G with G the Frank-Wolfe gap of the box-constrained quadratic.
+// 0 no overlap, 1 overlap, 2 undecided (FP64).  d = p_j - p_i, ai/aj unit axes.
+__device__ __forceinline__ int seg_stage(const FilterConsts &fc, float3 d, float3 ai, float3 aj) {
+    const float l = fc.len, h = fc.half_len;
+    float3 u = make_float3(l * ai.x, l * ai.y, l * ai.z);
+    float3 v = make_float3(l * aj.x, l * aj.y, l * aj.z);
+    float3 w = make_float3(-d.x - h * (ai.x - aj.x), -d.y - h * (ai.y - aj.y), -d.z - h * (ai.z - aj.z));
+    float a = dot3f(u, u), b = dot3f(u, v), c = dot3f(v, v), dd = dot3f(u, w), e = dot3f(v, w);
+    // D = |u|^2 |v|^2 - (u.v)^2 = |u x v|^2, evaluated without cancellation: nearly parallel
+    // axes (D below d_min) are left to FP64, whose own parameter error grows like 1/D
+    float3 cr = make_float3(fmaf(u.y, v.z, -u.z * v.y), fmaf(u.z, v.x, -u.x * v.z), fmaf(u.x, v.y, -u.y * v.x));
+    float D = dot3f(cr, cr);
+    if (D < fc.d_min) return 2;
+    float sN = fmaf(b, e, -c * dd), tN = fmaf(a, e, -b * dd), sD = D, tD = D;
+    if (sN < 0.f) {
+        sN = 0.f; tN = e; tD = c;
+    } else if (sN > sD) {
+        sN = sD; tN = e + b; tD = c;
+    }
+    if (tN < 0.f) {
+        tN = 0.f;
+        if (-dd < 0.f) sN = 0.f;
+        else if (-dd > a) sN = sD;
+        else { sN = -dd; sD = a; }
+    } else if (tN > tD) {
+        tN = tD;
+        if (b - dd < 0.f) sN = 0.f;
+        else if (b - dd > a) sN = sD;
+        else { sN = b - dd; sD = a; }
+    }
+    float sc = fminf(fmaxf(__fdividef(sN, sD), 0.f), 1.f);
+    float tc = fminf(fmaxf(__fdividef(tN, tD), 0.f), 1.f);
+    float3 dP = make_float3(fmaf(sc, u.x, fmaf(-tc, v.x, w.x)), fmaf(sc, u.y, fmaf(-tc, v.y, w.y)),
+                            fmaf(sc, u.z, fmaf(-tc, v.z, w.z)));
+    float f = dot3f(dP, dP);
+    float gs = dot3f(dP, u), gt = -dot3f(dP, v);
+    float G = 2.f * (gs * sc - fminf(gs, 0.f) + gt * tc - fminf(gt, 0.f));
+    if (f + fc.seg_err < fc.core_thr) return 1;
+    if (f - G - fc.seg_err >= fc.core_thr) return 0;
+    return 2;
+}
+
+// FP32 classification of one pair: 0 no overlap, 1 overlap, 2 undecided in FP32.
+template <int KIND>
+__device__ __forceinline__ int classify(const FilterConsts &fc, float3 d, float3 ai, float3 aj) {
+    int cls = d2_stage<KIND>(fc, dot3f(d, d));
+    if (KIND == 1 && cls == 3) cls = seg_stage(fc, d, ai, aj);
+    return cls;
 }
 
 // Image of candidate j relative to mover i, recovered from the FP32 separation dsep
@@ -234,6 +251,36 @@ __global__ void k_cell_finish(DevState s, GridDev g) {
 }
 
 // ---------------------------------------------------------------------------------
+// Rotation table of one sweep: random rotations R = I + k (K + v v^T - |v|^2 I),
+// k = 2 / (1 + |v|^2), the Cayley map of v = tan(theta / 2) * axis with theta uniform in
+// [-step, step] and the axis uniform on the sphere.  Each table entry is exactly the
+// FP64 evaluation of that formula; moves draw an entry or its transpose (the inverse
+// rotation) with equal probability, so the proposal distribution is symmetric.
+// ---------------------------------------------------------------------------------
+__global__ void k_rot_table(double *out64, float *out32, uint32_t count, uint64_t seed, uint64_t counter,
+                            float step) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    u4 r = philox(u4{i, 0x726f74u, (uint32_t)counter, (uint32_t)(counter >> 32)}, (uint32_t)seed,
+                  (uint32_t)(seed >> 32));
+    float z = pm1f(r.a);
+    float sphi, cphi;
+    sincosf(6.2831853f * u01f(r.b), &sphi, &cphi);
+    float rs = sqrtf(fmaxf(0.f, 1.f - z * z));
+    float tq = tanf(0.5f * pm1f(r.c) * step);
+    double v[3] = {tq * rs * cphi, tq * rs * sphi, tq * z};
+    double vv = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    double kap = 2.0 / (1.0 + vv);
+    double K[9] = {0.0, -v[2], v[1], v[2], 0.0, -v[0], -v[1], v[0], 0.0};
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) {
+            double e = (a == b ? 1.0 : 0.0) + kap * (K[3 * a + b] + v[a] * v[b] - (a == b ? vv : 0.0));
+            out64[9 * (size_t)i + 3 * a + b] = e;
+            out32[9 * (size_t)i + 3 * a + b] = (float)e;
+        }
+}
+
+// ---------------------------------------------------------------------------------
 // Box rescale: positions keep their relative coordinates (core/Packing.cpp:183-184:
 // newBox.relativeToAbsolute(oldBox.absoluteToRelative(pos))).
 // ---------------------------------------------------------------------------------
@@ -318,6 +365,14 @@ template __global__ void k_count<1>(DevState, GridDev, int, unsigned long long *
 
 // ---------------------------------------------------------------------------------
 // Checkerboard sweep: one warp per active cell.
+//
+// Per move, all lanes draw (or read) the same proposal; the FP32 pass tests the staged
+// neighbourhood 32 candidates at a time with a ballot for the early exit.  Pass 1 decides
+// on the centre distance alone and compacts the spherocylinder pairs that need the
+// segment test into a shared-memory queue, so that pass 2 runs the segment test on full
+// warps.  Pairs the FP32 filter cannot decide go to a second queue; only a move that
+// survives the FP32 filter builds its exact FP64 state (one box row per lane, one matrix
+// entry per lane), re-decides the queued pairs in FP64 and, when accepted, writes back.
 // ---------------------------------------------------------------------------------
 struct WarpStats {
     unsigned moves, accepted, rej_overlap, rej_domain, pairs, fp64, trans, rots;
@@ -325,9 +380,10 @@ struct WarpStats {
 
 template <int KIND, bool LIST>
 __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, float4 *cpos, float4 *cax,
-                                           uint16_t *queue, WarpStats &ws) {
+                                           uint16_t *qseg, uint16_t *qun, uint8_t *nacc, WarpStats &ws) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
     const DevState &S = A.s;
     const GridDev &G = A.g;
 
@@ -393,22 +449,26 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
             if (KIND == 1) cax[base + k] = G.maxis[st + k];
         }
     }
-    // does the own cell appear more than once (a grid dimension of one cell)?
     const bool self_images = (G.dims[0] == 1) || (G.dims[1] == 1) || (G.dims[2] == 1);
+    // per own-cell particle: FP32 roundings accumulated in its mirror position this sweep
+    for (int k = lane; k < occ; k += 32) nacc[k] = 0;
     __syncwarp();
 
-    // cell bounds (ActiveDomain) of this cell
-    double lo[3], hi[3];
-    for (int d = 0; d < 3; d++) {
-        lo[d] = G.bounds[G.boundsoff[d] + 2 * c[d]];
-        hi[d] = G.bounds[G.boundsoff[d] + 2 * c[d] + 1];
-    }
+    // this lane's dimension (lanes 0-2): ActiveDomain bounds and cell coordinate
+    const int ld = lane < 3 ? lane : 0;
+    const int c_ld = ld == 0 ? c[0] : (ld == 1 ? c[1] : c[2]);
+    const int dims_ld = ld == 0 ? G.dims[0] : (ld == 1 ? G.dims[1] : G.dims[2]);
+    const int boff_ld = ld == 0 ? G.boundsoff[0] : (ld == 1 ? G.boundsoff[1] : G.boundsoff[2]);
+    const double shift_ld = ld == 0 ? G.shift[0] : (ld == 1 ? G.shift[1] : G.shift[2]);
+    const double lo_d = G.bounds[boff_ld + 2 * c_ld];
+    const double hi_d = G.bounds[boff_ld + 2 * c_ld + 1];
+    // this lane's matrix entry (lanes 0-8)
+    const int ei = lane < 9 ? lane / 3 : 0, ej = lane < 9 ? lane % 3 : 0;
 
     int nmoves, mbeg = 0;
     if (LIST) {
         int li = A.work ? -1 : item;
         if (A.work) {
-            // overflow rerun in list mode: find this cell's range
             for (int q = 0; q < A.num_list; q++)
                 if (A.list_cells[q] == cell) li = q;
         }
@@ -419,19 +479,28 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
     }
     const int ntypes = (A.types & 1) + ((A.types >> 1) & 1);
 
+    u4 rnd_lane = u4{0u, 0u, 0u, 0u};  // Philox output of move (batch base + lane)
     for (int mi = 0; mi < nmoves; mi++) {
-        // ---- the proposal ----
-        int type, slot = -1;
-        double t64[3] = {0.0, 0.0, 0.0}, R64[9];
-        float R32[9];
-        float3 t32 = make_float3(0.f, 0.f, 0.f);
+        if (!LIST && (mi & 31) == 0) {
+            // draw the next 32 moves' random words at once, one move per lane
+            rnd_lane = philox(u4{(uint32_t)(mi + lane), (uint32_t)cell, (uint32_t)A.counter,
+                                 (uint32_t)(A.counter >> 32)},
+                              (uint32_t)A.seed, (uint32_t)(A.seed >> 32));
+        }
+        // ---- the proposal (FP32 view; FP64 inputs kept for the exact path) ----
+        int type, slot = -1, out_index = -1;
         double uni = 0.5;
-        int out_index = -1;
+        double t64_lane = 0.0;      // translation component of this lane's dimension
+        float3 t32 = make_float3(0.f, 0.f, 0.f);
+        float R32[9];
+        uint32_t rot_idx = 0;       // drawn rotation: table entry and transpose flag
+        bool rot_inv = false;
+        const rp_move *mrec = nullptr;
         if (LIST) {
             out_index = A.move_out[mbeg + mi];
-            const rp_move &m = A.moves[out_index];
-            type = m.type;
-            int want = m.particle;
+            mrec = A.moves + out_index;
+            type = mrec->type;
+            int want = mrec->particle;
             for (int kb = 0; kb < occ; kb += 32) {
                 int k = kb + lane;
                 bool hit = k < occ && __float_as_int(cpos[k].w) == want;
@@ -448,60 +517,36 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
                 }
                 continue;
             }
-            for (int q = 0; q < 3; q++) t64[q] = m.translation[q];
-            for (int q = 0; q < 9; q++) R64[q] = m.rotation[q];
-            uni = m.uniform;
-            t32 = make_float3((float)t64[0], (float)t64[1], (float)t64[2]);
-            for (int q = 0; q < 9; q++) R32[q] = (float)R64[q];
+            t32 = make_float3((float)mrec->translation[0], (float)mrec->translation[1], (float)mrec->translation[2]);
+            t64_lane = mrec->translation[ld];
+            uni = mrec->uniform;
+            for (int q = 0; q < 9; q++) R32[q] = (float)mrec->rotation[q];
         } else {
-            u4 r0 = philox(u4{(uint32_t)(2 * mi), (uint32_t)cell, (uint32_t)A.counter, (uint32_t)(A.counter >> 32)},
-                           (uint32_t)A.seed, (uint32_t)(A.seed >> 32));
-            u4 r1 = philox(u4{(uint32_t)(2 * mi + 1), (uint32_t)cell, (uint32_t)A.counter,
-                              (uint32_t)(A.counter >> 32)},
-                           (uint32_t)A.seed, (uint32_t)(A.seed >> 32));
-            if (ntypes == 2) type = (r0.a >> 31) ? 1 : 0;
+            const int src = mi & 31;
+            u4 r = u4{__shfl_sync(FULL, rnd_lane.a, src), __shfl_sync(FULL, rnd_lane.b, src),
+                      __shfl_sync(FULL, rnd_lane.c, src), __shfl_sync(FULL, rnd_lane.d, src)};
+            if (ntypes == 2) type = (r.a >> 31) ? 1 : 0;
             else type = (A.types & 1) ? 0 : 1;
-            slot = (int)__umulhi(r0.b, (uint32_t)occ);
+            slot = (int)(((uint64_t)(r.a & 0x7fffffffu) * (uint32_t)occ) >> 31);
             if (type == 0) {
-                t32 = make_float3(pm1f(r0.c) * A.tstep, pm1f(r0.d) * A.tstep, pm1f(r1.a) * A.tstep);
-                t64[0] = t32.x;
-                t64[1] = t32.y;
-                t64[2] = t32.z;
+                t32 = make_float3(pm1f(r.b) * A.tstep, pm1f(r.c) * A.tstep, pm1f(r.d) * A.tstep);
+                t64_lane = ld == 0 ? (double)t32.x : (ld == 1 ? (double)t32.y : (double)t32.z);
             } else {
-                // Cayley map of v = tan(theta/2) * axis: an exactly orthogonal rotation in
-                // FP64, angle theta uniform in [-step, step], axis uniform on the sphere.
-                float z = pm1f(r1.b);
-                float phi = 6.2831853f * u01f(r1.c);
-                float sphi, cphi;
-                sincosf(phi, &sphi, &cphi);
-                float rs = sqrtf(fmaxf(0.f, 1.f - z * z));
-                float th = pm1f(r1.d) * A.rstep;
-                float tq = tanf(0.5f * th);
-                float v[3] = {tq * rs * cphi, tq * rs * sphi, tq * z};
-                float v2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
-                float k32 = 2.f / (1.f + v2);
-                double vd[3] = {v[0], v[1], v[2]};
-                double v2d = vd[0] * vd[0] + vd[1] * vd[1] + vd[2] * vd[2];
-                double kd = 2.0 / (1.0 + v2d);
-                float K[9] = {0.f, -v[2], v[1], v[2], 0.f, -v[0], -v[1], v[0], 0.f};
-                double Kd[9] = {0.0, -vd[2], vd[1], vd[2], 0.0, -vd[0], -vd[1], vd[0], 0.0};
-                for (int i = 0; i < 3; i++)
-                    for (int j = 0; j < 3; j++) {
-                        float e32 = K[3 * i + j] + v[i] * v[j] - (i == j ? v2 : 0.f);
-                        R32[3 * i + j] = (i == j ? 1.f : 0.f) + k32 * e32;
-                        double e64 = Kd[3 * i + j] + vd[i] * vd[j] - (i == j ? v2d : 0.0);
-                        R64[3 * i + j] = (i == j ? 1.0 : 0.0) + kd * e64;
-                    }
-            }
-        }
-        if (type == 0) {
-            for (int q = 0; q < 9; q++) {
-                R32[q] = (q % 4 == 0) ? 1.f : 0.f;
-                R64[q] = (q % 4 == 0) ? 1.0 : 0.0;
+                // a rotation of this sweep's table, or its transpose (the inverse)
+                rot_idx = r.b & A.rtab_mask;
+                rot_inv = (r.c & 1u) != 0;
+                if (KIND == 1) {
+                    const float *R = A.rtab32 + 9 * (size_t)rot_idx;
+                    for (int q = 0; q < 9; q++) R32[q] = rot_inv ? R[3 * (q % 3) + q / 3] : R[q];
+                }
             }
         }
         const float4 pcur = cpos[slot];
         const int pid = __float_as_int(pcur.w);
+        // the mover's FP64 state, loaded now and first used after the FP32 filter:
+        // lanes 0-2 hold the position, lanes 0-8 the orientation entries
+        const double pos_own = S.pos64[3 * (size_t)pid + ld];
+        const double rot_own = S.rot64[9 * (size_t)pid + (lane < 9 ? lane : 0)];
         float3 ai = make_float3(0.f, 0.f, 1.f);
         if (KIND == 1) {
             float4 a = cax[slot];
@@ -509,197 +554,273 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
         }
         float3 pn = make_float3(pcur.x, pcur.y, pcur.z);
         float3 an = ai;
-        if (type == 0 || type == 2) pn = make_float3(pcur.x + t32.x, pcur.y + t32.y, pcur.z + t32.z);
-        if ((type == 1 || type == 2) && KIND == 1) an = mat32(R32, ai.x, ai.y, ai.z);
+        if (type != 1) pn = make_float3(pcur.x + t32.x, pcur.y + t32.y, pcur.z + t32.z);
+        if (type != 0 && KIND == 1) an = mat32(R32, ai.x, ai.y, ai.z);
 
-        // ---- FP32 ActiveDomain test (translations) ----
-        int dom = 0;  // 0 inside, 1 outside, 2 undecided
-        if (type == 0 || type == 2) {
+        // ---- FP32 ActiveDomain test (translations): 0 inside, 1 outside, 2 undecided;
+        //      and whether the PBC correction may move the particle through the box ----
+        int dom = 0;
+        bool maywrap = false;
+        if (type != 1) {
             float3 f = mat32(G.cellinv, pn.x, pn.y, pn.z);
-            float fm[3] = {f.x, f.y, f.z};
+            float3 f0 = mat32(G.cellinv, pcur.x, pcur.y, pcur.z);
+            float fm[3] = {f.x, f.y, f.z}, fo[3] = {f0.x, f0.y, f0.z};
             const float mg = S.fc.cell_margin;
             for (int d = 0; d < 3; d++) {
-                if (G.dims[d] == 1) continue;
-                if (fm[d] < -mg || fm[d] > 1.f + mg) dom = 1;
-                else if (dom == 0 && (fm[d] < mg || fm[d] > 1.f - mg)) dom = 2;
+                if (G.dims[d] > 1) {
+                    if (fm[d] < -mg || fm[d] > 1.f + mg) dom = 1;
+                    else if (dom == 0 && (fm[d] < mg || fm[d] > 1.f - mg)) dom = 2;
+                }
+                // relative coordinate of the stored (wrapped) position before the move, and of
+                // the translated position in the same image: s + (c + f) / n minus the wrap k
+                float rold = G.fshift[d] + ((float)c[d] + fo[d]) * G.finv_dims[d];
+                float rnew = G.fshift[d] + ((float)c[d] + fm[d]) * G.finv_dims[d];
+                float k = rold >= 1.f ? 1.f : 0.f;
+                if (fabsf(rold - 1.f) < mg) maywrap = true;
+                rnew -= k;
+                if (rnew < mg || rnew > 1.f - mg) maywrap = true;
             }
         }
 
-        // ---- FP32 overlap filter over the staged neighbourhood ----
+        // ---- FP32 pass 1: centre distances, two candidates per lane per round ----
         bool overlap = false;
-        int nq = 0;
-        unsigned pairs = 0;
+        int nseg = 0, nun = 0;
         if (dom != 1) {
-            for (int base = 0; base < total; base += 32) {
-                int k = base + lane;
-                int cls = 0;
-                if (k < total) {
-                    float4 q = cpos[k];
+            for (int base = 0; base < total; base += 64) {
+                int k0 = base + lane, k1 = base + 32 + lane;
+                int c0 = 0, c1 = 0;
+                if (k0 < total) {
+                    float4 q = cpos[k0];
                     if (__float_as_int(q.w) != pid) {
-                        float3 dsep = make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z);
-                        float3 aj = make_float3(0.f, 0.f, 1.f);
-                        if (KIND == 1) {
-                            float4 a = cax[k];
-                            aj = make_float3(a.x, a.y, a.z);
-                        }
-                        cls = A.fp64_only ? 2 : classify<KIND>(S.fc, dsep, an, aj);
-                        pairs++;
+                        float dx = q.x - pn.x, dy = q.y - pn.y, dz = q.z - pn.z;
+                        c0 = A.fp64_only ? 2 : d2_stage<KIND>(S.fc, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+                        ws.pairs++;
                     }
+                }
+                if (k1 < total) {
+                    float4 q = cpos[k1];
+                    if (__float_as_int(q.w) != pid) {
+                        float dx = q.x - pn.x, dy = q.y - pn.y, dz = q.z - pn.z;
+                        c1 = A.fp64_only ? 2 : d2_stage<KIND>(S.fc, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+                        ws.pairs++;
+                    }
+                }
+                if (__ballot_sync(FULL, c0 == 1 || c1 == 1)) {
+                    overlap = true;
+                    break;
+                }
+                if (KIND == 1) {
+                    unsigned b0 = __ballot_sync(FULL, c0 == 3), b1 = __ballot_sync(FULL, c1 == 3);
+                    if (c0 == 3) qseg[nseg + __popc(b0 & lt)] = (uint16_t)k0;
+                    nseg += __popc(b0);
+                    if (c1 == 3) qseg[nseg + __popc(b1 & lt)] = (uint16_t)k1;
+                    nseg += __popc(b1);
+                }
+                unsigned u0 = __ballot_sync(FULL, c0 == 2), u1 = __ballot_sync(FULL, c1 == 2);
+                if (c0 == 2) qun[nun + __popc(u0 & lt)] = (uint16_t)k0;
+                nun += __popc(u0);
+                if (c1 == 2) qun[nun + __popc(u1 & lt)] = (uint16_t)k1;
+                nun += __popc(u1);
+            }
+        }
+        __syncwarp();
+        // ---- FP32 pass 2 (spherocylinders): segment distances on full warps ----
+        if (KIND == 1 && !overlap) {
+            for (int base = 0; base < nseg; base += 32) {
+                int i = base + lane;
+                int cls = 0, k = 0;
+                if (i < nseg) {
+                    k = qseg[i];
+                    float4 q = cpos[k];
+                    float4 a = cax[k];
+                    cls = seg_stage(S.fc, make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z), an,
+                                    make_float3(a.x, a.y, a.z));
                 }
                 if (__ballot_sync(FULL, cls == 1)) {
                     overlap = true;
                     break;
                 }
-                unsigned un = __ballot_sync(FULL, cls == 2);
-                if (un) {
-                    if (cls == 2) queue[nq + __popc(un & ((1u << lane) - 1u))] = (uint16_t)k;
-                    nq += __popc(un);
-                }
+                unsigned b2 = __ballot_sync(FULL, cls == 2);
+                if (cls == 2) qun[nun + __popc(b2 & lt)] = (uint16_t)k;
+                nun += __popc(b2);
+            }
+            __syncwarp();
+        }
+
+        uint8_t code = dom == 1 ? 2 : (overlap ? 1 : 0);
+        // ---- FP64: the exact proposal of a surviving move (or of an accepted u == 0 move) ----
+        const bool need64 = (code == 0) || (uni <= 0.0);
+        const bool needR = type != 0 && (need64 || A.log != nullptr);
+        double rel_own = 0.0, pnew_own = 0.0, onew_own = 0.0, rrow[3] = {0.0, 0.0, 0.0};
+        bool exact_rel = false;     // rel_own holds the exact FP64 relative coordinate
+        d3 pnew{0, 0, 0}, anew{0, 0, 0};
+        if (needR) {
+            // row ei of the move's rotation (lanes 0-8 hold rows 0..2 three times over)
+            if (LIST) {
+                rrow[0] = mrec->rotation[3 * ei];
+                rrow[1] = mrec->rotation[3 * ei + 1];
+                rrow[2] = mrec->rotation[3 * ei + 2];
+            } else {
+                const double *R = A.rtab64 + 9 * (size_t)rot_idx;
+                rrow[0] = rot_inv ? R[ei] : R[3 * ei];
+                rrow[1] = rot_inv ? R[3 + ei] : R[3 * ei + 1];
+                rrow[2] = rot_inv ? R[6 + ei] : R[3 * ei + 2];
             }
         }
-        __syncwarp();
-
-        // ---- FP64: exact proposal for moves that survived, and the guard band ----
-        d3 p64 = load_d3(S.pos64 + 3 * (size_t)pid);
-        d3 pnew = p64;
-        double rel[3] = {0.0, 0.0, 0.0};
-        bool exact_done = false;
-        uint8_t code;
-        if (dom == 1) {
-            code = 2;
-        } else if (overlap) {
-            code = 1;
-        } else {
-            exact_done = true;
-            if (type == 0 || type == 2) {
-                // Shape::translate (core/Shape.cpp:9-12) with PBC correction
-                d3 p1 = add3(p64, d3{t64[0], t64[1], t64[2]});
-                bool wrapped = false;
-                d3 corr = pbc_correction(S.box, S.inv, p1, &wrapped);
-                pnew = add3(p1, corr);
-                d3 r = mv3(S.inv, pnew);
-                rel[0] = r.x;
-                rel[1] = r.y;
-                rel[2] = r.z;
-                if (!inside_domain(S.inv, pnew, lo, hi)) code = 2;
-                else code = 0;
-            } else {
-                code = 0;
-            }
-            if (code == 0 && nq > 0) {
-                // orientation after the move: R · O (core/Shape.cpp:14-16), column 2
-                const double *ro = S.rot64 + 9 * (size_t)pid;
-                d3 anew;
-                if (type == 1 || type == 2) {
-                    double o[9];
-                    for (int q = 0; q < 9; q++) o[q] = ro[q];
-                    anew = d3{mm_elem(R64, o, 0, 2), mm_elem(R64, o, 1, 2), mm_elem(R64, o, 2, 2)};
+        if (need64) {
+            if (type != 1) {
+                // Shape::translate with the PBC correction (core/Shape.cpp:9-12,
+                // core/PeriodicBoundaryConditions.cpp:11-22), one box row per lane
+                if (!LIST) t64_lane = (double)(ld == 0 ? t32.x : (ld == 1 ? t32.y : t32.z));
+                double p1 = dadd(pos_own, t64_lane);
+                if (!maywrap) {
+                    // FP32 shows every relative coordinate clear of 0 and 1: no correction,
+                    // which is box · 0 = +0 exactly
+                    pnew_own = dadd(p1, 0.0);
+                    if (dom == 2) {
+                        d3 P1{__shfl_sync(FULL, p1, 0), __shfl_sync(FULL, p1, 1), __shfl_sync(FULL, p1, 2)};
+                        rel_own = mrow(S.inv, ld, P1);
+                        exact_rel = true;
+                    }
                 } else {
-                    anew = d3{ro[2], ro[5], ro[8]};
+                    d3 P1{__shfl_sync(FULL, p1, 0), __shfl_sync(FULL, p1, 1), __shfl_sync(FULL, p1, 2)};
+                    double rel = mrow(S.inv, ld, P1);
+                    double cr = 0.0;
+                    while (dadd(rel, cr) < 0.0) cr = dadd(cr, 1.0);
+                    while (dadd(rel, cr) >= 1.0) cr = dsub(cr, 1.0);
+                    if (__ballot_sync(FULL, lane < 3 && cr != 0.0) == 0u) {
+                        pnew_own = dadd(p1, 0.0);
+                        rel_own = rel;
+                    } else {
+                        d3 C{__shfl_sync(FULL, cr, 0), __shfl_sync(FULL, cr, 1), __shfl_sync(FULL, cr, 2)};
+                        pnew_own = dadd(p1, mrow(S.box, ld, C));
+                        d3 PN{__shfl_sync(FULL, pnew_own, 0), __shfl_sync(FULL, pnew_own, 1),
+                              __shfl_sync(FULL, pnew_own, 2)};
+                        rel_own = mrow(S.inv, ld, PN);
+                    }
+                    exact_rel = true;
                 }
+                pnew = d3{__shfl_sync(FULL, pnew_own, 0), __shfl_sync(FULL, pnew_own, 1), __shfl_sync(FULL, pnew_own, 2)};
+                if (dom == 2) {
+                    // ActiveDomain::isInside (core/ActiveDomain.cpp:8-21) on the exact position
+                    bool out = false;
+                    if (lane < 3 && dims_ld > 1) {
+                        if (hi_d > lo_d) out = rel_own <= lo_d || rel_own >= hi_d;
+                        else out = rel_own <= lo_d && rel_own >= hi_d;
+                    }
+                    if (__ballot_sync(FULL, out)) code = 2;
+                }
+            } else {
+                pnew = d3{__shfl_sync(FULL, pos_own, 0), __shfl_sync(FULL, pos_own, 1), __shfl_sync(FULL, pos_own, 2)};
+            }
+            if (type != 0) {
+                // Shape::rotate: R · O (core/Shape.cpp:14-16, Matrix.tpp:104-113), entry (ei, ej) per lane
+                double oe = rot_own;
+                double o0 = __shfl_sync(FULL, oe, ej), o1 = __shfl_sync(FULL, oe, 3 + ej),
+                       o2 = __shfl_sync(FULL, oe, 6 + ej);
+                double s = 0.0;
+                s = dadd(s, dmul(rrow[0], o0));
+                s = dadd(s, dmul(rrow[1], o1));
+                s = dadd(s, dmul(rrow[2], o2));
+                onew_own = s;
+                anew = d3{__shfl_sync(FULL, s, 2), __shfl_sync(FULL, s, 5), __shfl_sync(FULL, s, 8)};
+            } else {
+                anew = d3{__shfl_sync(FULL, rot_own, 2), __shfl_sync(FULL, rot_own, 5), __shfl_sync(FULL, rot_own, 8)};
+            }
+            // the guard band: queued pairs re-decided in FP64
+            if (code == 0 && nun > 0) {
                 bool ov = false;
-                for (int qb = 0; qb < nq; qb += 32) {
+                for (int qb = 0; qb < nun; qb += 32) {
                     int qi = qb + lane;
                     bool hit = false;
-                    if (qi < nq) {
-                        int k = queue[qi];
+                    if (qi < nun) {
+                        int k = qun[qi];
                         float4 q = cpos[k];
-                        float3 dsep = make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z);
-                        hit = exact_pair(S, pnew, anew, __float_as_int(q.w), dsep);
+                        hit = exact_pair(S, pnew, anew, __float_as_int(q.w),
+                                         make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z));
                     }
                     if (__ballot_sync(FULL, hit)) {
                         ov = true;
                         break;
                     }
                 }
-                ws.fp64 += nq;
+                ws.fp64 += nun;
                 if (ov) code = 1;
             }
         }
-        ws.pairs += pairs;
 
         // ---- Metropolis (core/Simulation.cpp:483): u <= exp(-dE/T), dE in {0, +inf} ----
-        bool acc = (code == 0) ? (uni <= 1.0) : (uni <= 0.0);
+        const bool acc = (code == 0) ? (uni <= 1.0) : (uni <= 0.0);
         if (acc) {
-            if (!exact_done && (type == 0 || type == 2)) {
-                // an accepted move with dE = +inf (u == 0 exactly): the reference still
-                // commits the temp shape, so compute its translated position.
-                d3 p1 = add3(p64, d3{t64[0], t64[1], t64[2]});
-                d3 corr = pbc_correction(S.box, S.inv, p1, nullptr);
-                pnew = add3(p1, corr);
-                d3 r = mv3(S.inv, pnew);
-                rel[0] = r.x;
-                rel[1] = r.y;
-                rel[2] = r.z;
-            }
             const size_t gslot = (size_t)gbase + slot;
             float4 np = pcur;
-            if (type == 0 || type == 2) {
-                if (lane < 3) S.pos64[3 * (size_t)pid + lane] = lane == 0 ? pnew.x : (lane == 1 ? pnew.y : pnew.z);
+            float4 na = KIND == 1 ? cax[slot] : make_float4(0.f, 0.f, 0.f, 0.f);
+            __syncwarp();
+            if (type != 1) {
+                if (lane < 3) S.pos64[3 * (size_t)pid + lane] = pnew_own;
+            }
+            const int na_cnt = nacc[slot];
+            if (type != 1 && !exact_rel && na_cnt < MIRROR_ROUNDINGS) {
+                // the FP32 proposal becomes the mirror position: one more FP32 rounding
+                // (t32 is the exact FP32 value of the FP64 translation), bounded per sweep
+                np = make_float4(pn.x, pn.y, pn.z, pcur.w);
+                if (lane == 0) nacc[slot] = (uint8_t)(na_cnt + 1);
+            } else if (type != 1) {
+                if (!exact_rel) rel_own = mrow(S.inv, ld, pnew);
+                if (lane == 0) nacc[slot] = 0;
                 // new cell-local FP32 position from the FP64 relative coordinates
-                float fr[3];
-                for (int d = 0; d < 3; d++) {
-                    double u = rel[d] - G.shift[d];
-                    if (u < 0.0) u += 1.0;
-                    double fd = u * G.dims[d] - c[d];
-                    if (fd < -0.5) fd += G.dims[d];
-                    if (fd > G.dims[d] - 0.5) fd -= G.dims[d];
-                    fr[d] = (float)fd;
-                }
-                float3 loc = mat32(G.cellmat, fr[0], fr[1], fr[2]);
+                double u = rel_own - shift_ld;
+                if (u < 0.0) u += 1.0;
+                double fd = u * dims_ld - c_ld;
+                if (fd < -0.5) fd += dims_ld;
+                if (fd > dims_ld - 0.5) fd -= dims_ld;
+                float f = (float)fd;
+                float f0 = __shfl_sync(FULL, f, 0), f1 = __shfl_sync(FULL, f, 1), f2 = __shfl_sync(FULL, f, 2);
+                float3 loc = mat32(G.cellmat, f0, f1, f2);
                 np = make_float4(loc.x, loc.y, loc.z, pcur.w);
             }
-            float4 na = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (type == 1 || type == 2) {
-                double *ro = S.rot64 + 9 * (size_t)pid;
-                double o[9];
-                for (int q = 0; q < 9; q++) o[q] = ro[q];
-                __syncwarp();
-                double e = 0.0;
-                if (lane < 9) e = mm_elem(R64, o, lane / 3, lane % 3);
-                if (lane < 9) ro[lane] = e;
-                double a0 = __shfl_sync(FULL, e, 2), a1 = __shfl_sync(FULL, e, 5), a2 = __shfl_sync(FULL, e, 8);
-                na = make_float4((float)a0, (float)a1, (float)a2, 0.f);
+            if (type != 0) {
+                if (lane < 9) S.rot64[9 * (size_t)pid + lane] = onew_own;
+                const float of = (float)onew_own;
+                na = make_float4(__shfl_sync(FULL, of, 2), __shfl_sync(FULL, of, 5), __shfl_sync(FULL, of, 8), 0.f);
             }
-            __syncwarp();
             if (lane == 0) {
                 cpos[slot] = np;
                 G.mpos[gslot] = np;
-                if (KIND == 1 && (type == 1 || type == 2)) {
+                if (KIND == 1 && type != 0) {
                     cax[slot] = na;
                     G.maxis[gslot] = na;
                 }
             }
             if (self_images) {
-                // the own cell is staged several times (periodic images): refresh all copies
+                // the own cell is staged several times (periodic images): refresh every copy
                 __syncwarp();
                 for (int k = lane + occ; k < total; k += 32) {
                     float4 q = cpos[k];
                     if (__float_as_int(q.w) == pid) {
-                        float3 shift = make_float3(q.x - pcur.x, q.y - pcur.y, q.z - pcur.z);
-                        cpos[k] = make_float4(np.x + shift.x, np.y + shift.y, np.z + shift.z, q.w);
-                        if (KIND == 1 && (type == 1 || type == 2)) cax[k] = na;
+                        cpos[k] = make_float4(np.x + (q.x - pcur.x), np.y + (q.y - pcur.y), np.z + (q.z - pcur.z), q.w);
+                        if (KIND == 1 && type != 0) cax[k] = na;
                     }
                 }
             }
             __syncwarp();
         }
 
-        uint8_t full_code = code | (acc ? RP_CODE_ACCEPTED : 0);
-        if (lane == 0) {
-            if (LIST && A.codes) A.codes[out_index] = full_code;
-            if (!LIST && A.log) {
-                size_t li = (size_t)ntypes * (size_t)gbase + mi;
-                rp_move rec;
-                rec.particle = pid;
-                rec.type = type;
-                rec.domain = cell;
-                rec.reserved = 0;
-                for (int q = 0; q < 3; q++) rec.translation[q] = t64[q];
-                for (int q = 0; q < 9; q++) rec.rotation[q] = R64[q];
-                rec.uniform = uni;
-                A.log[li] = rec;
-                A.log_codes[li] = full_code;
+        const uint8_t full_code = code | (acc ? RP_CODE_ACCEPTED : 0);
+        if (LIST) {
+            if (lane == 0 && A.codes) A.codes[out_index] = full_code;
+        } else if (A.log) {
+            rp_move *rec = A.log + (size_t)ntypes * (size_t)gbase + mi;
+            if (lane < 3) rec->translation[lane] = t64_lane;
+            const double rj = ej == 0 ? rrow[0] : (ej == 1 ? rrow[1] : rrow[2]);
+            if (lane < 9) rec->rotation[lane] = type != 0 ? rj : (lane % 4 == 0 ? 1.0 : 0.0);
+            if (lane == 0) {
+                rec->particle = pid;
+                rec->type = type;
+                rec->domain = cell;
+                rec->reserved = 0;
+                rec->uniform = uni;
+                A.log_codes[(size_t)ntypes * (size_t)gbase + mi] = full_code;
             }
         }
         ws.moves++;
@@ -709,25 +830,26 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
         if (type == 0) ws.trans++;
         else ws.rots++;
     }
-
 }
 
 template <int KIND, bool LIST>
-__global__ void __launch_bounds__(SWEEP_WARPS * 32) k_sweep(const SweepArgs A) {
+__global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(const SweepArgs A) {
     extern __shared__ float4 smem[];
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const int warps_per_block = blockDim.x >> 5;
     const int warp = blockIdx.x * warps_per_block + wib;
-    const int per_warp = A.cap * (KIND == 1 ? 2 : 1) + A.cap / 8;  // float4 units
+    const int per_warp = A.cap * (KIND == 1 ? 2 : 1) + A.cap / 4 + A.cap / 16;  // float4 units
     float4 *cpos = smem + (size_t)wib * per_warp;
     float4 *cax = cpos + A.cap;  // only for spherocylinders
-    uint16_t *queue = reinterpret_cast<uint16_t *>(cpos + A.cap * (KIND == 1 ? 2 : 1));
+    uint16_t *qseg = reinterpret_cast<uint16_t *>(cpos + A.cap * (KIND == 1 ? 2 : 1));
+    uint16_t *qun = qseg + A.cap;
+    uint8_t *nacc = reinterpret_cast<uint8_t *>(qun + A.cap);
     int nitems = A.work ? *A.work_count : (LIST ? A.num_list : A.num_active);
     WarpStats ws = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int item = warp; item < nitems; item += gridDim.x * warps_per_block) {
-        sweep_cell<KIND, LIST>(A, item, cpos, cax, queue, ws);
+        sweep_cell<KIND, LIST>(A, item, cpos, cax, qseg, qun, nacc, ws);
         __syncwarp();
     }
     // ---- statistics ----
@@ -785,7 +907,13 @@ cudaError_t launch_count(const DevState &s, const GridDev &g, int early, unsigne
 }
 
 size_t sweep_smem_per_warp(int kind, int cap) {
-    return (size_t)(cap * (kind == 1 ? 2 : 1) + cap / 8) * sizeof(float4);
+    return (size_t)(cap * (kind == 1 ? 2 : 1) + cap / 4 + cap / 16) * sizeof(float4);
+}
+
+cudaError_t launch_rot_table(double *out64, float *out32, uint32_t count, uint64_t seed, uint64_t counter, float step,
+                             cudaStream_t st) {
+    k_rot_table<<<(count + 255) / 256, 256, 0, st>>>(out64, out32, count, seed, counter, step);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_sweep(const SweepArgs &a, bool list, int nwarps, cudaStream_t st) {

@@ -83,10 +83,10 @@ def test_known_answer_translation_with_active_domain(engine, oracle, dy):
     with GpuPacking(kind, prm, pos, rot, box) as pk:
         info = pk.set_grid((0.0, 0.0, 0.0))
         _, cells, bounds = pk.grid()
-        assert info["dims"] == (10, 10, 10)
+        assert info["dims"] == (8, 8, 8)  # floor(5 / (0.5 (1 + 1e-9))) = 9, rounded down to even
         mv = np.zeros(1, dtype=_lib.MOVE_DTYPE)
         mv["particle"], mv["type"], mv["domain"], mv["uniform"] = 2, 0, int(cells[2]), 0.5
-        mv["translation"][0] = [0.0, dy, 0.0] if dy < 0.1 else [2, dy, -3.5]
+        mv["translation"][0] = [dy, dy, dy] if dy < 0.1 else [2, dy, -3.5]
         codes = pk.run_moves(mv)
         cpu = oracle.CpuPacking("oracle", kind, prm, pos, rot, box)
         want, _ = cpu.replay(mv, bounds)
