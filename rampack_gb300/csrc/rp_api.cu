@@ -215,16 +215,21 @@ DevState dev_state(Handle *h) {
         lrow = std::max(lrow, r);
     }
     const double u32 = std::ldexp(1.0, -24);
-    // per-component bound of the FP32 separation error: rounded cell-local coordinates
-    // and offsets, the staging and difference roundings and a translated mover.
+    // Per-component bound of the FP32 separation error, in units of u32 times the largest
+    // cell-local coordinate L: candidate coordinates (rebuild 4, mirror updates
+    // MIRROR_ROUNDINGS, offset 3, staging 2), the difference (3) and the mover (4 + its
+    // mirror updates + the translation 1) sum to 25; 32 covers them.
     const double e_sep = 32.0 * u32 * (lrow + 1.0);
-    const double e_axis = 16.0 * u32;  // FP32 axes (a rotated mover included)
-    const double safety = 4.0;
+    // FP32 axes: the FP64 axis rounded (1), a rotated mover's FP32 product (<= 6)
+    const double e_axis = 8.0 * u32;
+    const double safety = 2.0;
     FilterConsts fc{};
     double r = h->shape.radius, l = h->shape.length;
+    // bound on |d2_32 - d2| at a threshold thr = d^2: 2 d |delta| + |delta|^2 with
+    // |delta| <= sqrt(3) e_sep, plus the FP32 evaluation of the squared norm (3 roundings)
     auto margin = [&](double thr) {
         double d = std::sqrt(thr);
-        return safety * (2.0 * d * std::sqrt(3.0) * e_sep + 3.0 * e_sep * e_sep + 8.0 * u32 * thr);
+        return safety * (2.0 * d * std::sqrt(3.0) * e_sep + 3.0 * e_sep * e_sep + 4.0 * u32 * thr);
     };
     if (h->shape.kind == RP_SHAPE_SPHERE) {
         double thr = std::pow(2 * r, 2);
@@ -232,28 +237,48 @@ DevState dev_state(Handle *h) {
         fc.sphere_hi = static_cast<float>(thr + margin(thr));
     } else {
         double core = 4 * r * r, far = std::pow(2 * r + l, 2);
-        fc.core_lo = static_cast<float>(core - margin(far));
-        fc.core_hi = static_cast<float>(core + margin(far));
+        fc.core_lo = static_cast<float>(core - margin(core));
+        fc.core_hi = static_cast<float>(core + margin(core));
         fc.far_lo = static_cast<float>(far - margin(far));
         fc.far_hi = static_cast<float>(far + margin(far));
         fc.core_thr = static_cast<float>(core);
-        // segment-distance certificate: endpoint displacement from input errors, plus
-        // FP32 evaluation of dP, f and the gap (|w| <= |d| + l, |u| = |v| = l)
+        // Segment certificate.  Input errors move each cap by at most dend, which changes
+        // the segment distance d by at most 2 dend; near the threshold (d ~ 2r; farther away
+        // the decision has a margin larger than any of these terms) that is
+        // 2 (2r)(2 dend) + (2 dend)^2 in d^2.  FP32 evaluation of dP = w + s u - t v
+        // (|w| <= 2r + 2l, |u| = |v| = l) errs by at most 4 u32 sqrt(3) (|w| + 2 l) per
+        // vector, giving 2 (1.1 * 2r) ddp + ddp^2 in f; the gap G adds 4 u32 (2r) l.
         double dend = std::sqrt(3.0) * (e_sep + l * e_axis);
-        double dmax = 2 * r + l;
-        double eval = 12.0 * u32 * (dmax + 3 * l) * (dmax + 3 * l);
-        // FP64's own closest-point parameters err by about its input noise over D (the
-        // coordinates reach |x| ~ pmax, so every FP64 difference carries ~ulp(pmax)):
-        // nearly parallel pairs with D < d_min are re-decided in FP64, and the remaining
-        // FP64 suboptimality (<= g64) is added to the certificate's margin
+        double ddp = 4.0 * u32 * std::sqrt(3.0) * (2 * r + 4 * l);
+        double eval = 2.0 * 1.1 * (2 * r) * ddp + ddp * ddp + 4.0 * u32 * (2 * r) * l;
+        // FP64 evaluates the distance at its own closest-point parameters, with its own
+        // inputs; rounding in sN = b e - c d and D = a c - b^2 (|b|, |c| <= l^2,
+        // |d|, |e| <= l (2r + 2l)) moves the parameters by at most noise / D, which raises
+        // its distance^2 above the minimum by at most g64 = 2 (2r) l sqrt(2) noise / D.
+        // Pairs whose (cancellation-free) D is below d_min are re-decided in FP64; g64 at
+        // d_min joins the certificate's margin.
         double pmax = 0;
         for (int i = 0; i < 3; i++)
             pmax = std::max(pmax, std::fabs(h->box[3 * i]) + std::fabs(h->box[3 * i + 1]) + std::fabs(h->box[3 * i + 2]));
         const double u64 = std::ldexp(1.0, -52);
-        const double noise = 8.0 * u64 * (pmax + l) * l * l * (dmax + 2 * l);
+        const double noise = 8.0 * u64 * 2.0 * l * l * l * (2 * r + 2 * l);
         const double g64 = 2e-6;
-        fc.d_min = static_cast<float>(std::max(64.0 * noise * l * (2 * r) / g64, 1e-7 * l * l * l * l));
+        fc.d_min = static_cast<float>(std::max(4.0 * (2 * r) * l * std::sqrt(2.0) * noise / g64 * 10.0,
+                                               1e-9 * l * l * l * l));
         fc.seg_err = static_cast<float>(safety * (2.0 * (2 * r) * 2.0 * dend + 4.0 * dend * dend + eval) + g64);
+        // Parallel branch (SegmentDistanceCalculator.h:35-39, taken when FP64's D < 1e-10):
+        // FP64's D = l^4 sin^2(theta) up to ~4 ulp(l^4), so sin(theta) < theta_lim keeps it
+        // there; FP32 axes add up to ~4 * 2^-24 to the angle.  The branch evaluates the
+        // distance from the s = 0 end, at most 2 (2r) l sin(theta) above the minimum.
+        const double d_noise = 16.0 * l * l * l * u64 * (pmax + l);  // FP64 rounding in its D
+        const double theta_lim = std::sqrt(std::max(0.0, 0.8e-10 - d_noise)) / (l * l) - 8.0 * u32;
+        if (l > 0 && theta_lim > 0) {
+            fc.d_par = static_cast<float>(l * l * l * l * theta_lim * theta_lim * 0.5);
+            fc.par_err = static_cast<float>(4.0 * (2 * r + 1e-3) * l * (theta_lim + 8.0 * u32) + 1e-6);
+        } else {
+            fc.d_par = 0.0f;
+            fc.par_err = 0.0f;
+        }
         fc.len = static_cast<float>(l);
         fc.half_len = static_cast<float>(0.5 * l);
     }

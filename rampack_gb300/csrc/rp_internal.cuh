@@ -30,6 +30,8 @@ struct FilterConsts {
     float core_thr;               // 4 r^2
     float seg_err;                // bound on |f32 - f| of the segment distance^2
     float d_min;                  // D = |u|^2 |v|^2 - (u.v)^2 below which FP64 decides
+    float d_par;                  // D below which FP64 certainly takes its parallel branch
+    float par_err;                // bound on that branch's excess over the true minimum
     float len;                    // spherocylinder cylinder length l
     float half_len;               // l / 2
     float cell_margin;            // relative in-cell margin of the FP32 ActiveDomain test

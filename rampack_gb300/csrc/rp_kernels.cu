@@ -62,12 +62,24 @@ __device__ __forceinline__ int seg_stage(const FilterConsts &fc, float3 d, float
     // axes (D below d_min) are left to FP64, whose own parameter error grows like 1/D
     float3 cr = make_float3(fmaf(u.y, v.z, -u.z * v.y), fmaf(u.z, v.x, -u.x * v.z), fmaf(u.x, v.y, -u.y * v.x));
     float D = dot3f(cr, cr);
-    if (D < fc.d_min) return 2;
-    float sN = fmaf(b, e, -c * dd), tN = fmaf(a, e, -b * dd), sD = D, tD = D;
-    if (sN < 0.f) {
-        sN = 0.f; tN = e; tD = c;
-    } else if (sN > sD) {
-        sN = sD; tN = e + b; tD = c;
+    // axes parallel to within d_par: the FP64 reference certainly takes its parallel branch
+    // (D < 1e-10: closest points from the s = 0 end), whose distance exceeds the true
+    // minimum by at most par_err; in between the two thresholds FP64 decides
+    const bool par = D < fc.d_par;
+    if (!par && D < fc.d_min) return 2;
+    float sN, tN, sD, tD;
+    if (par) {
+        sN = 0.f; sD = 1.f; tN = e; tD = c;
+    } else {
+        sN = fmaf(b, e, -c * dd);
+        tN = fmaf(a, e, -b * dd);
+        sD = D;
+        tD = D;
+        if (sN < 0.f) {
+            sN = 0.f; tN = e; tD = c;
+        } else if (sN > sD) {
+            sN = sD; tN = e + b; tD = c;
+        }
     }
     if (tN < 0.f) {
         tN = 0.f;
@@ -87,8 +99,9 @@ __device__ __forceinline__ int seg_stage(const FilterConsts &fc, float3 d, float
     float f = dot3f(dP, dP);
     float gs = dot3f(dP, u), gt = -dot3f(dP, v);
     float G = 2.f * (gs * sc - fminf(gs, 0.f) + gt * tc - fminf(gt, 0.f));
-    if (f + fc.seg_err < fc.core_thr) return 1;
-    if (f - G - fc.seg_err >= fc.core_thr) return 0;
+    const float err = par ? fc.seg_err + fc.par_err : fc.seg_err;
+    if (f + err < fc.core_thr) return 1;
+    if (f - G - err >= fc.core_thr) return 0;
     return 2;
 }
 
