@@ -60,6 +60,8 @@ struct Handle {
     unsigned long long *counters = nullptr;
     double *rtab64 = nullptr;   // per-sweep rotation table
     float *rtab32 = nullptr;
+    int32_t *item_counters = nullptr;  // work counters of persistent sweep launches
+    int num_sms = 0;
     unsigned long long *count_out = nullptr;
     int *flag = nullptr;
     int32_t *overflow = nullptr;
@@ -488,6 +490,7 @@ int rp_create(const rp_shape_desc *shape, int64_t n, int device, void **handle) 
     };
     cudaError_t e = cudaSetDevice(device);
     if (e != cudaSuccess) return bail(e);
+    if ((e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess) return bail(e);
     if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e);
     for (int i = 0; i < 2; i++) {
         if ((e = cudaMalloc(&h->pos64[i], sizeof(double) * 3 * n)) != cudaSuccess) return bail(e);
@@ -495,7 +498,8 @@ int rp_create(const rp_shape_desc *shape, int64_t n, int device, void **handle) 
     }
     if ((e = cudaMalloc(&h->rot64, sizeof(double) * 9 * n)) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc(&h->rtab64, sizeof(double) * 9 * ROT_TABLE)) != cudaSuccess) return bail(e);
-    if ((e = cudaMalloc(&h->rtab32, sizeof(float) * 9 * ROT_TABLE)) != cudaSuccess) return bail(e);
+    if ((e = cudaMalloc(&h->rtab32, sizeof(float) * 12 * ROT_TABLE)) != cudaSuccess) return bail(e);
+    if ((e = cudaMalloc(&h->item_counters, sizeof(int32_t) * 64)) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc(&h->status, sizeof(uint32_t))) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc(&h->counters, sizeof(unsigned long long) * 8)) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc(&h->count_out, sizeof(unsigned long long))) != cudaSuccess) return bail(e);
@@ -533,6 +537,7 @@ int rp_destroy(void *handle) {
     cudaFree(h->rot64);
     cudaFree(h->rtab64);
     cudaFree(h->rtab32);
+    cudaFree(h->item_counters);
     cudaFree(h->block_sums);
     cudaFree(h->status);
     cudaFree(h->counters);
@@ -830,13 +835,16 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
         }
     }
     if (stats) RP_CUDA(h, cudaMemsetAsync(h->counters, 0, sizeof(unsigned long long) * 8, h->stream));
+    RP_CUDA(h, cudaMemsetAsync(h->item_counters, 0, sizeof(int32_t) * 64, h->stream));
     if (types & 2) {
         Group grp(h, RP_KERNEL_REBUILD, 1);
         RP_CUDA(h, launch_rot_table(h->rtab64, h->rtab32, ROT_TABLE, p->seed, p->counter,
                                     static_cast<float>(p->rotation_step), h->stream));
     }
+    int phase_no = 0;
     for (int ph : phases) {
         SweepArgs a = base_args(h);
+        a.next_item = h->item_counters + phase_no++;
         int act[3];
         for (int d = 0; d < 3; d++) {
             a.phase[d] = (ph >> d) & 1;
@@ -859,8 +867,10 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
         }
         {
             Group grp(h, RP_KERNEL_SWEEP, 1);
-            RP_CUDA(h, launch_sweep(a, false, a.num_active, h->stream));
+            int resident = h->num_sms * SWEEP_WARPS * SWEEP_MIN_BLOCKS;
+            RP_CUDA(h, launch_sweep(a, false, std::min(a.num_active, resident), h->stream));
         }
+        a.next_item = nullptr;
         rc = run_overflow(h, a, false);
         if (rc) return rc;
     }

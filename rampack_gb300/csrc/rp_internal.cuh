@@ -99,7 +99,7 @@ struct SweepArgs {
     float tstep, rstep;
     int types;                     // bit 0 translation, bit 1 rotation
     const double *rtab64;          // rotation table of this sweep: [rtab_mask + 1][9] exact FP64
-    const float *rtab32;           // the same rotations rounded to FP32
+    const float *rtab32;           // the same rotations rounded to FP32, padded to 12 floats
     uint32_t rtab_mask;
     rp_move *log;                  // [ntypes * n] indexed by ntypes * start[cell] + k
     uint8_t *log_codes;
@@ -110,6 +110,7 @@ struct SweepArgs {
     const int32_t *work;           // optional explicit list of cells (overflow rerun)
     const int32_t *work_count;     // device-side length of `work`
     int num_work;
+    int32_t *next_item;            // persistent launch: shared cell counter (zeroed per launch)
 };
 
 }  // namespace rp

@@ -289,7 +289,7 @@ __global__ void k_rot_table(double *out64, float *out32, uint32_t count, uint64_
         for (int b = 0; b < 3; b++) {
             double e = (a == b ? 1.0 : 0.0) + kap * (K[3 * a + b] + v[a] * v[b] - (a == b ? vv : 0.0));
             out64[9 * (size_t)i + 3 * a + b] = e;
-            out32[9 * (size_t)i + 3 * a + b] = (float)e;
+            out32[12 * (size_t)i + 3 * a + b] = (float)e;
         }
 }
 
@@ -549,7 +549,9 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
                 rot_idx = r.b & A.rtab_mask;
                 rot_inv = (r.c & 1u) != 0;
                 if (KIND == 1) {
-                    const float *R = A.rtab32 + 9 * (size_t)rot_idx;
+                    const float4 *R4 = reinterpret_cast<const float4 *>(A.rtab32) + 3 * (size_t)rot_idx;
+                    float4 x0 = R4[0], x1 = R4[1], x2 = R4[2];
+                    float R[9] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w, x2.x};
                     for (int q = 0; q < 9; q++) R32[q] = rot_inv ? R[3 * (q % 3) + q / 3] : R[q];
                 }
             }
@@ -573,25 +575,16 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
         // ---- FP32 ActiveDomain test (translations): 0 inside, 1 outside, 2 undecided;
         //      and whether the PBC correction may move the particle through the box ----
         int dom = 0;
-        bool maywrap = false;
+        float3 fnew = make_float3(0.f, 0.f, 0.f);
         if (type != 1) {
-            float3 f = mat32(G.cellinv, pn.x, pn.y, pn.z);
-            float3 f0 = mat32(G.cellinv, pcur.x, pcur.y, pcur.z);
-            float fm[3] = {f.x, f.y, f.z}, fo[3] = {f0.x, f0.y, f0.z};
+            fnew = mat32(G.cellinv, pn.x, pn.y, pn.z);
+            float fm[3] = {fnew.x, fnew.y, fnew.z};
             const float mg = S.fc.cell_margin;
             for (int d = 0; d < 3; d++) {
                 if (G.dims[d] > 1) {
                     if (fm[d] < -mg || fm[d] > 1.f + mg) dom = 1;
                     else if (dom == 0 && (fm[d] < mg || fm[d] > 1.f - mg)) dom = 2;
                 }
-                // relative coordinate of the stored (wrapped) position before the move, and of
-                // the translated position in the same image: s + (c + f) / n minus the wrap k
-                float rold = G.fshift[d] + ((float)c[d] + fo[d]) * G.finv_dims[d];
-                float rnew = G.fshift[d] + ((float)c[d] + fm[d]) * G.finv_dims[d];
-                float k = rold >= 1.f ? 1.f : 0.f;
-                if (fabsf(rold - 1.f) < mg) maywrap = true;
-                rnew -= k;
-                if (rnew < mg || rnew > 1.f - mg) maywrap = true;
             }
         }
 
@@ -607,7 +600,6 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
                     if (__float_as_int(q.w) != pid) {
                         float dx = q.x - pn.x, dy = q.y - pn.y, dz = q.z - pn.z;
                         c0 = A.fp64_only ? 2 : d2_stage<KIND>(S.fc, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-                        ws.pairs++;
                     }
                 }
                 if (k1 < total) {
@@ -615,7 +607,6 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
                     if (__float_as_int(q.w) != pid) {
                         float dx = q.x - pn.x, dy = q.y - pn.y, dz = q.z - pn.z;
                         c1 = A.fp64_only ? 2 : d2_stage<KIND>(S.fc, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-                        ws.pairs++;
                     }
                 }
                 if (__ballot_sync(FULL, c0 == 1 || c1 == 1)) {
@@ -682,6 +673,23 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
         }
         if (need64) {
             if (type != 1) {
+                // May the PBC correction move the particle through the box?  FP32 relative
+                // coordinates of the stored (wrapped) position and of the translated one in
+                // the same image: s + (c + f) / n, minus the stored position's wrap k.
+                bool maywrap = false;
+                {
+                    float3 f0 = mat32(G.cellinv, pcur.x, pcur.y, pcur.z);
+                    float fm[3] = {fnew.x, fnew.y, fnew.z}, fo[3] = {f0.x, f0.y, f0.z};
+                    const float mg = S.fc.cell_margin;
+                    for (int d = 0; d < 3; d++) {
+                        float rold = G.fshift[d] + ((float)c[d] + fo[d]) * G.finv_dims[d];
+                        float rnew = G.fshift[d] + ((float)c[d] + fm[d]) * G.finv_dims[d];
+                        float k = rold >= 1.f ? 1.f : 0.f;
+                        if (fabsf(rold - 1.f) < mg) maywrap = true;
+                        rnew -= k;
+                        if (rnew < mg || rnew > 1.f - mg) maywrap = true;
+                    }
+                }
                 // Shape::translate with the PBC correction (core/Shape.cpp:9-12,
                 // core/PeriodicBoundaryConditions.cpp:11-22), one box row per lane
                 if (!LIST) t64_lane = (double)(ld == 0 ? t32.x : (ld == 1 ? t32.y : t32.z));
@@ -836,6 +844,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
                 A.log_codes[(size_t)ntypes * (size_t)gbase + mi] = full_code;
             }
         }
+        if (dom != 1 && lane == 0) ws.pairs += (unsigned)(total - 1);
         ws.moves++;
         if (acc) ws.accepted++;
         if (code == 1) ws.rej_overlap++;
@@ -861,13 +870,23 @@ __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(co
     uint8_t *nacc = reinterpret_cast<uint8_t *>(qun + A.cap);
     int nitems = A.work ? *A.work_count : (LIST ? A.num_list : A.num_active);
     WarpStats ws = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (int item = warp; item < nitems; item += gridDim.x * warps_per_block) {
+    // persistent launches (next_item set) take cells from a shared counter until none are
+    // left; otherwise warps stride over the cells
+    const int stride = gridDim.x * warps_per_block;
+    int item = warp;
+    for (;;) {
+        if (A.next_item) {
+            int it = 0;
+            if (lane == 0) it = atomicAdd(A.next_item, 1);
+            item = __shfl_sync(FULL, it, 0);
+        }
+        if (item >= nitems) break;
         sweep_cell<KIND, LIST>(A, item, cpos, cax, qseg, qun, nacc, ws);
         __syncwarp();
+        item += stride;
     }
     // ---- statistics ----
     unsigned pairs = ws.pairs;
-    for (int d = 16; d > 0; d >>= 1) pairs += __shfl_xor_sync(FULL, pairs, d);
     if (lane == 0 && ws.moves) {
         unsigned long long *C = A.s.counters;
         atomicAdd(C + 0, (unsigned long long)ws.moves);
