@@ -1,0 +1,83 @@
+// GpuPacking (rampack_gb300/host/GpuPacking.hpp) driven like the reference's own Packing
+// tests (test/unit_tests/core/PackingTest.cpp:86-166): hard spheres r = 0.25 at three
+// positions in a 5x5x5 box.  Prints "ok" and exits 0 when every check holds.
+#include <cmath>
+#include <limits>
+#include <cstdio>
+#include <vector>
+
+#include "../../rampack_gb300/host/GpuPacking.hpp"
+
+using rampack_gb300::GpuPacking;
+
+static int failures = 0;
+#define CHECK(cond)                                                        \
+    do {                                                                   \
+        if (!(cond)) {                                                     \
+            std::printf("FAILED line %d: %s\n", __LINE__, #cond);          \
+            failures++;                                                    \
+        }                                                                  \
+    } while (0)
+
+static std::vector<GpuPacking::Shape> three() {
+    std::vector<GpuPacking::Shape> s(3);
+    s[0].position = {0.5, 0.5, 0.5};
+    s[1].position = {4.5, 0.5, 0.5};
+    s[2].position = {2.5, 2.5, 4.0};
+    return s;
+}
+
+int main() {
+    const double inf = std::numeric_limits<double>::infinity();
+    GpuPacking::Mat3 box{5, 0, 0, 0, 5, 0, 0, 0, 5};
+    {
+        GpuPacking pk(box, three(), 0.25);
+        CHECK(pk.countTotalOverlaps() == 0);
+        GpuPacking::Mat3 b51{2.55, 0, 0, 0, 2.55, 0, 0, 0, 2.55};
+        CHECK(pk.tryScaling(b51) == 0);
+        auto s = pk.getShapes();
+        CHECK(std::fabs(s[1].position[0] - 2.295) < 1e-9);
+    }
+    {
+        GpuPacking pk(box, three(), 0.25);
+        GpuPacking::Mat3 b49{2.45, 0, 0, 0, 2.45, 0, 0, 0, 2.45};
+        CHECK(pk.tryScaling(b49) == inf);
+        pk.revertScaling();
+        auto s = pk.getShapes();
+        CHECK(s[2].position[2] == 4.0);
+        CHECK(pk.getBox()[0] == 5.0);
+    }
+    {
+        GpuPacking pk(box, three(), 0.25);
+        CHECK(pk.tryTranslation(2, {0.01, 0.01, 0.01}) == 0);
+        auto s = pk.getShapes();
+        CHECK(s[2].position[0] == 2.5);  // tried, not accepted
+        pk.acceptTranslation();
+        s = pk.getShapes();
+        CHECK(s[2].position[0] == 2.51 && s[2].position[2] == 4.01);
+        // a rotation by pi/2 about z changes the orientation only
+        CHECK(pk.tryRotation(0, {0, -1, 0, 1, 0, 0, 0, 0, 1}) == 0);
+        pk.acceptRotation();
+        s = pk.getShapes();
+        CHECK(s[0].orientation[1] == -1.0 && s[0].position[0] == 0.5);
+    }
+    {
+        // spherocylinders: a device sweep keeps the packing overlap-free
+        std::vector<GpuPacking::Shape> sc;
+        for (int i = 0; i < 6; i++)
+            for (int j = 0; j < 6; j++)
+                for (int k = 0; k < 6; k++) {
+                    GpuPacking::Shape s;
+                    s.position = {1.2 * (i + 0.5), 1.2 * (j + 0.5), 3.6 * (k + 0.5)};
+                    sc.push_back(s);
+                }
+        GpuPacking pk({7.2, 0, 0, 0, 7.2, 0, 0, 0, 21.6}, sc, 0.5, 2.0);
+        auto st = pk.performMoves(0.2, 0.2, 42, 0);
+        CHECK(st.moves == 2 * sc.size());
+        CHECK(st.accepted > 0 && st.accepted < st.moves);
+        CHECK(pk.countTotalOverlaps(true) == 0);
+    }
+    if (failures) return 1;
+    std::printf("ok\n");
+    return 0;
+}
