@@ -102,7 +102,7 @@ typedef struct rp_sweep_stats {
     uint64_t accepted;
     uint64_t rejected_overlap;
     uint64_t rejected_domain;
-    uint64_t pair_tests;          /* FP32-filtered pair tests */
+    uint64_t pair_tests;          /* candidate pairs the FP32 filter examined (scans stop at a certain overlap) */
     uint64_t fp64_pairs;          /* pairs re-decided in FP64 (the guard band) */
     uint64_t translations;
     uint64_t rotations;
@@ -115,7 +115,9 @@ typedef struct rp_sweep_stats {
 #define RP_KERNEL_COUNT 2         /* all-pairs overlap recount */
 #define RP_KERNEL_RESCALE 3       /* box rescale */
 #define RP_KERNEL_OVERFLOW 4      /* large-capacity rerun of oversized neighbourhoods */
-#define RP_NUM_KERNELS 5
+#define RP_KERNEL_ORDER 5         /* partner ranking of the learned ordering */
+#define RP_KERNEL_MLP 6           /* ranking-network training and inference */
+#define RP_NUM_KERNELS 7
 
 /* ---- lifetime ---------------------------------------------------------------------- */
 
@@ -213,6 +215,59 @@ int rp_set_timing(void *handle, int on);
 /* Accumulated device time (ms) and launch-group count per kernel group
  * (RP_NUM_KERNELS entries each) since timing was turned on; synchronizes the stream. */
 int rp_get_timing(void *handle, double *ms, uint64_t *groups);
+
+/* ---- learned ordering of overlap tests ----------------------------------------------
+ * No reference counterpart: the reference tests a mover against its neighbour-grid cells in
+ * cell order (countParticleOverlaps, core/Packing.cpp:373-430).  Here a small network (13 pair features -> 64 -> 64
+ * -> 1, ReLU, BF16 weights on the tensor cores, FP32 accumulation) scores each particle's
+ * in-range neighbours every few sweeps; the sweep pre-tests a mover's best-ranked
+ * partners before its full neighbourhood scan and stops early only on a certain overlap, so
+ * every decision, and the state after every sweep, is the plain sweep's.  The network is
+ * trained on the device from pair outcomes the sweep logs (forward, backward and Adam
+ * kernels of this library). */
+
+#define RP_MLP_NPARAM 5313        /* W1[64][16], b1[64], W2[64][64], b2[64], w3[64], b3 (FP32) */
+#define RP_MLP_FEATURES 16        /* per pair: 13 features, 3 zeros */
+
+#define RP_ORDER_OFF 0            /* plain cell-order scan */
+#define RP_ORDER_MLP 1            /* partners ranked by the network */
+#define RP_ORDER_DISTANCE 2       /* partners ranked by centre distance (untrained ordering) */
+
+/* Sets the network's parameters to a seeded random initialisation (He-uniform weights,
+ * zero biases); the Adam state is cleared.  A new handle starts from seed 0. */
+int rp_mlp_init(void *handle, uint64_t seed);
+
+/* Copies RP_MLP_NPARAM FP32 parameters to / from the host (layout above). */
+int rp_mlp_set_params(void *handle, const float *params);
+int rp_mlp_get_params(void *handle, float *params);
+
+/* Logits of n pairs (host arrays: feats n x RP_MLP_FEATURES, logits n) by the tensor-core
+ * inference path the ranking uses. */
+int rp_mlp_predict(void *handle, const float *feats, int64_t n, float *logits);
+
+/* Gradient (RP_MLP_NPARAM floats) and value of the mean binary cross-entropy of the logits
+ * of n labelled pairs (labels 0/1), computed by the training kernels. */
+int rp_mlp_gradient(void *handle, const float *feats, const uint8_t *labels, int64_t n, float *grad,
+                    float *loss);
+
+/* Pair-outcome log: with capacity > 0, every `every`-th move of each later sweep appends
+ * the pairs that reached its segment test (features before the move, label 1 if the moved
+ * pair overlaps for certain, 0 if it certainly does not) until `capacity` pairs are held.
+ * capacity 0 turns logging off and frees the log. */
+int rp_pair_log_enable(void *handle, int64_t capacity, int32_t every);
+
+/* Copies up to `capacity` logged pairs to the host (either pointer may be NULL) and reports
+ * how many the log holds in *count; rp_pair_log_clear empties it. */
+int rp_pair_log_read(void *handle, float *feats, uint8_t *labels, int64_t capacity, int64_t *count);
+int rp_pair_log_clear(void *handle);
+
+/* Trains the network on the logged pairs: `epochs` passes of Adam (learning rate lr) over
+ * the log in batches of `batch` pairs, visited in a seeded shuffled order.  *loss (may be
+ * NULL) receives the mean batch loss of the last epoch. */
+int rp_mlp_train(void *handle, int32_t epochs, int32_t batch, float lr, uint64_t seed, float *loss);
+
+/* Chooses the ordering of later sweeps (RP_ORDER_*), re-ranking every `every` sweeps. */
+int rp_set_ordering(void *handle, int32_t mode, int32_t every);
 
 /* ---- allocation-free overlap count ----------------------------------------------- */
 

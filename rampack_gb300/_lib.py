@@ -56,6 +56,7 @@ class SweepStats(C.Structure):
 
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
+_F = C.POINTER(C.c_float)
 
 # name -> (restype, argtypes); every function declared in include/rampack_gb300.h
 SIGNATURES = {
@@ -78,8 +79,21 @@ SIGNATURES = {
     "rp_get_timing": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]),
     "rp_count_overlaps_static": (C.c_int, [C.POINTER(ShapeDesc), C.c_int64, _P, _P, _D, C.c_int, _P,
                                            C.POINTER(C.c_int64)]),
+    "rp_mlp_init": (C.c_int, [_P, C.c_uint64]),
+    "rp_mlp_set_params": (C.c_int, [_P, _F]),
+    "rp_mlp_get_params": (C.c_int, [_P, _F]),
+    "rp_mlp_predict": (C.c_int, [_P, _F, C.c_int64, _F]),
+    "rp_mlp_gradient": (C.c_int, [_P, _F, _P, C.c_int64, _F, _F]),
+    "rp_pair_log_enable": (C.c_int, [_P, C.c_int64, C.c_int32]),
+    "rp_pair_log_read": (C.c_int, [_P, _F, _P, C.c_int64, C.POINTER(C.c_int64)]),
+    "rp_pair_log_clear": (C.c_int, [_P]),
+    "rp_mlp_train": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_float, C.c_uint64, _F]),
+    "rp_set_ordering": (C.c_int, [_P, C.c_int32, C.c_int32]),
 }
-KERNEL_GROUPS = ["sweep", "rebuild", "count", "rescale", "overflow"]
+KERNEL_GROUPS = ["sweep", "rebuild", "count", "rescale", "overflow", "order", "mlp"]
+MLP_NPARAM = 5313
+MLP_FEATURES = 16
+ORDER_OFF, ORDER_MLP, ORDER_DISTANCE = 0, 1, 2
 
 _LIB = None
 
@@ -108,3 +122,7 @@ class EngineError(RuntimeError):
 
 def dptr(a: np.ndarray):
     return a.ctypes.data_as(_D)
+
+
+def fptr(a: np.ndarray):
+    return a.ctypes.data_as(_F)

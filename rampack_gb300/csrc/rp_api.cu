@@ -22,6 +22,16 @@ cudaError_t launch_count(const DevState &s, const GridDev &g, int early, unsigne
                          cudaStream_t st);
 cudaError_t launch_sweep(const SweepArgs &a, bool list, int nwarps, cudaStream_t st);
 size_t sweep_smem_per_warp(int kind, int cap);
+cudaError_t launch_mlp_grad(const float *feats, const uint8_t *labels, int64_t total, int64_t i0, int n,
+                            int64_t mul, int64_t off, const float *w32, float *grad, float *loss, int num_sms,
+                            cudaStream_t st);
+cudaError_t launch_mlp_adam(float *w32, __nv_bfloat16 *w16, const float *grad, float *m, float *v, float lr,
+                            int step, cudaStream_t st);
+cudaError_t launch_mlp_sync16(const float *w32, __nv_bfloat16 *w16, cudaStream_t st);
+cudaError_t launch_mlp_predict(const float *feats, int n, const float *w32, const __nv_bfloat16 *w16, float *out,
+                               cudaStream_t st);
+cudaError_t launch_score_partners(const DevState &s, const GridDev &g, const float *w32, const __nv_bfloat16 *w16,
+                                  int mode, float inv_range, int32_t *partners, cudaStream_t st);
 cudaError_t launch_rot_table(double *out64, float *out32, uint32_t count, uint64_t seed, uint64_t counter, float step,
                              cudaStream_t st);
 
@@ -97,6 +107,25 @@ struct Handle {
     double kernel_ms[RP_NUM_KERNELS]{};
     uint64_t kernel_groups[RP_NUM_KERNELS]{};
     bool strict_box = false;
+    // learned ordering: network parameters (FP32 master + BF16 copy), Adam moments, scratch
+    float *mlp_w32 = nullptr, *mlp_grad = nullptr, *mlp_m = nullptr, *mlp_v = nullptr, *mlp_loss = nullptr;
+    __nv_bfloat16 *mlp_w16 = nullptr;
+    int mlp_step = 0;
+    float *mlp_feats = nullptr;     // host-supplied pairs (predict / gradient)
+    int64_t mlp_feats_alloc = 0;
+    uint8_t *mlp_labels = nullptr;
+    int64_t mlp_labels_alloc = 0;
+    float *mlp_out = nullptr;
+    int64_t mlp_out_alloc = 0;
+    int32_t *partners = nullptr;    // [n][MLP_PARTNERS]
+    bool partners_valid = false;
+    int order_mode = RP_ORDER_OFF, order_every = 1, since_rank = 0;
+    // pair-outcome log
+    float *pair_feats = nullptr;
+    uint8_t *pair_labels = nullptr;
+    unsigned long long *pair_count = nullptr;
+    int64_t pair_cap = 0;
+    int pair_every = 0;
 };
 
 cudaEvent_t pool_event(Handle *h) {
@@ -452,6 +481,69 @@ int run_overflow(Handle *h, SweepArgs a, bool list) {
     return RP_OK;
 }
 
+// ---- learned ordering -----------------------------------------------------------
+static_assert(MLP_NPARAM == RP_MLP_NPARAM && MLP_IN == RP_MLP_FEATURES, "network layout");
+
+
+// He-uniform weights from a splitmix64 stream, zero biases.
+void mlp_init_host(uint64_t seed, std::vector<float> &w) {
+    w.assign(MLP_NPARAM, 0.f);
+    uint64_t x = seed ^ 0x6a09e667f3bcc909ull;
+    auto next = [&x]() {
+        x += 0x9e3779b97f4a7c15ull;
+        uint64_t z = x;
+        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+        z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+        z ^= z >> 31;
+        return static_cast<double>(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+    };
+    const double a1 = std::sqrt(6.0 / MLP_FEATURES), a2 = std::sqrt(6.0 / MLP_H);
+    for (int o = 0; o < MLP_H; o++)
+        for (int k = 0; k < MLP_IN; k++) w[MLP_W1 + o * MLP_IN + k] = k < MLP_FEATURES ? static_cast<float>(a1 * next()) : 0.f;
+    for (int i = 0; i < MLP_H * MLP_H; i++) w[MLP_W2 + i] = static_cast<float>(a2 * next());
+    for (int i = 0; i < MLP_H; i++) w[MLP_W3 + i] = static_cast<float>(a2 * next());
+}
+
+int mlp_upload(Handle *h, const float *params) {
+    RP_CUDA(h, cudaMemcpyAsync(h->mlp_w32, params, sizeof(float) * MLP_NPARAM, cudaMemcpyHostToDevice, h->stream));
+    RP_CUDA(h, cudaMemsetAsync(h->mlp_m, 0, sizeof(float) * MLP_NPARAM, h->stream));
+    RP_CUDA(h, cudaMemsetAsync(h->mlp_v, 0, sizeof(float) * MLP_NPARAM, h->stream));
+    RP_CUDA(h, launch_mlp_sync16(h->mlp_w32, h->mlp_w16, h->stream));
+    RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->mlp_step = 0;
+    h->partners_valid = false;
+    return RP_OK;
+}
+
+// Allocates the network state on first use (seed-0 initialisation).
+int mlp_ready(Handle *h) {
+    if (h->mlp_w32) return RP_OK;
+    RP_CUDA(h, cudaMalloc(&h->mlp_w32, sizeof(float) * MLP_NPARAM));
+    RP_CUDA(h, cudaMalloc(&h->mlp_grad, sizeof(float) * MLP_NPARAM));
+    RP_CUDA(h, cudaMalloc(&h->mlp_m, sizeof(float) * MLP_NPARAM));
+    RP_CUDA(h, cudaMalloc(&h->mlp_v, sizeof(float) * MLP_NPARAM));
+    RP_CUDA(h, cudaMalloc(&h->mlp_loss, sizeof(float)));
+    RP_CUDA(h, cudaMalloc(&h->mlp_w16, sizeof(__nv_bfloat16) * (MLP_NPARAM + 7)));
+    std::vector<float> w;
+    mlp_init_host(0, w);
+    return mlp_upload(h, w.data());
+}
+
+// Ranks every particle's in-range neighbours on the current grid (one launch).
+int rank_partners(Handle *h) {
+    int rc = mlp_ready(h);
+    if (rc) return rc;
+    if (!h->partners) RP_CUDA(h, cudaMalloc(&h->partners, sizeof(int32_t) * MLP_PARTNERS * h->n));
+    {
+        Group grp(h, RP_KERNEL_ORDER, 1);
+        RP_CUDA(h, launch_score_partners(dev_state(h), h->grid[h->gcur].d, h->mlp_w32, h->mlp_w16, h->order_mode,
+                                         static_cast<float>(1.0 / h->range), h->partners, h->stream));
+    }
+    h->partners_valid = true;
+    h->since_rank = 0;
+    return RP_OK;
+}
+
 }  // namespace
 }  // namespace rp
 
@@ -550,6 +642,11 @@ int rp_destroy(void *handle) {
     cudaFree(h->d_codes);
     cudaFree(h->d_log);
     cudaFree(h->d_log_codes);
+    for (void *p : {(void *)h->mlp_w32, (void *)h->mlp_grad, (void *)h->mlp_m, (void *)h->mlp_v,
+                    (void *)h->mlp_loss, (void *)h->mlp_w16, (void *)h->mlp_feats, (void *)h->mlp_labels,
+                    (void *)h->mlp_out, (void *)h->partners, (void *)h->pair_feats, (void *)h->pair_labels,
+                    (void *)h->pair_count})
+        cudaFree(p);
     for (auto &m : h->marks) {
         cudaEventDestroy(m.a);
         cudaEventDestroy(m.b);
@@ -576,6 +673,7 @@ int rp_upload_state(void *handle, const double *pos, const double *rot, const do
     std::memcpy(h->inv, inv, sizeof(h->inv));
     h->pcur = 0;
     h->gcur = 0;
+    h->partners_valid = false;
     RP_CUDA(h, cudaMemcpyAsync(h->pos64[0], pos, sizeof(double) * 3 * h->n, cudaMemcpyHostToDevice, h->stream));
     RP_CUDA(h, cudaMemcpyAsync(h->rot64, rot, sizeof(double) * 9 * h->n, cudaMemcpyHostToDevice, h->stream));
     double tt[375];
@@ -841,9 +939,23 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
         RP_CUDA(h, launch_rot_table(h->rtab64, h->rtab32, ROT_TABLE, p->seed, p->counter,
                                     static_cast<float>(p->rotation_step), h->stream));
     }
+    if (h->order_mode != RP_ORDER_OFF && (!h->partners_valid || h->since_rank >= h->order_every)) {
+        int rc2 = rank_partners(h);
+        if (rc2) return rc2;
+    }
+    h->since_rank++;
     int phase_no = 0;
     for (int ph : phases) {
         SweepArgs a = base_args(h);
+        if (h->order_mode != RP_ORDER_OFF) a.partners = h->partners;
+        if (h->pair_cap > 0) {
+            a.pair_feats = h->pair_feats;
+            a.pair_labels = h->pair_labels;
+            a.pair_count = h->pair_count;
+            a.pair_cap = static_cast<unsigned long long>(h->pair_cap);
+            a.pair_every = h->pair_every;
+        }
+        a.inv_range = static_cast<float>(1.0 / h->range);
         a.next_item = h->item_counters + phase_no++;
         int act[3];
         for (int d = 0; d < 3; d++) {
@@ -1062,6 +1174,198 @@ int rp_get_timing(void *handle, double *ms, uint64_t *groups) {
         if (ms) ms[k] = h->kernel_ms[k];
         if (groups) groups[k] = h->kernel_groups[k];
     }
+    return RP_OK;
+}
+
+// ---- learned ordering ---------------------------------------------------------------
+
+int rp_mlp_init(void *handle, uint64_t seed) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h) return RP_ERR_ARG;
+    RP_CUDA(h, cudaSetDevice(h->device));
+    int rc = mlp_ready(h);
+    if (rc) return rc;
+    std::vector<float> w;
+    mlp_init_host(seed, w);
+    return mlp_upload(h, w.data());
+}
+
+int rp_mlp_set_params(void *handle, const float *params) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !params) return fail(h, RP_ERR_ARG, "null argument");
+    RP_CUDA(h, cudaSetDevice(h->device));
+    int rc = mlp_ready(h);
+    if (rc) return rc;
+    return mlp_upload(h, params);
+}
+
+int rp_mlp_get_params(void *handle, float *params) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !params) return fail(h, RP_ERR_ARG, "null argument");
+    RP_CUDA(h, cudaSetDevice(h->device));
+    int rc = mlp_ready(h);
+    if (rc) return rc;
+    RP_CUDA(h, cudaMemcpyAsync(params, h->mlp_w32, sizeof(float) * MLP_NPARAM, cudaMemcpyDeviceToHost, h->stream));
+    RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    return RP_OK;
+}
+
+int rp_mlp_predict(void *handle, const float *feats, int64_t n, float *logits) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || (n > 0 && (!feats || !logits)) || n < 0) return fail(h, RP_ERR_ARG, "bad argument");
+    if (n > (int64_t{1} << 30)) return fail(h, RP_ERR_ARG, "too many pairs");
+    if (n == 0) return RP_OK;
+    RP_CUDA(h, cudaSetDevice(h->device));
+    int rc = mlp_ready(h);
+    if (rc) return rc;
+    RP_CUDA(h, ensure(h->mlp_feats, h->mlp_feats_alloc, n * MLP_IN));
+    RP_CUDA(h, ensure(h->mlp_out, h->mlp_out_alloc, n));
+    RP_CUDA(h, cudaMemcpyAsync(h->mlp_feats, feats, sizeof(float) * MLP_IN * n, cudaMemcpyHostToDevice, h->stream));
+    {
+        Group grp(h, RP_KERNEL_MLP, 1);
+        RP_CUDA(h, launch_mlp_predict(h->mlp_feats, static_cast<int>(n), h->mlp_w32, h->mlp_w16, h->mlp_out, h->stream));
+    }
+    RP_CUDA(h, cudaMemcpyAsync(logits, h->mlp_out, sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream));
+    RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    return RP_OK;
+}
+
+int rp_mlp_gradient(void *handle, const float *feats, const uint8_t *labels, int64_t n, float *grad, float *loss) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !feats || !labels || !grad || n <= 0) return fail(h, RP_ERR_ARG, "bad argument");
+    if (n > (int64_t{1} << 30)) return fail(h, RP_ERR_ARG, "too many pairs");
+    RP_CUDA(h, cudaSetDevice(h->device));
+    int rc = mlp_ready(h);
+    if (rc) return rc;
+    RP_CUDA(h, ensure(h->mlp_feats, h->mlp_feats_alloc, n * MLP_IN));
+    RP_CUDA(h, ensure(h->mlp_labels, h->mlp_labels_alloc, n));
+    RP_CUDA(h, cudaMemcpyAsync(h->mlp_feats, feats, sizeof(float) * MLP_IN * n, cudaMemcpyHostToDevice, h->stream));
+    RP_CUDA(h, cudaMemcpyAsync(h->mlp_labels, labels, n, cudaMemcpyHostToDevice, h->stream));
+    RP_CUDA(h, cudaMemsetAsync(h->mlp_grad, 0, sizeof(float) * MLP_NPARAM, h->stream));
+    RP_CUDA(h, cudaMemsetAsync(h->mlp_loss, 0, sizeof(float), h->stream));
+    {
+        Group grp(h, RP_KERNEL_MLP, 1);
+        RP_CUDA(h, launch_mlp_grad(h->mlp_feats, h->mlp_labels, n, 0, static_cast<int>(n), 1, 0, h->mlp_w32,
+                                   h->mlp_grad, h->mlp_loss, h->num_sms, h->stream));
+    }
+    RP_CUDA(h, cudaMemcpyAsync(grad, h->mlp_grad, sizeof(float) * MLP_NPARAM, cudaMemcpyDeviceToHost, h->stream));
+    float l = 0;
+    RP_CUDA(h, cudaMemcpyAsync(&l, h->mlp_loss, sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (loss) *loss = l;
+    return RP_OK;
+}
+
+int rp_pair_log_enable(void *handle, int64_t capacity, int32_t every) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || capacity < 0 || (capacity > 0 && every <= 0)) return fail(h, RP_ERR_ARG, "bad argument");
+    RP_CUDA(h, cudaSetDevice(h->device));
+    RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    cudaFree(h->pair_feats);
+    cudaFree(h->pair_labels);
+    h->pair_feats = nullptr;
+    h->pair_labels = nullptr;
+    h->pair_cap = 0;
+    h->pair_every = 0;
+    if (capacity == 0) return RP_OK;
+    if (!h->pair_count) RP_CUDA(h, cudaMalloc(&h->pair_count, sizeof(unsigned long long)));
+    RP_CUDA(h, cudaMalloc(&h->pair_feats, sizeof(float) * MLP_IN * capacity));
+    RP_CUDA(h, cudaMalloc(&h->pair_labels, capacity));
+    RP_CUDA(h, cudaMemsetAsync(h->pair_count, 0, sizeof(unsigned long long), h->stream));
+    h->pair_cap = capacity;
+    h->pair_every = every;
+    return RP_OK;
+}
+
+static int pair_log_held(Handle *h, int64_t *held) {
+    unsigned long long c = 0;
+    if (h->pair_count) {
+        RP_CUDA(h, cudaMemcpyAsync(&c, h->pair_count, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
+        RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    }
+    *held = std::min<int64_t>(static_cast<int64_t>(c), h->pair_cap);
+    return RP_OK;
+}
+
+int rp_pair_log_read(void *handle, float *feats, uint8_t *labels, int64_t capacity, int64_t *count) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !count || capacity < 0) return fail(h, RP_ERR_ARG, "bad argument");
+    RP_CUDA(h, cudaSetDevice(h->device));
+    int64_t held = 0;
+    int rc = pair_log_held(h, &held);
+    if (rc) return rc;
+    *count = held;
+    int64_t k = std::min(held, capacity);
+    if (k > 0 && feats)
+        RP_CUDA(h, cudaMemcpyAsync(feats, h->pair_feats, sizeof(float) * MLP_IN * k, cudaMemcpyDeviceToHost, h->stream));
+    if (k > 0 && labels) RP_CUDA(h, cudaMemcpyAsync(labels, h->pair_labels, k, cudaMemcpyDeviceToHost, h->stream));
+    RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    return RP_OK;
+}
+
+int rp_pair_log_clear(void *handle) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h) return RP_ERR_ARG;
+    RP_CUDA(h, cudaSetDevice(h->device));
+    if (h->pair_count) RP_CUDA(h, cudaMemsetAsync(h->pair_count, 0, sizeof(unsigned long long), h->stream));
+    return RP_OK;
+}
+
+int rp_mlp_train(void *handle, int32_t epochs, int32_t batch, float lr, uint64_t seed, float *loss) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || epochs < 0 || batch <= 0 || !(lr > 0)) return fail(h, RP_ERR_ARG, "bad argument");
+    RP_CUDA(h, cudaSetDevice(h->device));
+    int rc = mlp_ready(h);
+    if (rc) return rc;
+    int64_t held = 0;
+    rc = pair_log_held(h, &held);
+    if (rc) return rc;
+    if (held == 0) return fail(h, RP_ERR_STATE, "the pair log is empty");
+    const int64_t nb = (held + batch - 1) / batch;
+    float last = 0;
+    for (int ep = 0; ep < epochs; ep++) {
+        // a multiplier coprime with the log size and an offset: a seeded permutation
+        uint64_t x = seed * 0x9e3779b97f4a7c15ull + static_cast<uint64_t>(ep) * 0xbf58476d1ce4e5b9ull + 1;
+        x ^= x >> 29;
+        int64_t mul = static_cast<int64_t>(x % static_cast<uint64_t>(held)) | 1;
+        auto gcd = [](int64_t a, int64_t b) {
+            while (b) {
+                int64_t t = a % b;
+                a = b;
+                b = t;
+            }
+            return a;
+        };
+        while (gcd(mul, held) != 1) mul += 2;
+        if (held == 1) mul = 1;
+        const int64_t off = static_cast<int64_t>((x >> 17) % static_cast<uint64_t>(held));
+        RP_CUDA(h, cudaMemsetAsync(h->mlp_loss, 0, sizeof(float), h->stream));
+        Group grp(h, RP_KERNEL_MLP, static_cast<int>(2 * nb));
+        for (int64_t b = 0; b < nb; b++) {
+            const int64_t i0 = b * batch;
+            const int cnt = static_cast<int>(std::min<int64_t>(batch, held - i0));
+            RP_CUDA(h, cudaMemsetAsync(h->mlp_grad, 0, sizeof(float) * MLP_NPARAM, h->stream));
+            RP_CUDA(h, launch_mlp_grad(h->pair_feats, h->pair_labels, held, i0, cnt, mul, off, h->mlp_w32,
+                                       h->mlp_grad, h->mlp_loss, h->num_sms, h->stream));
+            RP_CUDA(h, launch_mlp_adam(h->mlp_w32, h->mlp_w16, h->mlp_grad, h->mlp_m, h->mlp_v, lr, ++h->mlp_step,
+                                       h->stream));
+        }
+        if (ep == epochs - 1) {
+            RP_CUDA(h, cudaMemcpyAsync(&last, h->mlp_loss, sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+            RP_CUDA(h, cudaStreamSynchronize(h->stream));
+        }
+    }
+    if (loss) *loss = static_cast<float>(last / static_cast<double>(nb));
+    h->partners_valid = false;
+    return RP_OK;
+}
+
+int rp_set_ordering(void *handle, int32_t mode, int32_t every) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || mode < RP_ORDER_OFF || mode > RP_ORDER_DISTANCE || every <= 0) return fail(h, RP_ERR_ARG, "bad argument");
+    h->order_mode = mode;
+    h->order_every = every;
+    h->partners_valid = false;
     return RP_OK;
 }
 

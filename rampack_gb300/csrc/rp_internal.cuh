@@ -7,6 +7,7 @@
 #include <cstdint>
 
 #include "rp_geom.cuh"
+#include "rp_mlp.cuh"
 #include "../../include/rampack_gb300.h"
 
 namespace rp {
@@ -111,6 +112,15 @@ struct SweepArgs {
     const int32_t *work_count;     // device-side length of `work`
     int num_work;
     int32_t *next_item;            // persistent launch: shared cell counter (zeroed per launch)
+    // learned ordering: best-ranked partners per particle (pre-tested before the full scan)
+    const int32_t *partners;       // [n][MLP_PARTNERS] particle indices, -1 = none; NULL = off
+    // pair-outcome log for training the ranking network
+    float *pair_feats;             // [pair_cap][16]
+    uint8_t *pair_labels;          // [pair_cap]
+    unsigned long long *pair_count;
+    unsigned long long pair_cap;
+    int pair_every;                // log the pairs of every pair_every-th move (0 = off)
+    float inv_range;
 };
 
 }  // namespace rp

@@ -391,7 +391,7 @@ struct WarpStats {
     unsigned moves, accepted, rej_overlap, rej_domain, pairs, fp64, trans, rots;
 };
 
-template <int KIND, bool LIST>
+template <int KIND, bool LIST, bool LEARN>
 __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, float4 *cpos, float4 *cax,
                                            uint16_t *qseg, uint16_t *qun, uint8_t *nacc, WarpStats &ws) {
     const unsigned FULL = 0xffffffffu;
@@ -588,13 +588,50 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
             }
         }
 
-        // ---- FP32 pass 1: centre distances, two candidates per lane per round ----
+        // ---- learned ordering: pre-test the mover's best-ranked partners ----
         bool overlap = false;
+        if (LEARN && A.partners && dom != 1) {
+            int cls = 0;
+            bool tested = false;
+            if (lane < MLP_PARTNERS) {
+                const int pj = A.partners[MLP_PARTNERS * (size_t)pid + lane];
+                if (pj >= 0) {
+                    const int sj = G.pid_slot[pj], cj = G.pid_cell[pj];
+                    int o[3] = {cj % G.dims[0] - c[0], (cj / G.dims[0]) % G.dims[1] - c[1],
+                                cj / (G.dims[0] * G.dims[1]) - c[2]};
+                    bool near = true;
+                    for (int d = 0; d < 3; d++) {
+                        if (o[d] > 1) o[d] -= G.dims[d];
+                        if (o[d] < -1) o[d] += G.dims[d];
+                        if (o[d] > 1 || o[d] < -1) near = false;
+                    }
+                    if (near) {
+                        float3 of = mat32(G.cellmat, (float)o[0], (float)o[1], (float)o[2]);
+                        float4 q = G.mpos[sj];
+                        float3 dsep = make_float3((q.x + of.x) - pn.x, (q.y + of.y) - pn.y, (q.z + of.z) - pn.z);
+                        float3 aj = make_float3(0.f, 0.f, 1.f);
+                        if (KIND == 1) {
+                            float4 a = G.maxis[sj];
+                            aj = make_float3(a.x, a.y, a.z);
+                        }
+                        cls = classify<KIND>(S.fc, dsep, an, aj);
+                        tested = true;
+                    }
+                }
+            }
+            const unsigned nt = __popc(__ballot_sync(FULL, tested));
+            if (lane == 0) ws.pairs += nt;
+            // a certain overlap with any image of any partner is the reference's answer too
+            if (__ballot_sync(FULL, cls == 1)) overlap = true;
+        }
+
+        // ---- FP32 pass 1: centre distances, two candidates per lane per round ----
         int nseg = 0, nun = 0;
-        if (dom != 1) {
+        if (dom != 1 && !overlap) {
             for (int base = 0; base < total; base += 64) {
                 int k0 = base + lane, k1 = base + 32 + lane;
                 int c0 = 0, c1 = 0;
+                if (lane == 0) ws.pairs += (unsigned)min(64, total - base);
                 if (k0 < total) {
                     float4 q = cpos[k0];
                     if (__float_as_int(q.w) != pid) {
@@ -640,6 +677,29 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
                     cls = seg_stage(S.fc, make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z), an,
                                     make_float3(a.x, a.y, a.z));
                 }
+                if (LEARN && A.pair_every > 0 && ((mi + cell) % A.pair_every) == 0) {
+                    // training data of the ranking network: the pair as it was before the
+                    // move, labelled with the certain outcome after it
+                    const bool rec = i < nseg && cls != 2;
+                    const unsigned bal = __ballot_sync(FULL, rec);
+                    unsigned long long base_idx = 0;
+                    if (lane == 0 && bal) base_idx = atomicAdd(A.pair_count, (unsigned long long)__popc(bal));
+                    base_idx = __shfl_sync(FULL, base_idx, 0);
+                    const unsigned long long idx = base_idx + __popc(bal & lt);
+                    if (rec && idx < A.pair_cap) {
+                        float4 q = cpos[k];
+                        float4 a = cax[k];
+                        float f[MLP_IN];
+                        mlp_features(make_float3(q.x - pcur.x, q.y - pcur.y, q.z - pcur.z), ai,
+                                     make_float3(a.x, a.y, a.z), A.inv_range, f);
+                        float4 *dst = reinterpret_cast<float4 *>(A.pair_feats + idx * MLP_IN);
+                        dst[0] = make_float4(f[0], f[1], f[2], f[3]);
+                        dst[1] = make_float4(f[4], f[5], f[6], f[7]);
+                        dst[2] = make_float4(f[8], f[9], f[10], f[11]);
+                        dst[3] = make_float4(f[12], f[13], f[14], f[15]);
+                        A.pair_labels[idx] = cls == 1 ? 1 : 0;
+                    }
+                }
                 if (__ballot_sync(FULL, cls == 1)) {
                     overlap = true;
                     break;
@@ -653,7 +713,9 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
 
         uint8_t code = dom == 1 ? 2 : (overlap ? 1 : 0);
         // ---- FP64: the exact proposal of a surviving move (or of an accepted u == 0 move) ----
-        const bool need64 = (code == 0) || (uni <= 0.0);
+        // (an overlap found near the cell wall still needs the exact ActiveDomain test: the
+        // reference rejects a move that leaves the domain before it tests any overlap)
+        const bool need64 = (code == 0) || (uni <= 0.0) || (dom == 2);
         const bool needR = type != 0 && (need64 || A.log != nullptr);
         double rel_own = 0.0, pnew_own = 0.0, onew_own = 0.0, rrow[3] = {0.0, 0.0, 0.0};
         bool exact_rel = false;     // rel_own holds the exact FP64 relative coordinate
@@ -844,7 +906,6 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
                 A.log_codes[(size_t)ntypes * (size_t)gbase + mi] = full_code;
             }
         }
-        if (dom != 1 && lane == 0) ws.pairs += (unsigned)(total - 1);
         ws.moves++;
         if (acc) ws.accepted++;
         if (code == 1) ws.rej_overlap++;
@@ -854,7 +915,9 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
     }
 }
 
-template <int KIND, bool LIST>
+// LEARN instantiates the learned-ordering pre-test and the pair-outcome log (kept out of
+// the plain kernel, whose registers they would crowd)
+template <int KIND, bool LIST, bool LEARN>
 __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(const SweepArgs A) {
     extern __shared__ float4 smem[];
     const unsigned FULL = 0xffffffffu;
@@ -881,7 +944,7 @@ __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(co
             item = __shfl_sync(FULL, it, 0);
         }
         if (item >= nitems) break;
-        sweep_cell<KIND, LIST>(A, item, cpos, cax, qseg, qun, nacc, ws);
+        sweep_cell<KIND, LIST, LEARN>(A, item, cpos, cax, qseg, qun, nacc, ws);
         __syncwarp();
         item += stride;
     }
@@ -948,31 +1011,30 @@ cudaError_t launch_rot_table(double *out64, float *out32, uint32_t count, uint64
     return cudaGetLastError();
 }
 
+template <int KIND, bool LIST, bool LEARN>
+static cudaError_t launch_sweep_t(const SweepArgs &a, unsigned blocks, int threads, size_t smem, cudaStream_t st) {
+    cudaError_t e = cudaFuncSetAttribute(k_sweep<KIND, LIST, LEARN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    k_sweep<KIND, LIST, LEARN><<<blocks, threads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_sweep(const SweepArgs &a, bool list, int nwarps, cudaStream_t st) {
     if (nwarps <= 0) return cudaSuccess;
     const int wpb = a.work ? 1 : SWEEP_WARPS;
     size_t smem = sweep_smem_per_warp(a.s.kind, a.cap) * wpb;
     unsigned blocks = (unsigned)((nwarps + wpb - 1) / wpb);
-    cudaError_t e = cudaSuccess;
+    const int th = wpb * 32;
+    const bool learn = !list && (a.partners != nullptr || a.pair_every > 0);
     if (a.s.kind == 0) {
-        if (list) {
-            e = cudaFuncSetAttribute(k_sweep<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e == cudaSuccess) k_sweep<0, true><<<blocks, wpb * 32, smem, st>>>(a);
-        } else {
-            e = cudaFuncSetAttribute(k_sweep<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e == cudaSuccess) k_sweep<0, false><<<blocks, wpb * 32, smem, st>>>(a);
-        }
-    } else {
-        if (list) {
-            e = cudaFuncSetAttribute(k_sweep<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e == cudaSuccess) k_sweep<1, true><<<blocks, wpb * 32, smem, st>>>(a);
-        } else {
-            e = cudaFuncSetAttribute(k_sweep<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e == cudaSuccess) k_sweep<1, false><<<blocks, wpb * 32, smem, st>>>(a);
-        }
+        if (list) return launch_sweep_t<0, true, false>(a, blocks, th, smem, st);
+        return learn ? launch_sweep_t<0, false, true>(a, blocks, th, smem, st)
+                     : launch_sweep_t<0, false, false>(a, blocks, th, smem, st);
     }
-    if (e != cudaSuccess) return e;
-    return cudaGetLastError();
+    if (list) return launch_sweep_t<1, true, false>(a, blocks, th, smem, st);
+    return learn ? launch_sweep_t<1, false, true>(a, blocks, th, smem, st)
+                 : launch_sweep_t<1, false, false>(a, blocks, th, smem, st);
 }
 
 }  // namespace rp

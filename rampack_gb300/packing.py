@@ -22,7 +22,7 @@ import math
 import numpy as np
 
 from . import _lib
-from ._lib import (MOVE_DTYPE, EngineError, GridInfo, ShapeDesc, SweepParams, SweepStats, dptr)
+from ._lib import (MOVE_DTYPE, EngineError, GridInfo, ShapeDesc, SweepParams, SweepStats, dptr, fptr)
 
 
 class GpuPacking:
@@ -157,10 +157,62 @@ class GpuPacking:
         self._check(self.lib.rp_set_timing(self.h, 1 if on else 0))
 
     def timing(self) -> dict:
-        ms = (C.c_double * 5)()
-        groups = (C.c_uint64 * 5)()
+        ng = len(_lib.KERNEL_GROUPS)
+        ms = (C.c_double * ng)()
+        groups = (C.c_uint64 * ng)()
         self._check(self.lib.rp_get_timing(self.h, ms, groups))
         return {name: (float(ms[k]), int(groups[k])) for k, name in enumerate(_lib.KERNEL_GROUPS)}
+
+    # ---- learned ordering of the overlap tests ----
+    def mlp_init(self, seed: int = 0):
+        self._check(self.lib.rp_mlp_init(self.h, seed))
+
+    def mlp_params(self) -> np.ndarray:
+        w = np.zeros(_lib.MLP_NPARAM, dtype=np.float32)
+        self._check(self.lib.rp_mlp_get_params(self.h, fptr(w)))
+        return w
+
+    def set_mlp_params(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32).reshape(_lib.MLP_NPARAM)
+        self._check(self.lib.rp_mlp_set_params(self.h, fptr(w)))
+
+    def mlp_predict(self, feats) -> np.ndarray:
+        f = np.ascontiguousarray(feats, dtype=np.float32).reshape(-1, _lib.MLP_FEATURES)
+        out = np.zeros(len(f), dtype=np.float32)
+        self._check(self.lib.rp_mlp_predict(self.h, fptr(f), len(f), fptr(out)))
+        return out
+
+    def mlp_gradient(self, feats, labels):
+        f = np.ascontiguousarray(feats, dtype=np.float32).reshape(-1, _lib.MLP_FEATURES)
+        lab = np.ascontiguousarray(labels, dtype=np.uint8).reshape(len(f))
+        g = np.zeros(_lib.MLP_NPARAM, dtype=np.float32)
+        loss = C.c_float()
+        self._check(self.lib.rp_mlp_gradient(self.h, fptr(f), lab.ctypes.data_as(C.c_void_p), len(f), fptr(g),
+                                             C.byref(loss)))
+        return g, float(loss.value)
+
+    def pair_log_enable(self, capacity: int, every: int = 1):
+        self._check(self.lib.rp_pair_log_enable(self.h, capacity, every))
+
+    def pair_log(self, capacity: int | None = None):
+        cnt = C.c_int64()
+        self._check(self.lib.rp_pair_log_read(self.h, None, None, 0, C.byref(cnt)))
+        k = cnt.value if capacity is None else min(cnt.value, capacity)
+        f = np.zeros((k, _lib.MLP_FEATURES), dtype=np.float32)
+        lab = np.zeros(k, dtype=np.uint8)
+        self._check(self.lib.rp_pair_log_read(self.h, fptr(f), lab.ctypes.data_as(C.c_void_p), k, C.byref(cnt)))
+        return f, lab
+
+    def pair_log_clear(self):
+        self._check(self.lib.rp_pair_log_clear(self.h))
+
+    def mlp_train(self, epochs: int, batch: int, lr: float, seed: int = 0) -> float:
+        loss = C.c_float()
+        self._check(self.lib.rp_mlp_train(self.h, epochs, batch, lr, seed, C.byref(loss)))
+        return float(loss.value)
+
+    def set_ordering(self, mode: int, every: int = 1):
+        self._check(self.lib.rp_set_ordering(self.h, mode, every))
 
     # ---- box moves ----
     def try_scaling(self, box) -> float:
