@@ -11,6 +11,7 @@ and recounts all overlaps.  Synthetic seeded input; no dataset.
 
   python bench.py [--gpus N] [--steps K] [--warmup W]           GPU engine (this repo)
   python bench.py --impl reference [--steps K] [--warmup W]     CPU implementation of the path
+  python bench.py --ordering [--steps K]                        learned test ordering vs plain scan
 
 Metric: attempted particle moves per second (higher is better).
 """
@@ -49,6 +50,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--seed", type=int, default=1234)
+    ap.add_argument("--ordering", action="store_true",
+                    help="compare the plain scan with centre-distance and learned partner ordering")
     return ap.parse_args()
 
 
@@ -392,10 +395,81 @@ def main_gpu(args):
     return 0
 
 
+def main_ordering(args):
+    """Sweeps of the bench workload with the plain neighbourhood scan, with partners ranked by
+    centre distance, and with partners ranked by the network trained on pair outcomes logged
+    by the sweep itself.  Every ordering must leave the state bit-identical to the plain
+    sweep's; reported: device time of the move sweep and of the ranking per sweep, and the
+    candidate pairs examined per move."""
+    from rampack_gb300 import _lib
+    from rampack_gb300 import build as rb
+    rb.build()
+    from rampack_gb300.packing import GpuPacking
+
+    kind, prm, pos, rot, box = workload(args.n_side)
+    g = GpuPacking(kind, prm, pos, rot, box)
+    for c in range(20):
+        g.sweep(TRANS_STEP, ROT_STEP, seed=args.seed, counter=c, stats=False)
+    start = g.state()
+    # training data: pairs of every 16th move of 4 sweeps, then 4 epochs of Adam
+    g.pair_log_enable(4_000_000, 16)
+    for c in range(4):
+        g.sweep(TRANS_STEP, ROT_STEP, seed=args.seed + 1, counter=c, stats=False)
+    feats, labels = g.pair_log()
+    _, loss0 = g.mlp_gradient(feats[:200_000], labels[:200_000])
+    g.set_timing(True)
+    t0 = time.perf_counter()
+    loss = g.mlp_train(epochs=4, batch=1024, lr=2e-3, seed=args.seed)
+    train_s = time.perf_counter() - t0
+    train_ms = g.timing()["mlp"][0]
+    g.set_timing(False)
+    _, loss1 = g.mlp_gradient(feats[:200_000], labels[:200_000])
+    g.pair_log_enable(0)
+
+    sweeps = max(args.steps, 4)
+    rows = []
+    ref_state = None
+    for label, mode, every in [("plain", _lib.ORDER_OFF, 1), ("distance", _lib.ORDER_DISTANCE, 1),
+                               ("distance", _lib.ORDER_DISTANCE, 16), ("mlp", _lib.ORDER_MLP, 1),
+                               ("mlp", _lib.ORDER_MLP, 16), ("mlp", _lib.ORDER_MLP, 64)]:
+        g.upload(*start)
+        g.set_ordering(mode, every)
+        g.set_timing(True)
+        pairs = moves = 0
+        for c in range(sweeps):
+            st = g.sweep(TRANS_STEP, ROT_STEP, seed=args.seed + 2, counter=c)
+            pairs += st["pair_tests"]
+            moves += st["moves"]
+        t = g.timing()
+        g.set_timing(False)
+        state = g.state()
+        if ref_state is None:
+            ref_state = state
+        same = bool(np.array_equal(state[0], ref_state[0]) and np.array_equal(state[1], ref_state[1]))
+        sweep_ms = (t["sweep"][0] + t["overflow"][0]) / sweeps
+        order_ms = t["order"][0] / sweeps
+        rows.append({"ordering": label, "rerank_every": every, "sweep_ms": round(sweep_ms, 4),
+                     "ranking_ms": round(order_ms, 4), "total_ms": round(sweep_ms + order_ms, 4),
+                     "pairs_per_move": round(pairs / moves, 2), "state_identical_to_plain": same})
+    base = rows[0]["total_ms"]
+    for r in rows:
+        r["speedup_vs_plain"] = round(base / r["total_ms"], 3)
+    print(json.dumps({"metric": "learned ordering vs plain scan", "unit": "ms per sweep",
+                      "workload": WORKLOAD.format(n=len(pos)), "sweeps": sweeps,
+                      "training": {"pairs": int(len(feats)), "positive_fraction": round(float(labels.mean()), 4),
+                                   "epochs": 4, "batch": 1024, "loss_before": round(loss0, 4),
+                                   "loss_after": round(loss1, 4), "last_epoch_loss": round(loss, 4),
+                                   "device_ms": round(train_ms, 1), "wall_s": round(train_s, 2)},
+                      "rows": rows}))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return main_reference(args)
+    if args.ordering:
+        return main_ordering(args)
     return main_gpu(args)
 
 

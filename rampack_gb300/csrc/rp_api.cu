@@ -21,7 +21,7 @@ cudaError_t launch_rescale(const double *src, double *dst, int64_t n, const doub
 cudaError_t launch_count(const DevState &s, const GridDev &g, int early, unsigned long long *out, int *flag,
                          cudaStream_t st);
 cudaError_t launch_sweep(const SweepArgs &a, bool list, int nwarps, cudaStream_t st);
-size_t sweep_smem_per_warp(int kind, int cap);
+size_t sweep_smem_per_warp(int kind, int cap, bool learn = false);
 cudaError_t launch_mlp_grad(const float *feats, const uint8_t *labels, int64_t total, int64_t i0, int n,
                             int64_t mul, int64_t off, const float *w32, float *grad, float *loss, int num_sms,
                             cudaStream_t st);
@@ -471,6 +471,8 @@ int run_overflow(Handle *h, SweepArgs a, bool list) {
     a.cap = cap;
     a.work = h->overflow;
     a.work_count = h->overflow_count;
+    a.partners = nullptr;  // the plain kernel: no partner pre-test, no pair log
+    a.pair_every = 0;
     a.num_work = -1;
     a.overflow = nullptr;
     {

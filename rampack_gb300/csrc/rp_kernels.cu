@@ -393,7 +393,8 @@ struct WarpStats {
 
 template <int KIND, bool LIST, bool LEARN>
 __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, float4 *cpos, float4 *cax,
-                                           uint16_t *qseg, uint16_t *qun, uint8_t *nacc, WarpStats &ws) {
+                                           uint16_t *qseg, uint16_t *qun, uint8_t *nacc, uint16_t *pstage,
+                                           WarpStats &ws) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -465,6 +466,27 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
     const bool self_images = (G.dims[0] == 1) || (G.dims[1] == 1) || (G.dims[2] == 1);
     // per own-cell particle: FP32 roundings accumulated in its mirror position this sweep
     for (int k = lane; k < occ; k += 32) nacc[k] = 0;
+    if (LEARN && A.partners) {
+        // the ranked partners of the cell's particles, as indices into the staged
+        // neighbourhood (a partner out of reach of this cell's neighbourhood gets none)
+        const int base_nb = incl - cnt;
+        for (int eb = 0; eb < occ * MLP_PARTNERS; eb += 32) {
+            const int e = eb + lane;
+            int sj = -1;
+            if (e < occ * MLP_PARTNERS) {
+                const int pk = __float_as_int(cpos[e / MLP_PARTNERS].w);
+                const int pj = A.partners[MLP_PARTNERS * (size_t)pk + e % MLP_PARTNERS];
+                if (pj >= 0) sj = G.pid_slot[pj];
+            }
+            int idx = 0xffff;
+            for (int nb = 0; nb < 27; nb++) {
+                const int s0 = __shfl_sync(FULL, st, nb), c0 = __shfl_sync(FULL, cnt, nb),
+                          b0 = __shfl_sync(FULL, base_nb, nb);
+                if (idx == 0xffff && sj >= s0 && sj < s0 + c0) idx = b0 + sj - s0;
+            }
+            if (e < occ * MLP_PARTNERS) pstage[e] = (uint16_t)idx;
+        }
+    }
     __syncwarp();
 
     // this lane's dimension (lanes 0-2): ActiveDomain bounds and cell coordinate
@@ -589,39 +611,29 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
         }
 
         // ---- learned ordering: pre-test the mover's best-ranked partners ----
+        // (the staged candidate and the FP32 arithmetic of the full scan, so a certain
+        // overlap here is one the scan would find)
         bool overlap = false;
         if (LEARN && A.partners && dom != 1) {
             int cls = 0;
             bool tested = false;
             if (lane < MLP_PARTNERS) {
-                const int pj = A.partners[MLP_PARTNERS * (size_t)pid + lane];
-                if (pj >= 0) {
-                    const int sj = G.pid_slot[pj], cj = G.pid_cell[pj];
-                    int o[3] = {cj % G.dims[0] - c[0], (cj / G.dims[0]) % G.dims[1] - c[1],
-                                cj / (G.dims[0] * G.dims[1]) - c[2]};
-                    bool near = true;
-                    for (int d = 0; d < 3; d++) {
-                        if (o[d] > 1) o[d] -= G.dims[d];
-                        if (o[d] < -1) o[d] += G.dims[d];
-                        if (o[d] > 1 || o[d] < -1) near = false;
-                    }
-                    if (near) {
-                        float3 of = mat32(G.cellmat, (float)o[0], (float)o[1], (float)o[2]);
-                        float4 q = G.mpos[sj];
-                        float3 dsep = make_float3((q.x + of.x) - pn.x, (q.y + of.y) - pn.y, (q.z + of.z) - pn.z);
+                const int k = pstage[MLP_PARTNERS * slot + lane];
+                if (k != 0xffff) {
+                    const float4 q = cpos[k];
+                    if (__float_as_int(q.w) != pid) {
                         float3 aj = make_float3(0.f, 0.f, 1.f);
                         if (KIND == 1) {
-                            float4 a = G.maxis[sj];
+                            const float4 a = cax[k];
                             aj = make_float3(a.x, a.y, a.z);
                         }
-                        cls = classify<KIND>(S.fc, dsep, an, aj);
+                        cls = classify<KIND>(S.fc, make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z), an, aj);
                         tested = true;
                     }
                 }
             }
             const unsigned nt = __popc(__ballot_sync(FULL, tested));
             if (lane == 0) ws.pairs += nt;
-            // a certain overlap with any image of any partner is the reference's answer too
             if (__ballot_sync(FULL, cls == 1)) overlap = true;
         }
 
@@ -925,12 +937,13 @@ __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(co
     const int wib = threadIdx.x >> 5;
     const int warps_per_block = blockDim.x >> 5;
     const int warp = blockIdx.x * warps_per_block + wib;
-    const int per_warp = A.cap * (KIND == 1 ? 2 : 1) + A.cap / 4 + A.cap / 16;  // float4 units
+    const int per_warp = A.cap * (KIND == 1 ? 2 : 1) + A.cap / 4 + A.cap / 16 + (LEARN ? A.cap / 4 : 0);  // float4
     float4 *cpos = smem + (size_t)wib * per_warp;
     float4 *cax = cpos + A.cap;  // only for spherocylinders
     uint16_t *qseg = reinterpret_cast<uint16_t *>(cpos + A.cap * (KIND == 1 ? 2 : 1));
     uint16_t *qun = qseg + A.cap;
     uint8_t *nacc = reinterpret_cast<uint8_t *>(qun + A.cap);
+    uint16_t *pstage = reinterpret_cast<uint16_t *>(nacc + A.cap);  // LEARN only: MLP_PARTNERS x cap
     int nitems = A.work ? *A.work_count : (LIST ? A.num_list : A.num_active);
     WarpStats ws = {0, 0, 0, 0, 0, 0, 0, 0};
     // persistent launches (next_item set) take cells from a shared counter until none are
@@ -944,7 +957,7 @@ __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(co
             item = __shfl_sync(FULL, it, 0);
         }
         if (item >= nitems) break;
-        sweep_cell<KIND, LIST, LEARN>(A, item, cpos, cax, qseg, qun, nacc, ws);
+        sweep_cell<KIND, LIST, LEARN>(A, item, cpos, cax, qseg, qun, nacc, pstage, ws);
         __syncwarp();
         item += stride;
     }
@@ -1001,8 +1014,8 @@ cudaError_t launch_count(const DevState &s, const GridDev &g, int early, unsigne
     return cudaGetLastError();
 }
 
-size_t sweep_smem_per_warp(int kind, int cap) {
-    return (size_t)(cap * (kind == 1 ? 2 : 1) + cap / 4 + cap / 16) * sizeof(float4);
+size_t sweep_smem_per_warp(int kind, int cap, bool learn) {
+    return (size_t)(cap * (kind == 1 ? 2 : 1) + cap / 4 + cap / 16 + (learn ? cap / 4 : 0)) * sizeof(float4);
 }
 
 cudaError_t launch_rot_table(double *out64, float *out32, uint32_t count, uint64_t seed, uint64_t counter, float step,
@@ -1023,10 +1036,10 @@ static cudaError_t launch_sweep_t(const SweepArgs &a, unsigned blocks, int threa
 cudaError_t launch_sweep(const SweepArgs &a, bool list, int nwarps, cudaStream_t st) {
     if (nwarps <= 0) return cudaSuccess;
     const int wpb = a.work ? 1 : SWEEP_WARPS;
-    size_t smem = sweep_smem_per_warp(a.s.kind, a.cap) * wpb;
+    const bool learn = !list && (a.partners != nullptr || a.pair_every > 0);
+    size_t smem = sweep_smem_per_warp(a.s.kind, a.cap, learn) * wpb;
     unsigned blocks = (unsigned)((nwarps + wpb - 1) / wpb);
     const int th = wpb * 32;
-    const bool learn = !list && (a.partners != nullptr || a.pair_every > 0);
     if (a.s.kind == 0) {
         if (list) return launch_sweep_t<0, true, false>(a, blocks, th, smem, st);
         return learn ? launch_sweep_t<0, false, true>(a, blocks, th, smem, st)

@@ -131,7 +131,10 @@ def test_ordered_sweeps_leave_the_plain_state(engine, name):
         (p, rr, b), acc, pairs = results[mode]
         assert np.array_equal(p, p0) and np.array_equal(rr, r0), f"mode {mode}: state differs"
         assert acc == acc0
-        assert pairs <= pairs0
+        if cfg[0] == 1:
+            # spherocylinders find most overlaps in the segment stage: pre-testing the
+            # ranked partners skips most of the scan of a rejected move
+            assert pairs < pairs0, (mode, pairs, pairs0)
 
 
 def test_ordered_sweep_log_replays_on_oracle(oracle, engine):
