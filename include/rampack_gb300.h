@@ -36,6 +36,8 @@ extern "C" {
 
 #define RP_SHAPE_SPHERE 0
 #define RP_SHAPE_SPHEROCYLINDER 1
+#define RP_SHAPE_POLYSPHERE 2     /* created by rp_create_polysphere */
+#define RP_MAX_CENTRES 8          /* spheres per polysphere */
 
 #define RP_MOVE_TRANSLATION 0
 #define RP_MOVE_ROTATION 1
@@ -126,6 +128,16 @@ typedef struct rp_sweep_stats {
  * (core/Packing.h:152-168) together with Packing::reset (core/Packing.cpp:67-82); the
  * state itself arrives through rp_upload_state. */
 int rp_create(const rp_shape_desc *shape, int64_t n, int device, void **handle);
+
+/* Creates an engine for n polyspheres: rigid bodies of num_centres hard spheres
+ * (1..RP_MAX_CENTRES) with body-frame centres (num_centres x 3) and radii.
+ * Replaces: Packing::Packing(..., PolysphereTraits(sphereData)) (core/Packing.h:152-168,
+ * core/shapes/PolysphereTraits.h) with Packing::setupForInteraction
+ * (core/Packing.cpp:931-950); bent chains (PolysphereBananaTraits) pass their generated
+ * sphere data.  Each particle carries the reference's rotated centres and absolute centres
+ * (core/Packing.cpp:1035-1047, :357-361). */
+int rp_create_polysphere(int32_t num_centres, const double *centres, const double *radii, int64_t n, int device,
+                         void **handle);
 
 /* Releases the handle and all of its device memory. */
 int rp_destroy(void *handle);

@@ -19,7 +19,8 @@ ERRORS = {
     -1: "RP_ERR_ARG", -2: "RP_ERR_CUDA", -3: "RP_ERR_STATE", -4: "RP_ERR_OVERLAP",
     -5: "RP_ERR_UNSUPPORTED", -6: "RP_ERR_DEVICE", -7: "RP_ERR_CAPACITY",
 }
-SHAPE_SPHERE, SHAPE_SPHEROCYLINDER = 0, 1
+SHAPE_SPHERE, SHAPE_SPHEROCYLINDER, SHAPE_POLYSPHERE = 0, 1, 2
+MAX_CENTRES = 8
 MOVE_TRANSLATION, MOVE_ROTATION, MOVE_ROTOTRANSLATION = 0, 1, 2
 CODE_ACCEPTED = 0x80
 SWEEP_LOG, SWEEP_FP64_ONLY = 1, 2
@@ -61,6 +62,7 @@ _F = C.POINTER(C.c_float)
 # name -> (restype, argtypes); every function declared in include/rampack_gb300.h
 SIGNATURES = {
     "rp_create": (C.c_int, [C.POINTER(ShapeDesc), C.c_int64, C.c_int, C.POINTER(C.c_void_p)]),
+    "rp_create_polysphere": (C.c_int, [C.c_int32, _D, _D, C.c_int64, C.c_int, C.POINTER(C.c_void_p)]),
     "rp_destroy": (C.c_int, [_P]),
     "rp_last_error": (C.c_char_p, [_P]),
     "rp_upload_state": (C.c_int, [_P, _D, _D, _D]),

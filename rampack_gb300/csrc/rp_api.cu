@@ -21,7 +21,8 @@ cudaError_t launch_rescale(const double *src, double *dst, int64_t n, const doub
 cudaError_t launch_count(const DevState &s, const GridDev &g, int early, unsigned long long *out, int *flag,
                          cudaStream_t st);
 cudaError_t launch_sweep(const SweepArgs &a, bool list, int nwarps, cudaStream_t st);
-size_t sweep_smem_per_warp(int kind, int cap, bool learn = false);
+size_t sweep_smem_per_warp(int kind, int cap, bool learn = false, int ncen = 0);
+cudaError_t launch_abs_centres(const DevState &s, cudaStream_t st);
 cudaError_t launch_mlp_grad(const float *feats, const uint8_t *labels, int64_t total, int64_t i0, int n,
                             int64_t mul, int64_t off, const float *w32, float *grad, float *loss, int num_sms,
                             cudaStream_t st);
@@ -46,6 +47,7 @@ struct GridHost {
     int64_t bounds_alloc = 0;
     int cap = 0;
     double cellmat64[9]{};
+    std::vector<float> cthr;  // host copy of the FP32 centre-pair thresholds (polyspheres)
 };
 
 struct Handle {
@@ -107,6 +109,15 @@ struct Handle {
     double kernel_ms[RP_NUM_KERNELS]{};
     uint64_t kernel_groups[RP_NUM_KERNELS]{};
     bool strict_box = false;
+    // polyspheres: body-frame centres and radii, the reference's centre range (its
+    // neighbour-grid cell), rotated and absolute centres, exact pair thresholds
+    int ncen = 0;
+    double cbody[3 * MAX_CEN]{}, crad[MAX_CEN]{};
+    double cthr_host[MAX_CEN * MAX_CEN]{};
+    double ref_range = 0;
+    double *cen64 = nullptr;
+    double *abs64[2] = {nullptr, nullptr};
+    double *cthr64 = nullptr;
     // learned ordering: network parameters (FP32 master + BF16 copy), Adam moments, scratch
     float *mlp_w32 = nullptr, *mlp_grad = nullptr, *mlp_m = nullptr, *mlp_v = nullptr, *mlp_loss = nullptr;
     __nv_bfloat16 *mlp_w16 = nullptr;
@@ -223,6 +234,33 @@ void translation_table(const double *box, double *out) {
             }
 }
 
+double cell_lrow(const GridHost &g) {
+    double lrow = 0;
+    for (int i = 0; i < 3; i++) {
+        double r = 0;
+        for (int j = 0; j < 3; j++) r += std::fabs(g.cellmat64[3 * i + j]);
+        lrow = std::max(lrow, r);
+    }
+    return lrow;
+}
+
+// Margin of an FP32 polysphere distance^2 at threshold thr = d^2: the centre separation
+// ((q - p) + c_j) - c_a carries the position error of the sphere filter (32 u32 (L + 1)
+// per component, L the largest cell-local coordinate) plus the FP32 centres' error (the
+// rounding of c, the FP32 rotation of the mover's centres: 8 u32 |c|) and the roundings of
+// the two extra sums (2 u32 (2 L + 2 |c|)); 32 u32 (|c|max + L + 1) covers the latter.
+double poly_margin(const Handle *h, const GridHost &g, double thr) {
+    const double u32 = std::ldexp(1.0, -24);
+    double cmax = 0;
+    for (int b = 0; b < h->ncen; b++)
+        cmax = std::max(cmax, std::sqrt(h->cbody[3 * b] * h->cbody[3 * b] + h->cbody[3 * b + 1] * h->cbody[3 * b + 1] +
+                                        h->cbody[3 * b + 2] * h->cbody[3 * b + 2]));
+    const double L = cell_lrow(g);
+    const double e = 32.0 * u32 * (L + 1.0) + 32.0 * u32 * (cmax + L + 1.0);
+    const double d = std::sqrt(thr);
+    return 2.0 * (2.0 * d * std::sqrt(3.0) * e + 3.0 * e * e + 4.0 * u32 * thr);
+}
+
 DevState dev_state(Handle *h) {
     DevState s{};
     s.n = h->n;
@@ -237,6 +275,10 @@ DevState dev_state(Handle *h) {
     s.status = h->status;
     s.counters = h->counters;
     s.strict_box = h->strict_box ? 1 : 0;
+    s.ncen = h->ncen;
+    s.cen64 = h->cen64;
+    s.abs64 = h->abs64[h->pcur];
+    s.cthr64 = h->cthr64;
     // ---- FP32 filter margins for the current grid ----
     const GridHost &g = h->grid[h->gcur];
     double lrow = 0;
@@ -266,6 +308,12 @@ DevState dev_state(Handle *h) {
         double thr = std::pow(2 * r, 2);
         fc.sphere_lo = static_cast<float>(thr - margin(thr));
         fc.sphere_hi = static_cast<float>(thr + margin(thr));
+    } else if (h->shape.kind == RP_SHAPE_POLYSPHERE) {
+        // bodies whose centres are farther apart than twice the largest centre reach
+        // (|c| + r) cannot touch; the centre-pair thresholds live in the grid (setup_grid)
+        double far = h->range * h->range;
+        fc.far_lo = static_cast<float>(far - poly_margin(h, g, far));
+        fc.far_hi = static_cast<float>(far + poly_margin(h, g, far));
     } else {
         double core = 4 * r * r, far = std::pow(2 * r + l, 2);
         fc.core_lo = static_cast<float>(core - margin(core));
@@ -339,7 +387,7 @@ int setup_grid(Handle *h, GridHost &G, const double *box, const double *shift) {
     // and then tests pairs through full periodic boundary conditions, an arithmetic this
     // engine does not reproduce.
     {
-        double ref_cell = h->range;
+        double ref_cell = h->ref_range;
         double min_cell = std::cbrt(volume_of(box) / static_cast<double>(h->n)) / 5;
         if (h->range < min_cell) ref_cell = min_cell;
         double mx = std::max({hgt[0], hgt[1], hgt[2]}), mn = std::min({hgt[0], hgt[1], hgt[2]});
@@ -383,6 +431,23 @@ int setup_grid(Handle *h, GridHost &G, const double *box, const double *shift) {
         RP_CUDA(h, cudaMalloc(&g.maxis, sizeof(float4) * n));
         RP_CUDA(h, cudaMalloc(&g.plocal, sizeof(float4) * n));
         RP_CUDA(h, cudaMalloc(&g.max_occ, sizeof(int32_t)));
+        if (h->ncen > 0) {
+            RP_CUDA(h, cudaMalloc(&g.mcen, sizeof(float4) * n * h->ncen));
+            RP_CUDA(h, cudaMalloc(&g.cthr, sizeof(float) * 2 * MAX_CEN * MAX_CEN));
+        }
+    }
+    if (h->ncen > 0) {
+        // FP32 centre-pair thresholds of this grid: (r_a + r_b)^2 -/+ margin
+        std::vector<float> &t = G.cthr;
+        t.assign(2 * MAX_CEN * MAX_CEN, 0.0f);
+        for (int a = 0; a < h->ncen; a++)
+            for (int b = 0; b < h->ncen; b++) {
+                double thr = h->cthr_host[a * MAX_CEN + b];
+                double m = poly_margin(h, G, thr);
+                t[a * MAX_CEN + b] = static_cast<float>(thr - m);
+                t[MAX_CEN * MAX_CEN + a * MAX_CEN + b] = static_cast<float>(thr + m);
+            }
+        RP_CUDA(h, cudaMemcpyAsync(g.cthr, t.data(), sizeof(float) * t.size(), cudaMemcpyHostToDevice, h->stream));
     }
     // ActiveDomain bounds per cell and dimension
     int64_t nb = 2ll * (dims[0] + dims[1] + dims[2]);
@@ -412,7 +477,7 @@ int setup_grid(Handle *h, GridHost &G, const double *box, const double *shift) {
     double mean = 27.0 * static_cast<double>(h->n) / static_cast<double>(ncell);
     int cap = static_cast<int>(mean + 6.0 * std::sqrt(mean) + 32.0);
     cap = (cap + 31) / 32 * 32;
-    int maxcap = static_cast<int>(48 * 1024 / (sweep_smem_per_warp(h->shape.kind, 32) / 32));
+    int maxcap = static_cast<int>(48 * 1024 / (sweep_smem_per_warp(h->shape.kind, 32, false, h->ncen) / 32));
     G.cap = std::min(cap, maxcap / 32 * 32);
     int64_t nblocks = (ncell + 4095) / 4096;
     RP_CUDA(h, ensure(h->block_sums, h->block_sums_alloc, nblocks));
@@ -466,7 +531,7 @@ SweepArgs base_args(Handle *h) {
 // Re-runs the cells of a phase whose neighbourhood did not fit the normal staging
 // capacity, with one large-capacity warp per block (device-side work count).
 int run_overflow(Handle *h, SweepArgs a, bool list) {
-    int cap = static_cast<int>(OVF_SMEM / sweep_smem_per_warp(a.s.kind, 8) * 8);
+    int cap = static_cast<int>(OVF_SMEM / sweep_smem_per_warp(a.s.kind, 32, false, a.s.ncen) * 32);
     cap = cap / 32 * 32;
     a.cap = cap;
     a.work = h->overflow;
@@ -553,30 +618,10 @@ using namespace rp;
 
 extern "C" {
 
-int rp_create(const rp_shape_desc *shape, int64_t n, int device, void **handle) {
-    if (!shape || !handle || n <= 0 || n > (1ll << 31) - 1) return RP_ERR_ARG;
-    if (shape->kind != RP_SHAPE_SPHERE && shape->kind != RP_SHAPE_SPHEROCYLINDER) return RP_ERR_UNSUPPORTED;
-    if (!(shape->radius > 0) || (shape->kind == RP_SHAPE_SPHEROCYLINDER && !(shape->length >= 0))) return RP_ERR_ARG;
-    Handle *h = new (std::nothrow) Handle();
-    if (!h) return RP_ERR_ARG;
+// Device allocations and the stream of a new handle whose shape fields are set.
+static int create_common(Handle *h, int64_t n, int device, void **handle) {
     h->device = device;
-    h->shape = *shape;
     h->n = n;
-    double r = shape->radius, l = shape->length;
-    ExactShape ex{};
-    ex.kind = shape->kind;
-    if (shape->kind == RP_SHAPE_SPHERE) {
-        h->range = 2 * r;                      // SphereTraits.h:34
-        ex.sphere_thr = std::pow(2 * r, 2);     // SphereTraits.cpp:64
-    } else {
-        h->range = 2 * r + l;                  // SpherocylinderTraits.h:81
-        ex.core_thr = 4 * r * r;                // SpherocylinderTraits.cpp:35
-        ex.far_thr = std::pow(2 * r + l, 2);    // SpherocylinderTraits.cpp:37
-        short beg = -1, end = 1;                // SpherocylinderTraits.cpp:23-25
-        ex.neg_cap_half = 0.5 * beg * l;
-        ex.cap_half = 0.5 * end * l;
-    }
-    h->ex = ex;
     auto bail = [&](cudaError_t e) {
         h->err = cudaGetErrorString(e);
         rp_destroy(h);
@@ -589,6 +634,14 @@ int rp_create(const rp_shape_desc *shape, int64_t n, int device, void **handle) 
     for (int i = 0; i < 2; i++) {
         if ((e = cudaMalloc(&h->pos64[i], sizeof(double) * 3 * n)) != cudaSuccess) return bail(e);
         if ((e = cudaMalloc(&h->trans[i], sizeof(double) * 3 * 125)) != cudaSuccess) return bail(e);
+        if (h->ncen > 0 && (e = cudaMalloc(&h->abs64[i], sizeof(double) * 3 * n * h->ncen)) != cudaSuccess)
+            return bail(e);
+    }
+    if (h->ncen > 0) {
+        if ((e = cudaMalloc(&h->cen64, sizeof(double) * 3 * n * h->ncen)) != cudaSuccess) return bail(e);
+        if ((e = cudaMalloc(&h->cthr64, sizeof(double) * MAX_CEN * MAX_CEN)) != cudaSuccess) return bail(e);
+        if ((e = cudaMemcpy(h->cthr64, h->cthr_host, sizeof(h->cthr_host), cudaMemcpyHostToDevice)) != cudaSuccess)
+            return bail(e);
     }
     if ((e = cudaMalloc(&h->rot64, sizeof(double) * 9 * n)) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc(&h->rtab64, sizeof(double) * 9 * ROT_TABLE)) != cudaSuccess) return bail(e);
@@ -605,6 +658,67 @@ int rp_create(const rp_shape_desc *shape, int64_t n, int device, void **handle) 
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return bail(e);
     *handle = h;
     return RP_OK;
+}
+
+int rp_create(const rp_shape_desc *shape, int64_t n, int device, void **handle) {
+    if (!shape || !handle || n <= 0 || n > (1ll << 31) - 1) return RP_ERR_ARG;
+    if (shape->kind != RP_SHAPE_SPHERE && shape->kind != RP_SHAPE_SPHEROCYLINDER) return RP_ERR_UNSUPPORTED;
+    if (!(shape->radius > 0) || (shape->kind == RP_SHAPE_SPHEROCYLINDER && !(shape->length >= 0))) return RP_ERR_ARG;
+    Handle *h = new (std::nothrow) Handle();
+    if (!h) return RP_ERR_ARG;
+    h->shape = *shape;
+    double r = shape->radius, l = shape->length;
+    ExactShape ex{};
+    ex.kind = shape->kind;
+    if (shape->kind == RP_SHAPE_SPHERE) {
+        h->range = 2 * r;                      // SphereTraits.h:34
+        ex.sphere_thr = std::pow(2 * r, 2);     // SphereTraits.cpp:64
+    } else {
+        h->range = 2 * r + l;                  // SpherocylinderTraits.h:81
+        ex.core_thr = 4 * r * r;                // SpherocylinderTraits.cpp:35
+        ex.far_thr = std::pow(2 * r + l, 2);    // SpherocylinderTraits.cpp:37
+        short beg = -1, end = 1;                // SpherocylinderTraits.cpp:23-25
+        ex.neg_cap_half = 0.5 * beg * l;
+        ex.cap_half = 0.5 * end * l;
+    }
+    h->ref_range = h->range;
+    h->ex = ex;
+    return create_common(h, n, device, handle);
+}
+
+int rp_create_polysphere(int32_t num_centres, const double *centres, const double *radii, int64_t n, int device,
+                         void **handle) {
+    if (!centres || !radii || !handle || n <= 0 || n > (1ll << 31) - 1) return RP_ERR_ARG;
+    if (num_centres < 1 || num_centres > MAX_CEN) return RP_ERR_UNSUPPORTED;
+    for (int b = 0; b < num_centres; b++) {
+        if (!(radii[b] > 0)) return RP_ERR_ARG;
+        for (int d = 0; d < 3; d++)
+            if (!std::isfinite(centres[3 * b + d])) return RP_ERR_ARG;
+    }
+    Handle *h = new (std::nothrow) Handle();
+    if (!h) return RP_ERR_ARG;
+    h->shape.kind = RP_SHAPE_POLYSPHERE;
+    h->ncen = num_centres;
+    double rmax = 0, reach = 0;
+    for (int b = 0; b < num_centres; b++) {
+        for (int d = 0; d < 3; d++) h->cbody[3 * b + d] = centres[3 * b + d];
+        h->crad[b] = radii[b];
+        rmax = std::max(rmax, radii[b]);
+        double c = std::sqrt(centres[3 * b] * centres[3 * b] + centres[3 * b + 1] * centres[3 * b + 1] +
+                             centres[3 * b + 2] * centres[3 * b + 2]);
+        reach = std::max(reach, c + radii[b]);
+    }
+    for (int a = 0; a < num_centres; a++)
+        for (int b = 0; b < num_centres; b++) {
+            double r = radii[a] + radii[b];      // PolysphereTraits.cpp:104-105
+            h->cthr_host[a * MAX_CEN + b] = r * r;
+        }
+    h->shape.radius = rmax;
+    h->ref_range = 2 * rmax;                   // PolysphereTraits.cpp:115-120 (the neighbour-grid cell)
+    // cells of the checkerboard: two bodies farther apart than twice the largest reach
+    // |c| + r cannot touch (rotated centres keep |c| up to FP64 rounding)
+    h->range = 2 * reach * (1.0 + 1e-12);
+    return create_common(h, n, device, handle);
 }
 
 int rp_destroy(void *handle) {
@@ -627,8 +741,14 @@ int rp_destroy(void *handle) {
         cudaFree(g.plocal);
         cudaFree(g.bounds);
         cudaFree(g.max_occ);
+        cudaFree(g.mcen);
+        cudaFree(g.cthr);
     }
     cudaFree(h->rot64);
+    cudaFree(h->cen64);
+    cudaFree(h->abs64[0]);
+    cudaFree(h->abs64[1]);
+    cudaFree(h->cthr64);
     cudaFree(h->rtab64);
     cudaFree(h->rtab32);
     cudaFree(h->item_counters);
@@ -678,6 +798,21 @@ int rp_upload_state(void *handle, const double *pos, const double *rot, const do
     h->partners_valid = false;
     RP_CUDA(h, cudaMemcpyAsync(h->pos64[0], pos, sizeof(double) * 3 * h->n, cudaMemcpyHostToDevice, h->stream));
     RP_CUDA(h, cudaMemcpyAsync(h->rot64, rot, sizeof(double) * 9 * h->n, cudaMemcpyHostToDevice, h->stream));
+    if (h->ncen > 0) {
+        // interactionCentres = orientation · centre (Packing::setupForInteraction,
+        // core/Packing.cpp:940-944); absolute centres on the device below
+        std::vector<double> cen(3 * h->n * h->ncen);
+        for (int64_t i = 0; i < h->n; i++)
+            for (int b = 0; b < h->ncen; b++) {
+                d3 c = mv3(rot + 9 * i, d3{h->cbody[3 * b], h->cbody[3 * b + 1], h->cbody[3 * b + 2]});
+                double *o = cen.data() + 3 * (i * h->ncen + b);
+                o[0] = c.x;
+                o[1] = c.y;
+                o[2] = c.z;
+            }
+        RP_CUDA(h, cudaStreamSynchronize(h->stream));
+        RP_CUDA(h, cudaMemcpy(h->cen64, cen.data(), sizeof(double) * cen.size(), cudaMemcpyHostToDevice));
+    }
     double tt[375];
     translation_table(h->box, tt);
     RP_CUDA(h, cudaMemcpyAsync(h->trans[0], tt, sizeof(tt), cudaMemcpyHostToDevice, h->stream));
@@ -691,6 +826,7 @@ int rp_upload_state(void *handle, const double *pos, const double *rot, const do
     if (rc) return rc;
     rc = check_status(h);  // the rebuild checks that every particle lies inside the box
     if (rc) return rc;
+    if (h->ncen > 0) RP_CUDA(h, launch_abs_centres(dev_state(h), h->stream));
     h->has_state = true;
     h->can_revert = false;
     h->log_valid = false;
@@ -1079,6 +1215,12 @@ int rp_try_scaling(void *handle, const double *new_box9, double *dE) {
     double shift[3] = {h->grid[old_g].d.shift[0], h->grid[old_g].d.shift[1], h->grid[old_g].d.shift[2]};
     int rc = setup_grid(h, h->grid[ng], h->box, shift);
     if (rc == RP_OK) rc = rebuild(h, ng, np);
+    if (rc == RP_OK && h->ncen > 0) {
+        // Packing::tryScaling recalculates the absolute centres (core/Packing.cpp:186-187)
+        Group grp(h, RP_KERNEL_RESCALE, 1);
+        cudaError_t e = launch_abs_centres(dev_state(h), h->stream);
+        if (e != cudaSuccess) rc = fail(h, RP_ERR_CUDA, cudaGetErrorString(e));
+    }
     if (rc) {
         std::memcpy(h->box, h->saved_box, sizeof(h->box));
         std::memcpy(h->inv, h->saved_inv, sizeof(h->inv));
@@ -1088,8 +1230,9 @@ int rp_try_scaling(void *handle, const double *new_box9, double *dE) {
     }
     h->can_revert = true;
     h->log_valid = false;
-    // A convex shape in a box that only grew cannot overlap (core/Packing.cpp:199-200).
-    if (box_upscaled(h->saved_box, h->box)) {
+    // A convex shape in a box that only grew cannot overlap (core/Packing.cpp:199-200);
+    // polyspheres are not convex (PolysphereTraits.h:133).
+    if (h->shape.kind != RP_SHAPE_POLYSPHERE && box_upscaled(h->saved_box, h->box)) {
         *dE = 0;
         RP_CUDA(h, cudaStreamSynchronize(h->stream));
         return RP_OK;
@@ -1365,6 +1508,8 @@ int rp_mlp_train(void *handle, int32_t epochs, int32_t batch, float lr, uint64_t
 int rp_set_ordering(void *handle, int32_t mode, int32_t every) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h || mode < RP_ORDER_OFF || mode > RP_ORDER_DISTANCE || every <= 0) return fail(h, RP_ERR_ARG, "bad argument");
+    if (mode != RP_ORDER_OFF && h->shape.kind == RP_SHAPE_POLYSPHERE)
+        return fail(h, RP_ERR_UNSUPPORTED, "test ordering is built for spheres and spherocylinders");
     h->order_mode = mode;
     h->order_every = every;
     h->partners_valid = false;

@@ -59,6 +59,9 @@ struct GridDev {
     double *bounds;       // ActiveDomain bounds: dim d at boundsoff[d], 2 doubles per cell
     int boundsoff[3];
     int32_t *max_occ;     // device scalar
+    // polyspheres
+    float4 *mcen;         // [n][ncen] FP32 rotated centre offsets, cell order
+    float *cthr;          // [2][MAX_CEN^2] FP32 centre-pair thresholds (r_a + r_b)^2 -/+ margin
 };
 
 struct DevState {
@@ -74,7 +77,19 @@ struct DevState {
     uint32_t *status;
     unsigned long long *counters;  // rp_sweep_stats layout
     int strict_box;                // rebuild: flag positions outside [0, 1) relative (uploads)
+    // polyspheres (kind 2): the reference's interactionCentres (orientation-rotated body
+    // offsets, rotated incrementally by accepted moves) and absoluteInteractionCentres
+    int ncen;
+    double *cen64;                 // [n][ncen][3]
+    double *abs64;                 // [n][ncen][3] (position + centre, wrapped into the box)
+    const double *cthr64;          // [MAX_CEN^2] (r_a + r_b)^2, FP64 as the reference forms it
 };
+
+constexpr int MAX_CEN = RP_MAX_CENTRES;
+// per-warp polysphere scratch of the sweep (float4 units): the mover's FP32 centres
+// [MAX_CEN], the centre-pair thresholds [2 MAX_CEN^2 floats], the mover's exact centres
+// and absolute centres [2 x 3 MAX_CEN doubles]
+constexpr int SWEEP_POLY_SCRATCH = MAX_CEN + MAX_CEN * MAX_CEN / 2 + 3 * MAX_CEN;
 
 constexpr int SWEEP_WARPS = 4;       // warps per block of the sweep kernel
 constexpr int SWEEP_MIN_BLOCKS = 4;  // resident blocks per SM the register budget allows

@@ -40,6 +40,10 @@ __device__ __forceinline__ int d2_stage(const FilterConsts &fc, float d2) {
         if (d2 < fc.sphere_lo) return 1;
         if (d2 > fc.sphere_hi) return 0;
         return 2;
+    } else if (KIND == 2) {
+        // polyspheres: bodies farther apart than twice the largest centre reach cannot
+        // touch; closer ones go to the sphere-pair stage
+        return d2 > fc.far_hi ? 0 : 3;
     } else {
         if (d2 > fc.far_hi) return 0;
         if (d2 < fc.core_lo) return 1;
@@ -260,7 +264,28 @@ __global__ void k_cell_finish(DevState s, GridDev g) {
         g.mpos[k] = make_float4(l.x, l.y, l.z, __int_as_float(pid));
         const double *r = s.rot64 + 9 * (size_t)pid;
         g.maxis[k] = make_float4(static_cast<float>(r[2]), static_cast<float>(r[5]), static_cast<float>(r[8]), 0.f);
+        for (int b = 0; b < s.ncen; b++) {
+            const double *c = s.cen64 + 3 * ((size_t)pid * s.ncen + b);
+            g.mcen[(size_t)k * s.ncen + b] =
+                make_float4(static_cast<float>(c[0]), static_cast<float>(c[1]), static_cast<float>(c[2]), 0.f);
+        }
     }
+}
+
+// Absolute centres of every polysphere (Packing::recalculateAbsoluteInteractionCentres,
+// core/Packing.cpp:1041-1047): position + rotated centre, then the PBC correction of
+// that point (core/PeriodicBoundaryConditions.cpp:11-22).  One thread per centre.
+__global__ void k_abs_centres(DevState s) {
+    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= s.n * s.ncen) return;
+    const int64_t pid = t / s.ncen;
+    d3 p = load_d3(s.pos64 + 3 * pid);
+    d3 c = load_d3(s.cen64 + 3 * t);
+    d3 q = add3(p, c);
+    d3 a = add3(q, pbc_correction(s.box, s.inv, q, nullptr));
+    s.abs64[3 * t] = a.x;
+    s.abs64[3 * t + 1] = a.y;
+    s.abs64[3 * t + 2] = a.z;
 }
 
 // ---------------------------------------------------------------------------------
@@ -376,6 +401,70 @@ __global__ void k_count(DevState s, GridDev g, int early, unsigned long long *ou
 template __global__ void k_count<0>(DevState, GridDev, int, unsigned long long *, int *);
 template __global__ void k_count<1>(DevState, GridDev, int, unsigned long long *, int *);
 
+// Exact FP64 test of centre a of a body, at absolute position pa, against centre j of
+// body pid_j seen at FP32 separation dsep (candidate minus mover): the reference's
+// (pos2 + t - pos1).norm2() < (r_a + r_j)^2 (core/Packing.cpp:40-42,
+// core/shapes/PolysphereTraits.cpp:97-106) with t the box translation of that image.
+__device__ __forceinline__ bool exact_centre_pair(const DevState &s, d3 pa, int a, int pid_j, int j, float3 dsep) {
+    d3 pb = load_d3(s.abs64 + 3 * ((size_t)pid_j * s.ncen + j));
+    int m = image_index(s, dsep, pa, pb);
+    d3 t = load_d3(s.trans + 3 * m);
+    d3 d = sub3(add3(pb, t), pa);
+    return norm2(d) < s.cthr64[a * MAX_CEN + j];
+}
+
+// All-pairs recount of polyspheres: one thread per body; every unordered body pair and
+// periodic image once, every pair of their centres (the count of overlapping centre pairs,
+// as the reference's countTotalOverlaps counts them, core/Packing.cpp:468-512).
+__global__ void k_count_poly(DevState s, GridDev g, int early, unsigned long long *out, int *flag) {
+    int64_t slot = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (slot >= s.n) return;
+    const int K = s.ncen;
+    float4 pi4 = g.mpos[slot];
+    int pid = __float_as_int(pi4.w);
+    int cell = g.pid_cell[pid];
+    int cx = cell % g.dims[0], cy = (cell / g.dims[0]) % g.dims[1], cz = cell / (g.dims[0] * g.dims[1]);
+    unsigned long long cnt = 0;
+    for (int o = 0; o < 27; o++) {
+        if (early && *(volatile int *)flag) break;
+        int ox = o % 3 - 1, oy = (o / 3) % 3 - 1, oz = o / 9 - 1;
+        int nb = wrap_cell(cx + ox, g.dims[0]) +
+                 g.dims[0] * (wrap_cell(cy + oy, g.dims[1]) + g.dims[1] * wrap_cell(cz + oz, g.dims[2]));
+        float3 off = mat32(g.cellmat, (float)ox, (float)oy, (float)oz);
+        int b = g.start[nb], e = g.start[nb + 1];
+        for (int k = b; k < e; k++) {
+            float4 q = g.mpos[k];
+            int pj = __float_as_int(q.w);
+            if (pj <= pid) continue;
+            float3 dq = make_float3((q.x + off.x) - pi4.x, (q.y + off.y) - pi4.y, (q.z + off.z) - pi4.z);
+            if (dot3f(dq, dq) > s.fc.far_hi) continue;
+            for (int j = 0; j < K; j++) {
+                float4 cj = g.mcen[(size_t)k * K + j];
+                float3 bj = make_float3(dq.x + cj.x, dq.y + cj.y, dq.z + cj.z);
+                for (int a = 0; a < K; a++) {
+                    float4 ca = g.mcen[(size_t)slot * K + a];
+                    float3 d = make_float3(bj.x - ca.x, bj.y - ca.y, bj.z - ca.z);
+                    float d2 = dot3f(d, d);
+                    bool ov = d2 < g.cthr[a * MAX_CEN + j];
+                    if (!ov && d2 <= g.cthr[MAX_CEN * MAX_CEN + a * MAX_CEN + j]) {
+                        atomicAdd(s.counters + 5, 1ull);
+                        ov = exact_centre_pair(s, load_d3(s.abs64 + 3 * ((size_t)pid * K + a)), a, pj, j, d);
+                    }
+                    if (ov) {
+                        cnt++;
+                        if (early) {
+                            atomicExch(flag, 1);
+                            atomicAdd(out, cnt);
+                            return;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    if (cnt) atomicAdd(out, cnt);
+}
+
 // ---------------------------------------------------------------------------------
 // Checkerboard sweep: one warp per active cell.
 //
@@ -394,7 +483,7 @@ struct WarpStats {
 template <int KIND, bool LIST, bool LEARN>
 __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, float4 *cpos, float4 *cax,
                                            uint16_t *qseg, uint16_t *qun, uint8_t *nacc, uint16_t *pstage,
-                                           WarpStats &ws) {
+                                           float *ccen, float4 *wx, WarpStats &ws) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -461,8 +550,24 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
             p.z += off.z;
             cpos[base + k] = p;
             if (KIND == 1) cax[base + k] = G.maxis[st + k];
+            if (KIND == 2) {
+                for (int b = 0; b < S.ncen; b++) {
+                    float4 c = G.mcen[(size_t)(st + k) * S.ncen + b];
+                    float *dst = ccen + 3 * ((size_t)(base + k) * S.ncen + b);
+                    dst[0] = c.x;
+                    dst[1] = c.y;
+                    dst[2] = c.z;
+                }
+            }
         }
     }
+    // polyspheres: the warp's scratch holds the mover's FP32 centres (wx[0..K)), the
+    // centre-pair thresholds (lo, hi) and the mover's exact new centres and absolute centres
+    float *wthr = reinterpret_cast<float *>(wx + MAX_CEN);
+    double *wabs = reinterpret_cast<double *>(wx + MAX_CEN + MAX_CEN * MAX_CEN / 2);
+    double *wcen = wabs + 3 * MAX_CEN;
+    if (KIND == 2)
+        for (int t = lane; t < 2 * MAX_CEN * MAX_CEN; t += 32) wthr[t] = G.cthr[t];
     const bool self_images = (G.dims[0] == 1) || (G.dims[1] == 1) || (G.dims[2] == 1);
     // per own-cell particle: FP32 roundings accumulated in its mirror position this sweep
     for (int k = lane; k < occ; k += 32) nacc[k] = 0;
@@ -570,7 +675,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
                 // a rotation of this sweep's table, or its transpose (the inverse)
                 rot_idx = r.b & A.rtab_mask;
                 rot_inv = (r.c & 1u) != 0;
-                if (KIND == 1) {
+                if (KIND >= 1) {
                     const float4 *R4 = reinterpret_cast<const float4 *>(A.rtab32) + 3 * (size_t)rot_idx;
                     float4 x0 = R4[0], x1 = R4[1], x2 = R4[2];
                     float R[9] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w, x2.x};
@@ -593,6 +698,16 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
         float3 an = ai;
         if (type != 1) pn = make_float3(pcur.x + t32.x, pcur.y + t32.y, pcur.z + t32.z);
         if (type != 0 && KIND == 1) an = mat32(R32, ai.x, ai.y, ai.z);
+        if (KIND == 2) {
+            // the mover's FP32 centres after the move (rotated by the FP32 rotation)
+            if (lane < S.ncen) {
+                const float *c = ccen + 3 * ((size_t)slot * S.ncen + lane);
+                float3 cn = make_float3(c[0], c[1], c[2]);
+                if (type != 0) cn = mat32(R32, cn.x, cn.y, cn.z);
+                wx[lane] = make_float4(cn.x, cn.y, cn.z, 0.f);
+            }
+            __syncwarp();
+        }
 
         // ---- FP32 ActiveDomain test (translations): 0 inside, 1 outside, 2 undecided;
         //      and whether the PBC correction may move the particle through the box ----
@@ -662,7 +777,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
                     overlap = true;
                     break;
                 }
-                if (KIND == 1) {
+                if (KIND >= 1) {
                     unsigned b0 = __ballot_sync(FULL, c0 == 3), b1 = __ballot_sync(FULL, c1 == 3);
                     if (c0 == 3) qseg[nseg + __popc(b0 & lt)] = (uint16_t)k0;
                     nseg += __popc(b0);
@@ -677,6 +792,41 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
             }
         }
         __syncwarp();
+        // ---- FP32 pass 2 (polyspheres): every centre pair of a near body, one body per lane ----
+        if (KIND == 2 && !overlap) {
+            const int K = S.ncen;
+            for (int base = 0; base < nseg; base += 32) {
+                const int i = base + lane;
+                int cls = 0, k = 0;
+                if (i < nseg) {
+                    k = qseg[i];
+                    const float4 q = cpos[k];
+                    const float3 dq = make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z);
+                    const float *cj = ccen + 3 * (size_t)k * K;
+                    for (int j = 0; j < K && cls != 1; j++) {
+                        const float3 bj = make_float3(dq.x + cj[3 * j], dq.y + cj[3 * j + 1], dq.z + cj[3 * j + 2]);
+                        for (int a = 0; a < K; a++) {
+                            const float4 m = wx[a];
+                            const float3 d = make_float3(bj.x - m.x, bj.y - m.y, bj.z - m.z);
+                            const float d2 = dot3f(d, d);
+                            if (d2 < wthr[a * MAX_CEN + j]) {
+                                cls = 1;
+                                break;
+                            }
+                            if (d2 <= wthr[MAX_CEN * MAX_CEN + a * MAX_CEN + j]) cls = 2;
+                        }
+                    }
+                }
+                if (__ballot_sync(FULL, cls == 1)) {
+                    overlap = true;
+                    break;
+                }
+                unsigned b2 = __ballot_sync(FULL, cls == 2);
+                if (cls == 2) qun[nun + __popc(b2 & lt)] = (uint16_t)k;
+                nun += __popc(b2);
+            }
+            __syncwarp();
+        }
         // ---- FP32 pass 2 (spherocylinders): segment distances on full warps ----
         if (KIND == 1 && !overlap) {
             for (int base = 0; base < nseg; base += 32) {
@@ -822,8 +972,61 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
             } else {
                 anew = d3{__shfl_sync(FULL, rot_own, 2), __shfl_sync(FULL, rot_own, 5), __shfl_sync(FULL, rot_own, 8)};
             }
+            if (KIND == 2) {
+                // the mover's centres: rotated by R (Packing::rotateTempInteractionCentres,
+                // core/Packing.cpp:357-361), then position + centre wrapped into the box
+                // (core/Packing.cpp:1041-1047); one centre per lane
+                double R[9];
+                for (int d = 0; d < 3; d++) {
+                    R[3 * d] = __shfl_sync(FULL, rrow[0], 3 * d);
+                    R[3 * d + 1] = __shfl_sync(FULL, rrow[1], 3 * d);
+                    R[3 * d + 2] = __shfl_sync(FULL, rrow[2], 3 * d);
+                }
+                if (lane < S.ncen) {
+                    d3 c = load_d3(S.cen64 + 3 * ((size_t)pid * S.ncen + lane));
+                    if (type != 0) c = mv3(R, c);
+                    d3 q = add3(pnew, c);
+                    d3 a = add3(q, pbc_correction(S.box, S.inv, q, nullptr));
+                    wcen[3 * lane] = c.x;
+                    wcen[3 * lane + 1] = c.y;
+                    wcen[3 * lane + 2] = c.z;
+                    wabs[3 * lane] = a.x;
+                    wabs[3 * lane + 1] = a.y;
+                    wabs[3 * lane + 2] = a.z;
+                }
+                __syncwarp();
+            }
             // the guard band: queued pairs re-decided in FP64
-            if (code == 0 && nun > 0) {
+            if (KIND == 2 && code == 0 && nun > 0) {
+                // every centre pair of each queued body, one pair per lane
+                const int K = S.ncen;
+                bool ov = false;
+                for (int qi = 0; qi < nun && !ov; qi++) {
+                    const int k = qun[qi];
+                    const float4 q = cpos[k];
+                    const float3 dq = make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z);
+                    const float *cj = ccen + 3 * (size_t)k * K;
+                    for (int tb = 0; tb < K * K; tb += 32) {
+                        const int t = tb + lane;
+                        bool hit = false;
+                        if (t < K * K) {
+                            const int a = t / K, j = t % K;
+                            const float4 m = wx[a];
+                            const float3 d = make_float3((dq.x + cj[3 * j]) - m.x, (dq.y + cj[3 * j + 1]) - m.y,
+                                                         (dq.z + cj[3 * j + 2]) - m.z);
+                            hit = exact_centre_pair(S, d3{wabs[3 * a], wabs[3 * a + 1], wabs[3 * a + 2]}, a,
+                                                    __float_as_int(q.w), j, d);
+                        }
+                        if (__ballot_sync(FULL, hit)) {
+                            ov = true;
+                            break;
+                        }
+                    }
+                }
+                ws.fp64 += nun;
+                if (ov) code = 1;
+            }
+            if (KIND != 2 && code == 0 && nun > 0) {
                 bool ov = false;
                 for (int qb = 0; qb < nun; qb += 32) {
                     int qi = qb + lane;
@@ -887,6 +1090,21 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
                     G.maxis[gslot] = na;
                 }
             }
+            if (KIND == 2 && lane < S.ncen) {
+                // Packing::acceptTempInteractionCentres (core/Packing.cpp:339-348)
+                const size_t ci = (size_t)pid * S.ncen + lane;
+                for (int d = 0; d < 3; d++) S.abs64[3 * ci + d] = wabs[3 * lane + d];
+                if (type != 0) {
+                    for (int d = 0; d < 3; d++) S.cen64[3 * ci + d] = wcen[3 * lane + d];
+                    const float4 c32 = make_float4((float)wcen[3 * lane], (float)wcen[3 * lane + 1],
+                                                   (float)wcen[3 * lane + 2], 0.f);
+                    G.mcen[gslot * S.ncen + lane] = c32;
+                    float *dst = ccen + 3 * ((size_t)slot * S.ncen + lane);
+                    dst[0] = c32.x;
+                    dst[1] = c32.y;
+                    dst[2] = c32.z;
+                }
+            }
             if (self_images) {
                 // the own cell is staged several times (periodic images): refresh every copy
                 __syncwarp();
@@ -895,6 +1113,9 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, f
                     if (__float_as_int(q.w) == pid) {
                         cpos[k] = make_float4(np.x + (q.x - pcur.x), np.y + (q.y - pcur.y), np.z + (q.z - pcur.z), q.w);
                         if (KIND == 1 && type != 0) cax[k] = na;
+                        if (KIND == 2 && type != 0)
+                            for (int e = 0; e < 3 * S.ncen; e++)
+                                ccen[3 * (size_t)k * S.ncen + e] = ccen[3 * (size_t)slot * S.ncen + e];
                     }
                 }
             }
@@ -937,13 +1158,21 @@ __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(co
     const int wib = threadIdx.x >> 5;
     const int warps_per_block = blockDim.x >> 5;
     const int warp = blockIdx.x * warps_per_block + wib;
-    const int per_warp = A.cap * (KIND == 1 ? 2 : 1) + A.cap / 4 + A.cap / 16 + (LEARN ? A.cap / 4 : 0);  // float4
+    // per-warp shared memory (float4 units): staged positions [cap], spherocylinder axes
+    // [cap] or polysphere centres [cap x 3K floats], two uint16 queues and a byte counter
+    // per slot [5 cap bytes], partner slots [LEARN], polysphere scratch [SWEEP_POLY_SCRATCH]
+    const int K = KIND == 2 ? A.s.ncen : 0;
+    const int extra = KIND == 1 ? A.cap : (KIND == 2 ? A.cap * 3 * K / 4 : 0);
+    const int per_warp = A.cap + extra + A.cap / 4 + A.cap / 16 + (LEARN ? A.cap / 4 : 0) +
+                         (KIND == 2 ? SWEEP_POLY_SCRATCH : 0);
     float4 *cpos = smem + (size_t)wib * per_warp;
-    float4 *cax = cpos + A.cap;  // only for spherocylinders
-    uint16_t *qseg = reinterpret_cast<uint16_t *>(cpos + A.cap * (KIND == 1 ? 2 : 1));
+    float4 *cax = cpos + A.cap;                                  // spherocylinders
+    float *ccen = reinterpret_cast<float *>(cpos + A.cap);       // polyspheres
+    uint16_t *qseg = reinterpret_cast<uint16_t *>(cpos + A.cap + extra);
     uint16_t *qun = qseg + A.cap;
     uint8_t *nacc = reinterpret_cast<uint8_t *>(qun + A.cap);
     uint16_t *pstage = reinterpret_cast<uint16_t *>(nacc + A.cap);  // LEARN only: MLP_PARTNERS x cap
+    float4 *wx = reinterpret_cast<float4 *>(nacc + A.cap);          // polyspheres (never with LEARN)
     int nitems = A.work ? *A.work_count : (LIST ? A.num_list : A.num_active);
     WarpStats ws = {0, 0, 0, 0, 0, 0, 0, 0};
     // persistent launches (next_item set) take cells from a shared counter until none are
@@ -957,7 +1186,7 @@ __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(co
             item = __shfl_sync(FULL, it, 0);
         }
         if (item >= nitems) break;
-        sweep_cell<KIND, LIST, LEARN>(A, item, cpos, cax, qseg, qun, nacc, pstage, ws);
+        sweep_cell<KIND, LIST, LEARN>(A, item, cpos, cax, qseg, qun, nacc, pstage, ccen, wx, ws);
         __syncwarp();
         item += stride;
     }
@@ -1010,12 +1239,22 @@ cudaError_t launch_count(const DevState &s, const GridDev &g, int early, unsigne
                          cudaStream_t st) {
     unsigned nb = (unsigned)((s.n + 127) / 128);
     if (s.kind == 0) k_count<0><<<nb, 128, 0, st>>>(s, g, early, out, flag);
-    else k_count<1><<<nb, 128, 0, st>>>(s, g, early, out, flag);
+    else if (s.kind == 1) k_count<1><<<nb, 128, 0, st>>>(s, g, early, out, flag);
+    else k_count_poly<<<nb, 128, 0, st>>>(s, g, early, out, flag);
     return cudaGetLastError();
 }
 
-size_t sweep_smem_per_warp(int kind, int cap, bool learn) {
-    return (size_t)(cap * (kind == 1 ? 2 : 1) + cap / 4 + cap / 16 + (learn ? cap / 4 : 0)) * sizeof(float4);
+cudaError_t launch_abs_centres(const DevState &s, cudaStream_t st) {
+    int64_t t = s.n * s.ncen;
+    if (t == 0) return cudaSuccess;
+    k_abs_centres<<<(unsigned)((t + 255) / 256), 256, 0, st>>>(s);
+    return cudaGetLastError();
+}
+
+size_t sweep_smem_per_warp(int kind, int cap, bool learn, int ncen) {
+    const int extra = kind == 1 ? cap : (kind == 2 ? cap * 3 * ncen / 4 : 0);
+    return (size_t)(cap + extra + cap / 4 + cap / 16 + (learn ? cap / 4 : 0) + (kind == 2 ? SWEEP_POLY_SCRATCH : 0)) *
+           sizeof(float4);
 }
 
 cudaError_t launch_rot_table(double *out64, float *out32, uint32_t count, uint64_t seed, uint64_t counter, float step,
@@ -1036,14 +1275,18 @@ static cudaError_t launch_sweep_t(const SweepArgs &a, unsigned blocks, int threa
 cudaError_t launch_sweep(const SweepArgs &a, bool list, int nwarps, cudaStream_t st) {
     if (nwarps <= 0) return cudaSuccess;
     const int wpb = a.work ? 1 : SWEEP_WARPS;
-    const bool learn = !list && (a.partners != nullptr || a.pair_every > 0);
-    size_t smem = sweep_smem_per_warp(a.s.kind, a.cap, learn) * wpb;
+    const bool learn = !list && a.s.kind != 2 && (a.partners != nullptr || a.pair_every > 0);
+    size_t smem = sweep_smem_per_warp(a.s.kind, a.cap, learn, a.s.ncen) * wpb;
     unsigned blocks = (unsigned)((nwarps + wpb - 1) / wpb);
     const int th = wpb * 32;
     if (a.s.kind == 0) {
         if (list) return launch_sweep_t<0, true, false>(a, blocks, th, smem, st);
         return learn ? launch_sweep_t<0, false, true>(a, blocks, th, smem, st)
                      : launch_sweep_t<0, false, false>(a, blocks, th, smem, st);
+    }
+    if (a.s.kind == 2) {
+        if (list) return launch_sweep_t<2, true, false>(a, blocks, th, smem, st);
+        return launch_sweep_t<2, false, false>(a, blocks, th, smem, st);
     }
     if (list) return launch_sweep_t<1, true, false>(a, blocks, th, smem, st);
     return learn ? launch_sweep_t<1, false, true>(a, blocks, th, smem, st)

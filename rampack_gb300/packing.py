@@ -31,20 +31,30 @@ class GpuPacking:
         params = np.asarray(params, dtype=np.float64).reshape(-1)
         desc = ShapeDesc()
         desc.kind = kind
-        if kind == _lib.SHAPE_SPHERE:
-            desc.radius = float(params[0])
-        elif kind == _lib.SHAPE_SPHEROCYLINDER:
-            desc.length, desc.radius = float(params[0]), float(params[1])
-        else:
-            raise EngineError(-5, f"shape kind {kind} is not handled by the GPU engine")
-        self.kind = kind
-        self.params = params
         pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
         self.n = pos.shape[0]
+        self.kind = kind
+        self.params = params
         h = C.c_void_p()
-        rc = self.lib.rp_create(C.byref(desc), self.n, device, C.byref(h))
-        if rc != 0:
-            raise EngineError(rc, "rp_create failed")
+        if kind == _lib.SHAPE_POLYSPHERE:
+            # params as the oracle's: [k, (x, y, z, r) per centre]
+            k = int(params[0])
+            data = params[1:1 + 4 * k].reshape(k, 4)
+            centres = np.ascontiguousarray(data[:, :3])
+            radii = np.ascontiguousarray(data[:, 3])
+            rc = self.lib.rp_create_polysphere(k, dptr(centres), dptr(radii), self.n, device, C.byref(h))
+            if rc != 0:
+                raise EngineError(rc, "rp_create_polysphere failed")
+        else:
+            if kind == _lib.SHAPE_SPHERE:
+                desc.radius = float(params[0])
+            elif kind == _lib.SHAPE_SPHEROCYLINDER:
+                desc.length, desc.radius = float(params[0]), float(params[1])
+            else:
+                raise EngineError(-5, f"shape kind {kind} is not handled by the GPU engine")
+            rc = self.lib.rp_create(C.byref(desc), self.n, device, C.byref(h))
+            if rc != 0:
+                raise EngineError(rc, "rp_create failed")
         self.h = h
         self.upload(pos, rot, box)
 

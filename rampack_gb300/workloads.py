@@ -72,6 +72,70 @@ def spherocylinders(counts, phi: float, length: float, radius: float = 0.5, aspe
     return SPHEROCYLINDER, np.array([length, radius]), pos, aligned_rotations(n), box
 
 
+def banana_centres(arc_radius: float, arc_angle: float, n: int) -> np.ndarray:
+    """Body-frame sphere centres of a bent chain, PolysphereBananaTraits::generateGeometry
+    (core/shapes/PolysphereBananaTraits.cpp:46-82): n points on an arc of radius
+    arc_radius spanning arc_angle in the xz plane, the point at -(arc_radius, 0, 0)
+    rotated about y by -arc_angle/2 + i arc_angle/(n-1); for arc_angle < pi the chain is
+    shifted along x so that its first sphere sits at x = 0."""
+    if not (arc_radius > 0 and 0 < arc_angle < 2 * math.pi and n >= 2):
+        raise ValueError("bad banana geometry")
+    step = arc_angle / (n - 1)
+    angle = -arc_angle / 2
+    pts = []
+    for _ in range(n):
+        # Matrix<3,3>::rotation(0, angle, 0) applied to (-R, 0, 0)
+        c, s = math.cos(angle), math.sin(angle)
+        pts.append([c * -arc_radius, 0.0, -s * -arc_radius])
+        angle += step
+    pts = np.array(pts, dtype=np.float64)
+    if arc_angle < math.pi:
+        pts[:, 0] += -pts[0, 0]
+    return pts
+
+
+def banana_volume(centres: np.ndarray, radius: float, arc_angle: float) -> float:
+    """PolysphereBananaTraits::calculateVolume (core/shapes/PolysphereBananaTraits.cpp:95-117):
+    n spheres minus n-1 lenses of neighbouring spheres (plus the first-last lens past pi)."""
+    n = len(centres)
+
+    def lens(d):
+        return math.pi * (4 * radius + d) * (2 * radius - d) ** 2 / 12 if d < 2 * radius else 0.0
+
+    v = n * sphere_volume(radius) - (n - 1) * lens(float(np.linalg.norm(centres[0] - centres[1])))
+    if arc_angle > math.pi and n > 2:
+        v -= lens(float(np.linalg.norm(centres[0] - centres[-1])))
+    return v
+
+
+def polysphere_params(centres: np.ndarray, radii) -> np.ndarray:
+    """Shape parameters of a polysphere: [k, (x, y, z, r) per centre]."""
+    radii = np.broadcast_to(np.asarray(radii, dtype=np.float64), (len(centres),))
+    out = [float(len(centres))]
+    for c, r in zip(centres, radii):
+        out += [float(c[0]), float(c[1]), float(c[2]), float(r)]
+    return np.array(out, dtype=np.float64)
+
+
+def bananas(counts, phi: float, arc_radius: float, arc_angle: float, n_spheres: int, radius: float = 0.5):
+    """Aligned bent chains on an orthorhombic lattice whose cell is the chain's bounding
+    box (spheres included) scaled uniformly to packing fraction phi."""
+    centres = banana_centres(arc_radius, arc_angle, n_spheres)
+    lo, hi = centres.min(0) - radius, centres.max(0) + radius
+    ext = hi - lo
+    v = banana_volume(centres, radius, arc_angle)
+    s = (v / (phi * ext.prod())) ** (1.0 / 3.0)
+    if s < 1.0:
+        raise ValueError("packing fraction too high for an aligned lattice")
+    cell = ext * s
+    nx, ny, nz = counts
+    n = nx * ny * nz
+    pos = lattice(counts, cell) - (lo + hi) / 2  # bounding boxes centred in the lattice cells
+    box = diag_box(cell[0] * nx, cell[1] * ny, cell[2] * nz)
+    pos = np.mod(pos, np.array([cell[0] * nx, cell[1] * ny, cell[2] * nz]))
+    return POLYSPHERE, polysphere_params(centres, radius), np.ascontiguousarray(pos), aligned_rotations(n), box
+
+
 # The benchmark systems (sizes as quoted for the reference's hot path).
 def config_hs_1000():
     """Hard spheres d=1, N=1000 on a 10^3 simple-cubic lattice at phi=0.30."""
@@ -86,3 +150,10 @@ def config_sc_64000():
 def config_sc_1e6():
     """Spherocylinders l=2 r=0.5, N=1,000,000 (100^3), aligned, cell aspect 1:1:3, phi=0.50."""
     return spherocylinders((100, 100, 100), 0.50, 2.0, 0.5, aspect=(1.0, 1.0, 3.0))
+
+
+def config_banana_1e5():
+    """Bent 5-sphere chains (sphere radius 0.5, 30 degrees between successive bonds of
+    length 0.6: arc angle 120 degrees, arc radius 0.6 / (2 sin 15 degrees)),
+    N = 100,000 (50 x 80 x 25), aligned, phi = 0.45."""
+    return bananas((50, 80, 25), 0.45, 0.6 / (2 * math.sin(math.radians(15))), math.radians(120), 5)

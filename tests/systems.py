@@ -55,6 +55,22 @@ def sc_l5():
                       translation_step=0.2, rotation_step=0.2, box_kind=1, box_step=0.005, pressure=1.5)
 
 
+BANANA = dict(arc_radius=0.6 / (2 * np.sin(np.radians(15))), arc_angle=np.radians(120), n_spheres=5)
+
+
+@functools.lru_cache(maxsize=None)
+def poly_banana():
+    """Bent 5-sphere chains (r=0.5, arc 120 degrees), N=400, phi=0.35, triclinic after 10 NpT cycles."""
+    return thermalise(W.bananas((8, 10, 5), 0.35, **BANANA), 10, translation_step=0.2, rotation_step=0.2,
+                      box_kind=1, box_step=0.005, pressure=1.5)
+
+
+@functools.lru_cache(maxsize=None)
+def poly_dense():
+    """Bent 5-sphere chains, N=480, phi=0.45, 10 NVT cycles (dense, many rejections)."""
+    return thermalise(W.bananas((8, 10, 6), 0.45, **BANANA), 10, translation_step=0.2, rotation_step=0.2)
+
+
 def compressed(cfg, factor: float):
     """The same configuration with box and positions scaled by `factor` (overlaps for factor < 1)."""
     kind, prm, pos, rot, box = cfg
@@ -65,4 +81,5 @@ def compressed(cfg, factor: float):
     return kind, prm, np.ascontiguousarray(p), rot, nb.reshape(9)
 
 
-ALL = {"hs_small": hs_small, "hs_dense": hs_dense, "sc_l2": sc_l2, "sc_l2_dense": sc_l2_dense, "sc_l5": sc_l5}
+ALL = {"hs_small": hs_small, "hs_dense": hs_dense, "sc_l2": sc_l2, "sc_l2_dense": sc_l2_dense, "sc_l5": sc_l5,
+       "poly_banana": poly_banana, "poly_dense": poly_dense}

@@ -14,7 +14,7 @@ from rampack_gb300 import _lib
 
 pytestmark = pytest.mark.gpu
 
-CASES = ["hs_small", "hs_dense", "sc_l2", "sc_l2_dense", "sc_l5"]
+CASES = ["hs_small", "hs_dense", "sc_l2", "sc_l2_dense", "sc_l5", "poly_banana", "poly_dense"]
 
 
 def gpu_packing(cfg):
@@ -113,8 +113,9 @@ def test_sweep_log_replays_on_oracle(oracle, engine, name, fp64_only):
             assert g.count_total_overlaps(True) == 0
 
 
-def test_fp32_filter_matches_fp64_only(engine):
-    cfg = systems.sc_l2_dense()
+@pytest.mark.parametrize("name", ["sc_l2_dense", "poly_dense"])
+def test_fp32_filter_matches_fp64_only(engine, name):
+    cfg = systems.ALL[name]()
     t, r = steps(cfg)
     states = []
     for fp64_only in (False, True):

@@ -60,3 +60,18 @@ def test_reduce_max_two_gloo_ranks():
         p.join(timeout=120)
         assert p.exitcode == 0
     assert sorted(res) == [(0, 20.0), (1, 20.0)]
+
+
+def test_banana_centres_match_the_reference(oracle):
+    # the workload builder restates PolysphereBananaTraits::generateGeometry; pinned
+    # against the reference's own generator where the reference is built
+    import math
+    import pyoracle as po
+    from rampack_gb300 import workloads as W
+    if not po.reference_available():
+        pytest.skip("reference library not built here")
+    for arc_r, arc_a, n in [(0.6 / (2 * math.sin(math.radians(15))), math.radians(120), 5), (2.0, math.radians(200), 7),
+                            (1.0, math.radians(60), 2)]:
+        mine = W.banana_centres(arc_r, arc_a, n)
+        ref = po.banana_centres(arc_r, arc_a, n, 0.5)
+        assert np.array_equal(mine, ref[:, :3])
