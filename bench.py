@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--n-side", type=int, default=100, help="particles per lattice side (default 100 -> 1e6)")
+    ap.add_argument("--workload", default="sc-1e6", choices=sorted(WORKLOADS),
+                    help="sc-1e6: the headline system; the others are further systems of the same path")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--seed", type=int, default=1234)
@@ -55,9 +57,45 @@ def parse():
     return ap.parse_args()
 
 
-def workload(n_side):
+def _sc_1e6(args):
     from rampack_gb300 import workloads as W
+    n_side = args.n_side
     return W.spherocylinders((n_side, n_side, n_side), 0.50, 2.0, 0.5, aspect=(1.0, 1.0, 3.0))
+
+
+def _banana_1e5(args):
+    from rampack_gb300 import workloads as W
+    return W.config_banana_1e5()
+
+
+def _sc_64000(args):
+    from rampack_gb300 import workloads as W
+    return W.config_sc_64000()
+
+
+# name -> (builder, description, metric)
+WORKLOADS = {
+    "sc-1e6": (_sc_1e6, WORKLOAD, METRIC),
+    "banana-1e5": (_banana_1e5, "bent 5-sphere chains (sphere r=0.5, bond 0.6, 30 degrees between bonds: arc "
+                   "120 degrees), N={n:,} (50x80x25), aligned orthorhombic start at phi=0.45, triclinic box; per "
+                   "cycle 2N moves (translation 0.2, rotation 0.2) + 1 isotension box move (delta 0.005, p*=1.5, "
+                   "T=1)", "moves/sec, bent chains N=1e5"),
+    "sc-64000": (_sc_64000, "hard spherocylinders l=5 r=0.5, N={n:,} (40^3), aligned orthorhombic start at "
+                 "phi=0.35 (cell aspect 1:1:6), triclinic box; per cycle 2N moves (translation 0.2, rotation "
+                 "0.2) + 1 isotension box move (delta 0.005, p*=1.5, T=1)", "moves/sec, spherocylinders N=64000"),
+}
+
+
+def workload(args):
+    return WORKLOADS[args.workload][0](args)
+
+
+def describe(args, n):
+    return WORKLOADS[args.workload][1].format(n=n)
+
+
+def metric(args):
+    return WORKLOADS[args.workload][2]
 
 
 # ----------------------------------------------------------------------------------
@@ -160,15 +198,15 @@ def main_reference(args):
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    cfg = workload(args.n_side)
+    cfg = workload(args)
     moves, times, dom, dom_used = cpu_run(cfg, max(1, args.steps), max(0, args.warmup), threads, args.seed)
     total = sum(times)
     value = moves * len(times) / total
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "impl": "reference", "metric": metric(args), "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": len(times), "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD.format(n=len(cfg[2])), "n": len(cfg[2]), "moves_per_step": moves,
+        "config": {"workload": describe(args, len(cfg[2])), "n": len(cfg[2]), "moves_per_step": moves,
                    "parallelism": f"OpenMP domain decomposition {dom_used}"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{len(times)} full cycles of the N={len(cfg[2]):,} system after "
@@ -251,7 +289,7 @@ def main_gpu(args):
     rb.build()
     from rampack_gb300.packing import GpuPacking
 
-    cfg = workload(args.n_side)
+    cfg = workload(args)
     kind, prm, pos, rot, box = cfg
     n = len(pos)
     g = GpuPacking(kind, prm, pos, rot, box, device=local)
@@ -312,8 +350,13 @@ def main_gpu(args):
     moves_per_sweep = 2 * n
     # algorithmic bytes per sweep: each phase streams every particle's FP32 record (28 B) and
     # cell index (4 B) and the cell offsets; every move reads the mover's FP64 state (96 B)
-    # and an accepted move writes FP64 (96 B) and FP32 (28 B) state back.
-    b_sweep = phases * n * (28 + 4) + phases * (ncell + 1) * 4 + moves_per_sweep * (96 + acc_rate * (96 + 28))
+    # and an accepted move writes FP64 (96 B) and FP32 (28 B) state back.  Polyspheres of K
+    # centres add per particle K FP32 centres (16 B each) to the record, K FP64 rotated
+    # centres (24 B each) to the mover's read, and K rotated + K absolute FP64 centres and
+    # K FP32 centres to an accepted move's write.
+    kcen = int(prm[0]) if kind == 2 else 0
+    rec32, s64, w64 = 28 + 16 * kcen, 96 + 24 * kcen, 96 + 28 + 64 * kcen
+    b_sweep = phases * n * (rec32 + 4) + phases * (ncell + 1) * 4 + moves_per_sweep * (s64 + acc_rate * w64)
     b_launch = b_sweep / phases
     avg_launch_ms = sweep_ms / max(1, sweep_launches)
     achieved = b_launch / (avg_launch_ms / 1e3) / 1e9
@@ -322,7 +365,10 @@ def main_gpu(args):
         peak, peak_src = json.load(open(peaks_path))["hbm_gbs"], "measured"
     else:
         peak, peak_src = 6800.0, "fallback"
-    traffic = read_profile_traffic()
+    traffic = read_profile_traffic() if args.workload == "sc-1e6" else None
+    state_mb = n * (96 + 32 + 64 * kcen) / 1e6
+    l2_note = (f"inputs larger than L2 (FP64 state + FP32 mirror {state_mb:.0f} MB + cell lists)" if state_mb > 129
+               else f"inputs smaller than L2 ({state_mb:.0f} MB of state; no flush between steps)")
 
     # ---- end to end through the C ABI with host buffers ----
     e2e = None
@@ -369,12 +415,12 @@ def main_gpu(args):
     g.close()
     if rank == 0:
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "metric": metric(args), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(3, args.warmup), "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD.format(n=n), "n": n, "moves_per_step": 2 * n,
+            "config": {"workload": describe(args, n), "n": n, "moves_per_step": 2 * n,
                        "variant": "plain (unordered FP32 filter + FP64 guard band)",
-                       "l2": "inputs larger than L2 (FP64 state 96 MB + FP32 mirror 32 MB + cell lists)",
+                       "l2": l2_note,
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "grid_dims": list(info["dims"]), "box_moves_accepted": box_acc},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -406,7 +452,7 @@ def main_ordering(args):
     rb.build()
     from rampack_gb300.packing import GpuPacking
 
-    kind, prm, pos, rot, box = workload(args.n_side)
+    kind, prm, pos, rot, box = workload(args)
     g = GpuPacking(kind, prm, pos, rot, box)
     for c in range(20):
         g.sweep(TRANS_STEP, ROT_STEP, seed=args.seed, counter=c, stats=False)

@@ -119,7 +119,8 @@ typedef struct rp_sweep_stats {
 #define RP_KERNEL_OVERFLOW 4      /* large-capacity rerun of oversized neighbourhoods */
 #define RP_KERNEL_ORDER 5         /* partner ranking of the learned ordering */
 #define RP_KERNEL_MLP 6           /* ranking-network training and inference */
-#define RP_NUM_KERNELS 7
+#define RP_KERNEL_FIX 7           /* orientation renormalisation */
+#define RP_NUM_KERNELS 8
 
 /* ---- lifetime ---------------------------------------------------------------------- */
 
@@ -210,6 +211,16 @@ int rp_try_scaling(void *handle, const double *new_box9, double *dE);
 /* Restores the state from before the last rp_try_scaling (buffer swap, no copy).
  * Replaces: Packing::revertScaling (core/Packing.cpp:363-371). */
 int rp_revert_scaling(void *handle);
+
+/* Orientation renormalisation.  Replaces: Packing::renormalizeOrientations(interaction,
+ * allowOverlaps) (core/Packing.cpp:1178-1212) as Simulation::fixRotationMatrices calls it
+ * (core/Simulation.cpp:750-760).  Without allow_overlaps every particle, in index order,
+ * tries its orientation after three Newton-Schulz steps (core/Packing.cpp:1214-1219) as a
+ * rotation move and keeps it unless it then overlaps; *rejected = the particles that kept
+ * their old orientation.  With allow_overlaps the reference resets the packing with the
+ * shapes as they were before the fix (so orientations do not change) and recomputes the
+ * polysphere centres from the body frame; this call does the same and reports 0. */
+int rp_renormalize_orientations(void *handle, int allow_overlaps, int64_t *rejected);
 
 /* ---- statistics --------------------------------------------------------------------- */
 

@@ -81,6 +81,7 @@ def _lib(which: str):
         "replay": (C.c_int, [_P, _P, C.c_int64, _D, C.c_double, _P, _P]),
         "try_scaling": (C.c_double, [_P, _D]),
         "revert_scaling": (None, [_P]),
+        "renormalize": (C.c_int64, [_P, C.c_int]),
         "get_state": (None, [_P, _D, _D, _D]),
         "ng_divisions": (C.c_int, [_P, _I64]),
         "pair_overlap": (C.c_int, [C.c_int, _D, C.c_int, _D, _D, C.c_int, _D, _D, C.c_int, C.c_int, _D, _D]),
@@ -191,6 +192,10 @@ class CpuPacking:
 
     def revert_scaling(self) -> None:
         self._f("revert_scaling")(self.h)
+
+    def renormalize_orientations(self, allow_overlaps: bool = False) -> int:
+        """Packing::renormalizeOrientations: the number of particles whose fix was rejected."""
+        return int(self._f("renormalize")(self.h, 1 if allow_overlaps else 0))
 
     def state(self):
         pos = np.zeros((self.n, 3))

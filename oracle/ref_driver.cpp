@@ -193,6 +193,11 @@ double ref_try_scaling(void *hp, const double *box9) {
 
 void ref_revert_scaling(void *hp) { static_cast<Handle *>(hp)->pk->revertScaling(); }
 
+int64_t ref_renormalize(void *hp, int allow_overlaps) {
+    auto *h = static_cast<Handle *>(hp);
+    return static_cast<int64_t>(h->pk->renormalizeOrientations(h->traits->getInteraction(), allow_overlaps != 0));
+}
+
 void ref_get_state(void *hp, double *pos, double *rot, double *box9) {
     auto *h = static_cast<Handle *>(hp);
     for (std::size_t i = 0; i < h->pk->size(); i++) {

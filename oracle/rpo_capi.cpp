@@ -146,6 +146,11 @@ double rpo_try_scaling(void *hp, const double *box9) {
 
 void rpo_revert_scaling(void *hp) { static_cast<Handle *>(hp)->pk->revert_scaling(); }
 
+int64_t rpo_renormalize(void *hp, int allow_overlaps) {
+    auto *h = static_cast<Handle *>(hp);
+    return static_cast<int64_t>(h->pk->renormalize_orientations(h->inter, allow_overlaps != 0));
+}
+
 void rpo_get_state(void *hp, double *pos, double *rot, double *box9) {
     auto *h = static_cast<Handle *>(hp);
     std::size_t n = h->pk->size();

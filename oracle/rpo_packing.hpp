@@ -683,6 +683,36 @@ public:
     static void fix_rotation(M3 &r) {
         for (int i = 0; i < 3; i++) r = msub(mscale(r, 1.5), mm(mm(mscale(r, 0.5), transpose(r)), r));
     }
+
+    // Packing.cpp:1178-1212 (renormalizeOrientations) with tryOrientationFix
+    // (:1221-1240).  With allow_overlaps the reference copies the shapes before fixing them
+    // and resets the packing with that copy, so orientations stay as they were and only the
+    // rotated centres are recomputed from the body frame.  Otherwise every particle, in index
+    // order, tries its fixed orientation (centres rotated afresh from the body frame) as a
+    // rotation move on thread slot 0 and keeps it when the move energy is not positive.
+    std::size_t renormalize_orientations(const Interaction &inter, bool allow_overlaps) {
+        if (allow_overlaps) {
+            std::vector<Shape> copy(shapes.begin(), shapes.begin() + static_cast<std::ptrdiff_t>(size()));
+            reset(std::move(copy), box, inter);
+            return 0;
+        }
+        std::size_t rejected = 0;
+        std::size_t temp = size();
+        for (std::size_t i = 0; i < size(); i++) {
+            last_altered[0] = i;
+            shapes[temp].pos = shapes[i].pos;
+            M3 r = shapes[i].rot;
+            fix_rotation(r);
+            shapes[temp].rot = r;
+            if (num_centres > 0) {
+                for (std::size_t c = 0; c < num_centres; c++) centres[temp * num_centres + c] = mv(r, inter.centres[c]);
+                recalc_abs_centres(temp);
+            }
+            if (move_overlap_energy(i, temp, inter) > 0) rejected++;
+            else accept(1);
+        }
+        return rejected;
+    }
 };
 
 }  // namespace rpo

@@ -91,8 +91,9 @@ SIGNATURES = {
     "rp_pair_log_clear": (C.c_int, [_P]),
     "rp_mlp_train": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_float, C.c_uint64, _F]),
     "rp_set_ordering": (C.c_int, [_P, C.c_int32, C.c_int32]),
+    "rp_renormalize_orientations": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int64)]),
 }
-KERNEL_GROUPS = ["sweep", "rebuild", "count", "rescale", "overflow", "order", "mlp"]
+KERNEL_GROUPS = ["sweep", "rebuild", "count", "rescale", "overflow", "order", "mlp", "fix"]
 MLP_NPARAM = 5313
 MLP_FEATURES = 16
 ORDER_OFF, ORDER_MLP, ORDER_DISTANCE = 0, 1, 2

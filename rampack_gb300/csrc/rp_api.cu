@@ -23,6 +23,15 @@ cudaError_t launch_count(const DevState &s, const GridDev &g, int early, unsigne
 cudaError_t launch_sweep(const SweepArgs &a, bool list, int nwarps, cudaStream_t st);
 size_t sweep_smem_per_warp(int kind, int cap, bool learn = false, int ncen = 0);
 cudaError_t launch_abs_centres(const DevState &s, cudaStream_t st);
+cudaError_t launch_fix_prepare(const DevState &s, const double *cbody, double *rotfix, double *cenfix, double *absfix,
+                               cudaStream_t st);
+cudaError_t launch_fresh_centres(const DevState &s, const double *cbody, cudaStream_t st);
+cudaError_t launch_fix_check(const DevState &s, const GridDev &g, const double *rotfix, const double *absfix,
+                             uint8_t *rejected, unsigned long long *first, cudaStream_t st);
+cudaError_t launch_fix_commit(const DevState &s, const double *rotfix, const double *cenfix, const double *absfix,
+                              int64_t from, int64_t to, cudaStream_t st);
+cudaError_t launch_fix_serial(const DevState &s, const GridDev &g, const double *rotfix, const double *cenfix,
+                              const double *absfix, int64_t from, unsigned long long *nrej, cudaStream_t st);
 cudaError_t launch_mlp_grad(const float *feats, const uint8_t *labels, int64_t total, int64_t i0, int n,
                             int64_t mul, int64_t off, const float *w32, float *grad, float *loss, int num_sms,
                             cudaStream_t st);
@@ -118,6 +127,7 @@ struct Handle {
     double *cen64 = nullptr;
     double *abs64[2] = {nullptr, nullptr};
     double *cthr64 = nullptr;
+    double *cbody_dev = nullptr;    // body-frame centres on the device
     // learned ordering: network parameters (FP32 master + BF16 copy), Adam moments, scratch
     float *mlp_w32 = nullptr, *mlp_grad = nullptr, *mlp_m = nullptr, *mlp_v = nullptr, *mlp_loss = nullptr;
     __nv_bfloat16 *mlp_w16 = nullptr;
@@ -642,6 +652,9 @@ static int create_common(Handle *h, int64_t n, int device, void **handle) {
         if ((e = cudaMalloc(&h->cthr64, sizeof(double) * MAX_CEN * MAX_CEN)) != cudaSuccess) return bail(e);
         if ((e = cudaMemcpy(h->cthr64, h->cthr_host, sizeof(h->cthr_host), cudaMemcpyHostToDevice)) != cudaSuccess)
             return bail(e);
+        if ((e = cudaMalloc(&h->cbody_dev, sizeof(h->cbody))) != cudaSuccess) return bail(e);
+        if ((e = cudaMemcpy(h->cbody_dev, h->cbody, sizeof(h->cbody), cudaMemcpyHostToDevice)) != cudaSuccess)
+            return bail(e);
     }
     if ((e = cudaMalloc(&h->rot64, sizeof(double) * 9 * n)) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc(&h->rtab64, sizeof(double) * 9 * ROT_TABLE)) != cudaSuccess) return bail(e);
@@ -749,6 +762,7 @@ int rp_destroy(void *handle) {
     cudaFree(h->abs64[0]);
     cudaFree(h->abs64[1]);
     cudaFree(h->cthr64);
+    cudaFree(h->cbody_dev);
     cudaFree(h->rtab64);
     cudaFree(h->rtab32);
     cudaFree(h->item_counters);
@@ -1319,6 +1333,78 @@ int rp_get_timing(void *handle, double *ms, uint64_t *groups) {
         if (ms) ms[k] = h->kernel_ms[k];
         if (groups) groups[k] = h->kernel_groups[k];
     }
+    return RP_OK;
+}
+
+// ---- orientation renormalisation ----------------------------------------------------
+
+int rp_renormalize_orientations(void *handle, int allow_overlaps, int64_t *rejected) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !rejected) return fail(h, RP_ERR_ARG, "null argument");
+    if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
+    RP_CUDA(h, cudaSetDevice(h->device));
+    *rejected = 0;
+    h->can_revert = false;
+    h->log_valid = false;
+    h->partners_valid = false;
+    if (allow_overlaps) {
+        if (h->ncen > 0) {
+            Group grp(h, RP_KERNEL_FIX, 2);
+            RP_CUDA(h, launch_fresh_centres(dev_state(h), h->cbody_dev, h->stream));
+            RP_CUDA(h, launch_abs_centres(dev_state(h), h->stream));
+        }
+        int rc = rebuild(h, h->gcur, h->pcur);
+        if (rc) return rc;
+        RP_CUDA(h, cudaStreamSynchronize(h->stream));
+        return RP_OK;
+    }
+    const int64_t n = h->n, nc = std::max(1, h->ncen);
+    double *rotfix = nullptr, *cenfix = nullptr, *absfix = nullptr;
+    uint8_t *rej = nullptr;
+    unsigned long long *words = nullptr;  // [0] first rejected index, [1] serial rejections
+    struct Scratch {
+        std::vector<void *> p;
+        ~Scratch() {
+            for (void *q : p) cudaFree(q);
+        }
+    } scratch;
+    auto alloc = [&](void **q, size_t bytes) {
+        cudaError_t e = cudaMalloc(q, bytes);
+        if (e == cudaSuccess) scratch.p.push_back(*q);
+        return e;
+    };
+    RP_CUDA(h, alloc(reinterpret_cast<void **>(&rotfix), sizeof(double) * 9 * n));
+    RP_CUDA(h, alloc(reinterpret_cast<void **>(&cenfix), sizeof(double) * 3 * n * nc));
+    RP_CUDA(h, alloc(reinterpret_cast<void **>(&absfix), sizeof(double) * 3 * n * nc));
+    RP_CUDA(h, alloc(reinterpret_cast<void **>(&rej), n));
+    RP_CUDA(h, alloc(reinterpret_cast<void **>(&words), 2 * sizeof(unsigned long long)));
+    unsigned long long init[2] = {static_cast<unsigned long long>(n), 0};
+    RP_CUDA(h, cudaMemcpyAsync(words, init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
+    const DevState s = dev_state(h);
+    const GridDev &g = h->grid[h->gcur].d;
+    {
+        Group grp(h, RP_KERNEL_FIX, 2);
+        RP_CUDA(h, launch_fix_prepare(s, h->cbody_dev, rotfix, cenfix, absfix, h->stream));
+        RP_CUDA(h, launch_fix_check(s, g, rotfix, absfix, rej, words, h->stream));
+    }
+    unsigned long long first = 0;
+    RP_CUDA(h, cudaMemcpyAsync(&first, words, sizeof(first), cudaMemcpyDeviceToHost, h->stream));
+    RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    const int64_t from = static_cast<int64_t>(first);
+    {
+        Group grp(h, RP_KERNEL_FIX, from < n ? 2 : 1);
+        RP_CUDA(h, launch_fix_commit(s, rotfix, cenfix, absfix, 0, from, h->stream));
+        if (from < n) RP_CUDA(h, launch_fix_serial(s, g, rotfix, cenfix, absfix, from, words + 1, h->stream));
+    }
+    if (from < n) {
+        unsigned long long nr = 0;
+        RP_CUDA(h, cudaMemcpyAsync(&nr, words + 1, sizeof(nr), cudaMemcpyDeviceToHost, h->stream));
+        RP_CUDA(h, cudaStreamSynchronize(h->stream));
+        *rejected = static_cast<int64_t>(nr);
+    }
+    int rc = rebuild(h, h->gcur, h->pcur);  // FP32 mirrors of the new orientations and centres
+    if (rc) return rc;
+    RP_CUDA(h, cudaStreamSynchronize(h->stream));
     return RP_OK;
 }
 

@@ -222,6 +222,27 @@ RP_HD bool exact_overlap(const ExactShape &s, d3 p1, d3 a1, d3 p2, d3 a2, d3 t) 
     return segment_distance2(c11, c12, c21, c22) < s.core_thr;
 }
 
+// Packing::fixRotationMatrix (core/Packing.cpp:1214-1219): three Newton-Schulz steps
+// R <- 1.5 R - 0.5 R R^T R as the reference's Matrix operators evaluate them: the scalar
+// products element-wise, then (0.5 R) R^T, then that times R (i-j-k sums from zero), then
+// the element-wise difference.
+RP_HD void fix_rotation(double *r) {
+    for (int it = 0; it < 3; it++) {
+        double a[9], h[9], t[9], p[9], q[9];
+        for (int k = 0; k < 9; k++) {
+            a[k] = dmul(r[k], 1.5);
+            h[k] = dmul(r[k], 0.5);
+        }
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) t[3 * i + j] = r[3 * j + i];
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) p[3 * i + j] = mm_elem(h, t, i, j);
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) q[3 * i + j] = mm_elem(p, r, i, j);
+        for (int k = 0; k < 9; k++) r[k] = dsub(a[k], q[k]);
+    }
+}
+
 // --------------------------------------------------------------------------------
 // Philox-4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw, SC'11,
 // "Parallel random numbers: as easy as 1, 2, 3"): ten rounds of two 32x32->64

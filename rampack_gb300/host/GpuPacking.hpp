@@ -112,6 +112,14 @@ public:
         box_ = prev_box_;
     }
 
+    // Packing::renormalizeOrientations (core/Packing.cpp:1178-1212): the number of
+    // particles whose Newton-Schulz-fixed orientation was rejected.
+    std::size_t renormalizeOrientations(bool allowOverlaps) {
+        int64_t rejected = 0;
+        check(rp_renormalize_orientations(h_, allowOverlaps ? 1 : 0, &rejected), "rp_renormalize_orientations");
+        return static_cast<std::size_t>(rejected);
+    }
+
     // The batched move entry: one device sweep (2N moves for translation + rotation).
     rp_sweep_stats performMoves(double translationStep, double rotationStep, uint64_t seed, uint64_t cycle) {
         rp_sweep_params p{};

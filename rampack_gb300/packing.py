@@ -224,6 +224,13 @@ class GpuPacking:
     def set_ordering(self, mode: int, every: int = 1):
         self._check(self.lib.rp_set_ordering(self.h, mode, every))
 
+    # ---- orientation renormalisation ----
+    def renormalize_orientations(self, allow_overlaps: bool = False) -> int:
+        """Packing::renormalizeOrientations: the number of particles whose fix was rejected."""
+        r = C.c_int64()
+        self._check(self.lib.rp_renormalize_orientations(self.h, 1 if allow_overlaps else 0, C.byref(r)))
+        return int(r.value)
+
     # ---- box moves ----
     def try_scaling(self, box) -> float:
         b = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
