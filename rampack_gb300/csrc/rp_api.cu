@@ -518,6 +518,8 @@ int check_status(Handle *h) {
                       (st & ST_PARTICLE_NOT_IN_CELL) ? " (a move's particle is not in its cell)" : "",
                       (st & ST_CAPACITY) ? " (a cell neighbourhood exceeds the staging capacity)" : "");
         if (st & ST_OUTSIDE) return fail(h, RP_ERR_ARG, "a particle lies outside the box");
+        if (st & ST_NOT_ROTATION)
+            return fail(h, RP_ERR_ARG, "an orientation is not a rotation matrix (|O^T O - I| >= 1e-6)");
         return fail(h, (st & ST_CAPACITY) ? RP_ERR_CAPACITY : RP_ERR_DEVICE, buf);
     }
     return RP_OK;

@@ -156,6 +156,18 @@ __global__ void k_assign(DevState s, GridDev g) {
     if (s.strict_box) {
         if (!(rr[0] >= 0.0 && rr[0] < 1.0 && rr[1] >= 0.0 && rr[1] < 1.0 && rr[2] >= 0.0 && rr[2] < 1.0))
             atomicOr(s.status, ST_OUTSIDE);
+        // the engine's cell sizes and FP32 margins take orientations to be rotations: a
+        // unit axis (spherocylinders) or an orthonormal matrix (polyspheres)
+        const double *o = s.rot64 + 9 * i;
+        bool bad = false;
+        for (int a = 0; a < 3; a++)
+            for (int b = a; b < 3; b++) {
+                if (s.kind == 1 && (a != 2 || b != 2)) continue;
+                if (s.kind == 0) continue;
+                double g2 = o[a] * o[b] + o[3 + a] * o[3 + b] + o[6 + a] * o[6 + b];
+                if (!(fabs(g2 - (a == b ? 1.0 : 0.0)) < 1e-6)) bad = true;
+            }
+        if (bad) atomicOr(s.status, ST_NOT_ROTATION);
     } else if (!(fabs(rr[0] - 0.5) < 0.5 + 1e-9 && fabs(rr[1] - 0.5) < 0.5 + 1e-9 && fabs(rr[2] - 0.5) < 0.5 + 1e-9)) {
         atomicOr(s.status, ST_NUMERIC);  // rescaled positions drift at most a few ulp outside
     }

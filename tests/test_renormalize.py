@@ -16,8 +16,11 @@ def perturbed(cfg, noise, seed=3, factor=1.0):
     return kind, prm, pos, np.ascontiguousarray(rot), box
 
 
-CASES = [("sc_l2_dense", 1e-9, 1.0), ("sc_l2_dense", 0.03, 1.0), ("sc_l5", 0.05, 1.0), ("hs_dense", 0.1, 1.0),
-         ("poly_dense", 1e-9, 1.0), ("poly_dense", 0.05, 1.0), ("poly_banana", 0.02, 0.995)]
+# (system, orientation noise, box factor): orientations off orthonormal by up to 1e-7 (the
+# engine takes rotations to within 1e-6); compressed systems hold overlaps, so some fixes
+# are rejected and the serial remainder of the pass runs
+CASES = [("sc_l2_dense", 1e-9, 1.0), ("sc_l2_dense", 1e-7, 0.99), ("sc_l5", 1e-7, 0.995), ("hs_dense", 1e-7, 0.98),
+         ("poly_dense", 1e-9, 1.0), ("poly_dense", 1e-7, 0.995), ("poly_banana", 1e-7, 0.99)]
 
 
 @pytest.mark.parametrize("name,noise,factor", CASES)
@@ -49,13 +52,24 @@ def test_engine_matches_oracle(oracle, engine, name, noise, factor, allow):
         gp, gr, _ = g.state()
         cp, cr, _ = cpu.state()
         assert np.array_equal(gp, cp) and np.array_equal(gr, cr)
-        if factor == 1.0:
-            t, r = (0.1, 0.0) if kind == 0 else (0.2, 0.2)
-            g.sweep(t, r, seed=77, counter=0, log=True)
-            moves, codes = g.sweep_log()
-            _, _, bounds = g.grid()
-            got, _ = cpu.replay(moves, bounds)
-            assert np.array_equal(codes, got)
-            gp, gr, _ = g.state()
-            cp, cr, _ = cpu.state()
-            assert np.array_equal(gp, cp) and np.array_equal(gr, cr)
+        # the moves after the pass depend on the recomputed polysphere centres
+        t, r = (0.1, 0.0) if kind == 0 else (0.2, 0.2)
+        g.sweep(t, r, seed=77, counter=0, log=True)
+        moves, codes = g.sweep_log()
+        _, _, bounds = g.grid()
+        got, _ = cpu.replay(moves, bounds)
+        assert np.array_equal(codes, got)
+        gp, gr, _ = g.state()
+        cp, cr, _ = cpu.state()
+        assert np.array_equal(gp, cp) and np.array_equal(gr, cr)
+
+
+@pytest.mark.gpu
+def test_upload_refuses_non_rotations(engine):
+    from rampack_gb300.packing import GpuPacking
+    from rampack_gb300._lib import EngineError
+    kind, prm, pos, rot, box = systems.sc_l2()
+    bad = rot.copy()
+    bad[5] *= 1.01  # one axis 1 % too long
+    with pytest.raises(EngineError):
+        GpuPacking(kind, prm, pos, bad, box)
