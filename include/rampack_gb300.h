@@ -222,6 +222,14 @@ int rp_revert_scaling(void *handle);
  * polysphere centres from the body frame; this call does the same and reports 0. */
 int rp_renormalize_orientations(void *handle, int allow_overlaps, int64_t *rejected);
 
+/* Nematic order of the current state: NematicOrder::calculate
+ * (core/observables/NematicOrder.cpp:9-56).  q9 (row-major, may be NULL) receives
+ * Q = 1/2 (3 <u u^T> - I) over the particles' primary axes (orientation column 2), *p2 the
+ * eigenvalue of largest magnitude (Cardano, as the reference).  The sums are reduced on the
+ * device in a fixed order, so Q matches the reference's serial sum to rounding (~1e-15
+ * relative), not bit for bit.  Spheres have no primary axis: RP_ERR_UNSUPPORTED. */
+int rp_nematic_order(void *handle, double *q9, double *p2);
+
 /* ---- statistics --------------------------------------------------------------------- */
 
 /* Cumulative counters of all sweeps and move lists since creation. */

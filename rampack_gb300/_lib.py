@@ -92,6 +92,7 @@ SIGNATURES = {
     "rp_mlp_train": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_float, C.c_uint64, _F]),
     "rp_set_ordering": (C.c_int, [_P, C.c_int32, C.c_int32]),
     "rp_renormalize_orientations": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int64)]),
+    "rp_nematic_order": (C.c_int, [_P, _D, _D]),
 }
 KERNEL_GROUPS = ["sweep", "rebuild", "count", "rescale", "overflow", "order", "mlp", "fix"]
 MLP_NPARAM = 5313

@@ -26,6 +26,8 @@ cudaError_t launch_abs_centres(const DevState &s, cudaStream_t st);
 cudaError_t launch_fix_prepare(const DevState &s, const double *cbody, double *rotfix, double *cenfix, double *absfix,
                                cudaStream_t st);
 cudaError_t launch_fresh_centres(const DevState &s, const double *cbody, cudaStream_t st);
+int axis_moment_blocks(int64_t n);
+cudaError_t launch_axis_moments(const double *rot64, int64_t n, double *partial, cudaStream_t st);
 cudaError_t launch_fix_check(const DevState &s, const GridDev &g, const double *rotfix, const double *absfix,
                              uint8_t *rejected, unsigned long long *first, cudaStream_t st);
 cudaError_t launch_fix_commit(const DevState &s, const double *rotfix, const double *cenfix, const double *absfix,
@@ -382,10 +384,15 @@ DevState dev_state(Handle *h) {
 int setup_grid(Handle *h, GridHost &G, const double *box, const double *shift) {
     double hgt[3];
     heights_of(box, hgt);
-    const double cell_min = h->range * (1.0 + 1e-9);
+    // at least one interaction range (bodies in two cells of one colour never interact) and
+    // at least the mean particle spacing (dilute systems would otherwise spread a few
+    // particles over many nearly empty cells)
+    const double spacing = std::cbrt(volume_of(box) / static_cast<double>(h->n));
+    const double cell_min = std::max(h->range, spacing) * (1.0 + 1e-9);
     int dims[3];
     for (int d = 0; d < 3; d++) {
-        if (!(hgt[d] >= cell_min)) return fail(h, RP_ERR_UNSUPPORTED, "box height smaller than the interaction range");
+        if (!(hgt[d] >= h->range * (1.0 + 1e-9)))
+            return fail(h, RP_ERR_UNSUPPORTED, "box height smaller than the interaction range");
         double nd = std::floor(hgt[d] / cell_min);
         if (nd > 1 << 20) return fail(h, RP_ERR_UNSUPPORTED, "too many cells");
         int n = static_cast<int>(nd);
@@ -1335,6 +1342,68 @@ int rp_get_timing(void *handle, double *ms, uint64_t *groups) {
         if (ms) ms[k] = h->kernel_ms[k];
         if (groups) groups[k] = h->kernel_groups[k];
     }
+    return RP_OK;
+}
+
+// ---- observables ----------------------------------------------------------------------
+
+// NematicOrder::calculateEigenvalues (core/observables/NematicOrder.cpp:29-56), the Cardano
+// formula of arXiv:1306.6291; a multiple of the identity has the triple eigenvalue b / 3.
+static void q_eigenvalues(const double *q, double ev[3]) {
+    double A11 = q[0], A12 = q[1], A13 = q[2], A22 = q[4], A23 = q[5], A33 = q[8];
+    double b = A11 + A22 + A33;
+    double c = A11 * A22 + A11 * A33 + A22 * A33 - A12 * A12 - A13 * A13 - A23 * A23;
+    double d = A11 * A23 * A23 + A22 * A13 * A13 + A33 * A12 * A12 - A11 * A22 * A33 - 2 * A12 * A13 * A23;
+    double p = b * b - 3 * c;
+    if (!(p > 0)) {
+        ev[0] = ev[1] = ev[2] = b / 3;
+        return;
+    }
+    double sp = std::sqrt(p);
+    double qq = 2 * b * b * b - 9 * b * c - 27 * d;
+    double ratio = qq / 2 / (sp * sp * sp);
+    if (std::abs(ratio) > 1) ratio = ratio < 0 ? -1 : 1;
+    double delta = std::acos(ratio);
+    ev[0] = 1. / 3 * (b + 2 * sp * std::cos(delta / 3));
+    ev[1] = 1. / 3 * (b + 2 * sp * std::cos((delta + 2 * M_PI) / 3));
+    ev[2] = 1. / 3 * (b + 2 * sp * std::cos((delta - 2 * M_PI) / 3));
+}
+
+int rp_nematic_order(void *handle, double *q9, double *p2) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !p2) return fail(h, RP_ERR_ARG, "null argument");
+    if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
+    if (h->shape.kind == RP_SHAPE_SPHERE) return fail(h, RP_ERR_UNSUPPORTED, "spheres have no primary axis");
+    RP_CUDA(h, cudaSetDevice(h->device));
+    const int nb = axis_moment_blocks(h->n);
+    double *partial = nullptr;
+    RP_CUDA(h, cudaMalloc(&partial, sizeof(double) * 6 * nb));
+    std::vector<double> host(6 * nb);
+    cudaError_t e = launch_axis_moments(h->rot64, h->n, partial, h->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(host.data(), partial, sizeof(double) * 6 * nb, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(partial);
+    RP_CUDA(h, e);
+    h->launches += 1;
+    double m[6] = {0, 0, 0, 0, 0, 0};
+    for (int b = 0; b < nb; b++)
+        for (int k = 0; k < 6; k++) m[k] += host[6 * b + k];
+    const double S[9] = {m[0], m[1], m[2], m[1], m[3], m[4], m[2], m[4], m[5]};
+    double q[9];
+    const double n = static_cast<double>(h->n);
+    for (int i = 0; i < 9; i++) {
+        double s = S[i] / n;                               // QTensor /= size()
+        double t = 3. * s - ((i % 4 == 0) ? 1.0 : 0.0);    // 3 Q - I
+        q[i] = 0.5 * t;
+    }
+    double ev[3];
+    q_eigenvalues(q, ev);
+    double best = ev[0];
+    for (int k = 1; k < 3; k++)
+        if (std::abs(best) < std::abs(ev[k])) best = ev[k];
+    *p2 = best;
+    if (q9) std::memcpy(q9, q, sizeof(q));
     return RP_OK;
 }
 

@@ -224,6 +224,14 @@ class GpuPacking:
     def set_ordering(self, mode: int, every: int = 1):
         self._check(self.lib.rp_set_ordering(self.h, mode, every))
 
+    # ---- observables ----
+    def nematic_order(self):
+        """(Q tensor 3x3, P2) of the current state (NematicOrder::calculate)."""
+        q = np.zeros(9)
+        p2 = C.c_double()
+        self._check(self.lib.rp_nematic_order(self.h, dptr(q), C.byref(p2)))
+        return q.reshape(3, 3), float(p2.value)
+
     # ---- orientation renormalisation ----
     def renormalize_orientations(self, allow_overlaps: bool = False) -> int:
         """Packing::renormalizeOrientations: the number of particles whose fix was rejected."""
