@@ -24,6 +24,7 @@
 #include "core/shapes/SphereTraits.h"
 #include "core/shapes/SpherocylinderTraits.h"
 #include "core/volume_scalers/AnisotropicVolumeScaler.h"
+#include "core/volume_scalers/DeltaVolumeScaler.h"
 #include "core/volume_scalers/LogScalingFactorSampler.h"
 #include "core/volume_scalers/TriclinicAdapter.h"
 #include "core/volume_scalers/TriclinicDeltaScaler.h"
@@ -331,6 +332,8 @@ int ref_sim_run(void *hp, const ref_sim_params *p, int64_t cycles, ref_sim_stats
                                                                 AnisotropicVolumeScaler::X & AnisotropicVolumeScaler::Y
                                                                     & AnisotropicVolumeScaler::Z);
             scaler = std::make_unique<TriclinicAdapter>(std::move(vs), p->box_step);
+        } else if (p->box_kind == 3) {
+            scaler = std::make_unique<TriclinicAdapter>(std::make_unique<DeltaVolumeScaler>(), p->box_step);
         }
         std::array<std::size_t, 3> dd{static_cast<std::size_t>(p->domains[0]), static_cast<std::size_t>(p->domains[1]),
                                       static_cast<std::size_t>(p->domains[2])};

@@ -131,7 +131,7 @@ struct SimParams {
     double temperature = 1, pressure = 1;
     double translation_step = 0;   // 0 disables the translation sampler
     double rotation_step = 0;      // 0 disables the rotation sampler
-    int box_kind = 0;              // 0 none, 1 delta_triclinic(scale together), 2 isotropic log
+    int box_kind = 0;              // 0 none, 1 delta_triclinic(scale together), 2 isotropic log, 3 delta volume
     double box_step = 0;
     std::array<std::size_t, 3> domains{1, 1, 1};
     unsigned long seed = 1234;
@@ -280,6 +280,22 @@ public:
             for (int i = 0; i < 3; i++)
                 for (int j = 0; j < 3; j++) d[3 * i + j] += sd(mt);
             return Box(d);
+        }
+        if (p.box_kind == 3) {
+            // DeltaVolumeScaler.cpp:10-19 through TriclinicAdapter.h:27-33: dV uniform in
+            // +-step, every side times cbrt((dV + V) / V) with V the product of the heights
+            std::uniform_real_distribution<double> u01(0, 1);
+            double dv = (2 * u01(mt) - 1) * p.box_step;
+            V3 h = ob.heights();
+            double cur = 1.;
+            for (int i = 0; i < 3; i++) cur *= h[i];
+            double f3 = std::cbrt((dv + cur) / cur);
+            auto s3 = ob.sides();
+            for (int i = 0; i < 3; i++) s3[i] = vscale(s3[i], f3);
+            M3 d3m{};
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) d3m[3 * i + j] = s3[j][i];
+            return Box(d3m);
         }
         std::uniform_real_distribution<double> ld(-p.box_step, p.box_step);
         double f = std::exp(ld(mt));

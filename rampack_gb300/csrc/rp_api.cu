@@ -384,11 +384,11 @@ DevState dev_state(Handle *h) {
 int setup_grid(Handle *h, GridHost &G, const double *box, const double *shift) {
     double hgt[3];
     heights_of(box, hgt);
-    // at least one interaction range (bodies in two cells of one colour never interact) and
-    // at least the mean particle spacing (dilute systems would otherwise spread a few
-    // particles over many nearly empty cells)
-    const double spacing = std::cbrt(volume_of(box) / static_cast<double>(h->n));
-    const double cell_min = std::max(h->range, spacing) * (1.0 + 1e-9);
+    // at least one interaction range (bodies in two cells of one colour never interact),
+    // and large enough that the grid has at most max(4096, 8 N) cells (a dilute system
+    // would otherwise spread a few particles over millions of empty cells)
+    const double max_cells = std::max(4096.0, 8.0 * static_cast<double>(h->n));
+    const double cell_min = std::max(h->range, std::cbrt(volume_of(box) / max_cells)) * (1.0 + 1e-9);
     int dims[3];
     for (int d = 0; d < 3; d++) {
         if (!(hgt[d] >= h->range * (1.0 + 1e-9)))

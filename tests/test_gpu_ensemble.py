@@ -8,9 +8,9 @@ the reference's, through equilibrium averages:
   (test/validation_tests/SimulationTest.cpp:91-111, Carnahan-Starling), within 3 sigma and
   with a relative error under 3 %, sampled as that test samples (100 samples, one every
   100 cycles after 5000 cycles);
-* spherocylinders l=3 r=0.5 (N=512) under isotropic log box moves: number density and
+* spherocylinders l=3 r=0.5 (N=108) under delta-volume box moves: number density and
   nematic order P2 of the GPU run agree with a run of the CPU oracle (the reference's
-  algorithm, mt19937 proposals) within 3 combined sigma.
+  algorithm, mt19937 proposals) within 3 combined sigma of block averages.
 
 The runs are seeded, so the outcome is deterministic.
 """
@@ -76,18 +76,43 @@ def test_hard_sphere_density_matches_the_reference_expectation(engine):
     assert err / mean < 0.03
 
 
+def blocked(samples, block=10):
+    """Means of consecutive blocks of samples (decorrelates slow volume fluctuations)."""
+    x = np.asarray(samples, dtype=np.float64)
+    n = len(x) // block
+    return x[:n * block].reshape(n, block).mean(1)
+
+
 def test_spherocylinder_ensemble_matches_the_oracle(oracle, engine):
+    # the reference's spherocylinder validation system (l=3, r=0.5, T=1, p=0.5, translation
+    # 0.5 + rotation 1, delta-volume box moves), with 108 instead of 50 particles so that the
+    # box stays more than two interaction ranges high
     from rampack_gb300.packing import GpuPacking
-    kind, prm, pos, rot, box = W.spherocylinders((8, 8, 8), 0.20, 3.0, 0.5, aspect=(1, 1, 3))
-    pressure, trans, rot_step, box_step = 0.3, 0.5, 0.5, 0.01
-    skip, samples, every = 1500, 120, 40
+    kind, prm = W.SPHEROCYLINDER, np.array([3.0, 0.5])
+    pos = W.lattice((6, 6, 3), (2.0, 2.0, 4.2))
+    rot = W.aligned_rotations(len(pos))
+    box = W.diag_box(12.0, 12.0, 12.6)
+    pressure, trans, rot_step, box_step = 0.5, 0.5, 1.0, 3.0
+    skip, samples, every = 5000, 100, 100
+
+    def heights_volume(b):
+        m = b.reshape(3, 3)
+        s = [m[:, k] for k in range(3)]
+        v = abs(np.dot(np.cross(s[0], s[1]), s[2]))
+        return np.prod([v / np.linalg.norm(np.cross(s[(k + 1) % 3], s[(k + 2) % 3])) for k in range(3)])
+
+    def delta_volume_heights(box, rng):
+        # DeltaVolumeScaler: the "volume" is the product of the box heights
+        v = heights_volume(box)
+        dv = (2 * rng.uniform() - 1) * box_step
+        return box * np.cbrt((dv + v) / v)
 
     with GpuPacking(kind, prm, pos, rot, box) as g:
-        gs = gpu_npt(g, samples * every, every, skip, trans, rot_step, pressure, log_isotropic(box_step), 99,
+        gs = gpu_npt(g, samples * every, every, skip, trans, rot_step, pressure, delta_volume_heights, 99,
                      lambda g, box: (obs.number_density(g.n, box), g.nematic_order()[1]))
 
-    cpu = po.CpuPacking("oracle", kind, prm, pos, rot, box, threads=4)
-    kw = dict(translation_step=trans, rotation_step=rot_step, box_kind=2, box_step=box_step, pressure=pressure,
+    cpu = po.CpuPacking("oracle", kind, prm, pos, rot, box, threads=1)
+    kw = dict(translation_step=trans, rotation_step=rot_step, box_kind=3, box_step=box_step, pressure=pressure,
               temperature=1.0)
     po.run_cycles(cpu, skip, seed=7, **kw)
     cs = []
@@ -97,8 +122,8 @@ def test_spherocylinder_ensemble_matches_the_oracle(oracle, engine):
         cs.append((obs.number_density(len(p), b), obs.nematic_order(r)[1]))
 
     for q, name in ((0, "density"), (1, "P2")):
-        mg, eg = obs.sem([s[q] for s in gs])
-        mc, ec = obs.sem([s[q] for s in cs])
+        mg, eg = obs.sem(blocked([s[q] for s in gs]))
+        mc, ec = obs.sem(blocked([s[q] for s in cs]))
         assert abs(mg - mc) <= 3 * math.hypot(eg, ec), (name, mg, eg, mc, ec)
 
 
