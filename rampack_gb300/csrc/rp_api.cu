@@ -59,6 +59,7 @@ struct GridHost {
     int cap = 0;
     double cellmat64[9]{};
     std::vector<float> cthr;  // host copy of the FP32 centre-pair thresholds (polyspheres)
+    bool no_ng = false;       // the reference keeps no neighbour grid for this grid's box
 };
 
 struct Handle {
@@ -291,6 +292,7 @@ DevState dev_state(Handle *h) {
     s.cen64 = h->cen64;
     s.abs64 = h->abs64[h->pcur];
     s.cthr64 = h->cthr64;
+    s.pbc_fold = h->grid[h->gcur].no_ng ? 1 : 0;
     // ---- FP32 filter margins for the current grid ----
     const GridHost &g = h->grid[h->gcur];
     double lrow = 0;
@@ -400,16 +402,20 @@ int setup_grid(Handle *h, GridHost &G, const double *box, const double *shift) {
         else n = 1;
         dims[d] = n;
     }
-    // The reference keeps no neighbour grid for small boxes (core/Packing.cpp:862-881)
-    // and then tests pairs through full periodic boundary conditions, an arithmetic this
-    // engine does not reproduce.
+    // The reference keeps no neighbour grid for small boxes (core/Packing.cpp:862-881) and
+    // then tests every pair at its nearest periodic image, measuring sphere distances with
+    // the periodic boundary conditions' formula.  That is the engine's decision too as long
+    // as a pair has at most one image within range: every box height at least twice the
+    // reference's interaction range.
     {
         double ref_cell = h->ref_range;
         double min_cell = std::cbrt(volume_of(box) / static_cast<double>(h->n)) / 5;
-        if (h->range < min_cell) ref_cell = min_cell;
+        if (h->ref_range < min_cell) ref_cell = min_cell;
         double mx = std::max({hgt[0], hgt[1], hgt[2]}), mn = std::min({hgt[0], hgt[1], hgt[2]});
-        if (ref_cell * 4 > mx || ref_cell * (1 + 1e-12) > mn)
-            return fail(h, RP_ERR_UNSUPPORTED, "box too small: the reference uses no neighbour grid here");
+        G.no_ng = ref_cell * 4 > mx || ref_cell * (1 + 1e-12) > mn;
+        if (G.no_ng && !(mn >= 2 * h->ref_range * (1 + 1e-9)))
+            return fail(h, RP_ERR_UNSUPPORTED,
+                        "box too small: the reference keeps no neighbour grid and pairs have several images in range");
     }
     int64_t ncell = static_cast<int64_t>(dims[0]) * dims[1] * dims[2];
     if (ncell > (1ll << 30)) return fail(h, RP_ERR_UNSUPPORTED, "too many cells");

@@ -69,6 +69,7 @@ struct Version {
 __device__ __forceinline__ bool overlaps_pair(const DevState &s, d3 pi, const double *ri, const double *ai, int64_t j,
                                               const Version &v) {
     d3 pj = ld3(s.pos64 + 3 * j);
+    if (s.ncen == 0 && s.kind == 0 && s.pbc_fold) return pbc_distance2(s.box, s.inv, pi, pj) < s.ex.sphere_thr;
     if (s.ncen == 0) {
         d3 t = pbc_translation(s.box, s.inv, pi, pj);
         const double *rj = v.rot + 9 * j;
@@ -78,6 +79,10 @@ __device__ __forceinline__ bool overlaps_pair(const DevState &s, d3 pi, const do
         d3 pa = ld3(ai + 3 * a);
         for (int b = 0; b < s.ncen; b++) {
             d3 pb = ld3(v.abs + 3 * ((size_t)j * s.ncen + b));
+            if (s.pbc_fold) {
+                if (pbc_distance2(s.box, s.inv, pa, pb) < s.cthr64[a * MAX_CEN + b]) return true;
+                continue;
+            }
             d3 t = pbc_translation(s.box, s.inv, pa, pb);
             if (norm2(sub3(add3(pb, t), pa)) < s.cthr64[a * MAX_CEN + b]) return true;
         }

@@ -136,6 +136,20 @@ RP_HD d3 pbc_translation(const double *box, const double *inv, d3 p1, d3 p2) {
     return mv3(box, d3{t[0], t[1], t[2]});
 }
 
+// core/PeriodicBoundaryConditions.cpp:38-50 — the distance^2 the reference uses for sphere
+// centres when it keeps no neighbour grid: per relative coordinate |r2 - r1| folded down
+// by whole boxes into (-1/2, 1/2], back to absolute coordinates, squared norm.
+RP_HD double pbc_distance2(const double *box, const double *inv, d3 p1, d3 p2) {
+    d3 r1 = mv3(inv, p1), r2 = mv3(inv, p2);
+    double a[3] = {r1.x, r1.y, r1.z}, b[3] = {r2.x, r2.y, r2.z}, d[3];
+    for (int i = 0; i < 3; i++) {
+        double c = fabs(dsub(b[i], a[i]));
+        while (c > 0.5) c = dsub(c, 1.0);
+        d[i] = c;
+    }
+    return norm2(mv3(box, d3{d[0], d[1], d[2]}));
+}
+
 // core/ActiveDomain.cpp:8-21 — strict bounds in relative coordinates; end <= beg wraps.
 RP_HD bool inside_domain(const double *inv, d3 pos, const double *lo, const double *hi) {
     d3 rel = mv3(inv, pos);

@@ -84,6 +84,10 @@ struct DevState {
     double *cen64;                 // [n][ncen][3]
     double *abs64;                 // [n][ncen][3] (position + centre, wrapped into the box)
     const double *cthr64;          // [MAX_CEN^2] (r_a + r_b)^2, FP64 as the reference forms it
+    // 1 when the reference keeps no neighbour grid for this box (core/Packing.cpp:862-881):
+    // it then measures sphere and polysphere-centre distances with the periodic boundary
+    // conditions' own formula (pbc_distance2) instead of a cell translation
+    int pbc_fold;
 };
 
 constexpr int MAX_CEN = RP_MAX_CENTRES;

@@ -138,6 +138,7 @@ __device__ __forceinline__ bool exact_pair(const DevState &s, d3 pi, d3 ai, int 
     d3 pj = load_d3(s.pos64 + 3 * (size_t)pid_j);
     const double *rj = s.rot64 + 9 * (size_t)pid_j;
     d3 aj = d3{rj[2], rj[5], rj[8]};
+    if (s.kind == 0 && s.pbc_fold) return pbc_distance2(s.box, s.inv, pi, pj) < s.ex.sphere_thr;
     int m = image_index(s, dsep, pi, pj);
     d3 t = load_d3(s.trans + 3 * m);
     return exact_overlap(s.ex, pi, ai, pj, aj, t);
@@ -419,6 +420,7 @@ template __global__ void k_count<1>(DevState, GridDev, int, unsigned long long *
 // core/shapes/PolysphereTraits.cpp:97-106) with t the box translation of that image.
 __device__ __forceinline__ bool exact_centre_pair(const DevState &s, d3 pa, int a, int pid_j, int j, float3 dsep) {
     d3 pb = load_d3(s.abs64 + 3 * ((size_t)pid_j * s.ncen + j));
+    if (s.pbc_fold) return pbc_distance2(s.box, s.inv, pa, pb) < s.cthr64[a * MAX_CEN + j];
     int m = image_index(s, dsep, pa, pb);
     d3 t = load_d3(s.trans + 3 * m);
     d3 d = sub3(add3(pb, t), pa);

@@ -71,6 +71,21 @@ def poly_dense():
     return thermalise(W.bananas((8, 10, 6), 0.45, **BANANA), 10, translation_step=0.2, rotation_step=0.2)
 
 
+@functools.lru_cache(maxsize=None)
+def hs_tiny():
+    """Hard spheres d=1, N=27 in a 3.9^3 box: the reference keeps no neighbour grid here."""
+    return thermalise((W.SPHERE, np.array([0.5]), W.lattice((3, 3, 3), (1.3, 1.3, 1.3)), W.aligned_rotations(27),
+                       W.diag_box(3.9, 3.9, 3.9)), 20, translation_step=0.1)
+
+
+@functools.lru_cache(maxsize=None)
+def sc_tiny():
+    """Spherocylinders l=3 r=0.5, N=50 in a 10^3 box (no neighbour grid in the reference), 20 NVT cycles."""
+    return thermalise((W.SPHEROCYLINDER, np.array([3.0, 0.5]), W.lattice((5, 5, 2), (2.0, 2.0, 5.0)),
+                       W.aligned_rotations(50), W.diag_box(10.0, 10.0, 10.0)), 20,
+                      translation_step=0.5, rotation_step=0.5)
+
+
 def compressed(cfg, factor: float):
     """The same configuration with box and positions scaled by `factor` (overlaps for factor < 1)."""
     kind, prm, pos, rot, box = cfg
@@ -82,4 +97,4 @@ def compressed(cfg, factor: float):
 
 
 ALL = {"hs_small": hs_small, "hs_dense": hs_dense, "sc_l2": sc_l2, "sc_l2_dense": sc_l2_dense, "sc_l5": sc_l5,
-       "poly_banana": poly_banana, "poly_dense": poly_dense}
+       "poly_banana": poly_banana, "poly_dense": poly_dense, "hs_tiny": hs_tiny, "sc_tiny": sc_tiny}

@@ -14,7 +14,7 @@ from rampack_gb300 import _lib
 
 pytestmark = pytest.mark.gpu
 
-CASES = ["hs_small", "hs_dense", "sc_l2", "sc_l2_dense", "sc_l5", "poly_banana", "poly_dense"]
+CASES = ["hs_small", "hs_dense", "sc_l2", "sc_l2_dense", "sc_l5", "poly_banana", "poly_dense", "hs_tiny", "sc_tiny"]
 
 
 def gpu_packing(cfg):
