@@ -7,188 +7,16 @@
 //   * FP64 box rescale.
 #include <cuda_runtime.h>
 
-#include "rp_internal.cuh"
+#include "rp_sweep.cuh"
 
 namespace rp {
-
-__device__ __forceinline__ int wrap_cell(int c, int n) { return c < 0 ? c + n : (c >= n ? c - n : c); }
-
-// Neighbour enumeration: lane 0 is the cell itself, lanes 1..26 the other offsets.
-__device__ __forceinline__ void lane_offset(int lane, int &ox, int &oy, int &oz) {
-    int t = lane == 0 ? 13 : (lane <= 13 ? lane - 1 : lane);
-    ox = t % 3 - 1;
-    oy = (t / 3) % 3 - 1;
-    oz = t / 9 - 1;
-}
-
-__device__ __forceinline__ float3 mat32(const float *m, float x, float y, float z) {
-    return make_float3(fmaf(m[0], x, fmaf(m[1], y, m[2] * z)), fmaf(m[3], x, fmaf(m[4], y, m[5] * z)),
-                       fmaf(m[6], x, fmaf(m[7], y, m[8] * z)));
-}
-
-__device__ __forceinline__ float dot3f(float3 a, float3 b) { return fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)); }
-
-// ---------------------------------------------------------------------------------
-// FP32 classification of one pair.  0: no overlap, 1: overlap, 2: undecided in FP32
-// (re-decided in FP64).  d = p_j - p_i (candidate minus mover), a_i/a_j unit axes.
-// ---------------------------------------------------------------------------------
-// Centre-distance stage: 0 no overlap, 1 overlap, 2 undecided (FP64), 3 needs the
-// segment stage (spherocylinders).
-template <int KIND>
-__device__ __forceinline__ int d2_stage(const FilterConsts &fc, float d2) {
-    if (KIND == 0) {
-        if (d2 < fc.sphere_lo) return 1;
-        if (d2 > fc.sphere_hi) return 0;
-        return 2;
-    } else if (KIND == 2) {
-        // polyspheres: bodies farther apart than twice the largest centre reach cannot
-        // touch; closer ones go to the sphere-pair stage
-        return d2 > fc.far_hi ? 0 : 3;
-    } else {
-        if (d2 > fc.far_hi) return 0;
-        if (d2 < fc.core_lo) return 1;
-        if (d2 < fc.core_hi || d2 > fc.far_lo) return 2;
-        return 3;
-    }
-}
-
-// Segment stage of a spherocylinder pair: the closest points of the two axes (same
-// branch structure as the FP64 reference), then a convexity certificate: for any feasible
-// (s, t), f* >= f(s, t) - G with G the Frank-Wolfe gap of the box-constrained quadratic.
-// 0 no overlap, 1 overlap, 2 undecided (FP64).  d = p_j - p_i, ai/aj unit axes.
-__device__ __forceinline__ int seg_stage(const FilterConsts &fc, float3 d, float3 ai, float3 aj) {
-    const float l = fc.len, h = fc.half_len;
-    float3 u = make_float3(l * ai.x, l * ai.y, l * ai.z);
-    float3 v = make_float3(l * aj.x, l * aj.y, l * aj.z);
-    float3 w = make_float3(-d.x - h * (ai.x - aj.x), -d.y - h * (ai.y - aj.y), -d.z - h * (ai.z - aj.z));
-    float a = dot3f(u, u), b = dot3f(u, v), c = dot3f(v, v), dd = dot3f(u, w), e = dot3f(v, w);
-    // D = |u|^2 |v|^2 - (u.v)^2 = |u x v|^2, evaluated without cancellation: nearly parallel
-    // axes (D below d_min) are left to FP64, whose own parameter error grows like 1/D
-    float3 cr = make_float3(fmaf(u.y, v.z, -u.z * v.y), fmaf(u.z, v.x, -u.x * v.z), fmaf(u.x, v.y, -u.y * v.x));
-    float D = dot3f(cr, cr);
-    // axes parallel to within d_par: the FP64 reference certainly takes its parallel branch
-    // (D < 1e-10: closest points from the s = 0 end), whose distance exceeds the true
-    // minimum by at most par_err; in between the two thresholds FP64 decides
-    const bool par = D < fc.d_par;
-    if (!par && D < fc.d_min) return 2;
-    float sN, tN, sD, tD;
-    if (par) {
-        sN = 0.f; sD = 1.f; tN = e; tD = c;
-    } else {
-        sN = fmaf(b, e, -c * dd);
-        tN = fmaf(a, e, -b * dd);
-        sD = D;
-        tD = D;
-        if (sN < 0.f) {
-            sN = 0.f; tN = e; tD = c;
-        } else if (sN > sD) {
-            sN = sD; tN = e + b; tD = c;
-        }
-    }
-    if (tN < 0.f) {
-        tN = 0.f;
-        if (-dd < 0.f) sN = 0.f;
-        else if (-dd > a) sN = sD;
-        else { sN = -dd; sD = a; }
-    } else if (tN > tD) {
-        tN = tD;
-        if (b - dd < 0.f) sN = 0.f;
-        else if (b - dd > a) sN = sD;
-        else { sN = b - dd; sD = a; }
-    }
-    float sc = fminf(fmaxf(__fdividef(sN, sD), 0.f), 1.f);
-    float tc = fminf(fmaxf(__fdividef(tN, tD), 0.f), 1.f);
-    float3 dP = make_float3(fmaf(sc, u.x, fmaf(-tc, v.x, w.x)), fmaf(sc, u.y, fmaf(-tc, v.y, w.y)),
-                            fmaf(sc, u.z, fmaf(-tc, v.z, w.z)));
-    float f = dot3f(dP, dP);
-    float gs = dot3f(dP, u), gt = -dot3f(dP, v);
-    float G = 2.f * (gs * sc - fminf(gs, 0.f) + gt * tc - fminf(gt, 0.f));
-    const float err = par ? fc.seg_err + fc.par_err : fc.seg_err;
-    if (f + err < fc.core_thr) return 1;
-    if (f - G - err >= fc.core_thr) return 0;
-    return 2;
-}
-
-// FP32 classification of one pair: 0 no overlap, 1 overlap, 2 undecided in FP32.
-template <int KIND>
-__device__ __forceinline__ int classify(const FilterConsts &fc, float3 d, float3 ai, float3 aj) {
-    int cls = d2_stage<KIND>(fc, dot3f(d, d));
-    if (KIND == 1 && cls == 3) cls = seg_stage(fc, d, ai, aj);
-    return cls;
-}
-
-// Image of candidate j relative to mover i, recovered from the FP32 separation dsep
-// (candidate minus mover, in the right image) and the FP64 positions: the integer box
-// translation m with p_j + box·m - p_i ≈ dsep.  Returns the index into the translation table.
-__device__ __forceinline__ int image_index(const DevState &s, float3 dsep, d3 pi, d3 pj) {
-    float3 raw = make_float3(static_cast<float>(pj.x - pi.x), static_cast<float>(pj.y - pi.y),
-                             static_cast<float>(pj.z - pi.z));
-    float3 rel = mat32(s.inv32, dsep.x - raw.x, dsep.y - raw.y, dsep.z - raw.z);
-    int mx = __float2int_rn(rel.x), my = __float2int_rn(rel.y), mz = __float2int_rn(rel.z);
-    mx = max(-2, min(2, mx));
-    my = max(-2, min(2, my));
-    mz = max(-2, min(2, mz));
-    return ((mx + 2) * 5 + (my + 2)) * 5 + (mz + 2);
-}
-
-__device__ __forceinline__ d3 load_d3(const double *p) { return d3{p[0], p[1], p[2]}; }
-
-// Exact FP64 test of mover (pi, ai) against particle pid_j seen at FP32 separation dsep.
-__device__ __forceinline__ bool exact_pair(const DevState &s, d3 pi, d3 ai, int pid_j, float3 dsep) {
-    d3 pj = load_d3(s.pos64 + 3 * (size_t)pid_j);
-    const double *rj = s.rot64 + 9 * (size_t)pid_j;
-    d3 aj = d3{rj[2], rj[5], rj[8]};
-    if (s.kind == 0 && s.pbc_fold) return pbc_distance2(s.box, s.inv, pi, pj) < s.ex.sphere_thr;
-    int m = image_index(s, dsep, pi, pj);
-    d3 t = load_d3(s.trans + 3 * m);
-    return exact_overlap(s.ex, pi, ai, pj, aj, t);
-}
 
 // ---------------------------------------------------------------------------------
 // Cell-list rebuild
 // ---------------------------------------------------------------------------------
 __global__ void k_assign(DevState s, GridDev g) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= s.n) return;
-    d3 p = load_d3(s.pos64 + 3 * i);
-    d3 r = mv3(s.inv, p);
-    double rr[3] = {r.x, r.y, r.z};
-    // core/Packing.cpp:1069-1075 (areShapesWithinBox): relative coordinates in [0, 1)
-    if (s.strict_box) {
-        if (!(rr[0] >= 0.0 && rr[0] < 1.0 && rr[1] >= 0.0 && rr[1] < 1.0 && rr[2] >= 0.0 && rr[2] < 1.0))
-            atomicOr(s.status, ST_OUTSIDE);
-        // the engine's cell sizes and FP32 margins take orientations to be rotations: a
-        // unit axis (spherocylinders) or an orthonormal matrix (polyspheres)
-        const double *o = s.rot64 + 9 * i;
-        bool bad = false;
-        for (int a = 0; a < 3; a++)
-            for (int b = a; b < 3; b++) {
-                if (s.kind == 1 && (a != 2 || b != 2)) continue;
-                if (s.kind == 0) continue;
-                double g2 = o[a] * o[b] + o[3 + a] * o[3 + b] + o[6 + a] * o[6 + b];
-                if (!(fabs(g2 - (a == b ? 1.0 : 0.0)) < 1e-6)) bad = true;
-            }
-        if (bad) atomicOr(s.status, ST_NOT_ROTATION);
-    } else if (!(fabs(rr[0] - 0.5) < 0.5 + 1e-9 && fabs(rr[1] - 0.5) < 0.5 + 1e-9 && fabs(rr[2] - 0.5) < 0.5 + 1e-9)) {
-        atomicOr(s.status, ST_NUMERIC);  // rescaled positions drift at most a few ulp outside
-    }
-    int c[3];
-    float f[3];
-    for (int d = 0; d < 3; d++) {
-        double u = rr[d] - g.shift[d];
-        if (u < 0.0) u += 1.0;
-        double un = u * g.dims[d];
-        int cd = static_cast<int>(un);
-        if (cd >= g.dims[d]) cd = g.dims[d] - 1;
-        if (cd < 0) cd = 0;
-        c[d] = cd;
-        f[d] = static_cast<float>(un - cd);
-    }
-    int cell = c[0] + g.dims[0] * (c[1] + g.dims[1] * c[2]);
-    float3 loc = mat32(g.cellmat, f[0], f[1], f[2]);
-    g.plocal[i] = make_float4(loc.x, loc.y, loc.z, 0.f);
-    g.pid_cell[i] = cell;
-    g.rank[i] = atomicAdd(g.count + cell, 1);
+    if (i < s.n) assign_one(s, g, i);
 }
 
 // Two-level exclusive scan of the cell counts (4096 cells per block).
@@ -251,38 +79,14 @@ __global__ void k_scan_add(int32_t *start, const int32_t *block_sums, int ncell)
 
 __global__ void k_scatter(DevState s, GridDev g) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= s.n) return;
-    g.slot_pid[g.start[g.pid_cell[i]] + g.rank[i]] = static_cast<int32_t>(i);
+    if (i < s.n) scatter_one(g, i);
 }
 
 // Sorts each cell's particles by index (a deterministic order independent of the
 // atomic arrival order) and writes the FP32 mirror in cell order.
 __global__ void k_cell_finish(DevState s, GridDev g) {
     int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= g.ncell) return;
-    int b = g.start[cell], e = g.start[cell + 1];
-    for (int k = b + 1; k < e; k++) {
-        int v = g.slot_pid[k];
-        int j = k - 1;
-        while (j >= b && g.slot_pid[j] > v) {
-            g.slot_pid[j + 1] = g.slot_pid[j];
-            j--;
-        }
-        g.slot_pid[j + 1] = v;
-    }
-    for (int k = b; k < e; k++) {
-        int pid = g.slot_pid[k];
-        g.pid_slot[pid] = k;
-        float4 l = g.plocal[pid];
-        g.mpos[k] = make_float4(l.x, l.y, l.z, __int_as_float(pid));
-        const double *r = s.rot64 + 9 * (size_t)pid;
-        g.maxis[k] = make_float4(static_cast<float>(r[2]), static_cast<float>(r[5]), static_cast<float>(r[8]), 0.f);
-        for (int b = 0; b < s.ncen; b++) {
-            const double *c = s.cen64 + 3 * ((size_t)pid * s.ncen + b);
-            g.mcen[(size_t)k * s.ncen + b] =
-                make_float4(static_cast<float>(c[0]), static_cast<float>(c[1]), static_cast<float>(c[2]), 0.f);
-        }
-    }
+    if (cell < g.ncell) finish_one(s, g, cell);
 }
 
 // Absolute centres of every polysphere (Packing::recalculateAbsoluteInteractionCentres,
@@ -357,809 +161,18 @@ __global__ void k_rescale(const double *src, double *dst, int64_t n, Mat9 old_in
 template <int KIND>
 __global__ void k_count(DevState s, GridDev g, int early, unsigned long long *out, int *flag) {
     int64_t slot = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (slot >= s.n) return;
-    float4 pi4 = g.mpos[slot];
-    int pid = __float_as_int(pi4.w);
-    int cell = g.pid_cell[pid];
-    int cx = cell % g.dims[0], cy = (cell / g.dims[0]) % g.dims[1], cz = cell / (g.dims[0] * g.dims[1]);
-    float3 ai = make_float3(0.f, 0.f, 0.f);
-    if (KIND == 1) {
-        float4 a = g.maxis[slot];
-        ai = make_float3(a.x, a.y, a.z);
-    }
-    unsigned long long cnt = 0;
-    bool have64 = false;
-    d3 pi64{0, 0, 0}, ai64{0, 0, 0};
-    for (int o = 0; o < 27; o++) {
-        if (early && *(volatile int *)flag) break;
-        int ox = o % 3 - 1, oy = (o / 3) % 3 - 1, oz = o / 9 - 1;
-        int nb = wrap_cell(cx + ox, g.dims[0]) +
-                 g.dims[0] * (wrap_cell(cy + oy, g.dims[1]) + g.dims[1] * wrap_cell(cz + oz, g.dims[2]));
-        float3 off = mat32(g.cellmat, (float)ox, (float)oy, (float)oz);
-        int b = g.start[nb], e = g.start[nb + 1];
-        for (int k = b; k < e; k++) {
-            float4 q = g.mpos[k];
-            int pj = __float_as_int(q.w);
-            if (pj <= pid) continue;
-            float3 dsep = make_float3((q.x + off.x) - pi4.x, (q.y + off.y) - pi4.y, (q.z + off.z) - pi4.z);
-            float3 aj = make_float3(0.f, 0.f, 0.f);
-            if (KIND == 1) {
-                float4 a = g.maxis[k];
-                aj = make_float3(a.x, a.y, a.z);
-            }
-            int cls = classify<KIND>(s.fc, dsep, ai, aj);
-            bool ov = cls == 1;
-            if (cls == 2) {
-                if (!have64) {
-                    pi64 = load_d3(s.pos64 + 3 * (size_t)pid);
-                    const double *r = s.rot64 + 9 * (size_t)pid;
-                    ai64 = d3{r[2], r[5], r[8]};
-                    have64 = true;
-                }
-                atomicAdd(s.counters + 5, 1ull);
-                ov = exact_pair(s, pi64, ai64, pj, dsep);
-            }
-            if (ov) {
-                cnt++;
-                if (early) {
-                    atomicExch(flag, 1);
-                    break;
-                }
-            }
-        }
-    }
-    if (cnt) atomicAdd(out, cnt);
+    if (slot < s.n) count_one<KIND>(s, g, slot, early, out, flag);
 }
 
 template __global__ void k_count<0>(DevState, GridDev, int, unsigned long long *, int *);
 template __global__ void k_count<1>(DevState, GridDev, int, unsigned long long *, int *);
-
-// Exact FP64 test of centre a of a body, at absolute position pa, against centre j of
-// body pid_j seen at FP32 separation dsep (candidate minus mover): the reference's
-// (pos2 + t - pos1).norm2() < (r_a + r_j)^2 (core/Packing.cpp:40-42,
-// core/shapes/PolysphereTraits.cpp:97-106) with t the box translation of that image.
-__device__ __forceinline__ bool exact_centre_pair(const DevState &s, d3 pa, int a, int pid_j, int j, float3 dsep) {
-    d3 pb = load_d3(s.abs64 + 3 * ((size_t)pid_j * s.ncen + j));
-    if (s.pbc_fold) return pbc_distance2(s.box, s.inv, pa, pb) < s.cthr64[a * MAX_CEN + j];
-    int m = image_index(s, dsep, pa, pb);
-    d3 t = load_d3(s.trans + 3 * m);
-    d3 d = sub3(add3(pb, t), pa);
-    return norm2(d) < s.cthr64[a * MAX_CEN + j];
-}
 
 // All-pairs recount of polyspheres: one thread per body; every unordered body pair and
 // periodic image once, every pair of their centres (the count of overlapping centre pairs,
 // as the reference's countTotalOverlaps counts them, core/Packing.cpp:468-512).
 __global__ void k_count_poly(DevState s, GridDev g, int early, unsigned long long *out, int *flag) {
     int64_t slot = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (slot >= s.n) return;
-    const int K = s.ncen;
-    float4 pi4 = g.mpos[slot];
-    int pid = __float_as_int(pi4.w);
-    int cell = g.pid_cell[pid];
-    int cx = cell % g.dims[0], cy = (cell / g.dims[0]) % g.dims[1], cz = cell / (g.dims[0] * g.dims[1]);
-    unsigned long long cnt = 0;
-    for (int o = 0; o < 27; o++) {
-        if (early && *(volatile int *)flag) break;
-        int ox = o % 3 - 1, oy = (o / 3) % 3 - 1, oz = o / 9 - 1;
-        int nb = wrap_cell(cx + ox, g.dims[0]) +
-                 g.dims[0] * (wrap_cell(cy + oy, g.dims[1]) + g.dims[1] * wrap_cell(cz + oz, g.dims[2]));
-        float3 off = mat32(g.cellmat, (float)ox, (float)oy, (float)oz);
-        int b = g.start[nb], e = g.start[nb + 1];
-        for (int k = b; k < e; k++) {
-            float4 q = g.mpos[k];
-            int pj = __float_as_int(q.w);
-            if (pj <= pid) continue;
-            float3 dq = make_float3((q.x + off.x) - pi4.x, (q.y + off.y) - pi4.y, (q.z + off.z) - pi4.z);
-            if (dot3f(dq, dq) > s.fc.far_hi) continue;
-            for (int j = 0; j < K; j++) {
-                float4 cj = g.mcen[(size_t)k * K + j];
-                float3 bj = make_float3(dq.x + cj.x, dq.y + cj.y, dq.z + cj.z);
-                for (int a = 0; a < K; a++) {
-                    float4 ca = g.mcen[(size_t)slot * K + a];
-                    float3 d = make_float3(bj.x - ca.x, bj.y - ca.y, bj.z - ca.z);
-                    float d2 = dot3f(d, d);
-                    bool ov = d2 < g.cthr[a * MAX_CEN + j];
-                    if (!ov && d2 <= g.cthr[MAX_CEN * MAX_CEN + a * MAX_CEN + j]) {
-                        atomicAdd(s.counters + 5, 1ull);
-                        ov = exact_centre_pair(s, load_d3(s.abs64 + 3 * ((size_t)pid * K + a)), a, pj, j, d);
-                    }
-                    if (ov) {
-                        cnt++;
-                        if (early) {
-                            atomicExch(flag, 1);
-                            atomicAdd(out, cnt);
-                            return;
-                        }
-                    }
-                }
-            }
-        }
-    }
-    if (cnt) atomicAdd(out, cnt);
-}
-
-// ---------------------------------------------------------------------------------
-// Checkerboard sweep: one warp per active cell.
-//
-// Per move, all lanes draw (or read) the same proposal; the FP32 pass tests the staged
-// neighbourhood 32 candidates at a time with a ballot for the early exit.  Pass 1 decides
-// on the centre distance alone and compacts the spherocylinder pairs that need the
-// segment test into a shared-memory queue, so that pass 2 runs the segment test on full
-// warps.  Pairs the FP32 filter cannot decide go to a second queue; only a move that
-// survives the FP32 filter builds its exact FP64 state (one box row per lane, one matrix
-// entry per lane), re-decides the queued pairs in FP64 and, when accepted, writes back.
-// ---------------------------------------------------------------------------------
-struct WarpStats {
-    unsigned moves, accepted, rej_overlap, rej_domain, pairs, fp64, trans, rots;
-};
-
-template <int KIND, bool LIST, bool LEARN>
-__device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, float4 *cpos, float4 *cax,
-                                           uint16_t *qseg, uint16_t *qun, uint8_t *nacc, uint16_t *pstage,
-                                           float *ccen, float4 *wx, WarpStats &ws) {
-    const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const unsigned lt = (1u << lane) - 1u;
-    const DevState &S = A.s;
-    const GridDev &G = A.g;
-
-    // ---- which cell ----
-    int cell, c[3];
-    if (A.work) {
-        cell = A.work[item];
-    } else if (LIST) {
-        cell = A.list_cells[item];
-    } else {
-        int w = item;
-        int a0 = w % A.active[0];
-        w /= A.active[0];
-        int a1 = w % A.active[1];
-        int a2 = w / A.active[1];
-        int cc[3] = {a0, a1, a2};
-        for (int d = 0; d < 3; d++) c[d] = G.dims[d] == 1 ? 0 : 2 * cc[d] + A.phase[d];
-        cell = c[0] + G.dims[0] * (c[1] + G.dims[1] * c[2]);
-    }
-    c[0] = cell % G.dims[0];
-    c[1] = (cell / G.dims[0]) % G.dims[1];
-    c[2] = cell / (G.dims[0] * G.dims[1]);
-
-    // ---- stage the 3x3x3 neighbourhood (own cell first) ----
-    int cnt = 0, st = 0;
-    float3 off = make_float3(0.f, 0.f, 0.f);
-    if (lane < 27) {
-        int ox, oy, oz;
-        lane_offset(lane, ox, oy, oz);
-        int nb = wrap_cell(c[0] + ox, G.dims[0]) +
-                 G.dims[0] * (wrap_cell(c[1] + oy, G.dims[1]) + G.dims[1] * wrap_cell(c[2] + oz, G.dims[2]));
-        st = G.start[nb];
-        cnt = G.start[nb + 1] - st;
-        off = mat32(G.cellmat, (float)ox, (float)oy, (float)oz);
-    }
-    int incl = cnt;
-    for (int d = 1; d < 32; d <<= 1) {
-        int y = __shfl_up_sync(FULL, incl, d);
-        if (lane >= d) incl += y;
-    }
-    const int total = __shfl_sync(FULL, incl, 31);
-    const int occ = __shfl_sync(FULL, cnt, 0);
-    const int gbase = __shfl_sync(FULL, st, 0);
-    if (total > A.cap) {
-        if (lane == 0) {
-            if (A.overflow) {
-                int k = atomicAdd(A.overflow_count, 1);
-                A.overflow[k] = cell;
-            } else {
-                atomicOr(S.status, ST_CAPACITY);
-            }
-        }
-        return;
-    }
-    {
-        int base = incl - cnt;
-        for (int k = 0; k < cnt; k++) {
-            float4 p = G.mpos[st + k];
-            p.x += off.x;
-            p.y += off.y;
-            p.z += off.z;
-            cpos[base + k] = p;
-            if (KIND == 1) cax[base + k] = G.maxis[st + k];
-            if (KIND == 2) {
-                for (int b = 0; b < S.ncen; b++) {
-                    float4 c = G.mcen[(size_t)(st + k) * S.ncen + b];
-                    float *dst = ccen + 3 * ((size_t)(base + k) * S.ncen + b);
-                    dst[0] = c.x;
-                    dst[1] = c.y;
-                    dst[2] = c.z;
-                }
-            }
-        }
-    }
-    // polyspheres: the warp's scratch holds the mover's FP32 centres (wx[0..K)), the
-    // centre-pair thresholds (lo, hi) and the mover's exact new centres and absolute centres
-    float *wthr = reinterpret_cast<float *>(wx + MAX_CEN);
-    double *wabs = reinterpret_cast<double *>(wx + MAX_CEN + MAX_CEN * MAX_CEN / 2);
-    double *wcen = wabs + 3 * MAX_CEN;
-    if (KIND == 2)
-        for (int t = lane; t < 2 * MAX_CEN * MAX_CEN; t += 32) wthr[t] = G.cthr[t];
-    const bool self_images = (G.dims[0] == 1) || (G.dims[1] == 1) || (G.dims[2] == 1);
-    // per own-cell particle: FP32 roundings accumulated in its mirror position this sweep
-    for (int k = lane; k < occ; k += 32) nacc[k] = 0;
-    if (LEARN && A.partners) {
-        // the ranked partners of the cell's particles, as indices into the staged
-        // neighbourhood (a partner out of reach of this cell's neighbourhood gets none)
-        const int base_nb = incl - cnt;
-        for (int eb = 0; eb < occ * MLP_PARTNERS; eb += 32) {
-            const int e = eb + lane;
-            int sj = -1;
-            if (e < occ * MLP_PARTNERS) {
-                const int pk = __float_as_int(cpos[e / MLP_PARTNERS].w);
-                const int pj = A.partners[MLP_PARTNERS * (size_t)pk + e % MLP_PARTNERS];
-                if (pj >= 0) sj = G.pid_slot[pj];
-            }
-            int idx = 0xffff;
-            for (int nb = 0; nb < 27; nb++) {
-                const int s0 = __shfl_sync(FULL, st, nb), c0 = __shfl_sync(FULL, cnt, nb),
-                          b0 = __shfl_sync(FULL, base_nb, nb);
-                if (idx == 0xffff && sj >= s0 && sj < s0 + c0) idx = b0 + sj - s0;
-            }
-            if (e < occ * MLP_PARTNERS) pstage[e] = (uint16_t)idx;
-        }
-    }
-    __syncwarp();
-
-    // this lane's dimension (lanes 0-2): ActiveDomain bounds and cell coordinate
-    const int ld = lane < 3 ? lane : 0;
-    const int c_ld = ld == 0 ? c[0] : (ld == 1 ? c[1] : c[2]);
-    const int dims_ld = ld == 0 ? G.dims[0] : (ld == 1 ? G.dims[1] : G.dims[2]);
-    const int boff_ld = ld == 0 ? G.boundsoff[0] : (ld == 1 ? G.boundsoff[1] : G.boundsoff[2]);
-    const double shift_ld = ld == 0 ? G.shift[0] : (ld == 1 ? G.shift[1] : G.shift[2]);
-    const double lo_d = G.bounds[boff_ld + 2 * c_ld];
-    const double hi_d = G.bounds[boff_ld + 2 * c_ld + 1];
-    // this lane's matrix entry (lanes 0-8)
-    const int ei = lane < 9 ? lane / 3 : 0, ej = lane < 9 ? lane % 3 : 0;
-
-    int nmoves, mbeg = 0;
-    if (LIST) {
-        int li = A.work ? -1 : item;
-        if (A.work) {
-            for (int q = 0; q < A.num_list; q++)
-                if (A.list_cells[q] == cell) li = q;
-        }
-        mbeg = A.list_begin[li];
-        nmoves = A.list_begin[li + 1] - mbeg;
-    } else {
-        nmoves = ((A.types & 1) + ((A.types >> 1) & 1)) * occ;
-    }
-    const int ntypes = (A.types & 1) + ((A.types >> 1) & 1);
-
-    u4 rnd_lane = u4{0u, 0u, 0u, 0u};  // Philox output of move (batch base + lane)
-    for (int mi = 0; mi < nmoves; mi++) {
-        if (!LIST && (mi & 31) == 0) {
-            // draw the next 32 moves' random words at once, one move per lane
-            rnd_lane = philox(u4{(uint32_t)(mi + lane), (uint32_t)cell, (uint32_t)A.counter,
-                                 (uint32_t)(A.counter >> 32)},
-                              (uint32_t)A.seed, (uint32_t)(A.seed >> 32));
-        }
-        // ---- the proposal (FP32 view; FP64 inputs kept for the exact path) ----
-        int type, slot = -1, out_index = -1;
-        double uni = 0.5;
-        double t64_lane = 0.0;      // translation component of this lane's dimension
-        float3 t32 = make_float3(0.f, 0.f, 0.f);
-        float R32[9];
-        uint32_t rot_idx = 0;       // drawn rotation: table entry and transpose flag
-        bool rot_inv = false;
-        const rp_move *mrec = nullptr;
-        if (LIST) {
-            out_index = A.move_out[mbeg + mi];
-            mrec = A.moves + out_index;
-            type = mrec->type;
-            int want = mrec->particle;
-            for (int kb = 0; kb < occ; kb += 32) {
-                int k = kb + lane;
-                bool hit = k < occ && __float_as_int(cpos[k].w) == want;
-                unsigned bal = __ballot_sync(FULL, hit);
-                if (bal) {
-                    slot = kb + __ffs(bal) - 1;
-                    break;
-                }
-            }
-            if (slot < 0) {
-                if (lane == 0) {
-                    atomicOr(S.status, ST_PARTICLE_NOT_IN_CELL);
-                    if (A.codes) A.codes[out_index] = 0xff;
-                }
-                continue;
-            }
-            t32 = make_float3((float)mrec->translation[0], (float)mrec->translation[1], (float)mrec->translation[2]);
-            t64_lane = mrec->translation[ld];
-            uni = mrec->uniform;
-            for (int q = 0; q < 9; q++) R32[q] = (float)mrec->rotation[q];
-        } else {
-            const int src = mi & 31;
-            u4 r = u4{__shfl_sync(FULL, rnd_lane.a, src), __shfl_sync(FULL, rnd_lane.b, src),
-                      __shfl_sync(FULL, rnd_lane.c, src), __shfl_sync(FULL, rnd_lane.d, src)};
-            if (ntypes == 2) type = (r.a >> 31) ? 1 : 0;
-            else type = (A.types & 1) ? 0 : 1;
-            slot = (int)(((uint64_t)(r.a & 0x7fffffffu) * (uint32_t)occ) >> 31);
-            if (type == 0) {
-                t32 = make_float3(pm1f(r.b) * A.tstep, pm1f(r.c) * A.tstep, pm1f(r.d) * A.tstep);
-                t64_lane = ld == 0 ? (double)t32.x : (ld == 1 ? (double)t32.y : (double)t32.z);
-            } else {
-                // a rotation of this sweep's table, or its transpose (the inverse)
-                rot_idx = r.b & A.rtab_mask;
-                rot_inv = (r.c & 1u) != 0;
-                if (KIND >= 1) {
-                    const float4 *R4 = reinterpret_cast<const float4 *>(A.rtab32) + 3 * (size_t)rot_idx;
-                    float4 x0 = R4[0], x1 = R4[1], x2 = R4[2];
-                    float R[9] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w, x2.x};
-                    for (int q = 0; q < 9; q++) R32[q] = rot_inv ? R[3 * (q % 3) + q / 3] : R[q];
-                }
-            }
-        }
-        const float4 pcur = cpos[slot];
-        const int pid = __float_as_int(pcur.w);
-        // the mover's FP64 state, loaded now and first used after the FP32 filter:
-        // lanes 0-2 hold the position, lanes 0-8 the orientation entries
-        const double pos_own = S.pos64[3 * (size_t)pid + ld];
-        const double rot_own = S.rot64[9 * (size_t)pid + (lane < 9 ? lane : 0)];
-        float3 ai = make_float3(0.f, 0.f, 1.f);
-        if (KIND == 1) {
-            float4 a = cax[slot];
-            ai = make_float3(a.x, a.y, a.z);
-        }
-        float3 pn = make_float3(pcur.x, pcur.y, pcur.z);
-        float3 an = ai;
-        if (type != 1) pn = make_float3(pcur.x + t32.x, pcur.y + t32.y, pcur.z + t32.z);
-        if (type != 0 && KIND == 1) an = mat32(R32, ai.x, ai.y, ai.z);
-        if (KIND == 2) {
-            // the mover's FP32 centres after the move (rotated by the FP32 rotation)
-            if (lane < S.ncen) {
-                const float *c = ccen + 3 * ((size_t)slot * S.ncen + lane);
-                float3 cn = make_float3(c[0], c[1], c[2]);
-                if (type != 0) cn = mat32(R32, cn.x, cn.y, cn.z);
-                wx[lane] = make_float4(cn.x, cn.y, cn.z, 0.f);
-            }
-            __syncwarp();
-        }
-
-        // ---- FP32 ActiveDomain test (translations): 0 inside, 1 outside, 2 undecided;
-        //      and whether the PBC correction may move the particle through the box ----
-        int dom = 0;
-        float3 fnew = make_float3(0.f, 0.f, 0.f);
-        if (type != 1) {
-            fnew = mat32(G.cellinv, pn.x, pn.y, pn.z);
-            float fm[3] = {fnew.x, fnew.y, fnew.z};
-            const float mg = S.fc.cell_margin;
-            for (int d = 0; d < 3; d++) {
-                if (G.dims[d] > 1) {
-                    if (fm[d] < -mg || fm[d] > 1.f + mg) dom = 1;
-                    else if (dom == 0 && (fm[d] < mg || fm[d] > 1.f - mg)) dom = 2;
-                }
-            }
-        }
-
-        // ---- learned ordering: pre-test the mover's best-ranked partners ----
-        // (the staged candidate and the FP32 arithmetic of the full scan, so a certain
-        // overlap here is one the scan would find)
-        bool overlap = false;
-        if (LEARN && A.partners && dom != 1) {
-            int cls = 0;
-            bool tested = false;
-            if (lane < MLP_PARTNERS) {
-                const int k = pstage[MLP_PARTNERS * slot + lane];
-                if (k != 0xffff) {
-                    const float4 q = cpos[k];
-                    if (__float_as_int(q.w) != pid) {
-                        float3 aj = make_float3(0.f, 0.f, 1.f);
-                        if (KIND == 1) {
-                            const float4 a = cax[k];
-                            aj = make_float3(a.x, a.y, a.z);
-                        }
-                        cls = classify<KIND>(S.fc, make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z), an, aj);
-                        tested = true;
-                    }
-                }
-            }
-            const unsigned nt = __popc(__ballot_sync(FULL, tested));
-            if (lane == 0) ws.pairs += nt;
-            if (__ballot_sync(FULL, cls == 1)) overlap = true;
-        }
-
-        // ---- FP32 pass 1: centre distances, two candidates per lane per round ----
-        int nseg = 0, nun = 0;
-        if (dom != 1 && !overlap) {
-            for (int base = 0; base < total; base += 64) {
-                int k0 = base + lane, k1 = base + 32 + lane;
-                int c0 = 0, c1 = 0;
-                if (lane == 0) ws.pairs += (unsigned)min(64, total - base);
-                if (k0 < total) {
-                    float4 q = cpos[k0];
-                    if (__float_as_int(q.w) != pid) {
-                        float dx = q.x - pn.x, dy = q.y - pn.y, dz = q.z - pn.z;
-                        c0 = A.fp64_only ? 2 : d2_stage<KIND>(S.fc, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-                    }
-                }
-                if (k1 < total) {
-                    float4 q = cpos[k1];
-                    if (__float_as_int(q.w) != pid) {
-                        float dx = q.x - pn.x, dy = q.y - pn.y, dz = q.z - pn.z;
-                        c1 = A.fp64_only ? 2 : d2_stage<KIND>(S.fc, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-                    }
-                }
-                if (__ballot_sync(FULL, c0 == 1 || c1 == 1)) {
-                    overlap = true;
-                    break;
-                }
-                if (KIND >= 1) {
-                    unsigned b0 = __ballot_sync(FULL, c0 == 3), b1 = __ballot_sync(FULL, c1 == 3);
-                    if (c0 == 3) qseg[nseg + __popc(b0 & lt)] = (uint16_t)k0;
-                    nseg += __popc(b0);
-                    if (c1 == 3) qseg[nseg + __popc(b1 & lt)] = (uint16_t)k1;
-                    nseg += __popc(b1);
-                }
-                unsigned u0 = __ballot_sync(FULL, c0 == 2), u1 = __ballot_sync(FULL, c1 == 2);
-                if (c0 == 2) qun[nun + __popc(u0 & lt)] = (uint16_t)k0;
-                nun += __popc(u0);
-                if (c1 == 2) qun[nun + __popc(u1 & lt)] = (uint16_t)k1;
-                nun += __popc(u1);
-            }
-        }
-        __syncwarp();
-        // ---- FP32 pass 2 (polyspheres): every centre pair of a near body, one body per lane ----
-        if (KIND == 2 && !overlap) {
-            const int K = S.ncen;
-            for (int base = 0; base < nseg; base += 32) {
-                const int i = base + lane;
-                int cls = 0, k = 0;
-                if (i < nseg) {
-                    k = qseg[i];
-                    const float4 q = cpos[k];
-                    const float3 dq = make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z);
-                    const float *cj = ccen + 3 * (size_t)k * K;
-                    for (int j = 0; j < K && cls != 1; j++) {
-                        const float3 bj = make_float3(dq.x + cj[3 * j], dq.y + cj[3 * j + 1], dq.z + cj[3 * j + 2]);
-                        for (int a = 0; a < K; a++) {
-                            const float4 m = wx[a];
-                            const float3 d = make_float3(bj.x - m.x, bj.y - m.y, bj.z - m.z);
-                            const float d2 = dot3f(d, d);
-                            if (d2 < wthr[a * MAX_CEN + j]) {
-                                cls = 1;
-                                break;
-                            }
-                            if (d2 <= wthr[MAX_CEN * MAX_CEN + a * MAX_CEN + j]) cls = 2;
-                        }
-                    }
-                }
-                if (__ballot_sync(FULL, cls == 1)) {
-                    overlap = true;
-                    break;
-                }
-                unsigned b2 = __ballot_sync(FULL, cls == 2);
-                if (cls == 2) qun[nun + __popc(b2 & lt)] = (uint16_t)k;
-                nun += __popc(b2);
-            }
-            __syncwarp();
-        }
-        // ---- FP32 pass 2 (spherocylinders): segment distances on full warps ----
-        if (KIND == 1 && !overlap) {
-            for (int base = 0; base < nseg; base += 32) {
-                int i = base + lane;
-                int cls = 0, k = 0;
-                if (i < nseg) {
-                    k = qseg[i];
-                    float4 q = cpos[k];
-                    float4 a = cax[k];
-                    cls = seg_stage(S.fc, make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z), an,
-                                    make_float3(a.x, a.y, a.z));
-                }
-                if (LEARN && A.pair_every > 0 && ((mi + cell) % A.pair_every) == 0) {
-                    // training data of the ranking network: the pair as it was before the
-                    // move, labelled with the certain outcome after it
-                    const bool rec = i < nseg && cls != 2;
-                    const unsigned bal = __ballot_sync(FULL, rec);
-                    unsigned long long base_idx = 0;
-                    if (lane == 0 && bal) base_idx = atomicAdd(A.pair_count, (unsigned long long)__popc(bal));
-                    base_idx = __shfl_sync(FULL, base_idx, 0);
-                    const unsigned long long idx = base_idx + __popc(bal & lt);
-                    if (rec && idx < A.pair_cap) {
-                        float4 q = cpos[k];
-                        float4 a = cax[k];
-                        float f[MLP_IN];
-                        mlp_features(make_float3(q.x - pcur.x, q.y - pcur.y, q.z - pcur.z), ai,
-                                     make_float3(a.x, a.y, a.z), A.inv_range, f);
-                        float4 *dst = reinterpret_cast<float4 *>(A.pair_feats + idx * MLP_IN);
-                        dst[0] = make_float4(f[0], f[1], f[2], f[3]);
-                        dst[1] = make_float4(f[4], f[5], f[6], f[7]);
-                        dst[2] = make_float4(f[8], f[9], f[10], f[11]);
-                        dst[3] = make_float4(f[12], f[13], f[14], f[15]);
-                        A.pair_labels[idx] = cls == 1 ? 1 : 0;
-                    }
-                }
-                if (__ballot_sync(FULL, cls == 1)) {
-                    overlap = true;
-                    break;
-                }
-                unsigned b2 = __ballot_sync(FULL, cls == 2);
-                if (cls == 2) qun[nun + __popc(b2 & lt)] = (uint16_t)k;
-                nun += __popc(b2);
-            }
-            __syncwarp();
-        }
-
-        uint8_t code = dom == 1 ? 2 : (overlap ? 1 : 0);
-        // ---- FP64: the exact proposal of a surviving move (or of an accepted u == 0 move) ----
-        // (an overlap found near the cell wall still needs the exact ActiveDomain test: the
-        // reference rejects a move that leaves the domain before it tests any overlap)
-        const bool need64 = (code == 0) || (uni <= 0.0) || (dom == 2);
-        const bool needR = type != 0 && (need64 || A.log != nullptr);
-        double rel_own = 0.0, pnew_own = 0.0, onew_own = 0.0, rrow[3] = {0.0, 0.0, 0.0};
-        bool exact_rel = false;     // rel_own holds the exact FP64 relative coordinate
-        d3 pnew{0, 0, 0}, anew{0, 0, 0};
-        if (needR) {
-            // row ei of the move's rotation (lanes 0-8 hold rows 0..2 three times over)
-            if (LIST) {
-                rrow[0] = mrec->rotation[3 * ei];
-                rrow[1] = mrec->rotation[3 * ei + 1];
-                rrow[2] = mrec->rotation[3 * ei + 2];
-            } else {
-                const double *R = A.rtab64 + 9 * (size_t)rot_idx;
-                rrow[0] = rot_inv ? R[ei] : R[3 * ei];
-                rrow[1] = rot_inv ? R[3 + ei] : R[3 * ei + 1];
-                rrow[2] = rot_inv ? R[6 + ei] : R[3 * ei + 2];
-            }
-        }
-        if (need64) {
-            if (type != 1) {
-                // May the PBC correction move the particle through the box?  FP32 relative
-                // coordinates of the stored (wrapped) position and of the translated one in
-                // the same image: s + (c + f) / n, minus the stored position's wrap k.
-                bool maywrap = false;
-                {
-                    float3 f0 = mat32(G.cellinv, pcur.x, pcur.y, pcur.z);
-                    float fm[3] = {fnew.x, fnew.y, fnew.z}, fo[3] = {f0.x, f0.y, f0.z};
-                    const float mg = S.fc.cell_margin;
-                    for (int d = 0; d < 3; d++) {
-                        float rold = G.fshift[d] + ((float)c[d] + fo[d]) * G.finv_dims[d];
-                        float rnew = G.fshift[d] + ((float)c[d] + fm[d]) * G.finv_dims[d];
-                        float k = rold >= 1.f ? 1.f : 0.f;
-                        if (fabsf(rold - 1.f) < mg) maywrap = true;
-                        rnew -= k;
-                        if (rnew < mg || rnew > 1.f - mg) maywrap = true;
-                    }
-                }
-                // Shape::translate with the PBC correction (core/Shape.cpp:9-12,
-                // core/PeriodicBoundaryConditions.cpp:11-22), one box row per lane
-                if (!LIST) t64_lane = (double)(ld == 0 ? t32.x : (ld == 1 ? t32.y : t32.z));
-                double p1 = dadd(pos_own, t64_lane);
-                if (!maywrap) {
-                    // FP32 shows every relative coordinate clear of 0 and 1: no correction,
-                    // which is box · 0 = +0 exactly
-                    pnew_own = dadd(p1, 0.0);
-                    if (dom == 2) {
-                        d3 P1{__shfl_sync(FULL, p1, 0), __shfl_sync(FULL, p1, 1), __shfl_sync(FULL, p1, 2)};
-                        rel_own = mrow(S.inv, ld, P1);
-                        exact_rel = true;
-                    }
-                } else {
-                    d3 P1{__shfl_sync(FULL, p1, 0), __shfl_sync(FULL, p1, 1), __shfl_sync(FULL, p1, 2)};
-                    double rel = mrow(S.inv, ld, P1);
-                    double cr = 0.0;
-                    while (dadd(rel, cr) < 0.0) cr = dadd(cr, 1.0);
-                    while (dadd(rel, cr) >= 1.0) cr = dsub(cr, 1.0);
-                    if (__ballot_sync(FULL, lane < 3 && cr != 0.0) == 0u) {
-                        pnew_own = dadd(p1, 0.0);
-                        rel_own = rel;
-                    } else {
-                        d3 C{__shfl_sync(FULL, cr, 0), __shfl_sync(FULL, cr, 1), __shfl_sync(FULL, cr, 2)};
-                        pnew_own = dadd(p1, mrow(S.box, ld, C));
-                        d3 PN{__shfl_sync(FULL, pnew_own, 0), __shfl_sync(FULL, pnew_own, 1),
-                              __shfl_sync(FULL, pnew_own, 2)};
-                        rel_own = mrow(S.inv, ld, PN);
-                    }
-                    exact_rel = true;
-                }
-                pnew = d3{__shfl_sync(FULL, pnew_own, 0), __shfl_sync(FULL, pnew_own, 1), __shfl_sync(FULL, pnew_own, 2)};
-                if (dom == 2) {
-                    // ActiveDomain::isInside (core/ActiveDomain.cpp:8-21) on the exact position
-                    bool out = false;
-                    if (lane < 3 && dims_ld > 1) {
-                        if (hi_d > lo_d) out = rel_own <= lo_d || rel_own >= hi_d;
-                        else out = rel_own <= lo_d && rel_own >= hi_d;
-                    }
-                    if (__ballot_sync(FULL, out)) code = 2;
-                }
-            } else {
-                pnew = d3{__shfl_sync(FULL, pos_own, 0), __shfl_sync(FULL, pos_own, 1), __shfl_sync(FULL, pos_own, 2)};
-            }
-            if (type != 0) {
-                // Shape::rotate: R · O (core/Shape.cpp:14-16, Matrix.tpp:104-113), entry (ei, ej) per lane
-                double oe = rot_own;
-                double o0 = __shfl_sync(FULL, oe, ej), o1 = __shfl_sync(FULL, oe, 3 + ej),
-                       o2 = __shfl_sync(FULL, oe, 6 + ej);
-                double s = 0.0;
-                s = dadd(s, dmul(rrow[0], o0));
-                s = dadd(s, dmul(rrow[1], o1));
-                s = dadd(s, dmul(rrow[2], o2));
-                onew_own = s;
-                anew = d3{__shfl_sync(FULL, s, 2), __shfl_sync(FULL, s, 5), __shfl_sync(FULL, s, 8)};
-            } else {
-                anew = d3{__shfl_sync(FULL, rot_own, 2), __shfl_sync(FULL, rot_own, 5), __shfl_sync(FULL, rot_own, 8)};
-            }
-            if (KIND == 2) {
-                // the mover's centres: rotated by R (Packing::rotateTempInteractionCentres,
-                // core/Packing.cpp:357-361), then position + centre wrapped into the box
-                // (core/Packing.cpp:1041-1047); one centre per lane
-                double R[9];
-                for (int d = 0; d < 3; d++) {
-                    R[3 * d] = __shfl_sync(FULL, rrow[0], 3 * d);
-                    R[3 * d + 1] = __shfl_sync(FULL, rrow[1], 3 * d);
-                    R[3 * d + 2] = __shfl_sync(FULL, rrow[2], 3 * d);
-                }
-                if (lane < S.ncen) {
-                    d3 c = load_d3(S.cen64 + 3 * ((size_t)pid * S.ncen + lane));
-                    if (type != 0) c = mv3(R, c);
-                    d3 q = add3(pnew, c);
-                    d3 a = add3(q, pbc_correction(S.box, S.inv, q, nullptr));
-                    wcen[3 * lane] = c.x;
-                    wcen[3 * lane + 1] = c.y;
-                    wcen[3 * lane + 2] = c.z;
-                    wabs[3 * lane] = a.x;
-                    wabs[3 * lane + 1] = a.y;
-                    wabs[3 * lane + 2] = a.z;
-                }
-                __syncwarp();
-            }
-            // the guard band: queued pairs re-decided in FP64
-            if (KIND == 2 && code == 0 && nun > 0) {
-                // every centre pair of each queued body, one pair per lane
-                const int K = S.ncen;
-                bool ov = false;
-                for (int qi = 0; qi < nun && !ov; qi++) {
-                    const int k = qun[qi];
-                    const float4 q = cpos[k];
-                    const float3 dq = make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z);
-                    const float *cj = ccen + 3 * (size_t)k * K;
-                    for (int tb = 0; tb < K * K; tb += 32) {
-                        const int t = tb + lane;
-                        bool hit = false;
-                        if (t < K * K) {
-                            const int a = t / K, j = t % K;
-                            const float4 m = wx[a];
-                            const float3 d = make_float3((dq.x + cj[3 * j]) - m.x, (dq.y + cj[3 * j + 1]) - m.y,
-                                                         (dq.z + cj[3 * j + 2]) - m.z);
-                            hit = exact_centre_pair(S, d3{wabs[3 * a], wabs[3 * a + 1], wabs[3 * a + 2]}, a,
-                                                    __float_as_int(q.w), j, d);
-                        }
-                        if (__ballot_sync(FULL, hit)) {
-                            ov = true;
-                            break;
-                        }
-                    }
-                }
-                ws.fp64 += nun;
-                if (ov) code = 1;
-            }
-            if (KIND != 2 && code == 0 && nun > 0) {
-                bool ov = false;
-                for (int qb = 0; qb < nun; qb += 32) {
-                    int qi = qb + lane;
-                    bool hit = false;
-                    if (qi < nun) {
-                        int k = qun[qi];
-                        float4 q = cpos[k];
-                        hit = exact_pair(S, pnew, anew, __float_as_int(q.w),
-                                         make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z));
-                    }
-                    if (__ballot_sync(FULL, hit)) {
-                        ov = true;
-                        break;
-                    }
-                }
-                ws.fp64 += nun;
-                if (ov) code = 1;
-            }
-        }
-
-        // ---- Metropolis (core/Simulation.cpp:483): u <= exp(-dE/T), dE in {0, +inf} ----
-        const bool acc = (code == 0) ? (uni <= 1.0) : (uni <= 0.0);
-        if (acc) {
-            const size_t gslot = (size_t)gbase + slot;
-            float4 np = pcur;
-            float4 na = KIND == 1 ? cax[slot] : make_float4(0.f, 0.f, 0.f, 0.f);
-            __syncwarp();
-            if (type != 1) {
-                if (lane < 3) S.pos64[3 * (size_t)pid + lane] = pnew_own;
-            }
-            const int na_cnt = nacc[slot];
-            if (type != 1 && !exact_rel && na_cnt < MIRROR_ROUNDINGS) {
-                // the FP32 proposal becomes the mirror position: one more FP32 rounding
-                // (t32 is the exact FP32 value of the FP64 translation), bounded per sweep
-                np = make_float4(pn.x, pn.y, pn.z, pcur.w);
-                if (lane == 0) nacc[slot] = (uint8_t)(na_cnt + 1);
-            } else if (type != 1) {
-                if (!exact_rel) rel_own = mrow(S.inv, ld, pnew);
-                if (lane == 0) nacc[slot] = 0;
-                // new cell-local FP32 position from the FP64 relative coordinates
-                double u = rel_own - shift_ld;
-                if (u < 0.0) u += 1.0;
-                double fd = u * dims_ld - c_ld;
-                if (fd < -0.5) fd += dims_ld;
-                if (fd > dims_ld - 0.5) fd -= dims_ld;
-                float f = (float)fd;
-                float f0 = __shfl_sync(FULL, f, 0), f1 = __shfl_sync(FULL, f, 1), f2 = __shfl_sync(FULL, f, 2);
-                float3 loc = mat32(G.cellmat, f0, f1, f2);
-                np = make_float4(loc.x, loc.y, loc.z, pcur.w);
-            }
-            if (type != 0) {
-                if (lane < 9) S.rot64[9 * (size_t)pid + lane] = onew_own;
-                const float of = (float)onew_own;
-                na = make_float4(__shfl_sync(FULL, of, 2), __shfl_sync(FULL, of, 5), __shfl_sync(FULL, of, 8), 0.f);
-            }
-            if (lane == 0) {
-                cpos[slot] = np;
-                G.mpos[gslot] = np;
-                if (KIND == 1 && type != 0) {
-                    cax[slot] = na;
-                    G.maxis[gslot] = na;
-                }
-            }
-            if (KIND == 2 && lane < S.ncen) {
-                // Packing::acceptTempInteractionCentres (core/Packing.cpp:339-348)
-                const size_t ci = (size_t)pid * S.ncen + lane;
-                for (int d = 0; d < 3; d++) S.abs64[3 * ci + d] = wabs[3 * lane + d];
-                if (type != 0) {
-                    for (int d = 0; d < 3; d++) S.cen64[3 * ci + d] = wcen[3 * lane + d];
-                    const float4 c32 = make_float4((float)wcen[3 * lane], (float)wcen[3 * lane + 1],
-                                                   (float)wcen[3 * lane + 2], 0.f);
-                    G.mcen[gslot * S.ncen + lane] = c32;
-                    float *dst = ccen + 3 * ((size_t)slot * S.ncen + lane);
-                    dst[0] = c32.x;
-                    dst[1] = c32.y;
-                    dst[2] = c32.z;
-                }
-            }
-            if (self_images) {
-                // the own cell is staged several times (periodic images): refresh every copy
-                __syncwarp();
-                for (int k = lane + occ; k < total; k += 32) {
-                    float4 q = cpos[k];
-                    if (__float_as_int(q.w) == pid) {
-                        cpos[k] = make_float4(np.x + (q.x - pcur.x), np.y + (q.y - pcur.y), np.z + (q.z - pcur.z), q.w);
-                        if (KIND == 1 && type != 0) cax[k] = na;
-                        if (KIND == 2 && type != 0)
-                            for (int e = 0; e < 3 * S.ncen; e++)
-                                ccen[3 * (size_t)k * S.ncen + e] = ccen[3 * (size_t)slot * S.ncen + e];
-                    }
-                }
-            }
-            __syncwarp();
-        }
-
-        const uint8_t full_code = code | (acc ? RP_CODE_ACCEPTED : 0);
-        if (LIST) {
-            if (lane == 0 && A.codes) A.codes[out_index] = full_code;
-        } else if (A.log) {
-            rp_move *rec = A.log + (size_t)ntypes * (size_t)gbase + mi;
-            if (lane < 3) rec->translation[lane] = t64_lane;
-            const double rj = ej == 0 ? rrow[0] : (ej == 1 ? rrow[1] : rrow[2]);
-            if (lane < 9) rec->rotation[lane] = type != 0 ? rj : (lane % 4 == 0 ? 1.0 : 0.0);
-            if (lane == 0) {
-                rec->particle = pid;
-                rec->type = type;
-                rec->domain = cell;
-                rec->reserved = 0;
-                rec->uniform = uni;
-                A.log_codes[(size_t)ntypes * (size_t)gbase + mi] = full_code;
-            }
-        }
-        ws.moves++;
-        if (acc) ws.accepted++;
-        if (code == 1) ws.rej_overlap++;
-        if (code == 2) ws.rej_domain++;
-        if (type == 0) ws.trans++;
-        else ws.rots++;
-    }
+    if (slot < s.n) count_poly_one(s, g, slot, early, out, flag);
 }
 
 // LEARN instantiates the learned-ordering pre-test and the pair-outcome log (kept out of
@@ -1200,7 +213,8 @@ __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(co
             item = __shfl_sync(FULL, it, 0);
         }
         if (item >= nitems) break;
-        sweep_cell<KIND, LIST, LEARN>(A, item, cpos, cax, qseg, qun, nacc, pstage, ccen, wx, ws);
+        sweep_cell<KIND, LIST, LEARN>(A, item, -1, A.cap, A.overflow, A.overflow_count, cpos, cax, qseg, qun, nacc,
+                                      pstage, ccen, wx, ws);
         __syncwarp();
         item += stride;
     }
