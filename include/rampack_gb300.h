@@ -300,6 +300,47 @@ int rp_mlp_train(void *handle, int32_t epochs, int32_t batch, float lr, uint64_t
 /* Chooses the ordering of later sweeps (RP_ORDER_*), re-ranking every `every` sweeps. */
 int rp_set_ordering(void *handle, int32_t mode, int32_t every);
 
+/* ---- batched replicas -----------------------------------------------------------------
+ * No single reference counterpart: many independent packings of one shape (spheres or
+ * spherocylinders) advanced together, as a set of rampack Simulations would be, but with
+ * every device step covering all replicas in one launch (one persistent sweep launch per
+ * checkerboard phase for the whole batch).  Replica r behaves exactly as a handle would
+ * under rp_sweep with the seed seed + RP_BATCH_SEED_STRIDE * r, except that all replicas draw
+ * rotations from one table per sweep (from the batch seed and counter); its logged sweeps
+ * replay on the reference's Packing like a handle's.  Box moves stay host-driven
+ * (Simulation::tryScaling, core/Simulation.cpp:493-531): the caller proposes a box per
+ * replica and the batch rescales, rebuilds and recounts all proposing replicas at once. */
+
+/* Replica r's sweep seed: seed + 0x9E3779B97F4A7C15 * r (mod 2^64). */
+#define RP_BATCH_SEED_STRIDE 0x9E3779B97F4A7C15ull
+
+int rp_batch_create(const rp_shape_desc *shape, int32_t replicas, const int64_t *n, int device, void **batch);
+int rp_batch_destroy(void *batch);
+const char *rp_batch_last_error(void *batch);
+
+/* Per replica, as rp_upload_state / rp_download_state / rp_count_overlaps / rp_get_grid /
+ * rp_sweep_log on a handle. */
+int rp_batch_upload_state(void *batch, int32_t replica, const double *pos, const double *rot, const double *box9);
+int rp_batch_download_state(void *batch, int32_t replica, double *pos, double *rot, double *box9);
+int rp_batch_count_overlaps(void *batch, int32_t replica, int early_exit, int64_t *count);
+int rp_batch_get_grid(void *batch, int32_t replica, rp_grid_info *info, int32_t *cells, double *bounds);
+int rp_batch_sweep_log(void *batch, int32_t replica, rp_move *moves, uint8_t *codes, int64_t capacity,
+                       int64_t *count);
+
+/* One sweep of every replica (2 N_r moves each with both steps > 0); stats (may be NULL)
+ * receives one entry per replica. */
+int rp_batch_sweep(void *batch, const rp_sweep_params *params, rp_sweep_stats *stats);
+
+/* Box moves: replicas with propose[r] != 0 move to boxes[9 r ..]; dE[r] = +inf if the new
+ * box makes an overlap (the caller then reverts those), else 0.  As Packing::tryScaling /
+ * revertScaling per replica (core/Packing.cpp:172-208, :363-371). */
+int rp_batch_try_scaling(void *batch, const double *boxes, const uint8_t *propose, double *dE);
+int rp_batch_revert_scaling(void *batch, const uint8_t *mask);
+
+/* Launch shape: checkerboard cells at least cell_factor (>= 1) interaction ranges high and
+ * 2, 4 or 8 warps per block of the sweep kernel (defaults 1.0 and 4). */
+int rp_batch_set_tuning(void *batch, double cell_factor, int32_t warps_per_block);
+
 /* ---- allocation-free overlap count ----------------------------------------------- */
 
 /* Limits of rp_count_overlaps_static and the size of the scratch array behind it. */

@@ -93,11 +93,25 @@ SIGNATURES = {
     "rp_set_ordering": (C.c_int, [_P, C.c_int32, C.c_int32]),
     "rp_renormalize_orientations": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int64)]),
     "rp_nematic_order": (C.c_int, [_P, _D, _D]),
+    "rp_batch_create": (C.c_int, [C.POINTER(ShapeDesc), C.c_int32, C.POINTER(C.c_int64), C.c_int,
+                                  C.POINTER(C.c_void_p)]),
+    "rp_batch_destroy": (C.c_int, [_P]),
+    "rp_batch_last_error": (C.c_char_p, [_P]),
+    "rp_batch_upload_state": (C.c_int, [_P, C.c_int32, _D, _D, _D]),
+    "rp_batch_download_state": (C.c_int, [_P, C.c_int32, _D, _D, _D]),
+    "rp_batch_count_overlaps": (C.c_int, [_P, C.c_int32, C.c_int, C.POINTER(C.c_int64)]),
+    "rp_batch_get_grid": (C.c_int, [_P, C.c_int32, C.POINTER(GridInfo), C.POINTER(C.c_int32), _D]),
+    "rp_batch_sweep_log": (C.c_int, [_P, C.c_int32, _P, _P, C.c_int64, C.POINTER(C.c_int64)]),
+    "rp_batch_sweep": (C.c_int, [_P, C.POINTER(SweepParams), C.POINTER(SweepStats)]),
+    "rp_batch_try_scaling": (C.c_int, [_P, _D, _P, _D]),
+    "rp_batch_revert_scaling": (C.c_int, [_P, _P]),
+    "rp_batch_set_tuning": (C.c_int, [_P, C.c_double, C.c_int32]),
 }
 KERNEL_GROUPS = ["sweep", "rebuild", "count", "rescale", "overflow", "order", "mlp", "fix"]
 MLP_NPARAM = 5313
 MLP_FEATURES = 16
 ORDER_OFF, ORDER_MLP, ORDER_DISTANCE = 0, 1, 2
+BATCH_SEED_STRIDE = 0x9E3779B97F4A7C15
 
 _LIB = None
 

@@ -27,6 +27,15 @@ cudaError_t launch_fix_prepare(const DevState &s, const double *cbody, double *r
                                cudaStream_t st);
 cudaError_t launch_fresh_centres(const DevState &s, const double *cbody, cudaStream_t st);
 int axis_moment_blocks(int64_t n);
+cudaError_t launch_b_rebuild(const BatchRep *T, const int *pbase, const int *cbase, int R, int total_particles,
+                             int total_cells, cudaStream_t st);
+cudaError_t launch_b_rescale(const BatchRep *T, const int *pbase, int R, int total_particles, cudaStream_t st);
+cudaError_t launch_b_count(const BatchRep *T, const int *pbase, int R, int total_particles, int kind, int early,
+                           unsigned long long *out, int *flags, cudaStream_t st);
+size_t batch_smem_per_warp(int kind, int cap);
+cudaError_t launch_b_sweep(const BatchRep *T, const int *item_base, int R, int kind, int k, int *next_item, int cap,
+                           int wpb, int blocks, cudaStream_t st);
+cudaError_t launch_b_overflow(const BatchRep *T, int R, int kind, int k, int cap, cudaStream_t st);
 cudaError_t launch_axis_moments(const double *rot64, int64_t n, double *partial, cudaStream_t st);
 cudaError_t launch_fix_check(const DevState &s, const GridDev &g, const double *rotfix, const double *absfix,
                              uint8_t *rejected, unsigned long long *first, cudaStream_t st);
@@ -59,6 +68,7 @@ struct GridHost {
     int cap = 0;
     double cellmat64[9]{};
     std::vector<float> cthr;  // host copy of the FP32 centre-pair thresholds (polyspheres)
+    std::vector<double> bounds_host;  // batch members: this grid's bounds, packed by the batch
     bool no_ng = false;       // the reference keeps no neighbour grid for this grid's box
 };
 
@@ -131,6 +141,10 @@ struct Handle {
     double *abs64[2] = {nullptr, nullptr};
     double *cthr64 = nullptr;
     double *cbody_dev = nullptr;    // body-frame centres on the device
+    // batched replicas: the batch owns the rotation table, counters, status word and the
+    // device copy of the ActiveDomain bounds (setup_grid leaves the bounds in bounds_host)
+    bool batch_member = false;
+    double cell_factor = 1.0;       // checkerboard cells at least cell_factor x the range
     // learned ordering: network parameters (FP32 master + BF16 copy), Adam moments, scratch
     float *mlp_w32 = nullptr, *mlp_grad = nullptr, *mlp_m = nullptr, *mlp_v = nullptr, *mlp_loss = nullptr;
     __nv_bfloat16 *mlp_w16 = nullptr;
@@ -390,7 +404,8 @@ int setup_grid(Handle *h, GridHost &G, const double *box, const double *shift) {
     // and large enough that the grid has at most max(4096, 8 N) cells (a dilute system
     // would otherwise spread a few particles over millions of empty cells)
     const double max_cells = std::max(4096.0, 8.0 * static_cast<double>(h->n));
-    const double cell_min = std::max(h->range, std::cbrt(volume_of(box) / max_cells)) * (1.0 + 1e-9);
+    const double cell_min =
+        std::max(h->range * h->cell_factor, std::cbrt(volume_of(box) / max_cells)) * (1.0 + 1e-9);
     int dims[3];
     for (int d = 0; d < 3; d++) {
         if (!(hgt[d] >= h->range * (1.0 + 1e-9)))
@@ -494,8 +509,12 @@ int setup_grid(Handle *h, GridHost &G, const double *box, const double *shift) {
         }
         off += 2 * dims[d];
     }
-    RP_CUDA(h, ensure(g.bounds, G.bounds_alloc, nb));
-    RP_CUDA(h, cudaMemcpyAsync(g.bounds, bounds.data(), sizeof(double) * nb, cudaMemcpyHostToDevice, h->stream));
+    if (h->batch_member) {
+        G.bounds_host = bounds;  // the batch packs every replica's bounds into one copy
+    } else {
+        RP_CUDA(h, ensure(g.bounds, G.bounds_alloc, nb));
+        RP_CUDA(h, cudaMemcpyAsync(g.bounds, bounds.data(), sizeof(double) * nb, cudaMemcpyHostToDevice, h->stream));
+    }
     // staged-candidate capacity per warp: mean neighbourhood plus six standard deviations
     double mean = 27.0 * static_cast<double>(h->n) / static_cast<double>(ncell);
     int cap = static_cast<int>(mean + 6.0 * std::sqrt(mean) + 32.0);
@@ -636,6 +655,139 @@ int rank_partners(Handle *h) {
     return RP_OK;
 }
 
+// ---- batched replicas ----------------------------------------------------------------
+
+struct Batch {
+    int device = 0, kind = 0, R = 0, num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<Handle *> rep;
+    BatchRep *d_table = nullptr;                      // [R]
+    int *d_bases = nullptr;                           // item_base, pbase, cbase: 3 x (R + 1)
+    double *d_bounds = nullptr;                       // packed ActiveDomain bounds
+    int64_t d_bounds_alloc = 0;
+    // two pinned staging sets used alternately; a set is rewritten only after its copies ran
+    struct Staging {
+        BatchRep *table = nullptr;
+        int *bases = nullptr;
+        double *bounds = nullptr;
+        int64_t bounds_alloc = 0;
+        cudaEvent_t done = nullptr;
+        bool pending = false;
+    } stage[2];
+    int cur = 0;
+    double *rtab64 = nullptr;
+    float *rtab32 = nullptr;
+    int32_t *item_counters = nullptr;                 // [8]
+    unsigned long long *stats = nullptr;              // [R][8]
+    uint32_t *status = nullptr;                       // [R]
+    unsigned long long *counts = nullptr, *h_counts = nullptr;  // [R]
+    int *flags = nullptr, *h_flags = nullptr;         // [R]
+    int wpb = 4;
+    uint64_t launches = 0;
+    std::string err;
+};
+
+int bfail(Batch *b, int code, const std::string &msg) {
+    if (b) b->err = msg;
+    return code;
+}
+
+#define RB_CUDA(b, call)                                                                                  \
+    do {                                                                                                  \
+        cudaError_t e_ = (call);                                                                          \
+        if (e_ != cudaSuccess) return bfail((b), RP_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+// The grid origin and phase order of one replica's sweep, from the replica's Philox stream
+// (the single-system sweep derives them the same way).
+void sweep_origin(uint64_t seed, uint64_t counter, double shift[3], uint32_t &shuffle) {
+    u4 r = philox(u4{0x5eedu, 0x9e37u, static_cast<uint32_t>(counter), static_cast<uint32_t>(counter >> 32)},
+                  static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
+    shift[0] = (r.a >> 8) * (1.0 / 16777216.0);
+    shift[1] = (r.b >> 8) * (1.0 / 16777216.0);
+    shift[2] = (r.c >> 8) * (1.0 / 16777216.0);
+    shuffle = r.d;
+}
+
+void phase_order(const GridDev &g, uint32_t x, std::vector<int> &phases) {
+    phases.clear();
+    for (int ph = 0; ph < 8; ph++) {
+        bool ok = true;
+        for (int d = 0; d < 3; d++)
+            if (g.dims[d] == 1 && ((ph >> d) & 1)) ok = false;
+        if (ok) phases.push_back(ph);
+    }
+    for (int k = static_cast<int>(phases.size()) - 1; k > 0; k--) {
+        x = x * 1664525u + 1013904223u;
+        int j = static_cast<int>((static_cast<uint64_t>(x) * (k + 1)) >> 32);
+        std::swap(phases[k], phases[j]);
+    }
+}
+
+uint64_t replica_seed(uint64_t seed, int r) { return seed + RP_BATCH_SEED_STRIDE * static_cast<uint64_t>(r); }
+
+// Packs every replica's current-grid bounds and fills the table entries and prefix
+// arrays in the current pinned staging set (after its previous copies have run).
+int batch_tables(Batch *b, int &total_items, int &total_p, int &total_c) {
+    Batch::Staging &S = b->stage[b->cur];
+    if (S.pending) RB_CUDA(b, cudaEventSynchronize(S.done));
+    S.pending = false;
+    int64_t nb = 0;
+    for (Handle *h : b->rep) nb += static_cast<int64_t>(h->grid[h->gcur].bounds_host.size());
+    if (nb > S.bounds_alloc) {
+        cudaFreeHost(S.bounds);
+        S.bounds = nullptr;
+        S.bounds_alloc = 0;
+        RB_CUDA(b, cudaMallocHost(&S.bounds, sizeof(double) * nb * 2));
+        S.bounds_alloc = nb * 2;
+    }
+    if (nb > b->d_bounds_alloc) {
+        RB_CUDA(b, cudaStreamSynchronize(b->stream));  // the old array may still be read
+        cudaFree(b->d_bounds);
+        b->d_bounds = nullptr;
+        b->d_bounds_alloc = 0;
+        RB_CUDA(b, cudaMalloc(&b->d_bounds, sizeof(double) * nb * 2));
+        b->d_bounds_alloc = nb * 2;
+    }
+    int64_t off = 0;
+    int *ib = S.bases, *pb = S.bases + (b->R + 1), *cb = S.bases + 2 * (b->R + 1);
+    ib[0] = pb[0] = cb[0] = 0;
+    for (int r = 0; r < b->R; r++) {
+        Handle *h = b->rep[r];
+        GridHost &G = h->grid[h->gcur];
+        std::memcpy(S.bounds + off, G.bounds_host.data(), sizeof(double) * G.bounds_host.size());
+        G.d.bounds = b->d_bounds + off;
+        off += static_cast<int64_t>(G.bounds_host.size());
+        BatchRep &T = S.table[r];
+        T = BatchRep{};
+        T.a = base_args(h);
+        int act = 1;
+        for (int d = 0; d < 3; d++) act *= G.d.dims[d] == 1 ? 1 : G.d.dims[d] / 2;
+        T.a.num_active = act;
+        ib[r + 1] = ib[r] + act;
+        pb[r + 1] = pb[r] + static_cast<int>(h->n);
+        cb[r + 1] = cb[r] + G.d.ncell;
+    }
+    total_items = ib[b->R];
+    total_p = pb[b->R];
+    total_c = cb[b->R];
+    return RP_OK;
+}
+
+// Copies the current staging set to the device and moves on to the other set.
+int batch_copy(Batch *b) {
+    Batch::Staging &S = b->stage[b->cur];
+    int64_t nb = 0;
+    for (Handle *h : b->rep) nb += static_cast<int64_t>(h->grid[h->gcur].bounds_host.size());
+    RB_CUDA(b, cudaMemcpyAsync(b->d_bounds, S.bounds, sizeof(double) * nb, cudaMemcpyHostToDevice, b->stream));
+    RB_CUDA(b, cudaMemcpyAsync(b->d_table, S.table, sizeof(BatchRep) * b->R, cudaMemcpyHostToDevice, b->stream));
+    RB_CUDA(b, cudaMemcpyAsync(b->d_bases, S.bases, sizeof(int) * 3 * (b->R + 1), cudaMemcpyHostToDevice, b->stream));
+    RB_CUDA(b, cudaEventRecord(S.done, b->stream));
+    S.pending = true;
+    b->cur ^= 1;
+    return RP_OK;
+}
+
 }  // namespace
 }  // namespace rp
 
@@ -672,16 +824,20 @@ static int create_common(Handle *h, int64_t n, int device, void **handle) {
             return bail(e);
     }
     if ((e = cudaMalloc(&h->rot64, sizeof(double) * 9 * n)) != cudaSuccess) return bail(e);
-    if ((e = cudaMalloc(&h->rtab64, sizeof(double) * 9 * ROT_TABLE)) != cudaSuccess) return bail(e);
-    if ((e = cudaMalloc(&h->rtab32, sizeof(float) * 12 * ROT_TABLE)) != cudaSuccess) return bail(e);
+    if (!h->batch_member) {
+        if ((e = cudaMalloc(&h->rtab64, sizeof(double) * 9 * ROT_TABLE)) != cudaSuccess) return bail(e);
+        if ((e = cudaMalloc(&h->rtab32, sizeof(float) * 12 * ROT_TABLE)) != cudaSuccess) return bail(e);
+    }
     if ((e = cudaMalloc(&h->item_counters, sizeof(int32_t) * 64)) != cudaSuccess) return bail(e);
-    if ((e = cudaMalloc(&h->status, sizeof(uint32_t))) != cudaSuccess) return bail(e);
-    if ((e = cudaMalloc(&h->counters, sizeof(unsigned long long) * 8)) != cudaSuccess) return bail(e);
+    if (!h->batch_member) {
+        if ((e = cudaMalloc(&h->status, sizeof(uint32_t))) != cudaSuccess) return bail(e);
+        if ((e = cudaMalloc(&h->counters, sizeof(unsigned long long) * 8)) != cudaSuccess) return bail(e);
+        cudaMemset(h->status, 0, sizeof(uint32_t));
+        cudaMemset(h->counters, 0, sizeof(unsigned long long) * 8);
+    }
     if ((e = cudaMalloc(&h->count_out, sizeof(unsigned long long))) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc(&h->flag, sizeof(int))) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc(&h->overflow_count, sizeof(int32_t))) != cudaSuccess) return bail(e);
-    cudaMemset(h->status, 0, sizeof(uint32_t));
-    cudaMemset(h->counters, 0, sizeof(unsigned long long) * 8);
     cudaMemset(h->overflow_count, 0, sizeof(int32_t));
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return bail(e);
     *handle = h;
@@ -767,7 +923,7 @@ int rp_destroy(void *handle) {
         cudaFree(g.mpos);
         cudaFree(g.maxis);
         cudaFree(g.plocal);
-        cudaFree(g.bounds);
+        if (!h->batch_member) cudaFree(g.bounds);
         cudaFree(g.max_occ);
         cudaFree(g.mcen);
         cudaFree(g.cthr);
@@ -778,12 +934,16 @@ int rp_destroy(void *handle) {
     cudaFree(h->abs64[1]);
     cudaFree(h->cthr64);
     cudaFree(h->cbody_dev);
-    cudaFree(h->rtab64);
-    cudaFree(h->rtab32);
+    if (!h->batch_member) {
+        cudaFree(h->rtab64);
+        cudaFree(h->rtab32);
+    }
     cudaFree(h->item_counters);
     cudaFree(h->block_sums);
-    cudaFree(h->status);
-    cudaFree(h->counters);
+    if (!h->batch_member) {
+        cudaFree(h->status);
+        cudaFree(h->counters);
+    }
     cudaFree(h->count_out);
     cudaFree(h->flag);
     cudaFree(h->overflow);
@@ -1676,6 +1836,389 @@ int rp_set_ordering(void *handle, int32_t mode, int32_t every) {
     h->order_mode = mode;
     h->order_every = every;
     h->partners_valid = false;
+    return RP_OK;
+}
+
+// ---- batched replicas ---------------------------------------------------------------
+
+int rp_batch_create(const rp_shape_desc *shape, int32_t replicas, const int64_t *n, int device, void **batch) {
+    if (!shape || !n || !batch || replicas <= 0 || replicas > 4096) return RP_ERR_ARG;
+    if (shape->kind != RP_SHAPE_SPHERE && shape->kind != RP_SHAPE_SPHEROCYLINDER) return RP_ERR_UNSUPPORTED;
+    int64_t total = 0;
+    for (int r = 0; r < replicas; r++) {
+        if (n[r] <= 0) return RP_ERR_ARG;
+        total += n[r];
+    }
+    if (total > (1ll << 31) - 1) return RP_ERR_ARG;
+    Batch *b = new (std::nothrow) Batch();
+    if (!b) return RP_ERR_ARG;
+    b->device = device;
+    b->kind = shape->kind;
+    b->R = replicas;
+    auto bail = [&](int rc) {
+        rp_batch_destroy(b);
+        return rc;
+    };
+    if (cudaSetDevice(device) != cudaSuccess) return bail(RP_ERR_CUDA);
+    cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(RP_ERR_CUDA);
+    const int R = replicas;
+    bool ok = cudaMalloc(&b->d_table, sizeof(BatchRep) * R) == cudaSuccess &&
+              cudaMalloc(&b->d_bases, sizeof(int) * 3 * (R + 1)) == cudaSuccess &&
+              cudaMalloc(&b->rtab64, sizeof(double) * 9 * ROT_TABLE) == cudaSuccess &&
+              cudaMalloc(&b->rtab32, sizeof(float) * 12 * ROT_TABLE) == cudaSuccess &&
+              cudaMalloc(&b->item_counters, sizeof(int32_t) * 8) == cudaSuccess &&
+              cudaMalloc(&b->stats, sizeof(unsigned long long) * 8 * R) == cudaSuccess &&
+              cudaMalloc(&b->status, sizeof(uint32_t) * R) == cudaSuccess &&
+              cudaMalloc(&b->counts, sizeof(unsigned long long) * R) == cudaSuccess &&
+              cudaMallocHost(&b->h_counts, sizeof(unsigned long long) * R) == cudaSuccess &&
+              cudaMalloc(&b->flags, sizeof(int) * R) == cudaSuccess &&
+              cudaMallocHost(&b->h_flags, sizeof(int) * R) == cudaSuccess;
+    for (auto &S : b->stage)
+        ok = ok && cudaMallocHost(&S.table, sizeof(BatchRep) * R) == cudaSuccess &&
+             cudaMallocHost(&S.bases, sizeof(int) * 3 * (R + 1)) == cudaSuccess &&
+             cudaEventCreateWithFlags(&S.done, cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) return bail(RP_ERR_CUDA);
+    cudaMemset(b->stats, 0, sizeof(unsigned long long) * 8 * R);
+    cudaMemset(b->status, 0, sizeof(uint32_t) * R);
+    for (int r = 0; r < R; r++) {
+        Handle *h = new (std::nothrow) Handle();
+        if (!h) return bail(RP_ERR_ARG);
+        h->batch_member = true;
+        h->shape = *shape;
+        double rad = shape->radius, l = shape->length;
+        ExactShape ex{};
+        ex.kind = shape->kind;
+        if (shape->kind == RP_SHAPE_SPHERE) {
+            h->range = 2 * rad;
+            ex.sphere_thr = std::pow(2 * rad, 2);
+        } else {
+            h->range = 2 * rad + l;
+            ex.core_thr = 4 * rad * rad;
+            ex.far_thr = std::pow(2 * rad + l, 2);
+            short beg = -1, end = 1;
+            ex.neg_cap_half = 0.5 * beg * l;
+            ex.cap_half = 0.5 * end * l;
+        }
+        h->ref_range = h->range;
+        h->ex = ex;
+        h->status = b->status + r;
+        h->counters = b->stats + 8 * r;
+        h->rtab64 = b->rtab64;
+        h->rtab32 = b->rtab32;
+        void *hh = nullptr;
+        int rc = create_common(h, n[r], device, &hh);
+        if (rc) return bail(rc);
+        b->rep.push_back(h);
+    }
+    *batch = b;
+    return RP_OK;
+}
+
+int rp_batch_destroy(void *batch) {
+    Batch *b = static_cast<Batch *>(batch);
+    if (!b) return RP_ERR_ARG;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    for (Handle *h : b->rep) rp_destroy(h);
+    cudaFree(b->d_table);
+    cudaFree(b->d_bases);
+    cudaFree(b->d_bounds);
+    cudaFree(b->rtab64);
+    cudaFree(b->rtab32);
+    cudaFree(b->item_counters);
+    cudaFree(b->stats);
+    cudaFree(b->status);
+    cudaFree(b->counts);
+    cudaFreeHost(b->h_counts);
+    cudaFree(b->flags);
+    cudaFreeHost(b->h_flags);
+    for (auto &S : b->stage) {
+        cudaFreeHost(S.table);
+        cudaFreeHost(S.bases);
+        cudaFreeHost(S.bounds);
+        if (S.done) cudaEventDestroy(S.done);
+    }
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return RP_OK;
+}
+
+const char *rp_batch_last_error(void *batch) {
+    Batch *b = static_cast<Batch *>(batch);
+    if (!b) return "null batch";
+    if (!b->err.empty()) return b->err.c_str();
+    for (Handle *h : b->rep)
+        if (!h->err.empty()) return h->err.c_str();
+    return "";
+}
+
+static Handle *batch_rep(Batch *b, int32_t r) {
+    if (!b || r < 0 || r >= b->R) return nullptr;
+    return b->rep[r];
+}
+
+int rp_batch_upload_state(void *batch, int32_t replica, const double *pos, const double *rot, const double *box9) {
+    Batch *b = static_cast<Batch *>(batch);
+    Handle *h = batch_rep(b, replica);
+    if (!h) return bfail(b, RP_ERR_ARG, "bad replica");
+    RB_CUDA(b, cudaStreamSynchronize(b->stream));
+    int rc = rp_upload_state(h, pos, rot, box9);
+    if (rc) b->err = h->err;
+    return rc;
+}
+
+int rp_batch_download_state(void *batch, int32_t replica, double *pos, double *rot, double *box9) {
+    Batch *b = static_cast<Batch *>(batch);
+    Handle *h = batch_rep(b, replica);
+    if (!h) return bfail(b, RP_ERR_ARG, "bad replica");
+    RB_CUDA(b, cudaStreamSynchronize(b->stream));
+    int rc = rp_download_state(h, pos, rot, box9);
+    if (rc) b->err = h->err;
+    return rc;
+}
+
+int rp_batch_count_overlaps(void *batch, int32_t replica, int early_exit, int64_t *count) {
+    Batch *b = static_cast<Batch *>(batch);
+    Handle *h = batch_rep(b, replica);
+    if (!h) return bfail(b, RP_ERR_ARG, "bad replica");
+    RB_CUDA(b, cudaStreamSynchronize(b->stream));
+    int rc = rp_count_overlaps(h, early_exit, count);
+    if (rc) b->err = h->err;
+    return rc;
+}
+
+int rp_batch_set_tuning(void *batch, double cell_factor, int32_t warps_per_block) {
+    Batch *b = static_cast<Batch *>(batch);
+    if (!b || !(cell_factor >= 1.0) || (warps_per_block != 2 && warps_per_block != 4 && warps_per_block != 8))
+        return bfail(b, RP_ERR_ARG, "cell factor >= 1 and 2, 4 or 8 warps per block");
+    for (Handle *h : b->rep) h->cell_factor = cell_factor;
+    b->wpb = warps_per_block;
+    return RP_OK;
+}
+
+int rp_batch_sweep(void *batch, const rp_sweep_params *p, rp_sweep_stats *stats) {
+    Batch *b = static_cast<Batch *>(batch);
+    if (!b || !p) return bfail(b, RP_ERR_ARG, "null argument");
+    int types = (p->translation_step > 0 ? 1 : 0) | (p->rotation_step > 0 ? 2 : 0);
+    if (!types) return bfail(b, RP_ERR_ARG, "no move type enabled");
+    for (Handle *h : b->rep)
+        if (!h->has_state) return bfail(b, RP_ERR_STATE, "a replica has no state");
+    RB_CUDA(b, cudaSetDevice(b->device));
+    const bool log = (p->flags & RP_SWEEP_LOG) != 0;
+    const int ntypes = (types & 1) + ((types >> 1) & 1);
+    std::vector<std::vector<int>> phases(b->R);
+    std::vector<double> tstep(b->R);
+    int cap = 0, maxph = 0;
+    for (int r = 0; r < b->R; r++) {
+        Handle *h = b->rep[r];
+        double shift[3];
+        uint32_t shuffle = 0;
+        sweep_origin(replica_seed(p->seed, r), p->counter, shift, shuffle);
+        int rc = setup_grid(h, h->grid[h->gcur], h->box, shift);
+        if (rc) return bfail(b, rc, h->err);
+        const GridHost &G = h->grid[h->gcur];
+        phase_order(G.d, shuffle, phases[r]);
+        maxph = std::max(maxph, static_cast<int>(phases[r].size()));
+        cap = std::max(cap, G.cap);
+        double hgt[3];
+        heights_of(h->box, hgt);
+        tstep[r] = std::min(p->translation_step, std::min({hgt[0], hgt[1], hgt[2]}) / 2);
+        if (log) {
+            int64_t before = h->log_alloc;
+            RB_CUDA(b, ensure(h->d_log, h->log_alloc, ntypes * h->n));
+            if (!h->d_log_codes || h->log_alloc != before) {
+                cudaFree(h->d_log_codes);
+                h->d_log_codes = nullptr;
+                RB_CUDA(b, cudaMalloc(&h->d_log_codes, h->log_alloc));
+            }
+        }
+    }
+    int total_items = 0, total_p = 0, total_c = 0;
+    int rc = batch_tables(b, total_items, total_p, total_c);
+    if (rc) return rc;
+    BatchRep *T = b->stage[b->cur].table;
+    for (int r = 0; r < b->R; r++) {
+        Handle *h = b->rep[r];
+        SweepArgs &a = T[r].a;
+        a.cap = cap;
+        a.seed = replica_seed(p->seed, r);
+        a.counter = p->counter;
+        a.tstep = static_cast<float>(tstep[r]);
+        a.rstep = static_cast<float>(p->rotation_step);
+        a.types = types;
+        a.rtab64 = b->rtab64;
+        a.rtab32 = b->rtab32;
+        a.rtab_mask = ROT_TABLE - 1;
+        a.fp64_only = (p->flags & RP_SWEEP_FP64_ONLY) ? 1 : 0;
+        if (log) {
+            a.log = h->d_log;
+            a.log_codes = h->d_log_codes;
+        }
+        T[r].nphases = static_cast<int>(phases[r].size());
+        for (int k = 0; k < 8; k++) T[r].phases[k] = k < T[r].nphases ? phases[r][k] : 0;
+    }
+    rc = batch_copy(b);
+    if (rc) return rc;
+    const int *ib = b->d_bases, *pb = b->d_bases + (b->R + 1), *cb = b->d_bases + 2 * (b->R + 1);
+    if (stats) RB_CUDA(b, cudaMemsetAsync(b->stats, 0, sizeof(unsigned long long) * 8 * b->R, b->stream));
+    RB_CUDA(b, launch_b_rebuild(b->d_table, pb, cb, b->R, total_p, total_c, b->stream));
+    b->launches += 5;
+    if (types & 2) {
+        RB_CUDA(b, launch_rot_table(b->rtab64, b->rtab32, ROT_TABLE, p->seed, p->counter,
+                                    static_cast<float>(p->rotation_step), b->stream));
+        b->launches += 1;
+    }
+    RB_CUDA(b, cudaMemsetAsync(b->item_counters, 0, sizeof(int32_t) * 8, b->stream));
+    const int wpb = b->wpb;
+    const int ovf_cap = static_cast<int>(OVF_SMEM / (batch_smem_per_warp(b->kind, 32) / 32)) / 32 * 32;
+    for (int k = 0; k < maxph; k++) {
+        int blocks = std::max(1, std::min((total_items + wpb - 1) / wpb, b->num_sms * (16 / wpb)));
+        RB_CUDA(b, launch_b_sweep(b->d_table, ib, b->R, b->kind, k, b->item_counters + k, cap, wpb, blocks, b->stream));
+        RB_CUDA(b, launch_b_overflow(b->d_table, b->R, b->kind, k, ovf_cap, b->stream));
+        b->launches += 2;
+    }
+    for (int r = 0; r < b->R; r++) {
+        Handle *h = b->rep[r];
+        h->can_revert = false;
+        h->log_valid = false;
+        if (log) {
+            const GridDev &g = h->grid[h->gcur].d;
+            h->log_valid = true;
+            h->log_types = ntypes;
+            h->log_phases = phases[r];
+            for (int d = 0; d < 3; d++) h->log_dims[d] = g.dims[d];
+            h->log_start.resize(g.ncell + 1);
+            RB_CUDA(b, cudaMemcpyAsync(h->log_start.data(), g.start, sizeof(int32_t) * (g.ncell + 1),
+                                       cudaMemcpyDeviceToHost, b->stream));
+        }
+    }
+    if (stats || log) {
+        std::vector<unsigned long long> c(8 * b->R);
+        std::vector<uint32_t> st(b->R);
+        RB_CUDA(b, cudaMemcpyAsync(c.data(), b->stats, sizeof(unsigned long long) * 8 * b->R, cudaMemcpyDeviceToHost,
+                                   b->stream));
+        RB_CUDA(b, cudaMemcpyAsync(st.data(), b->status, sizeof(uint32_t) * b->R, cudaMemcpyDeviceToHost, b->stream));
+        RB_CUDA(b, cudaStreamSynchronize(b->stream));
+        for (int r = 0; r < b->R; r++)
+            if (st[r]) return bfail(b, (st[r] & ST_CAPACITY) ? RP_ERR_CAPACITY : RP_ERR_DEVICE, "device status set");
+        if (stats)
+            for (int r = 0; r < b->R; r++) {
+                const unsigned long long *q = c.data() + 8 * r;
+                stats[r].moves = q[0];
+                stats[r].accepted = q[1];
+                stats[r].rejected_overlap = q[2];
+                stats[r].rejected_domain = q[3];
+                stats[r].pair_tests = q[4];
+                stats[r].fp64_pairs = q[5];
+                stats[r].translations = q[6];
+                stats[r].rotations = q[7];
+                stats[r].kernel_launches = b->launches;
+            }
+    }
+    return RP_OK;
+}
+
+int rp_batch_sweep_log(void *batch, int32_t replica, rp_move *moves, uint8_t *codes, int64_t capacity,
+                       int64_t *count) {
+    Batch *b = static_cast<Batch *>(batch);
+    Handle *h = batch_rep(b, replica);
+    if (!h) return bfail(b, RP_ERR_ARG, "bad replica");
+    RB_CUDA(b, cudaStreamSynchronize(b->stream));
+    int rc = rp_sweep_log(h, moves, codes, capacity, count);
+    if (rc) b->err = h->err;
+    return rc;
+}
+
+int rp_batch_get_grid(void *batch, int32_t replica, rp_grid_info *info, int32_t *cells, double *bounds) {
+    Batch *b = static_cast<Batch *>(batch);
+    Handle *h = batch_rep(b, replica);
+    if (!h) return bfail(b, RP_ERR_ARG, "bad replica");
+    RB_CUDA(b, cudaStreamSynchronize(b->stream));
+    int rc = rp_get_grid(h, info, cells, bounds);
+    if (rc) b->err = h->err;
+    return rc;
+}
+
+int rp_batch_try_scaling(void *batch, const double *boxes, const uint8_t *propose, double *dE) {
+    Batch *b = static_cast<Batch *>(batch);
+    if (!b || !boxes || !propose || !dE) return bfail(b, RP_ERR_ARG, "null argument");
+    RB_CUDA(b, cudaSetDevice(b->device));
+    std::vector<uint8_t> upscaled(b->R, 0);
+    std::vector<double> old_inv(9 * b->R);
+    for (int r = 0; r < b->R; r++) {
+        Handle *h = b->rep[r];
+        dE[r] = 0;
+        if (!propose[r]) continue;
+        const double *nb = boxes + 9 * r;
+        if (!h->has_state) return bfail(b, RP_ERR_STATE, "a replica has no state");
+        if (det3(nb) == 0 || volume_of(nb) == 0) return bfail(b, RP_ERR_ARG, "box volume is zero");
+        std::memcpy(old_inv.data() + 9 * r, h->inv, sizeof(h->inv));
+        double new_inv[9];
+        inverse3(nb, new_inv);
+        std::memcpy(h->saved_box, h->box, sizeof(h->box));
+        std::memcpy(h->saved_inv, h->inv, sizeof(h->inv));
+        std::memcpy(h->box, nb, sizeof(h->box));
+        std::memcpy(h->inv, new_inv, sizeof(h->inv));
+        int old_g = h->gcur;
+        h->pcur = 1 - h->pcur;
+        h->gcur = 1 - h->gcur;
+        double shift[3] = {h->grid[old_g].d.shift[0], h->grid[old_g].d.shift[1], h->grid[old_g].d.shift[2]};
+        int rc = setup_grid(h, h->grid[h->gcur], h->box, shift);
+        if (rc) {
+            // undo this replica's switch; the replicas already switched are reverted by the caller
+            std::memcpy(h->box, h->saved_box, sizeof(h->box));
+            std::memcpy(h->inv, h->saved_inv, sizeof(h->inv));
+            h->pcur = 1 - h->pcur;
+            h->gcur = old_g;
+            return bfail(b, rc, h->err);
+        }
+        h->can_revert = true;
+        h->log_valid = false;
+        h->partners_valid = false;
+        upscaled[r] = box_upscaled(h->saved_box, h->box) ? 1 : 0;  // convex shapes only in a batch
+    }
+    int total_items = 0, total_p = 0, total_c = 0;
+    int rc = batch_tables(b, total_items, total_p, total_c);
+    if (rc) return rc;
+    BatchRep *T = b->stage[b->cur].table;
+    for (int r = 0; r < b->R; r++) {
+        Handle *h = b->rep[r];
+        T[r].scale = propose[r] ? 1 : 0;
+        b->h_flags[r] = (propose[r] && !upscaled[r]) ? 0 : 1;  // a set flag skips the recount
+        if (!propose[r]) continue;
+        std::memcpy(T[r].old_inv, old_inv.data() + 9 * r, sizeof(T[r].old_inv));
+        std::memcpy(T[r].new_box, h->box, sizeof(T[r].new_box));
+        T[r].scale_src = h->pos64[1 - h->pcur];
+        T[r].scale_dst = h->pos64[h->pcur];
+        T[r].trans_dst = h->trans[h->pcur];
+    }
+    rc = batch_copy(b);
+    if (rc) return rc;
+    const int *pb = b->d_bases + (b->R + 1), *cb = b->d_bases + 2 * (b->R + 1);
+    RB_CUDA(b, cudaMemcpyAsync(b->flags, b->h_flags, sizeof(int) * b->R, cudaMemcpyHostToDevice, b->stream));
+    RB_CUDA(b, cudaMemsetAsync(b->counts, 0, sizeof(unsigned long long) * b->R, b->stream));
+    RB_CUDA(b, launch_b_rescale(b->d_table, pb, b->R, total_p, b->stream));
+    RB_CUDA(b, launch_b_rebuild(b->d_table, pb, cb, b->R, total_p, total_c, b->stream));
+    RB_CUDA(b, launch_b_count(b->d_table, pb, b->R, total_p, b->kind, 1, b->counts, b->flags, b->stream));
+    b->launches += 8;
+    RB_CUDA(b, cudaMemcpyAsync(b->h_counts, b->counts, sizeof(unsigned long long) * b->R, cudaMemcpyDeviceToHost,
+                               b->stream));
+    RB_CUDA(b, cudaStreamSynchronize(b->stream));
+    for (int r = 0; r < b->R; r++)
+        if (propose[r] && !upscaled[r] && b->h_counts[r] > 0) dE[r] = std::numeric_limits<double>::infinity();
+    return RP_OK;
+}
+
+int rp_batch_revert_scaling(void *batch, const uint8_t *mask) {
+    Batch *b = static_cast<Batch *>(batch);
+    if (!b || !mask) return bfail(b, RP_ERR_ARG, "null argument");
+    RB_CUDA(b, cudaStreamSynchronize(b->stream));
+    for (int r = 0; r < b->R; r++)
+        if (mask[r]) {
+            int rc = rp_revert_scaling(b->rep[r]);
+            if (rc) return bfail(b, rc, b->rep[r]->err);
+        }
     return RP_OK;
 }
 

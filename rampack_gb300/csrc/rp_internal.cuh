@@ -143,4 +143,19 @@ struct SweepArgs {
     float inv_range;
 };
 
+// One replica of a batched launch (rp_batch_*): its sweep arguments, this sweep's phase
+// order, and its box move when the batch rescales it.  Particles, cells and sweep items of
+// all replicas are numbered consecutively; the prefix offsets live in separate compact
+// arrays that the kernels search.
+struct BatchRep {
+    SweepArgs a;
+    int phases[8];
+    int nphases;
+    int scale;                     // 1: this replica's positions are rescaled (box move)
+    double old_inv[9], new_box[9];
+    const double *scale_src;
+    double *scale_dst;
+    double *trans_dst;             // translation table of the new box
+};
+
 }  // namespace rp

@@ -251,3 +251,118 @@ class GpuPacking:
 
 
 INF = math.inf
+
+
+class BatchPacking:
+    """Many independent packings of one shape kind advanced together (rp_batch_*).
+
+    ``systems`` is a list of (pos, rot, box); every replica shares the shape ``kind`` and
+    ``params`` (sphere radius, or spherocylinder length and radius)."""
+
+    def __init__(self, kind: int, params, systems, device: int = 0):
+        self.lib = _lib.load()
+        params = np.asarray(params, dtype=np.float64).reshape(-1)
+        desc = ShapeDesc()
+        desc.kind = kind
+        if kind == _lib.SHAPE_SPHERE:
+            desc.radius = float(params[0])
+        elif kind == _lib.SHAPE_SPHEROCYLINDER:
+            desc.length, desc.radius = float(params[0]), float(params[1])
+        else:
+            raise EngineError(-5, f"shape kind {kind} is not batched")
+        self.kind, self.params = kind, params
+        self.sizes = [len(np.asarray(p).reshape(-1, 3)) for p, _, _ in systems]
+        self.R = len(systems)
+        n = (C.c_int64 * self.R)(*self.sizes)
+        h = C.c_void_p()
+        rc = self.lib.rp_batch_create(C.byref(desc), self.R, n, device, C.byref(h))
+        if rc != 0:
+            raise EngineError(rc, "rp_batch_create failed")
+        self.h = h
+        for r, (pos, rot, box) in enumerate(systems):
+            self.upload(r, pos, rot, box)
+
+    def _check(self, rc: int):
+        if rc != 0:
+            msg = self.lib.rp_batch_last_error(self.h)
+            raise EngineError(rc, msg.decode() if msg else "")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.rp_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def upload(self, r: int, pos, rot, box):
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        rot = np.ascontiguousarray(rot, dtype=np.float64).reshape(-1, 9)
+        box = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
+        self._check(self.lib.rp_batch_upload_state(self.h, r, dptr(pos), dptr(rot), dptr(box)))
+
+    def state(self, r: int):
+        n = self.sizes[r]
+        pos, rot, box = np.zeros((n, 3)), np.zeros((n, 9)), np.zeros(9)
+        self._check(self.lib.rp_batch_download_state(self.h, r, dptr(pos), dptr(rot), dptr(box)))
+        return pos, rot, box
+
+    def count_total_overlaps(self, r: int, early_exit: bool = False) -> int:
+        c = C.c_int64()
+        self._check(self.lib.rp_batch_count_overlaps(self.h, r, 1 if early_exit else 0, C.byref(c)))
+        return int(c.value)
+
+    def grid(self, r: int):
+        info = GridInfo()
+        self._check(self.lib.rp_batch_get_grid(self.h, r, C.byref(info), None, None))
+        cells = np.zeros(self.sizes[r], dtype=np.int32)
+        bounds = np.zeros((int(info.num_cells), 6))
+        self._check(self.lib.rp_batch_get_grid(self.h, r, None, cells.ctypes.data_as(C.POINTER(C.c_int32)),
+                                               dptr(bounds)))
+        return GpuPacking._info(info), cells, bounds
+
+    def sweep(self, translation_step: float, rotation_step: float, seed: int, counter: int, log: bool = False,
+              stats: bool = True, fp64_only: bool = False):
+        p = SweepParams()
+        p.translation_step, p.rotation_step, p.seed, p.counter = translation_step, rotation_step, seed, counter
+        p.flags = (_lib.SWEEP_LOG if log else 0) | (_lib.SWEEP_FP64_ONLY if fp64_only else 0)
+        st = (SweepStats * self.R)() if stats else None
+        self._check(self.lib.rp_batch_sweep(self.h, C.byref(p), st))
+        return [s.as_dict() for s in st] if stats else None
+
+    def sweep_log(self, r: int):
+        cnt = C.c_int64()
+        self._check(self.lib.rp_batch_sweep_log(self.h, r, None, None, 0, C.byref(cnt)))
+        moves = np.zeros(cnt.value, dtype=MOVE_DTYPE)
+        codes = np.zeros(cnt.value, dtype=np.uint8)
+        self._check(self.lib.rp_batch_sweep_log(self.h, r, moves.ctypes.data_as(C.c_void_p),
+                                                codes.ctypes.data_as(C.c_void_p), cnt.value, C.byref(cnt)))
+        return moves, codes
+
+    def try_scaling(self, boxes, propose) -> np.ndarray:
+        b = np.ascontiguousarray(boxes, dtype=np.float64).reshape(self.R, 9)
+        m = np.ascontiguousarray(propose, dtype=np.uint8).reshape(self.R)
+        dE = np.zeros(self.R)
+        self._check(self.lib.rp_batch_try_scaling(self.h, dptr(b), m.ctypes.data_as(C.c_void_p), dptr(dE)))
+        return dE
+
+    def revert_scaling(self, mask):
+        m = np.ascontiguousarray(mask, dtype=np.uint8).reshape(self.R)
+        self._check(self.lib.rp_batch_revert_scaling(self.h, m.ctypes.data_as(C.c_void_p)))
+
+    def set_tuning(self, cell_factor: float = 1.0, warps_per_block: int = 4):
+        self._check(self.lib.rp_batch_set_tuning(self.h, cell_factor, warps_per_block))
+
+
+def replica_seed(seed: int, r: int) -> int:
+    """The sweep seed replica r of a batch uses (rp_batch_sweep)."""
+    return (seed + _lib.BATCH_SEED_STRIDE * r) % (1 << 64)
