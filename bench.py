@@ -80,6 +80,11 @@ WORKLOADS = {
                    "120 degrees), N={n:,} (50x80x25), aligned orthorhombic start at phi=0.45, triclinic box; per "
                    "cycle 2N moves (translation 0.2, rotation 0.2) + 1 isotension box move (delta 0.005, p*=1.5, "
                    "T=1)", "moves/sec, bent chains N=1e5"),
+    "replicas-64": (None, "64 replicas: 32 hard-sphere (r=0.5) and 32 spherocylinder (l=3, r=0.5) systems, "
+                    "N_i = round(exp(U(ln 500, ln 20000))) (seeded; {n:,} particles in all), pressures log-spaced "
+                    "on [1, 20], lattice start at phi=0.30, triclinic boxes; per cycle one translation (0.2) per "
+                    "sphere, a translation (0.2) and a rotation (0.2) per spherocylinder, one isotension box move "
+                    "(delta 0.005, T=1) per replica", "moves/sec, 64 replicas"),
     "sc-64000": (_sc_64000, "hard spherocylinders l=5 r=0.5, N={n:,} (40^3), aligned orthorhombic start at "
                  "phi=0.35 (cell aspect 1:1:6), triclinic box; per cycle 2N moves (translation 0.2, rotation "
                  "0.2) + 1 isotension box move (delta 0.005, p*=1.5, T=1)", "moves/sec, spherocylinders N=64000"),
@@ -510,12 +515,140 @@ def main_ordering(args):
     return 0
 
 
+def _replica_cpu(job):
+    """One replica of the CPU baseline (spawned worker): `cycles` timed cycles after one."""
+    kind, prm, pos, rot, box, pressure, cycles, seed = job
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    pk = po.CpuPacking("oracle", kind, prm, pos, rot, box, threads=1)
+    kw = dict(translation_step=TRANS_STEP, rotation_step=ROT_STEP if kind == 1 else 0.0, box_kind=1,
+              box_step=BOX_STEP, pressure=pressure, temperature=TEMPERATURE)
+    po.run_cycles(pk, 1, seed=seed, **kw)
+    t = time.perf_counter()
+    po.run_cycles(pk, cycles, seed=seed + 1, **kw)
+    dt = time.perf_counter() - t
+    pk.close()
+    return (2 if kind == 1 else 1) * len(pos) * cycles, dt
+
+
+def main_replicas(args):
+    """64 replicas in two batches (one per shape), every step of a batch one launch for all
+    its replicas; box moves proposed and pre-checked on the host per replica (isotension
+    delta 0.005, each replica at its own pressure), overlap checks batched.  The launch shape
+    (cell factor x warps per block) is autotuned first."""
+    import multiprocessing as mp
+    from rampack_gb300 import workloads as W
+    reps = W.config_replicas_64(args.seed)
+    # the CPU baseline first, in spawned workers, before this process touches the GPU
+    cpu_base = None
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        sample = list(range(0, 64, 4))
+        jobs = [tuple(reps[i][:5]) + (reps[i][5], 2, args.seed + i) for i in sample]
+        ctx = mp.get_context("spawn")
+        t0 = time.perf_counter()
+        with ctx.Pool(min(threads, len(jobs))) as pool:
+            res = pool.map(_replica_cpu, jobs)
+        wall = time.perf_counter() - t0
+        moves = sum(m for m, _ in res)
+        busy = max(d for _, d in res)
+        cpu_base = {"value": moves / busy, "unit": UNIT, "cores": min(threads, len(jobs)), "kind": "port",
+                    "sample": f"16 of the 64 replicas (every 4th), one per spawned process, 2 timed cycles after 1; "
+                              f"value = their moves / the slowest replica's time (wall {wall:.1f} s incl. start-up)"}
+
+    from rampack_gb300 import build as rb
+    rb.build()
+    from rampack_gb300.packing import BatchPacking
+    groups = {k: [i for i in range(64) if reps[i][0] == k] for k in (0, 1)}
+    batches = {k: BatchPacking(k, reps[idx[0]][1], [reps[i][2:5] for i in idx]) for k, idx in groups.items()}
+    steps = {0: (TRANS_STEP, 0.0), 1: (TRANS_STEP, ROT_STEP)}
+    boxes = {k: [np.array(reps[i][4], dtype=np.float64) for i in idx] for k, idx in groups.items()}
+    sizes = {k: [len(reps[i][2]) for i in idx] for k, idx in groups.items()}
+    press = {k: [reps[i][5] for i in idx] for k, idx in groups.items()}
+    rng = np.random.default_rng(args.seed)
+    moves_per_cycle = sum(sizes[0]) + 2 * sum(sizes[1])
+    state = {"k": 0, "box_acc": 0}
+
+    def one_cycle():
+        k = state["k"]
+        for kind, b in batches.items():
+            b.sweep(*steps[kind], seed=args.seed + kind, counter=k, stats=False)
+        for kind, b in batches.items():
+            R = b.R
+            new, prop = [], np.zeros(R, dtype=np.uint8)
+            for j in range(R):
+                box = boxes[kind][j]
+                nb = propose_box(box, rng)
+                v0, v1 = box_volume(box), box_volume(nb)
+                expo = sizes[kind][j] * math.log(v1 / v0) - press[kind][j] * (v1 - v0) / TEMPERATURE
+                prop[j] = rng.uniform() <= math.exp(min(expo, 700.0))
+                new.append(nb if prop[j] else box)
+            dE = b.try_scaling(np.array(new), prop)
+            bad = (prop == 1) & (dE > 0)
+            b.revert_scaling(bad.astype(np.uint8))
+            for j in range(R):
+                if prop[j] and not bad[j]:
+                    boxes[kind][j] = new[j]
+                    state["box_acc"] += 1
+        state["k"] += 1
+
+    # autotune the launch shape: cell factor x warps per block
+    tune = []
+    for cf in (1.0, 1.1, 1.25):
+        for wpb in (2, 4, 8):
+            for b in batches.values():
+                b.set_tuning(cf, wpb)
+            one_cycle()
+            t = time.perf_counter()
+            for _ in range(3):
+                one_cycle()
+            tune.append({"cell_factor": cf, "warps_per_block": wpb, "ms_per_cycle": (time.perf_counter() - t) / 3 * 1e3})
+    best = min(tune, key=lambda x: x["ms_per_cycle"])
+    for b in batches.values():
+        b.set_tuning(best["cell_factor"], best["warps_per_block"])
+    for _ in range(max(3, args.warmup)):
+        one_cycle()
+    s0 = {k: b.sweep(*steps[k], seed=args.seed + 99, counter=0, stats=True) for k, b in batches.items()}
+    acc = sum(x["accepted"] for v in s0.values() for x in v) / max(1, sum(x["moves"] for v in s0.values() for x in v))
+    state["box_acc"] = 0
+    clocks = Clocks(0)
+    clocks.start()
+    time.sleep(0.3)
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.time()
+    tp = time.perf_counter()
+    for _ in range(args.steps):
+        one_cycle()
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - tp
+    clk = clocks.stop(t0, time.time())
+    value = moves_per_cycle * args.steps / dt
+    n = sum(len(r[2]) for r in reps)
+    for b in batches.values():
+        b.close()
+    print(json.dumps({
+        "metric": "moves/sec, 64 replicas", "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOADS["replicas-64"][1].format(n=n), "n": n, "moves_per_step": moves_per_cycle,
+                   "timing": "host wall clock per cycle (both batches, host box-move pre-checks and the batched "
+                             "overlap checks; each cycle ends in a device synchronisation)",
+                   "autotune": tune, "tuning": best, "box_moves_accepted": state["box_acc"],
+                   "l2": "inputs smaller than L2 (no flush between steps)"},
+        "acceptance": acc, "roofline": None, "e2e": None, "clocks": clk, "cpu_baseline": cpu_base,
+    }))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return main_reference(args)
     if args.ordering:
         return main_ordering(args)
+    if args.workload == "replicas-64":
+        return main_replicas(args)
     return main_gpu(args)
 
 

@@ -683,6 +683,7 @@ struct Batch {
     unsigned long long *counts = nullptr, *h_counts = nullptr;  // [R]
     int *flags = nullptr, *h_flags = nullptr;         // [R]
     int wpb = 4;
+    int smem_optin = 48 * 1024;                       // largest dynamic shared memory per block
     uint64_t launches = 0;
     std::string err;
 };
@@ -1861,6 +1862,7 @@ int rp_batch_create(const rp_shape_desc *shape, int32_t replicas, const int64_t 
     };
     if (cudaSetDevice(device) != cudaSuccess) return bail(RP_ERR_CUDA);
     cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, device);
+    cudaDeviceGetAttribute(&b->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(RP_ERR_CUDA);
     const int R = replicas;
     bool ok = cudaMalloc(&b->d_table, sizeof(BatchRep) * R) == cudaSuccess &&
@@ -2034,6 +2036,12 @@ int rp_batch_sweep(void *batch, const rp_sweep_params *p, rp_sweep_stats *stats)
             }
         }
     }
+    // the staging capacity of every replica: two warps per block must fit
+    {
+        const size_t per_cap = batch_smem_per_warp(b->kind, 32) / 32;
+        const int fit = static_cast<int>(static_cast<size_t>(b->smem_optin) / 2 / per_cap) / 32 * 32;
+        cap = std::min(cap, fit);
+    }
     int total_items = 0, total_p = 0, total_c = 0;
     int rc = batch_tables(b, total_items, total_p, total_c);
     if (rc) return rc;
@@ -2070,7 +2078,10 @@ int rp_batch_sweep(void *batch, const rp_sweep_params *p, rp_sweep_stats *stats)
         b->launches += 1;
     }
     RB_CUDA(b, cudaMemsetAsync(b->item_counters, 0, sizeof(int32_t) * 8, b->stream));
-    const int wpb = b->wpb;
+    // fewer warps per block when the staging of `cap` candidates per warp would not fit
+    int wpb = b->wpb;
+    while (wpb > 2 && static_cast<size_t>(wpb) * batch_smem_per_warp(b->kind, cap) > static_cast<size_t>(b->smem_optin))
+        wpb /= 2;
     const int ovf_cap = static_cast<int>(OVF_SMEM / (batch_smem_per_warp(b->kind, 32) / 32)) / 32 * 32;
     for (int k = 0; k < maxph; k++) {
         int blocks = std::max(1, std::min((total_items + wpb - 1) / wpb, b->num_sms * (16 / wpb)));

@@ -157,3 +157,37 @@ def config_banana_1e5():
     length 0.6: arc angle 120 degrees, arc radius 0.6 / (2 sin 15 degrees)),
     N = 100,000 (50 x 80 x 25), aligned, phi = 0.45."""
     return bananas((50, 80, 25), 0.45, 0.6 / (2 * math.sin(math.radians(15))), math.radians(120), 5)
+
+
+def replica_lattice(kind: int, n: int, phi: float, length: float = 3.0, radius: float = 0.5):
+    """N particles (spheres, or spherocylinders aligned along z) on the first N sites of an
+    orthorhombic lattice whose cell aspect follows the particle's extents, in a box of
+    packing fraction phi."""
+    if kind == SPHERE:
+        v, aspect = sphere_volume(radius), np.array([1.0, 1.0, 1.0])
+    else:
+        v, aspect = spherocylinder_volume(length, radius), np.array([1.0, 1.0, (length + 2 * radius) / (2 * radius)])
+    m = max(1, int(math.ceil((n * aspect[2]) ** (1.0 / 3.0))))  # a near-cubic box
+    q = int(math.ceil(n / (m * m)))
+    a = (n * v / phi / (aspect[2] * m * m * q)) ** (1.0 / 3.0)
+    cell = a * aspect
+    if kind == SPHERE and a < 2 * radius or kind == SPHEROCYLINDER and (a < 2 * radius or cell[2] < length + 2 * radius):
+        raise ValueError("packing fraction too high for the lattice")
+    pos = lattice((m, m, q), cell)[:n]
+    prm = np.array([radius]) if kind == SPHERE else np.array([length, radius])
+    return kind, prm, np.ascontiguousarray(pos), aligned_rotations(n), diag_box(cell[0] * m, cell[1] * m, cell[2] * q)
+
+
+def config_replicas_64(seed: int = 1234):
+    """64 replicas: 32 hard-sphere (r=0.5) and 32 spherocylinder (l=3, r=0.5) systems with
+    N_i = round(exp(U(ln 500, ln 20000))) (numpy generator seeded with `seed`), pressures
+    log-spaced on [1, 20], started on lattices at phi=0.30.  Returns a list of
+    (kind, params, pos, rot, box, pressure)."""
+    rng = np.random.default_rng(seed)
+    sizes = np.round(np.exp(rng.uniform(math.log(500), math.log(20000), 64))).astype(int)
+    pressures = np.exp(np.linspace(math.log(1.0), math.log(20.0), 64))
+    out = []
+    for i in range(64):
+        kind = SPHERE if i < 32 else SPHEROCYLINDER
+        out.append(replica_lattice(kind, int(sizes[i]), 0.30) + (float(pressures[i]),))
+    return out
