@@ -10,8 +10,6 @@
 
 namespace rp {
 
-size_t batch_smem_per_warp(int kind, int cap);
-
 namespace {
 
 // Largest r with base[r] <= x (base ascending, base[0] = 0, base[R] = total).
@@ -158,9 +156,8 @@ __global__ void __launch_bounds__(WPB * 32, 16 / WPB)
     extern __shared__ float4 smem[];
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int per_warp = cap * (KIND == 1 ? 2 : 1) + cap / 4 + cap / 16 + (KIND == 1 ? SWEEP_ROT_STAGE : 0);
+    const int per_warp = cap * (KIND == 1 ? 2 : 1) + cap / 4 + cap / 16;
     float4 *cpos = smem + (size_t)wib * per_warp;
-    float4 *rtab_s = cpos + per_warp - SWEEP_ROT_STAGE;
     float4 *cax = cpos + cap;
     uint16_t *qseg = reinterpret_cast<uint16_t *>(cpos + cap * (KIND == 1 ? 2 : 1));
     uint16_t *qun = qseg + cap;
@@ -187,7 +184,7 @@ __global__ void __launch_bounds__(WPB * 32, 16 / WPB)
         for (int d = 0; d < 3; d++) c[d] = G.dims[d] == 1 ? 0 : 2 * cc[d] + ((ph >> d) & 1);
         const int cell = c[0] + G.dims[0] * (c[1] + G.dims[1] * c[2]);
         sweep_cell<KIND, false, false>(A, local, cell, cap, A.overflow, A.overflow_count, cpos, cax, qseg, qun, nacc,
-                                       nullptr, nullptr, nullptr, rtab_s, ws);
+                                       nullptr, nullptr, nullptr, ws);
         __syncwarp();
         flush_stats(A, ws);
     }
@@ -203,14 +200,13 @@ __global__ void __launch_bounds__(32) k_b_overflow(const BatchRep *T, int k, int
     if (count == 0) return;
     float4 *cpos = smem;
     float4 *cax = cpos + cap;
-    float4 *rtab_s = cpos + cap * (KIND == 1 ? 2 : 1) + cap / 4 + cap / 16;
     uint16_t *qseg = reinterpret_cast<uint16_t *>(cpos + cap * (KIND == 1 ? 2 : 1));
     uint16_t *qun = qseg + cap;
     uint8_t *nacc = reinterpret_cast<uint8_t *>(qun + cap);
     WarpStats ws = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int q = 0; q < count; q++) {
         sweep_cell<KIND, false, false>(A, q, A.overflow[q], cap, nullptr, nullptr, cpos, cax, qseg, qun, nacc,
-                                       nullptr, nullptr, nullptr, rtab_s, ws);
+                                       nullptr, nullptr, nullptr, ws);
         __syncwarp();
     }
     flush_stats(A, ws);
@@ -221,7 +217,7 @@ __global__ void __launch_bounds__(32) k_b_overflow(const BatchRep *T, int k, int
 template <int KIND, int WPB>
 cudaError_t launch_b_sweep_t(const BatchRep *T, const int *item_base, int R, int k, int *next_item, int cap,
                              int blocks, cudaStream_t st) {
-    const size_t smem = (size_t)WPB * batch_smem_per_warp(KIND, cap);
+    const size_t smem = (size_t)WPB * (cap * (KIND == 1 ? 2 : 1) + cap / 4 + cap / 16) * sizeof(float4);
     cudaError_t e = cudaFuncSetAttribute(k_b_sweep<KIND, WPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k_b_sweep<KIND, WPB><<<blocks, WPB * 32, smem, st>>>(T, item_base, R, k, next_item, cap);
@@ -258,7 +254,7 @@ cudaError_t launch_b_count(const BatchRep *T, const int *pbase, int R, int total
 }
 
 size_t batch_smem_per_warp(int kind, int cap) {
-    return (size_t)(cap * (kind == 1 ? 2 : 1) + cap / 4 + cap / 16 + (kind == 1 ? SWEEP_ROT_STAGE : 0)) * sizeof(float4);
+    return (size_t)(cap * (kind == 1 ? 2 : 1) + cap / 4 + cap / 16) * sizeof(float4);
 }
 
 cudaError_t launch_b_sweep(const BatchRep *T, const int *item_base, int R, int kind, int k, int *next_item, int cap,

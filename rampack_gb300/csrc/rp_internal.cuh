@@ -95,8 +95,6 @@ constexpr int MAX_CEN = RP_MAX_CENTRES;
 // [MAX_CEN], the centre-pair thresholds [2 MAX_CEN^2 floats], the mover's exact centres
 // and absolute centres [2 x 3 MAX_CEN doubles]
 constexpr int SWEEP_POLY_SCRATCH = MAX_CEN + MAX_CEN * MAX_CEN / 2 + 3 * MAX_CEN;
-// per-warp staging of the FP32 rotations of 32 consecutive moves (float4 units)
-constexpr int SWEEP_ROT_STAGE = 32 * 3;
 
 constexpr int SWEEP_WARPS = 4;       // warps per block of the sweep kernel
 constexpr int SWEEP_MIN_BLOCKS = 4;  // resident blocks per SM the register budget allows

@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(co
     const int K = KIND == 2 ? A.s.ncen : 0;
     const int extra = KIND == 1 ? A.cap : (KIND == 2 ? A.cap * 3 * K / 4 : 0);
     const int per_warp = A.cap + extra + A.cap / 4 + A.cap / 16 + (LEARN ? A.cap / 4 : 0) +
-                         (KIND == 2 ? SWEEP_POLY_SCRATCH : 0) + (KIND >= 1 ? SWEEP_ROT_STAGE : 0);
+                         (KIND == 2 ? SWEEP_POLY_SCRATCH : 0);
     float4 *cpos = smem + (size_t)wib * per_warp;
     float4 *cax = cpos + A.cap;                                  // spherocylinders
     float *ccen = reinterpret_cast<float *>(cpos + A.cap);       // polyspheres
@@ -200,7 +200,6 @@ __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(co
     uint8_t *nacc = reinterpret_cast<uint8_t *>(qun + A.cap);
     uint16_t *pstage = reinterpret_cast<uint16_t *>(nacc + A.cap);  // LEARN only: MLP_PARTNERS x cap
     float4 *wx = reinterpret_cast<float4 *>(nacc + A.cap);          // polyspheres (never with LEARN)
-    float4 *rtab_s = cpos + per_warp - SWEEP_ROT_STAGE;              // rotations of 32 moves (KIND >= 1)
     int nitems = A.work ? *A.work_count : (LIST ? A.num_list : A.num_active);
     WarpStats ws = {0, 0, 0, 0, 0, 0, 0, 0};
     // persistent launches (next_item set) take cells from a shared counter until none are
@@ -215,7 +214,7 @@ __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(co
         }
         if (item >= nitems) break;
         sweep_cell<KIND, LIST, LEARN>(A, item, -1, A.cap, A.overflow, A.overflow_count, cpos, cax, qseg, qun, nacc,
-                                      pstage, ccen, wx, rtab_s, ws);
+                                      pstage, ccen, wx, ws);
         __syncwarp();
         item += stride;
     }
@@ -282,8 +281,7 @@ cudaError_t launch_abs_centres(const DevState &s, cudaStream_t st) {
 
 size_t sweep_smem_per_warp(int kind, int cap, bool learn, int ncen) {
     const int extra = kind == 1 ? cap : (kind == 2 ? cap * 3 * ncen / 4 : 0);
-    return (size_t)(cap + extra + cap / 4 + cap / 16 + (learn ? cap / 4 : 0) + (kind == 2 ? SWEEP_POLY_SCRATCH : 0) +
-                    (kind >= 1 ? SWEEP_ROT_STAGE : 0)) *
+    return (size_t)(cap + extra + cap / 4 + cap / 16 + (learn ? cap / 4 : 0) + (kind == 2 ? SWEEP_POLY_SCRATCH : 0)) *
            sizeof(float4);
 }
 

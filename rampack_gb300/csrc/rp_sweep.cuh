@@ -175,7 +175,7 @@ template <int KIND, bool LIST, bool LEARN>
 __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, const int cell_direct, const int cap,
                                            int32_t *ovf, int32_t *ovf_count, float4 *cpos, float4 *cax,
                                            uint16_t *qseg, uint16_t *qun, uint8_t *nacc, uint16_t *pstage,
-                                           float *ccen, float4 *wx, float4 *rtab_s, WarpStats &ws) {
+                                           float *ccen, float4 *wx, WarpStats &ws) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -320,18 +320,6 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
             rnd_lane = philox(u4{(uint32_t)(mi + lane), (uint32_t)cell, (uint32_t)A.counter,
                                  (uint32_t)(A.counter >> 32)},
                               (uint32_t)A.seed, (uint32_t)(A.seed >> 32));
-            if (KIND >= 1) {
-                // the FP32 rotations of these 32 moves, fetched at once (one table entry per
-                // lane) into shared memory, off the moves' critical path
-                const bool rot_l = ntypes == 2 ? (rnd_lane.a >> 31) != 0 : (A.types & 1) == 0;
-                if (rot_l && mi + lane < nmoves) {
-                    const float4 *R4 = reinterpret_cast<const float4 *>(A.rtab32) + 3 * (size_t)(rnd_lane.b & A.rtab_mask);
-                    rtab_s[3 * lane] = R4[0];
-                    rtab_s[3 * lane + 1] = R4[1];
-                    rtab_s[3 * lane + 2] = R4[2];
-                }
-                __syncwarp();
-            }
         }
         // ---- the proposal (FP32 view; FP64 inputs kept for the exact path) ----
         int type, slot = -1, out_index = -1;
@@ -382,7 +370,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                 rot_idx = r.b & A.rtab_mask;
                 rot_inv = (r.c & 1u) != 0;
                 if (KIND >= 1) {
-                    const float4 *R4 = rtab_s + 3 * (mi & 31);
+                    const float4 *R4 = reinterpret_cast<const float4 *>(A.rtab32) + 3 * (size_t)rot_idx;
                     float4 x0 = R4[0], x1 = R4[1], x2 = R4[2];
                     float R[9] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w, x2.x};
                     for (int q = 0; q < 9; q++) R32[q] = rot_inv ? R[3 * (q % 3) + q / 3] : R[q];
