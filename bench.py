@@ -380,24 +380,19 @@ def main_gpu(args):
     if not args.no_e2e:
         hpos = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
         hrot = torch.empty((n, 9), dtype=torch.float64, pin_memory=True).numpy()
-        p0, r0, b0 = g.state()
-        hpos[:] = p0
-        hrot[:] = r0
-        hbox = b0.copy()
+        hbox = torch.empty(9, dtype=torch.float64, pin_memory=True).numpy()
+        g.state(out=(hpos, hrot, hbox))
         torch.cuda.synchronize()
         e_steps = max(1, args.steps)
         f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         m0 = g.stats()["moves"]
         f0.record(stream)
         for _ in range(e_steps):
-            g.upload(hpos, hrot, hbox)   # H2D of the step's input state
+            g.upload(hpos, hrot, hbox)   # H2D of the step's input state (pinned)
             g.box = hbox.copy()
             cycle(g, k, seed, rng)
             k += 1
-            p1, r1, b1 = g.state()       # D2H of the step's result
-            hpos[:] = p1
-            hrot[:] = r1
-            hbox = b1
+            g.state(out=(hpos, hrot, hbox))  # D2H of the step's result into the same pinned buffers
         f1.record(stream)
         f1.synchronize()
         e_ms = f0.elapsed_time(f1)
@@ -406,7 +401,7 @@ def main_gpu(args):
             e_ms = reduce_max(e_ms, dist, device=f"cuda:{local}")
         e2e = {"value": e_moves * world / (e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": int(n * 12 * 8),
                "d2h_bytes_per_step": int(n * 12 * 8),
-               "step": "rp_upload_state (pinned host -> device) + one cycle + rp_download_state"}
+               "step": "rp_upload_state (pinned host -> device) + one cycle + rp_download_state (device -> pinned host)"}
 
     # ---- CPU baseline (rank 0, N=1 only) ----
     cpu_base = None

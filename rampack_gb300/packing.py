@@ -90,10 +90,15 @@ class GpuPacking:
             raise EngineError(-1, "state size mismatch")
         self._check(self.lib.rp_upload_state(self.h, dptr(pos), dptr(rot), dptr(box)))
 
-    def state(self):
-        pos = np.zeros((self.n, 3))
-        rot = np.zeros((self.n, 9))
-        box = np.zeros(9)
+    def state(self, out=None):
+        """(positions N x 3, orientations N x 9, box 9).  With out = (pos, rot, box), downloads
+        into those C-contiguous float64 arrays (pinned host memory makes it a direct DMA)."""
+        if out is None:
+            out = (np.zeros((self.n, 3)), np.zeros((self.n, 9)), np.zeros(9))
+        pos, rot, box = out
+        for a, shape in ((pos, (self.n, 3)), (rot, (self.n, 9)), (box, (9,))):
+            if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"] or a.size != int(np.prod(shape)):
+                raise EngineError(-1, "state buffers must be C-contiguous float64 of the packing's size")
         self._check(self.lib.rp_download_state(self.h, dptr(pos), dptr(rot), dptr(box)))
         return pos, rot, box
 
