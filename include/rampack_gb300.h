@@ -212,6 +212,16 @@ int rp_try_scaling(void *handle, const double *new_box9, double *dE);
  * Replaces: Packing::revertScaling (core/Packing.cpp:363-371). */
 int rp_revert_scaling(void *handle);
 
+/* Overlap counting.  Replaces: Packing::toggleOverlapCounting / getCachedNumberOfOverlaps
+ * (core/Packing.cpp:1049-1060).  With counting on, a move's energy is the sign of the change
+ * of the mover's overlap count (core/Packing.cpp:304-323): outcome code 3 (dE = -inf, always
+ * accepted) when it falls, 1 (+inf) when it grows, 0 when it stays; an accepted move adds its
+ * change to the cached total; a box move recounts everything (dE = -inf / 0 / +inf by the
+ * change of the total) and rp_revert_scaling restores the count.  Turning counting on counts
+ * all overlaps first.  Spheres and spherocylinders. */
+int rp_set_counting(void *handle, int on);
+int rp_cached_overlaps(void *handle, int64_t *count);
+
 /* Orientation renormalisation.  Replaces: Packing::renormalizeOrientations(interaction,
  * allowOverlaps) (core/Packing.cpp:1178-1212) as Simulation::fixRotationMatrices calls it
  * (core/Simulation.cpp:750-760).  Without allow_overlaps every particle, in index order,

@@ -93,6 +93,8 @@ SIGNATURES = {
     "rp_set_ordering": (C.c_int, [_P, C.c_int32, C.c_int32]),
     "rp_renormalize_orientations": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int64)]),
     "rp_nematic_order": (C.c_int, [_P, _D, _D]),
+    "rp_set_counting": (C.c_int, [_P, C.c_int]),
+    "rp_cached_overlaps": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "rp_batch_create": (C.c_int, [C.POINTER(ShapeDesc), C.c_int32, C.POINTER(C.c_int64), C.c_int,
                                   C.POINTER(C.c_void_p)]),
     "rp_batch_destroy": (C.c_int, [_P]),

@@ -144,6 +144,10 @@ struct Handle {
     // batched replicas: the batch owns the rotation table, counters, status word and the
     // device copy of the ActiveDomain bounds (setup_grid leaves the bounds in bounds_host)
     bool batch_member = false;
+    // overlap counting (Packing::toggleOverlapCounting): the cached count lives on the device
+    bool counting = false;
+    unsigned long long *d_overlaps = nullptr;
+    unsigned long long saved_overlaps = 0;  // count before the last box move (revertScaling)
     double cell_factor = 1.0;       // checkerboard cells at least cell_factor x the range
     // learned ordering: network parameters (FP32 master + BF16 copy), Adam moments, scratch
     float *mlp_w32 = nullptr, *mlp_grad = nullptr, *mlp_m = nullptr, *mlp_v = nullptr, *mlp_loss = nullptr;
@@ -307,6 +311,8 @@ DevState dev_state(Handle *h) {
     s.abs64 = h->abs64[h->pcur];
     s.cthr64 = h->cthr64;
     s.pbc_fold = h->grid[h->gcur].no_ng ? 1 : 0;
+    s.counting = h->counting ? 1 : 0;
+    s.overlaps = h->d_overlaps;
     // ---- FP32 filter margins for the current grid ----
     const GridHost &g = h->grid[h->gcur];
     double lrow = 0;
@@ -839,6 +845,8 @@ static int create_common(Handle *h, int64_t n, int device, void **handle) {
     if ((e = cudaMalloc(&h->count_out, sizeof(unsigned long long))) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc(&h->flag, sizeof(int))) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc(&h->overflow_count, sizeof(int32_t))) != cudaSuccess) return bail(e);
+    if ((e = cudaMalloc(&h->d_overlaps, sizeof(unsigned long long))) != cudaSuccess) return bail(e);
+    cudaMemset(h->d_overlaps, 0, sizeof(unsigned long long));
     cudaMemset(h->overflow_count, 0, sizeof(int32_t));
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return bail(e);
     *handle = h;
@@ -949,6 +957,7 @@ int rp_destroy(void *handle) {
     cudaFree(h->flag);
     cudaFree(h->overflow);
     cudaFree(h->overflow_count);
+    cudaFree(h->d_overlaps);
     cudaFree(h->d_moves);
     cudaFree(h->d_list);
     cudaFree(h->d_codes);
@@ -1420,6 +1429,21 @@ int rp_try_scaling(void *handle, const double *new_box9, double *dE) {
     }
     h->can_revert = true;
     h->log_valid = false;
+    if (h->counting) {
+        // counting mode: the full recount against the count before the move (core/Packing.cpp:189-196)
+        RP_CUDA(h, cudaMemcpyAsync(&h->saved_overlaps, h->d_overlaps, sizeof(unsigned long long),
+                                   cudaMemcpyDeviceToHost, h->stream));
+        int64_t cnt = 0;
+        rc = rp_count_overlaps(h, 0, &cnt);
+        if (rc) return rc;
+        unsigned long long c = static_cast<unsigned long long>(cnt);
+        RP_CUDA(h, cudaMemcpyAsync(h->d_overlaps, &c, sizeof(c), cudaMemcpyHostToDevice, h->stream));
+        RP_CUDA(h, cudaStreamSynchronize(h->stream));
+        const long long delta = cnt - static_cast<long long>(h->saved_overlaps);
+        *dE = delta < 0 ? -std::numeric_limits<double>::infinity()
+                        : (delta > 0 ? std::numeric_limits<double>::infinity() : 0.0);
+        return RP_OK;
+    }
     // A convex shape in a box that only grew cannot overlap (core/Packing.cpp:199-200);
     // polyspheres are not convex (PolysphereTraits.h:133).
     if (h->shape.kind != RP_SHAPE_POLYSPHERE && box_upscaled(h->saved_box, h->box)) {
@@ -1444,6 +1468,11 @@ int rp_revert_scaling(void *handle) {
     h->gcur = 1 - h->gcur;
     h->can_revert = false;
     h->log_valid = false;
+    if (h->counting) {
+        RP_CUDA(h, cudaMemcpyAsync(h->d_overlaps, &h->saved_overlaps, sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                                   h->stream));
+        RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    }
     return RP_OK;
 }
 
@@ -1571,6 +1600,41 @@ int rp_nematic_order(void *handle, double *q9, double *p2) {
         if (std::abs(best) < std::abs(ev[k])) best = ev[k];
     *p2 = best;
     if (q9) std::memcpy(q9, q, sizeof(q));
+    return RP_OK;
+}
+
+// ---- overlap counting ---------------------------------------------------------------------
+
+int rp_set_counting(void *handle, int on) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h) return RP_ERR_ARG;
+    if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
+    if (on && h->shape.kind == RP_SHAPE_POLYSPHERE)
+        return fail(h, RP_ERR_UNSUPPORTED, "overlap counting is built for spheres and spherocylinders");
+    RP_CUDA(h, cudaSetDevice(h->device));
+    h->counting = on != 0;
+    h->can_revert = false;
+    if (h->counting) {
+        // Packing::toggleOverlapCounting: the cached count starts from a full recount
+        int64_t cnt = 0;
+        int rc = rp_count_overlaps(h, 0, &cnt);
+        if (rc) return rc;
+        unsigned long long c = static_cast<unsigned long long>(cnt);
+        RP_CUDA(h, cudaMemcpyAsync(h->d_overlaps, &c, sizeof(c), cudaMemcpyHostToDevice, h->stream));
+        RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    }
+    return RP_OK;
+}
+
+int rp_cached_overlaps(void *handle, int64_t *count) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !count) return fail(h, RP_ERR_ARG, "null argument");
+    if (!h->counting) return fail(h, RP_ERR_STATE, "overlap counting is off");
+    RP_CUDA(h, cudaSetDevice(h->device));
+    unsigned long long c = 0;
+    RP_CUDA(h, cudaMemcpyAsync(&c, h->d_overlaps, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
+    RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    *count = static_cast<int64_t>(c);
     return RP_OK;
 }
 

@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(WPB * 32, 16 / WPB)
         cc[2] = local / (act[0] * act[1]);
         for (int d = 0; d < 3; d++) c[d] = G.dims[d] == 1 ? 0 : 2 * cc[d] + ((ph >> d) & 1);
         const int cell = c[0] + G.dims[0] * (c[1] + G.dims[1] * c[2]);
-        sweep_cell<KIND, false, false>(A, local, cell, cap, A.overflow, A.overflow_count, cpos, cax, qseg, qun, nacc,
+        sweep_cell<KIND, false, 0>(A, local, cell, cap, A.overflow, A.overflow_count, cpos, cax, qseg, qun, nacc,
                                        nullptr, nullptr, nullptr, ws);
         __syncwarp();
         flush_stats(A, ws);
@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(32) k_b_overflow(const BatchRep *T, int k, int
     uint8_t *nacc = reinterpret_cast<uint8_t *>(qun + cap);
     WarpStats ws = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int q = 0; q < count; q++) {
-        sweep_cell<KIND, false, false>(A, q, A.overflow[q], cap, nullptr, nullptr, cpos, cax, qseg, qun, nacc,
+        sweep_cell<KIND, false, 0>(A, q, A.overflow[q], cap, nullptr, nullptr, cpos, cax, qseg, qun, nacc,
                                        nullptr, nullptr, nullptr, ws);
         __syncwarp();
     }

@@ -88,6 +88,10 @@ struct DevState {
     // it then measures sphere and polysphere-centre distances with the periodic boundary
     // conditions' own formula (pbc_distance2) instead of a cell translation
     int pbc_fold;
+    // overlap counting (Packing::toggleOverlapCounting): the cached total count, which
+    // accepted moves update by their overlap delta
+    int counting;
+    unsigned long long *overlaps;
 };
 
 constexpr int MAX_CEN = RP_MAX_CENTRES;

@@ -175,9 +175,9 @@ __global__ void k_count_poly(DevState s, GridDev g, int early, unsigned long lon
     if (slot < s.n) count_poly_one(s, g, slot, early, out, flag);
 }
 
-// LEARN instantiates the learned-ordering pre-test and the pair-outcome log (kept out of
-// the plain kernel, whose registers they would crowd)
-template <int KIND, bool LIST, bool LEARN>
+// MODE 1 instantiates the learned-ordering pre-test and the pair-outcome log, MODE 2 the
+// overlap counting (kept out of the plain kernel, whose registers they would crowd)
+template <int KIND, bool LIST, int MODE>
 __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(const SweepArgs A) {
     extern __shared__ float4 smem[];
     const unsigned FULL = 0xffffffffu;
@@ -190,6 +190,7 @@ __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(co
     // per slot [5 cap bytes], partner slots [LEARN], polysphere scratch [SWEEP_POLY_SCRATCH]
     const int K = KIND == 2 ? A.s.ncen : 0;
     const int extra = KIND == 1 ? A.cap : (KIND == 2 ? A.cap * 3 * K / 4 : 0);
+    constexpr bool LEARN = MODE == 1;
     const int per_warp = A.cap + extra + A.cap / 4 + A.cap / 16 + (LEARN ? A.cap / 4 : 0) +
                          (KIND == 2 ? SWEEP_POLY_SCRATCH : 0);
     float4 *cpos = smem + (size_t)wib * per_warp;
@@ -213,7 +214,7 @@ __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(co
             item = __shfl_sync(FULL, it, 0);
         }
         if (item >= nitems) break;
-        sweep_cell<KIND, LIST, LEARN>(A, item, -1, A.cap, A.overflow, A.overflow_count, cpos, cax, qseg, qun, nacc,
+        sweep_cell<KIND, LIST, MODE>(A, item, -1, A.cap, A.overflow, A.overflow_count, cpos, cax, qseg, qun, nacc,
                                       pstage, ccen, wx, ws);
         __syncwarp();
         item += stride;
@@ -291,34 +292,39 @@ cudaError_t launch_rot_table(double *out64, float *out32, uint32_t count, uint64
     return cudaGetLastError();
 }
 
-template <int KIND, bool LIST, bool LEARN>
+template <int KIND, bool LIST, int MODE>
 static cudaError_t launch_sweep_t(const SweepArgs &a, unsigned blocks, int threads, size_t smem, cudaStream_t st) {
-    cudaError_t e = cudaFuncSetAttribute(k_sweep<KIND, LIST, LEARN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(k_sweep<KIND, LIST, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    k_sweep<KIND, LIST, LEARN><<<blocks, threads, smem, st>>>(a);
+    k_sweep<KIND, LIST, MODE><<<blocks, threads, smem, st>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t launch_sweep(const SweepArgs &a, bool list, int nwarps, cudaStream_t st) {
     if (nwarps <= 0) return cudaSuccess;
     const int wpb = a.work ? 1 : SWEEP_WARPS;
-    const bool learn = !list && a.s.kind != 2 && (a.partners != nullptr || a.pair_every > 0);
+    const bool count = a.s.counting != 0 && a.s.kind != 2;
+    const bool learn = !list && !count && a.s.kind != 2 && (a.partners != nullptr || a.pair_every > 0);
     size_t smem = sweep_smem_per_warp(a.s.kind, a.cap, learn, a.s.ncen) * wpb;
     unsigned blocks = (unsigned)((nwarps + wpb - 1) / wpb);
     const int th = wpb * 32;
-    if (a.s.kind == 0) {
-        if (list) return launch_sweep_t<0, true, false>(a, blocks, th, smem, st);
-        return learn ? launch_sweep_t<0, false, true>(a, blocks, th, smem, st)
-                     : launch_sweep_t<0, false, false>(a, blocks, th, smem, st);
-    }
     if (a.s.kind == 2) {
-        if (list) return launch_sweep_t<2, true, false>(a, blocks, th, smem, st);
-        return launch_sweep_t<2, false, false>(a, blocks, th, smem, st);
+        if (list) return launch_sweep_t<2, true, 0>(a, blocks, th, smem, st);
+        return launch_sweep_t<2, false, 0>(a, blocks, th, smem, st);
     }
-    if (list) return launch_sweep_t<1, true, false>(a, blocks, th, smem, st);
-    return learn ? launch_sweep_t<1, false, true>(a, blocks, th, smem, st)
-                 : launch_sweep_t<1, false, false>(a, blocks, th, smem, st);
+    if (a.s.kind == 0) {
+        if (count) return list ? launch_sweep_t<0, true, 2>(a, blocks, th, smem, st)
+                               : launch_sweep_t<0, false, 2>(a, blocks, th, smem, st);
+        if (list) return launch_sweep_t<0, true, 0>(a, blocks, th, smem, st);
+        return learn ? launch_sweep_t<0, false, 1>(a, blocks, th, smem, st)
+                     : launch_sweep_t<0, false, 0>(a, blocks, th, smem, st);
+    }
+    if (count) return list ? launch_sweep_t<1, true, 2>(a, blocks, th, smem, st)
+                           : launch_sweep_t<1, false, 2>(a, blocks, th, smem, st);
+    if (list) return launch_sweep_t<1, true, 0>(a, blocks, th, smem, st);
+    return learn ? launch_sweep_t<1, false, 1>(a, blocks, th, smem, st)
+                 : launch_sweep_t<1, false, 0>(a, blocks, th, smem, st);
 }
 
 }  // namespace rp

@@ -171,11 +171,16 @@ struct WarpStats {
     unsigned moves, accepted, rej_overlap, rej_domain, pairs, fp64, trans, rots;
 };
 
-template <int KIND, bool LIST, bool LEARN>
+// MODE 0: plain sweep; 1: learned-ordering pre-test and pair log; 2: overlap counting
+// (Packing::toggleOverlapCounting, core/Packing.cpp:304-323: the move's energy is the sign of
+// the change of the mover's overlap count).
+template <int KIND, bool LIST, int MODE>
 __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, const int cell_direct, const int cap,
                                            int32_t *ovf, int32_t *ovf_count, float4 *cpos, float4 *cax,
                                            uint16_t *qseg, uint16_t *qun, uint8_t *nacc, uint16_t *pstage,
                                            float *ccen, float4 *wx, WarpStats &ws) {
+    constexpr bool LEARN = MODE == 1;
+    constexpr bool COUNT = MODE == 2;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -448,7 +453,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
 
         // ---- FP32 pass 1: centre distances, two candidates per lane per round ----
         int nseg = 0, nun = 0;
-        if (dom != 1 && !overlap) {
+        if (!COUNT && dom != 1 && !overlap) {
             for (int base = 0; base < total; base += 64) {
                 int k0 = base + lane, k1 = base + 32 + lane;
                 int c0 = 0, c1 = 0;
@@ -487,7 +492,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
         }
         __syncwarp();
         // ---- FP32 pass 2 (polyspheres): every centre pair of a near body, one body per lane ----
-        if (KIND == 2 && !overlap) {
+        if (!COUNT && KIND == 2 && !overlap) {
             const int K = S.ncen;
             for (int base = 0; base < nseg; base += 32) {
                 const int i = base + lane;
@@ -522,7 +527,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
             __syncwarp();
         }
         // ---- FP32 pass 2 (spherocylinders): segment distances on full warps ----
-        if (KIND == 1 && !overlap) {
+        if (!COUNT && KIND == 1 && !overlap) {
             for (int base = 0; base < nseg; base += 32) {
                 int i = base + lane;
                 int cls = 0, k = 0;
@@ -741,10 +746,46 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
             }
         }
 
-        // ---- Metropolis (core/Simulation.cpp:483): u <= exp(-dE/T), dE in {0, +inf} ----
-        const bool acc = (code == 0) ? (uni <= 1.0) : (uni <= 0.0);
+        // ---- overlap counting: the mover's overlaps before and after the move, every
+        //      candidate classified (no early exit), undecided pairs in FP64 ----
+        int cdelta = 0;
+        if (COUNT && code == 0) {
+            const d3 pc64{__shfl_sync(FULL, pos_own, 0), __shfl_sync(FULL, pos_own, 1), __shfl_sync(FULL, pos_own, 2)};
+            const d3 ac64{__shfl_sync(FULL, rot_own, 2), __shfl_sync(FULL, rot_own, 5), __shfl_sync(FULL, rot_own, 8)};
+            int before = 0, after = 0;
+            for (int k = lane; k < total; k += 32) {
+                const float4 q = cpos[k];
+                const int pj = __float_as_int(q.w);
+                if (pj == pid) continue;
+                float3 aj = make_float3(0.f, 0.f, 1.f);
+                if (KIND == 1) {
+                    const float4 a = cax[k];
+                    aj = make_float3(a.x, a.y, a.z);
+                }
+                const float3 db = make_float3(q.x - pcur.x, q.y - pcur.y, q.z - pcur.z);
+                int cb = A.fp64_only ? 2 : classify<KIND>(S.fc, db, ai, aj);
+                if (cb == 2) cb = exact_pair(S, pc64, ac64, pj, db) ? 1 : 0;
+                const float3 da = make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z);
+                int ca = A.fp64_only ? 2 : classify<KIND>(S.fc, da, an, aj);
+                if (ca == 2) ca = exact_pair(S, pnew, anew, pj, da) ? 1 : 0;
+                before += cb == 1 ? 1 : 0;
+                after += ca == 1 ? 1 : 0;
+            }
+            for (int d = 16; d > 0; d >>= 1) {
+                before += __shfl_xor_sync(FULL, before, d);
+                after += __shfl_xor_sync(FULL, after, d);
+            }
+            if (lane == 0) ws.pairs += (unsigned)(2 * (total - 1));
+            cdelta = after - before;
+            code = cdelta < 0 ? 3 : (cdelta > 0 ? 1 : 0);
+        }
+
+        // ---- Metropolis (core/Simulation.cpp:483): u <= exp(-dE/T), dE in {-inf, 0, +inf} ----
+        const bool acc = code == 3 ? true : ((code == 0) ? (uni <= 1.0) : (uni <= 0.0));
         if (acc) {
             const size_t gslot = (size_t)gbase + slot;
+            // Packing::acceptMove adds the move's overlap delta in counting mode (core/Packing.cpp:298-300)
+            if (COUNT && lane == 0) atomicAdd(S.overlaps, (unsigned long long)(long long)cdelta);
             float4 np = pcur;
             float4 na = KIND == 1 ? cax[slot] : make_float4(0.f, 0.f, 0.f, 0.f);
             __syncwarp();

@@ -229,6 +229,17 @@ class GpuPacking:
     def set_ordering(self, mode: int, every: int = 1):
         self._check(self.lib.rp_set_ordering(self.h, mode, every))
 
+    # ---- overlap counting ----
+    def set_counting(self, on: bool = True):
+        """Packing::toggleOverlapCounting."""
+        self._check(self.lib.rp_set_counting(self.h, 1 if on else 0))
+
+    def cached_overlaps(self) -> int:
+        """Packing::getCachedNumberOfOverlaps."""
+        c = C.c_int64()
+        self._check(self.lib.rp_cached_overlaps(self.h, C.byref(c)))
+        return int(c.value)
+
     # ---- observables ----
     def nematic_order(self):
         """(Q tensor 3x3, P2) of the current state (NematicOrder::calculate)."""
