@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--seed", type=int, default=1234)
+    ap.add_argument("--tuning", default=None,
+                    help="replicas-64: fixed launch shape 'cell_factor,warps_per_block' instead of autotuning")
     ap.add_argument("--ordering", action="store_true",
                     help="compare the plain scan with centre-distance and learned partner ordering")
     return ap.parse_args()
@@ -589,15 +591,18 @@ def main_replicas(args):
 
     # autotune the launch shape: cell factor x warps per block
     tune = []
-    for cf in (1.0, 1.1, 1.25):
-        for wpb in (2, 4, 8):
-            for b in batches.values():
-                b.set_tuning(cf, wpb)
+    grid = [(cf, wpb) for cf in (1.0, 1.1, 1.25) for wpb in (2, 4, 8)]
+    if args.tuning:
+        cf, wpb = args.tuning.split(",")
+        grid = [(float(cf), int(wpb))]
+    for cf, wpb in grid:
+        for b in batches.values():
+            b.set_tuning(cf, wpb)
+        one_cycle()
+        t = time.perf_counter()
+        for _ in range(3):
             one_cycle()
-            t = time.perf_counter()
-            for _ in range(3):
-                one_cycle()
-            tune.append({"cell_factor": cf, "warps_per_block": wpb, "ms_per_cycle": (time.perf_counter() - t) / 3 * 1e3})
+        tune.append({"cell_factor": cf, "warps_per_block": wpb, "ms_per_cycle": (time.perf_counter() - t) / 3 * 1e3})
     best = min(tune, key=lambda x: x["ms_per_cycle"])
     for b in batches.values():
         b.set_tuning(best["cell_factor"], best["warps_per_block"])

@@ -10,6 +10,10 @@
 
 namespace rp {
 
+// SweepArgs in float4 units (each warp keeps a shared-memory copy of its replica's arguments)
+constexpr int ARGS_F4 = (int)((sizeof(SweepArgs) + sizeof(float4) - 1) / sizeof(float4));
+size_t batch_smem_per_warp(int kind, int cap);
+
 namespace {
 
 // Largest r with base[r] <= x (base ascending, base[0] = 0, base[R] = total).
@@ -156,8 +160,9 @@ __global__ void __launch_bounds__(WPB * 32, 16 / WPB)
     extern __shared__ float4 smem[];
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int per_warp = cap * (KIND == 1 ? 2 : 1) + cap / 4 + cap / 16;
-    float4 *cpos = smem + (size_t)wib * per_warp;
+    const int per_warp = ARGS_F4 + cap * (KIND == 1 ? 2 : 1) + cap / 4 + cap / 16;
+    SweepArgs *Aw = reinterpret_cast<SweepArgs *>(smem + (size_t)wib * per_warp);
+    float4 *cpos = smem + (size_t)wib * per_warp + ARGS_F4;
     float4 *cax = cpos + cap;
     uint16_t *qseg = reinterpret_cast<uint16_t *>(cpos + cap * (KIND == 1 ? 2 : 1));
     uint16_t *qun = qseg + cap;
@@ -172,7 +177,14 @@ __global__ void __launch_bounds__(WPB * 32, 16 / WPB)
         const int r = find_rep(item_base, R, item);
         const BatchRep &B = T[r];
         if (k >= B.nphases) continue;
-        const SweepArgs &A = B.a;
+        // the replica's arguments, copied into this warp's shared memory (read all through the cell)
+        {
+            const float4 *src = reinterpret_cast<const float4 *>(&B.a);
+            float4 *dst = reinterpret_cast<float4 *>(Aw);
+            for (int q = lane; q < ARGS_F4; q += 32) dst[q] = src[q];
+            __syncwarp();
+        }
+        const SweepArgs &A = *Aw;
         const GridDev &G = A.g;
         const int local = item - item_base[r];
         const int ph = B.phases[k];
@@ -187,6 +199,7 @@ __global__ void __launch_bounds__(WPB * 32, 16 / WPB)
                                        nullptr, nullptr, nullptr, ws);
         __syncwarp();
         flush_stats(A, ws);
+        __syncwarp();
     }
 }
 
@@ -217,7 +230,7 @@ __global__ void __launch_bounds__(32) k_b_overflow(const BatchRep *T, int k, int
 template <int KIND, int WPB>
 cudaError_t launch_b_sweep_t(const BatchRep *T, const int *item_base, int R, int k, int *next_item, int cap,
                              int blocks, cudaStream_t st) {
-    const size_t smem = (size_t)WPB * (cap * (KIND == 1 ? 2 : 1) + cap / 4 + cap / 16) * sizeof(float4);
+    const size_t smem = (size_t)WPB * batch_smem_per_warp(KIND, cap);
     cudaError_t e = cudaFuncSetAttribute(k_b_sweep<KIND, WPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k_b_sweep<KIND, WPB><<<blocks, WPB * 32, smem, st>>>(T, item_base, R, k, next_item, cap);
@@ -254,7 +267,7 @@ cudaError_t launch_b_count(const BatchRep *T, const int *pbase, int R, int total
 }
 
 size_t batch_smem_per_warp(int kind, int cap) {
-    return (size_t)(cap * (kind == 1 ? 2 : 1) + cap / 4 + cap / 16) * sizeof(float4);
+    return (size_t)(ARGS_F4 + cap * (kind == 1 ? 2 : 1) + cap / 4 + cap / 16) * sizeof(float4);
 }
 
 cudaError_t launch_b_sweep(const BatchRep *T, const int *item_base, int R, int kind, int k, int *next_item, int cap,
