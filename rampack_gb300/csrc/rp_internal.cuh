@@ -151,7 +151,7 @@ struct SweepArgs {
 // order, and its box move when the batch rescales it.  Particles, cells and sweep items of
 // all replicas are numbered consecutively; the prefix offsets live in separate compact
 // arrays that the kernels search.
-struct BatchRep {
+struct alignas(16) BatchRep {
     SweepArgs a;
     int phases[8];
     int nphases;
@@ -161,5 +161,9 @@ struct BatchRep {
     double *scale_dst;
     double *trans_dst;             // translation table of the new box
 };
+// table entries are copied into shared memory as float4 words: every entry, and the
+// arguments at its start, must sit on a 16-byte boundary
+static_assert(sizeof(BatchRep) % 16 == 0, "BatchRep size");
+static_assert(alignof(BatchRep) == 16, "BatchRep alignment");
 
 }  // namespace rp
