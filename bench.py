@@ -559,11 +559,11 @@ def main_replicas(args):
     groups = {k: [i for i in range(64) if reps[i][0] == k] for k in (0, 1)}
     batches = {k: BatchPacking(k, reps[idx[0]][1], [reps[i][2:5] for i in idx]) for k, idx in groups.items()}
     steps = {0: (TRANS_STEP, 0.0), 1: (TRANS_STEP, ROT_STEP)}
-    boxes = {k: [np.array(reps[i][4], dtype=np.float64) for i in idx] for k, idx in groups.items()}
-    sizes = {k: [len(reps[i][2]) for i in idx] for k, idx in groups.items()}
-    press = {k: [reps[i][5] for i in idx] for k, idx in groups.items()}
+    boxes = {k: np.array([reps[i][4] for i in idx], dtype=np.float64) for k, idx in groups.items()}
+    sizes = {k: np.array([len(reps[i][2]) for i in idx], dtype=np.float64) for k, idx in groups.items()}
+    press = {k: np.array([reps[i][5] for i in idx]) for k, idx in groups.items()}
     rng = np.random.default_rng(args.seed)
-    moves_per_cycle = sum(sizes[0]) + 2 * sum(sizes[1])
+    moves_per_cycle = int(sizes[0].sum() + 2 * sizes[1].sum())
     state = {"k": 0, "box_acc": 0}
 
     def one_cycle():
@@ -571,22 +571,19 @@ def main_replicas(args):
         for kind, b in batches.items():
             b.sweep(*steps[kind], seed=args.seed + kind, counter=k, stats=False)
         for kind, b in batches.items():
-            R = b.R
-            new, prop = [], np.zeros(R, dtype=np.uint8)
-            for j in range(R):
-                box = boxes[kind][j]
-                nb = propose_box(box, rng)
-                v0, v1 = box_volume(box), box_volume(nb)
-                expo = sizes[kind][j] * math.log(v1 / v0) - press[kind][j] * (v1 - v0) / TEMPERATURE
-                prop[j] = rng.uniform() <= math.exp(min(expo, 700.0))
-                new.append(nb if prop[j] else box)
-            dE = b.try_scaling(np.array(new), prop)
+            # every replica's isotension proposal and Metropolis pre-check, vectorised
+            old = boxes[kind]
+            new = old + rng.uniform(-BOX_STEP, BOX_STEP, size=old.shape)
+            v0 = np.abs(np.linalg.det(old.reshape(-1, 3, 3)))
+            v1 = np.abs(np.linalg.det(new.reshape(-1, 3, 3)))
+            expo = sizes[kind] * np.log(v1 / v0) - press[kind] * (v1 - v0) / TEMPERATURE
+            prop = (rng.uniform(size=b.R) <= np.exp(np.minimum(expo, 700.0))).astype(np.uint8)
+            dE = b.try_scaling(np.where(prop[:, None] == 1, new, old), prop)
             bad = (prop == 1) & (dE > 0)
             b.revert_scaling(bad.astype(np.uint8))
-            for j in range(R):
-                if prop[j] and not bad[j]:
-                    boxes[kind][j] = new[j]
-                    state["box_acc"] += 1
+            keep = (prop == 1) & ~bad
+            boxes[kind][keep] = new[keep]
+            state["box_acc"] += int(keep.sum())
         state["k"] += 1
 
     # autotune the launch shape: cell factor x warps per block
