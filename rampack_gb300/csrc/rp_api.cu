@@ -419,8 +419,10 @@ int setup_grid(Handle *h, GridHost &G, const double *box, const double *shift) {
         double nd = std::floor(hgt[d] / cell_min);
         if (nd > 1 << 20) return fail(h, RP_ERR_UNSUPPORTED, "too many cells");
         int n = static_cast<int>(nd);
-        if (n >= 2) n &= ~1;
-        else n = 1;
+        // an odd count up to 9 keeps its cell size (three colours along this dimension);
+        // larger odd counts drop one cell (two colours, cells at most 1/9 larger)
+        if (n < 1) n = 1;
+        if (n > 9 && (n & 1)) n -= 1;
         dims[d] = n;
     }
     // The reference keeps no neighbour grid for small boxes (core/Packing.cpp:862-881) and
@@ -563,9 +565,25 @@ int check_status(Handle *h) {
     return RP_OK;
 }
 
-void phase_bits(const GridDev &g, int cell, int &ph) {
-    int cx = cell % g.dims[0], cy = (cell / g.dims[0]) % g.dims[1], cz = cell / (g.dims[0] * g.dims[1]);
-    ph = (g.dims[0] > 1 ? (cx & 1) : 0) | ((g.dims[1] > 1 ? (cy & 1) : 0) << 1) | ((g.dims[2] > 1 ? (cz & 1) : 0) << 2);
+void phase_bits(const GridDev &g, int cell, int &ph) { ph = cell_phase(g.dims, cell); }
+
+// Every phase of a grid (one colour per dimension), in a shuffled order.
+void grid_phases(const GridDev &g, uint32_t x, std::vector<int> &phases) {
+    phases.clear();
+    for (int p2 = 0; p2 < ring_ncol(g.dims[2]); p2++)
+        for (int p1 = 0; p1 < ring_ncol(g.dims[1]); p1++)
+            for (int p0 = 0; p0 < ring_ncol(g.dims[0]); p0++) phases.push_back(p0 + 3 * p1 + 9 * p2);
+    for (int k = static_cast<int>(phases.size()) - 1; k > 0; k--) {
+        x = x * 1664525u + 1013904223u;
+        int j = static_cast<int>((static_cast<uint64_t>(x) * (k + 1)) >> 32);
+        std::swap(phases[k], phases[j]);
+    }
+}
+
+// Cells of one phase.
+int phase_cells(const GridDev &g, int ph, int act[3]) {
+    for (int d = 0; d < 3; d++) act[d] = ring_count(g.dims[d], phase_digit(ph, d));
+    return act[0] * act[1] * act[2];
 }
 
 SweepArgs base_args(Handle *h) {
@@ -668,7 +686,7 @@ struct Batch {
     cudaStream_t stream = nullptr;
     std::vector<Handle *> rep;
     BatchRep *d_table = nullptr;                      // [R]
-    int *d_bases = nullptr;                           // item_base, pbase, cbase: 3 x (R + 1)
+    int *d_bases = nullptr;                           // pbase, cbase, item_base of each phase: (2 + MAX_PHASES) x (R + 1)
     double *d_bounds = nullptr;                       // packed ActiveDomain bounds
     int64_t d_bounds_alloc = 0;
     // two pinned staging sets used alternately; a set is rewritten only after its copies ran
@@ -683,7 +701,7 @@ struct Batch {
     int cur = 0;
     double *rtab64 = nullptr;
     float *rtab32 = nullptr;
-    int32_t *item_counters = nullptr;                 // [8]
+    int32_t *item_counters = nullptr;                 // [MAX_PHASES]
     unsigned long long *stats = nullptr;              // [R][8]
     uint32_t *status = nullptr;                       // [R]
     unsigned long long *counts = nullptr, *h_counts = nullptr;  // [R]
@@ -716,20 +734,7 @@ void sweep_origin(uint64_t seed, uint64_t counter, double shift[3], uint32_t &sh
     shuffle = r.d;
 }
 
-void phase_order(const GridDev &g, uint32_t x, std::vector<int> &phases) {
-    phases.clear();
-    for (int ph = 0; ph < 8; ph++) {
-        bool ok = true;
-        for (int d = 0; d < 3; d++)
-            if (g.dims[d] == 1 && ((ph >> d) & 1)) ok = false;
-        if (ok) phases.push_back(ph);
-    }
-    for (int k = static_cast<int>(phases.size()) - 1; k > 0; k--) {
-        x = x * 1664525u + 1013904223u;
-        int j = static_cast<int>((static_cast<uint64_t>(x) * (k + 1)) >> 32);
-        std::swap(phases[k], phases[j]);
-    }
-}
+void phase_order(const GridDev &g, uint32_t x, std::vector<int> &phases) { grid_phases(g, x, phases); }
 
 uint64_t replica_seed(uint64_t seed, int r) { return seed + RP_BATCH_SEED_STRIDE * static_cast<uint64_t>(r); }
 
@@ -757,8 +762,8 @@ int batch_tables(Batch *b, int &total_items, int &total_p, int &total_c) {
         b->d_bounds_alloc = nb * 2;
     }
     int64_t off = 0;
-    int *ib = S.bases, *pb = S.bases + (b->R + 1), *cb = S.bases + 2 * (b->R + 1);
-    ib[0] = pb[0] = cb[0] = 0;
+    int *pb = S.bases, *cb = S.bases + (b->R + 1);
+    pb[0] = cb[0] = 0;
     for (int r = 0; r < b->R; r++) {
         Handle *h = b->rep[r];
         GridHost &G = h->grid[h->gcur];
@@ -768,14 +773,10 @@ int batch_tables(Batch *b, int &total_items, int &total_p, int &total_c) {
         BatchRep &T = S.table[r];
         T = BatchRep{};
         T.a = base_args(h);
-        int act = 1;
-        for (int d = 0; d < 3; d++) act *= G.d.dims[d] == 1 ? 1 : G.d.dims[d] / 2;
-        T.a.num_active = act;
-        ib[r + 1] = ib[r] + act;
         pb[r + 1] = pb[r] + static_cast<int>(h->n);
         cb[r + 1] = cb[r] + G.d.ncell;
     }
-    total_items = ib[b->R];
+    total_items = 0;
     total_p = pb[b->R];
     total_c = cb[b->R];
     return RP_OK;
@@ -788,7 +789,8 @@ int batch_copy(Batch *b) {
     for (Handle *h : b->rep) nb += static_cast<int64_t>(h->grid[h->gcur].bounds_host.size());
     RB_CUDA(b, cudaMemcpyAsync(b->d_bounds, S.bounds, sizeof(double) * nb, cudaMemcpyHostToDevice, b->stream));
     RB_CUDA(b, cudaMemcpyAsync(b->d_table, S.table, sizeof(BatchRep) * b->R, cudaMemcpyHostToDevice, b->stream));
-    RB_CUDA(b, cudaMemcpyAsync(b->d_bases, S.bases, sizeof(int) * 3 * (b->R + 1), cudaMemcpyHostToDevice, b->stream));
+    RB_CUDA(b, cudaMemcpyAsync(b->d_bases, S.bases, sizeof(int) * (2 + MAX_PHASES) * (b->R + 1), cudaMemcpyHostToDevice,
+                               b->stream));
     RB_CUDA(b, cudaEventRecord(S.done, b->stream));
     S.pending = true;
     b->cur ^= 1;
@@ -1246,18 +1248,7 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
     heights_of(h->box, hgt);
     double tstep = std::min(p->translation_step, std::min({hgt[0], hgt[1], hgt[2]}) / 2);
     std::vector<int> phases;
-    for (int ph = 0; ph < 8; ph++) {
-        bool ok = true;
-        for (int d = 0; d < 3; d++)
-            if (g.dims[d] == 1 && ((ph >> d) & 1)) ok = false;
-        if (ok) phases.push_back(ph);
-    }
-    uint32_t x = r.d;
-    for (int k = static_cast<int>(phases.size()) - 1; k > 0; k--) {
-        x = x * 1664525u + 1013904223u;
-        int j = static_cast<int>((static_cast<uint64_t>(x) * (k + 1)) >> 32);
-        std::swap(phases[k], phases[j]);
-    }
+    grid_phases(g, r.d, phases);
     int ntypes = (types & 1) + ((types >> 1) & 1);
     bool log = (p->flags & RP_SWEEP_LOG) != 0;
     if (log) {
@@ -1295,12 +1286,11 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
         a.inv_range = static_cast<float>(1.0 / h->range);
         a.next_item = h->item_counters + phase_no++;
         int act[3];
+        a.num_active = phase_cells(g, ph, act);
         for (int d = 0; d < 3; d++) {
-            a.phase[d] = (ph >> d) & 1;
-            act[d] = g.dims[d] == 1 ? 1 : g.dims[d] / 2;
+            a.phase[d] = phase_digit(ph, d);
             a.active[d] = act[d];
         }
-        a.num_active = act[0] * act[1] * act[2];
         a.seed = p->seed;
         a.counter = p->counter;
         a.tstep = static_cast<float>(tstep);
@@ -1372,8 +1362,7 @@ int rp_sweep_log(void *handle, rp_move *moves, uint8_t *codes, int64_t capacity,
         for (int64_t cell = 0; cell < ncell; cell++) {
             int cx = static_cast<int>(cell % dims[0]), cy = static_cast<int>((cell / dims[0]) % dims[1]),
                 cz = static_cast<int>(cell / (static_cast<int64_t>(dims[0]) * dims[1]));
-            int cp = (dims[0] > 1 ? (cx & 1) : 0) | ((dims[1] > 1 ? (cy & 1) : 0) << 1) |
-                     ((dims[2] > 1 ? (cz & 1) : 0) << 2);
+            int cp = ring_colour(dims[0], cx) + 3 * ring_colour(dims[1], cy) + 9 * ring_colour(dims[2], cz);
             if (cp != ph) continue;
             int64_t b = static_cast<int64_t>(h->log_types) * h->log_start[cell];
             int64_t e = static_cast<int64_t>(h->log_types) * h->log_start[cell + 1];
@@ -1930,10 +1919,10 @@ int rp_batch_create(const rp_shape_desc *shape, int32_t replicas, const int64_t 
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(RP_ERR_CUDA);
     const int R = replicas;
     bool ok = cudaMalloc(&b->d_table, sizeof(BatchRep) * R) == cudaSuccess &&
-              cudaMalloc(&b->d_bases, sizeof(int) * 3 * (R + 1)) == cudaSuccess &&
+              cudaMalloc(&b->d_bases, sizeof(int) * (2 + MAX_PHASES) * (R + 1)) == cudaSuccess &&
               cudaMalloc(&b->rtab64, sizeof(double) * 9 * ROT_TABLE) == cudaSuccess &&
               cudaMalloc(&b->rtab32, sizeof(float) * 12 * ROT_TABLE) == cudaSuccess &&
-              cudaMalloc(&b->item_counters, sizeof(int32_t) * 8) == cudaSuccess &&
+              cudaMalloc(&b->item_counters, sizeof(int32_t) * MAX_PHASES) == cudaSuccess &&
               cudaMalloc(&b->stats, sizeof(unsigned long long) * 8 * R) == cudaSuccess &&
               cudaMalloc(&b->status, sizeof(uint32_t) * R) == cudaSuccess &&
               cudaMalloc(&b->counts, sizeof(unsigned long long) * R) == cudaSuccess &&
@@ -1942,7 +1931,7 @@ int rp_batch_create(const rp_shape_desc *shape, int32_t replicas, const int64_t 
               cudaMallocHost(&b->h_flags, sizeof(int) * R) == cudaSuccess;
     for (auto &S : b->stage)
         ok = ok && cudaMallocHost(&S.table, sizeof(BatchRep) * R) == cudaSuccess &&
-             cudaMallocHost(&S.bases, sizeof(int) * 3 * (R + 1)) == cudaSuccess &&
+             cudaMallocHost(&S.bases, sizeof(int) * (2 + MAX_PHASES) * (R + 1)) == cudaSuccess &&
              cudaEventCreateWithFlags(&S.done, cudaEventDisableTiming) == cudaSuccess;
     if (!ok) return bail(RP_ERR_CUDA);
     cudaMemset(b->stats, 0, sizeof(unsigned long long) * 8 * R);
@@ -2128,11 +2117,26 @@ int rp_batch_sweep(void *batch, const rp_sweep_params *p, rp_sweep_stats *stats)
             a.log_codes = h->d_log_codes;
         }
         T[r].nphases = static_cast<int>(phases[r].size());
-        for (int k = 0; k < 8; k++) T[r].phases[k] = k < T[r].nphases ? phases[r][k] : 0;
+        for (int k = 0; k < MAX_PHASES; k++) T[r].phases[k] = k < T[r].nphases ? phases[r][k] : 0;
+    }
+    // the cells of phase k of every replica, numbered consecutively
+    std::vector<int> phase_total(maxph, 0);
+    {
+        int *bases = b->stage[b->cur].bases;
+        for (int k = 0; k < maxph; k++) {
+            int *ibk = bases + (2 + k) * (b->R + 1);
+            ibk[0] = 0;
+            for (int r = 0; r < b->R; r++) {
+                int act[3];
+                const int items = k < T[r].nphases ? phase_cells(b->rep[r]->grid[b->rep[r]->gcur].d, T[r].phases[k], act) : 0;
+                ibk[r + 1] = ibk[r] + items;
+            }
+            phase_total[k] = ibk[b->R];
+        }
     }
     rc = batch_copy(b);
     if (rc) return rc;
-    const int *ib = b->d_bases, *pb = b->d_bases + (b->R + 1), *cb = b->d_bases + 2 * (b->R + 1);
+    const int *pb = b->d_bases, *cb = b->d_bases + (b->R + 1);
     if (stats) RB_CUDA(b, cudaMemsetAsync(b->stats, 0, sizeof(unsigned long long) * 8 * b->R, b->stream));
     RB_CUDA(b, launch_b_rebuild(b->d_table, pb, cb, b->R, total_p, total_c, b->stream));
     b->launches += 5;
@@ -2141,14 +2145,15 @@ int rp_batch_sweep(void *batch, const rp_sweep_params *p, rp_sweep_stats *stats)
                                     static_cast<float>(p->rotation_step), b->stream));
         b->launches += 1;
     }
-    RB_CUDA(b, cudaMemsetAsync(b->item_counters, 0, sizeof(int32_t) * 8, b->stream));
+    RB_CUDA(b, cudaMemsetAsync(b->item_counters, 0, sizeof(int32_t) * MAX_PHASES, b->stream));
     // fewer warps per block when the staging of `cap` candidates per warp would not fit
     int wpb = b->wpb;
     while (wpb > 2 && static_cast<size_t>(wpb) * batch_smem_per_warp(b->kind, cap) > static_cast<size_t>(b->smem_optin))
         wpb /= 2;
     const int ovf_cap = static_cast<int>(OVF_SMEM / (batch_smem_per_warp(b->kind, 32) / 32)) / 32 * 32;
     for (int k = 0; k < maxph; k++) {
-        int blocks = std::max(1, std::min((total_items + wpb - 1) / wpb, b->num_sms * (16 / wpb)));
+        const int *ib = b->d_bases + (2 + k) * (b->R + 1);
+        int blocks = std::max(1, std::min((phase_total[k] + wpb - 1) / wpb, b->num_sms * (16 / wpb)));
         RB_CUDA(b, launch_b_sweep(b->d_table, ib, b->R, b->kind, k, b->item_counters + k, cap, wpb, blocks, b->stream));
         RB_CUDA(b, launch_b_overflow(b->d_table, b->R, b->kind, k, ovf_cap, b->stream));
         b->launches += 2;
@@ -2270,7 +2275,7 @@ int rp_batch_try_scaling(void *batch, const double *boxes, const uint8_t *propos
     }
     rc = batch_copy(b);
     if (rc) return rc;
-    const int *pb = b->d_bases + (b->R + 1), *cb = b->d_bases + 2 * (b->R + 1);
+    const int *pb = b->d_bases, *cb = b->d_bases + (b->R + 1);
     RB_CUDA(b, cudaMemcpyAsync(b->flags, b->h_flags, sizeof(int) * b->R, cudaMemcpyHostToDevice, b->stream));
     RB_CUDA(b, cudaMemsetAsync(b->counts, 0, sizeof(unsigned long long) * b->R, b->stream));
     RB_CUDA(b, launch_b_rescale(b->d_table, pb, b->R, total_p, b->stream));

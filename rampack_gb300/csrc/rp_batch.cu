@@ -153,7 +153,8 @@ __device__ __forceinline__ void flush_stats(const SweepArgs &A, WarpStats &ws) {
 }
 
 // Phase k of every replica: persistent warps take checkerboard cells of the whole batch
-// from one counter.  Every replica's staging capacity is `cap`.
+// from one counter.  item_base holds the prefix offsets of this phase's cells per replica;
+// every replica's staging capacity is `cap`.
 template <int KIND, int WPB>
 __global__ void __launch_bounds__(WPB * 32, 16 / WPB)
     k_b_sweep(const BatchRep *T, const int *item_base, int R, int k, int *next_item, int cap) {
@@ -189,11 +190,11 @@ __global__ void __launch_bounds__(WPB * 32, 16 / WPB)
         const int local = item - item_base[r];
         const int ph = B.phases[k];
         int act[3], cc[3], c[3];
-        for (int d = 0; d < 3; d++) act[d] = G.dims[d] == 1 ? 1 : G.dims[d] / 2;
+        for (int d = 0; d < 3; d++) act[d] = ring_count(G.dims[d], phase_digit(ph, d));
         cc[0] = local % act[0];
         cc[1] = (local / act[0]) % act[1];
         cc[2] = local / (act[0] * act[1]);
-        for (int d = 0; d < 3; d++) c[d] = G.dims[d] == 1 ? 0 : 2 * cc[d] + ((ph >> d) & 1);
+        for (int d = 0; d < 3; d++) c[d] = ring_cell(G.dims[d], phase_digit(ph, d), cc[d]);
         const int cell = c[0] + G.dims[0] * (c[1] + G.dims[1] * c[2]);
         sweep_cell<KIND, false, 0>(A, local, cell, cap, A.overflow, A.overflow_count, cpos, cax, qseg, qun, nacc,
                                        nullptr, nullptr, nullptr, ws);

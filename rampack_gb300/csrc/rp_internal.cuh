@@ -95,6 +95,42 @@ struct DevState {
 };
 
 constexpr int MAX_CEN = RP_MAX_CENTRES;
+
+// ---- checkerboard colouring ------------------------------------------------------------
+// Along each dimension the cells form a ring of n cells, coloured so that neighbours differ:
+// one colour for n = 1, two alternating colours for even n, and for odd n the colours
+// c mod 3 (the last cell of a ring with n mod 3 = 1 takes colour 1).  A phase is one colour
+// per dimension, coded p0 + 3 p1 + 9 p2; the cells of a phase never interact, since two of
+// them differ in some dimension where they sit at least one cell apart.
+constexpr int MAX_PHASES = 27;
+RP_HD int ring_ncol(int n) { return n == 1 ? 1 : (n % 2 == 0 ? 2 : 3); }
+RP_HD int ring_colour(int n, int c) {
+    const int k = ring_ncol(n);
+    if (k == 1) return 0;
+    if (k == 2) return c & 1;
+    if (n % 3 == 1 && c == n - 1) return 1;
+    return c % 3;
+}
+RP_HD int ring_count(int n, int p) {  // cells of colour p
+    const int k = ring_ncol(n);
+    if (k == 1) return 1;
+    if (k == 2) return n / 2;
+    int cnt = (n - p + 2) / 3;
+    if (n % 3 == 1) cnt += (p == 1) - (p == 0);
+    return cnt;
+}
+RP_HD int ring_cell(int n, int p, int i) {  // the i-th cell of colour p
+    const int k = ring_ncol(n);
+    if (k == 1) return 0;
+    if (k == 2) return 2 * i + p;
+    if (n % 3 == 1 && p == 1 && i == ring_count(n, 1) - 1) return n - 1;
+    return 3 * i + p;
+}
+RP_HD int phase_digit(int ph, int d) { return d == 0 ? ph % 3 : (d == 1 ? (ph / 3) % 3 : ph / 9); }
+RP_HD int cell_phase(const int *dims, int cell) {
+    const int cx = cell % dims[0], cy = (cell / dims[0]) % dims[1], cz = cell / (dims[0] * dims[1]);
+    return ring_colour(dims[0], cx) + 3 * ring_colour(dims[1], cy) + 9 * ring_colour(dims[2], cz);
+}
 // per-warp polysphere scratch of the sweep (float4 units): the mover's FP32 centres
 // [MAX_CEN], the centre-pair thresholds [2 MAX_CEN^2 floats], the mover's exact centres
 // and absolute centres [2 x 3 MAX_CEN doubles]
@@ -153,7 +189,7 @@ struct SweepArgs {
 // arrays that the kernels search.
 struct alignas(16) BatchRep {
     SweepArgs a;
-    int phases[8];
+    int phases[MAX_PHASES];
     int nphases;
     int scale;                     // 1: this replica's positions are rescaled (box move)
     double old_inv[9], new_box[9];

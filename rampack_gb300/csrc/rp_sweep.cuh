@@ -202,7 +202,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
         int a1 = w % A.active[1];
         int a2 = w / A.active[1];
         int cc[3] = {a0, a1, a2};
-        for (int d = 0; d < 3; d++) c[d] = G.dims[d] == 1 ? 0 : 2 * cc[d] + A.phase[d];
+        for (int d = 0; d < 3; d++) c[d] = ring_cell(G.dims[d], A.phase[d], cc[d]);
         cell = c[0] + G.dims[0] * (c[1] + G.dims[1] * c[2]);
     }
     c[0] = cell % G.dims[0];

@@ -25,6 +25,25 @@ from . import _lib
 from ._lib import (MOVE_DTYPE, EngineError, GridInfo, ShapeDesc, SweepParams, SweepStats, dptr, fptr)
 
 
+def ring_colour(n: int, c: int) -> int:
+    """Checkerboard colour of cell coordinate c on a ring of n cells (the engine's rule:
+    one colour for n = 1, alternating for even n, c mod 3 for odd n with the last cell of a
+    ring with n mod 3 = 1 taking colour 1)."""
+    if n == 1:
+        return 0
+    if n % 2 == 0:
+        return c & 1
+    if n % 3 == 1 and c == n - 1:
+        return 1
+    return c % 3
+
+
+def cell_phase(dims, cell: int) -> int:
+    """The sweep phase of a cell: colours coded p0 + 3 p1 + 9 p2."""
+    cx, cy, cz = cell % dims[0], (cell // dims[0]) % dims[1], cell // (dims[0] * dims[1])
+    return ring_colour(dims[0], cx) + 3 * ring_colour(dims[1], cy) + 9 * ring_colour(dims[2], cz)
+
+
 class GpuPacking:
     def __init__(self, kind: int, params, pos, rot, box, device: int = 0):
         self.lib = _lib.load()

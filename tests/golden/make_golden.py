@@ -94,18 +94,20 @@ def gen_geometry(rng):
 
 
 def grid_cells(pos, box, range_, shift):
-    """Checkerboard cells of the GPU engine's grid rule (even counts, cells >= range),
-    restated in numpy to pick each cell's particles; particles within 1e-9 (relative) of a
-    cell face are left out of the per-cell lists so the membership never hinges on rounding."""
+    """Checkerboard cells of the GPU engine's grid rule (cells at least one range high and
+    at most max(4096, 8 N) of them; an odd count above 9 drops one cell), restated in numpy
+    to pick each cell's particles; particles within 1e-9 (relative) of a cell face are left
+    out of the per-cell lists so the membership never hinges on rounding."""
     b = box.reshape(3, 3)
     s = [b[:, 0], b[:, 1], b[:, 2]]
     vol = abs(np.dot(np.cross(s[0], s[1]), s[2]))
     h = [vol / np.linalg.norm(np.cross(s[1], s[2])), vol / np.linalg.norm(np.cross(s[2], s[0])),
          vol / np.linalg.norm(np.cross(s[0], s[1]))]
     dims = []
+    cell_min = max(range_, (vol / max(4096.0, 8.0 * len(pos))) ** (1 / 3)) * (1 + 1e-9)
     for d in range(3):
-        n = int(np.floor(h[d] / (range_ * (1 + 1e-9))))
-        dims.append(n & ~1 if n >= 2 else 1)
+        n = max(1, int(np.floor(h[d] / cell_min)))
+        dims.append(n - 1 if n > 9 and n % 2 else n)
     rel = pos @ np.linalg.inv(b).T
     u = (rel - np.array(shift)) % 1.0
     un = u * np.array(dims)
@@ -151,13 +153,11 @@ def gen_system(name, cfg, trans, rot, rng, nshift=2, seed=77):
         cur_pos, _, cur_box = ref.state()
         dims, cell, safe, bounds = grid_cells(cur_pos, cur_box, range_, shift)
         chunk = []
-        for ph in range(8):
-            par = [(ph >> d) & 1 for d in range(3)]
-            if any(dims[d] == 1 and par[d] for d in range(3)):
-                continue
+        from rampack_gb300.packing import cell_phase
+        phase = [cell_phase(dims, ci) for ci in range(len(bounds))]
+        for ph in sorted(set(phase)):
             for ci in range(len(bounds)):
-                cc = (ci % dims[0], (ci // dims[0]) % dims[1], ci // (dims[0] * dims[1]))
-                if any(dims[d] > 1 and (cc[d] & 1) != par[d] for d in range(3)):
+                if phase[ci] != ph:
                     continue
                 idx = np.nonzero((cell == ci) & safe)[0]
                 if len(idx) == 0:

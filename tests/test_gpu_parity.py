@@ -53,18 +53,16 @@ def test_count_overlaps(oracle, engine, name, factor):
 def draw_cell_moves(cpu, g, seed, trans, rot, shift):
     """Moves for every active cell, phase by phase, drawn with the reference samplers'
     algorithm from each cell's particle list (DD domain = cell)."""
+    from rampack_gb300.packing import cell_phase
     info = g.set_grid(shift)
     _, cells, bounds = g.grid()
     dims = info["dims"]
     rng = cpu.rng(seed)
     chunks = []
-    for ph in range(8):
-        par = [(ph >> d) & 1 for d in range(3)]
-        if any(dims[d] == 1 and par[d] for d in range(3)):
-            continue
+    phase = [cell_phase(dims, c) for c in range(info["num_cells"])]
+    for ph in sorted(set(phase)):
         for cell in range(info["num_cells"]):
-            c = (cell % dims[0], (cell // dims[0]) % dims[1], cell // (dims[0] * dims[1]))
-            if any(dims[d] > 1 and (c[d] & 1) != par[d] for d in range(3)):
+            if phase[cell] != ph:
                 continue
             idx = np.nonzero(cells == cell)[0]
             if len(idx) == 0:
