@@ -310,7 +310,13 @@ DevState dev_state(Handle *h) {
     s.cen64 = h->cen64;
     s.abs64 = h->abs64[h->pcur];
     s.cthr64 = h->cthr64;
-    s.pbc_fold = h->grid[h->gcur].no_ng ? 1 : 0;
+    if (h->grid[h->gcur].no_ng) {
+        const bool sheared = h->box[1] != 0 || h->box[2] != 0 || h->box[3] != 0 || h->box[5] != 0 || h->box[6] != 0 ||
+                             h->box[7] != 0;
+        s.pbc_fold = sheared ? 2 : 1;
+    } else {
+        s.pbc_fold = 0;
+    }
     s.counting = h->counting ? 1 : 0;
     s.overlaps = h->d_overlaps;
     // ---- FP32 filter margins for the current grid ----
@@ -591,6 +597,9 @@ SweepArgs base_args(Handle *h) {
     a.s = dev_state(h);
     a.g = h->grid[h->gcur].d;
     a.cap = h->grid[h->gcur].cap;
+    // sphere distances of a sheared box without the reference's grid are not geometric:
+    // no FP32 certificate, every pair in FP64
+    a.fp64_only = (a.s.pbc_fold == 2 && a.s.kind != 1) ? 1 : 0;
     a.overflow = h->overflow;
     a.overflow_count = h->overflow_count;
     return a;
@@ -1299,7 +1308,7 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
         a.rtab64 = h->rtab64;
         a.rtab32 = h->rtab32;
         a.rtab_mask = ROT_TABLE - 1;
-        a.fp64_only = (p->flags & RP_SWEEP_FP64_ONLY) ? 1 : 0;
+        if (p->flags & RP_SWEEP_FP64_ONLY) a.fp64_only = 1;
         if (log) {
             a.log = h->d_log;
             a.log_codes = h->d_log_codes;
@@ -2111,7 +2120,7 @@ int rp_batch_sweep(void *batch, const rp_sweep_params *p, rp_sweep_stats *stats)
         a.rtab64 = b->rtab64;
         a.rtab32 = b->rtab32;
         a.rtab_mask = ROT_TABLE - 1;
-        a.fp64_only = (p->flags & RP_SWEEP_FP64_ONLY) ? 1 : 0;
+        if (p->flags & RP_SWEEP_FP64_ONLY) a.fp64_only = 1;
         if (log) {
             a.log = h->d_log;
             a.log_codes = h->d_log_codes;

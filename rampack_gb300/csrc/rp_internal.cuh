@@ -84,9 +84,12 @@ struct DevState {
     double *cen64;                 // [n][ncen][3]
     double *abs64;                 // [n][ncen][3] (position + centre, wrapped into the box)
     const double *cthr64;          // [MAX_CEN^2] (r_a + r_b)^2, FP64 as the reference forms it
-    // 1 when the reference keeps no neighbour grid for this box (core/Packing.cpp:862-881):
+    // nonzero when the reference keeps no neighbour grid for this box (core/Packing.cpp:862-881):
     // it then measures sphere and polysphere-centre distances with the periodic boundary
-    // conditions' own formula (pbc_distance2) instead of a cell translation
+    // conditions' own formula (pbc_distance2: per-coordinate |relative separation| folded
+    // into [0, 1/2]) instead of a cell translation.  1: orthorhombic box, where that is the
+    // true distance and the FP32 filter holds; 2: sheared box, where it is not, and every
+    // sphere or centre pair is decided in FP64
     int pbc_fold;
     // overlap counting (Packing::toggleOverlapCounting): the cached total count, which
     // accepted moves update by their overlap delta

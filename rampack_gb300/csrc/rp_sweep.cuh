@@ -428,7 +428,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
         // (the staged candidate and the FP32 arithmetic of the full scan, so a certain
         // overlap here is one the scan would find)
         bool overlap = false;
-        if (LEARN && A.partners && dom != 1) {
+        if (LEARN && A.partners && dom != 1 && !A.fp64_only) {
             int cls = 0;
             bool tested = false;
             if (lane < MLP_PARTNERS) {
@@ -993,7 +993,7 @@ __device__ __forceinline__ void count_one(const DevState &s, const GridDev &g, i
                 float4 a = g.maxis[k];
                 aj = make_float3(a.x, a.y, a.z);
             }
-            int cls = classify<KIND>(s.fc, dsep, ai, aj);
+            int cls = (KIND != 1 && s.pbc_fold == 2) ? 2 : classify<KIND>(s.fc, dsep, ai, aj);
             bool ov = cls == 1;
             if (cls == 2) {
                 if (!have64) {
@@ -1045,8 +1045,9 @@ __device__ __forceinline__ void count_poly_one(const DevState &s, const GridDev 
                     float4 ca = g.mcen[(size_t)slot * K + a];
                     float3 d = make_float3(bj.x - ca.x, bj.y - ca.y, bj.z - ca.z);
                     float d2 = dot3f(d, d);
-                    bool ov = d2 < g.cthr[a * MAX_CEN + j];
-                    if (!ov && d2 <= g.cthr[MAX_CEN * MAX_CEN + a * MAX_CEN + j]) {
+                    const bool exact = s.pbc_fold == 2;
+                    bool ov = !exact && d2 < g.cthr[a * MAX_CEN + j];
+                    if (!ov && (exact || d2 <= g.cthr[MAX_CEN * MAX_CEN + a * MAX_CEN + j])) {
                         atomicAdd(s.counters + 5, 1ull);
                         ov = exact_centre_pair(s, load_d3(s.abs64 + 3 * ((size_t)pid * K + a)), a, pj, j, d);
                     }

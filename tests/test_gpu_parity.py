@@ -149,3 +149,28 @@ def test_box_moves(oracle, engine, name):
             gp, gr, gb = g.state()
             cp, cr, cb = cpu.state()
             assert np.array_equal(gp, cp) and np.array_equal(gb, cb)
+
+
+@pytest.mark.parametrize("shear", [0.0, 0.04])
+def test_tiny_box_without_reference_grid(oracle, engine, shear):
+    """Boxes where the reference keeps no neighbour grid measure sphere distances with the
+    periodic boundary conditions' formula; in a sheared box that is not the geometric
+    distance, so every pair is decided in FP64 (and the decisions still match)."""
+    kind, prm, pos, rot, box = systems.hs_tiny()
+    b = box.reshape(3, 3).copy()
+    b[0, 1] = shear * b[1, 1]
+    b[1, 2] = -shear * b[2, 2]
+    rel = pos @ np.linalg.inv(box.reshape(3, 3)).T
+    cfg = (kind, prm, np.ascontiguousarray(rel @ b.T), rot, b.reshape(9))
+    cpu = cpu_packing(cfg)
+    with gpu_packing(cfg) as g:
+        assert g.count_total_overlaps(False) == cpu.count_overlaps(False)
+        for cycle in range(4):
+            g.sweep(0.1, 0.0, seed=31, counter=cycle, log=True)
+            moves, codes = g.sweep_log()
+            _, _, bounds = g.grid()
+            want, _ = cpu.replay(moves, bounds)
+            assert np.array_equal(codes, want)
+        gp, _, _ = g.state()
+        cp, _, _ = cpu.state()
+        assert np.array_equal(gp, cp)
