@@ -95,7 +95,7 @@ def gen_geometry(rng):
 
 def grid_cells(pos, box, range_, shift):
     """Checkerboard cells of the GPU engine's grid rule (cells at least one range high and
-    at most max(4096, 8 N) of them; an odd count above 9 drops one cell), restated in numpy
+    at most max(4096, 8 N) of them; an odd count above 3 drops one cell), restated in numpy
     to pick each cell's particles; particles within 1e-9 (relative) of a cell face are left
     out of the per-cell lists so the membership never hinges on rounding."""
     b = box.reshape(3, 3)
@@ -107,7 +107,7 @@ def grid_cells(pos, box, range_, shift):
     cell_min = max(range_, (vol / max(4096.0, 8.0 * len(pos))) ** (1 / 3)) * (1 + 1e-9)
     for d in range(3):
         n = max(1, int(np.floor(h[d] / cell_min)))
-        dims.append(n - 1 if n > 9 and n % 2 else n)
+        dims.append(n - 1 if n > 3 and n % 2 else n)
     rel = pos @ np.linalg.inv(b).T
     u = (rel - np.array(shift)) % 1.0
     un = u * np.array(dims)

@@ -83,7 +83,7 @@ def test_known_answer_translation_with_active_domain(engine, oracle, dy):
     with GpuPacking(kind, prm, pos, rot, box) as pk:
         info = pk.set_grid((0.0, 0.0, 0.0))
         _, cells, bounds = pk.grid()
-        assert info["dims"] == (9, 9, 9)  # floor(5 / (0.5 (1 + 1e-9))) = 9: odd, three colours
+        assert info["dims"] == (8, 8, 8)  # floor(5 / (0.5 (1 + 1e-9))) = 9, odd above 3: one cell fewer
         mv = np.zeros(1, dtype=_lib.MOVE_DTYPE)
         mv["particle"], mv["type"], mv["domain"], mv["uniform"] = 2, 0, int(cells[2]), 0.5
         mv["translation"][0] = [dy, dy, dy] if dy < 0.1 else [2, dy, -3.5]
