@@ -186,16 +186,15 @@ __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(co
     const int warps_per_block = blockDim.x >> 5;
     const int warp = blockIdx.x * warps_per_block + wib;
     // per-warp shared memory (float4 units): staged positions [cap], spherocylinder axes
-    // [cap] or polysphere centres [cap x 3K floats], two uint16 queues and a byte counter
+    // [cap] or polysphere mirror slots [cap uint32], two uint16 queues and a byte counter
     // per slot [5 cap bytes], partner slots [LEARN], polysphere scratch [SWEEP_POLY_SCRATCH]
-    const int K = KIND == 2 ? A.s.ncen : 0;
-    const int extra = KIND == 1 ? A.cap : (KIND == 2 ? A.cap * 3 * K / 4 : 0);
+    const int extra = KIND == 1 ? A.cap : (KIND == 2 ? A.cap / 4 : 0);
     constexpr bool LEARN = MODE == 1;
     const int per_warp = A.cap + extra + A.cap / 4 + A.cap / 16 + (LEARN ? A.cap / 4 : 0) +
                          (KIND == 2 ? SWEEP_POLY_SCRATCH : 0);
     float4 *cpos = smem + (size_t)wib * per_warp;
     float4 *cax = cpos + A.cap;                                  // spherocylinders
-    float *ccen = reinterpret_cast<float *>(cpos + A.cap);       // polyspheres
+    uint32_t *cslot = reinterpret_cast<uint32_t *>(cpos + A.cap); // polyspheres: mirror slot of each candidate
     uint16_t *qseg = reinterpret_cast<uint16_t *>(cpos + A.cap + extra);
     uint16_t *qun = qseg + A.cap;
     uint8_t *nacc = reinterpret_cast<uint8_t *>(qun + A.cap);
@@ -215,7 +214,7 @@ __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(co
         }
         if (item >= nitems) break;
         sweep_cell<KIND, LIST, MODE>(A, item, -1, A.cap, A.overflow, A.overflow_count, cpos, cax, qseg, qun, nacc,
-                                      pstage, ccen, wx, ws);
+                                      pstage, cslot, wx, ws);
         __syncwarp();
         item += stride;
     }
@@ -281,7 +280,7 @@ cudaError_t launch_abs_centres(const DevState &s, cudaStream_t st) {
 }
 
 size_t sweep_smem_per_warp(int kind, int cap, bool learn, int ncen) {
-    const int extra = kind == 1 ? cap : (kind == 2 ? cap * 3 * ncen / 4 : 0);
+    const int extra = kind == 1 ? cap : (kind == 2 ? cap / 4 : 0);
     return (size_t)(cap + extra + cap / 4 + cap / 16 + (learn ? cap / 4 : 0) + (kind == 2 ? SWEEP_POLY_SCRATCH : 0)) *
            sizeof(float4);
 }

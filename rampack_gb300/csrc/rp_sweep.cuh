@@ -178,7 +178,7 @@ template <int KIND, bool LIST, int MODE>
 __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, const int cell_direct, const int cap,
                                            int32_t *ovf, int32_t *ovf_count, float4 *cpos, float4 *cax,
                                            uint16_t *qseg, uint16_t *qun, uint8_t *nacc, uint16_t *pstage,
-                                           float *ccen, float4 *wx, WarpStats &ws) {
+                                           uint32_t *cslot, float4 *wx, WarpStats &ws) {
     constexpr bool LEARN = MODE == 1;
     constexpr bool COUNT = MODE == 2;
     const unsigned FULL = 0xffffffffu;
@@ -249,15 +249,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
             p.z += off.z;
             cpos[base + k] = p;
             if (KIND == 1) cax[base + k] = G.maxis[st + k];
-            if (KIND == 2) {
-                for (int b = 0; b < S.ncen; b++) {
-                    float4 c = G.mcen[(size_t)(st + k) * S.ncen + b];
-                    float *dst = ccen + 3 * ((size_t)(base + k) * S.ncen + b);
-                    dst[0] = c.x;
-                    dst[1] = c.y;
-                    dst[2] = c.z;
-                }
-            }
+            if (KIND == 2) cslot[base + k] = (uint32_t)(st + k);  // its centres stay in the L2-resident mirror
         }
     }
     // polyspheres: the warp's scratch holds the mover's FP32 centres (wx[0..K)), the
@@ -400,8 +392,8 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
         if (KIND == 2) {
             // the mover's FP32 centres after the move (rotated by the FP32 rotation)
             if (lane < S.ncen) {
-                const float *c = ccen + 3 * ((size_t)slot * S.ncen + lane);
-                float3 cn = make_float3(c[0], c[1], c[2]);
+                const float4 c = G.mcen[((size_t)gbase + slot) * S.ncen + lane];
+                float3 cn = make_float3(c.x, c.y, c.z);
                 if (type != 0) cn = mat32(R32, cn.x, cn.y, cn.z);
                 wx[lane] = make_float4(cn.x, cn.y, cn.z, 0.f);
             }
@@ -501,9 +493,10 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                     k = qseg[i];
                     const float4 q = cpos[k];
                     const float3 dq = make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z);
-                    const float *cj = ccen + 3 * (size_t)k * K;
+                    const float4 *cj = G.mcen + (size_t)cslot[k] * K;
                     for (int j = 0; j < K && cls != 1; j++) {
-                        const float3 bj = make_float3(dq.x + cj[3 * j], dq.y + cj[3 * j + 1], dq.z + cj[3 * j + 2]);
+                        const float4 c = cj[j];
+                        const float3 bj = make_float3(dq.x + c.x, dq.y + c.y, dq.z + c.z);
                         for (int a = 0; a < K; a++) {
                             const float4 m = wx[a];
                             const float3 d = make_float3(bj.x - m.x, bj.y - m.y, bj.z - m.z);
@@ -704,15 +697,15 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                     const int k = qun[qi];
                     const float4 q = cpos[k];
                     const float3 dq = make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z);
-                    const float *cj = ccen + 3 * (size_t)k * K;
+                    const float4 *cj = G.mcen + (size_t)cslot[k] * K;
                     for (int tb = 0; tb < K * K; tb += 32) {
                         const int t = tb + lane;
                         bool hit = false;
                         if (t < K * K) {
                             const int a = t / K, j = t % K;
                             const float4 m = wx[a];
-                            const float3 d = make_float3((dq.x + cj[3 * j]) - m.x, (dq.y + cj[3 * j + 1]) - m.y,
-                                                         (dq.z + cj[3 * j + 2]) - m.z);
+                            const float4 c = cj[j];
+                            const float3 d = make_float3((dq.x + c.x) - m.x, (dq.y + c.y) - m.y, (dq.z + c.z) - m.z);
                             hit = exact_centre_pair(S, d3{wabs[3 * a], wabs[3 * a + 1], wabs[3 * a + 2]}, a,
                                                     __float_as_int(q.w), j, d);
                         }
@@ -834,10 +827,6 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                     const float4 c32 = make_float4((float)wcen[3 * lane], (float)wcen[3 * lane + 1],
                                                    (float)wcen[3 * lane + 2], 0.f);
                     G.mcen[gslot * S.ncen + lane] = c32;
-                    float *dst = ccen + 3 * ((size_t)slot * S.ncen + lane);
-                    dst[0] = c32.x;
-                    dst[1] = c32.y;
-                    dst[2] = c32.z;
                 }
             }
             if (self_images) {
@@ -848,9 +837,6 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                     if (__float_as_int(q.w) == pid) {
                         cpos[k] = make_float4(np.x + (q.x - pcur.x), np.y + (q.y - pcur.y), np.z + (q.z - pcur.z), q.w);
                         if (KIND == 1 && type != 0) cax[k] = na;
-                        if (KIND == 2 && type != 0)
-                            for (int e = 0; e < 3 * S.ncen; e++)
-                                ccen[3 * (size_t)k * S.ncen + e] = ccen[3 * (size_t)slot * S.ncen + e];
                     }
                 }
             }
