@@ -256,10 +256,16 @@ def cycle(g, k, seed, rng, stats=False):
     return st, accepted
 
 
-def read_profile_traffic():
-    """Per-launch DRAM traffic of the sweep kernel from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "k_sweep_sc_n1e6.md")
-    if not os.path.exists(path):
+PROFILES = {"sc-1e6": "k_sweep_sc_n1e6.md", "banana-1e5": "k_sweep_banana_n1e5.md",
+            "replicas-64": "k_b_sweep_replicas_64.md"}
+
+
+def read_profile_traffic(workload):
+    """Per-launch DRAM traffic of the workload's sweep kernel from its committed ncu summary
+    (one --set full capture of a steady-state launch), if any."""
+    name = PROFILES.get(workload)
+    path = os.path.join(ROOT, "profiles", name) if name else ""
+    if not name or not os.path.exists(path):
         return None
     for line in open(path):
         if line.strip().startswith("traffic_bytes_per_launch:"):
@@ -372,7 +378,7 @@ def main_gpu(args):
         peak, peak_src = json.load(open(peaks_path))["hbm_gbs"], "measured"
     else:
         peak, peak_src = 6800.0, "fallback"
-    traffic = read_profile_traffic() if args.workload == "sc-1e6" else None
+    traffic = read_profile_traffic(args.workload)
     state_mb = n * (96 + 32 + 64 * kcen) / 1e6
     l2_note = (f"inputs larger than L2 (FP64 state + FP32 mirror {state_mb:.0f} MB + cell lists)" if state_mb > 129
                else f"inputs smaller than L2 ({state_mb:.0f} MB of state; no flush between steps)")
@@ -608,6 +614,21 @@ def main_replicas(args):
     s0 = {k: b.sweep(*steps[k], seed=args.seed + 99, counter=0, stats=True) for k, b in batches.items()}
     acc = sum(x["accepted"] for v in s0.values() for x in v) / max(1, sum(x["moves"] for v in s0.values() for x in v))
     state["box_acc"] = 0
+    # per-launch sweep bytes (the single-system formula per replica, summed): P·n·(28+4) +
+    # P·(C+1)·4 + M·(96 + a·(96+28)) with P the replica's phases, C its cells, M its moves
+    b_cycle, sweep_launches_per_cycle = 0.0, 0
+    for kind, b in batches.items():
+        maxph = 0
+        for r in range(b.R):
+            info, _, _ = b.grid(r)
+            P = int(np.prod([1 if d == 1 else (3 if d == 3 else 2) for d in info["dims"]]))
+            maxph = max(maxph, P)
+            m = (2 if kind == 1 else 1) * b.sizes[r]
+            b_cycle += P * b.sizes[r] * 32 + P * (info["num_cells"] + 1) * 4 + m * (96 + acc * 124)
+        sweep_launches_per_cycle += maxph
+    for b in batches.values():
+        b.set_timing(True)
+    launches0 = sum(b.timing()[1] for b in batches.values())
     clocks = Clocks(0)
     clocks.start()
     time.sleep(0.3)
@@ -622,6 +643,57 @@ def main_replicas(args):
     clk = clocks.stop(t0, time.time())
     value = moves_per_cycle * args.steps / dt
     n = sum(len(r[2]) for r in reps)
+    timing = {}
+    launches = -launches0
+    for b in batches.values():
+        t, l = b.timing()
+        launches += l
+        for name, (ms_, g) in t.items():
+            a = timing.setdefault(name, [0.0, 0])
+            a[0] += ms_
+            a[1] += g
+        b.set_timing(False)
+    sweep_ms, sweep_groups = timing["sweep"]
+    avg_launch_ms = sweep_ms / max(1, sweep_groups)
+    b_launch = b_cycle / sweep_launches_per_cycle
+    achieved = b_launch / (avg_launch_ms / 1e3) / 1e9
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peak, peak_src = json.load(open(peaks_path))["hbm_gbs"], "measured (MEASURED_PEAKS.json hbm_gbs)"
+    else:
+        peak, peak_src = 6800.0, "fallback 6.8 TB/s"
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": read_profile_traffic("replicas-64"),
+                "kernel": "k_b_sweep (one launch per checkerboard phase and batch)", "peak_source": peak_src,
+                "avg_launch_ms": avg_launch_ms, "bytes_per_launch": b_launch}
+
+    # ---- end to end through the C ABI: every replica's state from pinned host buffers,
+    # one cycle, every state back into the same buffers ----
+    e2e = None
+    if not args.no_e2e:
+        host = {}
+        for kind, b in batches.items():
+            tot = sum(b.sizes)
+            host[kind] = (torch.empty((tot, 3), dtype=torch.float64, pin_memory=True).numpy(),
+                          torch.empty((tot, 9), dtype=torch.float64, pin_memory=True).numpy(),
+                          torch.empty((b.R, 9), dtype=torch.float64, pin_memory=True).numpy())
+            b.states(out=host[kind])
+            boxes[kind][:] = host[kind][2]
+        torch.cuda.synchronize()
+        tp = time.perf_counter()
+        for _ in range(args.steps):
+            for kind, b in batches.items():
+                b.upload_all(*host[kind])
+            one_cycle()
+            for kind, b in batches.items():
+                b.states(out=host[kind])
+        torch.cuda.synchronize()
+        e_dt = time.perf_counter() - tp
+        nbytes = sum(h[0].nbytes + h[1].nbytes + h[2].nbytes for h in host.values())
+        e2e = {"value": moves_per_cycle * args.steps / e_dt, "unit": UNIT, "h2d_bytes_per_step": int(nbytes),
+               "d2h_bytes_per_step": int(nbytes),
+               "step": "rp_batch_upload_states (pinned host -> device, both batches) + one cycle + "
+                       "rp_batch_download_states (device -> pinned host)"}
     for b in batches.values():
         b.close()
     print(json.dumps({
@@ -633,7 +705,9 @@ def main_replicas(args):
                              "overlap checks; each cycle ends in a device synchronisation)",
                    "autotune": tune, "tuning": best, "box_moves_accepted": state["box_acc"],
                    "l2": "inputs smaller than L2 (no flush between steps)"},
-        "acceptance": acc, "roofline": None, "e2e": None, "clocks": clk, "cpu_baseline": cpu_base,
+        "acceptance": acc, "roofline": roofline,
+        "kernel_ms": {name: {"ms": v[0], "groups": v[1]} for name, v in timing.items()},
+        "gpu_launches": launches, "e2e": e2e, "clocks": clk, "cpu_baseline": cpu_base,
     }))
     return 0
 

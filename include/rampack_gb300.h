@@ -351,6 +351,19 @@ int rp_batch_revert_scaling(void *batch, const uint8_t *mask);
  * 2, 4 or 8 warps per block of the sweep kernel (defaults 1.0 and 4). */
 int rp_batch_set_tuning(void *batch, double cell_factor, int32_t warps_per_block);
 
+/* Every replica's state at once: pos [sum n][3], rot [sum n][9] with the replicas' particles
+ * in replica order, boxes [R][9].  The upload copies on the batch's stream (one copy per
+ * array and replica), rebuilds every replica's cell grid in one batched launch and checks
+ * that each particle lies inside its box; the download waits for the batch's work. */
+int rp_batch_upload_states(void *batch, const double *pos, const double *rot, const double *boxes);
+int rp_batch_download_states(void *batch, double *pos, double *rot, double *boxes);
+
+/* Per-group device timing of the batch's own launches (RP_KERNEL_* groups), as
+ * rp_set_timing / rp_get_timing; `launches` (may be null) receives the kernels launched by
+ * the batch and its replicas since creation. */
+int rp_batch_set_timing(void *batch, int on);
+int rp_batch_get_timing(void *batch, double *ms, uint64_t *groups, uint64_t *launches);
+
 /* ---- allocation-free overlap count ----------------------------------------------- */
 
 /* Limits of rp_count_overlaps_static and the size of the scratch array behind it. */

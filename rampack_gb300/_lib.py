@@ -108,6 +108,10 @@ SIGNATURES = {
     "rp_batch_try_scaling": (C.c_int, [_P, _D, _P, _D]),
     "rp_batch_revert_scaling": (C.c_int, [_P, _P]),
     "rp_batch_set_tuning": (C.c_int, [_P, C.c_double, C.c_int32]),
+    "rp_batch_upload_states": (C.c_int, [_P, _D, _D, _D]),
+    "rp_batch_download_states": (C.c_int, [_P, _D, _D, _D]),
+    "rp_batch_set_timing": (C.c_int, [_P, C.c_int]),
+    "rp_batch_get_timing": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
 }
 KERNEL_GROUPS = ["sweep", "rebuild", "count", "rescale", "overflow", "order", "mlp", "fix"]
 MLP_NPARAM = 5313

@@ -72,6 +72,70 @@ struct GridHost {
     bool no_ng = false;       // the reference keeps no neighbour grid for this grid's box
 };
 
+// Per-group device timing: CUDA events around groups of launches, summed per group kind.
+struct Timing {
+    struct Mark {
+        int kid;
+        cudaEvent_t a, b;
+    };
+    bool on = false;
+    std::vector<Mark> marks;
+    std::vector<cudaEvent_t> pool;
+    double ms[RP_NUM_KERNELS]{};
+    uint64_t groups[RP_NUM_KERNELS]{};
+
+    cudaEvent_t event() {
+        if (!pool.empty()) {
+            cudaEvent_t e = pool.back();
+            pool.pop_back();
+            return e;
+        }
+        cudaEvent_t e = nullptr;
+        cudaEventCreate(&e);
+        return e;
+    }
+    // the owner's stream has been synchronized
+    void reset(bool enable) {
+        for (auto &m : marks) {
+            pool.push_back(m.a);
+            pool.push_back(m.b);
+        }
+        marks.clear();
+        for (int k = 0; k < RP_NUM_KERNELS; k++) {
+            ms[k] = 0;
+            groups[k] = 0;
+        }
+        on = enable;
+    }
+    // the owner's stream has been synchronized
+    cudaError_t collect(double *out_ms, uint64_t *out_groups) {
+        for (auto &m : marks) {
+            float t = 0;
+            cudaError_t e = cudaEventElapsedTime(&t, m.a, m.b);
+            if (e != cudaSuccess) return e;
+            ms[m.kid] += t;
+            groups[m.kid] += 1;
+            pool.push_back(m.a);
+            pool.push_back(m.b);
+        }
+        marks.clear();
+        for (int k = 0; k < RP_NUM_KERNELS; k++) {
+            if (out_ms) out_ms[k] = ms[k];
+            if (out_groups) out_groups[k] = groups[k];
+        }
+        return cudaSuccess;
+    }
+    void release() {
+        for (auto &m : marks) {
+            cudaEventDestroy(m.a);
+            cudaEventDestroy(m.b);
+        }
+        marks.clear();
+        for (auto e : pool) cudaEventDestroy(e);
+        pool.clear();
+    }
+};
+
 struct Handle {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -121,15 +185,7 @@ struct Handle {
     std::vector<int> log_phases;
     // launch accounting and optional per-group device timing
     uint64_t launches = 0;
-    bool timing = false;
-    struct Mark {
-        int kid;
-        cudaEvent_t a, b;
-    };
-    std::vector<Mark> marks;
-    std::vector<cudaEvent_t> event_pool;
-    double kernel_ms[RP_NUM_KERNELS]{};
-    uint64_t kernel_groups[RP_NUM_KERNELS]{};
+    Timing tm;
     bool strict_box = false;
     // polyspheres: body-frame centres and radii, the reference's centre range (its
     // neighbour-grid cell), rotated and absolute centres, exact pair thresholds
@@ -170,37 +226,29 @@ struct Handle {
     int pair_every = 0;
 };
 
-cudaEvent_t pool_event(Handle *h) {
-    if (!h->event_pool.empty()) {
-        cudaEvent_t e = h->event_pool.back();
-        h->event_pool.pop_back();
-        return e;
-    }
-    cudaEvent_t e = nullptr;
-    cudaEventCreate(&e);
-    return e;
-}
-
-// One group of kernel launches: counted, and bracketed by CUDA events when timing is on.
-struct Group {
-    Handle *h;
+// One group of kernel launches of a handle or a batch: counted, and bracketed by CUDA events
+// on the owner's stream when its timing is on.
+template <class Owner>
+struct GroupOf {
+    Owner *h;
     int kid;
     cudaEvent_t a = nullptr;
-    Group(Handle *h_, int kid_, int nkernels) : h{h_}, kid{kid_} {
+    GroupOf(Owner *h_, int kid_, int nkernels) : h{h_}, kid{kid_} {
         h->launches += static_cast<uint64_t>(nkernels);
-        if (h->timing) {
-            a = pool_event(h);
+        if (h->tm.on) {
+            a = h->tm.event();
             cudaEventRecord(a, h->stream);
         }
     }
-    ~Group() {
+    ~GroupOf() {
         if (a) {
-            cudaEvent_t b = pool_event(h);
+            cudaEvent_t b = h->tm.event();
             cudaEventRecord(b, h->stream);
-            h->marks.push_back({kid, a, b});
+            h->tm.marks.push_back({kid, a, b});
         }
     }
 };
+using Group = GroupOf<Handle>;
 
 int fail(Handle *h, int code, const std::string &msg) {
     if (h) h->err = msg;
@@ -719,8 +767,10 @@ struct Batch {
     int wpb = 4;
     int smem_optin = 48 * 1024;                       // largest dynamic shared memory per block
     uint64_t launches = 0;
+    Timing tm;
     std::string err;
 };
+using BGroup = GroupOf<Batch>;
 
 int bfail(Batch *b, int code, const std::string &msg) {
     if (b) b->err = msg;
@@ -980,11 +1030,7 @@ int rp_destroy(void *handle) {
                     (void *)h->mlp_out, (void *)h->partners, (void *)h->pair_feats, (void *)h->pair_labels,
                     (void *)h->pair_count})
         cudaFree(p);
-    for (auto &m : h->marks) {
-        cudaEventDestroy(m.a);
-        cudaEventDestroy(m.b);
-    }
-    for (auto e : h->event_pool) cudaEventDestroy(e);
+    h->tm.release();
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return RP_OK;
@@ -1011,18 +1057,9 @@ int rp_upload_state(void *handle, const double *pos, const double *rot, const do
     RP_CUDA(h, cudaMemcpyAsync(h->rot64, rot, sizeof(double) * 9 * h->n, cudaMemcpyHostToDevice, h->stream));
     if (h->ncen > 0) {
         // interactionCentres = orientation · centre (Packing::setupForInteraction,
-        // core/Packing.cpp:940-944); absolute centres on the device below
-        std::vector<double> cen(3 * h->n * h->ncen);
-        for (int64_t i = 0; i < h->n; i++)
-            for (int b = 0; b < h->ncen; b++) {
-                d3 c = mv3(rot + 9 * i, d3{h->cbody[3 * b], h->cbody[3 * b + 1], h->cbody[3 * b + 2]});
-                double *o = cen.data() + 3 * (i * h->ncen + b);
-                o[0] = c.x;
-                o[1] = c.y;
-                o[2] = c.z;
-            }
-        RP_CUDA(h, cudaStreamSynchronize(h->stream));
-        RP_CUDA(h, cudaMemcpy(h->cen64, cen.data(), sizeof(double) * cen.size(), cudaMemcpyHostToDevice));
+        // core/Packing.cpp:940-944), on the device; absolute centres after the rebuild
+        Group grp(h, RP_KERNEL_REBUILD, 1);
+        RP_CUDA(h, launch_fresh_centres(dev_state(h), h->cbody_dev, h->stream));
     }
     double tt[375];
     translation_table(h->box, tt);
@@ -1037,7 +1074,10 @@ int rp_upload_state(void *handle, const double *pos, const double *rot, const do
     if (rc) return rc;
     rc = check_status(h);  // the rebuild checks that every particle lies inside the box
     if (rc) return rc;
-    if (h->ncen > 0) RP_CUDA(h, launch_abs_centres(dev_state(h), h->stream));
+    if (h->ncen > 0) {
+        Group grp(h, RP_KERNEL_REBUILD, 1);
+        RP_CUDA(h, launch_abs_centres(dev_state(h), h->stream));
+    }
     h->has_state = true;
     h->can_revert = false;
     h->log_valid = false;
@@ -1506,16 +1546,7 @@ int rp_set_timing(void *handle, int on) {
     if (!h) return RP_ERR_ARG;
     RP_CUDA(h, cudaSetDevice(h->device));
     RP_CUDA(h, cudaStreamSynchronize(h->stream));
-    for (auto &m : h->marks) {
-        h->event_pool.push_back(m.a);
-        h->event_pool.push_back(m.b);
-    }
-    h->marks.clear();
-    for (int k = 0; k < RP_NUM_KERNELS; k++) {
-        h->kernel_ms[k] = 0;
-        h->kernel_groups[k] = 0;
-    }
-    h->timing = on != 0;
+    h->tm.reset(on != 0);
     return RP_OK;
 }
 
@@ -1524,19 +1555,7 @@ int rp_get_timing(void *handle, double *ms, uint64_t *groups) {
     if (!h) return RP_ERR_ARG;
     RP_CUDA(h, cudaSetDevice(h->device));
     RP_CUDA(h, cudaStreamSynchronize(h->stream));
-    for (auto &m : h->marks) {
-        float t = 0;
-        RP_CUDA(h, cudaEventElapsedTime(&t, m.a, m.b));
-        h->kernel_ms[m.kid] += t;
-        h->kernel_groups[m.kid] += 1;
-        h->event_pool.push_back(m.a);
-        h->event_pool.push_back(m.b);
-    }
-    h->marks.clear();
-    for (int k = 0; k < RP_NUM_KERNELS; k++) {
-        if (ms) ms[k] = h->kernel_ms[k];
-        if (groups) groups[k] = h->kernel_groups[k];
-    }
+    RP_CUDA(h, h->tm.collect(ms, groups));
     return RP_OK;
 }
 
@@ -2004,6 +2023,7 @@ int rp_batch_destroy(void *batch) {
         cudaFreeHost(S.bounds);
         if (S.done) cudaEventDestroy(S.done);
     }
+    b->tm.release();
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return RP_OK;
@@ -2041,6 +2061,107 @@ int rp_batch_download_state(void *batch, int32_t replica, double *pos, double *r
     int rc = rp_download_state(h, pos, rot, box9);
     if (rc) b->err = h->err;
     return rc;
+}
+
+int rp_batch_upload_states(void *batch, const double *pos, const double *rot, const double *boxes) {
+    Batch *b = static_cast<Batch *>(batch);
+    if (!b || !pos || !rot || !boxes) return bfail(b, RP_ERR_ARG, "null argument");
+    RB_CUDA(b, cudaSetDevice(b->device));
+    RB_CUDA(b, cudaStreamSynchronize(b->stream));
+    int64_t off = 0;
+    for (int r = 0; r < b->R; r++) {
+        Handle *h = b->rep[r];
+        const double *box9 = boxes + 9 * r;
+        if (det3(box9) == 0) return bfail(b, RP_ERR_ARG, "box volume is zero");
+        h->has_state = false;
+        std::memcpy(h->box, box9, sizeof(h->box));
+        inverse3(box9, h->inv);
+        h->pcur = 0;
+        h->gcur = 0;
+        h->partners_valid = false;
+        h->can_revert = false;
+        h->log_valid = false;
+        RB_CUDA(b, cudaMemcpyAsync(h->pos64[0], pos + 3 * off, sizeof(double) * 3 * h->n, cudaMemcpyHostToDevice,
+                                   b->stream));
+        RB_CUDA(b, cudaMemcpyAsync(h->rot64, rot + 9 * off, sizeof(double) * 9 * h->n, cudaMemcpyHostToDevice,
+                                   b->stream));
+        double tt[375];
+        translation_table(h->box, tt);
+        RB_CUDA(b, cudaMemcpyAsync(h->trans[0], tt, sizeof(tt), cudaMemcpyHostToDevice, b->stream));
+        double shift[3] = {0, 0, 0};
+        int rc = setup_grid(h, h->grid[0], h->box, shift);
+        if (rc) return bfail(b, rc, h->err);
+        h->strict_box = true;  // the rebuild checks that every particle lies inside its box
+        off += h->n;
+    }
+    int total_items = 0, total_p = 0, total_c = 0;
+    int rc = batch_tables(b, total_items, total_p, total_c);
+    for (Handle *h : b->rep) h->strict_box = false;
+    if (rc) return rc;
+    rc = batch_copy(b);
+    if (rc) return rc;
+    RB_CUDA(b, cudaMemsetAsync(b->status, 0, sizeof(uint32_t) * b->R, b->stream));
+    {
+        BGroup grp(b, RP_KERNEL_REBUILD, 5);
+        RB_CUDA(b, launch_b_rebuild(b->d_table, b->d_bases, b->d_bases + (b->R + 1), b->R, total_p, total_c,
+                                    b->stream));
+    }
+    std::vector<uint32_t> st(b->R);
+    RB_CUDA(b, cudaMemcpyAsync(st.data(), b->status, sizeof(uint32_t) * b->R, cudaMemcpyDeviceToHost, b->stream));
+    RB_CUDA(b, cudaStreamSynchronize(b->stream));
+    for (int r = 0; r < b->R; r++)
+        if (st[r]) {
+            RB_CUDA(b, cudaMemsetAsync(b->status, 0, sizeof(uint32_t) * b->R, b->stream));
+            if (st[r] & ST_OUTSIDE) return bfail(b, RP_ERR_ARG, "replica " + std::to_string(r) + ": a particle lies outside the box");
+            return bfail(b, RP_ERR_DEVICE, "replica " + std::to_string(r) + ": device status set");
+        }
+    for (Handle *h : b->rep) h->has_state = true;
+    return RP_OK;
+}
+
+int rp_batch_download_states(void *batch, double *pos, double *rot, double *boxes) {
+    Batch *b = static_cast<Batch *>(batch);
+    if (!b) return RP_ERR_ARG;
+    for (Handle *h : b->rep)
+        if (!h->has_state) return bfail(b, RP_ERR_STATE, "a replica has no state");
+    RB_CUDA(b, cudaSetDevice(b->device));
+    int64_t off = 0;
+    for (Handle *h : b->rep) {
+        if (pos)
+            RB_CUDA(b, cudaMemcpyAsync(pos + 3 * off, h->pos64[h->pcur], sizeof(double) * 3 * h->n,
+                                       cudaMemcpyDeviceToHost, b->stream));
+        if (rot)
+            RB_CUDA(b, cudaMemcpyAsync(rot + 9 * off, h->rot64, sizeof(double) * 9 * h->n, cudaMemcpyDeviceToHost,
+                                       b->stream));
+        off += h->n;
+    }
+    RB_CUDA(b, cudaStreamSynchronize(b->stream));
+    if (boxes)
+        for (int r = 0; r < b->R; r++) std::memcpy(boxes + 9 * r, b->rep[r]->box, sizeof(b->rep[r]->box));
+    return RP_OK;
+}
+
+int rp_batch_set_timing(void *batch, int on) {
+    Batch *b = static_cast<Batch *>(batch);
+    if (!b) return RP_ERR_ARG;
+    RB_CUDA(b, cudaSetDevice(b->device));
+    RB_CUDA(b, cudaStreamSynchronize(b->stream));
+    b->tm.reset(on != 0);
+    return RP_OK;
+}
+
+int rp_batch_get_timing(void *batch, double *ms, uint64_t *groups, uint64_t *launches) {
+    Batch *b = static_cast<Batch *>(batch);
+    if (!b) return RP_ERR_ARG;
+    RB_CUDA(b, cudaSetDevice(b->device));
+    RB_CUDA(b, cudaStreamSynchronize(b->stream));
+    RB_CUDA(b, b->tm.collect(ms, groups));
+    if (launches) {
+        uint64_t l = b->launches;
+        for (Handle *h : b->rep) l += h->launches;
+        *launches = l;
+    }
+    return RP_OK;
 }
 
 int rp_batch_count_overlaps(void *batch, int32_t replica, int early_exit, int64_t *count) {
@@ -2148,12 +2269,12 @@ int rp_batch_sweep(void *batch, const rp_sweep_params *p, rp_sweep_stats *stats)
     if (rc) return rc;
     const int *pb = b->d_bases, *cb = b->d_bases + (b->R + 1);
     if (stats) RB_CUDA(b, cudaMemsetAsync(b->stats, 0, sizeof(unsigned long long) * 8 * b->R, b->stream));
-    RB_CUDA(b, launch_b_rebuild(b->d_table, pb, cb, b->R, total_p, total_c, b->stream));
-    b->launches += 5;
-    if (types & 2) {
-        RB_CUDA(b, launch_rot_table(b->rtab64, b->rtab32, ROT_TABLE, p->seed, p->counter,
-                                    static_cast<float>(p->rotation_step), b->stream));
-        b->launches += 1;
+    {
+        BGroup grp(b, RP_KERNEL_REBUILD, (types & 2) ? 6 : 5);
+        RB_CUDA(b, launch_b_rebuild(b->d_table, pb, cb, b->R, total_p, total_c, b->stream));
+        if (types & 2)
+            RB_CUDA(b, launch_rot_table(b->rtab64, b->rtab32, ROT_TABLE, p->seed, p->counter,
+                                        static_cast<float>(p->rotation_step), b->stream));
     }
     RB_CUDA(b, cudaMemsetAsync(b->item_counters, 0, sizeof(int32_t) * MAX_PHASES, b->stream));
     // fewer warps per block when the staging of `cap` candidates per warp would not fit
@@ -2164,9 +2285,15 @@ int rp_batch_sweep(void *batch, const rp_sweep_params *p, rp_sweep_stats *stats)
     for (int k = 0; k < maxph; k++) {
         const int *ib = b->d_bases + (2 + k) * (b->R + 1);
         int blocks = std::max(1, std::min((phase_total[k] + wpb - 1) / wpb, b->num_sms * (16 / wpb)));
-        RB_CUDA(b, launch_b_sweep(b->d_table, ib, b->R, b->kind, k, b->item_counters + k, cap, wpb, blocks, b->stream));
-        RB_CUDA(b, launch_b_overflow(b->d_table, b->R, b->kind, k, ovf_cap, b->stream));
-        b->launches += 2;
+        {
+            BGroup grp(b, RP_KERNEL_SWEEP, 1);
+            RB_CUDA(b, launch_b_sweep(b->d_table, ib, b->R, b->kind, k, b->item_counters + k, cap, wpb, blocks,
+                                      b->stream));
+        }
+        {
+            BGroup grp(b, RP_KERNEL_OVERFLOW, 1);
+            RB_CUDA(b, launch_b_overflow(b->d_table, b->R, b->kind, k, ovf_cap, b->stream));
+        }
     }
     for (int r = 0; r < b->R; r++) {
         Handle *h = b->rep[r];
@@ -2192,6 +2319,8 @@ int rp_batch_sweep(void *batch, const rp_sweep_params *p, rp_sweep_stats *stats)
         RB_CUDA(b, cudaStreamSynchronize(b->stream));
         for (int r = 0; r < b->R; r++)
             if (st[r]) return bfail(b, (st[r] & ST_CAPACITY) ? RP_ERR_CAPACITY : RP_ERR_DEVICE, "device status set");
+        uint64_t all_launches = b->launches;
+        for (Handle *h : b->rep) all_launches += h->launches;
         if (stats)
             for (int r = 0; r < b->R; r++) {
                 const unsigned long long *q = c.data() + 8 * r;
@@ -2203,7 +2332,7 @@ int rp_batch_sweep(void *batch, const rp_sweep_params *p, rp_sweep_stats *stats)
                 stats[r].fp64_pairs = q[5];
                 stats[r].translations = q[6];
                 stats[r].rotations = q[7];
-                stats[r].kernel_launches = b->launches;
+                stats[r].kernel_launches = all_launches;
             }
     }
     return RP_OK;
@@ -2288,10 +2417,18 @@ int rp_batch_try_scaling(void *batch, const double *boxes, const uint8_t *propos
     const int *pb = b->d_bases, *cb = b->d_bases + (b->R + 1);
     RB_CUDA(b, cudaMemcpyAsync(b->flags, b->h_flags, sizeof(int) * b->R, cudaMemcpyHostToDevice, b->stream));
     RB_CUDA(b, cudaMemsetAsync(b->counts, 0, sizeof(unsigned long long) * b->R, b->stream));
-    RB_CUDA(b, launch_b_rescale(b->d_table, pb, b->R, total_p, b->stream));
-    RB_CUDA(b, launch_b_rebuild(b->d_table, pb, cb, b->R, total_p, total_c, b->stream));
-    RB_CUDA(b, launch_b_count(b->d_table, pb, b->R, total_p, b->kind, 1, b->counts, b->flags, b->stream));
-    b->launches += 8;
+    {
+        BGroup grp(b, RP_KERNEL_RESCALE, 2);
+        RB_CUDA(b, launch_b_rescale(b->d_table, pb, b->R, total_p, b->stream));
+    }
+    {
+        BGroup grp(b, RP_KERNEL_REBUILD, 5);
+        RB_CUDA(b, launch_b_rebuild(b->d_table, pb, cb, b->R, total_p, total_c, b->stream));
+    }
+    {
+        BGroup grp(b, RP_KERNEL_COUNT, 1);
+        RB_CUDA(b, launch_b_count(b->d_table, pb, b->R, total_p, b->kind, 1, b->counts, b->flags, b->stream));
+    }
     RB_CUDA(b, cudaMemcpyAsync(b->h_counts, b->counts, sizeof(unsigned long long) * b->R, cudaMemcpyDeviceToHost,
                                b->stream));
     RB_CUDA(b, cudaStreamSynchronize(b->stream));

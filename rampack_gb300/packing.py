@@ -397,6 +397,40 @@ class BatchPacking:
     def set_tuning(self, cell_factor: float = 1.0, warps_per_block: int = 4):
         self._check(self.lib.rp_batch_set_tuning(self.h, cell_factor, warps_per_block))
 
+    def upload_all(self, pos, rot, boxes):
+        """Every replica's state at once (rp_batch_upload_states): pos [sum n, 3] and
+        rot [sum n, 9] with the replicas' particles in replica order, boxes [R, 9]."""
+        total = sum(self.sizes)
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(total, 3)
+        rot = np.ascontiguousarray(rot, dtype=np.float64).reshape(total, 9)
+        boxes = np.ascontiguousarray(boxes, dtype=np.float64).reshape(self.R, 9)
+        self._check(self.lib.rp_batch_upload_states(self.h, dptr(pos), dptr(rot), dptr(boxes)))
+
+    def states(self, out=None):
+        """Every replica's state at once (rp_batch_download_states), into ``out`` =
+        (pos, rot, boxes) when given (e.g. pinned buffers)."""
+        total = sum(self.sizes)
+        if out is None:
+            out = (np.zeros((total, 3)), np.zeros((total, 9)), np.zeros((self.R, 9)))
+        pos, rot, boxes = out
+        for a, shape in ((pos, (total, 3)), (rot, (total, 9)), (boxes, (self.R, 9))):
+            if a.dtype != np.float64 or not a.flags.c_contiguous or a.size != shape[0] * shape[1]:
+                raise ValueError("out arrays must be C-contiguous float64 of the batch's sizes")
+        self._check(self.lib.rp_batch_download_states(self.h, dptr(pos), dptr(rot), dptr(boxes)))
+        return pos.reshape(total, 3), rot.reshape(total, 9), boxes.reshape(self.R, 9)
+
+    def set_timing(self, on: bool = True):
+        self._check(self.lib.rp_batch_set_timing(self.h, 1 if on else 0))
+
+    def timing(self):
+        """({group: (ms, groups)}, kernel launches of the batch and its replicas)."""
+        ng = len(_lib.KERNEL_GROUPS)
+        ms = (C.c_double * ng)()
+        groups = (C.c_uint64 * ng)()
+        launches = C.c_uint64()
+        self._check(self.lib.rp_batch_get_timing(self.h, ms, groups, C.byref(launches)))
+        return {name: (float(ms[k]), int(groups[k])) for k, name in enumerate(_lib.KERNEL_GROUPS)}, int(launches.value)
+
 
 def replica_seed(seed: int, r: int) -> int:
     """The sweep seed replica r of a batch uses (rp_batch_sweep)."""

@@ -97,3 +97,47 @@ def test_batch_replica_seeds(engine):
     from rampack_gb300 import packing
     assert packing.replica_seed(7, 0) == 7
     assert packing.replica_seed(7, 2) == (7 + 2 * 0x9E3779B97F4A7C15) % (1 << 64)
+
+
+def test_batch_upload_all_and_states(oracle, engine):
+    # every replica's state through one batched upload (rp_batch_upload_states) after some
+    # oracle cycles, read back at once (rp_batch_download_states), then sweeps replayed
+    from rampack_gb300.packing import BatchPacking, EngineError
+    cfgs = [f() for f in SETS["spherocylinders"]]
+    kind, prm = cfgs[0][0], cfgs[0][1]
+    cpus = [po.CpuPacking("oracle", c[0], c[1], c[2], c[3], c[4], threads=1) for c in cfgs]
+    for k, cpu in enumerate(cpus):
+        po.run_cycles(cpu, 2, seed=40 + k, translation_step=0.2, rotation_step=0.2, box_kind=1, box_step=0.003,
+                      pressure=2.0, temperature=1.0)
+    st = [cpu.state() for cpu in cpus]
+    pos = np.concatenate([s[0] for s in st])
+    rot = np.concatenate([s[1] for s in st])
+    boxes = np.stack([s[2] for s in st])
+    with BatchPacking(kind, prm, [c[2:] for c in cfgs]) as b:
+        b.upload_all(pos, rot, boxes)
+        gp, gr, gb = b.states()
+        assert np.array_equal(gp, pos) and np.array_equal(gr, rot) and np.array_equal(gb, boxes)
+        for k in range(b.R):
+            assert b.count_total_overlaps(k) == 0
+        for cycle in range(2):
+            b.sweep(0.2, 0.2, seed=17, counter=cycle, log=True)
+            for k, cpu in enumerate(cpus):
+                moves, codes = b.sweep_log(k)
+                _, _, bounds = b.grid(k)
+                want, _ = cpu.replay(moves, bounds)
+                assert np.array_equal(codes, want)
+        gp, gr, gb = b.states()
+        off = 0
+        for k, cpu in enumerate(cpus):
+            cp, cr, cb = cpu.state()
+            n = len(cp)
+            assert np.array_equal(gp[off:off + n], cp) and np.array_equal(gr[off:off + n], cr)
+            assert np.array_equal(gb[k], cb)
+            off += n
+        # a particle outside its box is refused (the rebuild clamps its cell and sets a status)
+        bad = pos.copy()
+        bad[sum(b.sizes[:2]) + 3] += boxes[2].reshape(3, 3)[:, 0] * 1.5
+        with pytest.raises(EngineError, match="outside"):
+            b.upload_all(bad, rot, boxes)
+        b.upload_all(pos, rot, boxes)
+        assert b.count_total_overlaps(1) == 0
