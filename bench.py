@@ -56,6 +56,9 @@ def parse():
                     help="replicas-64: fixed launch shape 'cell_factor,warps_per_block' instead of autotuning")
     ap.add_argument("--ordering", action="store_true",
                     help="compare the plain scan with centre-distance and learned partner ordering")
+    ap.add_argument("--io", action="store_true",
+                    help="snapshot files of the workload: RAMSNAP store / restore time and the cost of recording "
+                         "a RAMTRJ snapshot every cycle while sweeping")
     return ap.parse_args()
 
 
@@ -712,10 +715,83 @@ def main_replicas(args):
     return 0
 
 
+def main_io(args):
+    """Snapshot files of the workload's packing: RAMSNAP store (device state -> text file) and
+    restore (file -> device) wall time, and the sweep rate with a RAMTRJ snapshot recorded
+    every cycle (asynchronous: device-side copy, side-stream download, host writer thread)
+    against the same cycles without recording."""
+    import tempfile
+    import torch
+    from rampack_gb300 import build as rb
+    rb.build()
+    from rampack_gb300.packing import GpuPacking
+    from rampack_gb300.snapshots import RamtrjRecorder
+    kind, prm, pos, rot, box = workload(args)
+    n = len(pos)
+    g = GpuPacking(kind, prm, pos, rot, box)
+    t, r = (0.2, 0.2)
+    k = 0
+    for _ in range(max(3, args.warmup)):
+        g.sweep(t, r, seed=args.seed, counter=k, stats=False)
+        k += 1
+    torch.cuda.synchronize()
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        f = os.path.join(d, "s.ramsnap")
+        t0 = time.perf_counter()
+        g.store(f, {"cycles": str(k)})
+        out["store_s"] = time.perf_counter() - t0
+        out["ramsnap_mb"] = os.path.getsize(f) / 1e6
+        t0 = time.perf_counter()
+        g.restore(f)
+        torch.cuda.synchronize()
+        out["restore_s"] = time.perf_counter() - t0
+        os.remove(f)
+        steps = max(4, args.steps)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            g.sweep(t, r, seed=args.seed, counter=k, stats=False)
+            k += 1
+        torch.cuda.synchronize()
+        plain = (time.perf_counter() - t0) / steps
+        rec_rate = {}
+        for every in (1, 10):
+            tf = os.path.join(d, f"t{every}.ramtrj")
+            cycles = steps * every
+            with RamtrjRecorder(tf, n, every) as rec:
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                for c in range(1, cycles + 1):
+                    g.sweep(t, r, seed=args.seed, counter=k, stats=False)
+                    k += 1
+                    if c % every == 0:
+                        rec.record(g, c)
+                torch.cuda.synchronize()
+                rec.flush()
+                rec_rate[every] = 2 * n * cycles / (time.perf_counter() - t0)
+            os.remove(tf)
+        out["ramtrj_mb_per_snapshot"] = (9 * 8 + n * 48) / 1e6
+    g.close()
+    moves = 2 * n
+    print(json.dumps({
+        "metric": f"snapshot files, {args.workload}", "unit": "s / moves/s", "n": n,
+        "ramsnap": {"store_s": out["store_s"], "restore_s": out["restore_s"], "mb": out["ramsnap_mb"],
+                    "store_mb_per_s": out["ramsnap_mb"] / out["store_s"]},
+        "ramtrj": {"moves_per_s_plain": moves / plain, "moves_per_s_recording_every_cycle": rec_rate[1],
+                   "moves_per_s_recording_every_10_cycles": rec_rate[10],
+                   "mb_per_snapshot": out["ramtrj_mb_per_snapshot"], "snapshots": steps,
+                   "note": "host wall clock incl. the final flush; files in the default temporary directory"},
+    }))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return main_reference(args)
+    if args.io:
+        return main_io(args)
     if args.ordering:
         return main_ordering(args)
     if args.workload == "replicas-64":

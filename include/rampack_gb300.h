@@ -33,6 +33,8 @@ extern "C" {
 #define RP_ERR_UNSUPPORTED (-5)  /* a configuration this engine does not handle */
 #define RP_ERR_DEVICE (-6)       /* a device-side check failed (status word set by a kernel) */
 #define RP_ERR_CAPACITY (-7)     /* a per-cell capacity was exceeded */
+#define RP_ERR_FORMAT (-8)       /* a broken file: the reference throws RamsnapException / RamtrjException */
+#define RP_ERR_IO (-9)           /* a file could not be opened, read or written */
 
 #define RP_SHAPE_SPHERE 0
 #define RP_SHAPE_SPHEROCYLINDER 1
@@ -388,6 +390,52 @@ int rp_batch_get_timing(void *batch, double *ms, uint64_t *groups, uint64_t *lau
  * (from several host threads or streams) race and must be serialised by the caller. */
 int rp_count_overlaps_static(const rp_shape_desc *shape, int64_t n, const double *d_pos, const double *d_rot,
                              const double *box9, int early_exit, void *stream, int64_t *out_count);
+
+/* ---- snapshot and trajectory files (RAMSNAP text, RAMTRJ binary) ------------------
+ *
+ * Byte for byte the reference's formats.  Errors of these calls are described by
+ * rp_io_last_error() (per host thread). */
+const char *rp_io_last_error(void);
+
+/* Packing::store → RamsnapWriter::write (core/Packing.cpp:956-959,
+ * core/io/RamsnapWriter.cpp:8-48): aux entries (keys without whitespace; written in key
+ * order, a repeated key keeps its last value), the box, then one line per shape.  From the
+ * handle's device state (downloaded through a consistent device-side snapshot), or from
+ * host arrays. */
+int rp_ramsnap_write(void *handle, const char *path, int32_t naux, const char *const *keys,
+                     const char *const *values);
+int rp_ramsnap_write_host(const char *path, int64_t n, const double *pos, const double *rot, const double *box9,
+                          int32_t naux, const char *const *keys, const char *const *values);
+
+/* Packing::restore → RamsnapReader::read (core/Packing.cpp:961-964,
+ * core/io/RamsnapReader.cpp:16-96): parses a file into an opaque snapshot (old-format
+ * three-number boxes are the sides of a cuboid); the state then goes to rp_upload_state.
+ * Aux strings stay valid until rp_ramsnap_free. */
+int rp_ramsnap_load(const char *path, void **snap);
+int rp_ramsnap_info(void *snap, int64_t *n, int32_t *naux);
+int rp_ramsnap_get(void *snap, double *pos, double *rot, double *box9);
+int rp_ramsnap_aux(void *snap, int32_t index, const char **key, const char **value);
+int rp_ramsnap_free(void *snap);
+
+/* RamtrjRecorder (core/io/RamtrjRecorder.cpp:9-67): a trajectory of `num_particles`
+ * particles, one snapshot every `cycle_step` cycles; `append` continues an existing file
+ * whose header matches.  rp_ramtrj_record takes the handle's state in order with its
+ * moves and returns; the download, the Euler-angle conversion and the write run while the
+ * handle goes on (one snapshot in flight; the next record, flush or close waits for it).
+ * `cycle` must be (recorded snapshots + 1) · cycle_step.  Close rewrites the header. */
+int rp_ramtrj_open(const char *path, int64_t num_particles, int64_t cycle_step, int append, void **rec);
+int rp_ramtrj_record(void *rec, void *handle, int64_t cycle);
+int rp_ramtrj_record_host(void *rec, const double *pos, const double *rot, const double *box9, int64_t cycle);
+int rp_ramtrj_flush(void *rec);
+int rp_ramtrj_snapshots(void *rec, int64_t *count);
+int rp_ramtrj_close(void *rec);
+
+/* RamtrjPlayer (core/io/RamtrjPlayer.cpp:11-86): the header (version = 256·major + minor)
+ * of a well-formed file, and snapshot `snapshot` (from 0; the reference's cycle
+ * (snapshot + 1) · cycle_step) with orientations rebuilt from the Euler angles. */
+int rp_ramtrj_info(const char *path, int64_t *num_particles, int64_t *snapshots, int64_t *cycle_step,
+                   int32_t *version);
+int rp_ramtrj_read(const char *path, int64_t snapshot, double *pos, double *rot, double *box9);
 
 #ifdef __cplusplus
 }

@@ -306,3 +306,78 @@ def banana_centres(arc_radius: float, arc_angle: float, n: int, sphere_radius: f
     out = np.zeros(4 * n)
     k = lib.ref_banana_centres(arc_radius, arc_angle, n, sphere_radius, _dp(out))
     return out[:4 * k].reshape(k, 4)
+
+
+# ---- the reference's own snapshot and trajectory writers / readers (fixture generation) ----
+
+def _errbuf():
+    return C.create_string_buffer(512)
+
+
+def ref_ramsnap_write(path: str, kind: int, params, pos, rot, box, aux=None) -> None:
+    """Packing::store of a reference packing built from the state."""
+    lib, _ = _lib("reference")
+    pk = CpuPacking("reference", kind, params, pos, rot, box, threads=1)
+    items = list((aux or {}).items())
+    keys = (C.c_char_p * max(1, len(items)))(*[k.encode() for k, _ in items])
+    vals = (C.c_char_p * max(1, len(items)))(*[v.encode() for _, v in items])
+    err = _errbuf()
+    lib.ref_ramsnap_write.restype = C.c_int
+    lib.ref_ramsnap_write.argtypes = [_P, C.c_char_p, C.c_int, _P, _P, C.c_char_p, C.c_int]
+    rc = lib.ref_ramsnap_write(pk.h, path.encode(), len(items), C.cast(keys, _P), C.cast(vals, _P), err, 512)
+    pk.close()
+    if rc != 0:
+        raise ValueError(err.value.decode())
+
+
+def ref_ramsnap_read(path: str, kind: int, params, cap: int = 1 << 20):
+    """Packing::restore: (pos, rot, box, aux) or ValueError with the reference's message."""
+    lib, _ = _lib("reference")
+    prm = np.ascontiguousarray(params, dtype=np.float64)
+    pos, rot, box = np.zeros((cap, 3)), np.zeros((cap, 9)), np.zeros(9)
+    aux, err = C.create_string_buffer(1 << 16), _errbuf()
+    lib.ref_ramsnap_read.restype = C.c_int64
+    lib.ref_ramsnap_read.argtypes = [C.c_char_p, C.c_int, _D, C.c_int, _D, _D, _D, C.c_int64, C.c_char_p, C.c_int,
+                                     C.c_char_p, C.c_int]
+    n = lib.ref_ramsnap_read(path.encode(), kind, _dp(prm), len(prm), _dp(pos), _dp(rot), _dp(box), cap, aux,
+                             1 << 16, err, 512)
+    if n < 0:
+        raise ValueError(err.value.decode())
+    entries = {}
+    for ln in aux.value.decode().split("\n"):
+        if ln:
+            k, v = ln.split("\t", 1)
+            entries[k] = v
+    return pos[:n].copy(), rot[:n].copy(), box, entries
+
+
+def ref_ramtrj_write(path: str, kind: int, params, states, cycle_step: int) -> None:
+    """RamtrjRecorder over `states` = [(pos, rot, box), ...]."""
+    lib, _ = _lib("reference")
+    prm = np.ascontiguousarray(params, dtype=np.float64)
+    pos = np.ascontiguousarray(np.concatenate([np.asarray(s[0]).reshape(-1, 3) for s in states]))
+    rot = np.ascontiguousarray(np.concatenate([np.asarray(s[1]).reshape(-1, 9) for s in states]))
+    boxes = np.ascontiguousarray(np.stack([np.asarray(s[2]).reshape(9) for s in states]))
+    n = len(np.asarray(states[0][0]).reshape(-1, 3))
+    err = _errbuf()
+    lib.ref_ramtrj_write.restype = C.c_int
+    lib.ref_ramtrj_write.argtypes = [C.c_char_p, C.c_int, _D, C.c_int, C.c_int64, C.c_int64, C.c_int64, _D, _D, _D,
+                                     C.c_char_p, C.c_int]
+    rc = lib.ref_ramtrj_write(path.encode(), kind, _dp(prm), len(prm), n, len(states), cycle_step, _dp(pos),
+                              _dp(rot), _dp(boxes), err, 512)
+    if rc != 0:
+        raise ValueError(err.value.decode())
+
+
+def ref_ramtrj_read(path: str, kind: int, params, index: int, n: int):
+    """RamtrjPlayer::jumpToSnapshot: (pos, rot, box) of snapshot `index` (from 0)."""
+    lib, _ = _lib("reference")
+    prm = np.ascontiguousarray(params, dtype=np.float64)
+    pos, rot, box = np.zeros((n, 3)), np.zeros((n, 9)), np.zeros(9)
+    err = _errbuf()
+    lib.ref_ramtrj_read.restype = C.c_int
+    lib.ref_ramtrj_read.argtypes = [C.c_char_p, C.c_int, _D, C.c_int, C.c_int64, _D, _D, _D, C.c_char_p, C.c_int]
+    rc = lib.ref_ramtrj_read(path.encode(), kind, _dp(prm), len(prm), index, _dp(pos), _dp(rot), _dp(box), err, 512)
+    if rc != 0:
+        raise ValueError(err.value.decode())
+    return pos, rot, box

@@ -7,6 +7,8 @@
 // tests/golden/.  Mirrors the rpo_* entry points of rpo_capi.cpp one for one.
 #include <cstdint>
 #include <cstring>
+#include <fstream>
+#include <map>
 #include <memory>
 #include <random>
 #include <sstream>
@@ -17,6 +19,8 @@
 #include "core/FreeBoundaryConditions.h"
 #include "core/Simulation.h"
 #include "core/ObservablesCollector.h"
+#include "core/io/RamtrjPlayer.h"
+#include "core/io/RamtrjRecorder.h"
 #include "core/move_samplers/RotationSampler.h"
 #include "core/move_samplers/TranslationSampler.h"
 #include "core/shapes/PolysphereTraits.h"
@@ -386,6 +390,113 @@ int ref_sim_run(void *hp, const ref_sim_params *p, int64_t cycles, ref_sim_stats
         return -1;
     }
     return 0;
+}
+
+// ---- snapshot and trajectory files through the reference's own readers and writers ----
+
+// Packing::store (core/Packing.cpp:956-959): RAMSNAP of the handle's packing; 0, or -1 with
+// the exception text in err
+int ref_ramsnap_write(void *hp, const char *path, int naux, const char *const *keys, const char *const *values,
+                      char *err, int errcap) {
+    auto *h = static_cast<Handle *>(hp);
+    std::map<std::string, std::string> aux;
+    for (int i = 0; i < naux; i++) aux[keys[i]] = values[i];
+    try {
+        std::ofstream out(path);
+        h->pk->store(out, aux);
+        return out ? 0 : -1;
+    } catch (const std::exception &e) {
+        std::snprintf(err, errcap, "%s", e.what());
+        return -1;
+    }
+}
+
+// Packing::restore (core/Packing.cpp:961-964) into an empty packing of a shape kind: the
+// number of shapes (at most cap are returned), or -1 with the exception text in err; aux
+// entries as "key\tvalue\n" lines in auxbuf
+int64_t ref_ramsnap_read(const char *path, int kind, const double *prm, int np, double *pos, double *rot,
+                         double *box9, int64_t cap, char *auxbuf, int auxcap, char *err, int errcap) {
+    auto traits = make_traits(kind, prm, np);
+    if (!traits) return -1;
+    try {
+        Packing pk(std::make_unique<PeriodicBoundaryConditions>(), 1, 1);
+        std::ifstream in(path);
+        auto aux = pk.restore(in, traits->getInteraction());
+        std::string a;
+        for (auto &kv : aux) a += kv.first + "\t" + kv.second + "\n";
+        std::snprintf(auxbuf, auxcap, "%s", a.c_str());
+        for (std::size_t i = 0; i < pk.size() && static_cast<int64_t>(i) < cap; i++) {
+            for (int k = 0; k < 3; k++) pos[3 * i + k] = pk[i].getPosition()[k];
+            store_m(pk[i].getOrientation(), rot + 9 * i);
+        }
+        store_m(pk.getBox().getDimensions(), box9);
+        return static_cast<int64_t>(pk.size());
+    } catch (const std::exception &e) {
+        std::snprintf(err, errcap, "%s", e.what());
+        return -1;
+    }
+}
+
+// RamtrjRecorder (core/io/RamtrjRecorder.cpp): a new trajectory of `snapshots` states
+// (pos [snapshots][n][3], rot [snapshots][n][9], boxes [snapshots][9]) of a shape kind
+int ref_ramtrj_write(const char *path, int kind, const double *prm, int np, int64_t n, int64_t snapshots,
+                     int64_t cycle_step, const double *pos, const double *rot, const double *boxes, char *err,
+                     int errcap) {
+    auto traits = make_traits(kind, prm, np);
+    if (!traits) return -1;
+    try {
+        auto stream = std::make_unique<std::fstream>(path, std::ios::in | std::ios::out | std::ios::binary |
+                                                           std::ios::trunc);
+        RamtrjRecorder rec(std::move(stream), static_cast<std::size_t>(n), static_cast<std::size_t>(cycle_step),
+                           false);
+        for (int64_t s = 0; s < snapshots; s++) {
+            std::vector<Shape> shapes;
+            for (int64_t i = 0; i < n; i++) {
+                const double *p = pos + 3 * (s * n + i);
+                shapes.emplace_back(Vector<3>{p[0], p[1], p[2]}, load_m(rot + 9 * (s * n + i)));
+            }
+            Packing pk(TriclinicBox(load_m(boxes + 9 * s)), std::move(shapes),
+                       std::make_unique<PeriodicBoundaryConditions>(), traits->getInteraction(), 1, 1);
+            rec.recordSnapshot(pk, static_cast<std::size_t>((s + 1) * cycle_step));
+        }
+        rec.close();
+        return 0;
+    } catch (const std::exception &e) {
+        std::snprintf(err, errcap, "%s", e.what());
+        return -1;
+    }
+}
+
+// RamtrjPlayer::jumpToSnapshot (core/io/RamtrjPlayer.cpp:71-86): snapshot `index` (from 0)
+int ref_ramtrj_read(const char *path, int kind, const double *prm, int np, int64_t index, double *pos, double *rot,
+                    double *box9, char *err, int errcap) {
+    auto traits = make_traits(kind, prm, np);
+    if (!traits) return -1;
+    try {
+        auto in = std::make_unique<std::ifstream>(path, std::ios::in | std::ios::binary);
+        RamtrjPlayer player(std::move(in));
+        Packing pk(std::make_unique<PeriodicBoundaryConditions>(), 1, 1);
+        // an empty packing of the right size for the player to reset
+        std::ifstream probe(path, std::ios::binary);
+        char magic[7];
+        unsigned char ver[2];
+        std::size_t hdr[3];
+        probe.read(magic, 7);
+        probe.read(reinterpret_cast<char *>(ver), 2);
+        probe.read(reinterpret_cast<char *>(hdr), sizeof(hdr));
+        std::vector<Shape> shapes(hdr[0]);
+        pk.reset(std::move(shapes), TriclinicBox(1.0), traits->getInteraction());
+        player.jumpToSnapshot(pk, traits->getInteraction(), static_cast<std::size_t>((index + 1) * hdr[2]));
+        for (std::size_t i = 0; i < pk.size(); i++) {
+            for (int k = 0; k < 3; k++) pos[3 * i + k] = pk[i].getPosition()[k];
+            store_m(pk[i].getOrientation(), rot + 9 * i);
+        }
+        store_m(pk.getBox().getDimensions(), box9);
+        return 0;
+    } catch (const std::exception &e) {
+        std::snprintf(err, errcap, "%s", e.what());
+        return -1;
+    }
 }
 
 }  // extern "C"

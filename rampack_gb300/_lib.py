@@ -17,7 +17,7 @@ LIB_PATH = os.path.join(HERE, "librampack_gb300.so")
 RP_OK = 0
 ERRORS = {
     -1: "RP_ERR_ARG", -2: "RP_ERR_CUDA", -3: "RP_ERR_STATE", -4: "RP_ERR_OVERLAP",
-    -5: "RP_ERR_UNSUPPORTED", -6: "RP_ERR_DEVICE", -7: "RP_ERR_CAPACITY",
+    -5: "RP_ERR_UNSUPPORTED", -6: "RP_ERR_DEVICE", -7: "RP_ERR_CAPACITY", -8: "RP_ERR_FORMAT", -9: "RP_ERR_IO",
 }
 SHAPE_SPHERE, SHAPE_SPHEROCYLINDER, SHAPE_POLYSPHERE = 0, 1, 2
 MAX_CENTRES = 8
@@ -112,6 +112,24 @@ SIGNATURES = {
     "rp_batch_download_states": (C.c_int, [_P, _D, _D, _D]),
     "rp_batch_set_timing": (C.c_int, [_P, C.c_int]),
     "rp_batch_get_timing": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "rp_io_last_error": (C.c_char_p, []),
+    "rp_ramsnap_write": (C.c_int, [_P, C.c_char_p, C.c_int32, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p)]),
+    "rp_ramsnap_write_host": (C.c_int, [C.c_char_p, C.c_int64, _D, _D, _D, C.c_int32, C.POINTER(C.c_char_p),
+                                        C.POINTER(C.c_char_p)]),
+    "rp_ramsnap_load": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
+    "rp_ramsnap_info": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int32)]),
+    "rp_ramsnap_get": (C.c_int, [_P, _D, _D, _D]),
+    "rp_ramsnap_aux": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p)]),
+    "rp_ramsnap_free": (C.c_int, [_P]),
+    "rp_ramtrj_open": (C.c_int, [C.c_char_p, C.c_int64, C.c_int64, C.c_int, C.POINTER(C.c_void_p)]),
+    "rp_ramtrj_record": (C.c_int, [_P, _P, C.c_int64]),
+    "rp_ramtrj_record_host": (C.c_int, [_P, _D, _D, _D, C.c_int64]),
+    "rp_ramtrj_flush": (C.c_int, [_P]),
+    "rp_ramtrj_snapshots": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "rp_ramtrj_close": (C.c_int, [_P]),
+    "rp_ramtrj_info": (C.c_int, [C.c_char_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                 C.POINTER(C.c_int32)]),
+    "rp_ramtrj_read": (C.c_int, [C.c_char_p, C.c_int64, _D, _D, _D]),
 }
 KERNEL_GROUPS = ["sweep", "rebuild", "count", "rescale", "overflow", "order", "mlp", "fix"]
 MLP_NPARAM = 5313

@@ -194,6 +194,9 @@ struct Handle {
     double cthr_host[MAX_CEN * MAX_CEN]{};
     double ref_range = 0;
     double *cen64 = nullptr;
+    // consistent copy of the FP64 state for asynchronous snapshot downloads
+    double *snap64 = nullptr;          // [n][3] positions then [n][9] orientations
+    cudaEvent_t snap_free = nullptr;   // recorded when the last download out of snap64 ended
     double *abs64[2] = {nullptr, nullptr};
     double *cthr64 = nullptr;
     double *cbody_dev = nullptr;    // body-frame centres on the device
@@ -981,6 +984,11 @@ int rp_destroy(void *handle) {
     if (!h) return RP_ERR_ARG;
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->snap_free) {
+        cudaEventSynchronize(h->snap_free);
+        cudaEventDestroy(h->snap_free);
+    }
+    cudaFree(h->snap64);
     for (int i = 0; i < 2; i++) {
         cudaFree(h->pos64[i]);
         cudaFree(h->trans[i]);
@@ -2450,3 +2458,58 @@ int rp_batch_revert_scaling(void *batch, const uint8_t *mask) {
 }
 
 }  // extern "C"
+
+namespace rp {
+
+// The handle's FP64 state as a consistent snapshot: positions and orientations are copied
+// on the device (on the handle's stream, in order with its moves) into a snapshot buffer,
+// then downloaded on `side` into host memory (`pos` [n][3], `rot` [n][9], pinned for an
+// asynchronous copy) while later work of the handle goes on; `done` is recorded on `side`
+// after the download.  The box and the particle count are returned at once.
+int state_snapshot(void *handle, double *pos, double *rot, double *box9, int64_t *n, cudaStream_t side,
+                   cudaEvent_t done, std::string &err) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h) {
+        err = "null handle";
+        return RP_ERR_ARG;
+    }
+    if (!h->has_state) {
+        err = "no state uploaded";
+        return RP_ERR_STATE;
+    }
+    auto cuda = [&](cudaError_t e, const char *what) {
+        if (e == cudaSuccess) return false;
+        err = std::string(what) + ": " + cudaGetErrorString(e);
+        return true;
+    };
+    if (cuda(cudaSetDevice(h->device), "cudaSetDevice")) return RP_ERR_CUDA;
+    if (!h->snap64 && cuda(cudaMalloc(&h->snap64, sizeof(double) * 12 * h->n), "cudaMalloc")) return RP_ERR_CUDA;
+    if (!h->snap_free && cuda(cudaEventCreateWithFlags(&h->snap_free, cudaEventDisableTiming), "cudaEventCreate"))
+        return RP_ERR_CUDA;
+    double *sp = h->snap64, *sr = h->snap64 + 3 * h->n;
+    // the previous download out of the snapshot buffer has ended before it is overwritten
+    if (cuda(cudaStreamWaitEvent(h->stream, h->snap_free, 0), "cudaStreamWaitEvent")) return RP_ERR_CUDA;
+    if (cuda(cudaMemcpyAsync(sp, h->pos64[h->pcur], sizeof(double) * 3 * h->n, cudaMemcpyDeviceToDevice, h->stream),
+             "cudaMemcpyAsync") ||
+        cuda(cudaMemcpyAsync(sr, h->rot64, sizeof(double) * 9 * h->n, cudaMemcpyDeviceToDevice, h->stream),
+             "cudaMemcpyAsync"))
+        return RP_ERR_CUDA;
+    cudaEvent_t copied = nullptr;
+    if (cuda(cudaEventCreateWithFlags(&copied, cudaEventDisableTiming), "cudaEventCreate")) return RP_ERR_CUDA;
+    bool bad = cuda(cudaEventRecord(copied, h->stream), "cudaEventRecord") ||
+               cuda(cudaStreamWaitEvent(side, copied, 0), "cudaStreamWaitEvent") ||
+               cuda(cudaMemcpyAsync(pos, sp, sizeof(double) * 3 * h->n, cudaMemcpyDeviceToHost, side), "cudaMemcpyAsync") ||
+               cuda(cudaMemcpyAsync(rot, sr, sizeof(double) * 9 * h->n, cudaMemcpyDeviceToHost, side), "cudaMemcpyAsync") ||
+               cuda(cudaEventRecord(h->snap_free, side), "cudaEventRecord") ||
+               cuda(cudaEventRecord(done, side), "cudaEventRecord");
+    cudaEventDestroy(copied);  // released once the recorded work completes
+    if (bad) return RP_ERR_CUDA;
+    std::memcpy(box9, h->box, sizeof(h->box));
+    *n = h->n;
+    return RP_OK;
+}
+
+// Particle count of a handle (0 for a null handle).
+int64_t handle_size(void *handle) { return handle ? static_cast<Handle *>(handle)->n : 0; }
+
+}  // namespace rp

@@ -18,6 +18,7 @@
 #include <cmath>
 #include <cstdint>
 #include <limits>
+#include <map>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -120,6 +121,47 @@ public:
         return static_cast<std::size_t>(rejected);
     }
 
+    // Packing::store / Packing::restore (core/Packing.cpp:956-964) with a file path: the
+    // RAMSNAP file of the device state, byte for byte the reference's RamsnapWriter output;
+    // restore loads a file of this packing's size and returns its aux entries.
+    void store(const std::string &path, const std::map<std::string, std::string> &auxInfo = {}) const {
+        std::vector<const char *> keys, values;
+        for (auto &kv : auxInfo) {
+            keys.push_back(kv.first.c_str());
+            values.push_back(kv.second.c_str());
+        }
+        checkIo(rp_ramsnap_write(h_, path.c_str(), static_cast<int32_t>(keys.size()), keys.data(), values.data()),
+                "rp_ramsnap_write");
+    }
+    std::map<std::string, std::string> restore(const std::string &path) {
+        void *snap = nullptr;
+        checkIo(rp_ramsnap_load(path.c_str(), &snap), "rp_ramsnap_load");
+        int64_t n = 0;
+        int32_t naux = 0;
+        rp_ramsnap_info(snap, &n, &naux);
+        if (static_cast<std::size_t>(n) != n_) {
+            rp_ramsnap_free(snap);
+            throw std::runtime_error("restore: the file holds " + std::to_string(n) + " shapes, the packing " +
+                                     std::to_string(n_));
+        }
+        std::vector<double> pos(3 * n_), rot(9 * n_);
+        Mat3 box{};
+        rp_ramsnap_get(snap, pos.data(), rot.data(), box.data());
+        std::map<std::string, std::string> aux;
+        for (int32_t i = 0; i < naux; i++) {
+            const char *k = nullptr, *v = nullptr;
+            rp_ramsnap_aux(snap, i, &k, &v);
+            aux[k] = v;
+        }
+        rp_ramsnap_free(snap);
+        check(rp_upload_state(h_, pos.data(), rot.data(), box.data()), "rp_upload_state");
+        box_ = box;
+        return aux;
+    }
+
+    // The handle, for rp_* calls this class does not wrap (e.g. rp_ramtrj_record).
+    void *handle() const { return h_; }
+
     // The batched move entry: one device sweep (2N moves for translation + rotation).
     rp_sweep_stats performMoves(double translationStep, double rotationStep, uint64_t seed, uint64_t cycle) {
         rp_sweep_params p{};
@@ -142,6 +184,9 @@ private:
 
     void check(int rc, const char *what) const {
         if (rc != RP_OK) throw std::runtime_error(std::string(what) + ": " + rp_last_error(h_));
+    }
+    static void checkIo(int rc, const char *what) {
+        if (rc != RP_OK) throw std::runtime_error(std::string(what) + ": " + rp_io_last_error());
     }
 
     int cellOf(std::size_t idx) const {
@@ -175,6 +220,34 @@ private:
         uint8_t code = 0;
         check(rp_run_moves(h_, &m, 1, &code), "rp_run_moves");
     }
+};
+
+// RamtrjRecorder (core/io/RamtrjRecorder.cpp): a RAMTRJ trajectory; recordSnapshot takes a
+// GpuPacking's state in order with its moves and returns while the file is written.
+class RamtrjRecorder {
+public:
+    RamtrjRecorder(const std::string &path, std::size_t numParticles, std::size_t cycleStep, bool append = false) {
+        if (rp_ramtrj_open(path.c_str(), static_cast<int64_t>(numParticles), static_cast<int64_t>(cycleStep),
+                           append ? 1 : 0, &r_) != RP_OK)
+            throw std::runtime_error(std::string("rp_ramtrj_open: ") + rp_io_last_error());
+    }
+    RamtrjRecorder(const RamtrjRecorder &) = delete;
+    RamtrjRecorder &operator=(const RamtrjRecorder &) = delete;
+    ~RamtrjRecorder() {
+        if (r_) rp_ramtrj_close(r_);
+    }
+    void recordSnapshot(const GpuPacking &packing, std::size_t cycle) {
+        if (rp_ramtrj_record(r_, packing.handle(), static_cast<int64_t>(cycle)) != RP_OK)
+            throw std::runtime_error(std::string("rp_ramtrj_record: ") + rp_io_last_error());
+    }
+    void close() {
+        void *r = r_;
+        r_ = nullptr;
+        if (r && rp_ramtrj_close(r) != RP_OK) throw std::runtime_error(std::string("rp_ramtrj_close: ") + rp_io_last_error());
+    }
+
+private:
+    void *r_ = nullptr;
 };
 
 }  // namespace rampack_gb300

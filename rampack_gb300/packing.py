@@ -121,6 +121,20 @@ class GpuPacking:
         self._check(self.lib.rp_download_state(self.h, dptr(pos), dptr(rot), dptr(box)))
         return pos, rot, box
 
+    def store(self, path, aux=None) -> None:
+        """Packing::store (core/Packing.cpp:956-959): a RAMSNAP file of the device state."""
+        from .snapshots import _aux_arrays, _check, _path
+        n, keys, values = _aux_arrays(aux)
+        _check(self.lib, self.lib.rp_ramsnap_write(self.h, _path(path), n, keys, values))
+
+    def restore(self, path) -> dict:
+        """Packing::restore (core/Packing.cpp:961-964): loads a RAMSNAP file of this
+        packing's size onto the device; returns its aux entries."""
+        from .snapshots import read_ramsnap
+        pos, rot, box, aux = read_ramsnap(path)
+        self.upload(pos, rot, box)
+        return aux
+
     # ---- overlaps ----
     def count_total_overlaps(self, early_exit: bool = False) -> int:
         out = C.c_int64()

@@ -4,6 +4,7 @@
 #include <cmath>
 #include <limits>
 #include <cstdio>
+#include <string>
 #include <vector>
 
 #include "../../rampack_gb300/host/GpuPacking.hpp"
@@ -27,7 +28,7 @@ static std::vector<GpuPacking::Shape> three() {
     return s;
 }
 
-int main() {
+int main(int argc, char **argv) {
     const double inf = std::numeric_limits<double>::infinity();
     GpuPacking::Mat3 box{5, 0, 0, 0, 5, 0, 0, 0, 5};
     {
@@ -76,6 +77,29 @@ int main() {
         CHECK(st.moves == 2 * sc.size());
         CHECK(st.accepted > 0 && st.accepted < st.moves);
         CHECK(pk.countTotalOverlaps(true) == 0);
+        // Packing::store / restore through a RAMSNAP file, and a trajectory recorded while
+        // the packing keeps moving
+        const std::string dir = argc > 1 ? argv[1] : ".";
+        const std::vector<GpuPacking::Shape> before = pk.getShapes();
+        pk.store(dir + "/sc.ramsnap", {{"cycles", "1"}});
+        {
+            rampack_gb300::RamtrjRecorder rec(dir + "/sc.ramtrj", sc.size(), 1);
+            rec.recordSnapshot(pk, 1);
+            pk.performMoves(0.2, 0.2, 42, 1);
+            rec.recordSnapshot(pk, 2);
+            rec.close();
+        }
+        auto aux = pk.restore(dir + "/sc.ramsnap");
+        CHECK(aux.size() == 1 && aux["cycles"] == "1");
+        const std::vector<GpuPacking::Shape> after = pk.getShapes();
+        bool same = true;
+        for (std::size_t i = 0; i < sc.size(); i++)
+            for (int k = 0; k < 3; k++) same = same && after[i].position[k] == before[i].position[k];
+        CHECK(same);
+        int64_t np = 0, snaps = 0, step = 0;
+        int32_t ver = 0;
+        CHECK(rp_ramtrj_info((dir + "/sc.ramtrj").c_str(), &np, &snaps, &step, &ver) == RP_OK);
+        CHECK(np == static_cast<int64_t>(sc.size()) && snaps == 2 && step == 1 && ver == 0x101);
     }
     if (failures) return 1;
     std::printf("ok\n");

@@ -3,7 +3,8 @@
 Run in a checkout where the reference sources are present:
 
     make -C oracle ref            # compiles the reference's hot-path sources in place
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py        # every fixture
+    python tests/golden/make_golden.py io     # the snapshot / trajectory files only
 
 Every expected value below is produced by the reference library (oracle/_ref/librpref.so:
 rampack's Packing, NeighbourGrid, SpherocylinderTraits, samplers and Simulation compiled
@@ -226,9 +227,85 @@ def gen_proposals():
     print("proposals:", len(mv))
 
 
+# RAMSNAP inputs whose parse (or error) the reference fixes: old and new box formats,
+# number forms, aux entries, and broken files
+IO_CASES = {
+    "old_box": b"1\nk v\n10 11 12\n2\n1 2 3        1 0 0 0 1 0 0 0 1\n4 5 6 1 0 0 0 1 0 0 0 1\n",
+    "old_box_trailing": b"1\nk v\n10 11 12   \n1\n1 2 3 1 0 0 0 1 0 0 0 1\n",
+    "number_forms": b"1\nk v\n1e1 0 0 0 +10 0 0 0 10.\n1\n.5 +2.5e-1 3E0 1 0 0 0 1 0 0 0 1\n",
+    "aux_values": b"3\nb  two words \na x\nc\n\ny\n10 0 0 0 10 0 0 0 10\n1\n1 2 3 1 0 0 0 1 0 0 0 1\n",
+    "no_aux": b"0\n10 0 0 0 10 0 0 0 10\n1\n1 2 3        1 0 0 0 1 0 0 0 1\n",
+    "singular_box": b"1\nk v\n10 0 0 0 0 0 0 0 10\n1\n1 2 3 1 0 0 0 1 0 0 0 1\n",
+    "truncated": b"1\nk v\n10 0 0 0 10 0 0 0 10\n3\n1 2 3 1 0 0 0 1 0 0 0 1\n4 5 6 1 0 0\n",
+    "bad_dimensions": b"1\nk v\n10 x 0 0 10 0 0 0 10\n1\n1 2 3 1 0 0 0 1 0 0 0 1\n",
+    "eight_dimensions": b"1\nk v\n10 0 0 0 10 0 0 0\n1\n1 2 3 1 0 0 0 1 0 0 0 1\n",
+    "bad_size": b"1\nk v\n10 0 0 0 10 0 0 0 10\nx\n",
+    "bad_aux": b"2\nk v\n",
+    "empty": b"",
+    "infinity": b"1\nk v\n10 0 0 0 10 0 0 0 10\n1\ninf 2 3 1 0 0 0 1 0 0 0 1\n",
+    "overflow": b"1\nk v\n10 0 0 0 10 0 0 0 10\n1\n1e999 2 3 1 0 0 0 1 0 0 0 1\n",
+}
+
+
+def gen_io(rng):
+    """RAMSNAP and RAMTRJ files written by the reference's own writers, the reference's
+    reading of them, and its outcome (values or exception text) on edge-case inputs."""
+    import tempfile
+    import systems
+    kind, prm, pos, rot, box = systems.sc_l2()
+    sel = np.arange(0, len(pos), 25)  # 40 particles, enough to cover every number form
+    pos, rot = pos[sel], rot[sel]
+    box = box.copy()
+    box[1], box[2], box[5] = 0.125, -0.0625, 1e-17  # triclinic, one tiny entry
+    pos[0] = [1.0, 1.0, 1.0]
+    rot[0] = [1.0, 5e-324, 0.0, 1e-300, 1.0, 0.0, 0.0, 0.0, 1.0]  # denormals
+    pos[1] = [2.0, 1.0 / 3.0 + 1.0, 2.0 / 3.0 + 1.0]
+    rot[1] = [1.0, 0.0, -0.0, -0.0, 1.0, 0.0, 0.0, -0.0, 1.0]     # negative zeros
+    aux = {"cycles": "12000", "comment": "a value  with spaces", "a.key": "x", "zz": "trailing "}
+    d = tempfile.mkdtemp()
+    snap = os.path.join(HERE, "io_sc.ramsnap")
+    po.ref_ramsnap_write(snap, kind, prm, pos, rot, box, aux)
+    states = []
+    for k in range(3):
+        p = pos + rng.normal(scale=0.05, size=pos.shape)
+        r = rand_rot(rng, len(pos))
+        b = box * (1 + 0.01 * k)
+        states.append((p, r, b))
+    trj = os.path.join(HERE, "io_sc.ramtrj")
+    po.ref_ramtrj_write(trj, kind, prm, states, 50)
+    out = {"kind": kind, "params": prm, "pos": pos, "rot": rot, "box": box,
+           "aux_keys": np.array(list(aux.keys())), "aux_values": np.array(list(aux.values())),
+           "trj_pos": np.stack([s[0] for s in states]), "trj_rot": np.stack([s[1] for s in states]),
+           "trj_box": np.stack([s[2] for s in states]), "trj_cycle_step": 50}
+    # the reference's reading of its own files
+    rp, rr, rb, ra = po.ref_ramsnap_read(snap, kind, prm)
+    out.update(read_pos=rp, read_rot=rr, read_box=rb)
+    for k in range(3):
+        p, r, b = po.ref_ramtrj_read(trj, kind, prm, k, len(pos))
+        out.update({f"play{k}_pos": p, f"play{k}_rot": r, f"play{k}_box": b})
+    # edge cases
+    for name, data in IO_CASES.items():
+        f = os.path.join(d, name)
+        with open(f, "wb") as fh:
+            fh.write(data)
+        out[f"case_{name}_input"] = np.frombuffer(data, dtype=np.uint8)
+        try:
+            p, r, b, a = po.ref_ramsnap_read(f, po.SPHERE, [0.5])
+            out[f"case_{name}_pos"], out[f"case_{name}_rot"], out[f"case_{name}_box"] = p, r, b
+            out[f"case_{name}_aux"] = np.array([f"{k}\t{v}" for k, v in sorted(a.items())])
+            out[f"case_{name}_error"] = np.array("")
+        except ValueError as e:
+            out[f"case_{name}_error"] = np.array(str(e))
+    np.savez_compressed(os.path.join(HERE, "io.npz"), **out)
+    print("io: ramsnap", os.path.getsize(snap), "B, ramtrj", os.path.getsize(trj), "B,", len(IO_CASES), "cases")
+
+
 def main():
     if not po.reference_available():
         po.build(reference=True)
+    if sys.argv[1:] == ["io"]:
+        gen_io(np.random.default_rng(20261204))
+        return
     rng = np.random.default_rng(20241203)
     gen_pairs(rng)
     gen_geometry(rng)
@@ -241,6 +318,7 @@ def main():
             adjust_steps=True)
     gen_sim("sc_dd", W.spherocylinders((12, 12, 12), 0.35, 2.0, 0.5, aspect=(1, 1, 3)), 8, translation_step=0.2,
             rotation_step=0.2, box_kind=1, box_step=0.005, pressure=1.5, domains=(2, 2, 2), threads=8)
+    gen_io(np.random.default_rng(20261204))
 
 
 if __name__ == "__main__":

@@ -18,6 +18,6 @@ def test_gpupacking_known_answers(engine, tmp_path):
     libdir = os.path.dirname(engine.LIB_PATH)
     subprocess.run(["g++", "-std=c++17", "-O1", SRC, "-o", str(exe), f"-L{libdir}", "-lrampack_gb300",
                     f"-Wl,-rpath,{libdir}"], check=True)
-    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    out = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True, timeout=120)
     assert out.returncode == 0, out.stdout + out.stderr
     assert "ok" in out.stdout
