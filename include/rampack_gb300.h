@@ -111,6 +111,7 @@ typedef struct rp_sweep_stats {
     uint64_t translations;
     uint64_t rotations;
     uint64_t kernel_launches;     /* kernels this library launched (all calls since creation) */
+    uint64_t accepted_translations; /* accepted translations (accepted rotations: accepted minus these) */
 } rp_sweep_stats;
 
 /* Kernel groups timed by rp_get_timing. */
@@ -390,6 +391,64 @@ int rp_batch_get_timing(void *batch, double *ms, uint64_t *groups, uint64_t *lau
  * (from several host threads or streams) race and must be serialised by the caller. */
 int rp_count_overlaps_static(const rp_shape_desc *shape, int64_t n, const double *d_pos, const double *d_rot,
                              const double *box9, int early_exit, void *stream, int64_t *out_count);
+
+/* ---- the Monte Carlo cycle loop (Simulation for hard bodies) -----------------------
+ *
+ * Simulation::performCycle (core/Simulation.cpp:325-363) around a handle: one device sweep
+ * of translations and rotations at the current step sizes, then a box move proposed by
+ * the reference's TriclinicBoxScaler family from a std::mt19937 (seeded like the
+ * Simulation's first generator) and pre-checked on the host (Simulation::tryScaling,
+ * :493-531, incl. the overlap-counting branch); with `adjust_steps` the thermalisation's
+ * step-size adaptation (Simulation::evaluateCounters, :533-607: every 100·N moves of a
+ * sampler, or 100 box moves, the step grows by 1.1 above 20 % acceptance and shrinks below
+ * 10 %; translations stop at half the smallest box height, rotations at pi). */
+#define RP_SCALER_NONE 0
+#define RP_SCALER_DELTA_TRICLINIC 1  /* TriclinicDeltaScaler (core/volume_scalers/TriclinicDeltaScaler.cpp:7-25) */
+#define RP_SCALER_LOG 2              /* TriclinicAdapter + AnisotropicVolumeScaler + LogScalingFactorSampler */
+#define RP_SCALER_LINEAR 3           /* TriclinicAdapter + AnisotropicVolumeScaler + LinearScalingFactorSampler */
+#define RP_SCALER_DELTA_VOLUME 4     /* TriclinicAdapter + DeltaVolumeScaler */
+
+typedef struct rp_box_scaler_desc {
+    int32_t kind;            /* RP_SCALER_* */
+    int32_t scale_together;  /* delta triclinic: every entry moves (1) or one random side (0) */
+    int32_t num_groups;      /* log / linear: the scaling directions, 1-3 ... */
+    int32_t groups[3];       /* ... each a mask of axes scaled by one factor (1 x, 2 y, 4 z; 7 isotropic) */
+    int32_t independent;     /* one random direction per move (1) or the product over all (0) */
+    int32_t reserved;
+    double step;             /* initial step size */
+} rp_box_scaler_desc;
+
+typedef struct rp_sim_params {
+    double temperature;
+    double pressure;
+    double translation_step;  /* initial TranslationSampler step; 0 disables translations */
+    double rotation_step;     /* initial RotationSampler step; 0 disables rotations */
+    rp_box_scaler_desc scaler;
+    uint64_t seed;            /* the box moves' std::mt19937 seed and the sweeps' Philox key */
+} rp_sim_params;
+
+typedef struct rp_sim_stats {
+    uint64_t cycles;          /* cycles run since creation (the sweeps' Philox counters) */
+    uint64_t translations, accepted_translations, rotations, accepted_rotations;
+    uint64_t box_moves, accepted_box_moves;
+    double translation_step, rotation_step, box_step;  /* current step sizes */
+    double box[9];            /* current box */
+    double move_ms, scaling_ms;  /* host wall clock of the sweeps and of the box moves */
+} rp_sim_stats;
+
+int rp_sim_create(void *handle, const rp_sim_params *params, void **sim);
+int rp_sim_run(void *sim, int64_t cycles, int adjust_steps, rp_sim_stats *stats);
+int rp_sim_get_stats(void *sim, rp_sim_stats *stats);
+int rp_sim_set_steps(void *sim, double translation_step, double rotation_step, double box_step);
+int rp_sim_set_conditions(void *sim, double temperature, double pressure);
+const char *rp_sim_last_error(void *sim);
+int rp_sim_destroy(void *sim);
+
+/* The box scaler alone, as Simulation::tryScaling draws from its generator: `count` times a
+ * proposal from the same `box9` followed by the Metropolis uniform (boxes [count][9],
+ * uniforms [count], may be null). */
+int rp_box_proposals(const rp_box_scaler_desc *scaler, uint64_t seed, const double *box9, int64_t count,
+                     double *boxes, double *uniforms);
 
 /* ---- snapshot and trajectory files (RAMSNAP text, RAMTRJ binary) ------------------
  *

@@ -381,3 +381,20 @@ def ref_ramtrj_read(path: str, kind: int, params, index: int, n: int):
     if rc != 0:
         raise ValueError(err.value.decode())
     return pos, rot, box
+
+
+def ref_box_proposals(kind: int, together: int, groups, independent: int, step: float, seed: int, box, count: int):
+    """The reference's box scalers (TriclinicDeltaScaler, TriclinicAdapter over
+    AnisotropicVolumeScaler / DeltaVolumeScaler) drawing `count` proposals from one box with
+    std::mt19937(seed), each followed by Simulation's unit-interval draw."""
+    lib, _ = _lib("reference")
+    lib.ref_box_proposals.restype = C.c_int
+    lib.ref_box_proposals.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.c_int, C.c_double, C.c_uint64,
+                                      _D, C.c_int64, _D, _D]
+    g = (C.c_int * 3)(*(list(groups) + [0, 0, 0])[:3])
+    b = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
+    boxes, u = np.zeros((count, 9)), np.zeros(count)
+    if lib.ref_box_proposals(kind, together, len(groups), g, independent, step, seed, _dp(b), count, _dp(boxes),
+                             _dp(u)) != 0:
+        raise ValueError("bad scaler")
+    return boxes, u

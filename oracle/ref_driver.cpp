@@ -29,6 +29,7 @@
 #include "core/shapes/SpherocylinderTraits.h"
 #include "core/volume_scalers/AnisotropicVolumeScaler.h"
 #include "core/volume_scalers/DeltaVolumeScaler.h"
+#include "core/volume_scalers/LinearScalingFactorSampler.h"
 #include "core/volume_scalers/LogScalingFactorSampler.h"
 #include "core/volume_scalers/TriclinicAdapter.h"
 #include "core/volume_scalers/TriclinicDeltaScaler.h"
@@ -497,6 +498,50 @@ int ref_ramtrj_read(const char *path, int kind, const double *prm, int np, int64
         std::snprintf(err, errcap, "%s", e.what());
         return -1;
     }
+}
+
+// TriclinicBoxScaler::updateBox then Simulation's unit-interval draw, `count` times from the
+// same box with one std::mt19937(seed): the box-move proposal stream of the reference.
+// kind 1 TriclinicDeltaScaler, 2 log / 3 linear AnisotropicVolumeScaler through
+// TriclinicAdapter (groups: axis masks combined with & inside, | between), 4 DeltaVolumeScaler.
+int ref_box_proposals(int kind, int together, int ngroups, const int *groups, int independent, double step,
+                      uint64_t seed, const double *box9, int64_t count, double *boxes, double *uniforms) {
+    std::unique_ptr<TriclinicBoxScaler> sc;
+    if (kind == 1) {
+        sc = std::make_unique<TriclinicDeltaScaler>(step, together != 0);
+    } else if (kind == 4) {
+        sc = std::make_unique<TriclinicAdapter>(std::make_unique<DeltaVolumeScaler>(), step);
+    } else if (kind == 2 || kind == 3) {
+        using SD = AnisotropicVolumeScaler::ScalingDirection;
+        SD dir;
+        for (int g = 0; g < ngroups; g++) {
+            SD one;
+            bool first = true;
+            const SD axes[3] = {AnisotropicVolumeScaler::X, AnisotropicVolumeScaler::Y, AnisotropicVolumeScaler::Z};
+            for (int a = 0; a < 3; a++)
+                if (groups[g] & (1 << a)) {
+                    one = first ? axes[a] : (one & axes[a]);
+                    first = false;
+                }
+            dir = g == 0 ? one : (dir | one);
+        }
+        std::unique_ptr<ScalingFactorSampler> fs;
+        if (kind == 2) fs = std::make_unique<LogScalingFactorSampler>();
+        else fs = std::make_unique<LinearScalingFactorSampler>();
+        sc = std::make_unique<TriclinicAdapter>(
+            std::make_unique<AnisotropicVolumeScaler>(std::move(fs), dir, independent != 0), step);
+    } else {
+        return -1;
+    }
+    std::mt19937 mt(seed);
+    std::uniform_real_distribution<double> unit;
+    TriclinicBox box(load_m(box9));
+    for (int64_t k = 0; k < count; k++) {
+        TriclinicBox nb = sc->updateBox(box, mt);
+        store_m(nb.getDimensions(), boxes + 9 * k);
+        uniforms[k] = unit(mt);
+    }
+    return 0;
 }
 
 }  // extern "C"

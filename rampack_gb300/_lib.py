@@ -49,11 +49,37 @@ class SweepParams(C.Structure):
 class SweepStats(C.Structure):
     _fields_ = [("moves", C.c_uint64), ("accepted", C.c_uint64), ("rejected_overlap", C.c_uint64),
                 ("rejected_domain", C.c_uint64), ("pair_tests", C.c_uint64), ("fp64_pairs", C.c_uint64),
-                ("translations", C.c_uint64), ("rotations", C.c_uint64), ("kernel_launches", C.c_uint64)]
+                ("translations", C.c_uint64), ("rotations", C.c_uint64), ("kernel_launches", C.c_uint64),
+                ("accepted_translations", C.c_uint64)]
 
     def as_dict(self) -> dict:
         return {name: int(getattr(self, name)) for name, _ in self._fields_}
 
+
+class BoxScalerDesc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("scale_together", C.c_int32), ("num_groups", C.c_int32),
+                ("groups", C.c_int32 * 3), ("independent", C.c_int32), ("reserved", C.c_int32), ("step", C.c_double)]
+
+
+class SimParams(C.Structure):
+    _fields_ = [("temperature", C.c_double), ("pressure", C.c_double), ("translation_step", C.c_double),
+                ("rotation_step", C.c_double), ("scaler", BoxScalerDesc), ("seed", C.c_uint64)]
+
+
+class SimStats(C.Structure):
+    _fields_ = [("cycles", C.c_uint64), ("translations", C.c_uint64), ("accepted_translations", C.c_uint64),
+                ("rotations", C.c_uint64), ("accepted_rotations", C.c_uint64), ("box_moves", C.c_uint64),
+                ("accepted_box_moves", C.c_uint64), ("translation_step", C.c_double), ("rotation_step", C.c_double),
+                ("box_step", C.c_double), ("box", C.c_double * 9), ("move_ms", C.c_double),
+                ("scaling_ms", C.c_double)]
+
+    def as_dict(self) -> dict:
+        out = {name: getattr(self, name) for name, _ in self._fields_}
+        out["box"] = np.array(list(self.box))
+        return out
+
+
+SCALER_NONE, SCALER_DELTA_TRICLINIC, SCALER_LOG, SCALER_LINEAR, SCALER_DELTA_VOLUME = 0, 1, 2, 3, 4
 
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
@@ -112,6 +138,14 @@ SIGNATURES = {
     "rp_batch_download_states": (C.c_int, [_P, _D, _D, _D]),
     "rp_batch_set_timing": (C.c_int, [_P, C.c_int]),
     "rp_batch_get_timing": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "rp_sim_create": (C.c_int, [_P, C.POINTER(SimParams), C.POINTER(C.c_void_p)]),
+    "rp_sim_run": (C.c_int, [_P, C.c_int64, C.c_int, C.POINTER(SimStats)]),
+    "rp_sim_get_stats": (C.c_int, [_P, C.POINTER(SimStats)]),
+    "rp_sim_set_steps": (C.c_int, [_P, C.c_double, C.c_double, C.c_double]),
+    "rp_sim_set_conditions": (C.c_int, [_P, C.c_double, C.c_double]),
+    "rp_sim_last_error": (C.c_char_p, [_P]),
+    "rp_sim_destroy": (C.c_int, [_P]),
+    "rp_box_proposals": (C.c_int, [C.POINTER(BoxScalerDesc), C.c_uint64, _D, C.c_int64, _D, _D]),
     "rp_io_last_error": (C.c_char_p, []),
     "rp_ramsnap_write": (C.c_int, [_P, C.c_char_p, C.c_int32, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p)]),
     "rp_ramsnap_write_host": (C.c_int, [C.c_char_p, C.c_int64, _D, _D, _D, C.c_int32, C.POINTER(C.c_char_p),

@@ -763,7 +763,7 @@ struct Batch {
     double *rtab64 = nullptr;
     float *rtab32 = nullptr;
     int32_t *item_counters = nullptr;                 // [MAX_PHASES]
-    unsigned long long *stats = nullptr;              // [R][8]
+    unsigned long long *stats = nullptr;              // [R][NUM_COUNTERS]
     uint32_t *status = nullptr;                       // [R]
     unsigned long long *counts = nullptr, *h_counts = nullptr;  // [R]
     int *flags = nullptr, *h_flags = nullptr;         // [R]
@@ -903,9 +903,9 @@ static int create_common(Handle *h, int64_t n, int device, void **handle) {
     if ((e = cudaMalloc(&h->item_counters, sizeof(int32_t) * 64)) != cudaSuccess) return bail(e);
     if (!h->batch_member) {
         if ((e = cudaMalloc(&h->status, sizeof(uint32_t))) != cudaSuccess) return bail(e);
-        if ((e = cudaMalloc(&h->counters, sizeof(unsigned long long) * 8)) != cudaSuccess) return bail(e);
+        if ((e = cudaMalloc(&h->counters, sizeof(unsigned long long) * NUM_COUNTERS)) != cudaSuccess) return bail(e);
         cudaMemset(h->status, 0, sizeof(uint32_t));
-        cudaMemset(h->counters, 0, sizeof(unsigned long long) * 8);
+        cudaMemset(h->counters, 0, sizeof(unsigned long long) * NUM_COUNTERS);
     }
     if ((e = cudaMalloc(&h->count_out, sizeof(unsigned long long))) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc(&h->flag, sizeof(int))) != cudaSuccess) return bail(e);
@@ -1318,7 +1318,7 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
             RP_CUDA(h, cudaMalloc(&h->d_log_codes, h->log_alloc));
         }
     }
-    if (stats) RP_CUDA(h, cudaMemsetAsync(h->counters, 0, sizeof(unsigned long long) * 8, h->stream));
+    if (stats) RP_CUDA(h, cudaMemsetAsync(h->counters, 0, sizeof(unsigned long long) * NUM_COUNTERS, h->stream));
     RP_CUDA(h, cudaMemsetAsync(h->item_counters, 0, sizeof(int32_t) * 64, h->stream));
     if (types & 2) {
         Group grp(h, RP_KERNEL_REBUILD, 1);
@@ -1381,7 +1381,7 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
                                    cudaMemcpyDeviceToHost, h->stream));
     }
     if (stats) {
-        unsigned long long c[8];
+        unsigned long long c[NUM_COUNTERS];
         RP_CUDA(h, cudaMemcpyAsync(c, h->counters, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
         RP_CUDA(h, cudaStreamSynchronize(h->stream));
         stats->moves = c[0];
@@ -1392,6 +1392,7 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
         stats->fp64_pairs = c[5];
         stats->translations = c[6];
         stats->rotations = c[7];
+        stats->accepted_translations = c[8];
         stats->kernel_launches = h->launches;
     }
     h->can_revert = false;
@@ -1527,7 +1528,7 @@ int rp_get_stats(void *handle, rp_sweep_stats *stats) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h || !stats) return RP_ERR_ARG;
     RP_CUDA(h, cudaSetDevice(h->device));
-    unsigned long long c[8];
+    unsigned long long c[NUM_COUNTERS];
     RP_CUDA(h, cudaMemcpyAsync(c, h->counters, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
     RP_CUDA(h, cudaStreamSynchronize(h->stream));
     stats->moves = c[0];
@@ -1538,6 +1539,7 @@ int rp_get_stats(void *handle, rp_sweep_stats *stats) {
     stats->fp64_pairs = c[5];
     stats->translations = c[6];
     stats->rotations = c[7];
+    stats->accepted_translations = c[8];
     stats->kernel_launches = h->launches;
     return RP_OK;
 }
@@ -1960,7 +1962,7 @@ int rp_batch_create(const rp_shape_desc *shape, int32_t replicas, const int64_t 
               cudaMalloc(&b->rtab64, sizeof(double) * 9 * ROT_TABLE) == cudaSuccess &&
               cudaMalloc(&b->rtab32, sizeof(float) * 12 * ROT_TABLE) == cudaSuccess &&
               cudaMalloc(&b->item_counters, sizeof(int32_t) * MAX_PHASES) == cudaSuccess &&
-              cudaMalloc(&b->stats, sizeof(unsigned long long) * 8 * R) == cudaSuccess &&
+              cudaMalloc(&b->stats, sizeof(unsigned long long) * NUM_COUNTERS * R) == cudaSuccess &&
               cudaMalloc(&b->status, sizeof(uint32_t) * R) == cudaSuccess &&
               cudaMalloc(&b->counts, sizeof(unsigned long long) * R) == cudaSuccess &&
               cudaMallocHost(&b->h_counts, sizeof(unsigned long long) * R) == cudaSuccess &&
@@ -1971,7 +1973,7 @@ int rp_batch_create(const rp_shape_desc *shape, int32_t replicas, const int64_t 
              cudaMallocHost(&S.bases, sizeof(int) * (2 + MAX_PHASES) * (R + 1)) == cudaSuccess &&
              cudaEventCreateWithFlags(&S.done, cudaEventDisableTiming) == cudaSuccess;
     if (!ok) return bail(RP_ERR_CUDA);
-    cudaMemset(b->stats, 0, sizeof(unsigned long long) * 8 * R);
+    cudaMemset(b->stats, 0, sizeof(unsigned long long) * NUM_COUNTERS * R);
     cudaMemset(b->status, 0, sizeof(uint32_t) * R);
     for (int r = 0; r < R; r++) {
         Handle *h = new (std::nothrow) Handle();
@@ -1995,7 +1997,7 @@ int rp_batch_create(const rp_shape_desc *shape, int32_t replicas, const int64_t 
         h->ref_range = h->range;
         h->ex = ex;
         h->status = b->status + r;
-        h->counters = b->stats + 8 * r;
+        h->counters = b->stats + NUM_COUNTERS * r;
         h->rtab64 = b->rtab64;
         h->rtab32 = b->rtab32;
         void *hh = nullptr;
@@ -2276,7 +2278,7 @@ int rp_batch_sweep(void *batch, const rp_sweep_params *p, rp_sweep_stats *stats)
     rc = batch_copy(b);
     if (rc) return rc;
     const int *pb = b->d_bases, *cb = b->d_bases + (b->R + 1);
-    if (stats) RB_CUDA(b, cudaMemsetAsync(b->stats, 0, sizeof(unsigned long long) * 8 * b->R, b->stream));
+    if (stats) RB_CUDA(b, cudaMemsetAsync(b->stats, 0, sizeof(unsigned long long) * NUM_COUNTERS * b->R, b->stream));
     {
         BGroup grp(b, RP_KERNEL_REBUILD, (types & 2) ? 6 : 5);
         RB_CUDA(b, launch_b_rebuild(b->d_table, pb, cb, b->R, total_p, total_c, b->stream));
@@ -2319,9 +2321,9 @@ int rp_batch_sweep(void *batch, const rp_sweep_params *p, rp_sweep_stats *stats)
         }
     }
     if (stats || log) {
-        std::vector<unsigned long long> c(8 * b->R);
+        std::vector<unsigned long long> c(NUM_COUNTERS * b->R);
         std::vector<uint32_t> st(b->R);
-        RB_CUDA(b, cudaMemcpyAsync(c.data(), b->stats, sizeof(unsigned long long) * 8 * b->R, cudaMemcpyDeviceToHost,
+        RB_CUDA(b, cudaMemcpyAsync(c.data(), b->stats, sizeof(unsigned long long) * NUM_COUNTERS * b->R, cudaMemcpyDeviceToHost,
                                    b->stream));
         RB_CUDA(b, cudaMemcpyAsync(st.data(), b->status, sizeof(uint32_t) * b->R, cudaMemcpyDeviceToHost, b->stream));
         RB_CUDA(b, cudaStreamSynchronize(b->stream));
@@ -2331,7 +2333,7 @@ int rp_batch_sweep(void *batch, const rp_sweep_params *p, rp_sweep_stats *stats)
         for (Handle *h : b->rep) all_launches += h->launches;
         if (stats)
             for (int r = 0; r < b->R; r++) {
-                const unsigned long long *q = c.data() + 8 * r;
+                const unsigned long long *q = c.data() + NUM_COUNTERS * r;
                 stats[r].moves = q[0];
                 stats[r].accepted = q[1];
                 stats[r].rejected_overlap = q[2];
@@ -2340,6 +2342,7 @@ int rp_batch_sweep(void *batch, const rp_sweep_params *p, rp_sweep_stats *stats)
                 stats[r].fp64_pairs = q[5];
                 stats[r].translations = q[6];
                 stats[r].rotations = q[7];
+                stats[r].accepted_translations = q[8];
                 stats[r].kernel_launches = all_launches;
             }
     }
@@ -2511,5 +2514,14 @@ int state_snapshot(void *handle, double *pos, double *rot, double *box9, int64_t
 
 // Particle count of a handle (0 for a null handle).
 int64_t handle_size(void *handle) { return handle ? static_cast<Handle *>(handle)->n : 0; }
+
+// The handle's current box (false without a state) and whether it counts overlaps.
+bool handle_box(void *handle, double *box9) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !h->has_state) return false;
+    std::memcpy(box9, h->box, sizeof(h->box));
+    return true;
+}
+bool handle_counting(void *handle) { return handle && static_cast<Handle *>(handle)->counting; }
 
 }  // namespace rp

@@ -148,8 +148,9 @@ __device__ __forceinline__ void flush_stats(const SweepArgs &A, WarpStats &ws) {
         atomicAdd(C + 5, (unsigned long long)ws.fp64);
         atomicAdd(C + 6, (unsigned long long)ws.trans);
         atomicAdd(C + 7, (unsigned long long)ws.rots);
+        atomicAdd(C + 8, (unsigned long long)ws.acc_trans);
     }
-    ws = WarpStats{0, 0, 0, 0, 0, 0, 0, 0};
+    ws = WarpStats{};
 }
 
 // Phase k of every replica: persistent warps take checkerboard cells of the whole batch
@@ -169,7 +170,7 @@ __global__ void __launch_bounds__(WPB * 32, 16 / WPB)
     uint16_t *qun = qseg + cap;
     uint8_t *nacc = reinterpret_cast<uint8_t *>(qun + cap);
     const int total = item_base[R];
-    WarpStats ws = {0, 0, 0, 0, 0, 0, 0, 0};
+    WarpStats ws{};
     for (;;) {
         int it = 0;
         if (lane == 0) it = atomicAdd(next_item, 1);
@@ -217,7 +218,7 @@ __global__ void __launch_bounds__(32) k_b_overflow(const BatchRep *T, int k, int
     uint16_t *qseg = reinterpret_cast<uint16_t *>(cpos + cap * (KIND == 1 ? 2 : 1));
     uint16_t *qun = qseg + cap;
     uint8_t *nacc = reinterpret_cast<uint8_t *>(qun + cap);
-    WarpStats ws = {0, 0, 0, 0, 0, 0, 0, 0};
+    WarpStats ws{};
     for (int q = 0; q < count; q++) {
         sweep_cell<KIND, false, 0>(A, q, A.overflow[q], cap, nullptr, nullptr, cpos, cax, qseg, qun, nacc,
                                        nullptr, nullptr, nullptr, ws);

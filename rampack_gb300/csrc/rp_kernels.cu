@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(co
     uint16_t *pstage = reinterpret_cast<uint16_t *>(nacc + A.cap);  // LEARN only: MLP_PARTNERS x cap
     float4 *wx = reinterpret_cast<float4 *>(nacc + A.cap);          // polyspheres (never with LEARN)
     int nitems = A.work ? *A.work_count : (LIST ? A.num_list : A.num_active);
-    WarpStats ws = {0, 0, 0, 0, 0, 0, 0, 0};
+    WarpStats ws{};
     // persistent launches (next_item set) take cells from a shared counter until none are
     // left; otherwise warps stride over the cells
     const int stride = gridDim.x * warps_per_block;
@@ -230,6 +230,7 @@ __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(co
         atomicAdd(C + 5, (unsigned long long)ws.fp64);
         atomicAdd(C + 6, (unsigned long long)ws.trans);
         atomicAdd(C + 7, (unsigned long long)ws.rots);
+        atomicAdd(C + 8, (unsigned long long)ws.acc_trans);
     }
 }
 

@@ -168,7 +168,7 @@ __device__ __forceinline__ bool exact_centre_pair(const DevState &s, d3 pa, int 
 // entry per lane), re-decides the queued pairs in FP64 and, when accepted, writes back.
 // ---------------------------------------------------------------------------------
 struct WarpStats {
-    unsigned moves, accepted, rej_overlap, rej_domain, pairs, fp64, trans, rots;
+    unsigned moves, accepted, rej_overlap, rej_domain, pairs, fp64, trans, rots, acc_trans;
 };
 
 // MODE 0: plain sweep; 1: learned-ordering pre-test and pair log; 2: overlap counting
@@ -865,6 +865,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
         if (code == 1) ws.rej_overlap++;
         if (code == 2) ws.rej_domain++;
         if (type == 0) ws.trans++;
+        if (type == 0 && acc) ws.acc_trans++;
         else ws.rots++;
     }
 }

@@ -1,0 +1,181 @@
+"""The Monte Carlo driver around a GpuPacking: the reference's Simulation for hard bodies.
+
+``Simulation.integrate`` follows ``Simulation::integrate`` (core/Simulation.cpp:93-200):
+a thermalisation phase whose step sizes adapt (``Simulation::evaluateCounters``), then an
+averaging phase sampling observables every ``averaging_every`` cycles, the averages with the
+standard error of ``Quantity::calculateFromSamples`` (utils/Quantity.cpp:45-61); snapshots go
+to an optional ``RamtrjRecorder``.  Each cycle is one device sweep plus one box move whose
+proposal comes from the reference's box scalers with a std::mt19937 (``rp_sim_*``, native
+loop in rampack_gb300/csrc/rp_sim.cu).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib
+from ._lib import BoxScalerDesc, EngineError, SimParams, SimStats, dptr
+
+AXES = {"x": 1, "y": 2, "z": 4}
+
+
+def _groups(spec) -> list[int]:
+    out = []
+    for g in spec:
+        m = 0
+        for a in g:
+            m |= AXES[a]
+        out.append(m)
+    return out
+
+
+def delta_triclinic(step: float, scale_together: bool = True) -> BoxScalerDesc:
+    """TriclinicDeltaScaler(step, scaleTogether)."""
+    return BoxScalerDesc(kind=_lib.SCALER_DELTA_TRICLINIC, scale_together=1 if scale_together else 0, step=step)
+
+
+def _volume(kind: int, step: float, groups, independent: bool) -> BoxScalerDesc:
+    g = _groups(groups)
+    if not 1 <= len(g) <= 3:
+        raise ValueError("one to three scaling directions")
+    d = BoxScalerDesc(kind=kind, num_groups=len(g), independent=1 if independent else 0, step=step)
+    for i, m in enumerate(g):
+        d.groups[i] = m
+    return d
+
+
+def log_volume(step: float, groups=("xyz",), independent: bool = False) -> BoxScalerDesc:
+    """TriclinicAdapter(AnisotropicVolumeScaler(LogScalingFactorSampler, directions)); each
+    group ("xyz", "xy", "z", ...) is one direction scaled by one factor (X & Y & Z ...), groups
+    joined by |."""
+    return _volume(_lib.SCALER_LOG, step, groups, independent)
+
+
+def linear_volume(step: float, groups=("xyz",), independent: bool = False) -> BoxScalerDesc:
+    """As log_volume with LinearScalingFactorSampler."""
+    return _volume(_lib.SCALER_LINEAR, step, groups, independent)
+
+
+def delta_volume(step: float) -> BoxScalerDesc:
+    """TriclinicAdapter(DeltaVolumeScaler)."""
+    return BoxScalerDesc(kind=_lib.SCALER_DELTA_VOLUME, step=step)
+
+
+def box_proposals(scaler: BoxScalerDesc, seed: int, box, count: int):
+    """(boxes [count, 9], uniforms [count]): the proposals and Metropolis draws
+    Simulation::tryScaling takes from std::mt19937(seed), every one from ``box``."""
+    lib = _lib.load()
+    b = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
+    boxes, u = np.zeros((count, 9)), np.zeros(count)
+    rc = lib.rp_box_proposals(C.byref(scaler), seed, dptr(b), count, dptr(boxes), dptr(u))
+    if rc != 0:
+        raise EngineError(rc, "rp_box_proposals: invalid scaler")
+    return boxes, u
+
+
+def quantity(samples) -> tuple[float, float]:
+    """Quantity::calculateFromSamples: the mean and its standard error."""
+    x = [float(v) for v in samples]
+    if not x:
+        return 0.0, 0.0
+    if len(x) == 1:
+        return x[0], 0.0
+    # std::accumulate order (plain left-to-right sums; Python's sum() compensates)
+    total = 0.0
+    for v in x:
+        total += v
+    mean = total / len(x)
+    err = 0.0
+    for v in x:
+        err += (mean - v) ** 2
+    return mean, math.sqrt(err / len(x) / (len(x) - 1))
+
+
+def number_density(packing, stats) -> float:
+    b = np.asarray(stats["box"]).reshape(3, 3)
+    return packing.n / abs(float(np.dot(np.cross(b[:, 0], b[:, 1]), b[:, 2])))
+
+
+def nematic_order(packing, stats) -> float:
+    return packing.nematic_order()[1]
+
+
+OBSERVABLES = {"number_density": number_density, "nematic_order": nematic_order}
+
+
+class Simulation:
+    """Simulation(packing, translationStep, rotationStep, seed, boxScaler) for hard bodies."""
+
+    def __init__(self, packing, translation_step: float, rotation_step: float, seed: int,
+                 scaler: BoxScalerDesc | None = None):
+        self.lib = _lib.load()
+        self.packing = packing
+        p = SimParams(temperature=1.0, pressure=0.0, translation_step=translation_step, rotation_step=rotation_step,
+                      seed=seed)
+        if scaler is not None:
+            p.scaler = scaler
+        self.h = C.c_void_p()
+        rc = self.lib.rp_sim_create(packing.h, C.byref(p), C.byref(self.h))
+        if rc != 0:
+            raise EngineError(rc, "rp_sim_create failed (a packing with a state and valid parameters are needed)")
+
+    def _check(self, rc: int):
+        if rc != 0:
+            msg = self.lib.rp_sim_last_error(self.h)
+            raise EngineError(rc, msg.decode() if msg else "")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.rp_sim_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_conditions(self, temperature: float, pressure: float):
+        self._check(self.lib.rp_sim_set_conditions(self.h, temperature, pressure))
+
+    def set_steps(self, translation_step: float, rotation_step: float, box_step: float = 0.0):
+        self._check(self.lib.rp_sim_set_steps(self.h, translation_step, rotation_step, box_step))
+
+    def run(self, cycles: int, adjust_steps: bool = False) -> dict:
+        """`cycles` cycles of Simulation::performCycle; the running totals and current steps."""
+        st = SimStats()
+        self._check(self.lib.rp_sim_run(self.h, int(cycles), 1 if adjust_steps else 0, C.byref(st)))
+        return st.as_dict()
+
+    def stats(self) -> dict:
+        st = SimStats()
+        self._check(self.lib.rp_sim_get_stats(self.h, C.byref(st)))
+        return st.as_dict()
+
+    def integrate(self, temperature: float, pressure: float, thermalisation_cycles: int, averaging_cycles: int,
+                  averaging_every: int, observables=("number_density",), snapshot_every: int = 0, recorder=None):
+        """Simulation::integrate: thermalisation with step adaptation, then averaging;
+        returns {observable: (mean, standard error)} and the samples."""
+        self.set_conditions(temperature, pressure)
+        done = 0
+        while done < thermalisation_cycles:
+            k = min(1000, thermalisation_cycles - done)
+            self.run(k, adjust_steps=True)
+            done += k
+        samples = {name: [] for name in observables}
+        for c in range(1, averaging_cycles + 1):
+            st = self.run(1)
+            if c % averaging_every == 0:
+                for name in observables:
+                    samples[name].append(OBSERVABLES[name](self.packing, st))
+            if recorder is not None and snapshot_every and c % snapshot_every == 0:
+                recorder.record(self.packing, c // snapshot_every * snapshot_every)
+        return {name: quantity(v) for name, v in samples.items()}, samples

@@ -23,7 +23,8 @@ def oracle():
 
 @pytest.fixture(scope="session")
 def engine():
-    """The GPU engine library (built on demand); GPU tests only."""
+    """The engine library (built on demand): GPU tests, and CPU tests of its host-only entry
+    points (file formats, box scalers)."""
     from rampack_gb300 import build as _build
     _build.build()
     from rampack_gb300 import _lib

@@ -5,6 +5,7 @@ Run in a checkout where the reference sources are present:
     make -C oracle ref            # compiles the reference's hot-path sources in place
     python tests/golden/make_golden.py        # every fixture
     python tests/golden/make_golden.py io     # the snapshot / trajectory files only
+    python tests/golden/make_golden.py box    # the box-move proposal streams only
 
 Every expected value below is produced by the reference library (oracle/_ref/librpref.so:
 rampack's Packing, NeighbourGrid, SpherocylinderTraits, samplers and Simulation compiled
@@ -300,11 +301,33 @@ def gen_io(rng):
     print("io: ramsnap", os.path.getsize(snap), "B, ramtrj", os.path.getsize(trj), "B,", len(IO_CASES), "cases")
 
 
+# box scalers: (kind, scale together, axis groups, independent, step); kinds as rp_box_scaler_desc
+SCALERS = [(1, 1, [], 0, 0.005), (1, 0, [], 0, 0.05), (2, 0, [7], 0, 0.01), (2, 0, [1, 2, 4], 1, 0.01),
+           (2, 0, [3, 4], 0, 0.02), (2, 0, [3, 4], 1, 0.02), (3, 0, [7], 0, 0.1), (3, 0, [1, 2, 4], 1, 0.1),
+           (4, 0, [], 0, 5.0)]
+
+
+def gen_box_proposals():
+    """Box-move proposals and Metropolis draws of the reference's scalers and generator."""
+    box = np.array([10.0, 0.3, -0.2, 0.1, 11.0, 0.05, -0.0, -0.4, 12.5])
+    out = {"box": box}
+    for i, (kind, tog, groups, ind, step) in enumerate(SCALERS):
+        b, u = po.ref_box_proposals(kind, tog, groups, ind, step, 1234 + i, box, 40)
+        out[f"s{i}_spec"] = np.array([kind, tog, ind] + (groups + [0, 0, 0])[:3] + [len(groups)])
+        out[f"s{i}_step"] = np.array(step)
+        out[f"s{i}_boxes"], out[f"s{i}_uniforms"] = b, u
+    np.savez_compressed(os.path.join(HERE, "box_proposals.npz"), **out)
+    print("box proposals:", len(SCALERS), "scalers")
+
+
 def main():
     if not po.reference_available():
         po.build(reference=True)
     if sys.argv[1:] == ["io"]:
         gen_io(np.random.default_rng(20261204))
+        return
+    if sys.argv[1:] == ["box"]:
+        gen_box_proposals()
         return
     rng = np.random.default_rng(20241203)
     gen_pairs(rng)
@@ -319,6 +342,7 @@ def main():
     gen_sim("sc_dd", W.spherocylinders((12, 12, 12), 0.35, 2.0, 0.5, aspect=(1, 1, 3)), 8, translation_step=0.2,
             rotation_step=0.2, box_kind=1, box_step=0.005, pressure=1.5, domains=(2, 2, 2), threads=8)
     gen_io(np.random.default_rng(20261204))
+    gen_box_proposals()
 
 
 if __name__ == "__main__":

@@ -111,6 +111,25 @@ def test_sweep_log_replays_on_oracle(oracle, engine, name, fp64_only):
             assert g.count_total_overlaps(True) == 0
 
 
+@pytest.mark.parametrize("name", ["hs_small", "hs_dense", "hs_tiny"])
+def test_sphere_sweeps_with_rotations_replay_on_oracle(oracle, engine, name):
+    # the Simulation's samplers rotate spheres too (an orientation change that never overlaps)
+    cfg = systems.ALL[name]()
+    cpu = cpu_packing(cfg)
+    with gpu_packing(cfg) as g:
+        for cycle in range(2):
+            st = g.sweep(0.1, 0.3, seed=31, counter=cycle, log=True)
+            moves, codes = g.sweep_log()
+            _, _, bounds = g.grid()
+            assert st["moves"] == len(moves) == 2 * g.n and st["rotations"] > 0
+            want, _ = cpu.replay(moves, bounds)
+            assert np.array_equal(codes, want)
+            assert st["accepted"] - st["accepted_translations"] == st["rotations"]  # every rotation accepted
+        gp, gr, _ = g.state()
+        cp, cr, _ = cpu.state()
+        assert np.array_equal(gp, cp) and np.array_equal(gr, cr)
+
+
 @pytest.mark.parametrize("name", ["sc_l2_dense", "poly_dense"])
 def test_fp32_filter_matches_fp64_only(engine, name):
     cfg = systems.ALL[name]()

@@ -16,7 +16,7 @@ TRJ = os.path.join(GOLD, "io_sc.ramtrj")
 
 
 @pytest.fixture(scope="module")
-def io():
+def io(engine):
     return np.load(os.path.join(GOLD, "io.npz"))
 
 
