@@ -311,18 +311,20 @@ def main_gpu(args):
     g = GpuPacking(kind, prm, pos, rot, box, device=local)
     g.box = np.array(box, dtype=np.float64)
     stream = torch.cuda.ExternalStream(g.stream(), device=local)
-    rng = np.random.default_rng(args.seed + rank)
     seed = args.seed + 7919 * rank
 
-    k = 0
-    for _ in range(max(3, args.warmup)):
-        cycle(g, k, seed, rng)
-        k += 1
+    # the native cycle loop (rp_sim): one device sweep, then one isotension box move
+    # (TriclinicDeltaScaler, every entry +- 0.005, std::mt19937) pre-checked on the host
+    from rampack_gb300 import simulation as SIM
+    sim = SIM.Simulation(g, TRANS_STEP, ROT_STEP, seed, SIM.delta_triclinic(BOX_STEP, True))
+    sim.set_conditions(TEMPERATURE, PRESSURE)
+    sim.run(max(3, args.warmup))
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
 
     s0 = g.stats()
+    b0 = sim.stats()
     g.set_timing(True)
     clocks = Clocks(local)
     clocks.start()
@@ -331,15 +333,12 @@ def main_gpu(args):
     torch.cuda.synchronize()
     t0 = time.time()
     ev0.record(stream)
-    box_acc = 0
-    for _ in range(args.steps):
-        _, acc = cycle(g, k, seed, rng)
-        box_acc += acc
-        k += 1
+    b1 = sim.run(args.steps)
     ev1.record(stream)
     ev1.synchronize()
     torch.cuda.synchronize()
     t1 = time.time()
+    box_acc = b1["accepted_box_moves"] - b0["accepted_box_moves"]
     ms = ev0.elapsed_time(ev1)
     clk = clocks.stop(t0, t1)
     timing = g.timing()
@@ -361,7 +360,7 @@ def main_gpu(args):
     info, _, _ = g.grid()
     phases = 1
     for d in info["dims"]:
-        phases *= 2 if d > 1 else 1
+        phases *= 1 if d == 1 else (3 if d == 3 else 2)  # colours per grid dimension
     ncell = info["num_cells"]
     moves_per_sweep = 2 * n
     # algorithmic bytes per sweep: each phase streams every particle's FP32 record (28 B) and
@@ -400,9 +399,7 @@ def main_gpu(args):
         f0.record(stream)
         for _ in range(e_steps):
             g.upload(hpos, hrot, hbox)   # H2D of the step's input state (pinned)
-            g.box = hbox.copy()
-            cycle(g, k, seed, rng)
-            k += 1
+            sim.run(1)
             g.state(out=(hpos, hrot, hbox))  # D2H of the step's result into the same pinned buffers
         f1.record(stream)
         f1.synchronize()
@@ -423,6 +420,7 @@ def main_gpu(args):
                     "sample": f"2 full cycles of the same N={n:,} system after 1 warm-up cycle, OpenMP domain "
                               f"decomposition {dom_used} (oracle/ restatement of the reference's path)"}
 
+    sim.close()
     g.close()
     if rank == 0:
         line = {
