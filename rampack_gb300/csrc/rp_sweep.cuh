@@ -865,8 +865,8 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
         if (code == 1) ws.rej_overlap++;
         if (code == 2) ws.rej_domain++;
         if (type == 0) ws.trans++;
-        if (type == 0 && acc) ws.acc_trans++;
         else ws.rots++;
+        if (type == 0 && acc) ws.acc_trans++;
     }
 }
 
