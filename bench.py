@@ -615,18 +615,19 @@ def main_replicas(args):
     s0 = {k: b.sweep(*steps[k], seed=args.seed + 99, counter=0, stats=True) for k, b in batches.items()}
     acc = sum(x["accepted"] for v in s0.values() for x in v) / max(1, sum(x["moves"] for v in s0.values() for x in v))
     state["box_acc"] = 0
-    # per-launch sweep bytes (the single-system formula per replica, summed): P·n·(28+4) +
-    # P·(C+1)·4 + M·(96 + a·(96+28)) with P the replica's phases, C its cells, M its moves
-    b_cycle, sweep_launches_per_cycle = 0.0, 0
-    for kind, b in batches.items():
-        maxph = 0
-        for r in range(b.R):
-            info, _, _ = b.grid(r)
-            P = int(np.prod([1 if d == 1 else (3 if d == 3 else 2) for d in info["dims"]]))
-            maxph = max(maxph, P)
-            m = (2 if kind == 1 else 1) * b.sizes[r]
-            b_cycle += P * b.sizes[r] * 32 + P * (info["num_cells"] + 1) * 4 + m * (96 + acc * 124)
-        sweep_launches_per_cycle += maxph
+    # per-launch sweep bytes of the dominant batch (the spherocylinders, k_b_sweep<1,4>): the
+    # single-system formula per replica, summed, P·n·(28+4) + P·(C+1)·4 + M·(96 + a·(96+28))
+    # with P the replica's phases, C its cells, M its moves, a the batch's acceptance; over
+    # the batch's phase launches per sweep (its largest P)
+    sc = batches[1]
+    acc_sc = sum(x["accepted"] for x in s0[1]) / max(1, sum(x["moves"] for x in s0[1]))
+    b_cycle, maxph = 0.0, 0
+    for r in range(sc.R):
+        info, _, _ = sc.grid(r)
+        P = int(np.prod([1 if d == 1 else (3 if d == 3 else 2) for d in info["dims"]]))
+        maxph = max(maxph, P)
+        m = 2 * sc.sizes[r]
+        b_cycle += P * sc.sizes[r] * 32 + P * (info["num_cells"] + 1) * 4 + m * (96 + acc_sc * 124)
     for b in batches.values():
         b.set_timing(True)
     launches0 = sum(b.timing()[1] for b in batches.values())
@@ -646,17 +647,19 @@ def main_replicas(args):
     n = sum(len(r[2]) for r in reps)
     timing = {}
     launches = -launches0
-    for b in batches.values():
+    sc_sweep = None
+    for kind, b in batches.items():
         t, l = b.timing()
         launches += l
+        if kind == 1:
+            sc_sweep = t["sweep"]
         for name, (ms_, g) in t.items():
             a = timing.setdefault(name, [0.0, 0])
             a[0] += ms_
             a[1] += g
         b.set_timing(False)
-    sweep_ms, sweep_groups = timing["sweep"]
-    avg_launch_ms = sweep_ms / max(1, sweep_groups)
-    b_launch = b_cycle / sweep_launches_per_cycle
+    avg_launch_ms = sc_sweep[0] / max(1, sc_sweep[1])
+    b_launch = b_cycle / maxph
     achieved = b_launch / (avg_launch_ms / 1e3) / 1e9
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(peaks_path):
@@ -665,7 +668,8 @@ def main_replicas(args):
         peak, peak_src = 6800.0, "fallback 6.8 TB/s"
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": read_profile_traffic("replicas-64"),
-                "kernel": "k_b_sweep (one launch per checkerboard phase and batch)", "peak_source": peak_src,
+                "kernel": "k_b_sweep<1,4> (the spherocylinder batch: one launch per checkerboard phase)",
+                "peak_source": peak_src,
                 "avg_launch_ms": avg_launch_ms, "bytes_per_launch": b_launch}
 
     # ---- end to end through the C ABI: every replica's state from pinned host buffers,
