@@ -100,6 +100,8 @@ typedef struct rp_sweep_params {
 
 #define RP_SWEEP_LOG 1            /* record every proposal and outcome (rp_sweep_log) */
 #define RP_SWEEP_FP64_ONLY 2      /* decide every pair in FP64 (no FP32 filter) */
+#define RP_SWEEP_ROTOTRANSLATION 4 /* RototranslationSampler (core/move_samplers/RototranslationSampler.cpp:22-48):
+                                      N moves, each a translation and a rotation together (both steps > 0) */
 
 typedef struct rp_sweep_stats {
     uint64_t moves;
@@ -425,11 +427,14 @@ typedef struct rp_sim_params {
     double rotation_step;     /* initial RotationSampler step; 0 disables rotations */
     rp_box_scaler_desc scaler;
     uint64_t seed;            /* the box moves' std::mt19937 seed and the sweeps' Philox key */
+    int32_t rototranslation;  /* one RototranslationSampler(translation_step, rotation_step) instead of
+                                 the two samplers: N moves per cycle, its step rule (RototranslationSampler.cpp:50-61) */
+    int32_t reserved;
 } rp_sim_params;
 
 typedef struct rp_sim_stats {
     uint64_t cycles;          /* cycles run since creation (the sweeps' Philox counters) */
-    uint64_t translations, accepted_translations, rotations, accepted_rotations;
+    uint64_t translations, accepted_translations, rotations, accepted_rotations;  /* rototranslations count as rotations */
     uint64_t box_moves, accepted_box_moves;
     double translation_step, rotation_step, box_step;  /* current step sizes */
     double box[9];            /* current box */

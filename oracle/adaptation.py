@@ -30,12 +30,31 @@ class Counter:
 
 
 class Adaptation:
-    def __init__(self, n: int, translation_step: float, rotation_step: float, box_step: float):
+    def __init__(self, n: int, translation_step: float, rotation_step: float, box_step: float,
+                 rototranslation: bool = False):
         self.n = n
         self.t, self.r, self.b = translation_step, rotation_step, box_step
         self.ct, self.cr, self.cb = Counter(), Counter(), Counter()
+        self.rototranslation = rototranslation
 
     def evaluate(self, max_translation: float):
+        if self.rototranslation:
+            # RototranslationSampler::increaseStepSize / decreaseStepSize
+            # (core/move_samplers/RototranslationSampler.cpp:50-61, :87-93); its moves are
+            # counted with the rotations
+            if self.cr.since >= 100 * self.n:
+                rate = self.cr.rate()
+                self.cr.reset()
+                if rate > 0.2:
+                    old = self.t
+                    if not (max_translation > 0 and self.t >= max_translation):
+                        self.t *= 1.1
+                    self.r *= self.t / old
+                elif rate < 0.1:
+                    self.t /= 1.1
+                    self.r /= 1.1
+            self._box()
+            return
         if self.t > 0 and self.ct.since >= 100 * self.n:
             rate = self.ct.rate()
             self.ct.reset()
@@ -53,6 +72,9 @@ class Adaptation:
                     self.r = math.pi
             elif rate < 0.1:
                 self.r /= 1.1
+        self._box()
+
+    def _box(self):
         if self.b > 0 and self.cb.since >= 100:
             rate = self.cb.rate()
             self.cb.reset()

@@ -23,7 +23,7 @@ SHAPE_SPHERE, SHAPE_SPHEROCYLINDER, SHAPE_POLYSPHERE = 0, 1, 2
 MAX_CENTRES = 8
 MOVE_TRANSLATION, MOVE_ROTATION, MOVE_ROTOTRANSLATION = 0, 1, 2
 CODE_ACCEPTED = 0x80
-SWEEP_LOG, SWEEP_FP64_ONLY = 1, 2
+SWEEP_LOG, SWEEP_FP64_ONLY, SWEEP_ROTOTRANSLATION = 1, 2, 4
 
 MOVE_DTYPE = np.dtype([
     ("particle", "<i4"), ("type", "<i4"), ("domain", "<i4"), ("reserved", "<i4"),
@@ -63,7 +63,8 @@ class BoxScalerDesc(C.Structure):
 
 class SimParams(C.Structure):
     _fields_ = [("temperature", C.c_double), ("pressure", C.c_double), ("translation_step", C.c_double),
-                ("rotation_step", C.c_double), ("scaler", BoxScalerDesc), ("seed", C.c_uint64)]
+                ("rotation_step", C.c_double), ("scaler", BoxScalerDesc), ("seed", C.c_uint64),
+                ("rototranslation", C.c_int32), ("reserved", C.c_int32)]
 
 
 class SimStats(C.Structure):

@@ -1290,6 +1290,10 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
     if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
     int types = (p->translation_step > 0 ? 1 : 0) | (p->rotation_step > 0 ? 2 : 0);
     if (!types) return fail(h, RP_ERR_ARG, "no move type enabled");
+    if (p->flags & RP_SWEEP_ROTOTRANSLATION) {
+        if (types != 3) return fail(h, RP_ERR_ARG, "rototranslations need a translation and a rotation step");
+        types = SWEEP_ROTOTRANSLATION;
+    }
     RP_CUDA(h, cudaSetDevice(h->device));
     // random grid origin and phase order from the Philox stream of this sweep
     u4 r = philox(u4{0x5eedu, 0x9e37u, static_cast<uint32_t>(p->counter), static_cast<uint32_t>(p->counter >> 32)},
@@ -1307,7 +1311,7 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
     double tstep = std::min(p->translation_step, std::min({hgt[0], hgt[1], hgt[2]}) / 2);
     std::vector<int> phases;
     grid_phases(g, r.d, phases);
-    int ntypes = (types & 1) + ((types >> 1) & 1);
+    int ntypes = sweep_move_types(types);
     bool log = (p->flags & RP_SWEEP_LOG) != 0;
     if (log) {
         int64_t before = h->log_alloc;
@@ -1320,7 +1324,7 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
     }
     if (stats) RP_CUDA(h, cudaMemsetAsync(h->counters, 0, sizeof(unsigned long long) * NUM_COUNTERS, h->stream));
     RP_CUDA(h, cudaMemsetAsync(h->item_counters, 0, sizeof(int32_t) * 64, h->stream));
-    if (types & 2) {
+    if (types & (2 | SWEEP_ROTOTRANSLATION)) {
         Group grp(h, RP_KERNEL_REBUILD, 1);
         RP_CUDA(h, launch_rot_table(h->rtab64, h->rtab32, ROT_TABLE, p->seed, p->counter,
                                     static_cast<float>(p->rotation_step), h->stream));
@@ -2198,11 +2202,15 @@ int rp_batch_sweep(void *batch, const rp_sweep_params *p, rp_sweep_stats *stats)
     if (!b || !p) return bfail(b, RP_ERR_ARG, "null argument");
     int types = (p->translation_step > 0 ? 1 : 0) | (p->rotation_step > 0 ? 2 : 0);
     if (!types) return bfail(b, RP_ERR_ARG, "no move type enabled");
+    if (p->flags & RP_SWEEP_ROTOTRANSLATION) {
+        if (types != 3) return bfail(b, RP_ERR_ARG, "rototranslations need a translation and a rotation step");
+        types = SWEEP_ROTOTRANSLATION;
+    }
     for (Handle *h : b->rep)
         if (!h->has_state) return bfail(b, RP_ERR_STATE, "a replica has no state");
     RB_CUDA(b, cudaSetDevice(b->device));
     const bool log = (p->flags & RP_SWEEP_LOG) != 0;
-    const int ntypes = (types & 1) + ((types >> 1) & 1);
+    const int ntypes = sweep_move_types(types);
     std::vector<std::vector<int>> phases(b->R);
     std::vector<double> tstep(b->R);
     int cap = 0, maxph = 0;
@@ -2280,9 +2288,10 @@ int rp_batch_sweep(void *batch, const rp_sweep_params *p, rp_sweep_stats *stats)
     const int *pb = b->d_bases, *cb = b->d_bases + (b->R + 1);
     if (stats) RB_CUDA(b, cudaMemsetAsync(b->stats, 0, sizeof(unsigned long long) * NUM_COUNTERS * b->R, b->stream));
     {
-        BGroup grp(b, RP_KERNEL_REBUILD, (types & 2) ? 6 : 5);
+        const bool rotations = (types & (2 | SWEEP_ROTOTRANSLATION)) != 0;
+        BGroup grp(b, RP_KERNEL_REBUILD, rotations ? 6 : 5);
         RB_CUDA(b, launch_b_rebuild(b->d_table, pb, cb, b->R, total_p, total_c, b->stream));
-        if (types & 2)
+        if (rotations)
             RB_CUDA(b, launch_rot_table(b->rtab64, b->rtab32, ROT_TABLE, p->seed, p->counter,
                                         static_cast<float>(p->rotation_step), b->stream));
     }

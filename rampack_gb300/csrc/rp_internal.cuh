@@ -143,7 +143,15 @@ constexpr int NUM_COUNTERS = 9;     // sweep statistics words per handle (rp_swe
 constexpr int SWEEP_WARPS = 4;       // warps per block of the sweep kernel
 constexpr int SWEEP_MIN_BLOCKS = 4;  // resident blocks per SM the register budget allows
 constexpr int MIRROR_ROUNDINGS = 4;  // FP32 mirror updates per particle and sweep before an exact refresh
-constexpr uint32_t ROT_TABLE = 65536;  // rotations drawn per sweep (plus their inverses)
+constexpr uint32_t ROT_TABLE = 65536;  // rotations drawn per sweep (plus their inverses); at most 2^16
+static_assert(ROT_TABLE <= 65536, "a rototranslation draws its table index from 16 random bits");
+
+// SweepArgs::types: 1 translations, 2 rotations, 3 both (each particle once per type), or
+// SWEEP_ROTOTRANSLATION (each particle once, translated and rotated together)
+constexpr int SWEEP_ROTOTRANSLATION = 4;
+__host__ __device__ inline int sweep_move_types(int types) {
+    return types == SWEEP_ROTOTRANSLATION ? 1 : (types & 1) + ((types >> 1) & 1);
+}
 
 struct SweepArgs {
     DevState s;

@@ -198,26 +198,45 @@ int try_scaling(Sim *s) {
 }
 
 // Simulation::evaluateMoleculeMoveCounter / evaluateScalingMoveCounter
+// (core/Simulation.cpp:533-607): a sampler is evaluated once 100·N of its moves were made
+// since its last evaluation (N requested moves per cycle), the box scaler after 100 moves
 void evaluate_counters(Sim *s) {
     const uint64_t requested = static_cast<uint64_t>(s->n);  // getNumOfRequestedMoves(N) = N
-    if (s->p.translation_step > 0 && s->trans.since >= 100 * requested) {
-        const double rate = s->trans.rate();
-        s->trans.reset();
-        if (rate > 0.2) {
-            // TranslationSampler::increaseStepSize: refused at the implicit maximum
-            if (!(s->max_trans > 0 && s->tstep >= s->max_trans)) s->tstep *= 1.1;
-        } else if (rate < 0.1) {
-            s->tstep /= 1.1;
+    if (s->p.rototranslation) {
+        // RototranslationSampler::increaseStepSize / decreaseStepSize
+        // (core/move_samplers/RototranslationSampler.cpp:50-61, :87-93)
+        if (s->rot.since >= 100 * requested) {
+            const double rate = s->rot.rate();
+            s->rot.reset();
+            if (rate > 0.2) {
+                const double old = s->tstep;
+                if (!(s->max_trans > 0 && s->tstep >= s->max_trans)) s->tstep *= 1.1;
+                s->rstep *= s->tstep / old;
+            } else if (rate < 0.1) {
+                s->tstep /= 1.1;
+                s->rstep /= 1.1;
+            }
         }
-    }
-    if (s->p.rotation_step > 0 && s->rot.since >= 100 * requested) {
-        const double rate = s->rot.rate();
-        s->rot.reset();
-        if (rate > 0.2) {
-            s->rstep *= 1.1;
-            if (s->rstep > PI) s->rstep = PI;
-        } else if (rate < 0.1) {
-            s->rstep /= 1.1;
+    } else {
+        if (s->p.translation_step > 0 && s->trans.since >= 100 * requested) {
+            const double rate = s->trans.rate();
+            s->trans.reset();
+            if (rate > 0.2) {
+                // TranslationSampler::increaseStepSize: refused at the implicit maximum
+                if (!(s->max_trans > 0 && s->tstep >= s->max_trans)) s->tstep *= 1.1;
+            } else if (rate < 0.1) {
+                s->tstep /= 1.1;
+            }
+        }
+        if (s->p.rotation_step > 0 && s->rot.since >= 100 * requested) {
+            const double rate = s->rot.rate();
+            s->rot.reset();
+            if (rate > 0.2) {
+                s->rstep *= 1.1;
+                if (s->rstep > PI) s->rstep = PI;
+            } else if (rate < 0.1) {
+                s->rstep /= 1.1;
+            }
         }
     }
     if (s->p.scaler.kind != RP_SCALER_NONE && s->box.since >= 100) {
@@ -285,7 +304,8 @@ int rp_sim_create(void *handle, const rp_sim_params *p, void **sim) {
     double box[9];
     if (!rp::handle_box(handle, box)) return RP_ERR_STATE;
     if (!(p->temperature > 0) || !valid_scaler(p->scaler) || p->translation_step < 0 || p->rotation_step < 0 ||
-        (p->translation_step == 0 && p->rotation_step == 0))
+        (p->translation_step == 0 && p->rotation_step == 0) ||
+        (p->rototranslation && !(p->translation_step > 0 && p->rotation_step > 0)))
         return RP_ERR_ARG;
     Sim *s = new (std::nothrow) Sim();
     if (!s) return RP_ERR_ARG;
@@ -322,6 +342,11 @@ int rp_sim_run(void *sim, int64_t cycles, int adjust_steps, rp_sim_stats *stats)
         rp_sweep_params sp{};
         sp.translation_step = s->tstep;
         sp.rotation_step = s->rstep;
+        if (s->p.rototranslation) {
+            // RototranslationSampler::sampleMove draws angles within min(step, pi)
+            sp.rotation_step = std::min(s->rstep, PI);
+            sp.flags |= RP_SWEEP_ROTOTRANSLATION;
+        }
         sp.seed = s->p.seed;
         sp.counter = s->cycles;
         if (rp_sweep(s->h, &sp, nullptr) != RP_OK) return sim_fail(s, RP_ERR_DEVICE, "rp_sweep", s->h);

@@ -306,9 +306,9 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
         mbeg = A.list_begin[li];
         nmoves = A.list_begin[li + 1] - mbeg;
     } else {
-        nmoves = ((A.types & 1) + ((A.types >> 1) & 1)) * occ;
+        nmoves = sweep_move_types(A.types) * occ;
     }
-    const int ntypes = (A.types & 1) + ((A.types >> 1) & 1);
+    const int ntypes = sweep_move_types(A.types);
 
     u4 rnd_lane = u4{0u, 0u, 0u, 0u};  // Philox output of move (batch base + lane)
     for (int mi = 0; mi < nmoves; mi++) {
@@ -356,16 +356,20 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
             const int src = mi & 31;
             u4 r = u4{__shfl_sync(FULL, rnd_lane.a, src), __shfl_sync(FULL, rnd_lane.b, src),
                       __shfl_sync(FULL, rnd_lane.c, src), __shfl_sync(FULL, rnd_lane.d, src)};
-            if (ntypes == 2) type = (r.a >> 31) ? 1 : 0;
+            if (A.types == SWEEP_ROTOTRANSLATION) type = 2;
+            else if (ntypes == 2) type = (r.a >> 31) ? 1 : 0;
             else type = (A.types & 1) ? 0 : 1;
             slot = (int)(((uint64_t)(r.a & 0x7fffffffu) * (uint32_t)occ) >> 31);
-            if (type == 0) {
+            if (type != 1) {
+                // pm1f takes the top 24 bits of a word: a rototranslation's rotation takes
+                // the low bytes
                 t32 = make_float3(pm1f(r.b) * A.tstep, pm1f(r.c) * A.tstep, pm1f(r.d) * A.tstep);
                 t64_lane = ld == 0 ? (double)t32.x : (ld == 1 ? (double)t32.y : (double)t32.z);
-            } else {
+            }
+            if (type != 0) {
                 // a rotation of this sweep's table, or its transpose (the inverse)
-                rot_idx = r.b & A.rtab_mask;
-                rot_inv = (r.c & 1u) != 0;
+                rot_idx = (type == 1 ? r.b : ((r.b & 0xffu) | ((r.c & 0xffu) << 8))) & A.rtab_mask;
+                rot_inv = ((type == 1 ? r.c : r.d) & 1u) != 0;
                 if (KIND >= 1) {
                     const float4 *R4 = reinterpret_cast<const float4 *>(A.rtab32) + 3 * (size_t)rot_idx;
                     float4 x0 = R4[0], x1 = R4[1], x2 = R4[2];

@@ -171,13 +171,15 @@ class GpuPacking:
         return codes
 
     def sweep(self, translation_step: float, rotation_step: float, seed: int, counter: int,
-              log: bool = False, fp64_only: bool = False, stats: bool = True):
+              log: bool = False, fp64_only: bool = False, stats: bool = True, rototranslation: bool = False):
+        """One device sweep: 2N moves (translations and rotations), or N rototranslations."""
         p = SweepParams()
         p.translation_step = translation_step
         p.rotation_step = rotation_step
         p.seed = seed
         p.counter = counter
-        p.flags = (_lib.SWEEP_LOG if log else 0) | (_lib.SWEEP_FP64_ONLY if fp64_only else 0)
+        p.flags = ((_lib.SWEEP_LOG if log else 0) | (_lib.SWEEP_FP64_ONLY if fp64_only else 0) |
+                   (_lib.SWEEP_ROTOTRANSLATION if rototranslation else 0))
         st = SweepStats()
         self._check(self.lib.rp_sweep(self.h, C.byref(p), C.byref(st) if stats else None))
         return st.as_dict() if stats else None
@@ -380,10 +382,11 @@ class BatchPacking:
         return GpuPacking._info(info), cells, bounds
 
     def sweep(self, translation_step: float, rotation_step: float, seed: int, counter: int, log: bool = False,
-              stats: bool = True, fp64_only: bool = False):
+              stats: bool = True, fp64_only: bool = False, rototranslation: bool = False):
         p = SweepParams()
         p.translation_step, p.rotation_step, p.seed, p.counter = translation_step, rotation_step, seed, counter
-        p.flags = (_lib.SWEEP_LOG if log else 0) | (_lib.SWEEP_FP64_ONLY if fp64_only else 0)
+        p.flags = ((_lib.SWEEP_LOG if log else 0) | (_lib.SWEEP_FP64_ONLY if fp64_only else 0) |
+                   (_lib.SWEEP_ROTOTRANSLATION if rototranslation else 0))
         st = (SweepStats * self.R)() if stats else None
         self._check(self.lib.rp_batch_sweep(self.h, C.byref(p), st))
         return [s.as_dict() for s in st] if stats else None

@@ -109,11 +109,13 @@ class Simulation:
     """Simulation(packing, translationStep, rotationStep, seed, boxScaler) for hard bodies."""
 
     def __init__(self, packing, translation_step: float, rotation_step: float, seed: int,
-                 scaler: BoxScalerDesc | None = None):
+                 scaler: BoxScalerDesc | None = None, rototranslation: bool = False):
+        """TranslationSampler + RotationSampler (a step of 0 disables one), or with
+        ``rototranslation`` one RototranslationSampler(translation_step, rotation_step)."""
         self.lib = _lib.load()
         self.packing = packing
         p = SimParams(temperature=1.0, pressure=0.0, translation_step=translation_step, rotation_step=rotation_step,
-                      seed=seed)
+                      seed=seed, rototranslation=1 if rototranslation else 0)
         if scaler is not None:
             p.scaler = scaler
         self.h = C.c_void_p()

@@ -141,3 +141,20 @@ def test_batch_upload_all_and_states(oracle, engine):
             b.upload_all(bad, rot, boxes)
         b.upload_all(pos, rot, boxes)
         assert b.count_total_overlaps(1) == 0
+
+
+def test_batch_rototranslation_sweeps_replay_on_oracle(oracle, engine):
+    b, cpus = make_batch(SETS["spherocylinders"])
+    with b:
+        for cycle in range(2):
+            st = b.sweep(0.2, 0.3, seed=404, counter=cycle, log=True, rototranslation=True)
+            for k, cpu in enumerate(cpus):
+                moves, codes = b.sweep_log(k)
+                assert st[k]["moves"] == len(moves) == b.sizes[k] and np.all(moves["type"] == 2)
+                _, _, bounds = b.grid(k)
+                want, _ = cpu.replay(moves, bounds)
+                assert np.array_equal(codes, want)
+        for k, cpu in enumerate(cpus):
+            gp, gr, gb = b.state(k)
+            cp, cr, cb = cpu.state()
+            assert np.array_equal(gp, cp) and np.array_equal(gr, cr)

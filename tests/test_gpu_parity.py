@@ -111,6 +111,33 @@ def test_sweep_log_replays_on_oracle(oracle, engine, name, fp64_only):
             assert g.count_total_overlaps(True) == 0
 
 
+@pytest.mark.parametrize("name", ["sc_l2", "sc_l2_dense", "sc_l5", "poly_banana", "poly_dense", "hs_dense",
+                                  "sc_tiny", "hs_tiny"])
+def test_rototranslation_sweeps_replay_on_oracle(oracle, engine, name):
+    # RototranslationSampler moves (translation and rotation in one move, ActiveDomain
+    # checked): every logged move of type 2 replays on the oracle's tryMove
+    cfg = systems.ALL[name]()
+    cpu = cpu_packing(cfg)
+    t = 0.1 if cfg[0] == 0 else 0.2
+    with gpu_packing(cfg) as g:
+        for cycle in range(3):
+            st = g.sweep(t, 0.3, seed=77, counter=cycle, log=True, rototranslation=True)
+            moves, codes = g.sweep_log()
+            _, _, bounds = g.grid()
+            assert st["moves"] == len(moves) == g.n and np.all(moves["type"] == 2)
+            assert st["rotations"] == g.n and st["translations"] == 0
+            want, _ = cpu.replay(moves, bounds)
+            assert np.array_equal(codes, want), f"cycle {cycle}: {np.count_nonzero(codes != want)} codes differ"
+            acc = np.count_nonzero(codes & _lib.CODE_ACCEPTED)
+            assert acc == st["accepted"] and 0 < acc < g.n
+        gp, gr, _ = g.state()
+        cp, cr, _ = cpu.state()
+        assert np.array_equal(gp, cp) and np.array_equal(gr, cr)
+        assert g.count_total_overlaps(True) == 0
+        with pytest.raises(Exception):
+            g.sweep(t, 0.0, seed=1, counter=9, rototranslation=True)  # both steps are needed
+
+
 @pytest.mark.parametrize("name", ["hs_small", "hs_dense", "hs_tiny"])
 def test_sphere_sweeps_with_rotations_replay_on_oracle(oracle, engine, name):
     # the Simulation's samplers rotate spheres too (an orientation change that never overlaps)

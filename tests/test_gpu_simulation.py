@@ -53,6 +53,31 @@ def test_step_adaptation_replays_the_reference_rule(engine, name, steps, scaler)
             assert st["cycles"] == 400 and st["box_moves"] == 400
 
 
+def test_rototranslation_adaptation_replays_the_reference_rule(engine):
+    # one RototranslationSampler: both steps shrink together, and grow with the translation's
+    # factor (its rotation step follows the translation's increase)
+    from rampack_gb300 import simulation as S
+    from rampack_gb300.packing import GpuPacking
+    for name, steps in (("sc_l2", (1.2, 1.5)), ("hs_small", (0.02, 0.05))):
+        kind, prm, pos, rot, box = systems.ALL[name]()
+        with GpuPacking(kind, prm, pos, rot, box) as g, \
+                S.Simulation(g, steps[0], steps[1], 17, rototranslation=True) as sim:
+            ref = Adaptation(g.n, steps[0], steps[1], 0.0, rototranslation=True)
+            last = sim.stats()
+            changed = 0
+            for c in range(350):
+                box_before = last["box"]
+                st = sim.run(1, adjust_steps=True)
+                assert st["translations"] == 0
+                ref.cr.add(st["rotations"] - last["rotations"], st["accepted_rotations"] - last["accepted_rotations"])
+                before = (ref.t, ref.r)
+                ref.evaluate(min(heights(box_before)) / 2)
+                changed += before != (ref.t, ref.r)
+                assert (st["translation_step"], st["rotation_step"]) == (ref.t, ref.r), (name, c)
+                last = st
+            assert changed >= 2
+
+
 def test_step_adaptation_stops_at_the_rotation_cap(engine):
     # spheres accept every rotation: the rotation step grows to pi and stays there
     from rampack_gb300 import simulation as S
@@ -85,6 +110,34 @@ def test_hard_sphere_gas_matches_the_reference_validation(engine, temperature, v
     assert len(samples["number_density"]) == 100
     assert abs(mean - expected) <= 3 * err, (mean, err, expected)
     assert err / mean < 0.03
+
+
+def test_rototranslation_ensemble_matches_separate_samplers(engine):
+    # the same NpT state (spherocylinders l=3 r=0.5 at p=0.5, delta-volume box moves) sampled
+    # with one RototranslationSampler and with translation + rotation samplers: number
+    # density and nematic order agree within 3 combined sigma of block averages
+    from rampack_gb300 import simulation as S
+    from rampack_gb300 import workloads as W
+    from rampack_gb300.packing import GpuPacking
+    kind, prm = W.SPHEROCYLINDER, np.array([3.0, 0.5])
+    pos = W.lattice((6, 6, 3), (2.0, 2.0, 4.2))
+    out = []
+    for rt, seed in ((True, 1234), (False, 4321)):
+        with GpuPacking(kind, prm, pos, W.aligned_rotations(len(pos)), W.diag_box(12.0, 12.0, 12.6)) as g:
+            with S.Simulation(g, 0.5, 1.0, seed, S.delta_volume(10.0), rototranslation=rt) as sim:
+                _, samples = sim.integrate(1.0, 0.5, 5000, 20000, 100, observables=("number_density",
+                                                                                     "nematic_order"))
+        out.append(samples)
+
+    def blocked(x, block=10):
+        x = np.asarray(x)
+        n = len(x) // block
+        b = x[:n * block].reshape(n, block).mean(1)
+        return b.mean(), b.std(ddof=1) / np.sqrt(n)
+
+    for q in ("number_density", "nematic_order"):
+        (m1, e1), (m2, e2) = blocked(out[0][q]), blocked(out[1][q])
+        assert abs(m1 - m2) <= 3 * math.hypot(e1, e2), (q, m1, e1, m2, e2)
 
 
 def test_integrate_records_a_trajectory(engine, tmp_path):
