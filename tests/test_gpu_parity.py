@@ -118,10 +118,12 @@ def test_rototranslation_sweeps_replay_on_oracle(oracle, engine, name):
     # checked): every logged move of type 2 replays on the oracle's tryMove
     cfg = systems.ALL[name]()
     cpu = cpu_packing(cfg)
-    t = 0.1 if cfg[0] == 0 else 0.2
+    t, r = (0.1 if cfg[0] == 0 else 0.2), 0.3
+    if "dense" in name:
+        t, r = 0.03, 0.03  # both parts at once: smaller steps keep some moves accepted
     with gpu_packing(cfg) as g:
         for cycle in range(3):
-            st = g.sweep(t, 0.3, seed=77, counter=cycle, log=True, rototranslation=True)
+            st = g.sweep(t, r, seed=77, counter=cycle, log=True, rototranslation=True)
             moves, codes = g.sweep_log()
             _, _, bounds = g.grid()
             assert st["moves"] == len(moves) == g.n and np.all(moves["type"] == 2)
