@@ -355,6 +355,8 @@ int rp_batch_revert_scaling(void *batch, const uint8_t *mask);
 /* Launch shape: checkerboard cells at least cell_factor (>= 1) interaction ranges high and
  * 2, 4 or 8 warps per block of the sweep kernel (defaults 1.0 and 4). */
 int rp_batch_set_tuning(void *batch, double cell_factor, int32_t warps_per_block);
+/* rp_set_staging_filter for every replica. */
+int rp_batch_set_staging_filter(void *batch, int32_t mode);
 
 /* Every replica's state at once: pos [sum n][3], rot [sum n][9] with the replicas' particles
  * in replica order, boxes [R][9].  The upload copies on the batch's stream (one copy per
@@ -393,6 +395,12 @@ int rp_batch_get_timing(void *batch, double *ms, uint64_t *groups, uint64_t *lau
  * (from several host threads or streams) race and must be serialised by the caller. */
 int rp_count_overlaps_static(const rp_shape_desc *shape, int64_t n, const double *d_pos, const double *d_rot,
                              const double *box9, int early_exit, void *stream, int64_t *out_count);
+
+/* Staging filter of the sweep: candidates of the 26 neighbour cells farther than the
+ * interaction range from every face-slab of the mover's cell (its ActiveDomain) are not
+ * staged; decisions are unchanged.  0 off, 1 (default) where cells are well above the range
+ * (keeps < 90 % of the neighbourhood), 2 wherever no grid dimension has a single cell. */
+int rp_set_staging_filter(void *handle, int32_t mode);
 
 /* ---- the Monte Carlo cycle loop (Simulation for hard bodies) -----------------------
  *

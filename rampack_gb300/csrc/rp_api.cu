@@ -194,6 +194,7 @@ struct Handle {
     double cthr_host[MAX_CEN * MAX_CEN]{};
     double ref_range = 0;
     double *cen64 = nullptr;
+    int stage_mode = 1;  // staging filter: 0 off, 1 where it pays (cells well above the range), 2 wherever valid
     // consistent copy of the FP64 state for asynchronous snapshot downloads
     double *snap64 = nullptr;          // [n][3] positions then [n][9] orientations
     cudaEvent_t snap_free = nullptr;   // recorded when the last download out of snap64 ended
@@ -581,8 +582,30 @@ int setup_grid(Handle *h, GridHost &G, const double *box, const double *shift) {
         RP_CUDA(h, ensure(g.bounds, G.bounds_alloc, nb));
         RP_CUDA(h, cudaMemcpyAsync(g.bounds, bounds.data(), sizeof(double) * nb, cudaMemcpyHostToDevice, h->stream));
     }
+    // staging filter: with cells well above the interaction range a mover (which stays in
+    // its cell, the ActiveDomain) cannot reach much of its neighbour cells; candidates beyond
+    // the range from every face-slab of the home cell are not staged.  Off where a dimension
+    // has a single cell (unbounded domain there) or where it would keep most candidates.
+    double kept = 1.0;
+    {
+        double hb[3];
+        heights_of(box, hb);
+        const double thr = h->range * (1.0 + 1e-3) + 1e-3;
+        g.stage_filter = 0;
+        g.stage_thr = static_cast<float>(thr);
+        for (int d = 0; d < 3; d++) {
+            const double hc = hb[d] / dims[d];
+            g.stage_h[d] = static_cast<float>(hc);
+            kept *= std::min(1.0, (hc + 2.0 * thr) / (3.0 * hc));
+        }
+        // the learned ordering maps partners to unfiltered staging positions
+        const bool allowed = h->stage_mode != 0 && h->order_mode == RP_ORDER_OFF && h->pair_cap == 0;
+        if (dims[0] > 1 && dims[1] > 1 && dims[2] > 1 && allowed && (kept < 0.9 || h->stage_mode == 2))
+            g.stage_filter = 1;
+        if (!g.stage_filter) kept = 1.0;
+    }
     // staged-candidate capacity per warp: mean neighbourhood plus six standard deviations
-    double mean = 27.0 * static_cast<double>(h->n) / static_cast<double>(ncell);
+    double mean = 27.0 * kept * static_cast<double>(h->n) / static_cast<double>(ncell);
     int cap = static_cast<int>(mean + 6.0 * std::sqrt(mean) + 32.0);
     cap = (cap + 31) / 32 * 32;
     int maxcap = static_cast<int>(48 * 1024 / (sweep_smem_per_warp(h->shape.kind, 32, false, h->ncen) / 32));
@@ -1925,6 +1948,13 @@ int rp_mlp_train(void *handle, int32_t epochs, int32_t batch, float lr, uint64_t
     return RP_OK;
 }
 
+int rp_set_staging_filter(void *handle, int32_t mode) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || mode < 0 || mode > 2) return fail(h, RP_ERR_ARG, "bad argument");
+    h->stage_mode = mode;
+    return RP_OK;
+}
+
 int rp_set_ordering(void *handle, int32_t mode, int32_t every) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h || mode < RP_ORDER_OFF || mode > RP_ORDER_DISTANCE || every <= 0) return fail(h, RP_ERR_ARG, "bad argument");
@@ -2075,6 +2105,13 @@ int rp_batch_download_state(void *batch, int32_t replica, double *pos, double *r
     int rc = rp_download_state(h, pos, rot, box9);
     if (rc) b->err = h->err;
     return rc;
+}
+
+int rp_batch_set_staging_filter(void *batch, int32_t mode) {
+    Batch *b = static_cast<Batch *>(batch);
+    if (!b || mode < 0 || mode > 2) return bfail(b, RP_ERR_ARG, "bad argument");
+    for (Handle *h : b->rep) h->stage_mode = mode;
+    return RP_OK;
 }
 
 int rp_batch_upload_states(void *batch, const double *pos, const double *rot, const double *boxes) {

@@ -63,6 +63,12 @@ struct GridDev {
     // polyspheres
     float4 *mcen;         // [n][ncen] FP32 rotated centre offsets, cell order
     float *cthr;          // [2][MAX_CEN^2] FP32 centre-pair thresholds (r_a + r_b)^2 -/+ margin
+    // staging filter (cells well above the interaction range): a neighbour is staged only
+    // if its distance from each face-slab of the home cell, in cell fractions times the
+    // cell height stage_h[d], is at most stage_thr (the range plus a margin)
+    int stage_filter;
+    float stage_h[3];
+    float stage_thr;
 };
 
 struct DevState {

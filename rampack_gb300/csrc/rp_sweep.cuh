@@ -221,7 +221,23 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
         cnt = G.start[nb + 1] - st;
         off = mat32(G.cellmat, (float)ox, (float)oy, (float)oz);
     }
-    int incl = cnt;
+    // with the staging filter, a neighbour cell's particles farther than the interaction
+    // range from the home cell (whose movers stay inside it: the cell is their ActiveDomain)
+    // are left out; the own cell (lane 0) is always staged whole
+    const bool filt = G.stage_filter && !LEARN;
+    auto keep = [&](const float4 &p) {
+        const float3 f = mat32(G.cellinv, p.x + off.x, p.y + off.y, p.z + off.z);
+        const float e0 = fmaxf(fmaxf(-f.x, f.x - 1.f), 0.f) * G.stage_h[0];
+        const float e1 = fmaxf(fmaxf(-f.y, f.y - 1.f), 0.f) * G.stage_h[1];
+        const float e2 = fmaxf(fmaxf(-f.z, f.z - 1.f), 0.f) * G.stage_h[2];
+        return fmaxf(e0, fmaxf(e1, e2)) <= G.stage_thr;
+    };
+    int kcnt = cnt;
+    if (filt && lane > 0 && lane < 27) {
+        kcnt = 0;
+        for (int k = 0; k < cnt; k++) kcnt += keep(G.mpos[st + k]) ? 1 : 0;
+    }
+    int incl = kcnt;
     for (int d = 1; d < 32; d <<= 1) {
         int y = __shfl_up_sync(FULL, incl, d);
         if (lane >= d) incl += y;
@@ -241,15 +257,17 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
         return;
     }
     {
-        int base = incl - cnt;
+        int j = incl - kcnt;
         for (int k = 0; k < cnt; k++) {
             float4 p = G.mpos[st + k];
+            if (filt && lane > 0 && !keep(p)) continue;
             p.x += off.x;
             p.y += off.y;
             p.z += off.z;
-            cpos[base + k] = p;
-            if (KIND == 1) cax[base + k] = G.maxis[st + k];
-            if (KIND == 2) cslot[base + k] = (uint32_t)(st + k);  // its centres stay in the L2-resident mirror
+            cpos[j] = p;
+            if (KIND == 1) cax[j] = G.maxis[st + k];
+            if (KIND == 2) cslot[j] = (uint32_t)(st + k);  // its centres stay in the L2-resident mirror
+            j++;
         }
     }
     // polyspheres: the warp's scratch holds the mover's FP32 centres (wx[0..K)), the

@@ -184,6 +184,10 @@ class GpuPacking:
         self._check(self.lib.rp_sweep(self.h, C.byref(p), C.byref(st) if stats else None))
         return st.as_dict() if stats else None
 
+    def set_staging_filter(self, mode: int = 1):
+        """0 off, 1 where it pays (default), 2 wherever valid (rp_set_staging_filter)."""
+        self._check(self.lib.rp_set_staging_filter(self.h, int(mode)))
+
     def sweep_log(self):
         cnt = C.c_int64()
         self._check(self.lib.rp_sweep_log(self.h, None, None, 0, C.byref(cnt)))
@@ -413,6 +417,10 @@ class BatchPacking:
 
     def set_tuning(self, cell_factor: float = 1.0, warps_per_block: int = 4):
         self._check(self.lib.rp_batch_set_tuning(self.h, cell_factor, warps_per_block))
+
+    def set_staging_filter(self, mode: int = 1):
+        """rp_set_staging_filter for every replica."""
+        self._check(self.lib.rp_batch_set_staging_filter(self.h, int(mode)))
 
     def upload_all(self, pos, rot, boxes):
         """Every replica's state at once (rp_batch_upload_states): pos [sum n, 3] and

@@ -35,9 +35,11 @@ def make_batch(builders, tuning=None):
 
 
 @pytest.mark.parametrize("which", sorted(SETS))
-@pytest.mark.parametrize("tuning", [None, (1.25, 2), (1.1, 8)])
+@pytest.mark.parametrize("tuning", [None, (1.25, 2), (1.1, 8), "filter"])
 def test_batch_sweeps_replay_on_oracle(oracle, engine, which, tuning):
-    b, cpus = make_batch(SETS[which], tuning)
+    b, cpus = make_batch(SETS[which], None if tuning == "filter" else tuning)
+    if tuning == "filter":
+        b.set_staging_filter(2)
     t, r = (0.1, 0.0) if which == "spheres" else (0.2, 0.2)
     with b:
         for cycle in range(2):

@@ -159,6 +159,28 @@ def test_sphere_sweeps_with_rotations_replay_on_oracle(oracle, engine, name):
         assert np.array_equal(gp, cp) and np.array_equal(gr, cr)
 
 
+@pytest.mark.parametrize("name", CASES)
+def test_staging_filter_keeps_every_decision(oracle, engine, name):
+    # candidates left out by the staging filter can never overlap a mover in its cell:
+    # forced on, the logged sweeps replay on the oracle and end in the state of the
+    # unfiltered sweeps
+    cfg = systems.ALL[name]()
+    t, r = steps(cfg)
+    states = []
+    for mode in (2, 0):
+        cpu = cpu_packing(cfg)
+        with gpu_packing(cfg) as g:
+            g.set_staging_filter(mode)
+            for cycle in range(3):
+                g.sweep(t, r, seed=91, counter=cycle, log=True)
+                moves, codes = g.sweep_log()
+                _, _, bounds = g.grid()
+                want, _ = cpu.replay(moves, bounds)
+                assert np.array_equal(codes, want), (mode, cycle)
+            states.append(g.state())
+    assert np.array_equal(states[0][0], states[1][0]) and np.array_equal(states[0][1], states[1][1])
+
+
 @pytest.mark.parametrize("name", ["sc_l2_dense", "poly_dense"])
 def test_fp32_filter_matches_fp64_only(engine, name):
     cfg = systems.ALL[name]()
