@@ -34,8 +34,9 @@ cudaError_t launch_b_count(const BatchRep *T, const int *pbase, int R, int total
                            unsigned long long *out, int *flags, cudaStream_t st);
 size_t batch_smem_per_warp(int kind, int cap);
 cudaError_t launch_b_sweep(const BatchRep *T, const int *item_base, int R, int kind, int k, int *next_item, int cap,
-                           int wpb, int blocks, cudaStream_t st);
-cudaError_t launch_b_overflow(const BatchRep *T, int R, int kind, int k, int cap, cudaStream_t st);
+                           int wpb, int blocks, bool rototranslation, cudaStream_t st);
+cudaError_t launch_b_overflow(const BatchRep *T, int R, int kind, int k, int cap, bool rototranslation,
+                              cudaStream_t st);
 cudaError_t launch_axis_moments(const double *rot64, int64_t n, double *partial, cudaStream_t st);
 cudaError_t launch_fix_check(const DevState &s, const GridDev &g, const double *rotfix, const double *absfix,
                              uint8_t *rejected, unsigned long long *first, cudaStream_t st);
@@ -2344,11 +2345,12 @@ int rp_batch_sweep(void *batch, const rp_sweep_params *p, rp_sweep_stats *stats)
         {
             BGroup grp(b, RP_KERNEL_SWEEP, 1);
             RB_CUDA(b, launch_b_sweep(b->d_table, ib, b->R, b->kind, k, b->item_counters + k, cap, wpb, blocks,
-                                      b->stream));
+                                      types == SWEEP_ROTOTRANSLATION, b->stream));
         }
         {
             BGroup grp(b, RP_KERNEL_OVERFLOW, 1);
-            RB_CUDA(b, launch_b_overflow(b->d_table, b->R, b->kind, k, ovf_cap, b->stream));
+            RB_CUDA(b, launch_b_overflow(b->d_table, b->R, b->kind, k, ovf_cap, types == SWEEP_ROTOTRANSLATION,
+                                         b->stream));
         }
     }
     for (int r = 0; r < b->R; r++) {

@@ -156,7 +156,7 @@ __device__ __forceinline__ void flush_stats(const SweepArgs &A, WarpStats &ws) {
 // Phase k of every replica: persistent warps take checkerboard cells of the whole batch
 // from one counter.  item_base holds the prefix offsets of this phase's cells per replica;
 // every replica's staging capacity is `cap`.
-template <int KIND, int WPB>
+template <int KIND, int WPB, int MODE>
 __global__ void __launch_bounds__(WPB * 32, 16 / WPB)
     k_b_sweep(const BatchRep *T, const int *item_base, int R, int k, int *next_item, int cap) {
     extern __shared__ float4 smem[];
@@ -197,8 +197,8 @@ __global__ void __launch_bounds__(WPB * 32, 16 / WPB)
         cc[2] = local / (act[0] * act[1]);
         for (int d = 0; d < 3; d++) c[d] = ring_cell(G.dims[d], phase_digit(ph, d), cc[d]);
         const int cell = c[0] + G.dims[0] * (c[1] + G.dims[1] * c[2]);
-        sweep_cell<KIND, false, 0>(A, local, cell, cap, A.overflow, A.overflow_count, cpos, cax, qseg, qun, nacc,
-                                       nullptr, nullptr, nullptr, ws);
+        sweep_cell<KIND, false, MODE>(A, local, cell, cap, A.overflow, A.overflow_count, cpos, cax, qseg, qun, nacc,
+                                          nullptr, nullptr, nullptr, ws);
         __syncwarp();
         flush_stats(A, ws);
         __syncwarp();
@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(WPB * 32, 16 / WPB)
 
 // The cells of phase k whose neighbourhood did not fit: one block (one warp, large shared
 // memory) per replica, over that replica's overflow list; the list is emptied afterwards.
-template <int KIND>
+template <int KIND, int MODE>
 __global__ void __launch_bounds__(32) k_b_overflow(const BatchRep *T, int k, int cap) {
     extern __shared__ float4 smem[];
     const SweepArgs &A = T[blockIdx.x].a;
@@ -220,8 +220,8 @@ __global__ void __launch_bounds__(32) k_b_overflow(const BatchRep *T, int k, int
     uint8_t *nacc = reinterpret_cast<uint8_t *>(qun + cap);
     WarpStats ws{};
     for (int q = 0; q < count; q++) {
-        sweep_cell<KIND, false, 0>(A, q, A.overflow[q], cap, nullptr, nullptr, cpos, cax, qseg, qun, nacc,
-                                       nullptr, nullptr, nullptr, ws);
+        sweep_cell<KIND, false, MODE>(A, q, A.overflow[q], cap, nullptr, nullptr, cpos, cax, qseg, qun, nacc,
+                                          nullptr, nullptr, nullptr, ws);
         __syncwarp();
     }
     flush_stats(A, ws);
@@ -229,13 +229,31 @@ __global__ void __launch_bounds__(32) k_b_overflow(const BatchRep *T, int k, int
     (void)k;
 }
 
-template <int KIND, int WPB>
+template <int KIND, int WPB, int MODE>
 cudaError_t launch_b_sweep_t(const BatchRep *T, const int *item_base, int R, int k, int *next_item, int cap,
                              int blocks, cudaStream_t st) {
     const size_t smem = (size_t)WPB * batch_smem_per_warp(KIND, cap);
-    cudaError_t e = cudaFuncSetAttribute(k_b_sweep<KIND, WPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_b_sweep<KIND, WPB, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_b_sweep<KIND, WPB><<<blocks, WPB * 32, smem, st>>>(T, item_base, R, k, next_item, cap);
+    k_b_sweep<KIND, WPB, MODE><<<blocks, WPB * 32, smem, st>>>(T, item_base, R, k, next_item, cap);
+    return cudaGetLastError();
+}
+
+template <int KIND, int MODE>
+cudaError_t launch_b_sweep_w(const BatchRep *T, const int *item_base, int R, int k, int *next_item, int cap, int wpb,
+                             int blocks, cudaStream_t st) {
+    if (wpb == 2) return launch_b_sweep_t<KIND, 2, MODE>(T, item_base, R, k, next_item, cap, blocks, st);
+    if (wpb == 8) return launch_b_sweep_t<KIND, 8, MODE>(T, item_base, R, k, next_item, cap, blocks, st);
+    return launch_b_sweep_t<KIND, 4, MODE>(T, item_base, R, k, next_item, cap, blocks, st);
+}
+
+template <int KIND, int MODE>
+cudaError_t launch_b_overflow_t(const BatchRep *T, int R, int k, int cap, cudaStream_t st) {
+    const size_t smem = batch_smem_per_warp(KIND, cap);
+    cudaError_t e = cudaFuncSetAttribute(k_b_overflow<KIND, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_b_overflow<KIND, MODE><<<R, 32, smem, st>>>(T, k, cap);
     return cudaGetLastError();
 }
 
@@ -273,29 +291,19 @@ size_t batch_smem_per_warp(int kind, int cap) {
 }
 
 cudaError_t launch_b_sweep(const BatchRep *T, const int *item_base, int R, int kind, int k, int *next_item, int cap,
-                           int wpb, int blocks, cudaStream_t st) {
-    if (kind == 0) {
-        if (wpb == 2) return launch_b_sweep_t<0, 2>(T, item_base, R, k, next_item, cap, blocks, st);
-        if (wpb == 8) return launch_b_sweep_t<0, 8>(T, item_base, R, k, next_item, cap, blocks, st);
-        return launch_b_sweep_t<0, 4>(T, item_base, R, k, next_item, cap, blocks, st);
-    }
-    if (wpb == 2) return launch_b_sweep_t<1, 2>(T, item_base, R, k, next_item, cap, blocks, st);
-    if (wpb == 8) return launch_b_sweep_t<1, 8>(T, item_base, R, k, next_item, cap, blocks, st);
-    return launch_b_sweep_t<1, 4>(T, item_base, R, k, next_item, cap, blocks, st);
+                           int wpb, int blocks, bool rototranslation, cudaStream_t st) {
+    if (kind == 0)
+        return rototranslation ? launch_b_sweep_w<0, 3>(T, item_base, R, k, next_item, cap, wpb, blocks, st)
+                               : launch_b_sweep_w<0, 0>(T, item_base, R, k, next_item, cap, wpb, blocks, st);
+    return rototranslation ? launch_b_sweep_w<1, 3>(T, item_base, R, k, next_item, cap, wpb, blocks, st)
+                           : launch_b_sweep_w<1, 0>(T, item_base, R, k, next_item, cap, wpb, blocks, st);
 }
 
-cudaError_t launch_b_overflow(const BatchRep *T, int R, int kind, int k, int cap, cudaStream_t st) {
-    const size_t smem = batch_smem_per_warp(kind, cap);
-    cudaError_t e;
-    if (kind == 0) {
-        e = cudaFuncSetAttribute(k_b_overflow<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e == cudaSuccess) k_b_overflow<0><<<R, 32, smem, st>>>(T, k, cap);
-    } else {
-        e = cudaFuncSetAttribute(k_b_overflow<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e == cudaSuccess) k_b_overflow<1><<<R, 32, smem, st>>>(T, k, cap);
-    }
-    if (e != cudaSuccess) return e;
-    return cudaGetLastError();
+cudaError_t launch_b_overflow(const BatchRep *T, int R, int kind, int k, int cap, bool rototranslation,
+                              cudaStream_t st) {
+    if (kind == 0)
+        return rototranslation ? launch_b_overflow_t<0, 3>(T, R, k, cap, st) : launch_b_overflow_t<0, 0>(T, R, k, cap, st);
+    return rototranslation ? launch_b_overflow_t<1, 3>(T, R, k, cap, st) : launch_b_overflow_t<1, 0>(T, R, k, cap, st);
 }
 
 }  // namespace rp

@@ -176,7 +176,8 @@ __global__ void k_count_poly(DevState s, GridDev g, int early, unsigned long lon
 }
 
 // MODE 1 instantiates the learned-ordering pre-test and the pair-outcome log, MODE 2 the
-// overlap counting (kept out of the plain kernel, whose registers they would crowd)
+// overlap counting, MODE 3 the plain scan of rototranslations (kept out of the plain
+// kernel, whose registers and branches they would crowd)
 template <int KIND, bool LIST, int MODE>
 __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(const SweepArgs A) {
     extern __shared__ float4 smem[];
@@ -305,14 +306,19 @@ cudaError_t launch_sweep(const SweepArgs &a, bool list, int nwarps, cudaStream_t
     if (nwarps <= 0) return cudaSuccess;
     const int wpb = a.work ? 1 : SWEEP_WARPS;
     const bool count = a.s.counting != 0 && a.s.kind != 2;
-    const bool learn = !list && !count && a.s.kind != 2 && (a.partners != nullptr || a.pair_every > 0);
+    // rototranslation sweeps have their own plain scan (no learned pre-test, no pair log)
+    const bool rt = !list && !count && a.types == SWEEP_ROTOTRANSLATION;
+    const bool learn = !list && !count && !rt && a.s.kind != 2 && (a.partners != nullptr || a.pair_every > 0);
     size_t smem = sweep_smem_per_warp(a.s.kind, a.cap, learn, a.s.ncen) * wpb;
     unsigned blocks = (unsigned)((nwarps + wpb - 1) / wpb);
     const int th = wpb * 32;
     if (a.s.kind == 2) {
         if (list) return launch_sweep_t<2, true, 0>(a, blocks, th, smem, st);
-        return launch_sweep_t<2, false, 0>(a, blocks, th, smem, st);
+        return rt ? launch_sweep_t<2, false, 3>(a, blocks, th, smem, st)
+                  : launch_sweep_t<2, false, 0>(a, blocks, th, smem, st);
     }
+    if (rt) return a.s.kind == 0 ? launch_sweep_t<0, false, 3>(a, blocks, th, smem, st)
+                                 : launch_sweep_t<1, false, 3>(a, blocks, th, smem, st);
     if (a.s.kind == 0) {
         if (count) return list ? launch_sweep_t<0, true, 2>(a, blocks, th, smem, st)
                                : launch_sweep_t<0, false, 2>(a, blocks, th, smem, st);

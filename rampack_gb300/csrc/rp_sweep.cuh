@@ -181,6 +181,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                                            uint32_t *cslot, float4 *wx, WarpStats &ws) {
     constexpr bool LEARN = MODE == 1;
     constexpr bool COUNT = MODE == 2;
+    constexpr bool RT = MODE == 3;  // every move a rototranslation (the plain scan otherwise)
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -256,17 +257,29 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
         }
         return;
     }
-    {
+    if (!filt) {
+        // every neighbour staged: positions known from the prefix sum (loads pipeline freely)
+        const int base = incl - cnt;
+        for (int k = 0; k < cnt; k++) {
+            float4 p = G.mpos[st + k];
+            p.x += off.x;
+            p.y += off.y;
+            p.z += off.z;
+            cpos[base + k] = p;
+            if (KIND == 1) cax[base + k] = G.maxis[st + k];
+            if (KIND == 2) cslot[base + k] = (uint32_t)(st + k);  // its centres stay in the L2-resident mirror
+        }
+    } else {
         int j = incl - kcnt;
         for (int k = 0; k < cnt; k++) {
             float4 p = G.mpos[st + k];
-            if (filt && lane > 0 && !keep(p)) continue;
+            if (lane > 0 && !keep(p)) continue;
             p.x += off.x;
             p.y += off.y;
             p.z += off.z;
             cpos[j] = p;
             if (KIND == 1) cax[j] = G.maxis[st + k];
-            if (KIND == 2) cslot[j] = (uint32_t)(st + k);  // its centres stay in the L2-resident mirror
+            if (KIND == 2) cslot[j] = (uint32_t)(st + k);
             j++;
         }
     }
@@ -374,11 +387,12 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
             const int src = mi & 31;
             u4 r = u4{__shfl_sync(FULL, rnd_lane.a, src), __shfl_sync(FULL, rnd_lane.b, src),
                       __shfl_sync(FULL, rnd_lane.c, src), __shfl_sync(FULL, rnd_lane.d, src)};
-            if (A.types == SWEEP_ROTOTRANSLATION) type = 2;
+            const bool rt = RT || (COUNT && A.types == SWEEP_ROTOTRANSLATION);
+            if (rt) type = 2;
             else if (ntypes == 2) type = (r.a >> 31) ? 1 : 0;
             else type = (A.types & 1) ? 0 : 1;
             slot = (int)(((uint64_t)(r.a & 0x7fffffffu) * (uint32_t)occ) >> 31);
-            if (type != 1) {
+            if (type == 0 || rt) {
                 // pm1f takes the top 24 bits of a word: a rototranslation's rotation takes
                 // the low bytes
                 t32 = make_float3(pm1f(r.b) * A.tstep, pm1f(r.c) * A.tstep, pm1f(r.d) * A.tstep);
@@ -386,8 +400,13 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
             }
             if (type != 0) {
                 // a rotation of this sweep's table, or its transpose (the inverse)
-                rot_idx = (type == 1 ? r.b : ((r.b & 0xffu) | ((r.c & 0xffu) << 8))) & A.rtab_mask;
-                rot_inv = ((type == 1 ? r.c : r.d) & 1u) != 0;
+                if (rt) {
+                    rot_idx = ((r.b & 0xffu) | ((r.c & 0xffu) << 8)) & A.rtab_mask;
+                    rot_inv = (r.d & 1u) != 0;
+                } else {
+                    rot_idx = r.b & A.rtab_mask;
+                    rot_inv = (r.c & 1u) != 0;
+                }
                 if (KIND >= 1) {
                     const float4 *R4 = reinterpret_cast<const float4 *>(A.rtab32) + 3 * (size_t)rot_idx;
                     float4 x0 = R4[0], x1 = R4[1], x2 = R4[2];
