@@ -16,6 +16,7 @@
 namespace rp {
 
 cudaError_t launch_rebuild(const DevState &s, const GridDev &g, int32_t *block_sums, cudaStream_t st);
+cudaError_t launch_validate(const DevState &s, cudaStream_t st);
 cudaError_t launch_rescale(const double *src, double *dst, int64_t n, const double *old_inv, const double *new_box,
                            cudaStream_t st);
 cudaError_t launch_count(const DevState &s, const GridDev &g, int early, unsigned long long *out, int *flag,
@@ -196,6 +197,7 @@ struct Handle {
     double ref_range = 0;
     double *cen64 = nullptr;
     int stage_mode = 1;  // staging filter: 0 off, 1 where it pays (cells well above the range), 2 wherever valid
+    bool grid_stale = false;  // an upload validated the state; the cell grid is built when first needed
     // consistent copy of the FP64 state for asynchronous snapshot downloads
     double *snap64 = nullptr;          // [n][3] positions then [n][9] orientations
     cudaEvent_t snap_free = nullptr;   // recorded when the last download out of snap64 ended
@@ -644,6 +646,18 @@ int check_status(Handle *h) {
             return fail(h, RP_ERR_ARG, "an orientation is not a rotation matrix (|O^T O - I| >= 1e-6)");
         return fail(h, (st & ST_CAPACITY) ? RP_ERR_CAPACITY : RP_ERR_DEVICE, buf);
     }
+    return RP_OK;
+}
+
+// The current cell grid, built (unshifted) if an upload left it stale.
+int ensure_grid(Handle *h) {
+    if (!h->grid_stale) return RP_OK;
+    double shift[3] = {0, 0, 0};
+    int rc = setup_grid(h, h->grid[h->gcur], h->box, shift);
+    if (rc) return rc;
+    rc = rebuild(h, h->gcur, h->pcur);
+    if (rc) return rc;
+    h->grid_stale = false;
     return RP_OK;
 }
 
@@ -1096,15 +1110,24 @@ int rp_upload_state(void *handle, const double *pos, const double *rot, const do
     double tt[375];
     translation_table(h->box, tt);
     RP_CUDA(h, cudaMemcpyAsync(h->trans[0], tt, sizeof(tt), cudaMemcpyHostToDevice, h->stream));
-    double shift[3] = {0, 0, 0};
-    int rc = setup_grid(h, h->grid[0], h->box, shift);
-    if (rc) return rc;
     h->has_state = false;
-    h->strict_box = true;
-    rc = rebuild(h, 0, 0);
-    h->strict_box = false;
-    if (rc) return rc;
-    rc = check_status(h);  // the rebuild checks that every particle lies inside the box
+    int rc = RP_OK;
+    if (h->batch_member) {
+        // replicas: the grid at once (the batch reads the replicas' grids directly)
+        double shift[3] = {0, 0, 0};
+        rc = setup_grid(h, h->grid[0], h->box, shift);
+        if (rc) return rc;
+        h->strict_box = true;
+        rc = rebuild(h, 0, 0);
+        h->strict_box = false;
+        if (rc) return rc;
+    } else {
+        // the checks alone; the next sweep builds its own grid, other calls build one first
+        Group grp(h, RP_KERNEL_REBUILD, 1);
+        RP_CUDA(h, launch_validate(dev_state(h), h->stream));
+        h->grid_stale = true;
+    }
+    rc = check_status(h);  // every particle inside the box, orientations rotations
     if (rc) return rc;
     if (h->ncen > 0) {
         Group grp(h, RP_KERNEL_REBUILD, 1);
@@ -1136,6 +1159,10 @@ int rp_count_overlaps(void *handle, int early_exit, int64_t *out_count) {
     if (!h || !out_count) return fail(h, RP_ERR_ARG, "null argument");
     if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
     RP_CUDA(h, cudaSetDevice(h->device));
+    {
+        int rg = ensure_grid(h);  // an upload defers the grid
+        if (rg) return rg;
+    }
     RP_CUDA(h, cudaMemsetAsync(h->count_out, 0, sizeof(unsigned long long), h->stream));
     RP_CUDA(h, cudaMemsetAsync(h->flag, 0, sizeof(int), h->stream));
     DevState s = dev_state(h);
@@ -1178,6 +1205,7 @@ int rp_set_grid(void *handle, const double *shift3, rp_grid_info *info) {
     if (rc) return rc;
     rc = rebuild(h, h->gcur, h->pcur);
     if (rc) return rc;
+    h->grid_stale = false;
     h->can_revert = false;
     if (info) {
         rc = fill_info(h, info);
@@ -1192,6 +1220,10 @@ int rp_get_grid(void *handle, rp_grid_info *info, int32_t *cell_of_particle, dou
     if (!h) return RP_ERR_ARG;
     if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
     RP_CUDA(h, cudaSetDevice(h->device));
+    {
+        int rg = ensure_grid(h);  // an upload defers the grid
+        if (rg) return rg;
+    }
     const GridDev &g = h->grid[h->gcur].d;
     if (info) {
         int rc = fill_info(h, info);
@@ -1225,6 +1257,10 @@ int rp_run_moves(void *handle, const rp_move *moves, int64_t n, uint8_t *out_cod
     if (n <= 0) return RP_OK;
     if (n > (1ll << 31) - 1) return fail(h, RP_ERR_ARG, "too many moves");
     RP_CUDA(h, cudaSetDevice(h->device));
+    {
+        int rg = ensure_grid(h);  // an upload defers the grid
+        if (rg) return rg;
+    }
     const GridDev &g = h->grid[h->gcur].d;
     // validation and phase blocks (runs of equal checkerboard colour)
     std::vector<int> phase(n);
@@ -1328,6 +1364,7 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
     if (rc) return rc;
     rc = rebuild(h, h->gcur, h->pcur);
     if (rc) return rc;
+    h->grid_stale = false;
     const GridDev &g = h->grid[h->gcur].d;
     // translation step limited to half the smallest box height (TranslationSampler.cpp:39-46)
     double hgt[3];
@@ -1469,6 +1506,10 @@ int rp_try_scaling(void *handle, const double *new_box9, double *dE) {
     if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
     if (det3(new_box9) == 0 || volume_of(new_box9) == 0) return fail(h, RP_ERR_ARG, "box volume is zero");
     RP_CUDA(h, cudaSetDevice(h->device));
+    {
+        int rg = ensure_grid(h);  // an upload defers the grid
+        if (rg) return rg;
+    }
     int np = 1 - h->pcur, ng = 1 - h->gcur;
     double new_inv[9];
     inverse3(new_box9, new_inv);
@@ -1668,6 +1709,10 @@ int rp_set_counting(void *handle, int on) {
     if (on && h->shape.kind == RP_SHAPE_POLYSPHERE)
         return fail(h, RP_ERR_UNSUPPORTED, "overlap counting is built for spheres and spherocylinders");
     RP_CUDA(h, cudaSetDevice(h->device));
+    {
+        int rg = ensure_grid(h);  // an upload defers the grid
+        if (rg) return rg;
+    }
     h->counting = on != 0;
     h->can_revert = false;
     if (h->counting) {
@@ -1701,6 +1746,10 @@ int rp_renormalize_orientations(void *handle, int allow_overlaps, int64_t *rejec
     if (!h || !rejected) return fail(h, RP_ERR_ARG, "null argument");
     if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
     RP_CUDA(h, cudaSetDevice(h->device));
+    {
+        int rg = ensure_grid(h);  // an upload defers the grid
+        if (rg) return rg;
+    }
     *rejected = 0;
     h->can_revert = false;
     h->log_valid = false;

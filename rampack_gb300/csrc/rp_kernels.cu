@@ -19,6 +19,12 @@ __global__ void k_assign(DevState s, GridDev g) {
     if (i < s.n) assign_one(s, g, i);
 }
 
+// An uploaded state's checks alone (the cell grid is built when first needed).
+__global__ void k_validate(DevState s) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < s.n) validate_particle(s, i);
+}
+
 // Two-level exclusive scan of the cell counts (4096 cells per block).
 __global__ void k_scan_blocks(const int32_t *count, int32_t *start, int32_t *block_sums, int ncell,
                               int32_t *max_occ) {
@@ -251,6 +257,12 @@ cudaError_t launch_rebuild(const DevState &s, const GridDev &g, int32_t *block_s
     k_scan_add<<<(g.ncell + 255) / 256, 256, 0, st>>>(g.start, block_sums, g.ncell);
     k_scatter<<<nb, tb, 0, st>>>(s, g);
     k_cell_finish<<<(g.ncell + 127) / 128, 128, 0, st>>>(s, g);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_validate(const DevState &s, cudaStream_t st) {
+    if (s.n == 0) return cudaSuccess;
+    k_validate<<<(unsigned)((s.n + 255) / 256), 256, 0, st>>>(s);
     return cudaGetLastError();
 }
 

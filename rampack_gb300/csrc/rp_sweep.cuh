@@ -915,26 +915,37 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
 // Per-particle and per-cell bodies of the cell-list rebuild and of the recount (the
 // single-system kernels in rp_kernels.cu and the batched ones in rp_batch.cu call them)
 // ---------------------------------------------------------------------------------
+// The checks of an uploaded state for one particle: core/Packing.cpp:1069-1075
+// (areShapesWithinBox: relative coordinates in [0, 1)), and orientations that are rotations
+// (the engine's cell sizes and FP32 margins take a unit axis for spherocylinders and an
+// orthonormal matrix for polyspheres).
+__device__ __forceinline__ void validate_one(const DevState &s, int64_t i, const double rr[3]) {
+    if (!(rr[0] >= 0.0 && rr[0] < 1.0 && rr[1] >= 0.0 && rr[1] < 1.0 && rr[2] >= 0.0 && rr[2] < 1.0))
+        atomicOr(s.status, ST_OUTSIDE);
+    const double *o = s.rot64 + 9 * i;
+    bool bad = false;
+    for (int a = 0; a < 3; a++)
+        for (int b = a; b < 3; b++) {
+            if (s.kind == 1 && (a != 2 || b != 2)) continue;
+            if (s.kind == 0) continue;
+            double g2 = o[a] * o[b] + o[3 + a] * o[3 + b] + o[6 + a] * o[6 + b];
+            if (!(fabs(g2 - (a == b ? 1.0 : 0.0)) < 1e-6)) bad = true;
+        }
+    if (bad) atomicOr(s.status, ST_NOT_ROTATION);
+}
+
+__device__ __forceinline__ void validate_particle(const DevState &s, int64_t i) {
+    const d3 r = mv3(s.inv, load_d3(s.pos64 + 3 * i));
+    const double rr[3] = {r.x, r.y, r.z};
+    validate_one(s, i, rr);
+}
+
 __device__ __forceinline__ void assign_one(const DevState &s, const GridDev &g, int64_t i) {
     d3 p = load_d3(s.pos64 + 3 * i);
     d3 r = mv3(s.inv, p);
     double rr[3] = {r.x, r.y, r.z};
-    // core/Packing.cpp:1069-1075 (areShapesWithinBox): relative coordinates in [0, 1)
     if (s.strict_box) {
-        if (!(rr[0] >= 0.0 && rr[0] < 1.0 && rr[1] >= 0.0 && rr[1] < 1.0 && rr[2] >= 0.0 && rr[2] < 1.0))
-            atomicOr(s.status, ST_OUTSIDE);
-        // the engine's cell sizes and FP32 margins take orientations to be rotations: a
-        // unit axis (spherocylinders) or an orthonormal matrix (polyspheres)
-        const double *o = s.rot64 + 9 * i;
-        bool bad = false;
-        for (int a = 0; a < 3; a++)
-            for (int b = a; b < 3; b++) {
-                if (s.kind == 1 && (a != 2 || b != 2)) continue;
-                if (s.kind == 0) continue;
-                double g2 = o[a] * o[b] + o[3 + a] * o[3 + b] + o[6 + a] * o[6 + b];
-                if (!(fabs(g2 - (a == b ? 1.0 : 0.0)) < 1e-6)) bad = true;
-            }
-        if (bad) atomicOr(s.status, ST_NOT_ROTATION);
+        validate_one(s, i, rr);
     } else if (!(fabs(rr[0] - 0.5) < 0.5 + 1e-9 && fabs(rr[1] - 0.5) < 0.5 + 1e-9 && fabs(rr[2] - 0.5) < 0.5 + 1e-9)) {
         atomicOr(s.status, ST_NUMERIC);  // rescaled positions drift at most a few ulp outside
     }
