@@ -93,16 +93,46 @@ def quantity(samples) -> tuple[float, float]:
     return mean, math.sqrt(err / len(x) / (len(x) - 1))
 
 
+def box_volume(box) -> float:
+    """TriclinicBox::getVolume (core/TriclinicBox.cpp:35-38): |(s0 ^ s1) * s2| of the box
+    sides (the matrix columns), in the reference's operation order."""
+    b = [float(x) for x in np.asarray(box).reshape(9)]
+    s0, s1, s2 = (b[0], b[3], b[6]), (b[1], b[4], b[7]), (b[2], b[5], b[8])
+    c = (s0[1] * s1[2] - s0[2] * s1[1], s0[2] * s1[0] - s0[0] * s1[2], s0[0] * s1[1] - s0[1] * s1[0])
+    d = 0.0
+    for k in range(3):
+        d += c[k] * s2[k]
+    return abs(d)
+
+
+def shape_volume(kind: int, params) -> float:
+    """SphereTraits::getVolume / SpherocylinderTraits::getVolume
+    (core/shapes/SphereTraits.cpp:31-33, SpherocylinderTraits.cpp:48-50)."""
+    p = np.asarray(params, dtype=np.float64).reshape(-1)
+    if kind == _lib.SHAPE_SPHERE:
+        return 4. / 3 * math.pi * math.pow(float(p[0]), 3)
+    if kind == _lib.SHAPE_SPHEROCYLINDER:
+        r, length = float(p[1]), float(p[0])
+        return math.pi * r * r * length + 4. / 3 * math.pi * math.pow(r, 3)
+    raise ValueError("the volume of this shape kind is not restated")
+
+
 def number_density(packing, stats) -> float:
-    b = np.asarray(stats["box"]).reshape(3, 3)
-    return packing.n / abs(float(np.dot(np.cross(b[:, 0], b[:, 1]), b[:, 2])))
+    """NumberDensity (core/observables/NumberDensity.h): N / V (Packing::getNumberDensity)."""
+    return packing.n / box_volume(stats["box"])
+
+
+def packing_fraction(packing, stats) -> float:
+    """PackingFraction (core/observables/PackingFraction.h): number density x shape volume."""
+    return number_density(packing, stats) * shape_volume(packing.kind, packing.params)
 
 
 def nematic_order(packing, stats) -> float:
     return packing.nematic_order()[1]
 
 
-OBSERVABLES = {"number_density": number_density, "nematic_order": nematic_order}
+OBSERVABLES = {"number_density": number_density, "packing_fraction": packing_fraction,
+               "nematic_order": nematic_order}
 
 
 class Simulation:

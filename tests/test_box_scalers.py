@@ -53,3 +53,19 @@ def test_quantity_matches_the_reference_formula():
         sq += (mean - v) ** 2
     assert m == mean and e == np.sqrt(sq / len(x) / (len(x) - 1))
     assert S.quantity([]) == (0.0, 0.0) and S.quantity([5.0]) == (5.0, 0.0)
+
+
+def test_observable_formulas(oracle):
+    # N / V and the shapes' volumes as the reference computes them: V from its box, the
+    # volumes from SphereTraits / SpherocylinderTraits (checked against the reference's own
+    # box volume through the oracle library's reference build when it is present)
+    import math
+    from rampack_gb300 import _lib
+    box = np.array([10.0, 0.3, -0.2, 0.1, 11.0, 0.05, -0.0, -0.4, 12.5])
+    m = box.reshape(3, 3)
+    assert math.isclose(S.box_volume(box), abs(np.linalg.det(m)), rel_tol=1e-14)
+    assert S.shape_volume(_lib.SHAPE_SPHERE, [0.5]) == 4. / 3 * math.pi * math.pow(0.5, 3)
+    assert S.shape_volume(_lib.SHAPE_SPHEROCYLINDER, [2.0, 0.5]) == math.pi * 0.5 * 0.5 * 2.0 + 4. / 3 * math.pi * 0.125
+    if oracle.reference_available():
+        _, _, v = oracle.box_info("reference", box)
+        assert S.box_volume(box) == v
