@@ -224,6 +224,30 @@ class CpuPacking:
             raise RuntimeError("draw_moves failed")
         return out
 
+    def draw_flips(self, rng, idxs, n: int, flip_axis=None, origin=(0.0, 0.0, 0.0), domain: int = -1) -> np.ndarray:
+        """FlipSampler moves: the oracle's restatement (flip_axis and origin in the body frame)
+        or the reference's own sampler set up for this packing's shape."""
+        from rampack_gb300._lib import MOVE_DTYPE
+        idxs = np.ascontiguousarray(idxs, dtype=np.int64)
+        out = np.zeros(n, dtype=MOVE_DTYPE)
+        if self.which == "oracle":
+            _, rot, _ = self.state()
+            rot = np.ascontiguousarray(rot)
+            fa = np.ascontiguousarray(flip_axis, dtype=np.float64)
+            go = np.ascontiguousarray(origin, dtype=np.float64)
+            self.lib.rpo_draw_flips.restype = C.c_int
+            self.lib.rpo_draw_flips.argtypes = [_P, _D, _D, _D, _I64, C.c_int64, C.c_int64, C.c_int32, _P]
+            rc = self.lib.rpo_draw_flips(rng, _dp(rot), _dp(fa), _dp(go), idxs.ctypes.data_as(_I64), len(idxs), n,
+                                         domain, out.ctypes.data_as(_P))
+        else:
+            self.lib.ref_draw_flips.restype = C.c_int
+            self.lib.ref_draw_flips.argtypes = [_P, _P, _I64, C.c_int64, C.c_int64, C.c_int32, _P]
+            rc = self.lib.ref_draw_flips(rng, self.h, idxs.ctypes.data_as(_I64), len(idxs), n, domain,
+                                         out.ctypes.data_as(_P))
+        if rc != 0:
+            raise ValueError("flip draw failed")
+        return out
+
     def rng(self, seed: int):
         return self._f("rng_create")(seed)
 

@@ -21,6 +21,7 @@
 #include "core/ObservablesCollector.h"
 #include "core/io/RamtrjPlayer.h"
 #include "core/io/RamtrjRecorder.h"
+#include "core/move_samplers/FlipSampler.h"
 #include "core/move_samplers/RotationSampler.h"
 #include "core/move_samplers/TranslationSampler.h"
 #include "core/shapes/PolysphereTraits.h"
@@ -300,6 +301,34 @@ int ref_draw_moves(void *rp, void *hp, double trans_step, double rot_step, const
         m.uniform = unit(mt);
     }
     return 0;
+}
+
+// FlipSampler (core/move_samplers/FlipSampler.cpp) set up for the handle's shape, drawing
+// `n` moves from the particle list
+int ref_draw_flips(void *rp, void *hp, const int64_t *idxs, int64_t nidx, int64_t n, int32_t domain, ref_move *out) {
+    auto &mt = static_cast<ref_rng *>(rp)->mt;
+    auto *h = static_cast<Handle *>(hp);
+    try {
+        FlipSampler fs(1);
+        fs.setupForShapeTraits(*h->traits);
+        std::vector<std::size_t> list(idxs, idxs + nidx);
+        std::uniform_real_distribution<double> unit;
+        for (int64_t i = 0; i < n; i++) {
+            auto data = fs.sampleMove(*h->pk, list, mt);
+            ref_move &m = out[i];
+            std::memset(&m, 0, sizeof(m));
+            m.particle = static_cast<int32_t>(data.particleIdx);
+            m.type = data.moveType == MoveSampler::MoveType::TRANSLATION ? 0
+                     : data.moveType == MoveSampler::MoveType::ROTATION ? 1 : 2;
+            m.domain = domain;
+            for (int q = 0; q < 3; q++) m.translation[q] = data.translation[q];
+            store_m(data.rotation, m.rotation);
+            m.uniform = unit(mt);
+        }
+        return 0;
+    } catch (const std::exception &) {
+        return -1;
+    }
 }
 
 struct ref_sim_params {

@@ -270,6 +270,44 @@ int rpo_draw_moves(void *rp, double trans_step, double rot_step, const double *b
     return 0;
 }
 
+// FlipSampler::sampleMove (core/move_samplers/FlipSampler.cpp:18-41): a particle from the
+// list, then a rotation by pi about its flip axis (the body-frame flip axis turned by its
+// orientation and normalised); with a geometric origin away from zero the move is a
+// rototranslation that keeps the origin in place.  `rot` holds every particle's orientation.
+int rpo_draw_flips(void *rp, const double *rot, const double *flip_axis, const double *origin, const int64_t *idxs,
+                   int64_t nidx, int64_t n, int32_t domain, rpo_move *out) {
+    auto &mt = static_cast<rpo_rng *>(rp)->mt;
+    if (nidx <= 0) return -1;
+    const V3 fa{flip_axis[0], flip_axis[1], flip_axis[2]}, go{origin[0], origin[1], origin[2]};
+    constexpr double EPS = 1e-14;
+    const bool origin_zero = norm2(go) < EPS * EPS;
+    std::uniform_real_distribution<double> unit;
+    for (int64_t i = 0; i < n; i++) {
+        std::uniform_int_distribution<std::size_t> pd(0, static_cast<std::size_t>(nidx) - 1);
+        const int64_t pid = idxs[pd(mt)];
+        const M3 o = load_m3(rot + 9 * pid);
+        const V3 a = mv(o, fa);
+        const M3 r = rotation_axis_angle(vdiv(a, std::sqrt(norm2(a))), M_PI);
+        rpo_move &m = out[i];
+        std::memset(&m, 0, sizeof(m));
+        V3 t{};
+        if (origin_zero) {
+            m.type = 1;
+        } else {
+            m.type = 2;
+            const V3 g = mv(o, go);
+            const V3 rg = mv(r, g);
+            t = {-rg[0] + g[0], -rg[1] + g[1], -rg[2] + g[2]};
+        }
+        m.particle = static_cast<int32_t>(pid);
+        m.domain = domain;
+        std::memcpy(m.translation, t.data(), sizeof(m.translation));
+        std::memcpy(m.rotation, r.data(), sizeof(m.rotation));
+        m.uniform = unit(mt);
+    }
+    return 0;
+}
+
 // ---- the cycle loop (CPU baseline and ensemble checks) ----
 struct rpo_sim_params {
     double temperature, pressure, translation_step, rotation_step;

@@ -6,6 +6,7 @@ Run in a checkout where the reference sources are present:
     python tests/golden/make_golden.py        # every fixture
     python tests/golden/make_golden.py io     # the snapshot / trajectory files only
     python tests/golden/make_golden.py box    # the box-move proposal streams only
+    python tests/golden/make_golden.py flips  # the FlipSampler moves only
 
 Every expected value below is produced by the reference library (oracle/_ref/librpref.so:
 rampack's Packing, NeighbourGrid, SpherocylinderTraits, samplers and Simulation compiled
@@ -320,9 +321,26 @@ def gen_box_proposals():
     print("box proposals:", len(SCALERS), "scalers")
 
 
+def gen_flips():
+    """FlipSampler moves of the reference's own sampler (spherocylinders: flips about the
+    body y axis, the primary axis z crossed with x)."""
+    import systems
+    cfg = systems.sc_l2()
+    ref = po.CpuPacking("reference", *cfg)
+    idx = np.arange(0, len(cfg[2]), 3)
+    r = ref.rng(2468)
+    mv = ref.draw_flips(r, idx, 300)
+    ref.rng_free(r)
+    np.savez_compressed(os.path.join(HERE, "flips.npz"), moves=mv, idx=idx, rot=cfg[3], seed=2468)
+    print("flips:", len(mv))
+
+
 def main():
     if not po.reference_available():
         po.build(reference=True)
+    if sys.argv[1:] == ["flips"]:
+        gen_flips()
+        return
     if sys.argv[1:] == ["io"]:
         gen_io(np.random.default_rng(20261204))
         return
@@ -343,6 +361,7 @@ def main():
             rotation_step=0.2, box_kind=1, box_step=0.005, pressure=1.5, domains=(2, 2, 2), threads=8)
     gen_io(np.random.default_rng(20261204))
     gen_box_proposals()
+    gen_flips()
 
 
 if __name__ == "__main__":

@@ -140,6 +140,36 @@ def test_rototranslation_sweeps_replay_on_oracle(oracle, engine, name):
             g.sweep(t, 0.0, seed=1, counter=9, rototranslation=True)  # both steps are needed
 
 
+@pytest.mark.parametrize("name", ["sc_l2", "sc_l2_dense", "sc_tiny"])
+def test_flip_moves(oracle, engine, name):
+    # FlipSampler moves (drawn per cell by the oracle's restatement of the reference's
+    # sampler, pinned by tests/test_oracle_golden.py) through the move-list entry
+    from rampack_gb300.packing import cell_phase
+    cfg = systems.ALL[name]()
+    cpu = cpu_packing(cfg)
+    with gpu_packing(cfg) as g:
+        for rnd, shift in enumerate([(0.0, 0.0, 0.0), (0.37, 0.71, 0.05)]):
+            info = g.set_grid(shift)
+            _, cells, bounds = g.grid()
+            phase = [cell_phase(info["dims"], c) for c in range(info["num_cells"])]
+            rng = cpu.rng(55 + rnd)
+            chunks = []
+            for ph in sorted(set(phase)):
+                for cell in range(info["num_cells"]):
+                    idx = np.nonzero(cells == cell)[0]
+                    if phase[cell] == ph and len(idx):
+                        chunks.append(cpu.draw_flips(rng, idx, len(idx), flip_axis=(0.0, 1.0, 0.0), domain=cell))
+            cpu.rng_free(rng)
+            moves = np.concatenate(chunks)
+            codes = g.run_moves(moves)
+            want, _ = cpu.replay(moves, bounds)
+            assert np.array_equal(codes, want)
+            assert np.count_nonzero(codes & _lib.CODE_ACCEPTED) > 0
+        gp, gr, _ = g.state()
+        cp, cr, _ = cpu.state()
+        assert np.array_equal(gp, cp) and np.array_equal(gr, cr)
+
+
 @pytest.mark.parametrize("name", ["hs_small", "hs_dense", "hs_tiny"])
 def test_sphere_sweeps_with_rotations_replay_on_oracle(oracle, engine, name):
     # the Simulation's samplers rotate spheres too (an orientation change that never overlaps)

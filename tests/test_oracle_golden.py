@@ -49,6 +49,20 @@ def test_proposal_stream(oracle):
     assert mv.tobytes() == g["moves"].tobytes()
 
 
+def test_flip_stream(oracle):
+    # FlipSampler (core/move_samplers/FlipSampler.cpp:18-41) for spherocylinders: the body
+    # flip axis is the primary axis z crossed with x, i.e. y (ShapeGeometry::findFlipAxis)
+    g = load("flips.npz")
+    import systems
+    kind, prm, pos, _, box = systems.sc_l2()
+    pk = po.CpuPacking("oracle", kind, prm, pos, g["rot"], box)
+    r = pk.rng(int(g["seed"]))
+    mv = pk.draw_flips(r, g["idx"], len(g["moves"]), flip_axis=(0.0, 1.0, 0.0))
+    pk.rng_free(r)
+    assert mv.tobytes() == g["moves"].tobytes()
+    assert np.all(mv["type"] == 1)
+
+
 @pytest.mark.parametrize("name", ["hs", "sc_l2", "sc_l5"])
 def test_system(oracle, name):
     g = load(f"system_{name}.npz")
