@@ -54,3 +54,26 @@ def test_full_size_fp32_filter_equals_fp64(engine):
             states.append(g.state())
             assert g.count_total_overlaps(True) == 0
     assert all(np.array_equal(a, b) for a, b in zip(states[0], states[1]))
+
+
+def test_replicas_64_sweeps_replay_on_oracle(oracle, engine):
+    # the 64-replica workload (408,345 particles in two batches): one logged batched sweep,
+    # every replica replayed on its own oracle packing
+    from rampack_gb300 import workloads as W
+    from rampack_gb300.packing import BatchPacking
+    reps = W.config_replicas_64(1234)
+    for kind in (W.SPHERE, W.SPHEROCYLINDER):
+        idx = [i for i, r in enumerate(reps) if r[0] == kind]
+        prm = reps[idx[0]][1]
+        t, r = (0.2, 0.0) if kind == W.SPHERE else (0.2, 0.2)
+        with BatchPacking(kind, prm, [reps[i][2:5] for i in idx]) as b:
+            b.sweep(t, r, seed=77, counter=3, log=True)
+            for k, i in enumerate(idx):
+                cpu = po.CpuPacking("oracle", kind, prm, *reps[i][2:5], threads=1)
+                moves, codes = b.sweep_log(k)
+                _, _, bounds = b.grid(k)
+                want, _ = cpu.replay(moves, bounds)
+                assert np.array_equal(codes, want), (kind, k)
+                gp, gr, _ = b.state(k)
+                cp, cr, _ = cpu.state()
+                assert np.array_equal(gp, cp) and np.array_equal(gr, cr)
