@@ -62,9 +62,6 @@ namespace {
 
 constexpr int OVF_WARPS = 152;          // overflow rerun: one warp per block, grid-stride over cells
 constexpr size_t OVF_SMEM = 200 * 1024; // shared memory of one overflow warp
-// batch prefix arrays: particles, cells, then the items of each phase for the replicas of
-// the light class and of the heavy class (staging capacity above what 16 warps per SM hold)
-constexpr int BASES_ROWS = 2 + 2 * MAX_PHASES;
 
 struct GridHost {
     GridDev d{};
@@ -788,7 +785,7 @@ struct Batch {
     cudaStream_t stream = nullptr;
     std::vector<Handle *> rep;
     BatchRep *d_table = nullptr;                      // [R]
-    int *d_bases = nullptr;                           // pbase, cbase, item_base of each phase and class: BASES_ROWS x (R + 1)
+    int *d_bases = nullptr;                           // pbase, cbase, item_base of each phase: (2 + MAX_PHASES) x (R + 1)
     double *d_bounds = nullptr;                       // packed ActiveDomain bounds
     int64_t d_bounds_alloc = 0;
     // two pinned staging sets used alternately; a set is rewritten only after its copies ran
@@ -803,16 +800,13 @@ struct Batch {
     int cur = 0;
     double *rtab64 = nullptr;
     float *rtab32 = nullptr;
-    int32_t *item_counters = nullptr;                 // [2][MAX_PHASES]: light and heavy class
-    cudaStream_t stream2 = nullptr;                   // the heavy class's sweep launches
-    cudaEvent_t fork[MAX_PHASES]{}, join[MAX_PHASES]{};
+    int32_t *item_counters = nullptr;                 // [MAX_PHASES]
     unsigned long long *stats = nullptr;              // [R][NUM_COUNTERS]
     uint32_t *status = nullptr;                       // [R]
     unsigned long long *counts = nullptr, *h_counts = nullptr;  // [R]
     int *flags = nullptr, *h_flags = nullptr;         // [R]
     int wpb = 4;
     int smem_optin = 48 * 1024;                       // largest dynamic shared memory per block
-    int smem_sm = 228 * 1024;                         // shared memory per SM
     uint64_t launches = 0;
     Timing tm;
     std::string err;
@@ -896,7 +890,7 @@ int batch_copy(Batch *b) {
     for (Handle *h : b->rep) nb += static_cast<int64_t>(h->grid[h->gcur].bounds_host.size());
     RB_CUDA(b, cudaMemcpyAsync(b->d_bounds, S.bounds, sizeof(double) * nb, cudaMemcpyHostToDevice, b->stream));
     RB_CUDA(b, cudaMemcpyAsync(b->d_table, S.table, sizeof(BatchRep) * b->R, cudaMemcpyHostToDevice, b->stream));
-    RB_CUDA(b, cudaMemcpyAsync(b->d_bases, S.bases, sizeof(int) * BASES_ROWS * (b->R + 1), cudaMemcpyHostToDevice,
+    RB_CUDA(b, cudaMemcpyAsync(b->d_bases, S.bases, sizeof(int) * (2 + MAX_PHASES) * (b->R + 1), cudaMemcpyHostToDevice,
                                b->stream));
     RB_CUDA(b, cudaEventRecord(S.done, b->stream));
     S.pending = true;
@@ -2045,19 +2039,13 @@ int rp_batch_create(const rp_shape_desc *shape, int32_t replicas, const int64_t 
     if (cudaSetDevice(device) != cudaSuccess) return bail(RP_ERR_CUDA);
     cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, device);
     cudaDeviceGetAttribute(&b->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
-    cudaDeviceGetAttribute(&b->smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device);
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(RP_ERR_CUDA);
-    if (cudaStreamCreateWithFlags(&b->stream2, cudaStreamNonBlocking) != cudaSuccess) return bail(RP_ERR_CUDA);
-    for (int k = 0; k < MAX_PHASES; k++)
-        if (cudaEventCreateWithFlags(&b->fork[k], cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming) != cudaSuccess)
-            return bail(RP_ERR_CUDA);
     const int R = replicas;
     bool ok = cudaMalloc(&b->d_table, sizeof(BatchRep) * R) == cudaSuccess &&
-              cudaMalloc(&b->d_bases, sizeof(int) * BASES_ROWS * (R + 1)) == cudaSuccess &&
+              cudaMalloc(&b->d_bases, sizeof(int) * (2 + MAX_PHASES) * (R + 1)) == cudaSuccess &&
               cudaMalloc(&b->rtab64, sizeof(double) * 9 * ROT_TABLE) == cudaSuccess &&
               cudaMalloc(&b->rtab32, sizeof(float) * 12 * ROT_TABLE) == cudaSuccess &&
-              cudaMalloc(&b->item_counters, sizeof(int32_t) * 2 * MAX_PHASES) == cudaSuccess &&
+              cudaMalloc(&b->item_counters, sizeof(int32_t) * MAX_PHASES) == cudaSuccess &&
               cudaMalloc(&b->stats, sizeof(unsigned long long) * NUM_COUNTERS * R) == cudaSuccess &&
               cudaMalloc(&b->status, sizeof(uint32_t) * R) == cudaSuccess &&
               cudaMalloc(&b->counts, sizeof(unsigned long long) * R) == cudaSuccess &&
@@ -2066,7 +2054,7 @@ int rp_batch_create(const rp_shape_desc *shape, int32_t replicas, const int64_t 
               cudaMallocHost(&b->h_flags, sizeof(int) * R) == cudaSuccess;
     for (auto &S : b->stage)
         ok = ok && cudaMallocHost(&S.table, sizeof(BatchRep) * R) == cudaSuccess &&
-             cudaMallocHost(&S.bases, sizeof(int) * BASES_ROWS * (R + 1)) == cudaSuccess &&
+             cudaMallocHost(&S.bases, sizeof(int) * (2 + MAX_PHASES) * (R + 1)) == cudaSuccess &&
              cudaEventCreateWithFlags(&S.done, cudaEventDisableTiming) == cudaSuccess;
     if (!ok) return bail(RP_ERR_CUDA);
     cudaMemset(b->stats, 0, sizeof(unsigned long long) * NUM_COUNTERS * R);
@@ -2130,14 +2118,6 @@ int rp_batch_destroy(void *batch) {
         if (S.done) cudaEventDestroy(S.done);
     }
     b->tm.release();
-    if (b->stream2) {
-        cudaStreamSynchronize(b->stream2);
-        cudaStreamDestroy(b->stream2);
-    }
-    for (int k = 0; k < MAX_PHASES; k++) {
-        if (b->fork[k]) cudaEventDestroy(b->fork[k]);
-        if (b->join[k]) cudaEventDestroy(b->join[k]);
-    }
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return RP_OK;
@@ -2345,34 +2325,11 @@ int rp_batch_sweep(void *batch, const rp_sweep_params *p, rp_sweep_stats *stats)
             }
         }
     }
-    // staging capacities: the light class holds the replicas whose neighbourhoods fit the
-    // shared memory of 16 resident warps per SM (the register limit of the sweep kernel);
-    // the others (small boxes with coarse cells) form the heavy class, launched beside it
-    // with the larger capacity; two warps per block must fit either way
-    const size_t per_cap = batch_smem_per_warp(b->kind, 32) / 32;
-    const int fit = static_cast<int>(static_cast<size_t>(b->smem_optin) / 2 / per_cap) / 32 * 32;
-    cap = std::min(cap, fit);
-    int cap_light = 0, cap_heavy = 0;
-    std::vector<uint8_t> heavy(b->R, 0);
+    // the staging capacity of every replica: two warps per block must fit
     {
-        const int blocks_sm = 16 / b->wpb;
-        const size_t per_block = static_cast<size_t>(b->smem_sm) / blocks_sm - 1024;
-        const size_t per_warp = per_block / b->wpb;
-        const size_t fixed = batch_smem_per_warp(b->kind, 0);
-        const int light_max = per_warp > fixed ? static_cast<int>((per_warp - fixed) / per_cap) / 32 * 32 : 0;
-        for (int r = 0; r < b->R; r++) {
-            const int c = std::min(b->rep[r]->grid[b->rep[r]->gcur].cap, fit);
-            if (c <= light_max) cap_light = std::max(cap_light, c);
-            else {
-                heavy[r] = 1;
-                cap_heavy = std::max(cap_heavy, c);
-            }
-        }
-        if (cap_light == 0) {  // every replica heavy: one class
-            std::fill(heavy.begin(), heavy.end(), 0);
-            cap_light = cap_heavy;
-            cap_heavy = 0;
-        }
+        const size_t per_cap = batch_smem_per_warp(b->kind, 32) / 32;
+        const int fit = static_cast<int>(static_cast<size_t>(b->smem_optin) / 2 / per_cap) / 32 * 32;
+        cap = std::min(cap, fit);
     }
     int total_items = 0, total_p = 0, total_c = 0;
     int rc = batch_tables(b, total_items, total_p, total_c);
@@ -2381,7 +2338,7 @@ int rp_batch_sweep(void *batch, const rp_sweep_params *p, rp_sweep_stats *stats)
     for (int r = 0; r < b->R; r++) {
         Handle *h = b->rep[r];
         SweepArgs &a = T[r].a;
-        a.cap = heavy[r] ? cap_heavy : cap_light;
+        a.cap = cap;
         a.seed = replica_seed(p->seed, r);
         a.counter = p->counter;
         a.tstep = static_cast<float>(tstep[r]);
@@ -2398,23 +2355,19 @@ int rp_batch_sweep(void *batch, const rp_sweep_params *p, rp_sweep_stats *stats)
         T[r].nphases = static_cast<int>(phases[r].size());
         for (int k = 0; k < MAX_PHASES; k++) T[r].phases[k] = k < T[r].nphases ? phases[r][k] : 0;
     }
-    // the cells of phase k of every replica of a class, numbered consecutively (the other
-    // class's replicas take no numbers)
-    std::vector<int> phase_total(maxph, 0), heavy_total(maxph, 0);
+    // the cells of phase k of every replica, numbered consecutively
+    std::vector<int> phase_total(maxph, 0);
     {
         int *bases = b->stage[b->cur].bases;
         for (int k = 0; k < maxph; k++) {
             int *ibk = bases + (2 + k) * (b->R + 1);
-            int *ihk = bases + (2 + MAX_PHASES + k) * (b->R + 1);
-            ibk[0] = ihk[0] = 0;
+            ibk[0] = 0;
             for (int r = 0; r < b->R; r++) {
                 int act[3];
                 const int items = k < T[r].nphases ? phase_cells(b->rep[r]->grid[b->rep[r]->gcur].d, T[r].phases[k], act) : 0;
-                ibk[r + 1] = ibk[r] + (heavy[r] ? 0 : items);
-                ihk[r + 1] = ihk[r] + (heavy[r] ? items : 0);
+                ibk[r + 1] = ibk[r] + items;
             }
             phase_total[k] = ibk[b->R];
-            heavy_total[k] = ihk[b->R];
         }
     }
     rc = batch_copy(b);
@@ -2429,41 +2382,24 @@ int rp_batch_sweep(void *batch, const rp_sweep_params *p, rp_sweep_stats *stats)
             RB_CUDA(b, launch_rot_table(b->rtab64, b->rtab32, ROT_TABLE, p->seed, p->counter,
                                         static_cast<float>(p->rotation_step), b->stream));
     }
-    RB_CUDA(b, cudaMemsetAsync(b->item_counters, 0, sizeof(int32_t) * 2 * MAX_PHASES, b->stream));
-    // fewer warps per block when the staging of a class's capacity per warp would not fit
-    auto warps_for = [&](int c) {
-        int w = b->wpb;
-        while (w > 2 && static_cast<size_t>(w) * batch_smem_per_warp(b->kind, c) > static_cast<size_t>(b->smem_optin))
-            w /= 2;
-        return w;
-    };
-    const int wpb = warps_for(cap_light), wpb_h = cap_heavy ? warps_for(cap_heavy) : wpb;
-    const bool rt = types == SWEEP_ROTOTRANSLATION;
+    RB_CUDA(b, cudaMemsetAsync(b->item_counters, 0, sizeof(int32_t) * MAX_PHASES, b->stream));
+    // fewer warps per block when the staging of `cap` candidates per warp would not fit
+    int wpb = b->wpb;
+    while (wpb > 2 && static_cast<size_t>(wpb) * batch_smem_per_warp(b->kind, cap) > static_cast<size_t>(b->smem_optin))
+        wpb /= 2;
     const int ovf_cap = static_cast<int>(OVF_SMEM / (batch_smem_per_warp(b->kind, 32) / 32)) / 32 * 32;
     for (int k = 0; k < maxph; k++) {
         const int *ib = b->d_bases + (2 + k) * (b->R + 1);
-        const int *ih = b->d_bases + (2 + MAX_PHASES + k) * (b->R + 1);
-        const int blocks = std::max(1, std::min((phase_total[k] + wpb - 1) / wpb, b->num_sms * (16 / wpb)));
+        int blocks = std::max(1, std::min((phase_total[k] + wpb - 1) / wpb, b->num_sms * (16 / wpb)));
         {
-            BGroup grp(b, RP_KERNEL_SWEEP, heavy_total[k] > 0 ? 2 : 1);
-            if (heavy_total[k] > 0) {
-                // the heavy class on the second stream, beside the light one; joined before
-                // the phase's overflow rerun
-                const int hblocks = std::max(1, std::min((heavy_total[k] + wpb_h - 1) / wpb_h, b->num_sms * (16 / wpb_h)));
-                RB_CUDA(b, cudaEventRecord(b->fork[k], b->stream));
-                RB_CUDA(b, cudaStreamWaitEvent(b->stream2, b->fork[k], 0));
-                RB_CUDA(b, launch_b_sweep(b->d_table, ih, b->R, b->kind, k, b->item_counters + MAX_PHASES + k,
-                                          cap_heavy, wpb_h, hblocks, rt, b->stream2));
-                RB_CUDA(b, cudaEventRecord(b->join[k], b->stream2));
-            }
-            if (phase_total[k] > 0)
-                RB_CUDA(b, launch_b_sweep(b->d_table, ib, b->R, b->kind, k, b->item_counters + k, cap_light, wpb,
-                                          blocks, rt, b->stream));
-            if (heavy_total[k] > 0) RB_CUDA(b, cudaStreamWaitEvent(b->stream, b->join[k], 0));
+            BGroup grp(b, RP_KERNEL_SWEEP, 1);
+            RB_CUDA(b, launch_b_sweep(b->d_table, ib, b->R, b->kind, k, b->item_counters + k, cap, wpb, blocks,
+                                      types == SWEEP_ROTOTRANSLATION, b->stream));
         }
         {
             BGroup grp(b, RP_KERNEL_OVERFLOW, 1);
-            RB_CUDA(b, launch_b_overflow(b->d_table, b->R, b->kind, k, ovf_cap, rt, b->stream));
+            RB_CUDA(b, launch_b_overflow(b->d_table, b->R, b->kind, k, ovf_cap, types == SWEEP_ROTOTRANSLATION,
+                                         b->stream));
         }
     }
     for (int r = 0; r < b->R; r++) {
