@@ -454,6 +454,8 @@ int rp_sim_run(void *sim, int64_t cycles, int adjust_steps, rp_sim_stats *stats)
 int rp_sim_get_stats(void *sim, rp_sim_stats *stats);
 int rp_sim_set_steps(void *sim, double translation_step, double rotation_step, double box_step);
 int rp_sim_set_conditions(void *sim, double temperature, double pressure);
+/* The cycle count a continued run starts from (the next sweep's Philox counter). */
+int rp_sim_set_cycles(void *sim, uint64_t cycles);
 const char *rp_sim_last_error(void *sim);
 int rp_sim_destroy(void *sim);
 

@@ -146,6 +146,7 @@ SIGNATURES = {
     "rp_sim_get_stats": (C.c_int, [_P, C.POINTER(SimStats)]),
     "rp_sim_set_steps": (C.c_int, [_P, C.c_double, C.c_double, C.c_double]),
     "rp_sim_set_conditions": (C.c_int, [_P, C.c_double, C.c_double]),
+    "rp_sim_set_cycles": (C.c_int, [_P, C.c_uint64]),
     "rp_sim_last_error": (C.c_char_p, [_P]),
     "rp_sim_destroy": (C.c_int, [_P]),
     "rp_box_proposals": (C.c_int, [C.POINTER(BoxScalerDesc), C.c_uint64, _D, C.c_int64, _D, _D]),

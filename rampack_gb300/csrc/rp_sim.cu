@@ -391,6 +391,13 @@ int rp_sim_set_steps(void *sim, double translation_step, double rotation_step, d
     return RP_OK;
 }
 
+int rp_sim_set_cycles(void *sim, uint64_t cycles) {
+    Sim *s = static_cast<Sim *>(sim);
+    if (!s) return RP_ERR_ARG;
+    s->cycles = cycles;
+    return RP_OK;
+}
+
 int rp_sim_set_conditions(void *sim, double temperature, double pressure) {
     Sim *s = static_cast<Sim *>(sim);
     if (!s || !(temperature > 0)) return RP_ERR_ARG;

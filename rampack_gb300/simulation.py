@@ -144,6 +144,9 @@ class Simulation:
         ``rototranslation`` one RototranslationSampler(translation_step, rotation_step)."""
         self.lib = _lib.load()
         self.packing = packing
+        self.translation_step, self.rotation_step = translation_step, rotation_step
+        self.rototranslation = rototranslation
+        self.has_scaler = scaler is not None and scaler.kind != _lib.SCALER_NONE
         p = SimParams(temperature=1.0, pressure=0.0, translation_step=translation_step, rotation_step=rotation_step,
                       seed=seed, rototranslation=1 if rototranslation else 0)
         if scaler is not None:
@@ -191,6 +194,46 @@ class Simulation:
         st = SimStats()
         self._check(self.lib.rp_sim_get_stats(self.h, C.byref(st)))
         return st.as_dict()
+
+    # ---- continuation (the reference's --continue through RAMSNAP aux entries) ----
+    def aux_info(self) -> dict:
+        """FileSnapshotWriter::prepareAuxInfo (frontend/FileSnapshotWriter.cpp:46-61):
+        "cycles" and "step.<sampler>.<step>" entries, step sizes at max_digits10."""
+        st = self.stats()
+        aux = {"cycles": str(int(st["cycles"]))}
+        if self.rototranslation:
+            aux["step.rototranslation.translation"] = "%.17g" % st["translation_step"]
+            aux["step.rototranslation.rotation"] = "%.17g" % st["rotation_step"]
+        else:
+            if self.translation_step > 0:
+                aux["step.translation.translation"] = "%.17g" % st["translation_step"]
+            if self.rotation_step > 0:
+                aux["step.rotation.rotation"] = "%.17g" % st["rotation_step"]
+        if self.has_scaler:
+            aux["step.scaling.scaling"] = "%.17g" % st["box_step"]
+        return aux
+
+    def store(self, path) -> dict:
+        """The packing as RAMSNAP with the aux entries a continued run needs."""
+        aux = self.aux_info()
+        self.packing.store(path, aux)
+        return aux
+
+    def restore(self, path) -> dict:
+        """PackingLoader's continuation (frontend/PackingLoader.cpp:177-223): the state, the
+        cycle count and the step sizes of a RAMSNAP file this packing's size."""
+        aux = self.packing.restore(path)
+        if "cycles" not in aux:
+            raise EngineError(-8, "No 'cycles' key in RAMSNAP metadata")
+        st = self.stats()
+        t = float(aux.get("step.rototranslation.translation" if self.rototranslation else "step.translation.translation",
+                          st["translation_step"]))
+        r = float(aux.get("step.rototranslation.rotation" if self.rototranslation else "step.rotation.rotation",
+                          st["rotation_step"]))
+        b = float(aux.get("step.scaling.scaling", st["box_step"]))
+        self.set_steps(t, r, b)
+        self._check(self.lib.rp_sim_set_cycles(self.h, int(aux["cycles"])))
+        return aux
 
     def integrate(self, temperature: float, pressure: float, thermalisation_cycles: int, averaging_cycles: int,
                   averaging_every: int, observables=("number_density",), snapshot_every: int = 0, recorder=None):
