@@ -396,6 +396,13 @@ int rp_batch_get_timing(void *batch, double *ms, uint64_t *groups, uint64_t *lau
 int rp_count_overlaps_static(const rp_shape_desc *shape, int64_t n, const double *d_pos, const double *d_rot,
                              const double *box9, int early_exit, void *stream, int64_t *out_count);
 
+/* Packing::toggleWalls (core/Packing.cpp:1075-1084): bit i of `mask` puts hard walls on the
+ * two planes across box side i (through the origin and through the far corner; periodic
+ * images are kept, as in the reference).  Every move, recount, box move and orientation fix
+ * then counts wall overlaps (core/Packing.cpp:1086-1139) after the pair overlaps. */
+int rp_set_walls(void *handle, int32_t mask);
+int rp_batch_set_walls(void *batch, int32_t mask);
+
 /* Staging filter of the sweep: candidates of the 26 neighbour cells farther than the
  * interaction range from every face-slab of the mover's cell (its ActiveDomain) are not
  * staged; decisions are unchanged.  0 off, 1 (default) where cells are well above the range

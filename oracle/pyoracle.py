@@ -168,6 +168,12 @@ class CpuPacking:
     def count_overlaps(self, early_exit: bool = False) -> int:
         return int(self._f("count_overlaps")(self.h, 1 if early_exit else 0))
 
+    def set_walls(self, mask: int) -> None:
+        """Packing::toggleWalls: bit i puts hard walls across box side i."""
+        f = self._f("set_walls")
+        f.restype, f.argtypes = None, [_P, C.c_int]
+        f(self.h, int(mask))
+
     def set_counting(self, on: bool) -> None:
         self._f("set_counting")(self.h, 1 if on else 0)
 

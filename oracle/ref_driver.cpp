@@ -128,6 +128,11 @@ int64_t ref_count_overlaps(void *hp, int early) {
     return static_cast<int64_t>(h->pk->countTotalOverlaps(h->traits->getInteraction(), early != 0));
 }
 
+void ref_set_walls(void *hp, int mask) {
+    auto *h = static_cast<Handle *>(hp);
+    h->pk->toggleWalls({(mask & 1) != 0, (mask & 2) != 0, (mask & 4) != 0});
+}
+
 void ref_set_counting(void *hp, int on) {
     auto *h = static_cast<Handle *>(hp);
     h->pk->toggleOverlapCounting(on != 0, h->traits->getInteraction());

@@ -91,6 +91,14 @@ int64_t rpo_count_overlaps(void *hp, int early) {
     return static_cast<int64_t>(h->pk->count_total_overlaps(h->inter, early != 0));
 }
 
+// Packing::toggleWalls (core/Packing.cpp:1081-1084): bit i walls the planes spanned by the
+// box sides other than side i
+void rpo_set_walls(void *hp, int mask) {
+    auto *h = static_cast<Handle *>(hp);
+    for (int i = 0; i < 3; i++) h->pk->has_wall[i] = ((mask >> i) & 1) != 0;
+    h->pk->has_any_walls = (mask & 7) != 0;
+}
+
 void rpo_set_counting(void *hp, int on) {
     auto *h = static_cast<Handle *>(hp);
     h->pk->set_counting(on != 0, h->inter);

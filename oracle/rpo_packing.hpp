@@ -65,6 +65,17 @@ struct Interaction {
         return 2 * std::sqrt(m2) + r;
     }
     std::size_t num_centres() const { return kind == POLYSPHERE ? centres.size() : 0; }
+
+    // overlapWithWall: SphereTraits.cpp:67-75, SpherocylinderTraits.cpp:56-73 (either cap
+    // closer to the wall plane than the radius), PolysphereTraits.cpp:129-136 (centre idx)
+    bool overlap_with_wall(const V3 &pos, const M3 &rot, std::size_t idx, const V3 &origin, const V3 &wall) const {
+        if (kind == SPHERE) return dot(wall, sub(pos, origin)) < radius;
+        if (kind == POLYSPHERE) return dot(wall, sub(pos, origin)) < radii[idx];
+        V3 half = vscale(column(rot, 2), length / 2);
+        if (dot(wall, sub(add(pos, half), origin)) < radius) return true;
+        if (dot(wall, sub(sub(pos, half), origin)) < radius) return true;
+        return false;
+    }
     bool convex() const { return kind != POLYSPHERE; }
 
     // SpherocylinderTraits.cpp:23-25
@@ -285,6 +296,8 @@ public:
     std::size_t num_centres = 0;
     std::size_t move_threads = 1, scaling_threads = 1;
     bool counting = false;
+    std::array<bool, 3> has_wall{};      // Packing::toggleWalls (core/Packing.cpp:1075-1084)
+    bool has_any_walls = false;
     std::size_t num_overlaps = 0;
     std::vector<std::size_t> last_altered;
     std::vector<int> last_delta;
@@ -417,6 +430,64 @@ public:
                 cnt += po;
             }
         }
+        std::size_t wall = 0;
+        if (has_any_walls) wall = count_particle_wall_overlaps(temp, inter, early);
+        return cnt + wall;
+    }
+
+    // Packing::countParticleWallOverlaps (core/Packing.cpp:1086-1139): the wall pair of each
+    // walled axis spans the other two box sides; a particle meets the nearer one (through the
+    // origin, or through the far corner) when its position lies within half the total
+    // interaction range of it
+    std::size_t count_particle_wall_overlaps(std::size_t idx, const Interaction &inter, bool early) const {
+        std::size_t cnt = 0;
+        const auto s = box.sides();
+        const V3 origin{0, 0, 0};
+        const V3 further = add(add(add(origin, s[0]), s[1]), s[2]);
+        const double half = inter.total_range() / 2;
+        for (std::size_t i = 0; i < 3; i++) {
+            if (!has_wall[i]) continue;
+            const V3 c = cross(s[(i + 1) % 3], s[(i + 2) % 3]);
+            const V3 wall = vdiv(c, std::sqrt(norm2(c)));
+            const V3 &pos = shapes[idx].pos;
+            const M3 &rot = shapes[idx].rot;
+            V3 o, w;
+            if (dot(pos, wall) < half) {
+                o = origin;
+                w = wall;
+            } else if (dot(sub(further, pos), wall) < half) {
+                o = further;
+                w = {-wall[0], -wall[1], -wall[2]};
+            } else {
+                continue;
+            }
+            if (num_centres == 0) {
+                if (inter.overlap_with_wall(pos, rot, 0, o, w)) {
+                    if (early) return 1;
+                    cnt++;
+                }
+            } else {
+                for (std::size_t k = 0; k < num_centres; k++) {
+                    const V3 cp = add(pos, centres[idx * num_centres + k]);
+                    if (inter.overlap_with_wall(cp, rot, k, o, w)) {
+                        if (early) return 1;
+                        cnt++;
+                    }
+                }
+            }
+        }
+        return cnt;
+    }
+
+    // Packing::countWallOverlaps (core/Packing.cpp:561-580)
+    std::size_t count_wall_overlaps(const Interaction &inter, bool early) const {
+        if (!has_any_walls) return 0;
+        std::size_t cnt = 0;
+        for (std::size_t i = 0; i < size(); i++) {
+            std::size_t c = count_particle_wall_overlaps(i, inter, early);
+            if (early && c > 0) return c;
+            cnt += c;
+        }
         return cnt;
     }
 
@@ -529,7 +600,7 @@ public:
                     cnt += po;
                 }
         }
-        return cnt;
+        return cnt + count_wall_overlaps(inter, early);
     }
 
     // ----- moves: Packing.cpp:84-164, :304-323 -----

@@ -140,6 +140,8 @@ SIGNATURES = {
     "rp_batch_set_timing": (C.c_int, [_P, C.c_int]),
     "rp_batch_get_timing": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "rp_set_staging_filter": (C.c_int, [_P, C.c_int32]),
+    "rp_set_walls": (C.c_int, [_P, C.c_int32]),
+    "rp_batch_set_walls": (C.c_int, [_P, C.c_int32]),
     "rp_batch_set_staging_filter": (C.c_int, [_P, C.c_int32]),
     "rp_sim_create": (C.c_int, [_P, C.POINTER(SimParams), C.POINTER(C.c_void_p)]),
     "rp_sim_run": (C.c_int, [_P, C.c_int64, C.c_int, C.POINTER(SimStats)]),

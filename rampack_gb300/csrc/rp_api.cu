@@ -39,7 +39,7 @@ cudaError_t launch_b_sweep(const BatchRep *T, const int *item_base, int R, int k
 cudaError_t launch_b_overflow(const BatchRep *T, int R, int kind, int k, int cap, bool rototranslation,
                               cudaStream_t st);
 cudaError_t launch_axis_moments(const double *rot64, int64_t n, double *partial, cudaStream_t st);
-cudaError_t launch_fix_check(const DevState &s, const GridDev &g, const double *rotfix, const double *absfix,
+cudaError_t launch_fix_check(const DevState &s, const GridDev &g, const double *rotfix, const double *cenfix, const double *absfix,
                              uint8_t *rejected, unsigned long long *first, cudaStream_t st);
 cudaError_t launch_fix_commit(const DevState &s, const double *rotfix, const double *cenfix, const double *absfix,
                               int64_t from, int64_t to, cudaStream_t st);
@@ -193,6 +193,8 @@ struct Handle {
     // neighbour-grid cell), rotated and absolute centres, exact pair thresholds
     int ncen = 0;
     double cbody[3 * MAX_CEN]{}, crad[MAX_CEN]{};
+    int walls = 0;            // Packing::toggleWalls mask (bit i: walls across box side i)
+    double total_range = 0;   // Interaction::getTotalRangeRadius (core/Interaction.cpp:55-70)
     double cthr_host[MAX_CEN * MAX_CEN]{};
     double ref_range = 0;
     double *cen64 = nullptr;
@@ -374,6 +376,30 @@ DevState dev_state(Handle *h) {
     }
     s.counting = h->counting ? 1 : 0;
     s.overlaps = h->d_overlaps;
+    s.walls = h->walls;
+    if (h->walls) {
+        // Packing::countParticleWallOverlaps (core/Packing.cpp:1089-1101): the box sides
+        // (TriclinicBox::getSides: box · e_i, accumulated from zero), the far corner as their
+        // sum from the origin, each wall's unit normal (side i+1 ^ side i+2).normalized()
+        d3 sd[3];
+        for (int j = 0; j < 3; j++) sd[j] = d3{h->box[j] + 0.0, h->box[3 + j] + 0.0, h->box[6 + j] + 0.0};
+        d3 far{0.0, 0.0, 0.0};
+        for (int j = 0; j < 3; j++) far = add3(far, sd[j]);
+        s.wall_far[0] = far.x;
+        s.wall_far[1] = far.y;
+        s.wall_far[2] = far.z;
+        for (int i = 0; i < 3; i++) {
+            const d3 c = cross3(sd[(i + 1) % 3], sd[(i + 2) % 3]);
+            const double nrm = std::sqrt(norm2(c));
+            s.wall_vec[i][0] = c.x / nrm;
+            s.wall_vec[i][1] = c.y / nrm;
+            s.wall_vec[i][2] = c.z / nrm;
+        }
+        s.wall_half = h->total_range / 2;
+        s.wall_half_len = h->shape.kind == RP_SHAPE_SPHEROCYLINDER ? h->shape.length / 2 : 0.0;
+        for (int k = 0; k < MAX_CEN; k++)
+            s.wall_radius[k] = h->ncen > 0 ? h->crad[k] : h->shape.radius;
+    }
     // ---- FP32 filter margins for the current grid ----
     const GridHost &g = h->grid[h->gcur];
     double lrow = 0;
@@ -978,6 +1004,7 @@ int rp_create(const rp_shape_desc *shape, int64_t n, int device, void **handle) 
         ex.cap_half = 0.5 * end * l;
     }
     h->ref_range = h->range;
+    h->total_range = h->range;  // no interaction centres
     h->ex = ex;
     return create_common(h, n, device, handle);
 }
@@ -1011,6 +1038,16 @@ int rp_create_polysphere(int32_t num_centres, const double *centres, const doubl
         }
     h->shape.radius = rmax;
     h->ref_range = 2 * rmax;                   // PolysphereTraits.cpp:115-120 (the neighbour-grid cell)
+    {
+        // Interaction::getTotalRangeRadius: 2 sqrt(max |centre|^2) + range
+        double m2 = 0;
+        for (int b = 0; b < num_centres; b++) {
+            const double r2 = centres[3 * b] * centres[3 * b] + centres[3 * b + 1] * centres[3 * b + 1] +
+                              centres[3 * b + 2] * centres[3 * b + 2];
+            if (r2 > m2) m2 = r2;
+        }
+        h->total_range = 2 * std::sqrt(m2) + h->ref_range;
+    }
     // cells of the checkerboard: two bodies farther apart than twice the largest reach
     // |c| + r cannot touch (rotated centres keep |c| up to FP64 rounding)
     h->range = 2 * reach * (1.0 + 1e-12);
@@ -1792,7 +1829,7 @@ int rp_renormalize_orientations(void *handle, int allow_overlaps, int64_t *rejec
     {
         Group grp(h, RP_KERNEL_FIX, 2);
         RP_CUDA(h, launch_fix_prepare(s, h->cbody_dev, rotfix, cenfix, absfix, h->stream));
-        RP_CUDA(h, launch_fix_check(s, g, rotfix, absfix, rej, words, h->stream));
+        RP_CUDA(h, launch_fix_check(s, g, rotfix, cenfix, absfix, rej, words, h->stream));
     }
     unsigned long long first = 0;
     RP_CUDA(h, cudaMemcpyAsync(&first, words, sizeof(first), cudaMemcpyDeviceToHost, h->stream));
@@ -1998,6 +2035,13 @@ int rp_mlp_train(void *handle, int32_t epochs, int32_t batch, float lr, uint64_t
     return RP_OK;
 }
 
+int rp_set_walls(void *handle, int32_t mask) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || mask < 0 || mask > 7) return fail(h, RP_ERR_ARG, "wall mask outside 0..7");
+    h->walls = mask;
+    return RP_OK;
+}
+
 int rp_set_staging_filter(void *handle, int32_t mode) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h || mode < 0 || mode > 2) return fail(h, RP_ERR_ARG, "bad argument");
@@ -2079,6 +2123,7 @@ int rp_batch_create(const rp_shape_desc *shape, int32_t replicas, const int64_t 
             ex.cap_half = 0.5 * end * l;
         }
         h->ref_range = h->range;
+        h->total_range = h->range;
         h->ex = ex;
         h->status = b->status + r;
         h->counters = b->stats + NUM_COUNTERS * r;
@@ -2155,6 +2200,13 @@ int rp_batch_download_state(void *batch, int32_t replica, double *pos, double *r
     int rc = rp_download_state(h, pos, rot, box9);
     if (rc) b->err = h->err;
     return rc;
+}
+
+int rp_batch_set_walls(void *batch, int32_t mask) {
+    Batch *b = static_cast<Batch *>(batch);
+    if (!b || mask < 0 || mask > 7) return bfail(b, RP_ERR_ARG, "wall mask outside 0..7");
+    for (Handle *h : b->rep) h->walls = mask;
+    return RP_OK;
 }
 
 int rp_batch_set_staging_filter(void *batch, int32_t mode) {

@@ -90,6 +90,14 @@ __device__ __forceinline__ bool overlaps_pair(const DevState &s, d3 pi, const do
     return false;
 }
 
+// The fixed particle against the hard walls (its position unchanged, its orientation and
+// rotated centres fixed).
+__device__ __forceinline__ bool overlaps_walls(const DevState &s, d3 pi, const double *ri, const double *ci) {
+    if (!s.walls) return false;
+    return wall_overlap_count(s.walls, s.wall_vec, s.wall_far, s.wall_half, s.ncen ? 2 : s.kind, s.wall_radius,
+                              s.wall_half_len, pi, d3{ri[2], ri[5], ri[8]}, ci, s.ncen, true) != 0;
+}
+
 // The candidates of particle i: the particles of its cell and the 26 around it.
 template <typename F>
 __device__ __forceinline__ bool any_candidate(const GridDev &g, int64_t i, F &&f) {
@@ -107,8 +115,8 @@ __device__ __forceinline__ bool any_candidate(const GridDev &g, int64_t i, F &&f
 
 // All particles at once, every earlier neighbour assumed fixed.  rejected[i] = 1 if the
 // fixed particle overlaps; first = the smallest rejected index.
-__global__ void k_fix_check(DevState s, GridDev g, const double *rotfix, const double *absfix, uint8_t *rejected,
-                            unsigned long long *first) {
+__global__ void k_fix_check(DevState s, GridDev g, const double *rotfix, const double *cenfix, const double *absfix,
+                            uint8_t *rejected, unsigned long long *first) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= s.n) return;
     const d3 pi = ld3(s.pos64 + 3 * i);
@@ -119,6 +127,7 @@ __global__ void k_fix_check(DevState s, GridDev g, const double *rotfix, const d
         if (j == i) return false;
         return overlaps_pair(s, pi, ri, ai, j, j < i ? fixed : current);
     });
+    if (!ov) ov = overlaps_walls(s, pi, ri, s.ncen ? cenfix + 3 * (size_t)i * s.ncen : nullptr);
     rejected[i] = ov ? 1 : 0;
     if (ov) atomicMin(first, (unsigned long long)i);
 }
@@ -168,6 +177,11 @@ __global__ void k_fix_serial(DevState s, GridDev g, const double *rotfix, const 
                 }
             }
         }
+        if (!ov) {
+            int w = 0;
+            if (lane == 0) w = overlaps_walls(s, pi, ri, s.ncen ? cenfix + 3 * (size_t)i * s.ncen : nullptr) ? 1 : 0;
+            ov = __shfl_sync(0xffffffffu, w, 0) != 0;
+        }
         if (ov) {
             rej++;
         } else if (lane < 9) {
@@ -199,9 +213,9 @@ cudaError_t launch_fresh_centres(const DevState &s, const double *cbody, cudaStr
     return cudaGetLastError();
 }
 
-cudaError_t launch_fix_check(const DevState &s, const GridDev &g, const double *rotfix, const double *absfix,
+cudaError_t launch_fix_check(const DevState &s, const GridDev &g, const double *rotfix, const double *cenfix, const double *absfix,
                              uint8_t *rejected, unsigned long long *first, cudaStream_t st) {
-    k_fix_check<<<(unsigned)((s.n + 127) / 128), 128, 0, st>>>(s, g, rotfix, absfix, rejected, first);
+    k_fix_check<<<(unsigned)((s.n + 127) / 128), 128, 0, st>>>(s, g, rotfix, cenfix, absfix, rejected, first);
     return cudaGetLastError();
 }
 

@@ -286,6 +286,46 @@ RP_HD u4 philox(u4 ctr, uint32_t k0, uint32_t k1) {
     return ctr;
 }
 
+// Wall overlaps of one body (Packing::countParticleWallOverlaps, core/Packing.cpp:1086-1139,
+// with SphereTraits.cpp:67-75, SpherocylinderTraits.cpp:56-73, PolysphereTraits.cpp:129-136):
+// per walled axis the nearer wall, if within `half` of the position; `axis` is the
+// spherocylinder axis, `cen` the polysphere's rotated centres (ncen of them).  Returns the
+// number of overlaps, or 1 at the first with early exit.
+RP_HD int wall_overlap_count(int walls, const double (*wall_vec)[3], const double *wall_far, double half, int kind,
+                             const double *radius, double half_len, d3 pos, d3 axis, const double *cen, int ncen,
+                             bool early) {
+    int cnt = 0;
+    for (int i = 0; i < 3; i++) {
+        if (!((walls >> i) & 1)) continue;
+        const d3 w{wall_vec[i][0], wall_vec[i][1], wall_vec[i][2]};
+        const d3 far{wall_far[0], wall_far[1], wall_far[2]};
+        d3 o{0.0, 0.0, 0.0}, ww = w;
+        if (dot3(pos, w) < half) {
+        } else if (dot3(sub3(far, pos), w) < half) {
+            o = far;
+            ww = d3{-w.x, -w.y, -w.z};
+        } else {
+            continue;
+        }
+        if (kind == 0) {
+            if (dot3(ww, sub3(pos, o)) < radius[0]) cnt++;
+        } else if (kind == 1) {
+            const d3 h{dmul(axis.x, half_len), dmul(axis.y, half_len), dmul(axis.z, half_len)};
+            if (dot3(ww, sub3(add3(pos, h), o)) < radius[0] || dot3(ww, sub3(sub3(pos, h), o)) < radius[0]) cnt++;
+        } else {
+            for (int k = 0; k < ncen; k++) {
+                const d3 cp = add3(pos, d3{cen[3 * k], cen[3 * k + 1], cen[3 * k + 2]});
+                if (dot3(ww, sub3(cp, o)) < radius[k]) {
+                    cnt++;
+                    if (early) return 1;
+                }
+            }
+        }
+        if (early && cnt) return 1;
+    }
+    return cnt;
+}
+
 // Uniform float in [0, 1) from the top 24 bits; uniform float in [-1, 1).
 RP_HD float u01f(uint32_t x) { return static_cast<float>(x >> 8) * (1.0f / 16777216.0f); }
 RP_HD float pm1f(uint32_t x) { return static_cast<float>(x >> 8) * (1.0f / 8388608.0f) - 1.0f; }

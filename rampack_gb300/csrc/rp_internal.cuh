@@ -101,6 +101,17 @@ struct DevState {
     // accepted moves update by their overlap delta
     int counting;
     unsigned long long *overlaps;
+    // hard walls (Packing::toggleWalls): bit i walls the planes across box side i, whose unit
+    // normal (side i+1 x side i+2, normalised) is wall_vec[i]; the far wall passes through
+    // the corner wall_far (the sum of the sides); a particle meets the wall nearer to it
+    // within wall_half (half the total interaction range); wall_radius holds the sphere,
+    // spherocylinder or polysphere-centre radii and wall_half_len half the cylinder length
+    int walls;
+    double wall_vec[3][3];
+    double wall_far[3];
+    double wall_half;
+    double wall_half_len;
+    double wall_radius[RP_MAX_CENTRES];
 };
 
 constexpr int MAX_CEN = RP_MAX_CENTRES;

@@ -778,6 +778,16 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                 ws.fp64 += nun;
                 if (ov) code = 1;
             }
+            // hard walls: the mover at its exact new state (Packing::countParticleOverlaps adds
+            // the wall overlaps after the pairs, core/Packing.cpp:424-428)
+            if (!COUNT && S.walls && code == 0) {
+                int wov = 0;
+                if (lane == 0)
+                    wov = wall_overlap_count(S.walls, S.wall_vec, S.wall_far, S.wall_half, KIND, S.wall_radius,
+                                             S.wall_half_len, pnew, anew, KIND == 2 ? wcen : nullptr,
+                                             KIND == 2 ? S.ncen : 0, true);
+                if (__shfl_sync(FULL, wov, 0)) code = 1;
+            }
         }
 
         // ---- overlap counting: the mover's overlaps before and after the move, every
@@ -804,6 +814,12 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                 if (ca == 2) ca = exact_pair(S, pnew, anew, pj, da) ? 1 : 0;
                 before += cb == 1 ? 1 : 0;
                 after += ca == 1 ? 1 : 0;
+            }
+            if (S.walls && lane == 0) {
+                before += wall_overlap_count(S.walls, S.wall_vec, S.wall_far, S.wall_half, KIND, S.wall_radius,
+                                             S.wall_half_len, pc64, ac64, nullptr, 0, false);
+                after += wall_overlap_count(S.walls, S.wall_vec, S.wall_far, S.wall_half, KIND, S.wall_radius,
+                                            S.wall_half_len, pnew, anew, nullptr, 0, false);
             }
             for (int d = 16; d > 0; d >>= 1) {
                 before += __shfl_xor_sync(FULL, before, d);
@@ -1053,6 +1069,15 @@ __device__ __forceinline__ void count_one(const DevState &s, const GridDev &g, i
             }
         }
     }
+    // Packing::countTotalOverlaps adds every particle's wall overlaps (core/Packing.cpp:558-580)
+    if (s.walls && !(early && *(volatile int *)flag)) {
+        const double *r = s.rot64 + 9 * (size_t)pid;
+        const int w = wall_overlap_count(s.walls, s.wall_vec, s.wall_far, s.wall_half, KIND, s.wall_radius,
+                                         s.wall_half_len, load_d3(s.pos64 + 3 * (size_t)pid), d3{r[2], r[5], r[8]},
+                                         nullptr, 0, early != 0);
+        if (w && early) atomicExch(flag, 1);
+        cnt += (unsigned long long)w;
+    }
     if (cnt) atomicAdd(out, cnt);
 }
 
@@ -1101,6 +1126,13 @@ __device__ __forceinline__ void count_poly_one(const DevState &s, const GridDev 
                 }
             }
         }
+    }
+    if (s.walls && !(early && *(volatile int *)flag)) {
+        const int w = wall_overlap_count(s.walls, s.wall_vec, s.wall_far, s.wall_half, 2, s.wall_radius, 0.0,
+                                         load_d3(s.pos64 + 3 * (size_t)pid), d3{0, 0, 0},
+                                         s.cen64 + 3 * (size_t)pid * K, K, early != 0);
+        if (w && early) atomicExch(flag, 1);
+        cnt += (unsigned long long)w;
     }
     if (cnt) atomicAdd(out, cnt);
 }

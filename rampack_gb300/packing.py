@@ -184,6 +184,10 @@ class GpuPacking:
         self._check(self.lib.rp_sweep(self.h, C.byref(p), C.byref(st) if stats else None))
         return st.as_dict() if stats else None
 
+    def set_walls(self, mask: int):
+        """Packing::toggleWalls: bit i puts hard walls across box side i (rp_set_walls)."""
+        self._check(self.lib.rp_set_walls(self.h, int(mask)))
+
     def set_staging_filter(self, mode: int = 1):
         """0 off, 1 where it pays (default), 2 wherever valid (rp_set_staging_filter)."""
         self._check(self.lib.rp_set_staging_filter(self.h, int(mode)))
@@ -417,6 +421,10 @@ class BatchPacking:
 
     def set_tuning(self, cell_factor: float = 1.0, warps_per_block: int = 4):
         self._check(self.lib.rp_batch_set_tuning(self.h, cell_factor, warps_per_block))
+
+    def set_walls(self, mask: int):
+        """rp_set_walls for every replica."""
+        self._check(self.lib.rp_batch_set_walls(self.h, int(mask)))
 
     def set_staging_filter(self, mode: int = 1):
         """rp_set_staging_filter for every replica."""

@@ -7,6 +7,7 @@ Run in a checkout where the reference sources are present:
     python tests/golden/make_golden.py io     # the snapshot / trajectory files only
     python tests/golden/make_golden.py box    # the box-move proposal streams only
     python tests/golden/make_golden.py flips  # the FlipSampler moves only
+    python tests/golden/make_golden.py walls  # the hard-wall packings only
 
 Every expected value below is produced by the reference library (oracle/_ref/librpref.so:
 rampack's Packing, NeighbourGrid, SpherocylinderTraits, samplers and Simulation compiled
@@ -335,9 +336,57 @@ def gen_flips():
     print("flips:", len(mv))
 
 
+def state_digest(pos, rot) -> np.ndarray:
+    import hashlib
+    h = hashlib.sha256(np.ascontiguousarray(pos, dtype=np.float64).tobytes())
+    h.update(np.ascontiguousarray(rot, dtype=np.float64).tobytes())
+    return np.frombuffer(h.digest(), dtype=np.uint8)
+
+
+# hard walls: (system, wall mask, translation step, rotation step)
+WALLS = [("hs_small", 1, 0.1, 0.0), ("sc_l2", 5, 0.2, 0.2), ("poly_banana", 2, 0.2, 0.2), ("sc_l2_dense", 7, 0.2, 0.2)]
+
+
+def gen_walls():
+    """Packings with hard walls (Packing::toggleWalls) through the reference: overlap counts,
+    a replayed move list (no ActiveDomain), a box move, and the same moves in counting mode."""
+    import systems
+    out = {}
+    for i, (name, mask, t, r) in enumerate(WALLS):
+        cfg = systems.ALL[name]()
+        kind, prm, pos, rot, box = cfg
+        ref = po.CpuPacking("reference", *cfg)
+        ref.set_walls(mask)
+        out[f"w{i}_counts"] = np.array([ref.count_overlaps(False), ref.count_overlaps(True)])
+        rng = ref.rng(500 + i)
+        n = len(pos)
+        mv = ref.draw_moves(rng, t, r, np.arange(n), n, 800)
+        ref.rng_free(rng)
+        codes, _ = ref.replay(mv)
+        p1, r1, b1 = ref.state()
+        nb = (b1.reshape(3, 3) * 0.995).reshape(9)
+        out[f"w{i}_moves"], out[f"w{i}_codes"] = mv, codes
+        # final states as SHA-256 digests of their bytes (the arrays would be megabytes)
+        out[f"w{i}_state"] = state_digest(p1, r1)
+        out[f"w{i}_box_dE"] = np.array(ref.try_scaling(nb))
+        out[f"w{i}_box_state"] = state_digest(*ref.state()[:2])
+        if kind != po.POLYSPHERE:
+            cnt = po.CpuPacking("reference", *cfg)
+            cnt.set_walls(mask)
+            cnt.set_counting(True)
+            c2, d2 = cnt.replay(mv)
+            out[f"w{i}_count_codes"], out[f"w{i}_count_deltas"] = c2, d2
+            out[f"w{i}_count_final"] = np.array(cnt.cached_overlaps())
+    np.savez_compressed(os.path.join(HERE, "walls.npz"), **out)
+    print("walls:", len(WALLS), "systems")
+
+
 def main():
     if not po.reference_available():
         po.build(reference=True)
+    if sys.argv[1:] == ["walls"]:
+        gen_walls()
+        return
     if sys.argv[1:] == ["flips"]:
         gen_flips()
         return
@@ -362,6 +411,7 @@ def main():
     gen_io(np.random.default_rng(20261204))
     gen_box_proposals()
     gen_flips()
+    gen_walls()
 
 
 if __name__ == "__main__":
