@@ -56,6 +56,10 @@ def parse():
                     help="replicas-64: fixed launch shape 'cell_factor,warps_per_block' instead of autotuning")
     ap.add_argument("--ordering", action="store_true",
                     help="compare the plain scan with centre-distance and learned partner ordering")
+    ap.add_argument("--correlation", action="store_true",
+                    help="time the pair density correlation g(r) of the workload's packing")
+    ap.add_argument("--corr-max-r", type=float, default=8.0)
+    ap.add_argument("--corr-bins", type=int, default=200)
     ap.add_argument("--io", action="store_true",
                     help="snapshot files of the workload: RAMSNAP store / restore time and the cost of recording "
                          "a RAMTRJ snapshot every cycle while sweeping")
@@ -788,12 +792,71 @@ def main_io(args):
     return 0
 
 
+def main_correlation(args):
+    """Pair density correlation g(r) (PairDensityCorrelation over a RadialEnumerator) of the
+    workload's packing: snapshots per second on the GPU (cell grid, FP32 pre-filter, FP64
+    decisions, bins exact), against the oracle's restatement of the reference's all-pairs loop
+    timed on a bounded sample and scaled by the number of pairs."""
+    import torch
+    from rampack_gb300 import build as rb
+    rb.build()
+    from rampack_gb300 import correlation as K
+    from rampack_gb300.packing import GpuPacking
+    kind, prm, pos, rot, box = workload(args)
+    n = len(pos)
+    max_r, bins = args.corr_max_r, args.corr_bins
+    g = GpuPacking(kind, prm, pos, rot, box)
+    obs = K.PairDensityCorrelation(K.RadialEnumerator(), max_r, bins)
+    for _ in range(max(3, args.warmup)):
+        obs.add_snapshot(g)
+    torch.cuda.synchronize()
+    steps = max(1, args.steps)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        obs.add_snapshot(g)
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / steps
+    counts, _ = obs.last_snapshot()
+    tested = obs.info()["pairs_tested"]
+    obs.close()
+    g.close()
+    line = {
+        "metric": f"g(r) snapshots/s ({args.workload}, r <= {max_r}, {bins} bins)", "value": 1.0 / dt,
+        "unit": "snapshots/s", "n_gpus": 1, "steps": steps, "warmup": max(3, args.warmup), "ms_per_step": dt * 1e3,
+        "higher_is_better": True, "dtype": "f64 decisions, f32 pre-filter", "data": "synthetic",
+        "config": {"workload": args.workload, "particles": n, "max_r": max_r, "bins": bins,
+                   "observable": "PairDensityCorrelation(RadialEnumerator)"},
+        "pairs_in_range": int(counts.sum()), "pairs_tested_fp64": tested,
+        "pairs_in_range_per_s": float(counts.sum()) / dt,
+        "timing": "host wall clock per addSnapshot (device work synchronous inside)",
+    }
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle as po
+        po.build()
+        ns = min(n, 20000)
+        d = po.pair_desc(enumerator=0, function=0, num_bins=bins, max_r=max_r)
+        c = po.OracleCorrelation(d)
+        t0 = time.perf_counter()
+        c.add_snapshot(pos[:ns], rot[:ns], box)
+        cpu = time.perf_counter() - t0
+        per_pair = cpu / (ns * (ns + 1) / 2)
+        full = per_pair * n * (n + 1) / 2
+        line["cpu_baseline"] = {"value": 1.0 / full, "unit": "snapshots/s", "cores": 1, "kind": "port",
+                                "sample": f"all {ns * (ns + 1) // 2} pairs of the first {ns} particles "
+                                          f"({cpu:.1f} s), scaled to the N(N+1)/2 pairs of one snapshot"}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return main_reference(args)
     if args.io:
         return main_io(args)
+    if args.correlation:
+        return main_correlation(args)
     if args.ordering:
         return main_ordering(args)
     if args.workload == "replicas-64":

@@ -518,6 +518,78 @@ int rp_ramtrj_info(const char *path, int64_t *num_particles, int64_t *snapshots,
                    int32_t *version);
 int rp_ramtrj_read(const char *path, int64_t snapshot, double *pos, double *rot, double *box9);
 
+/* ---- pair correlations (core/observables/correlation/*) ----------------------------- */
+
+/* PairEnumerator implementations: RadialEnumerator (RadialEnumerator.cpp:9-29, distance
+ * between focal points), LinearEnumerator (LinearEnumerator.cpp:37-67, separation
+ * projected on the normal of the box faces across side `linear_axis`) and
+ * LayerwiseRadialEnumerator (LayerwiseRadialEnumerator.cpp:18-46, pairs in the same layer
+ * of the Miller-index planes, separation projected into the layer). */
+#define RP_PAIRS_RADIAL 0
+#define RP_PAIRS_LINEAR 1
+#define RP_PAIRS_LAYERWISE 2
+/* The BulkObservable fed with the pairs: PairDensityCorrelation (PairDensityCorrelation.cpp:
+ * 4-37) or PairAveragedCorrelation (PairAveragedCorrelation.cpp:4-31) of S110Correlation,
+ * S220Correlation, S221Correlation or AxesAngle (core/observables/correlation_functions). */
+#define RP_CORR_DENSITY 0
+#define RP_CORR_S110 1
+#define RP_CORR_S220 2
+#define RP_CORR_S221 3
+#define RP_CORR_AXES_ANGLE 4
+/* ShapeGeometry::Axis of the axis correlations: orientation · primary, orientation ·
+ * secondary, or (primary ^ secondary).normalized() (core/ShapeGeometry.h:65-81). */
+#define RP_AXIS_PRIMARY 0
+#define RP_AXIS_SECONDARY 1
+#define RP_AXIS_AUXILIARY 2
+
+/* One correlation observable: histogram [0, max_r] in num_bins bins; `focal` is the named
+ * point (ShapeGeometry::getNamedPoint) in the body frame that the enumerator measures
+ * from; `primary` / `secondary` are the body-frame axes (SpherocylinderTraits: primary
+ * {0, 0, 1}); `miller` is read by the layerwise enumerator, `linear_axis` (0 x, 1 y, 2 z)
+ * by the linear one. */
+typedef struct rp_pair_desc {
+    int32_t enumerator;
+    int32_t linear_axis;
+    int32_t miller[3];
+    int32_t function;
+    int32_t axis;
+    int32_t num_bins;
+    int32_t flags;      /* RP_CORR_ALL_PAIRS | RP_CORR_FP64_ONLY */
+    int32_t reserved;
+    double max_r;
+    double focal[3];
+    double primary[3];
+    double secondary[3];
+} rp_pair_desc;
+
+/* RP_CORR_ALL_PAIRS: no cell grid, every pair examined as the reference's loops do (the
+ * counts do not change; for cross-checking the grid).  RP_CORR_FP64_ONLY: every examined
+ * pair decided in FP64 (no FP32 pre-filter or binning; the results do not change). */
+#define RP_CORR_ALL_PAIRS 1
+#define RP_CORR_FP64_ONLY 2
+
+/* The constructors PairDensityCorrelation(enumerator, maxR, numBins) and
+ * PairAveragedCorrelation(enumerator, function, maxR, numBins) with the enumerator built
+ * from the same description.  max_r > 0, 1 <= num_bins <= RP_CORR_MAX_BINS. */
+#define RP_CORR_MAX_BINS 65536
+int rp_correlation_create(const rp_pair_desc *desc, void **corr);
+/* BulkObservable::addSnapshot on the handle's current state: the pairs are enumerated and
+ * binned on the GPU (bin counts exact; the FP64 separations in the reference's operation
+ * order), then the snapshot is renormalised and added as HistogramBuilder does. */
+int rp_correlation_add_snapshot(void *corr, void *handle);
+/* HistogramBuilder::dumpValues: bin middles, values (SUM reduction: value / snapshots
+ * for the density correlation; AVERAGE: value / count for the averaged ones) and the
+ * accumulated counts, num_bins each.  The values printed by the reference's print(). */
+int rp_correlation_values(void *corr, double *x, double *y, uint64_t *count);
+/* The last snapshot's raw bins before renormalisation: pair counts and value sums. */
+int rp_correlation_last_snapshot(void *corr, uint64_t *count, double *sums);
+/* Snapshots added since creation or the last clear, and the pairs the last snapshot
+ * tested in FP64 (after the FP32 pre-filter). */
+int rp_correlation_info(void *corr, int64_t *snapshots, int64_t *pairs_tested);
+int rp_correlation_clear(void *corr);
+const char *rp_correlation_last_error(void *corr);
+int rp_correlation_destroy(void *corr);
+
 #ifdef __cplusplus
 }
 #endif

@@ -428,3 +428,173 @@ def ref_box_proposals(kind: int, together: int, groups, independent: int, step: 
                              _dp(u)) != 0:
         raise ValueError("bad scaler")
     return boxes, u
+
+
+# ---- pair correlations (core/observables/correlation/*) --------------------------------
+
+class PairDesc(C.Structure):
+    """Same layout as rpo_pair_desc (oracle/rpo_capi.cpp) and rp_pair_desc."""
+    _fields_ = [("enumerator", C.c_int32), ("linear_axis", C.c_int32), ("miller", C.c_int32 * 3),
+                ("function", C.c_int32), ("axis", C.c_int32), ("num_bins", C.c_int32), ("flags", C.c_int32),
+                ("reserved", C.c_int32), ("max_r", C.c_double),
+                ("focal", C.c_double * 3), ("primary", C.c_double * 3), ("secondary", C.c_double * 3)]
+
+
+def pair_desc(enumerator: int = 0, linear_axis: int = 0, miller=(0, 0, 1), function: int = 0, axis: int = 0,
+              num_bins: int = 10, max_r: float = 1.0, focal=(0.0, 0.0, 0.0), primary=(0.0, 0.0, 1.0),
+              secondary=(1.0, 0.0, 0.0)) -> PairDesc:
+    return PairDesc(enumerator, linear_axis, (C.c_int32 * 3)(*miller), function, axis, num_bins, 0, 0, max_r,
+                    (C.c_double * 3)(*focal), (C.c_double * 3)(*primary), (C.c_double * 3)(*secondary))
+
+
+def _corr_lib():
+    lib, _ = _lib("oracle")
+    if not getattr(lib, "_corr_bound", False):
+        PD = C.POINTER(PairDesc)
+        sig = {"rpo_corr_create": (_P, [PD]), "rpo_corr_destroy": (None, [_P]),
+               "rpo_corr_add_snapshot": (C.c_int, [_P, C.c_int64, _D, _D, _D]),
+               "rpo_corr_consume": (None, [_P, C.c_int64, C.c_int64, _D, C.c_double]),
+               "rpo_corr_renormalize": (None, [_P, _D]), "rpo_corr_next_snapshot": (None, [_P]),
+               "rpo_corr_dividers": (None, [_P, _D]),
+               "rpo_corr_dump": (None, [_P, _D, _D, C.POINTER(C.c_uint64)]),
+               "rpo_enumerate_pairs": (C.c_int64, [PD, C.c_int64, _D, _D, _D, C.c_int64, _I64, _D]),
+               "rpo_expected_in_shells": (C.c_int, [PD, C.c_int64, _D, _D, C.c_int, _D]),
+               "rpo_axis_function": (C.c_double, [C.c_int, _D, _D, _D]),
+               "rpo_pair_counts": (None, [PD, C.c_int64, _D, _D, _D, C.c_int, C.POINTER(C.c_uint64)])}
+        for name, (res, args) in sig.items():
+            f = getattr(lib, name)
+            f.restype, f.argtypes = res, args
+        lib._corr_bound = True
+    return lib
+
+
+def _state(pos, rot, box):
+    p = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+    r = np.ascontiguousarray(rot, dtype=np.float64).reshape(-1, 9)
+    b = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
+    return p, r, b
+
+
+class OracleCorrelation:
+    """PairDensityCorrelation (function 0) or PairAveragedCorrelation (functions 1-4:
+    S110, S220, S221, AxesAngle) restated single-threaded in oracle/rpo_correlation.hpp."""
+
+    def __init__(self, desc: PairDesc):
+        self.lib = _corr_lib()
+        self.desc = desc
+        self.h = self.lib.rpo_corr_create(C.byref(desc))
+        if not self.h:
+            raise ValueError("bad correlation description")
+
+    def add_snapshot(self, pos, rot, box) -> None:
+        p, r, b = _state(pos, rot, box)
+        if self.lib.rpo_corr_add_snapshot(self.h, len(p), _dp(p), _dp(r), _dp(b)) != 0:
+            raise ValueError("snapshot failed")
+
+    def consume(self, i: int, j: int, d, value: float = 0.0) -> None:
+        v = np.ascontiguousarray(d, dtype=np.float64)
+        self.lib.rpo_corr_consume(self.h, i, j, _dp(v), value)
+
+    def renormalize(self, factors) -> None:
+        f = np.ascontiguousarray(factors, dtype=np.float64)
+        self.lib.rpo_corr_renormalize(self.h, _dp(f))
+
+    def next_snapshot(self) -> None:
+        self.lib.rpo_corr_next_snapshot(self.h)
+
+    def dividers(self) -> np.ndarray:
+        out = np.zeros(self.desc.num_bins + 1)
+        self.lib.rpo_corr_dividers(self.h, _dp(out))
+        return out
+
+    def values(self):
+        nb = self.desc.num_bins
+        x, y, c = np.zeros(nb), np.zeros(nb), np.zeros(nb, dtype=np.uint64)
+        self.lib.rpo_corr_dump(self.h, _dp(x), _dp(y), c.ctypes.data_as(C.POINTER(C.c_uint64)))
+        return x, y, c
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.rpo_corr_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+def enumerate_pairs(desc: PairDesc, pos, rot, box):
+    """Every (i, j, separation) an enumerator hands its consumer, in its order."""
+    lib = _corr_lib()
+    p, r, b = _state(pos, rot, box)
+    n = len(p)
+    cap = n * (n + 1) // 2
+    ij, d = np.zeros((max(cap, 1), 2), dtype=np.int64), np.zeros((max(cap, 1), 3))
+    k = lib.rpo_enumerate_pairs(C.byref(desc), n, _dp(p), _dp(r), _dp(b), cap,
+                                ij.ctypes.data_as(_I64), _dp(d))
+    return ij[:k], d[:k]
+
+
+def pair_counts(desc: PairDesc, pos, rot, box, threads: int = 0) -> np.ndarray:
+    """One snapshot's bin counts (the density correlation's pairs i < j, the averaged ones'
+    i <= j), the rows shared among threads (0: all cores)."""
+    lib = _corr_lib()
+    p, r, b = _state(pos, rot, box)
+    out = np.zeros(desc.num_bins, dtype=np.uint64)
+    lib.rpo_pair_counts(C.byref(desc), len(p), _dp(p), _dp(r), _dp(b), threads or (os.cpu_count() or 1),
+                        out.ctypes.data_as(C.POINTER(C.c_uint64)))
+    return out
+
+
+def expected_in_shells(desc: PairDesc, n: int, box, bounds) -> np.ndarray:
+    lib = _corr_lib()
+    b = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
+    bd = np.ascontiguousarray(bounds, dtype=np.float64)
+    out = np.zeros(max(len(bd) - 1, 0))
+    lib.rpo_expected_in_shells(C.byref(desc), n, _dp(b), _dp(bd), len(bd), _dp(out))
+    return out
+
+
+def axis_function(f: int, a1, a2, d) -> float:
+    lib = _corr_lib()
+    v = [np.ascontiguousarray(x, dtype=np.float64) for x in (a1, a2, d)]
+    return lib.rpo_axis_function(f, *[_dp(x) for x in v])
+
+
+def ref_named_point(kind: int, params, name: str) -> np.ndarray:
+    """ShapeGeometry::getNamedPoint of the reference's own traits."""
+    lib, _ = _lib("reference")
+    lib.ref_named_point.restype = C.c_int
+    lib.ref_named_point.argtypes = [C.c_int, _D, C.c_int, C.c_char_p, _D]
+    prm = np.ascontiguousarray(params, dtype=np.float64)
+    out = np.zeros(3)
+    if lib.ref_named_point(kind, _dp(prm), len(prm), name.encode(), _dp(out)) != 0:
+        raise KeyError(name)
+    return out
+
+
+def ref_pair_correlation(kind: int, params, states, desc: PairDesc, focal_name: str = "o",
+                         primary=None, secondary=None):
+    """The reference's own PairDensityCorrelation / PairAveragedCorrelation over its
+    enumerators: one addSnapshot per (pos, rot, box) state, then print(), parsed at full
+    precision.  Polysphere axes come from `primary` / `secondary` (body frame)."""
+    lib, _ = _lib("reference")
+    lib.ref_pair_correlation.restype = C.c_int
+    lib.ref_pair_correlation.argtypes = [C.c_int, _D, C.c_int, _D, _D, C.c_int64, C.c_int, _D, _D, _D, C.c_int,
+                                         C.c_int, C.POINTER(C.c_int), C.c_char_p, C.c_int, C.c_int, C.c_double,
+                                         C.c_int, _D, _D, C.POINTER(C.c_uint64)]
+    prm = np.ascontiguousarray(params, dtype=np.float64)
+    n = len(np.asarray(states[0][0]).reshape(-1, 3))
+    pos = np.ascontiguousarray(np.concatenate([np.asarray(s[0]).reshape(-1) for s in states]), dtype=np.float64)
+    rot = np.ascontiguousarray(np.concatenate([np.asarray(s[1]).reshape(-1) for s in states]), dtype=np.float64)
+    box = np.ascontiguousarray(np.concatenate([np.asarray(s[2]).reshape(-1) for s in states]), dtype=np.float64)
+    a1 = None if primary is None else _dp(np.ascontiguousarray(primary, dtype=np.float64))
+    a2 = None if secondary is None else _dp(np.ascontiguousarray(secondary, dtype=np.float64))
+    nb = desc.num_bins
+    x, y, c = np.zeros(nb), np.zeros(nb), np.zeros(nb, dtype=np.uint64)
+    mil = (C.c_int * 3)(*desc.miller)
+    got = lib.ref_pair_correlation(kind, _dp(prm), len(prm), a1, a2, n, len(states), _dp(pos), _dp(rot), _dp(box),
+                                   desc.enumerator, desc.linear_axis, mil, focal_name.encode(), desc.function,
+                                   desc.axis, desc.max_r, nb, _dp(x), _dp(y), c.ctypes.data_as(C.POINTER(C.c_uint64)))
+    if got != nb:
+        raise ValueError(f"reference correlation failed ({got})")
+    return x, y, c

@@ -6,8 +6,10 @@
 // restatement in oracle/rpo_*.hpp and to generate the golden fixtures under
 // tests/golden/.  Mirrors the rpo_* entry points of rpo_capi.cpp one for one.
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <iomanip>
 #include <map>
 #include <memory>
 #include <random>
@@ -19,6 +21,15 @@
 #include "core/FreeBoundaryConditions.h"
 #include "core/Simulation.h"
 #include "core/ObservablesCollector.h"
+#include "core/observables/correlation/LayerwiseRadialEnumerator.h"
+#include "core/observables/correlation/LinearEnumerator.h"
+#include "core/observables/correlation/PairAveragedCorrelation.h"
+#include "core/observables/correlation/PairDensityCorrelation.h"
+#include "core/observables/correlation/RadialEnumerator.h"
+#include "core/observables/correlation_functions/AxesAngle.h"
+#include "core/observables/correlation_functions/S110Correlation.h"
+#include "core/observables/correlation_functions/S220Correlation.h"
+#include "core/observables/correlation_functions/S221Correlation.h"
 #include "core/io/RamtrjPlayer.h"
 #include "core/io/RamtrjRecorder.h"
 #include "core/move_samplers/FlipSampler.h"
@@ -576,6 +587,91 @@ int ref_box_proposals(int kind, int together, int ngroups, const int *groups, in
         uniforms[k] = unit(mt);
     }
     return 0;
+}
+
+// ---- pair correlations: the reference's own PairDensityCorrelation /
+// PairAveragedCorrelation over its RadialEnumerator, LinearEnumerator and
+// LayerwiseRadialEnumerator, one snapshot per packing state, printed at full precision
+
+std::shared_ptr<ShapeTraits> make_traits_axes(int kind, const double *prm, int np, const double *primary,
+                                              const double *secondary) {
+    if (kind != 2) return make_traits(kind, prm, np);
+    int k = static_cast<int>(prm[0]);
+    std::vector<PolysphereTraits::SphereData> data;
+    for (int i = 0; i < k; i++)
+        data.emplace_back(Vector<3>{prm[1 + 4 * i], prm[2 + 4 * i], prm[3 + 4 * i]}, prm[4 + 4 * i]);
+    std::optional<Vector<3>> a1, a2;
+    if (primary) a1 = Vector<3>{primary[0], primary[1], primary[2]};
+    if (secondary) a2 = Vector<3>{secondary[0], secondary[1], secondary[2]};
+    PolysphereTraits::PolysphereGeometry geom(std::move(data), a1, a2, {0, 0, 0}, 1.0);
+    return std::make_shared<PolysphereTraits>(std::move(geom));
+}
+
+int ref_named_point(int kind, const double *prm, int np, const char *name, double *out3) {
+    auto traits = make_traits(kind, prm, np);
+    try {
+        auto v = traits->getGeometry().getNamedPoint(name);
+        for (int i = 0; i < 3; i++) out3[i] = v[i];
+    } catch (const std::exception &) {
+        return -1;
+    }
+    return 0;
+}
+
+int ref_pair_correlation(int kind, const double *prm, int np, const double *primary, const double *secondary,
+                         int64_t n, int nsnap, const double *pos, const double *rot, const double *box9,
+                         int enumerator, int linear_axis, const int *miller, const char *focal, int function,
+                         int axis, double max_r, int num_bins, double *x, double *y, uint64_t *count) {
+    auto traits = make_traits_axes(kind, prm, np, primary, secondary);
+    if (!traits) return -1;
+    std::shared_ptr<PairEnumerator> en;
+    if (enumerator == 0)
+        en = std::make_shared<RadialEnumerator>(focal);
+    else if (enumerator == 1)
+        en = std::make_shared<LinearEnumerator>(static_cast<LinearEnumerator::Axis>(linear_axis), focal);
+    else
+        en = std::make_shared<LayerwiseRadialEnumerator>(std::array<int, 3>{miller[0], miller[1], miller[2]},
+                                                         focal);
+    auto ax = static_cast<ShapeGeometry::Axis>(axis);
+    std::unique_ptr<BulkObservable> obs;
+    std::shared_ptr<CorrelationFunction> fn;
+    if (function == 1) fn = std::make_shared<S110Correlation>(ax);
+    if (function == 2) fn = std::make_shared<S220Correlation>(ax);
+    if (function == 3) fn = std::make_shared<S221Correlation>(ax);
+    if (function == 4) fn = std::make_shared<AxesAngle>(ax);
+    if (function == 0)
+        obs = std::make_unique<PairDensityCorrelation>(en, max_r, num_bins, true);
+    else
+        obs = std::make_unique<PairAveragedCorrelation>(en, fn, max_r, num_bins, true);
+    try {
+        for (int s = 0; s < nsnap; s++) {
+            std::vector<Shape> shapes;
+            const double *p = pos + 3 * n * s, *r = rot + 9 * n * s;
+            for (int64_t i = 0; i < n; i++)
+                shapes.emplace_back(Vector<3>{p[3 * i], p[3 * i + 1], p[3 * i + 2]}, load_m(r + 9 * i));
+            Packing pk(TriclinicBox(load_m(box9 + 9 * s)), std::move(shapes),
+                       std::make_unique<PeriodicBoundaryConditions>(), traits->getInteraction(), 1, 1);
+            obs->addSnapshot(pk, 1, 1, *traits);
+        }
+    } catch (const std::exception &e) {
+        std::fprintf(stderr, "ref_pair_correlation: %s\n", e.what());
+        return -2;
+    }
+    std::ostringstream out;
+    out << std::setprecision(17);
+    obs->print(out);
+    std::istringstream in(out.str());
+    std::string line;
+    int b = 0;
+    while (std::getline(in, line) && b < num_bins) {
+        std::istringstream ls(line);
+        std::string xs, ys;
+        ls >> xs >> ys >> count[b];
+        x[b] = std::stod(xs);
+        y[b] = (ys.find("nan") != std::string::npos) ? std::nan("") : std::stod(ys);
+        b++;
+    }
+    return b;
 }
 
 }  // extern "C"

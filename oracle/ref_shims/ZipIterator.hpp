@@ -1,37 +1,47 @@
 // Minimal stand-in for the un-vendored ZipIterator submodule of the reference
-// (dpellegr/ZipIterator, pinned commit not mounted).  The reference's hot-path
-// sources include <ZipIterator.hpp> only for `Zip(a, b)` in a range-for with a
-// structured binding (core/Simulation.cpp:733, move statistics).  This header is
-// written for the oracle build and supports exactly that use: iterating two
-// equally long containers in lockstep and yielding a pair of references.
+// (dpellegr/ZipIterator, pinned commit not mounted).  The reference's sources include
+// <ZipIterator.hpp> only for `Zip(a, b, ...)` in a range-for with a structured binding
+// (core/Simulation.cpp:733 over two containers; core/observables/Histogram.tpp:13-100
+// and HistogramBuilder.tpp:86 over two or three).  This header is written for the oracle
+// build and supports exactly that use: iterating equally long containers in lockstep,
+// yielding a tuple of references.
 #pragma once
 #include <cstddef>
-#include <utility>
 #include <iterator>
+#include <tuple>
+#include <utility>
 
 namespace rpo_zip_shim {
-template <typename A, typename B>
+template <typename... C>
 class ZipRange {
-    A &a;
-    B &b;
+    std::tuple<C &...> cs;
+
 public:
-    using IA = decltype(std::begin(std::declval<A &>()));
-    using IB = decltype(std::begin(std::declval<B &>()));
+    using Iters = std::tuple<decltype(std::begin(std::declval<C &>()))...>;
     class iterator {
-        IA ia;
-        IB ib;
+        Iters its;
+
     public:
-        iterator(IA ia_, IB ib_) : ia{ia_}, ib{ib_} {}
-        auto operator*() const { return std::pair<decltype(*ia), decltype(*ib)>(*ia, *ib); }
-        iterator &operator++() { ++ia; ++ib; return *this; }
-        bool operator!=(const iterator &o) const { return ia != o.ia; }
-        bool operator==(const iterator &o) const { return ia == o.ia; }
+        explicit iterator(Iters its_) : its{its_} {}
+        auto operator*() const {
+            return std::apply([](auto &...i) { return std::tuple<decltype(*i)...>(*i...); }, its);
+        }
+        iterator &operator++() {
+            std::apply([](auto &...i) { (++i, ...); }, its);
+            return *this;
+        }
+        bool operator!=(const iterator &o) const { return std::get<0>(its) != std::get<0>(o.its); }
+        bool operator==(const iterator &o) const { return std::get<0>(its) == std::get<0>(o.its); }
     };
-    ZipRange(A &a_, B &b_) : a{a_}, b{b_} {}
-    iterator begin() const { return iterator(std::begin(a), std::begin(b)); }
-    iterator end() const { return iterator(std::end(a), std::end(b)); }
+    explicit ZipRange(C &...c) : cs{c...} {}
+    iterator begin() const {
+        return iterator(std::apply([](auto &...c) { return Iters(std::begin(c)...); }, cs));
+    }
+    iterator end() const {
+        return iterator(std::apply([](auto &...c) { return Iters(std::end(c)...); }, cs));
+    }
 };
 }  // namespace rpo_zip_shim
 
-template <typename A, typename B>
-rpo_zip_shim::ZipRange<A, B> Zip(A &a, B &b) { return rpo_zip_shim::ZipRange<A, B>(a, b); }
+template <typename... C>
+rpo_zip_shim::ZipRange<C...> Zip(C &...c) { return rpo_zip_shim::ZipRange<C...>(c...); }

@@ -7,6 +7,7 @@
 #include <cstring>
 #include <memory>
 
+#include "rpo_correlation.hpp"
 #include "rpo_sim.hpp"
 
 using namespace rpo;
@@ -388,6 +389,130 @@ int rpo_sim_run(void *sp, int64_t cycles, rpo_sim_stats *out) {
         out->box_step = sim.p.box_step;
     }
     return 0;
+}
+
+// ---- pair correlations (core/observables/correlation/*) ----------------------------
+
+// Same layout as rp_pair_desc in include/rampack_gb300.h.
+struct rpo_pair_desc {
+    int32_t enumerator;
+    int32_t linear_axis;
+    int32_t miller[3];
+    int32_t function;
+    int32_t axis;
+    int32_t num_bins;
+    int32_t flags;
+    int32_t reserved;
+    double max_r;
+    double focal[3];
+    double primary[3];
+    double secondary[3];
+};
+
+static CorrSpec load_spec(const rpo_pair_desc *d) {
+    CorrSpec s;
+    s.enumerator = d->enumerator;
+    s.linear_axis = d->linear_axis;
+    for (int i = 0; i < 3; i++) {
+        s.miller[i] = d->miller[i];
+        s.focal[i] = d->focal[i];
+        s.primary[i] = d->primary[i];
+        s.secondary[i] = d->secondary[i];
+    }
+    s.function = d->function;
+    s.axis = d->axis;
+    s.num_bins = d->num_bins;
+    s.max_r = d->max_r;
+    return s;
+}
+
+static void load_state(int64_t n, const double *pos, const double *rot, std::vector<V3> &p, std::vector<M3> &r) {
+    p.resize(n);
+    r.resize(n);
+    for (int64_t i = 0; i < n; i++) {
+        p[i] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+        r[i] = load_m3(rot + 9 * i);
+    }
+}
+
+void *rpo_corr_create(const rpo_pair_desc *d) {
+    if (!d || d->num_bins < 1 || !(d->max_r > 0)) return nullptr;
+    return new Correlation(load_spec(d));
+}
+void rpo_corr_destroy(void *c) { delete static_cast<Correlation *>(c); }
+
+int rpo_corr_add_snapshot(void *c, int64_t n, const double *pos, const double *rot, const double *box9) {
+    std::vector<V3> p;
+    std::vector<M3> r;
+    load_state(n, pos, rot, p, r);
+    try {
+        static_cast<Correlation *>(c)->add_snapshot(p, r, Box(load_m3(box9)));
+    } catch (const std::exception &) {
+        return -1;
+    }
+    return 0;
+}
+
+// one consumePair with the correlation function's value given (the mocked enumerators and
+// functions of the reference's unit tests), then renormalizeBins / nextSnapshot
+void rpo_corr_consume(void *c, int64_t i, int64_t j, const double *d3, double value) {
+    static_cast<Correlation *>(c)->consume(i, j, {d3[0], d3[1], d3[2]}, value);
+}
+void rpo_corr_renormalize(void *c, const double *factors) {
+    auto *k = static_cast<Correlation *>(c);
+    k->hist.renormalize(std::vector<double>(factors, factors + k->hist.bins));
+}
+void rpo_corr_next_snapshot(void *c) { static_cast<Correlation *>(c)->hist.next_snapshot(); }
+void rpo_corr_dividers(void *c, double *out) {
+    auto v = static_cast<Correlation *>(c)->hist.dividers();
+    std::memcpy(out, v.data(), sizeof(double) * v.size());
+}
+void rpo_corr_dump(void *c, double *x, double *y, uint64_t *count) {
+    auto *k = static_cast<Correlation *>(c);
+    k->hist.dump(!k->density(), x, y, count);
+}
+
+// the pairs an enumerator produces (i, j, separation) for n focal points at the given
+// positions (orientations apply the focal point); returns the number of pairs, writing at
+// most `cap` of them
+int64_t rpo_enumerate_pairs(const rpo_pair_desc *d, int64_t n, const double *pos, const double *rot,
+                            const double *box9, int64_t cap, int64_t *ij, double *diff) {
+    std::vector<V3> p;
+    std::vector<M3> r;
+    load_state(n, pos, rot, p, r);
+    CorrSpec s = load_spec(d);
+    int64_t k = 0;
+    enumerate_pairs(s, Box(load_m3(box9)), focal_points(p, r, s.focal), [&](std::size_t i, std::size_t j, const V3 &v) {
+        if (k < cap) {
+            ij[2 * k] = static_cast<int64_t>(i);
+            ij[2 * k + 1] = static_cast<int64_t>(j);
+            for (int a = 0; a < 3; a++) diff[3 * k + a] = v[a];
+        }
+        k++;
+    });
+    return k;
+}
+
+// one snapshot's bin counts, rows shared among `threads` threads
+void rpo_pair_counts(const rpo_pair_desc *d, int64_t n, const double *pos, const double *rot, const double *box9,
+                     int threads, uint64_t *out) {
+    std::vector<V3> p;
+    std::vector<M3> r;
+    load_state(n, pos, rot, p, r);
+    CorrSpec s = load_spec(d);
+    auto c = pair_counts(s, Box(load_m3(box9)), focal_points(p, r, s.focal), threads);
+    std::memcpy(out, c.data(), sizeof(uint64_t) * c.size());
+}
+
+int rpo_expected_in_shells(const rpo_pair_desc *d, int64_t n, const double *box9, const double *bounds, int nb,
+                           double *out) {
+    auto v = expected_in_shells(load_spec(d), Box(load_m3(box9)), n, std::vector<double>(bounds, bounds + nb));
+    std::memcpy(out, v.data(), sizeof(double) * v.size());
+    return static_cast<int>(v.size());
+}
+
+double rpo_axis_function(int f, const double *a1, const double *a2, const double *d) {
+    return axis_function(f, {a1[0], a1[1], a1[2]}, {a2[0], a2[1], a2[2]}, {d[0], d[1], d[2]});
 }
 
 }  // extern "C"

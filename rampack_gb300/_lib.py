@@ -67,6 +67,21 @@ class SimParams(C.Structure):
                 ("rototranslation", C.c_int32), ("reserved", C.c_int32)]
 
 
+class PairDesc(C.Structure):
+    """rp_pair_desc: one pair-correlation observable."""
+    _fields_ = [("enumerator", C.c_int32), ("linear_axis", C.c_int32), ("miller", C.c_int32 * 3),
+                ("function", C.c_int32), ("axis", C.c_int32), ("num_bins", C.c_int32), ("flags", C.c_int32),
+                ("reserved", C.c_int32), ("max_r", C.c_double),
+                ("focal", C.c_double * 3), ("primary", C.c_double * 3), ("secondary", C.c_double * 3)]
+
+
+PAIRS_RADIAL, PAIRS_LINEAR, PAIRS_LAYERWISE = 0, 1, 2
+CORR_DENSITY, CORR_S110, CORR_S220, CORR_S221, CORR_AXES_ANGLE = 0, 1, 2, 3, 4
+AXIS_PRIMARY, AXIS_SECONDARY, AXIS_AUXILIARY = 0, 1, 2
+CORR_MAX_BINS = 65536
+CORR_ALL_PAIRS, CORR_FP64_ONLY = 1, 2
+
+
 class SimStats(C.Structure):
     _fields_ = [("cycles", C.c_uint64), ("translations", C.c_uint64), ("accepted_translations", C.c_uint64),
                 ("rotations", C.c_uint64), ("accepted_rotations", C.c_uint64), ("box_moves", C.c_uint64),
@@ -170,6 +185,14 @@ SIGNATURES = {
     "rp_ramtrj_info": (C.c_int, [C.c_char_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                  C.POINTER(C.c_int32)]),
     "rp_ramtrj_read": (C.c_int, [C.c_char_p, C.c_int64, _D, _D, _D]),
+    "rp_correlation_create": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "rp_correlation_add_snapshot": (C.c_int, [_P, _P]),
+    "rp_correlation_values": (C.c_int, [_P, _D, _D, C.POINTER(C.c_uint64)]),
+    "rp_correlation_last_snapshot": (C.c_int, [_P, C.POINTER(C.c_uint64), _D]),
+    "rp_correlation_info": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "rp_correlation_clear": (C.c_int, [_P]),
+    "rp_correlation_last_error": (C.c_char_p, [_P]),
+    "rp_correlation_destroy": (C.c_int, [_P]),
 }
 KERNEL_GROUPS = ["sweep", "rebuild", "count", "rescale", "overflow", "order", "mlp", "fix"]
 MLP_NPARAM = 5313

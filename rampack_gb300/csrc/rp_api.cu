@@ -2673,4 +2673,34 @@ bool handle_box(void *handle, double *box9) {
 }
 bool handle_counting(void *handle) { return handle && static_cast<Handle *>(handle)->counting; }
 
+// The current state of a handle for the observables (positions, orientations, box and its
+// reference inverse), after its pending moves (in order on its stream).
+struct PackingView {
+    int device;
+    cudaStream_t stream;
+    int64_t n;
+    const double *pos64;
+    const double *rot64;
+    double box[9], inv[9];
+};
+int packing_view(void *handle, PackingView *v, std::string &err) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h) {
+        err = "null handle";
+        return RP_ERR_ARG;
+    }
+    if (!h->has_state) {
+        err = "no state uploaded";
+        return RP_ERR_STATE;
+    }
+    v->device = h->device;
+    v->stream = h->stream;
+    v->n = h->n;
+    v->pos64 = h->pos64[h->pcur];
+    v->rot64 = h->rot64;
+    std::memcpy(v->box, h->box, sizeof(v->box));
+    std::memcpy(v->inv, h->inv, sizeof(v->inv));
+    return RP_OK;
+}
+
 }  // namespace rp

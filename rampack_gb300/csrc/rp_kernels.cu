@@ -260,6 +260,17 @@ cudaError_t launch_rebuild(const DevState &s, const GridDev &g, int32_t *block_s
     return cudaGetLastError();
 }
 
+// Exclusive scan of `ncell` counts into start[0..ncell] (start[ncell] = total); block_sums
+// holds (ncell + 4095) / 4096 entries; max_occ receives the largest count.
+cudaError_t launch_cell_scan(const int32_t *count, int32_t *start, int32_t *block_sums, int ncell,
+                             int32_t *max_occ, cudaStream_t st) {
+    int nblocks = (ncell + 4095) / 4096;
+    k_scan_blocks<<<nblocks, 1024, 0, st>>>(count, start, block_sums, ncell, max_occ);
+    k_scan_sums<<<1, 32, 0, st>>>(block_sums, nblocks, start, ncell);
+    k_scan_add<<<(ncell + 255) / 256, 256, 0, st>>>(start, block_sums, ncell);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_validate(const DevState &s, cudaStream_t st) {
     if (s.n == 0) return cudaSuccess;
     k_validate<<<(unsigned)((s.n + 255) / 256), 256, 0, st>>>(s);

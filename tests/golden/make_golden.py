@@ -8,6 +8,7 @@ Run in a checkout where the reference sources are present:
     python tests/golden/make_golden.py box    # the box-move proposal streams only
     python tests/golden/make_golden.py flips  # the FlipSampler moves only
     python tests/golden/make_golden.py walls  # the hard-wall packings only
+    python tests/golden/make_golden.py correlation  # the pair-correlation observables only
 
 Every expected value below is produced by the reference library (oracle/_ref/librpref.so:
 rampack's Packing, NeighbourGrid, SpherocylinderTraits, samplers and Simulation compiled
@@ -381,11 +382,37 @@ def gen_walls():
     print("walls:", len(WALLS), "systems")
 
 
+def gen_correlation():
+    """PairDensityCorrelation / PairAveragedCorrelation of the reference over two snapshots
+    of each system (as thermalised, and compressed by 3%), printed at full precision, and the
+    reference's named points of the shapes."""
+    import systems
+    from correlation_cases import CORRELATIONS, NAMED_POINTS, POLY_AXES
+    out = {}
+    for i, (name, en, lax, mil, fn, ax, focal, max_r, nb) in enumerate(CORRELATIONS):
+        cfg = systems.ALL[name]()
+        kind, prm = cfg[0], cfg[1]
+        states = [cfg[2:5], systems.compressed(cfg, 0.97)[2:5]]
+        d = po.pair_desc(enumerator=en, linear_axis=lax, miller=mil, function=fn, axis=ax, num_bins=nb,
+                         max_r=max_r)
+        prim, sec = POLY_AXES if kind == po.POLYSPHERE else (None, None)
+        x, y, c = po.ref_pair_correlation(kind, prm, states, d, focal, primary=prim, secondary=sec)
+        out[f"c{i}_x"], out[f"c{i}_y"], out[f"c{i}_count"] = x, y, c
+    for i, (name, point) in enumerate(NAMED_POINTS):
+        cfg = systems.ALL[name]()
+        out[f"p{i}"] = po.ref_named_point(cfg[0], cfg[1], point)
+    np.savez_compressed(os.path.join(HERE, "correlation.npz"), **out)
+    print("correlation:", len(CORRELATIONS), "observables")
+
+
 def main():
     if not po.reference_available():
         po.build(reference=True)
     if sys.argv[1:] == ["walls"]:
         gen_walls()
+        return
+    if sys.argv[1:] == ["correlation"]:
+        gen_correlation()
         return
     if sys.argv[1:] == ["flips"]:
         gen_flips()
@@ -412,6 +439,7 @@ def main():
     gen_box_proposals()
     gen_flips()
     gen_walls()
+    gen_correlation()
 
 
 if __name__ == "__main__":
