@@ -806,6 +806,8 @@ def main_correlation(args):
     n = len(pos)
     max_r, bins = args.corr_max_r, args.corr_bins
     g = GpuPacking(kind, prm, pos, rot, box)
+    for c in range(3):   # a disordered state (the lattice's distances sit far from the bin edges)
+        g.sweep(0.2, 0.2, seed=args.seed, counter=c, stats=False)
     obs = K.PairDensityCorrelation(K.RadialEnumerator(), max_r, bins)
     for _ in range(max(3, args.warmup)):
         obs.add_snapshot(g)
@@ -823,10 +825,10 @@ def main_correlation(args):
     line = {
         "metric": f"g(r) snapshots/s ({args.workload}, r <= {max_r}, {bins} bins)", "value": 1.0 / dt,
         "unit": "snapshots/s", "n_gpus": 1, "steps": steps, "warmup": max(3, args.warmup), "ms_per_step": dt * 1e3,
-        "higher_is_better": True, "dtype": "f64 decisions, f32 pre-filter", "data": "synthetic",
+        "higher_is_better": True, "dtype": "f32 binning, f64 guard band", "data": "synthetic",
         "config": {"workload": args.workload, "particles": n, "max_r": max_r, "bins": bins,
                    "observable": "PairDensityCorrelation(RadialEnumerator)"},
-        "pairs_in_range": int(counts.sum()), "pairs_tested_fp64": tested,
+        "pairs_in_range": int(counts.sum()), "pairs_decided_fp64": tested,
         "pairs_in_range_per_s": float(counts.sum()) / dt,
         "timing": "host wall clock per addSnapshot (device work synchronous inside)",
     }

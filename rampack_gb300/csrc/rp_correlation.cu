@@ -59,6 +59,10 @@ struct CorrGeom {
     double max_r, step;
     float thr2_32;   // FP32 rejection: squared distance above this is out of reach
     float lin_thr32; // FP32 rejection: |relative separation| along lin_axis above this
+    float h32;       // the height across side lin_axis (linear enumerator)
+    // FP32 binning: with t = d32 / step (FP32), the FP64 distance / step lies within
+    // t -+ (bin_abs + bin_rel * t); in range for sure below in_lo, out of range above in_hi
+    float inv_step32, bin_abs, bin_rel, in_lo, in_hi;
     float edge32;    // no FP32 rejection when a folded relative separation is this near 1/2
     int fp64_only;   // RP_CORR_FP64_ONLY: no FP32 pre-filter
 };
@@ -208,7 +212,7 @@ __device__ void decide_pair(const CorrGeom &G, const SortedPoints &S, int64_t lo
 }
 
 template <int E, int F>
-__global__ void __launch_bounds__(CORR_THREADS) k_corr_pairs(CorrGeom G, SortedPoints S, const int32_t *start,
+__global__ void __launch_bounds__(CORR_THREADS, 2) k_corr_pairs(CorrGeom G, SortedPoints S, const int32_t *start,
                                                              int64_t n, int use_smem, unsigned long long *hist,
                                                              double *hsum, unsigned long long *tested) {
     extern __shared__ unsigned long long sh[];
@@ -255,9 +259,14 @@ __global__ void __launch_bounds__(CORR_THREADS) k_corr_pairs(CorrGeom G, SortedP
                             f[k] -= rintf(f[k]);
                             edge |= fabsf(f[k]) > e;
                         }
-                        if (!edge && !G.fp64_only) {
+                        const bool fast = !edge && !G.fp64_only;
+                        float d32 = 0.f;
+                        if (fast) {
                             if (E == RP_PAIRS_LINEAR) {
-                                if (fabsf(f[G.lin_axis]) > G.lin_thr32) continue;
+                                const float fa = fabsf(f[0] * (G.lin_axis == 0) + f[1] * (G.lin_axis == 1) +
+                                                       f[2] * (G.lin_axis == 2));
+                                if (fa > G.lin_thr32) continue;
+                                d32 = fa * G.h32;
                             } else {
                                 float d2 = 0.f;
                                 for (int i = 0; i < 3; i++) {
@@ -266,6 +275,29 @@ __global__ void __launch_bounds__(CORR_THREADS) k_corr_pairs(CorrGeom G, SortedP
                                     d2 += s * s;
                                 }
                                 if (d2 > G.thr2_32) continue;
+                                d32 = sqrtf(d2);
+                            }
+                        }
+                        // FP32 binning: when the FP64 distance's whole error interval lies in
+                        // one bin below max_r (or beyond max_r), that bin is the reference's;
+                        // pairs near a bin edge or max_r are decided in FP64 below.  The
+                        // layerwise enumerator and S221 (which reads the separation) always
+                        // take FP64.
+                        if (E != RP_PAIRS_LAYERWISE && F != RP_CORR_S221 && fast) {
+                            const float t = d32 * G.inv_step32;
+                            const float m = G.bin_abs + G.bin_rel * t;
+                            const float lo = t - m, hi = t + m;
+                            if (lo > G.in_hi) continue;
+                            if (hi < G.in_lo) {
+                                const float qlo = floorf(lo), qhi = floorf(hi);
+                                if (qlo == qhi) {
+                                    const int bin = min(static_cast<int>(qlo), G.nb - 1);
+                                    atomicAdd(hc + bin, 1ull);
+                                    if (F != RP_CORR_DENSITY)
+                                        atomicAdd(hs + bin, axis_function<F>(load3(S.ax64, a), load3(S.ax64, b),
+                                                                             d3{0.0, 0.0, 0.0}));
+                                    continue;
+                                }
                             }
                         }
                         my_tested++;
@@ -375,8 +407,6 @@ struct Corr {
 };
 
 bool is_density(const rp_pair_desc &d) { return d.function == RP_CORR_DENSITY; }
-
-d3 column(const double *m, int c) { return {m[c], m[3 + c], m[6 + c]}; }
 
 // TriclinicBox::getVolume / getHeights (core/TriclinicBox.cpp:35-51).
 double box_volume(const double *box) {
@@ -506,8 +536,6 @@ int add_snapshot(Corr *c, void *handle) {
 
     double h[3];
     box_heights(v.box, h);
-    double side_sum = 0;
-    for (int k = 0; k < 3; k++) side_sum += std::sqrt(norm2(column(v.box, k)));
     // the reach of a kept pair: the distance itself (radial), its projection on the axis
     // (linear) or the in-layer distance with at most one layer spacing across (layerwise)
     double reach = d.max_r;
@@ -525,11 +553,31 @@ int add_snapshot(Corr *c, void *handle) {
         d3 dir = normalized3(cross3(s[(a + 1) % 3], s[(a + 2) % 3]));
         G.dir[0] = dir.x, G.dir[1] = dir.y, G.dir[2] = dir.z;
     }
-    // FP32 pre-filter margins: relative coordinates rounded to FP32 move a point by at most
-    // ~2e-7 of the side lengths; the FP32 distance itself is good to ~1e-6
-    const double thr = reach * (1 + 1e-5) + 1e-6 * side_sum;
+    // FP32 error bound.  A focal point's relative coordinates lie within R of the box
+    // ([0, 1) plus the focal offset's reach); rounding them to FP32 moves a separation by at
+    // most 2^-24 (2R + 1/2) per coordinate, and the FP32 product with the box and the norm
+    // add at most a few 2^-24 of sum |B_ik| and of the distance: in all at most
+    // 6e-8 (2R + 2.5) sum |B_ik| + 2e-7 d.  m_abs and m_rel take 2.5 and 5 times that, so an
+    // FP32 distance d32 brackets the FP64 one in d32 -+ m with room for the FP64 rounding of
+    // the bracket itself.
+    double inv_row = 0, babs = 0;
+    for (int i = 0; i < 3; i++) {
+        inv_row = std::max(inv_row, std::sqrt(norm2(d3{v.inv[3 * i], v.inv[3 * i + 1], v.inv[3 * i + 2]})));
+        for (int k = 0; k < 3; k++) babs += std::abs(v.box[3 * i + k]);
+    }
+    const double R = 1.0 + std::sqrt(norm2(d3{d.focal[0], d.focal[1], d.focal[2]})) * inv_row;
+    const double m_abs = 1.5e-7 * (2 * R + 3) * babs, m_rel = 1e-6;
+    // in bin units, with the FP32 roundings of t (1 / step and the product) and of t -+ m
+    // (at most 2.4e-7 t in all) added to the relative part
+    G.inv_step32 = static_cast<float>(1.0 / G.step);
+    G.bin_abs = static_cast<float>(m_abs / G.step * (1 + 1e-6));
+    G.bin_rel = static_cast<float>(m_rel + 5e-7);
+    G.in_lo = static_cast<float>(d.num_bins * (1 - 1e-6));
+    G.in_hi = static_cast<float>(d.num_bins * (1 + 1e-6));
+    const double thr = reach * (1 + m_rel) + m_abs;
     G.thr2_32 = static_cast<float>(thr * thr);
     G.lin_thr32 = static_cast<float>(thr / h[std::min(std::max(d.linear_axis, 0), 2)]);
+    G.h32 = static_cast<float>(h[std::min(std::max(d.linear_axis, 0), 2)]);
     G.edge32 = 1e-4f;
     G.fp64_only = (d.flags & RP_CORR_FP64_ONLY) ? 1 : 0;
 

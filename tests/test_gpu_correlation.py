@@ -128,26 +128,36 @@ def test_full_size_counts_match_the_oracle(oracle, engine, workload, max_r, nb):
     with observable(case) as obs, GpuPacking(*cfg) as g:
         obs.add_snapshot(g)
         counts, _ = obs.last_snapshot()
-        tested = obs.info()["pairs_tested"]
     want = po.pair_counts(d, *cfg[2:5])
     assert np.array_equal(counts, want)
-    assert tested >= counts.sum()
 
 
-def test_full_size_grid_equals_all_pairs(engine):
-    # 10^6 spherocylinders: the cell grid finds every pair within reach exactly once (the
-    # all-pairs enumeration examines 5 x 10^11 pairs on the GPU); g(r) tends to 1
+@pytest.mark.parametrize("focal,fn", [("o", 0), ("beg", 1)])
+def test_full_size_grid_and_binning_equal_exhaustive(engine, focal, fn):
+    # 10^6 spherocylinders after a few sweeps: the cell grid finds every pair within reach
+    # exactly once (the all-pairs enumeration examines 5 x 10^11 pairs on the GPU), and the
+    # FP32 binning with its FP64 guard band bins every pair as FP64 alone; g(r) tends to 1
     from rampack_gb300 import _lib
     from rampack_gb300 import workloads as W
     from rampack_gb300.packing import GpuPacking
     cfg = W.config_sc_1e6()
-    case = ("sc_l2", 0, 0, (0, 0, 1), 0, 0, "o", 8.0, 100)
+    case = ("sc_l2", 0, 0, (0, 0, 1), fn, 0, focal, 8.0, 200)
     with GpuPacking(*cfg) as g:
+        for c in range(3):
+            g.sweep(0.2, 0.2, seed=11, counter=c, stats=False)
         res = []
-        for flags in (0, _lib.CORR_ALL_PAIRS):
+        for flags in (0, _lib.CORR_ALL_PAIRS, _lib.CORR_FP64_ONLY):
             with observable(case, flags) as obs:
                 obs.add_snapshot(g)
                 res.append(obs.values())
-    assert np.array_equal(res[0][2], res[1][2]) and np.array_equal(res[0][1], res[1][1])
-    assert res[0][2].sum() > 0
-    assert abs(res[0][1][-10:].mean() - 1.0) < 0.1
+                if flags == 0:
+                    fp64 = obs.info()["pairs_tested"]
+    for r in res[1:]:
+        assert np.array_equal(res[0][2], r[2])
+        if fn == 0:
+            assert np.array_equal(res[0][1], r[1])
+        else:
+            assert np.allclose(res[0][1], r[1], rtol=AVG_RTOL, atol=1e-12, equal_nan=True)
+    assert res[0][2].sum() > 0 and fp64 < res[0][2].sum() / 10
+    if fn == 0:
+        assert abs(res[0][1][-20:].mean() - 1.0) < 0.1
