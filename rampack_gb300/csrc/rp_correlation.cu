@@ -211,6 +211,66 @@ __device__ void decide_pair(const CorrGeom &G, const SortedPoints &S, int64_t lo
     if (F != RP_CORR_DENSITY) atomicAdd(hs + bin, axis_function<F>(load3(S.ax64, lo), load3(S.ax64, hi), d));
 }
 
+// One candidate pair (a, b), a's slot below b's: the FP32 pre-filter and binning.  Returns
+// true when the pair needs the FP64 decision (the caller queues it).
+template <int E, int F>
+__device__ __forceinline__ bool examine_pair(const CorrGeom &G, const SortedPoints &S, int64_t a, int64_t b,
+                                             float4 ra, unsigned long long *hc, double *hs) {
+    const float4 rb = S.rel32[b];
+    float f[3] = {rb.x - ra.x, rb.y - ra.y, rb.z - ra.z};
+    const float e = 0.5f - G.edge32;
+    bool edge = false;
+    for (int k = 0; k < 3; k++) {
+        f[k] -= rintf(f[k]);
+        edge |= fabsf(f[k]) > e;
+    }
+    const bool fast = !edge && !G.fp64_only;
+    float d32 = 0.f;
+    if (fast) {
+        if (E == RP_PAIRS_LINEAR) {
+            const float fa = fabsf(f[0] * (G.lin_axis == 0) + f[1] * (G.lin_axis == 1) + f[2] * (G.lin_axis == 2));
+            if (fa > G.lin_thr32) return false;
+            d32 = fa * G.h32;
+        } else {
+            float d2 = 0.f;
+            for (int i = 0; i < 3; i++) {
+                float v = G.box32[3 * i] * f[0] + G.box32[3 * i + 1] * f[1] + G.box32[3 * i + 2] * f[2];
+                d2 += v * v;
+            }
+            if (d2 > G.thr2_32) return false;
+            d32 = sqrtf(d2);
+        }
+    }
+    // FP32 binning: when the FP64 distance's whole error interval lies in one bin below max_r
+    // (or beyond max_r), that bin is the reference's; pairs near a bin edge or max_r are
+    // decided in FP64.  The layerwise enumerator and S221 (which reads the separation)
+    // always take FP64.
+    if (E != RP_PAIRS_LAYERWISE && F != RP_CORR_S221 && fast) {
+        const float t = d32 * G.inv_step32;
+        const float m = G.bin_abs + G.bin_rel * t;
+        const float lo = t - m, hi = t + m;
+        if (lo > G.in_hi) return false;
+        if (hi < G.in_lo) {
+            const float qlo = floorf(lo), qhi = floorf(hi);
+            if (qlo == qhi) {
+                const int bin = min(static_cast<int>(qlo), G.nb - 1);
+                atomicAdd(hc + bin, 1ull);
+                if (F != RP_CORR_DENSITY)
+                    atomicAdd(hs + bin, axis_function<F>(load3(S.ax64, a), load3(S.ax64, b), d3{0.0, 0.0, 0.0}));
+                return false;
+            }
+        }
+    }
+    return true;
+}
+
+// One warp per focal point a: the (up to 27) neighbour cells' slot ranges above a are laid
+// end to end and the lanes walk them together, so every lane has the same trip count and
+// the loads of consecutive slots coalesce.  Lane l < 27 holds neighbour cell l's first slot
+// and the running total of the range lengths; each lane finds the cell of its candidate by
+// advancing through that prefix with warp-uniform shuffles.  Pairs that need the FP64
+// decision (and the averaged correlations' pairs (i, i)) are queued per warp in shared
+// memory and decided 32 at a time, all lanes busy: FP64 issue is scarce on this part.
 template <int E, int F>
 __global__ void __launch_bounds__(CORR_THREADS, 2) k_corr_pairs(CorrGeom G, SortedPoints S, const int32_t *start,
                                                              int64_t n, int use_smem, unsigned long long *hist,
@@ -227,92 +287,90 @@ __global__ void __launch_bounds__(CORR_THREADS, 2) k_corr_pairs(CorrGeom G, Sort
         }
         __syncthreads();
     }
+    __shared__ int2 queue[CORR_THREADS / 32][64];
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    int2 *q = queue[threadIdx.x >> 5];
+    int qn = 0;   // queued pairs of this warp (warp-uniform)
+    // queue the lanes' pairs with `need` (slots ordered by particle index), and decide a full
+    // batch of 32 when there is one
+    auto enqueue = [&](bool need, int lo, int hi) {
+        const unsigned bal = __ballot_sync(full, need);
+        if (need) q[qn + __popc(bal & ((1u << lane) - 1))] = make_int2(lo, hi);
+        qn += __popc(bal);
+        __syncwarp();
+        if (qn >= 32) {
+            const int2 pr = q[qn - 32 + lane];
+            __syncwarp();
+            decide_pair<E, F>(G, S, pr.x, pr.y, hc, hs);
+            qn -= 32;
+        }
+    };
+    const int64_t warps = (int64_t)gridDim.x * (CORR_THREADS / 32);
     unsigned long long my_tested = 0;
-    const float e = 0.5f - G.edge32;
-    for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x) {
+    // neighbour offsets: -1..1 in a dimension of three or more cells, 0 otherwise
+    const int wx = G.nc[0] >= 3 ? 3 : 1, wy = G.nc[1] >= 3 ? 3 : 1, wz = G.nc[2] >= 3 ? 3 : 1;
+    const int ncells = wx * wy * wz;
+    for (int64_t a = blockIdx.x * (int64_t)(CORR_THREADS / 32) + (threadIdx.x >> 5); a < n; a += warps) {
         const int ia = S.idx[a];
         const int ca = S.cell[a];
         const float4 ra = S.rel32[a];
         if (F != RP_CORR_DENSITY) {  // the averaged correlations also take the pair (i, i)
-            decide_pair<E, F>(G, S, a, a, hc, hs);
-            my_tested++;
+            enqueue(lane == 0, static_cast<int>(a), static_cast<int>(a));
+            my_tested += lane == 0;
         }
-        const int cx = ca % G.nc[0], cy = (ca / G.nc[0]) % G.nc[1], cz = ca / (G.nc[0] * G.nc[1]);
-        const int lz = G.nc[2] >= 3 ? -1 : 0, hz = G.nc[2] >= 3 ? 1 : 0;
-        const int ly = G.nc[1] >= 3 ? -1 : 0, hy = G.nc[1] >= 3 ? 1 : 0;
-        const int lx = G.nc[0] >= 3 ? -1 : 0, hx = G.nc[0] >= 3 ? 1 : 0;
-        for (int dz = lz; dz <= hz; dz++) {
-            const int z = (cz + dz + G.nc[2]) % G.nc[2];
-            for (int dy = ly; dy <= hy; dy++) {
-                const int y = (cy + dy + G.nc[1]) % G.nc[1];
-                for (int dx = lx; dx <= hx; dx++) {
-                    const int x = (cx + dx + G.nc[0]) % G.nc[0];
-                    const int c = (z * G.nc[1] + y) * G.nc[0] + x;
-                    int64_t b0 = start[c];
-                    const int64_t b1 = start[c + 1];
-                    if (b0 <= a) b0 = a + 1;
-                    for (int64_t b = b0; b < b1; b++) {
-                        const float4 rb = S.rel32[b];
-                        float f[3] = {rb.x - ra.x, rb.y - ra.y, rb.z - ra.z};
-                        bool edge = false;
-                        for (int k = 0; k < 3; k++) {
-                            f[k] -= rintf(f[k]);
-                            edge |= fabsf(f[k]) > e;
-                        }
-                        const bool fast = !edge && !G.fp64_only;
-                        float d32 = 0.f;
-                        if (fast) {
-                            if (E == RP_PAIRS_LINEAR) {
-                                const float fa = fabsf(f[0] * (G.lin_axis == 0) + f[1] * (G.lin_axis == 1) +
-                                                       f[2] * (G.lin_axis == 2));
-                                if (fa > G.lin_thr32) continue;
-                                d32 = fa * G.h32;
-                            } else {
-                                float d2 = 0.f;
-                                for (int i = 0; i < 3; i++) {
-                                    float s = G.box32[3 * i] * f[0] + G.box32[3 * i + 1] * f[1] +
-                                              G.box32[3 * i + 2] * f[2];
-                                    d2 += s * s;
-                                }
-                                if (d2 > G.thr2_32) continue;
-                                d32 = sqrtf(d2);
-                            }
-                        }
-                        // FP32 binning: when the FP64 distance's whole error interval lies in
-                        // one bin below max_r (or beyond max_r), that bin is the reference's;
-                        // pairs near a bin edge or max_r are decided in FP64 below.  The
-                        // layerwise enumerator and S221 (which reads the separation) always
-                        // take FP64.
-                        if (E != RP_PAIRS_LAYERWISE && F != RP_CORR_S221 && fast) {
-                            const float t = d32 * G.inv_step32;
-                            const float m = G.bin_abs + G.bin_rel * t;
-                            const float lo = t - m, hi = t + m;
-                            if (lo > G.in_hi) continue;
-                            if (hi < G.in_lo) {
-                                const float qlo = floorf(lo), qhi = floorf(hi);
-                                if (qlo == qhi) {
-                                    const int bin = min(static_cast<int>(qlo), G.nb - 1);
-                                    atomicAdd(hc + bin, 1ull);
-                                    if (F != RP_CORR_DENSITY)
-                                        atomicAdd(hs + bin, axis_function<F>(load3(S.ax64, a), load3(S.ax64, b),
-                                                                             d3{0.0, 0.0, 0.0}));
-                                    continue;
-                                }
-                            }
-                        }
-                        my_tested++;
-                        const int ib = S.idx[b];
-                        if (ia < ib)
-                            decide_pair<E, F>(G, S, a, b, hc, hs);
-                        else
-                            decide_pair<E, F>(G, S, b, a, hc, hs);
-                    }
+        int first = 0, len = 0;
+        if (lane < ncells) {
+            const int cx = ca % G.nc[0], cy = (ca / G.nc[0]) % G.nc[1], cz = ca / (G.nc[0] * G.nc[1]);
+            const int ox = lane % wx - (wx == 3), oy = (lane / wx) % wy - (wy == 3), oz = lane / (wx * wy) - (wz == 3);
+            const int x = (cx + ox + G.nc[0]) % G.nc[0], y = (cy + oy + G.nc[1]) % G.nc[1],
+                      z = (cz + oz + G.nc[2]) % G.nc[2];
+            const int c = (z * G.nc[1] + y) * G.nc[0] + x;
+            int64_t b0 = start[c];
+            const int64_t b1 = start[c + 1];
+            if (b0 <= a) b0 = a + 1;
+            first = static_cast<int>(b0);
+            len = b1 > b0 ? static_cast<int>(b1 - b0) : 0;
+        }
+        int incl = len;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(full, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const int total = __shfl_sync(full, incl, 31);
+        int cur = 0;
+        for (int base = 0; base < total; base += 32) {
+            const int k = base + lane;
+            for (;;) {   // advance to the cell holding candidate k (at most 27 steps in all)
+                const int end = __shfl_sync(full, incl, cur);
+                const bool adv = k < total && k >= end;
+                if (!__any_sync(full, adv)) break;
+                if (adv) cur++;
+            }
+            const int cfirst = __shfl_sync(full, first, cur);
+            const int cend = __shfl_sync(full, incl, cur);
+            const int clen = __shfl_sync(full, len, cur);
+            bool need = false;
+            int lo = 0, hi = 0;
+            if (k < total) {
+                const int b = cfirst + (k - (cend - clen));
+                need = examine_pair<E, F>(G, S, a, b, ra, hc, hs);
+                if (need) {
+                    const bool a_first = ia < S.idx[b];
+                    lo = a_first ? static_cast<int>(a) : b;
+                    hi = a_first ? b : static_cast<int>(a);
+                    my_tested++;
                 }
             }
+            enqueue(need, lo, hi);
         }
     }
-    for (int o = 16; o > 0; o >>= 1) my_tested += __shfl_xor_sync(0xffffffffu, my_tested, o);
-    if ((threadIdx.x & 31) == 0 && my_tested) atomicAdd(tested, my_tested);
+    if (lane < qn) {   // the warp's last, partial batch
+        const int2 pr = q[lane];
+        decide_pair<E, F>(G, S, pr.x, pr.y, hc, hs);
+    }
+    for (int o = 16; o > 0; o >>= 1) my_tested += __shfl_xor_sync(full, my_tested, o);
+    if (lane == 0 && my_tested) atomicAdd(tested, my_tested);
     if (use_smem) {
         __syncthreads();
         for (int b = threadIdx.x; b < G.nb; b += blockDim.x) {
@@ -639,7 +697,8 @@ int add_snapshot(Corr *c, void *handle) {
         CORR_CUDA(c, cudaGetLastError());
         int dev_sms = 152;
         cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, v.device);
-        const int grid = static_cast<int>(std::min<int64_t>(nblk, int64_t(dev_sms) * 4));
+        const int64_t wblk = (v.n + CORR_THREADS / 32 - 1) / (CORR_THREADS / 32);   // one warp per point
+        const int grid = static_cast<int>(std::min<int64_t>(wblk, int64_t(dev_sms) * 6));
         const int use_smem = nb <= SMEM_BINS ? 1 : 0;
         const size_t smem = use_smem ? size_t(nb) * (axes ? 16 : 8) : 0;
         cudaError_t le;
