@@ -61,7 +61,8 @@ struct CorrGeom {
     float lin_thr32; // FP32 rejection: |relative separation| along lin_axis above this
     float h32;       // the height across side lin_axis (linear enumerator)
     // FP32 binning: with t = d32 / step (FP32), the FP64 distance / step lies within
-    // t -+ (bin_abs + bin_rel * t); in range for sure below in_lo, out of range above in_hi
+    // t -+ (bin_abs + bin_rel * t); in range for sure below in_lo, out of range above in_hi;
+    // the bin is floor(t) when the interval stays inside it
     float inv_step32, bin_abs, bin_rel, in_lo, in_hi;
     float edge32;    // no FP32 rejection when a folded relative separation is this near 1/2
     int fp64_only;   // RP_CORR_FP64_ONLY: no FP32 pre-filter
@@ -238,7 +239,7 @@ __device__ __forceinline__ bool examine_pair(const CorrGeom &G, const SortedPoin
                 d2 += v * v;
             }
             if (d2 > G.thr2_32) return false;
-            d32 = sqrtf(d2);
+            d32 = d2 > 0.f ? d2 * rsqrtf(d2) : 0.f;   // within 2^-21 relative: inside the margin
         }
     }
     // FP32 binning: when the FP64 distance's whole error interval lies in one bin below max_r
@@ -248,17 +249,14 @@ __device__ __forceinline__ bool examine_pair(const CorrGeom &G, const SortedPoin
     if (E != RP_PAIRS_LAYERWISE && F != RP_CORR_S221 && fast) {
         const float t = d32 * G.inv_step32;
         const float m = G.bin_abs + G.bin_rel * t;
-        const float lo = t - m, hi = t + m;
-        if (lo > G.in_hi) return false;
-        if (hi < G.in_lo) {
-            const float qlo = floorf(lo), qhi = floorf(hi);
-            if (qlo == qhi) {
-                const int bin = min(static_cast<int>(qlo), G.nb - 1);
-                atomicAdd(hc + bin, 1ull);
-                if (F != RP_CORR_DENSITY)
-                    atomicAdd(hs + bin, axis_function<F>(load3(S.ax64, a), load3(S.ax64, b), d3{0.0, 0.0, 0.0}));
-                return false;
-            }
+        if (t - m > G.in_hi) return false;
+        const float k = floorf(t), frac = t - k;   // exact
+        if (t + m < G.in_lo && frac >= m && frac + m < 1.f) {
+            const int bin = min(static_cast<int>(k), G.nb - 1);
+            atomicAdd(hc + bin, 1ull);
+            if (F != RP_CORR_DENSITY)
+                atomicAdd(hs + bin, axis_function<F>(load3(S.ax64, a), load3(S.ax64, b), d3{0.0, 0.0, 0.0}));
+            return false;
         }
     }
     return true;
@@ -296,6 +294,7 @@ __global__ void __launch_bounds__(CORR_THREADS, 2) k_corr_pairs(CorrGeom G, Sort
     // batch of 32 when there is one
     auto enqueue = [&](bool need, int lo, int hi) {
         const unsigned bal = __ballot_sync(full, need);
+        if (bal == 0) return;
         if (need) q[qn + __popc(bal & ((1u << lane) - 1))] = make_int2(lo, hi);
         qn += __popc(bal);
         __syncwarp();
@@ -628,8 +627,8 @@ int add_snapshot(Corr *c, void *handle) {
     // in bin units, with the FP32 roundings of t (1 / step and the product) and of t -+ m
     // (at most 2.4e-7 t in all) added to the relative part
     G.inv_step32 = static_cast<float>(1.0 / G.step);
-    G.bin_abs = static_cast<float>(m_abs / G.step * (1 + 1e-6));
-    G.bin_rel = static_cast<float>(m_rel + 5e-7);
+    G.bin_abs = static_cast<float>(m_abs / G.step * (1 + 1e-6) + 2.5e-7);
+    G.bin_rel = static_cast<float>(m_rel + 2.5e-6);   // also the rsqrt-based FP32 square root
     G.in_lo = static_cast<float>(d.num_bins * (1 - 1e-6));
     G.in_hi = static_cast<float>(d.num_bins * (1 + 1e-6));
     const double thr = reach * (1 + m_rel) + m_abs;
