@@ -50,6 +50,7 @@ struct CorrGeom {
     double box[9], inv[9];
     float box32[9];
     int nc[3];
+    int span[3];     // neighbour cells searched each way: 2 (cells of half the reach), 1, or 0 (one cell)
     int ncell;
     int nb;
     int lin_axis;
@@ -308,8 +309,8 @@ __global__ void __launch_bounds__(CORR_THREADS, 2) k_corr_pairs(CorrGeom G, Sort
     const int64_t warps = (int64_t)gridDim.x * (CORR_THREADS / 32);
     unsigned long long my_tested = 0;
     // neighbour offsets: -1..1 in a dimension of three or more cells, 0 otherwise
-    const int wx = G.nc[0] >= 3 ? 3 : 1, wy = G.nc[1] >= 3 ? 3 : 1, wz = G.nc[2] >= 3 ? 3 : 1;
-    const int ncells = wx * wy * wz;
+    const int wx = 2 * G.span[0] + 1, wy = 2 * G.span[1] + 1, wz = 2 * G.span[2] + 1;
+    const int ncells = wx * wy * wz;   // at most 125
     for (int64_t a = blockIdx.x * (int64_t)(CORR_THREADS / 32) + (threadIdx.x >> 5); a < n; a += warps) {
         const int ia = S.idx[a];
         const int ca = S.cell[a];
@@ -318,50 +319,53 @@ __global__ void __launch_bounds__(CORR_THREADS, 2) k_corr_pairs(CorrGeom G, Sort
             enqueue(lane == 0, static_cast<int>(a), static_cast<int>(a));
             my_tested += lane == 0;
         }
-        int first = 0, len = 0;
-        if (lane < ncells) {
-            const int cx = ca % G.nc[0], cy = (ca / G.nc[0]) % G.nc[1], cz = ca / (G.nc[0] * G.nc[1]);
-            const int ox = lane % wx - (wx == 3), oy = (lane / wx) % wy - (wy == 3), oz = lane / (wx * wy) - (wz == 3);
-            const int x = (cx + ox + G.nc[0]) % G.nc[0], y = (cy + oy + G.nc[1]) % G.nc[1],
-                      z = (cz + oz + G.nc[2]) % G.nc[2];
-            const int c = (z * G.nc[1] + y) * G.nc[0] + x;
-            int64_t b0 = start[c];
-            const int64_t b1 = start[c + 1];
-            if (b0 <= a) b0 = a + 1;
-            first = static_cast<int>(b0);
-            len = b1 > b0 ? static_cast<int>(b1 - b0) : 0;
-        }
-        int incl = len;
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(full, incl, o);
-            if (lane >= o) incl += y;
-        }
-        const int total = __shfl_sync(full, incl, 31);
-        int cur = 0;
-        for (int base = 0; base < total; base += 32) {
-            const int k = base + lane;
-            for (;;) {   // advance to the cell holding candidate k (at most 27 steps in all)
-                const int end = __shfl_sync(full, incl, cur);
-                const bool adv = k < total && k >= end;
-                if (!__any_sync(full, adv)) break;
-                if (adv) cur++;
+        const int cx = ca % G.nc[0], cy = (ca / G.nc[0]) % G.nc[1], cz = ca / (G.nc[0] * G.nc[1]);
+        for (int chunk = 0; chunk < ncells; chunk += 32) {   // up to 32 neighbour cells at a time
+            const int nbr = chunk + lane;
+            int first = 0, len = 0;
+            if (nbr < ncells) {
+                const int ox = nbr % wx - G.span[0], oy = (nbr / wx) % wy - G.span[1], oz = nbr / (wx * wy) - G.span[2];
+                const int x = (cx + ox + G.nc[0]) % G.nc[0], y = (cy + oy + G.nc[1]) % G.nc[1],
+                          z = (cz + oz + G.nc[2]) % G.nc[2];
+                const int c = (z * G.nc[1] + y) * G.nc[0] + x;
+                int64_t b0 = start[c];
+                const int64_t b1 = start[c + 1];
+                if (b0 <= a) b0 = a + 1;
+                first = static_cast<int>(b0);
+                len = b1 > b0 ? static_cast<int>(b1 - b0) : 0;
             }
-            const int cfirst = __shfl_sync(full, first, cur);
-            const int cend = __shfl_sync(full, incl, cur);
-            const int clen = __shfl_sync(full, len, cur);
-            bool need = false;
-            int lo = 0, hi = 0;
-            if (k < total) {
-                const int b = cfirst + (k - (cend - clen));
-                need = examine_pair<E, F>(G, S, a, b, ra, hc, hs);
-                if (need) {
-                    const bool a_first = ia < S.idx[b];
-                    lo = a_first ? static_cast<int>(a) : b;
-                    hi = a_first ? b : static_cast<int>(a);
-                    my_tested++;
+            int incl = len;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(full, incl, o);
+                if (lane >= o) incl += y;
+            }
+            const int total = __shfl_sync(full, incl, 31);
+            int cur = 0;
+            for (int base = 0; base < total; base += 32) {
+                const int k = base + lane;
+                for (;;) {   // advance to the cell holding candidate k (at most 32 steps in all)
+                    const int end = __shfl_sync(full, incl, cur);
+                    const bool adv = k < total && k >= end;
+                    if (!__any_sync(full, adv)) break;
+                    if (adv) cur++;
                 }
+                const int cfirst = __shfl_sync(full, first, cur);
+                const int cend = __shfl_sync(full, incl, cur);
+                const int clen = __shfl_sync(full, len, cur);
+                bool need = false;
+                int lo = 0, hi = 0;
+                if (k < total) {
+                    const int b = cfirst + (k - (cend - clen));
+                    need = examine_pair<E, F>(G, S, a, b, ra, hc, hs);
+                    if (need) {
+                        const bool a_first = ia < S.idx[b];
+                        lo = a_first ? static_cast<int>(a) : b;
+                        hi = a_first ? b : static_cast<int>(a);
+                        my_tested++;
+                    }
+                }
+                enqueue(need, lo, hi);
             }
-            enqueue(need, lo, hi);
         }
     }
     if (lane < qn) {   // the warp's last, partial batch
@@ -638,23 +642,49 @@ int add_snapshot(Corr *c, void *handle) {
     G.edge32 = 1e-4f;
     G.fp64_only = (d.flags & RP_CORR_FP64_ONLY) ? 1 : 0;
 
-    // cells: at least the reach across in every dimension that has three or more of them
+    // cells: in a dimension with room for five or more, half the reach across (searched two
+    // cells each way: the 5x5x5 block holds 15.6 reach^3 against 27 for reach-wide cells),
+    // else the reach across with three or more (one cell each way), else one cell.  A pair
+    // within reach is then at most `span` cells apart in every dimension, and the offsets
+    // -span..span name distinct cells.  Half-reach cells are used while they hold a few
+    // points each on average.
     int64_t ncell = 1;
+    const bool all_pairs = d.flags & RP_CORR_ALL_PAIRS;
+    double half_cells = 1;
     for (int k = 0; k < 3; k++) {
-        int m = 1;
         const bool restricted = d.enumerator != RP_PAIRS_LINEAR || k == d.linear_axis;
-        if (restricted && !(d.flags & RP_CORR_ALL_PAIRS)) {
-            double q = std::floor(h[k] / (reach * (1 + 1e-5)));
-            if (q >= 3) m = static_cast<int>(std::min(q, 1024.0));
+        half_cells *= restricted ? std::max(1.0, std::floor(2 * h[k] / (reach * (1 + 1e-5)))) : 1.0;
+    }
+    const bool halves = static_cast<double>(v.n) >= 4 * half_cells;
+    for (int k = 0; k < 3; k++) {
+        int m = 1, sp = 0;
+        const bool restricted = d.enumerator != RP_PAIRS_LINEAR || k == d.linear_axis;
+        if (restricted && !all_pairs) {
+            const double q2 = std::floor(2 * h[k] / (reach * (1 + 1e-5)));
+            const double q1 = std::floor(h[k] / (reach * (1 + 1e-5)));
+            if (halves && q2 >= 5) {
+                m = static_cast<int>(std::min(q2, 2048.0));
+                sp = 2;
+            } else if (q1 >= 3) {
+                m = static_cast<int>(std::min(q1, 1024.0));
+                sp = 1;
+            }
         }
         G.nc[k] = m;
+        G.span[k] = sp;
     }
-    const int64_t max_cells = std::max<int64_t>(27, 2 * v.n);
+    const int64_t max_cells = std::max<int64_t>(125, 2 * v.n);
     for (;;) {
         ncell = int64_t(G.nc[0]) * G.nc[1] * G.nc[2];
         if (ncell <= max_cells) break;
+        // coarser cells keep every pair within reach `span` cells apart; too few of them for
+        // distinct offsets: one cell in that dimension
         int k = (G.nc[0] >= G.nc[1] && G.nc[0] >= G.nc[2]) ? 0 : (G.nc[1] >= G.nc[2] ? 1 : 2);
-        G.nc[k] = G.nc[k] * 3 / 4 >= 3 ? G.nc[k] * 3 / 4 : 1;
+        G.nc[k] = G.nc[k] * 3 / 4;
+        if (G.nc[k] < 2 * G.span[k] + 1) {
+            G.nc[k] = 1;
+            G.span[k] = 0;
+        }
     }
     G.ncell = static_cast<int>(ncell);
 
