@@ -37,6 +37,7 @@
 #include "core/move_samplers/TranslationSampler.h"
 #include "core/shapes/PolysphereTraits.h"
 #include "core/shapes/PolysphereBananaTraits.h"
+#include "core/shapes/PolyspherocylinderTraits.h"
 #include "core/shapes/SphereTraits.h"
 #include "core/shapes/SpherocylinderTraits.h"
 #include "core/volume_scalers/AnisotropicVolumeScaler.h"
@@ -59,6 +60,17 @@ std::shared_ptr<ShapeTraits> make_traits(int kind, const double *prm, int np) {
             data.emplace_back(Vector<3>{prm[1 + 4 * i], prm[2 + 4 * i], prm[3 + 4 * i]}, prm[4 + 4 * i]);
         PolysphereTraits::PolysphereGeometry geom(std::move(data), std::nullopt, std::nullopt, {0, 0, 0}, 1.0);
         return std::make_shared<PolysphereTraits>(std::move(geom));
+    }
+    if (kind == 3 && np >= 1) {
+        int k = static_cast<int>(prm[0]);
+        std::vector<PolyspherocylinderTraits::SpherocylinderData> data;
+        for (int i = 0; i < k; i++) {
+            const double *d = prm + 1 + 7 * i;
+            data.emplace_back(Vector<3>{d[0], d[1], d[2]}, Vector<3>{d[3], d[4], d[5]}, d[6]);
+        }
+        PolyspherocylinderTraits::PolyspherocylinderGeometry geom(std::move(data), std::nullopt, std::nullopt,
+                                                                  {0, 0, 0}, 1.0);
+        return std::make_shared<PolyspherocylinderTraits>(std::move(geom));
     }
     return nullptr;
 }

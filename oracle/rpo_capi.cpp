@@ -36,6 +36,19 @@ bool make_interaction(int kind, const double *prm, int np, Interaction &out) {
             out.centres.push_back({prm[1 + 4 * i], prm[2 + 4 * i], prm[3 + 4 * i]});
             out.radii.push_back(prm[4 + 4 * i]);
         }
+    } else if (kind == 3) {
+        // polyspherocylinder {k, (x, y, z, hx, hy, hz, r) per spherocylinder}: a multi-centre
+        // body like the polysphere, each centre with a half axis
+        if (np < 1) return false;
+        int k = static_cast<int>(prm[0]);
+        if (k < 1 || np < 1 + 7 * k) return false;
+        out.kind = POLYSPHERE;
+        for (int i = 0; i < k; i++) {
+            const double *d = prm + 1 + 7 * i;
+            out.centres.push_back({d[0], d[1], d[2]});
+            out.half_axes.push_back({d[3], d[4], d[5]});
+            out.radii.push_back(d[6]);
+        }
     } else {
         return false;
     }

@@ -49,11 +49,25 @@ struct Interaction {
     double length = 0;     // spherocylinder cylinder length
     std::vector<V3> centres;      // polysphere body-frame sphere centres
     std::vector<double> radii;    // polysphere sphere radii
+    // polyspherocylinders (PolyspherocylinderTraits): each centre is a spherocylinder with
+    // this body-frame half axis (SpherocylinderData::halfAxis); empty for polyspheres
+    std::vector<V3> half_axes;
+
+    bool segments() const { return !half_axes.empty(); }
+    // SpherocylinderData::circumsphereRadius = radius + |halfAxis|
+    // (PolyspherocylinderTraits.cpp:78-84)
+    double circumsphere(std::size_t i) const { return radii[i] + std::sqrt(norm2(half_axes[i])); }
 
     // SphereTraits.h:34, SpherocylinderTraits.h:81, PolysphereTraits.cpp:115-121
     double range() const {
         if (kind == SPHERE) return 2 * radius;
         if (kind == SPHEROCYLINDER) return 2 * radius + length;
+        if (segments()) {   // PolyspherocylinderTraits.cpp:140-147
+            double m = circumsphere(0);
+            for (std::size_t i = 1; i < radii.size(); i++)
+                if (m < circumsphere(i)) m = circumsphere(i);
+            return 2 * m;
+        }
         return 2 * *std::max_element(radii.begin(), radii.end());
     }
     // Interaction.cpp:55-70
@@ -70,6 +84,12 @@ struct Interaction {
     // closer to the wall plane than the radius), PolysphereTraits.cpp:129-136 (centre idx)
     bool overlap_with_wall(const V3 &pos, const M3 &rot, std::size_t idx, const V3 &origin, const V3 &wall) const {
         if (kind == SPHERE) return dot(wall, sub(pos, origin)) < radius;
+        if (kind == POLYSPHERE && segments()) {   // PolyspherocylinderTraits.cpp:149-166
+            V3 half = mv(rot, half_axes[idx]);
+            if (dot(wall, sub(sub(pos, half), origin)) < radii[idx]) return true;
+            if (dot(wall, sub(add(pos, half), origin)) < radii[idx]) return true;
+            return false;
+        }
         if (kind == POLYSPHERE) return dot(wall, sub(pos, origin)) < radii[idx];
         V3 half = vscale(column(rot, 2), length / 2);
         if (dot(wall, sub(add(pos, half), origin)) < radius) return true;
@@ -96,6 +116,17 @@ struct Interaction {
             else if (d2 >= std::pow(2 * radius + length, 2)) return false;
             return segment_distance2(cap(-1, p1, o1), cap(1, p1, o1), cap(-1, p2bc, o2), cap(1, p2bc, o2))
                    < 4 * radius * radius;
+        } else if (segments()) {
+            // PolyspherocylinderTraits.cpp:102-124
+            V3 p2bc = add(p2, bc.translation(p1, p2));
+            double d2 = norm2(sub(p2bc, p1));
+            double in = radii[i1] + radii[i2];
+            double in2 = in * in;
+            if (d2 < in2) return true;
+            double circ = circumsphere(i1) + circumsphere(i2);
+            if (d2 >= circ * circ) return false;
+            V3 h1 = mv(o1, half_axes[i1]), h2 = mv(o2, half_axes[i2]);
+            return segment_distance2(add(p1, h1), sub(p1, h1), add(p2bc, h2), sub(p2bc, h2)) < in2;
         } else {
             // PolysphereTraits.cpp:97-106
             double r = radii[i1] + radii[i2];

@@ -16,6 +16,7 @@ import math
 import numpy as np
 
 SPHERE, SPHEROCYLINDER, POLYSPHERE = 0, 1, 2
+POLYSPHEROCYLINDER = 3
 
 
 def sphere_volume(r: float) -> float:
@@ -191,3 +192,21 @@ def config_replicas_64(seed: int = 1234):
         kind = SPHERE if i < 32 else SPHEROCYLINDER
         out.append(replica_lattice(kind, int(sizes[i]), 0.30) + (float(pressures[i]),))
     return out
+
+
+# A bent rod of two spherocylinders meeting at a 60 degree kink (PolyspherocylinderTraits
+# data: centre, half axis, radius per spherocylinder).
+BENT_ROD = ((-0.35, 0.0, 0.0, 0.3, 0.0, 0.15, 0.25), (0.35, 0.0, 0.0, 0.3, 0.0, -0.15, 0.25))
+
+
+def polyspherocylinder_params(data) -> np.ndarray:
+    """{k, (x, y, z, hx, hy, hz, r) per spherocylinder}."""
+    return np.array([float(len(data))] + [float(v) for d in data for v in d])
+
+
+def bent_rods(counts, spacing=(2.0, 0.62, 0.95)):
+    """Aligned bent rods on an orthorhombic lattice (contact-free at the given spacing)."""
+    pos = lattice(counts, spacing)
+    box = diag_box(counts[0] * spacing[0], counts[1] * spacing[1], counts[2] * spacing[2])
+    return POLYSPHEROCYLINDER, polyspherocylinder_params(BENT_ROD), pos, aligned_rotations(len(pos)), box
+

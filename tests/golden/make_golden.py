@@ -345,7 +345,8 @@ def state_digest(pos, rot) -> np.ndarray:
 
 
 # hard walls: (system, wall mask, translation step, rotation step)
-WALLS = [("hs_small", 1, 0.1, 0.0), ("sc_l2", 5, 0.2, 0.2), ("poly_banana", 2, 0.2, 0.2), ("sc_l2_dense", 7, 0.2, 0.2)]
+WALLS = [("hs_small", 1, 0.1, 0.0), ("sc_l2", 5, 0.2, 0.2), ("poly_banana", 2, 0.2, 0.2), ("sc_l2_dense", 7, 0.2, 0.2),
+         ("psc_bent", 3, 0.15, 0.15)]
 
 
 def gen_walls():

@@ -86,6 +86,20 @@ def sc_tiny():
                       translation_step=0.5, rotation_step=0.5)
 
 
+@functools.lru_cache(maxsize=None)
+def psc_bent():
+    """Bent rods of two spherocylinders (r = 0.25, 60 degree kink), N = 432, 12 NpT cycles."""
+    return thermalise(W.bent_rods((6, 8, 9)), 12, translation_step=0.15, rotation_step=0.15, box_kind=1,
+                      box_step=0.005, pressure=2.0)
+
+
+@functools.lru_cache(maxsize=None)
+def psc_tiny():
+    """Bent rods, N = 24 in a small box (no neighbour grid in the reference), 10 NVT cycles."""
+    return thermalise(W.bent_rods((2, 4, 3), spacing=(2.0, 0.9, 1.2)), 10, translation_step=0.2,
+                      rotation_step=0.2)
+
+
 def compressed(cfg, factor: float):
     """The same configuration with box and positions scaled by `factor` (overlaps for factor < 1)."""
     kind, prm, pos, rot, box = cfg
@@ -97,4 +111,5 @@ def compressed(cfg, factor: float):
 
 
 ALL = {"hs_small": hs_small, "hs_dense": hs_dense, "sc_l2": sc_l2, "sc_l2_dense": sc_l2_dense, "sc_l5": sc_l5,
-       "poly_banana": poly_banana, "poly_dense": poly_dense, "hs_tiny": hs_tiny, "sc_tiny": sc_tiny}
+       "poly_banana": poly_banana, "poly_dense": poly_dense, "hs_tiny": hs_tiny, "sc_tiny": sc_tiny,
+       "psc_bent": psc_bent, "psc_tiny": psc_tiny}

@@ -22,6 +22,11 @@ RUNS = {
     "sc_domains_8_threads": (lambda: W.spherocylinders((8, 8, 8), 0.35, 2.0, 0.5, aspect=(1, 1, 3)), 10,
                              dict(translation_step=0.2, rotation_step=0.2, box_kind=1, box_step=0.005, pressure=1.5,
                                   domains=(2, 2, 2), threads=8)),
+    "bent_rods_triclinic": (lambda: W.bent_rods((5, 7, 7)), 12,
+                            dict(translation_step=0.15, rotation_step=0.15, box_kind=1, box_step=0.005,
+                                 pressure=2.0)),
+    "bent_rods_dense_nvt": (lambda: W.bent_rods((4, 6, 6), spacing=(1.9, 0.6, 0.92)), 6,
+                                   dict(translation_step=0.2, rotation_step=0.3)),
     "sc_step_adaptation": (lambda: W.spherocylinders((6, 6, 6), 0.35, 2.0, 0.5, aspect=(1, 1, 3)), 200,
                            dict(translation_step=0.05, rotation_step=0.05, box_kind=1, box_step=0.05,
                                 pressure=1.5, adjust_steps=True)),

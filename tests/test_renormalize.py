@@ -20,7 +20,8 @@ def perturbed(cfg, noise, seed=3, factor=1.0):
 # engine takes rotations to within 1e-6); compressed systems hold overlaps, so some fixes
 # are rejected and the serial remainder of the pass runs
 CASES = [("sc_l2_dense", 1e-9, 1.0), ("sc_l2_dense", 1e-7, 0.99), ("sc_l5", 1e-7, 0.995), ("hs_dense", 1e-7, 0.98),
-         ("poly_dense", 1e-9, 1.0), ("poly_dense", 1e-7, 0.995), ("poly_banana", 1e-7, 0.99)]
+         ("poly_dense", 1e-9, 1.0), ("poly_dense", 1e-7, 0.995), ("poly_banana", 1e-7, 0.99),
+         ("psc_bent", 1e-7, 0.995), ("psc_bent", 1e-9, 1.0)]
 
 
 @pytest.mark.parametrize("name,noise,factor", CASES)

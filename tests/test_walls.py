@@ -11,7 +11,7 @@ import pyoracle as po
 import systems
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "walls.npz")
-WALLS = [("hs_small", 1), ("sc_l2", 5), ("poly_banana", 2), ("sc_l2_dense", 7)]
+WALLS = [("hs_small", 1), ("sc_l2", 5), ("poly_banana", 2), ("sc_l2_dense", 7), ("psc_bent", 3)]
 
 
 def digest(pos, rot):
