@@ -145,6 +145,17 @@ int rp_create(const rp_shape_desc *shape, int64_t n, int device, void **handle);
 int rp_create_polysphere(int32_t num_centres, const double *centres, const double *radii, int64_t n, int device,
                          void **handle);
 
+/* Creates an engine for n polyspherocylinders: rigid bodies of num_centres hard
+ * spherocylinders (1..RP_MAX_CENTRES) with body-frame centres, half axes (num_centres x 3
+ * each; the segment runs from centre - half axis to centre + half axis) and radii.
+ * Replaces: Packing::Packing(..., PolyspherocylinderTraits(spherocylinderData))
+ * (core/shapes/PolyspherocylinderTraits.h:26-60).  The handle behaves as a polysphere one
+ * (interaction centres rotated with the body) whose centre pairs are decided as
+ * PolyspherocylinderTraits::overlapBetween (PolyspherocylinderTraits.cpp:102-124): inspheres
+ * (r_a + r_b), circumspheres (c_a + c_b, c = r + |half axis|), then the segment distance. */
+int rp_create_polyspherocylinder(int32_t num_centres, const double *centres, const double *half_axes,
+                                 const double *radii, int64_t n, int device, void **handle);
+
 /* Releases the handle and all of its device memory. */
 int rp_destroy(void *handle);
 

@@ -20,6 +20,8 @@ ERRORS = {
     -5: "RP_ERR_UNSUPPORTED", -6: "RP_ERR_DEVICE", -7: "RP_ERR_CAPACITY", -8: "RP_ERR_FORMAT", -9: "RP_ERR_IO",
 }
 SHAPE_SPHERE, SHAPE_SPHEROCYLINDER, SHAPE_POLYSPHERE = 0, 1, 2
+# creation kind of polyspherocylinders (the handle then runs as a multi-centre body)
+SHAPE_POLYSPHEROCYLINDER = 3
 MAX_CENTRES = 8
 MOVE_TRANSLATION, MOVE_ROTATION, MOVE_ROTOTRANSLATION = 0, 1, 2
 CODE_ACCEPTED = 0x80
@@ -105,6 +107,7 @@ _F = C.POINTER(C.c_float)
 SIGNATURES = {
     "rp_create": (C.c_int, [C.POINTER(ShapeDesc), C.c_int64, C.c_int, C.POINTER(C.c_void_p)]),
     "rp_create_polysphere": (C.c_int, [C.c_int32, _D, _D, C.c_int64, C.c_int, C.POINTER(C.c_void_p)]),
+    "rp_create_polyspherocylinder": (C.c_int, [C.c_int32, _D, _D, _D, C.c_int64, C.c_int, C.POINTER(C.c_void_p)]),
     "rp_destroy": (C.c_int, [_P]),
     "rp_last_error": (C.c_char_p, [_P]),
     "rp_upload_state": (C.c_int, [_P, _D, _D, _D]),

@@ -56,6 +56,16 @@ def named_point(kind: int, params, name: str) -> tuple:
         i, k = int(name[1:]), int(params[0])
         if i < k:
             return tuple(float(x) for x in params[1 + 4 * i:4 + 4 * i])
+    if kind == _lib.SHAPE_POLYSPHEROCYLINDER and name[:1] in ("o", "b", "e") and name[1:].isdigit():
+        # "o<i>", "b<i>", "e<i>": centre, centre - half axis, centre + half axis of
+        # spherocylinder i (PolyspherocylinderTraits.cpp:42-47)
+        i, k = int(name[1:]), int(params[0])
+        if i < k:
+            d = [float(x) for x in params[1 + 7 * i:8 + 7 * i]]
+            c, h = d[:3], d[3:6]
+            if name[0] == "o":
+                return tuple(c)
+            return tuple(c[a] - h[a] for a in range(3)) if name[0] == "b" else tuple(c[a] + h[a] for a in range(3))
     raise EngineError(-1, f"ShapeGeometry::getNamedPoint : unknown point name '{name}'")
 
 

@@ -196,6 +196,11 @@ struct Handle {
     int walls = 0;            // Packing::toggleWalls mask (bit i: walls across box side i)
     double total_range = 0;   // Interaction::getTotalRangeRadius (core/Interaction.cpp:55-70)
     double cthr_host[MAX_CEN * MAX_CEN]{};
+    // polyspherocylinders: body-frame half axes and (c_a + c_b)^2 of the circumsphere radii
+    int segs = 0;
+    double chax[3 * MAX_CEN]{};
+    double circ_host[MAX_CEN * MAX_CEN]{};
+    double *circ64 = nullptr;
     double ref_range = 0;
     double *cen64 = nullptr;
     int stage_mode = 1;  // staging filter: 0 off, 1 where it pays (cells well above the range), 2 wherever valid
@@ -367,6 +372,10 @@ DevState dev_state(Handle *h) {
     s.cen64 = h->cen64;
     s.abs64 = h->abs64[h->pcur];
     s.cthr64 = h->cthr64;
+    s.segs = h->segs;
+    for (int k = 0; k < MAX_CEN; k++)
+        for (int d = 0; d < 3; d++) s.chax[k][d] = h->chax[3 * k + d];
+    s.circ64 = h->circ64;
     if (h->grid[h->gcur].no_ng) {
         const bool sheared = h->box[1] != 0 || h->box[2] != 0 || h->box[3] != 0 || h->box[5] != 0 || h->box[6] != 0 ||
                              h->box[7] != 0;
@@ -571,15 +580,17 @@ int setup_grid(Handle *h, GridHost &G, const double *box, const double *shift) {
         }
     }
     if (h->ncen > 0) {
-        // FP32 centre-pair thresholds of this grid: (r_a + r_b)^2 -/+ margin
+        // FP32 centre-pair thresholds of this grid: (r_a + r_b)^2 - margin (overlap below) and
+        // (r_a + r_b)^2 + margin (none above); for polyspherocylinders the upper one is the
+        // circumspheres' (c_a + c_b)^2 + margin, between the two the segments decide in FP64
         std::vector<float> &t = G.cthr;
         t.assign(2 * MAX_CEN * MAX_CEN, 0.0f);
         for (int a = 0; a < h->ncen; a++)
             for (int b = 0; b < h->ncen; b++) {
                 double thr = h->cthr_host[a * MAX_CEN + b];
-                double m = poly_margin(h, G, thr);
-                t[a * MAX_CEN + b] = static_cast<float>(thr - m);
-                t[MAX_CEN * MAX_CEN + a * MAX_CEN + b] = static_cast<float>(thr + m);
+                double hi = h->segs ? h->circ_host[a * MAX_CEN + b] : thr;
+                t[a * MAX_CEN + b] = static_cast<float>(thr - poly_margin(h, G, thr));
+                t[MAX_CEN * MAX_CEN + a * MAX_CEN + b] = static_cast<float>(hi + poly_margin(h, G, hi));
             }
         RP_CUDA(h, cudaMemcpyAsync(g.cthr, t.data(), sizeof(float) * t.size(), cudaMemcpyHostToDevice, h->stream));
     }
@@ -955,6 +966,9 @@ static int create_common(Handle *h, int64_t n, int device, void **handle) {
         if ((e = cudaMalloc(&h->cthr64, sizeof(double) * MAX_CEN * MAX_CEN)) != cudaSuccess) return bail(e);
         if ((e = cudaMemcpy(h->cthr64, h->cthr_host, sizeof(h->cthr_host), cudaMemcpyHostToDevice)) != cudaSuccess)
             return bail(e);
+        if ((e = cudaMalloc(&h->circ64, sizeof(double) * MAX_CEN * MAX_CEN)) != cudaSuccess) return bail(e);
+        if ((e = cudaMemcpy(h->circ64, h->circ_host, sizeof(h->circ_host), cudaMemcpyHostToDevice)) != cudaSuccess)
+            return bail(e);
         if ((e = cudaMalloc(&h->cbody_dev, sizeof(h->cbody))) != cudaSuccess) return bail(e);
         if ((e = cudaMemcpy(h->cbody_dev, h->cbody, sizeof(h->cbody), cudaMemcpyHostToDevice)) != cudaSuccess)
             return bail(e);
@@ -1009,35 +1023,57 @@ int rp_create(const rp_shape_desc *shape, int64_t n, int device, void **handle) 
     return create_common(h, n, device, handle);
 }
 
-int rp_create_polysphere(int32_t num_centres, const double *centres, const double *radii, int64_t n, int device,
-                         void **handle) {
+namespace {
+
+// Polyspheres (PolysphereTraits) and polyspherocylinders (PolyspherocylinderTraits, half
+// axes given): the multi-centre bodies of the engine.
+int create_multi_centre(int32_t num_centres, const double *centres, const double *half_axes, const double *radii,
+                        int64_t n, int device, void **handle) {
     if (!centres || !radii || !handle || n <= 0 || n > (1ll << 31) - 1) return RP_ERR_ARG;
     if (num_centres < 1 || num_centres > MAX_CEN) return RP_ERR_UNSUPPORTED;
     for (int b = 0; b < num_centres; b++) {
         if (!(radii[b] > 0)) return RP_ERR_ARG;
         for (int d = 0; d < 3; d++)
-            if (!std::isfinite(centres[3 * b + d])) return RP_ERR_ARG;
+            if (!std::isfinite(centres[3 * b + d]) || (half_axes && !std::isfinite(half_axes[3 * b + d])))
+                return RP_ERR_ARG;
     }
     Handle *h = new (std::nothrow) Handle();
     if (!h) return RP_ERR_ARG;
     h->shape.kind = RP_SHAPE_POLYSPHERE;
     h->ncen = num_centres;
-    double rmax = 0, reach = 0;
+    h->segs = half_axes ? 1 : 0;
+    // a centre's reach: its sphere radius, or the spherocylinder's circumsphere radius
+    // radius + |halfAxis| (PolyspherocylinderTraits.cpp:78-84)
+    double outer[MAX_CEN]{};
+    for (int b = 0; b < num_centres; b++) {
+        outer[b] = radii[b];
+        if (half_axes) {
+            for (int d = 0; d < 3; d++) h->chax[3 * b + d] = half_axes[3 * b + d];
+            const d3 ha{half_axes[3 * b], half_axes[3 * b + 1], half_axes[3 * b + 2]};
+            outer[b] = radii[b] + std::sqrt(norm2(ha));
+        }
+    }
+    double rmax = 0, omax = 0, reach = 0;
     for (int b = 0; b < num_centres; b++) {
         for (int d = 0; d < 3; d++) h->cbody[3 * b + d] = centres[3 * b + d];
         h->crad[b] = radii[b];
         rmax = std::max(rmax, radii[b]);
+        omax = std::max(omax, outer[b]);
         double c = std::sqrt(centres[3 * b] * centres[3 * b] + centres[3 * b + 1] * centres[3 * b + 1] +
                              centres[3 * b + 2] * centres[3 * b + 2]);
-        reach = std::max(reach, c + radii[b]);
+        reach = std::max(reach, c + outer[b]);
     }
     for (int a = 0; a < num_centres; a++)
         for (int b = 0; b < num_centres; b++) {
-            double r = radii[a] + radii[b];      // PolysphereTraits.cpp:104-105
+            double r = radii[a] + radii[b];      // PolysphereTraits.cpp:104-105, PolyspherocylinderTraits.cpp:111-112
             h->cthr_host[a * MAX_CEN + b] = r * r;
+            double c = outer[a] + outer[b];      // PolyspherocylinderTraits.cpp:115-116
+            h->circ_host[a * MAX_CEN + b] = c * c;
         }
     h->shape.radius = rmax;
-    h->ref_range = 2 * rmax;                   // PolysphereTraits.cpp:115-120 (the neighbour-grid cell)
+    // the reference's neighbour-grid cell: PolysphereTraits.cpp:115-120 (2 max r),
+    // PolyspherocylinderTraits.cpp:140-147 (2 max circumsphere radius)
+    h->ref_range = 2 * (half_axes ? omax : rmax);
     {
         // Interaction::getTotalRangeRadius: 2 sqrt(max |centre|^2) + range
         double m2 = 0;
@@ -1049,9 +1085,23 @@ int rp_create_polysphere(int32_t num_centres, const double *centres, const doubl
         h->total_range = 2 * std::sqrt(m2) + h->ref_range;
     }
     // cells of the checkerboard: two bodies farther apart than twice the largest reach
-    // |c| + r cannot touch (rotated centres keep |c| up to FP64 rounding)
+    // |c| + r (or |c| + circumsphere radius) cannot touch (rotated centres keep |c| up to
+    // FP64 rounding)
     h->range = 2 * reach * (1.0 + 1e-12);
     return create_common(h, n, device, handle);
+}
+
+}  // namespace
+
+int rp_create_polysphere(int32_t num_centres, const double *centres, const double *radii, int64_t n, int device,
+                         void **handle) {
+    return create_multi_centre(num_centres, centres, nullptr, radii, n, device, handle);
+}
+
+int rp_create_polyspherocylinder(int32_t num_centres, const double *centres, const double *half_axes,
+                                 const double *radii, int64_t n, int device, void **handle) {
+    if (!half_axes) return RP_ERR_ARG;
+    return create_multi_centre(num_centres, centres, half_axes, radii, n, device, handle);
 }
 
 int rp_destroy(void *handle) {
@@ -1087,6 +1137,7 @@ int rp_destroy(void *handle) {
     cudaFree(h->abs64[0]);
     cudaFree(h->abs64[1]);
     cudaFree(h->cthr64);
+    cudaFree(h->circ64);
     cudaFree(h->cbody_dev);
     if (!h->batch_member) {
         cudaFree(h->rtab64);

@@ -77,8 +77,21 @@ __device__ __forceinline__ bool overlaps_pair(const DevState &s, d3 pi, const do
     }
     for (int a = 0; a < s.ncen; a++) {
         d3 pa = ld3(ai + 3 * a);
+        d3 ha{0.0, 0.0, 0.0};
+        if (s.segs) ha = mv3(ri, d3{s.chax[a][0], s.chax[a][1], s.chax[a][2]});
         for (int b = 0; b < s.ncen; b++) {
             d3 pb = ld3(v.abs + 3 * ((size_t)j * s.ncen + b));
+            if (s.segs) {
+                // PolyspherocylinderTraits::overlapBetween (PolyspherocylinderTraits.cpp:102-124)
+                d3 q = add3(pb, pbc_translation(s.box, s.inv, pa, pb));
+                double d2 = norm2(sub3(q, pa));
+                const double in2 = s.cthr64[a * MAX_CEN + b];
+                if (d2 < in2) return true;
+                if (d2 >= s.circ64[a * MAX_CEN + b]) continue;
+                d3 hb = mv3(v.rot + 9 * j, d3{s.chax[b][0], s.chax[b][1], s.chax[b][2]});
+                if (segment_distance2(add3(pa, ha), sub3(pa, ha), add3(q, hb), sub3(q, hb)) < in2) return true;
+                continue;
+            }
             if (s.pbc_fold) {
                 if (pbc_distance2(s.box, s.inv, pa, pb) < s.cthr64[a * MAX_CEN + b]) return true;
                 continue;
@@ -94,8 +107,15 @@ __device__ __forceinline__ bool overlaps_pair(const DevState &s, d3 pi, const do
 // rotated centres fixed).
 __device__ __forceinline__ bool overlaps_walls(const DevState &s, d3 pi, const double *ri, const double *ci) {
     if (!s.walls) return false;
+    double hx[3 * MAX_CEN];
+    if (s.segs)
+        for (int a = 0; a < s.ncen; a++) {
+            d3 h = mv3(ri, d3{s.chax[a][0], s.chax[a][1], s.chax[a][2]});
+            hx[3 * a] = h.x, hx[3 * a + 1] = h.y, hx[3 * a + 2] = h.z;
+        }
     return wall_overlap_count(s.walls, s.wall_vec, s.wall_far, s.wall_half, s.ncen ? 2 : s.kind, s.wall_radius,
-                              s.wall_half_len, pi, d3{ri[2], ri[5], ri[8]}, ci, s.ncen, true) != 0;
+                              s.wall_half_len, pi, d3{ri[2], ri[5], ri[8]}, ci, s.ncen, true,
+                              s.segs ? hx : nullptr) != 0;
 }
 
 // The candidates of particle i: the particles of its cell and the 26 around it.

@@ -289,11 +289,12 @@ RP_HD u4 philox(u4 ctr, uint32_t k0, uint32_t k1) {
 // Wall overlaps of one body (Packing::countParticleWallOverlaps, core/Packing.cpp:1086-1139,
 // with SphereTraits.cpp:67-75, SpherocylinderTraits.cpp:56-73, PolysphereTraits.cpp:129-136):
 // per walled axis the nearer wall, if within `half` of the position; `axis` is the
-// spherocylinder axis, `cen` the polysphere's rotated centres (ncen of them).  Returns the
+// spherocylinder axis, `cen` the polysphere's rotated centres (ncen of them), `hax` the
+// polyspherocylinder's rotated half axes (orientation * body half axis).  Returns the
 // number of overlaps, or 1 at the first with early exit.
 RP_HD int wall_overlap_count(int walls, const double (*wall_vec)[3], const double *wall_far, double half, int kind,
                              const double *radius, double half_len, d3 pos, d3 axis, const double *cen, int ncen,
-                             bool early) {
+                             bool early, const double *hax = nullptr) {
     int cnt = 0;
     for (int i = 0; i < 3; i++) {
         if (!((walls >> i) & 1)) continue;
@@ -315,7 +316,14 @@ RP_HD int wall_overlap_count(int walls, const double (*wall_vec)[3], const doubl
         } else {
             for (int k = 0; k < ncen; k++) {
                 const d3 cp = add3(pos, d3{cen[3 * k], cen[3 * k + 1], cen[3 * k + 2]});
-                if (dot3(ww, sub3(cp, o)) < radius[k]) {
+                bool hit;
+                if (hax) {   // PolyspherocylinderTraits.cpp:149-166: either cap of the segment
+                    const d3 h{hax[3 * k], hax[3 * k + 1], hax[3 * k + 2]};
+                    hit = dot3(ww, sub3(sub3(cp, h), o)) < radius[k] || dot3(ww, sub3(add3(cp, h), o)) < radius[k];
+                } else {
+                    hit = dot3(ww, sub3(cp, o)) < radius[k];
+                }
+                if (hit) {
                     cnt++;
                     if (early) return 1;
                 }

@@ -90,6 +90,11 @@ struct DevState {
     double *cen64;                 // [n][ncen][3]
     double *abs64;                 // [n][ncen][3] (position + centre, wrapped into the box)
     const double *cthr64;          // [MAX_CEN^2] (r_a + r_b)^2, FP64 as the reference forms it
+    // polyspherocylinders (PolyspherocylinderTraits): each centre a spherocylinder with a
+    // body-frame half axis; circ64 [MAX_CEN^2] holds (c_a + c_b)^2 of the circumsphere radii
+    int segs;
+    double chax[RP_MAX_CENTRES][3];
+    const double *circ64;
     // nonzero when the reference keeps no neighbour grid for this box (core/Packing.cpp:862-881):
     // it then measures sphere and polysphere-centre distances with the periodic boundary
     // conditions' own formula (pbc_distance2: per-coordinate |relative separation| folded
@@ -154,7 +159,7 @@ RP_HD int cell_phase(const int *dims, int cell) {
 // per-warp polysphere scratch of the sweep (float4 units): the mover's FP32 centres
 // [MAX_CEN], the centre-pair thresholds [2 MAX_CEN^2 floats], the mover's exact centres
 // and absolute centres [2 x 3 MAX_CEN doubles]
-constexpr int SWEEP_POLY_SCRATCH = MAX_CEN + MAX_CEN * MAX_CEN / 2 + 3 * MAX_CEN;
+constexpr int SWEEP_POLY_SCRATCH = MAX_CEN + MAX_CEN * MAX_CEN / 2 + 3 * MAX_CEN + 3 * MAX_CEN / 2;
 
 constexpr int NUM_COUNTERS = 9;     // sweep statistics words per handle (rp_sweep_stats order)
 constexpr int SWEEP_WARPS = 4;       // warps per block of the sweep kernel

@@ -147,8 +147,24 @@ __device__ __forceinline__ bool exact_pair(const DevState &s, d3 pi, d3 ai, int 
 // body pid_j seen at FP32 separation dsep (candidate minus mover): the reference's
 // (pos2 + t - pos1).norm2() < (r_a + r_j)^2 (core/Packing.cpp:40-42,
 // core/shapes/PolysphereTraits.cpp:97-106) with t the box translation of that image.
-__device__ __forceinline__ bool exact_centre_pair(const DevState &s, d3 pa, int a, int pid_j, int j, float3 dsep) {
+// Polyspherocylinders (s.segs): PolyspherocylinderTraits::overlapBetween
+// (core/shapes/PolyspherocylinderTraits.cpp:102-124) with the image's translation (the
+// periodic boundary conditions' own when the reference keeps no grid): inspheres,
+// circumspheres, then the distance of the segments centre -+ orientation * half axis; `ha`
+// is the half axis of centre a of the first body (orientation already applied).
+__device__ __forceinline__ bool exact_centre_pair(const DevState &s, d3 pa, int a, int pid_j, int j, float3 dsep,
+                                                  d3 ha = d3{0.0, 0.0, 0.0}) {
     d3 pb = load_d3(s.abs64 + 3 * ((size_t)pid_j * s.ncen + j));
+    if (s.segs) {
+        d3 t = s.pbc_fold ? pbc_translation(s.box, s.inv, pa, pb) : load_d3(s.trans + 3 * image_index(s, dsep, pa, pb));
+        d3 q = add3(pb, t);
+        double d2 = norm2(sub3(q, pa));
+        const double in2 = s.cthr64[a * MAX_CEN + j];
+        if (d2 < in2) return true;
+        if (d2 >= s.circ64[a * MAX_CEN + j]) return false;
+        d3 hj = mv3(s.rot64 + 9 * (size_t)pid_j, d3{s.chax[j][0], s.chax[j][1], s.chax[j][2]});
+        return segment_distance2(add3(pa, ha), sub3(pa, ha), add3(q, hj), sub3(q, hj)) < in2;
+    }
     if (s.pbc_fold) return pbc_distance2(s.box, s.inv, pa, pb) < s.cthr64[a * MAX_CEN + j];
     int m = image_index(s, dsep, pa, pb);
     d3 t = load_d3(s.trans + 3 * m);
@@ -288,6 +304,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
     float *wthr = reinterpret_cast<float *>(wx + MAX_CEN);
     double *wabs = reinterpret_cast<double *>(wx + MAX_CEN + MAX_CEN * MAX_CEN / 2);
     double *wcen = wabs + 3 * MAX_CEN;
+    double *whax = wcen + 3 * MAX_CEN;   // polyspherocylinders: the mover's rotated half axes
     if (KIND == 2)
         for (int t = lane; t < 2 * MAX_CEN * MAX_CEN; t += 32) wthr[t] = G.cthr[t];
     const bool self_images = (G.dims[0] == 1) || (G.dims[1] == 1) || (G.dims[2] == 1);
@@ -727,6 +744,19 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                     wabs[3 * lane + 1] = a.y;
                     wabs[3 * lane + 2] = a.z;
                 }
+                if (S.segs) {
+                    // orientation * half axis with the mover's new orientation
+                    // (PolyspherocylinderTraits.cpp:118-119)
+                    const double oe = type != 0 ? onew_own : rot_own;
+                    double O[9];
+                    for (int e = 0; e < 9; e++) O[e] = __shfl_sync(FULL, oe, e);
+                    if (lane < S.ncen) {
+                        d3 h = mv3(O, d3{S.chax[lane][0], S.chax[lane][1], S.chax[lane][2]});
+                        whax[3 * lane] = h.x;
+                        whax[3 * lane + 1] = h.y;
+                        whax[3 * lane + 2] = h.z;
+                    }
+                }
                 __syncwarp();
             }
             // the guard band: queued pairs re-decided in FP64
@@ -748,7 +778,8 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                             const float4 c = cj[j];
                             const float3 d = make_float3((dq.x + c.x) - m.x, (dq.y + c.y) - m.y, (dq.z + c.z) - m.z);
                             hit = exact_centre_pair(S, d3{wabs[3 * a], wabs[3 * a + 1], wabs[3 * a + 2]}, a,
-                                                    __float_as_int(q.w), j, d);
+                                                    __float_as_int(q.w), j, d,
+                                                    d3{whax[3 * a], whax[3 * a + 1], whax[3 * a + 2]});
                         }
                         if (__ballot_sync(FULL, hit)) {
                             ov = true;
@@ -785,7 +816,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                 if (lane == 0)
                     wov = wall_overlap_count(S.walls, S.wall_vec, S.wall_far, S.wall_half, KIND, S.wall_radius,
                                              S.wall_half_len, pnew, anew, KIND == 2 ? wcen : nullptr,
-                                             KIND == 2 ? S.ncen : 0, true);
+                                             KIND == 2 ? S.ncen : 0, true, KIND == 2 && S.segs ? whax : nullptr);
                 if (__shfl_sync(FULL, wov, 0)) code = 1;
             }
         }
@@ -1089,6 +1120,12 @@ __device__ __forceinline__ void count_poly_one(const DevState &s, const GridDev 
     int cell = g.pid_cell[pid];
     int cx = cell % g.dims[0], cy = (cell / g.dims[0]) % g.dims[1], cz = cell / (g.dims[0] * g.dims[1]);
     unsigned long long cnt = 0;
+    double hx[3 * MAX_CEN];   // polyspherocylinders: orientation * half axis of each centre
+    if (s.segs)
+        for (int a = 0; a < K; a++) {
+            d3 h = mv3(s.rot64 + 9 * (size_t)pid, d3{s.chax[a][0], s.chax[a][1], s.chax[a][2]});
+            hx[3 * a] = h.x, hx[3 * a + 1] = h.y, hx[3 * a + 2] = h.z;
+        }
     for (int o = 0; o < 27; o++) {
         if (early && *(volatile int *)flag) break;
         int ox = o % 3 - 1, oy = (o / 3) % 3 - 1, oz = o / 9 - 1;
@@ -1113,7 +1150,8 @@ __device__ __forceinline__ void count_poly_one(const DevState &s, const GridDev 
                     bool ov = !exact && d2 < g.cthr[a * MAX_CEN + j];
                     if (!ov && (exact || d2 <= g.cthr[MAX_CEN * MAX_CEN + a * MAX_CEN + j])) {
                         atomicAdd(s.counters + 5, 1ull);
-                        ov = exact_centre_pair(s, load_d3(s.abs64 + 3 * ((size_t)pid * K + a)), a, pj, j, d);
+                        ov = exact_centre_pair(s, load_d3(s.abs64 + 3 * ((size_t)pid * K + a)), a, pj, j, d,
+                                               s.segs ? d3{hx[3 * a], hx[3 * a + 1], hx[3 * a + 2]} : d3{0, 0, 0});
                     }
                     if (ov) {
                         cnt++;
@@ -1130,7 +1168,7 @@ __device__ __forceinline__ void count_poly_one(const DevState &s, const GridDev 
     if (s.walls && !(early && *(volatile int *)flag)) {
         const int w = wall_overlap_count(s.walls, s.wall_vec, s.wall_far, s.wall_half, 2, s.wall_radius, 0.0,
                                          load_d3(s.pos64 + 3 * (size_t)pid), d3{0, 0, 0},
-                                         s.cen64 + 3 * (size_t)pid * K, K, early != 0);
+                                         s.cen64 + 3 * (size_t)pid * K, K, early != 0, s.segs ? hx : nullptr);
         if (w && early) atomicExch(flag, 1);
         cnt += (unsigned long long)w;
     }

@@ -64,6 +64,17 @@ class GpuPacking:
             rc = self.lib.rp_create_polysphere(k, dptr(centres), dptr(radii), self.n, device, C.byref(h))
             if rc != 0:
                 raise EngineError(rc, "rp_create_polysphere failed")
+        elif kind == _lib.SHAPE_POLYSPHEROCYLINDER:
+            # params as the oracle's: [k, (x, y, z, hx, hy, hz, r) per spherocylinder]
+            k = int(params[0])
+            data = params[1:1 + 7 * k].reshape(k, 7)
+            centres = np.ascontiguousarray(data[:, :3])
+            half_axes = np.ascontiguousarray(data[:, 3:6])
+            radii = np.ascontiguousarray(data[:, 6])
+            rc = self.lib.rp_create_polyspherocylinder(k, dptr(centres), dptr(half_axes), dptr(radii), self.n, device,
+                                                       C.byref(h))
+            if rc != 0:
+                raise EngineError(rc, "rp_create_polyspherocylinder failed")
         else:
             if kind == _lib.SHAPE_SPHERE:
                 desc.radius = float(params[0])

@@ -114,6 +114,17 @@ def shape_volume(kind: int, params) -> float:
     if kind == _lib.SHAPE_SPHEROCYLINDER:
         r, length = float(p[1]), float(p[0])
         return math.pi * r * r * length + 4. / 3 * math.pi * math.pow(r, 3)
+    if kind == _lib.SHAPE_POLYSPHEROCYLINDER:
+        # PolyspherocylinderGeometry::calculateVolume (PolyspherocylinderTraits.cpp:12-20) for
+        # non-overlapping spherocylinders: the sum of SpherocylinderData::getVolume (:86-91)
+        volume = 0.0
+        for i in range(int(p[0])):
+            d = p[1 + 7 * i:8 + 7 * i]
+            r = float(d[6])
+            half = math.sqrt(((0.0 + d[3] * d[3]) + d[4] * d[4]) + d[5] * d[5])
+            r2 = r * r
+            volume = volume + (4 * math.pi / 3 * (r2 * r) + math.pi * r2 * (2 * half))
+        return volume
     raise ValueError("the volume of this shape kind is not restated")
 
 

@@ -96,7 +96,7 @@ def psc_bent():
 @functools.lru_cache(maxsize=None)
 def psc_tiny():
     """Bent rods, N = 24 in a small box (no neighbour grid in the reference), 10 NVT cycles."""
-    return thermalise(W.bent_rods((2, 4, 3), spacing=(2.0, 0.9, 1.2)), 10, translation_step=0.2,
+    return thermalise(W.bent_rods((2, 4, 3), spacing=(2.0, 1.0, 1.3)), 10, translation_step=0.2,
                       rotation_step=0.2)
 
 

@@ -14,7 +14,8 @@ from rampack_gb300 import _lib
 
 pytestmark = pytest.mark.gpu
 
-CASES = ["hs_small", "hs_dense", "sc_l2", "sc_l2_dense", "sc_l5", "poly_banana", "poly_dense", "hs_tiny", "sc_tiny"]
+CASES = ["hs_small", "hs_dense", "sc_l2", "sc_l2_dense", "sc_l5", "poly_banana", "poly_dense", "hs_tiny", "sc_tiny",
+         "psc_bent", "psc_tiny"]
 
 
 def gpu_packing(cfg):
@@ -112,7 +113,7 @@ def test_sweep_log_replays_on_oracle(oracle, engine, name, fp64_only):
 
 
 @pytest.mark.parametrize("name", ["sc_l2", "sc_l2_dense", "sc_l5", "poly_banana", "poly_dense", "hs_dense",
-                                  "sc_tiny", "hs_tiny"])
+                                  "sc_tiny", "hs_tiny", "psc_bent"])
 def test_rototranslation_sweeps_replay_on_oracle(oracle, engine, name):
     # RototranslationSampler moves (translation and rotation in one move, ActiveDomain
     # checked): every logged move of type 2 replays on the oracle's tryMove

@@ -14,7 +14,9 @@ pytestmark = pytest.mark.gpu
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "walls.npz")
 CASES = [("hs_small", 1), ("sc_l2", 5), ("poly_banana", 2), ("sc_l2_dense", 7), ("hs_tiny", 3), ("sc_tiny", 6),
-         ("poly_dense", 4)]
+         ("poly_dense", 4), ("psc_bent", 3)]
+# (index in tests/golden/walls.npz, system, wall mask)
+GOLDEN = [(0, "hs_small", 1), (1, "sc_l2", 5), (2, "poly_banana", 2), (3, "sc_l2_dense", 7), (4, "psc_bent", 3)]
 
 
 def pair(name, mask, counting=False):
@@ -31,7 +33,7 @@ def pair(name, mask, counting=False):
 
 def test_wall_counts_match_the_reference(engine):
     z = np.load(GOLD)
-    for i, (name, mask) in enumerate(CASES[:4]):
+    for i, name, mask in GOLDEN:
         cfg = systems.ALL[name]()
         with gpu_packing(cfg) as g:
             g.set_walls(mask)
