@@ -77,6 +77,11 @@ def _banana_1e5(args):
     return W.config_banana_1e5()
 
 
+def _bent_rods_1e5(args):
+    from rampack_gb300 import workloads as W
+    return W.config_bent_rods_1e5()
+
+
 def _sc_64000(args):
     from rampack_gb300 import workloads as W
     return W.config_sc_64000()
@@ -94,6 +99,10 @@ WORKLOADS = {
                     "on [1, 20], lattice start at phi=0.30, triclinic boxes; per cycle one translation (0.2) per "
                     "sphere, a translation (0.2) and a rotation (0.2) per spherocylinder, one isotension box move "
                     "(delta 0.005, T=1) per replica", "moves/sec, 64 replicas"),
+    "bent-rods-1e5": (_bent_rods_1e5, "bent rods of two hard spherocylinders (r=0.25, half axes (0.3, 0, +-0.15) "
+                      "at x=-+0.35: a 60 degree kink), N={n:,} (25x40x100), aligned orthorhombic start at phi~0.33, "
+                      "triclinic box; per cycle 2N moves (translation 0.2, rotation 0.2) + 1 isotension box move "
+                      "(delta 0.005, p*=1.5, T=1)", "moves/sec, bent spherocylinder rods N=1e5"),
     "sc-64000": (_sc_64000, "hard spherocylinders l=5 r=0.5, N={n:,} (40^3), aligned orthorhombic start at "
                  "phi=0.35 (cell aspect 1:1:6), triclinic box; per cycle 2N moves (translation 0.2, rotation "
                  "0.2) + 1 isotension box move (delta 0.005, p*=1.5, T=1)", "moves/sec, spherocylinders N=64000"),

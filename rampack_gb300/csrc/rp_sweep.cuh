@@ -761,18 +761,23 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
             }
             // the guard band: queued pairs re-decided in FP64
             if (KIND == 2 && code == 0 && nun > 0) {
-                // every centre pair of each queued body, one pair per lane
+                // every centre pair of the queued bodies, one pair per lane: with K^2 <= 16,
+                // 32 / K^2 bodies per pass (the FP64 segment tests of polyspherocylinders
+                // keep the lanes busy), else one body per pass
                 const int K = S.ncen;
+                const int KK = K * K;
+                const int per = KK <= 16 ? 32 / KK : 1;
                 bool ov = false;
-                for (int qi = 0; qi < nun && !ov; qi++) {
-                    const int k = qun[qi];
+                for (int q0 = 0; q0 < nun && !ov; q0 += per) {
+                    const int qi = q0 + (per > 1 ? lane / KK : 0);
+                    const int k = qun[qi < nun ? qi : q0];
                     const float4 q = cpos[k];
                     const float3 dq = make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z);
                     const float4 *cj = G.mcen + (size_t)cslot[k] * K;
-                    for (int tb = 0; tb < K * K; tb += 32) {
-                        const int t = tb + lane;
+                    for (int tb = 0; tb < (per > 1 ? 1 : KK); tb += 32) {
+                        const int t = per > 1 ? lane % KK : tb + lane;
                         bool hit = false;
-                        if (t < K * K) {
+                        if (t < KK && qi < nun && (per == 1 || lane < per * KK)) {
                             const int a = t / K, j = t % K;
                             const float4 m = wx[a];
                             const float4 c = cj[j];

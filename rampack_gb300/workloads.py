@@ -160,6 +160,13 @@ def config_banana_1e5():
     return bananas((50, 80, 25), 0.45, 0.6 / (2 * math.sin(math.radians(15))), math.radians(120), 5)
 
 
+def config_bent_rods_1e5():
+    """Bent rods of two spherocylinders (radius 0.25, half axes (0.3, 0, +-0.15) at x = -+0.35:
+    a 60 degree kink), N = 100,000 (25 x 40 x 100), aligned on a lattice of cells
+    2.0 x 0.62 x 0.95 (packing fraction about 0.33)."""
+    return bent_rods((25, 40, 100))
+
+
 def replica_lattice(kind: int, n: int, phi: float, length: float = 3.0, radius: float = 0.5):
     """N particles (spheres, or spherocylinders aligned along z) on the first N sites of an
     orthorhombic lattice whose cell aspect follows the particle's extents, in a box of

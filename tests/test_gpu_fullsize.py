@@ -10,12 +10,13 @@ import pyoracle as po
 
 pytestmark = pytest.mark.gpu
 
-WORKLOADS = ["sc_1e6", "banana_1e5", "sc_64000"]
+WORKLOADS = ["sc_1e6", "banana_1e5", "sc_64000", "bent_rods_1e5"]
 
 
 def config(name):
     from rampack_gb300 import workloads as W
-    return {"sc_1e6": W.config_sc_1e6, "banana_1e5": W.config_banana_1e5, "sc_64000": W.config_sc_64000}[name]()
+    return {"sc_1e6": W.config_sc_1e6, "banana_1e5": W.config_banana_1e5, "sc_64000": W.config_sc_64000,
+            "bent_rods_1e5": W.config_bent_rods_1e5}[name]()
 
 
 @pytest.mark.parametrize("name", WORKLOADS)
