@@ -273,6 +273,7 @@ def cycle(g, k, seed, rng, stats=False):
 
 
 PROFILES = {"sc-1e6": "k_sweep_sc_n1e6.md", "banana-1e5": "k_sweep_banana_n1e5.md",
+            "bent-rods-1e5": "k_sweep_bent_rods_n1e5.md",
             "replicas-64": "k_b_sweep_replicas_64.md"}
 
 
