@@ -1794,8 +1794,6 @@ int rp_set_counting(void *handle, int on) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h) return RP_ERR_ARG;
     if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
-    if (on && h->shape.kind == RP_SHAPE_POLYSPHERE)
-        return fail(h, RP_ERR_UNSUPPORTED, "overlap counting is built for spheres and spherocylinders");
     RP_CUDA(h, cudaSetDevice(h->device));
     {
         int rg = ensure_grid(h);  // an upload defers the grid

@@ -328,7 +328,7 @@ static cudaError_t launch_sweep_t(const SweepArgs &a, unsigned blocks, int threa
 cudaError_t launch_sweep(const SweepArgs &a, bool list, int nwarps, cudaStream_t st) {
     if (nwarps <= 0) return cudaSuccess;
     const int wpb = a.work ? 1 : SWEEP_WARPS;
-    const bool count = a.s.counting != 0 && a.s.kind != 2;
+    const bool count = a.s.counting != 0;
     // rototranslation sweeps have their own plain scan (no learned pre-test, no pair log)
     const bool rt = !list && !count && a.types == SWEEP_ROTOTRANSLATION;
     const bool learn = !list && !count && !rt && a.s.kind != 2 && (a.partners != nullptr || a.pair_every > 0);
@@ -336,6 +336,8 @@ cudaError_t launch_sweep(const SweepArgs &a, bool list, int nwarps, cudaStream_t
     unsigned blocks = (unsigned)((nwarps + wpb - 1) / wpb);
     const int th = wpb * 32;
     if (a.s.kind == 2) {
+        if (count) return list ? launch_sweep_t<2, true, 2>(a, blocks, th, smem, st)
+                               : launch_sweep_t<2, false, 2>(a, blocks, th, smem, st);
         if (list) return launch_sweep_t<2, true, 0>(a, blocks, th, smem, st);
         return rt ? launch_sweep_t<2, false, 3>(a, blocks, th, smem, st)
                   : launch_sweep_t<2, false, 0>(a, blocks, th, smem, st);

@@ -132,11 +132,22 @@ __device__ __forceinline__ int image_index(const DevState &s, float3 dsep, d3 pi
 __device__ __forceinline__ d3 load_d3(const double *p) { return d3{p[0], p[1], p[2]}; }
 
 // Exact FP64 test of mover (pi, ai) against particle pid_j seen at FP32 separation dsep.
+// With no neighbour grid (s.pbc_fold) the reference tests each pair once, at its nearest
+// image; a box of two cells across stages a candidate once per image, so only the staged
+// copy that is the nearest image (relative separation within 1/2 in every dimension) is
+// tested.  The other copy lies at least half a box height away, beyond the interaction
+// range of the boxes this engine accepts.
+__device__ __forceinline__ bool nearest_copy(const DevState &s, float3 dsep) {
+    const float3 r = mat32(s.inv32, dsep.x, dsep.y, dsep.z);
+    const float h = 0.5f + 1e-5f;
+    return fabsf(r.x) <= h && fabsf(r.y) <= h && fabsf(r.z) <= h;
+}
+
 __device__ __forceinline__ bool exact_pair(const DevState &s, d3 pi, d3 ai, int pid_j, float3 dsep) {
     d3 pj = load_d3(s.pos64 + 3 * (size_t)pid_j);
     const double *rj = s.rot64 + 9 * (size_t)pid_j;
     d3 aj = d3{rj[2], rj[5], rj[8]};
-    if (s.kind == 0 && s.pbc_fold) return pbc_distance2(s.box, s.inv, pi, pj) < s.ex.sphere_thr;
+    if (s.kind == 0 && s.pbc_fold) return nearest_copy(s, dsep) && pbc_distance2(s.box, s.inv, pi, pj) < s.ex.sphere_thr;
     int m = image_index(s, dsep, pi, pj);
     d3 t = load_d3(s.trans + 3 * m);
     return exact_overlap(s.ex, pi, ai, pj, aj, t);
@@ -155,6 +166,7 @@ __device__ __forceinline__ bool exact_pair(const DevState &s, d3 pi, d3 ai, int 
 __device__ __forceinline__ bool exact_centre_pair(const DevState &s, d3 pa, int a, int pid_j, int j, float3 dsep,
                                                   d3 ha = d3{0.0, 0.0, 0.0}) {
     d3 pb = load_d3(s.abs64 + 3 * ((size_t)pid_j * s.ncen + j));
+    if (s.pbc_fold && !nearest_copy(s, dsep)) return false;
     if (s.segs) {
         d3 t = s.pbc_fold ? pbc_translation(s.box, s.inv, pa, pb) : load_d3(s.trans + 3 * image_index(s, dsep, pa, pb));
         d3 q = add3(pb, t);
@@ -833,7 +845,61 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
             const d3 pc64{__shfl_sync(FULL, pos_own, 0), __shfl_sync(FULL, pos_own, 1), __shfl_sync(FULL, pos_own, 2)};
             const d3 ac64{__shfl_sync(FULL, rot_own, 2), __shfl_sync(FULL, rot_own, 5), __shfl_sync(FULL, rot_own, 8)};
             int before = 0, after = 0;
-            for (int k = lane; k < total; k += 32) {
+            if (KIND == 2) {
+                // multi-centre bodies: every centre pair of every candidate body, the mover's
+                // current centres (FP32 mirror, FP64 absolute centres) and its new ones
+                const int K = S.ncen;
+                const float4 *mcur = G.mcen + ((size_t)gbase + slot) * K;
+                const bool exact = A.fp64_only || S.pbc_fold == 2;
+                for (int k = lane; k < total; k += 32) {
+                    const float4 q = cpos[k];
+                    const int pj = __float_as_int(q.w);
+                    if (pj == pid) continue;
+                    const float3 db = make_float3(q.x - pcur.x, q.y - pcur.y, q.z - pcur.z);
+                    const float3 da = make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z);
+                    const float4 *cj = G.mcen + (size_t)cslot[k] * K;
+                    for (int j = 0; j < K; j++) {
+                        const float4 c = cj[j];
+                        for (int a = 0; a < K; a++) {
+                            const float lo = wthr[a * MAX_CEN + j], hi = wthr[MAX_CEN * MAX_CEN + a * MAX_CEN + j];
+                            const float4 m0 = mcur[a];
+                            const float3 d0 = make_float3((db.x + c.x) - m0.x, (db.y + c.y) - m0.y, (db.z + c.z) - m0.z);
+                            const float q0 = dot3f(d0, d0);
+                            int cb = exact ? 2 : (q0 < lo ? 1 : (q0 <= hi ? 2 : 0));
+                            if (cb == 2) {
+                                d3 h0{0.0, 0.0, 0.0};
+                                if (S.segs)
+                                    h0 = mv3(S.rot64 + 9 * (size_t)pid, d3{S.chax[a][0], S.chax[a][1], S.chax[a][2]});
+                                cb = exact_centre_pair(S, load_d3(S.abs64 + 3 * ((size_t)pid * K + a)), a, pj, j, d0,
+                                                       h0) ? 1 : 0;
+                            }
+                            const float4 m1 = wx[a];
+                            const float3 d1 = make_float3((da.x + c.x) - m1.x, (da.y + c.y) - m1.y, (da.z + c.z) - m1.z);
+                            const float q1 = dot3f(d1, d1);
+                            int ca = exact ? 2 : (q1 < lo ? 1 : (q1 <= hi ? 2 : 0));
+                            if (ca == 2)
+                                ca = exact_centre_pair(S, d3{wabs[3 * a], wabs[3 * a + 1], wabs[3 * a + 2]}, a, pj, j, d1,
+                                                       d3{whax[3 * a], whax[3 * a + 1], whax[3 * a + 2]}) ? 1 : 0;
+                            before += cb;
+                            after += ca;
+                        }
+                    }
+                }
+                if (S.walls && lane == 0) {
+                    double hcur[3 * MAX_CEN];
+                    if (S.segs)
+                        for (int a = 0; a < K; a++) {
+                            d3 h = mv3(S.rot64 + 9 * (size_t)pid, d3{S.chax[a][0], S.chax[a][1], S.chax[a][2]});
+                            hcur[3 * a] = h.x, hcur[3 * a + 1] = h.y, hcur[3 * a + 2] = h.z;
+                        }
+                    before += wall_overlap_count(S.walls, S.wall_vec, S.wall_far, S.wall_half, 2, S.wall_radius, 0.0,
+                                                 pc64, ac64, S.cen64 + 3 * (size_t)pid * K, K, false,
+                                                 S.segs ? hcur : nullptr);
+                    after += wall_overlap_count(S.walls, S.wall_vec, S.wall_far, S.wall_half, 2, S.wall_radius, 0.0,
+                                                pnew, anew, wcen, K, false, S.segs ? whax : nullptr);
+                }
+            }
+            for (int k = lane; k < (KIND == 2 ? 0 : total); k += 32) {
                 const float4 q = cpos[k];
                 const int pj = __float_as_int(q.w);
                 if (pj == pid) continue;
@@ -851,7 +917,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                 before += cb == 1 ? 1 : 0;
                 after += ca == 1 ? 1 : 0;
             }
-            if (S.walls && lane == 0) {
+            if (KIND != 2 && S.walls && lane == 0) {
                 before += wall_overlap_count(S.walls, S.wall_vec, S.wall_far, S.wall_half, KIND, S.wall_radius,
                                              S.wall_half_len, pc64, ac64, nullptr, 0, false);
                 after += wall_overlap_count(S.walls, S.wall_vec, S.wall_far, S.wall_half, KIND, S.wall_radius,

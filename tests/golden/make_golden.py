@@ -372,13 +372,12 @@ def gen_walls():
         out[f"w{i}_state"] = state_digest(p1, r1)
         out[f"w{i}_box_dE"] = np.array(ref.try_scaling(nb))
         out[f"w{i}_box_state"] = state_digest(*ref.state()[:2])
-        if kind != po.POLYSPHERE:
-            cnt = po.CpuPacking("reference", *cfg)
-            cnt.set_walls(mask)
-            cnt.set_counting(True)
-            c2, d2 = cnt.replay(mv)
-            out[f"w{i}_count_codes"], out[f"w{i}_count_deltas"] = c2, d2
-            out[f"w{i}_count_final"] = np.array(cnt.cached_overlaps())
+        cnt = po.CpuPacking("reference", *cfg)
+        cnt.set_walls(mask)
+        cnt.set_counting(True)
+        c2, d2 = cnt.replay(mv)
+        out[f"w{i}_count_codes"], out[f"w{i}_count_deltas"] = c2, d2
+        out[f"w{i}_count_final"] = np.array(cnt.cached_overlaps())
     np.savez_compressed(os.path.join(HERE, "walls.npz"), **out)
     print("walls:", len(WALLS), "systems")
 

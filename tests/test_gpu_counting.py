@@ -11,7 +11,8 @@ from test_gpu_parity import draw_cell_moves, gpu_packing, steps
 
 pytestmark = pytest.mark.gpu
 
-CASES = [("hs_dense", 0.97), ("sc_l2_dense", 0.97), ("sc_l2", 0.94), ("hs_tiny", 0.95)]
+CASES = [("hs_dense", 0.97), ("sc_l2_dense", 0.97), ("sc_l2", 0.94), ("hs_tiny", 0.95), ("poly_banana", 0.97),
+         ("poly_dense", 0.98), ("psc_bent", 0.95), ("psc_tiny", 0.95)]
 
 
 def setup(name, factor):
@@ -61,7 +62,7 @@ def test_counting_sweeps_replay(oracle, engine, name, factor, fp64_only):
         assert np.array_equal(gp, cp) and np.array_equal(gr, cr)
 
 
-@pytest.mark.parametrize("name,factor", CASES[:3])
+@pytest.mark.parametrize("name,factor", CASES[:3] + [("poly_banana", 0.97), ("psc_bent", 0.95)])
 def test_counting_box_moves(oracle, engine, name, factor):
     cfg, cpu, g = setup(name, factor)
     rng = np.random.default_rng(3)

@@ -68,7 +68,8 @@ def test_wall_move_lists_and_sweeps(oracle, engine, name, mask):
         assert np.array_equal(gp, cp) and np.array_equal(gb, cb)
 
 
-@pytest.mark.parametrize("name,mask", [("hs_small", 1), ("sc_l2", 5), ("sc_l2_dense", 7)])
+@pytest.mark.parametrize("name,mask", [("hs_small", 1), ("sc_l2", 5), ("sc_l2_dense", 7), ("poly_banana", 2),
+                                       ("psc_bent", 3)])
 def test_wall_overlap_counting(oracle, engine, name, mask):
     cfg, cpu, g = pair(name, mask, counting=True)
     t, r = steps(cfg)
