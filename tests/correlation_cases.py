@@ -20,8 +20,10 @@ CORRELATIONS = [
     ("poly_banana", 0, 0, (0, 0, 1), 1, 2, "o", 5.0, 25),
     ("poly_banana", 2, 0, (1, 0, 0), 2, 1, "s2", 4.0, 20),
     ("poly_dense", 1, 0, (0, 0, 1), 4, 0, "s4", 3.0, 30),
+    ("psc_bent", 0, 0, (0, 0, 1), 0, 0, "e1", 4.0, 40),
+    ("psc_bent", 2, 0, (0, 1, 0), 0, 0, "o0", 3.0, 30),
 ]
 POLY_AXES = ((0.0, 0.3, 1.0), (1.0, 0.0, 0.2))
 NAMED_POINTS = [("sc_l2", "o"), ("sc_l2", "cm"), ("sc_l2", "beg"), ("sc_l2", "end"), ("sc_l5", "beg"),
                 ("hs_small", "o"), ("hs_small", "cm"), ("poly_banana", "o"), ("poly_banana", "s0"),
-                ("poly_banana", "s4")]
+                ("poly_banana", "s4"), ("psc_bent", "o1"), ("psc_bent", "b0"), ("psc_bent", "e1")]
