@@ -50,6 +50,35 @@ public:
         n_ = shapes.size();
         reset(shapes, box);
     }
+    // One sphere or spherocylinder of a multi-centre body: PolysphereTraits::SphereData
+    // (position, radius) or PolyspherocylinderTraits::SpherocylinderData (position, half axis,
+    // radius), in the body frame.
+    struct Centre {
+        Vec3 position{};
+        double radius = 0;
+        Vec3 half_axis{};
+    };
+
+    // Packing(box, shapes, bc, interaction, ...) for polyspheres (PolysphereTraits) or, with
+    // `spherocylinders`, polyspherocylinders (PolyspherocylinderTraits).
+    GpuPacking(const Mat3 &box, const std::vector<Shape> &shapes, const std::vector<Centre> &centres,
+               bool spherocylinders, int device = 0) {
+        std::vector<double> pos, half, radii;
+        for (const auto &c : centres) {
+            pos.insert(pos.end(), c.position.begin(), c.position.end());
+            half.insert(half.end(), c.half_axis.begin(), c.half_axis.end());
+            radii.push_back(c.radius);
+        }
+        const auto k = static_cast<int32_t>(centres.size());
+        const auto n = static_cast<int64_t>(shapes.size());
+        if (spherocylinders)
+            check(rp_create_polyspherocylinder(k, pos.data(), half.data(), radii.data(), n, device, &h_),
+                  "rp_create_polyspherocylinder");
+        else
+            check(rp_create_polysphere(k, pos.data(), radii.data(), n, device, &h_), "rp_create_polysphere");
+        n_ = shapes.size();
+        reset(shapes, box);
+    }
     GpuPacking(const GpuPacking &) = delete;
     GpuPacking &operator=(const GpuPacking &) = delete;
     ~GpuPacking() {

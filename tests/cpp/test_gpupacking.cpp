@@ -101,6 +101,22 @@ int main(int argc, char **argv) {
         CHECK(rp_ramtrj_info((dir + "/sc.ramtrj").c_str(), &np, &snaps, &step, &ver) == RP_OK);
         CHECK(np == static_cast<int64_t>(sc.size()) && snaps == 2 && step == 1 && ver == 0x101);
     }
+    {
+        // two bent rods (PolyspherocylinderTraits, two spherocylinders each): an overlap that
+        // only the segments find (centres 0.695 apart, inspheres 0.5), and none where only the
+        // circumspheres meet (parallel segments 0.56 apart)
+        const std::vector<GpuPacking::Centre> rod{{{-0.35, 0, 0}, 0.25, {0.3, 0, 0.15}},
+                                                  {{0.35, 0, 0}, 0.25, {0.3, 0, -0.15}}};
+        const GpuPacking::Mat3 big{10, 0, 0, 0, 10, 0, 0, 0, 10};
+        std::vector<GpuPacking::Shape> a(2), b(2);
+        a[0].position = {5, 5, 5};
+        a[1].position = {6.3, 5, 5.35};
+        b[0].position = {5, 5, 5};
+        b[1].position = {5, 5.56, 5};
+        GpuPacking pa(big, a, rod, true), pb(big, b, rod, true);
+        CHECK(pa.countTotalOverlaps() == 1);
+        CHECK(pb.countTotalOverlaps() == 0);
+    }
     if (failures) return 1;
     std::printf("ok\n");
     return 0;
