@@ -65,6 +65,10 @@ struct CorrGeom {
     // t -+ (bin_abs + bin_rel * t); in range for sure below in_lo, out of range above in_hi;
     // the bin is floor(t) when the interval stays inside it
     float inv_step32, bin_abs, bin_rel, in_lo, in_hi;
+    // layerwise: Miller indices, tau / 2 pi and k / |k| in FP32; the layer value of a point
+    // is r . h - tau / 2 pi in relative coordinates (p . k = 2 pi r . h), and bin_abs_lw the
+    // absolute bin margin of the in-layer distance (its error grows with the full separation)
+    float hm32[3], tau32, kn32[3], bin_abs_lw;
     float edge32;    // no FP32 rejection when a folded relative separation is this near 1/2
     int fp64_only;   // RP_CORR_FP64_ONLY: no FP32 pre-filter
 };
@@ -243,13 +247,32 @@ __device__ __forceinline__ bool examine_pair(const CorrGeom &G, const SortedPoin
             d32 = d2 > 0.f ? d2 * rsqrtf(d2) : 0.f;   // within 2^-21 relative: inside the margin
         }
     }
+    // layerwise: both layer values away from a rounding edge give the reference's layers
+    // (different layers: dropped), then the in-layer FP32 distance is binned as below
+    float babs = G.bin_abs;
+    if (E == RP_PAIRS_LAYERWISE && fast && F != RP_CORR_S221) {
+        const float va = ra.x * G.hm32[0] + ra.y * G.hm32[1] + ra.z * G.hm32[2] - G.tau32;
+        const float vb = va + (f[0] * G.hm32[0] + f[1] * G.hm32[1] + f[2] * G.hm32[2]);
+        const float la = rintf(va), lb = rintf(vb);
+        if (fabsf(va - la) > 0.499f || fabsf(vb - lb) > 0.499f) return true;   // near a layer edge: FP64
+        if (la != lb) return false;
+        float s[3];
+        for (int i = 0; i < 3; i++) s[i] = G.box32[3 * i] * f[0] + G.box32[3 * i + 1] * f[1] + G.box32[3 * i + 2] * f[2];
+        const float dn = s[0] * G.kn32[0] + s[1] * G.kn32[1] + s[2] * G.kn32[2];
+        float d2 = 0.f;
+        for (int i = 0; i < 3; i++) {
+            const float v = s[i] - dn * G.kn32[i];
+            d2 += v * v;
+        }
+        d32 = d2 > 0.f ? d2 * rsqrtf(d2) : 0.f;
+        babs = G.bin_abs_lw;
+    }
     // FP32 binning: when the FP64 distance's whole error interval lies in one bin below max_r
     // (or beyond max_r), that bin is the reference's; pairs near a bin edge or max_r are
-    // decided in FP64.  The layerwise enumerator and S221 (which reads the separation)
-    // always take FP64.
-    if (E != RP_PAIRS_LAYERWISE && F != RP_CORR_S221 && fast) {
+    // decided in FP64.  S221 (which reads the separation) always takes FP64.
+    if (F != RP_CORR_S221 && fast) {
         const float t = d32 * G.inv_step32;
-        const float m = G.bin_abs + G.bin_rel * t;
+        const float m = babs + G.bin_rel * t;
         if (t - m > G.in_hi) return false;
         const float k = floorf(t), frac = t - k;   // exact
         if (t + m < G.in_lo && frac >= m && frac + m < 1.f) {
@@ -635,6 +658,13 @@ int add_snapshot(Corr *c, void *handle) {
     G.bin_rel = static_cast<float>(m_rel + 2.5e-6);   // also the rsqrt-based FP32 square root
     G.in_lo = static_cast<float>(d.num_bins * (1 - 1e-6));
     G.in_hi = static_cast<float>(d.num_bins * (1 + 1e-6));
+    // layerwise: the in-layer distance is the separation minus its normal part, whose FP32
+    // error adds a few 2^-24 of the whole separation (at most the reach): 2e-6 reach, with room
+    G.bin_abs_lw = static_cast<float>((m_abs + 2e-6 * reach) / G.step * (1 + 1e-6) + 2.5e-7);
+    for (int i = 0; i < 3; i++) {
+        G.hm32[i] = static_cast<float>(d.miller[i]);
+        G.kn32[i] = static_cast<float>(G.kn[i]);
+    }
     const double thr = reach * (1 + m_rel) + m_abs;
     G.thr2_32 = static_cast<float>(thr * thr);
     G.lin_thr32 = static_cast<float>(thr / h[std::min(std::max(d.linear_axis, 0), 2)]);
@@ -718,6 +748,7 @@ int add_snapshot(Corr *c, void *handle) {
         const std::complex<double> im{0, 1};
         for (int64_t i = 0; i < v.n; i++) tau = tau + std::exp(im * dot3(k, d3{f[3 * i], f[3 * i + 1], f[3 * i + 2]}));
         G.tau = std::arg(tau);
+        G.tau32 = static_cast<float>(G.tau / (2 * PI));
     }
     CORR_CUDA(c, launch_cell_scan(c->count, c->start, c->block_sums, G.ncell, c->max_occ, st));
     if (v.n > 0) {

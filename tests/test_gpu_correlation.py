@@ -132,8 +132,8 @@ def test_full_size_counts_match_the_oracle(oracle, engine, workload, max_r, nb):
     assert np.array_equal(counts, want)
 
 
-@pytest.mark.parametrize("focal,fn", [("o", 0), ("beg", 1)])
-def test_full_size_grid_and_binning_equal_exhaustive(engine, focal, fn):
+@pytest.mark.parametrize("focal,fn,en", [("o", 0, 0), ("beg", 1, 0), ("o", 0, 2), ("end", 2, 2)])
+def test_full_size_grid_and_binning_equal_exhaustive(engine, focal, fn, en):
     # 10^6 spherocylinders after a few sweeps: the cell grid finds every pair within reach
     # exactly once (the all-pairs enumeration examines 5 x 10^11 pairs on the GPU), and the
     # FP32 binning with its FP64 guard band bins every pair as FP64 alone; g(r) tends to 1
@@ -141,7 +141,7 @@ def test_full_size_grid_and_binning_equal_exhaustive(engine, focal, fn):
     from rampack_gb300 import workloads as W
     from rampack_gb300.packing import GpuPacking
     cfg = W.config_sc_1e6()
-    case = ("sc_l2", 0, 0, (0, 0, 1), fn, 0, focal, 8.0, 200)
+    case = ("sc_l2", en, 0, (0, 0, 10), fn, 0, focal, 8.0, 200)
     with GpuPacking(*cfg) as g:
         for c in range(3):
             g.sweep(0.2, 0.2, seed=11, counter=c, stats=False)
@@ -159,5 +159,5 @@ def test_full_size_grid_and_binning_equal_exhaustive(engine, focal, fn):
         else:
             assert np.allclose(res[0][1], r[1], rtol=AVG_RTOL, atol=1e-12, equal_nan=True)
     assert res[0][2].sum() > 0 and fp64 < res[0][2].sum() / 10
-    if fn == 0:
+    if fn == 0 and en == 0:
         assert abs(res[0][1][-20:].mean() - 1.0) < 0.1
