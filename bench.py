@@ -60,6 +60,8 @@ def parse():
                     help="time the pair density correlation g(r) of the workload's packing")
     ap.add_argument("--corr-max-r", type=float, default=8.0)
     ap.add_argument("--corr-bins", type=int, default=200)
+    ap.add_argument("--corr-enumerator", default="radial", choices=["radial", "linear-z", "layerwise-z10"],
+                    help="RadialEnumerator, LinearEnumerator(z) or LayerwiseRadialEnumerator((0, 0, 10))")
     ap.add_argument("--io", action="store_true",
                     help="snapshot files of the workload: RAMSNAP store / restore time and the cost of recording "
                          "a RAMTRJ snapshot every cycle while sweeping")
@@ -818,7 +820,9 @@ def main_correlation(args):
     g = GpuPacking(kind, prm, pos, rot, box)
     for c in range(3):   # a disordered state (the lattice's distances sit far from the bin edges)
         g.sweep(0.2, 0.2, seed=args.seed, counter=c, stats=False)
-    obs = K.PairDensityCorrelation(K.RadialEnumerator(), max_r, bins)
+    enum = {"radial": K.RadialEnumerator(), "linear-z": K.LinearEnumerator("z"),
+            "layerwise-z10": K.LayerwiseRadialEnumerator((0, 0, 10))}[args.corr_enumerator]
+    obs = K.PairDensityCorrelation(enum, max_r, bins)
     for _ in range(max(3, args.warmup)):
         obs.add_snapshot(g)
     torch.cuda.synchronize()
@@ -833,11 +837,12 @@ def main_correlation(args):
     obs.close()
     g.close()
     line = {
-        "metric": f"g(r) snapshots/s ({args.workload}, r <= {max_r}, {bins} bins)", "value": 1.0 / dt,
+        "metric": f"pair density correlation snapshots/s ({args.workload}, {args.corr_enumerator}, r <= {max_r}, "
+                  f"{bins} bins)", "value": 1.0 / dt,
         "unit": "snapshots/s", "n_gpus": 1, "steps": steps, "warmup": max(3, args.warmup), "ms_per_step": dt * 1e3,
         "higher_is_better": True, "dtype": "f32 binning, f64 guard band", "data": "synthetic",
         "config": {"workload": args.workload, "particles": n, "max_r": max_r, "bins": bins,
-                   "observable": "PairDensityCorrelation(RadialEnumerator)"},
+                   "observable": f"PairDensityCorrelation({type(enum).__name__})"},
         "pairs_in_range": int(counts.sum()), "pairs_decided_fp64": tested,
         "pairs_in_range_per_s": float(counts.sum()) / dt,
         "timing": "host wall clock per addSnapshot (device work synchronous inside)",
@@ -847,7 +852,8 @@ def main_correlation(args):
         import pyoracle as po
         po.build()
         ns = min(n, 20000)
-        d = po.pair_desc(enumerator=0, function=0, num_bins=bins, max_r=max_r)
+        d = po.pair_desc(enumerator={"radial": 0, "linear-z": 1, "layerwise-z10": 2}[args.corr_enumerator],
+                         linear_axis=2, miller=(0, 0, 10), function=0, num_bins=bins, max_r=max_r)
         c = po.OracleCorrelation(d)
         t0 = time.perf_counter()
         c.add_snapshot(pos[:ns], rot[:ns], box)
