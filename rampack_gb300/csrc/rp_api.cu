@@ -164,6 +164,9 @@ struct Handle {
     int num_sms = 0;
     unsigned long long *count_out = nullptr;
     int *flag = nullptr;
+    DeferredPair *cq_buf = nullptr;   // multi-centre recounts: deferred FP64 centre pairs
+    int *cq_count = nullptr;
+    static constexpr int CQ_CAP = 1 << 20;
     int32_t *overflow = nullptr;
     int32_t *overflow_count = nullptr;
     int64_t overflow_alloc = 0;
@@ -1150,6 +1153,8 @@ int rp_destroy(void *handle) {
         cudaFree(h->counters);
     }
     cudaFree(h->count_out);
+    cudaFree(h->cq_buf);
+    cudaFree(h->cq_count);
     cudaFree(h->flag);
     cudaFree(h->overflow);
     cudaFree(h->overflow_count);
@@ -1253,9 +1258,24 @@ int rp_count_overlaps(void *handle, int early_exit, int64_t *out_count) {
     }
     RP_CUDA(h, cudaMemsetAsync(h->count_out, 0, sizeof(unsigned long long), h->stream));
     RP_CUDA(h, cudaMemsetAsync(h->flag, 0, sizeof(int), h->stream));
+    // polyspherocylinders: the FP64 segment tests of the recount go to a second, lane-dense
+    // kernel (polyspheres' centre tests are cheap enough inline)
+    const bool defer = h->ncen > 0 && h->segs;
+    if (defer) {
+        if (!h->cq_buf) {
+            RP_CUDA(h, cudaMalloc(&h->cq_buf, sizeof(DeferredPair) * Handle::CQ_CAP));
+            RP_CUDA(h, cudaMalloc(&h->cq_count, sizeof(int)));
+        }
+        RP_CUDA(h, cudaMemsetAsync(h->cq_count, 0, sizeof(int), h->stream));
+    }
     DevState s = dev_state(h);
+    if (defer) {
+        s.cq_buf = h->cq_buf;
+        s.cq_count = h->cq_count;
+        s.cq_cap = Handle::CQ_CAP;
+    }
     {
-        Group grp(h, RP_KERNEL_COUNT, 1);
+        Group grp(h, RP_KERNEL_COUNT, defer ? 2 : 1);
         RP_CUDA(h, launch_count(s, h->grid[h->gcur].d, early_exit ? 1 : 0, h->count_out, h->flag, h->stream));
     }
     unsigned long long c = 0;

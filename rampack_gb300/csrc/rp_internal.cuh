@@ -71,6 +71,13 @@ struct GridDev {
     float stage_thr;
 };
 
+// A centre pair of the recount left undecided by the FP32 thresholds: body pid's centre
+// aj / MAX_CEN against body pj's centre aj % MAX_CEN at FP32 separation d.
+struct DeferredPair {
+    int pid, pj, aj, pad;
+    float4 d;
+};
+
 struct DevState {
     int64_t n;
     int kind;
@@ -95,6 +102,11 @@ struct DevState {
     int segs;
     double chax[RP_MAX_CENTRES][3];
     const double *circ64;
+    // the recount's deferred FP64 centre pairs (multi-centre bodies): queued by k_count_poly,
+    // decided by k_count_deferred with every lane busy; null: decided inline
+    struct DeferredPair *cq_buf;
+    int *cq_count;
+    int cq_cap;
     // nonzero when the reference keeps no neighbour grid for this box (core/Packing.cpp:862-881):
     // it then measures sphere and polysphere-centre distances with the periodic boundary
     // conditions' own formula (pbc_distance2: per-coordinate |relative separation| folded

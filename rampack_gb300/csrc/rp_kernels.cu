@@ -288,12 +288,39 @@ cudaError_t launch_rescale(const double *src, double *dst, int64_t n, const doub
     return cudaGetLastError();
 }
 
+// The recount's deferred centre pairs, one per thread: the exact FP64 test (with the
+// polyspherocylinder segments' half axes), overlaps added to the count.
+__global__ void k_count_deferred(DevState s, int early, unsigned long long *out, int *flag) {
+    const int n = min(*s.cq_count, s.cq_cap);
+    unsigned long long cnt = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (early && *(volatile int *)flag) break;   // an overlap is already known
+        const DeferredPair e = s.cq_buf[i];
+        const int a = e.aj / MAX_CEN, j = e.aj % MAX_CEN;
+        d3 ha{0.0, 0.0, 0.0};
+        if (s.segs) ha = mv3(s.rot64 + 9 * (size_t)e.pid, d3{s.chax[a][0], s.chax[a][1], s.chax[a][2]});
+        const d3 pa = load_d3(s.abs64 + 3 * ((size_t)e.pid * s.ncen + a));
+        if (exact_centre_pair(s, pa, a, e.pj, j, make_float3(e.d.x, e.d.y, e.d.z), ha)) {
+            cnt++;
+            if (early) atomicExch(flag, 1);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(out, cnt);
+}
+
 cudaError_t launch_count(const DevState &s, const GridDev &g, int early, unsigned long long *out, int *flag,
                          cudaStream_t st) {
     unsigned nb = (unsigned)((s.n + 127) / 128);
     if (s.kind == 0) k_count<0><<<nb, 128, 0, st>>>(s, g, early, out, flag);
     else if (s.kind == 1) k_count<1><<<nb, 128, 0, st>>>(s, g, early, out, flag);
     else k_count_poly<<<nb, 128, 0, st>>>(s, g, early, out, flag);
+    if (s.kind == 2 && s.cq_buf) {
+        int sms = 152, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        k_count_deferred<<<sms * 8, 128, 0, st>>>(s, early, out, flag);
+    }
     return cudaGetLastError();
 }
 

@@ -1221,6 +1221,13 @@ __device__ __forceinline__ void count_poly_one(const DevState &s, const GridDev 
                     bool ov = !exact && d2 < g.cthr[a * MAX_CEN + j];
                     if (!ov && (exact || d2 <= g.cthr[MAX_CEN * MAX_CEN + a * MAX_CEN + j])) {
                         atomicAdd(s.counters + 5, 1ull);
+                        if (s.cq_buf) {
+                            const int qi = atomicAdd(s.cq_count, 1);
+                            if (qi < s.cq_cap) {
+                                s.cq_buf[qi] = DeferredPair{pid, pj, a * MAX_CEN + j, 0, make_float4(d.x, d.y, d.z, 0.f)};
+                                continue;
+                            }
+                        }
                         ov = exact_centre_pair(s, load_d3(s.abs64 + 3 * ((size_t)pid * K + a)), a, pj, j, d,
                                                s.segs ? d3{hx[3 * a], hx[3 * a + 1], hx[3 * a + 2]} : d3{0, 0, 0});
                     }
