@@ -395,15 +395,18 @@ int rp_batch_get_timing(void *batch, double *ms, uint64_t *groups, uint64_t *lau
  * framework that budgets or pools all device memory itself, or a stream-ordered pipeline
  * in which cudaMalloc/cudaFree would implicitly synchronise the device and stall its other
  * streams.  Inputs: d_pos (n x 3 doubles) and d_rot (n x 9 doubles) in device memory of the
- * current CUDA device, box9 and shape on the host; the work is ordered on `stream` (a
- * cudaStream_t, NULL for the default stream) and the call returns after it completes,
- * writing the count to *out_count (host).  Working memory is one fixed array of
- * RP_STATIC_SCRATCH_BYTES compiled into the library, which every GPU that loads the library
- * keeps until the process exits: n above RP_STATIC_MAX_PARTICLES, or a cell grid above
- * RP_STATIC_MAX_CELLS cells, is rejected with RP_ERR_CAPACITY.  The first call on a device
- * looks up the array's device address (with that device current), so make the first call
- * before any stream capture.  All calls share the array: calls whose GPU work overlaps
- * (from several host threads or streams) race and must be serialised by the caller. */
+ * current CUDA device (anything else, a host array for instance, is refused with
+ * RP_ERR_ARG before any launch), box9 and shape on the host.  The call is synchronous: its
+ * work is ordered on `stream` (a cudaStream_t, NULL for the default stream), and the call
+ * waits for it and writes the count to *out_count (host).  Working memory is one fixed
+ * array of RP_STATIC_SCRATCH_BYTES compiled into the library, which every GPU that loads
+ * the library keeps until the process exits: n above RP_STATIC_MAX_PARTICLES is rejected
+ * with RP_ERR_CAPACITY (dilute packings get cells larger than the interaction range, so the
+ * grid stays within RP_STATIC_MAX_CELLS).  The first call on a device looks up the array's
+ * device address (with that device current) and keeps it, so make the first call before
+ * any stream capture, and make no call on a device after cudaDeviceReset.  All calls share
+ * the array: calls whose GPU work overlaps (from several host threads or streams) race and
+ * must be serialised by the caller. */
 int rp_count_overlaps_static(const rp_shape_desc *shape, int64_t n, const double *d_pos, const double *d_rot,
                              const double *box9, int early_exit, void *stream, int64_t *out_count);
 

@@ -21,7 +21,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "librpref.so")
-REFERENCE_DIR = "/root/reference"
+# the reference checkout (read-only): RAMPACK_REFERENCE_DIR, else the default mount point
+REFERENCE_DIR = os.environ.get("RAMPACK_REFERENCE_DIR", "/root/reference")
 
 SPHERE, SPHEROCYLINDER, POLYSPHERE = 0, 1, 2
 
@@ -51,7 +52,8 @@ def build(reference: bool = False) -> None:
     """Compiles liboracle.so (and the reference library when asked and possible)."""
     subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
     if reference and os.path.isdir(os.path.join(REFERENCE_DIR, "src")):
-        subprocess.run(["make", "-s", "-j", str(os.cpu_count() or 4), "-C", HERE, "ref"], check=True)
+        subprocess.run(["make", "-s", "-j", str(os.cpu_count() or 4), "-C", HERE, "ref", f"REF={REFERENCE_DIR}"],
+                       check=True)
 
 
 def reference_available() -> bool:
@@ -112,6 +114,8 @@ def _lib(which: str):
         lib.ref_sim_run.argtypes = [_P, C.POINTER(SimParams), C.c_int64, C.POINTER(SimStats)]
         lib.ref_banana_centres.restype = C.c_int
         lib.ref_banana_centres.argtypes = [C.c_double, C.c_double, C.c_int, C.c_double, _D]
+        lib.ref_nematic_order.restype = C.c_int
+        lib.ref_nematic_order.argtypes = [_P, _D]
     _LIBS[which] = (lib, pre)
     return _LIBS[which]
 
@@ -164,6 +168,16 @@ class CpuPacking:
             self.close()
         except Exception:
             pass
+
+    def nematic_order(self):
+        """(Q tensor 3x3, P2) from the reference's own NematicOrder (reference library only)."""
+        if self.which != "reference":
+            raise ValueError("nematic_order: the reference's NematicOrder is in the reference library only")
+        out = np.zeros(7)
+        if self.lib.ref_nematic_order(self.h, _dp(out)) != 0:
+            raise RuntimeError("NematicOrder::calculate failed")
+        q = np.array([[out[1], out[2], out[3]], [out[2], out[4], out[5]], [out[3], out[5], out[6]]])
+        return q, float(out[0])
 
     def count_overlaps(self, early_exit: bool = False) -> int:
         return int(self._f("count_overlaps")(self.h, 1 if early_exit else 0))

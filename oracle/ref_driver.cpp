@@ -21,6 +21,7 @@
 #include "core/FreeBoundaryConditions.h"
 #include "core/Simulation.h"
 #include "core/ObservablesCollector.h"
+#include "core/observables/NematicOrder.h"
 #include "core/observables/correlation/LayerwiseRadialEnumerator.h"
 #include "core/observables/correlation/LinearEnumerator.h"
 #include "core/observables/correlation/PairAveragedCorrelation.h"
@@ -145,6 +146,22 @@ void *ref_create(int kind, const double *prm, int np, int64_t n, const double *p
 }
 
 void ref_destroy(void *hp) { delete static_cast<Handle *>(hp); }
+
+// NematicOrder::calculate (core/observables/NematicOrder.cpp:9-28) of the handle's packing
+// with the Q tensor dumped: out7 = P2, Q_11, Q_12, Q_13, Q_22, Q_23, Q_33.
+int ref_nematic_order(void *hp, double *out7) {
+    auto *h = static_cast<Handle *>(hp);
+    try {
+        NematicOrder no(true);
+        no.calculate(*h->pk, 1.0, 1.0, *h->traits);
+        std::vector<double> v = no.getIntervalValues();
+        if (v.size() != 7) return -1;
+        for (int i = 0; i < 7; i++) out7[i] = v[i];
+    } catch (const std::exception &) {
+        return -1;
+    }
+    return 0;
+}
 
 int64_t ref_count_overlaps(void *hp, int early) {
     auto *h = static_cast<Handle *>(hp);

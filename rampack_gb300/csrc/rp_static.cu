@@ -21,6 +21,7 @@
 #include <mutex>
 
 #include "rp_internal.cuh"
+#include "rp_margins.cuh"
 
 namespace rp {
 
@@ -57,7 +58,9 @@ static __device__ __align__(256) unsigned char g_static_scratch[RP_STATIC_SCRATC
 namespace {
 
 // Device address of the scratch array, looked up once per device with that device current
-// (in host code the array's name is only a host-side stand-in, not a device address).
+// (in host code the array's name is only a host-side stand-in, not a device address).  The
+// address belongs to the device's primary context: cudaDeviceReset destroys that context,
+// and this entry point must not be called on that device after a reset.
 std::mutex g_addr_mutex;
 void *g_addr[64] = {};
 
@@ -88,6 +91,17 @@ extern "C" int rp_count_overlaps_static(const rp_shape_desc *shape, int64_t n, c
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     int device = 0;
     if (cudaGetDevice(&device) != cudaSuccess) return RP_ERR_CUDA;
+    // The kernels read d_pos and d_rot directly: refuse, before any launch, pointers that
+    // are not device (or managed) memory of the current device, e.g. a host array.
+    for (const void *p : {static_cast<const void *>(d_pos), static_cast<const void *>(d_rot)}) {
+        cudaPointerAttributes attr{};
+        if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+            cudaGetLastError();  // clear the (non-sticky) error an unknown pointer leaves
+            return RP_ERR_ARG;
+        }
+        if ((attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged) || attr.device != device)
+            return RP_ERR_ARG;
+    }
     void *base_v = nullptr;
     int rc = scratch_address(device, &base_v);
     if (rc != RP_OK) return rc;
@@ -110,19 +124,28 @@ extern "C" int rp_count_overlaps_static(const rp_shape_desc *shape, int64_t n, c
             return RP_ERR_UNSUPPORTED;
     }
     GridDev g{};
-    const double cell_min = range * (1.0 + 1e-9);
-    int64_t ncell = 1;
-    for (int d = 0; d < 3; d++) {
+    // Cells at least one interaction range high; a dilute packing whose range-sized cells
+    // would exceed the scratch's cell table gets larger cells (still correct: every pair
+    // within range lies in neighbouring cells), so only n itself is ever too large.
+    double cell_min = range * (1.0 + 1e-9);
+    for (int d = 0; d < 3; d++)
         if (!(hgt[d] >= cell_min)) return RP_ERR_UNSUPPORTED;
-        double nd = std::floor(hgt[d] / cell_min);
-        int nn = nd > SMAX_CELLS ? static_cast<int>(SMAX_CELLS) : static_cast<int>(nd);
-        nn = nn >= 2 ? (nn & ~1) : 1;
-        g.dims[d] = nn;
-        g.shift[d] = 0.0;
-        ncell *= nn;
+    for (;;) {
+        int64_t ncell = 1;
+        for (int d = 0; d < 3; d++) {
+            double nd = std::floor(hgt[d] / cell_min);
+            int nn = nd > SMAX_CELLS ? static_cast<int>(SMAX_CELLS) : static_cast<int>(nd);
+            nn = nn >= 2 ? (nn & ~1) : 1;
+            g.dims[d] = nn;
+            g.shift[d] = 0.0;
+            ncell *= nn;
+        }
+        if (ncell <= SMAX_CELLS) {
+            g.ncell = static_cast<int>(ncell);
+            break;
+        }
+        cell_min *= 1.125;
     }
-    if (ncell > SMAX_CELLS) return RP_ERR_CAPACITY;
-    g.ncell = static_cast<int>(ncell);
     double cm[9], cminv[9];
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) cm[3 * i + j] = box9[3 * i + j] / g.dims[j];
@@ -166,38 +189,18 @@ extern "C" int rp_count_overlaps_static(const rp_shape_desc *shape, int64_t n, c
     s.strict_box = 1;
     ExactShape ex{};
     ex.kind = shape->kind;
-    FilterConsts fc{};
-    const double u32 = std::ldexp(1.0, -24), safety = 4.0;
-    const double e_sep = 24.0 * u32 * (lrow + 1.0), e_axis = 16.0 * u32;
-    auto margin = [&](double thr) {
-        double d = std::sqrt(thr);
-        return safety * (2.0 * d * std::sqrt(3.0) * e_sep + 3.0 * e_sep * e_sep + 8.0 * u32 * thr);
-    };
     if (shape->kind == RP_SHAPE_SPHERE) {
         ex.sphere_thr = std::pow(2 * r, 2);  // SphereTraits.cpp:64
-        fc.sphere_lo = static_cast<float>(ex.sphere_thr - margin(ex.sphere_thr));
-        fc.sphere_hi = static_cast<float>(ex.sphere_thr + margin(ex.sphere_thr));
     } else {
         ex.core_thr = 4 * r * r;                // SpherocylinderTraits.cpp:35
         ex.far_thr = std::pow(2 * r + l, 2);    // SpherocylinderTraits.cpp:37
         short beg = -1, end = 1;
         ex.neg_cap_half = 0.5 * beg * l;
         ex.cap_half = 0.5 * end * l;
-        fc.core_lo = static_cast<float>(ex.core_thr - margin(ex.far_thr));
-        fc.core_hi = static_cast<float>(ex.core_thr + margin(ex.far_thr));
-        fc.far_lo = static_cast<float>(ex.far_thr - margin(ex.far_thr));
-        fc.far_hi = static_cast<float>(ex.far_thr + margin(ex.far_thr));
-        fc.core_thr = static_cast<float>(ex.core_thr);
-        double dend = std::sqrt(3.0) * (e_sep + l * e_axis), dmax = 2 * r + l;
-        double eval = 12.0 * u32 * (dmax + 3 * l) * (dmax + 3 * l);
-        fc.seg_err = static_cast<float>(safety * (2.0 * (2 * r) * 2.0 * dend + 4.0 * dend * dend + eval));
-        fc.d_min = static_cast<float>(2e-4 * l * l * l * l);
-        fc.len = static_cast<float>(l);
-        fc.half_len = static_cast<float>(0.5 * l);
     }
-    fc.cell_margin = 1e-5f;
     s.ex = ex;
-    s.fc = fc;
+    // the same FP32 margins as the handle's recount (a fresh grid, no mirror updates)
+    s.fc = hard_filter_consts(shape->kind, r, l, lrow, box9);
     double tt[375];
     for (int a = 0; a < 5; a++)
         for (int b = 0; b < 5; b++)

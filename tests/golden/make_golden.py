@@ -9,6 +9,7 @@ Run in a checkout where the reference sources are present:
     python tests/golden/make_golden.py flips  # the FlipSampler moves only
     python tests/golden/make_golden.py walls  # the hard-wall packings only
     python tests/golden/make_golden.py correlation  # the pair-correlation observables only
+    python tests/golden/make_golden.py nematic  # the nematic order of orientation sets only
 
 Every expected value below is produced by the reference library (oracle/_ref/librpref.so:
 rampack's Packing, NeighbourGrid, SpherocylinderTraits, samplers and Simulation compiled
@@ -405,6 +406,43 @@ def gen_correlation():
     print("correlation:", len(CORRELATIONS), "observables")
 
 
+def nematic_orientations(rng):
+    """Orientation sets of spherocylinders for the nematic-order fixture: aligned, isotropic,
+    near-aligned along z, nematic along a tilted director, and a thermalised packing."""
+    import systems
+    sets = {}
+    sets["aligned"] = np.tile(np.eye(3).reshape(9), (100, 1))
+    sets["isotropic"] = rand_rot(rng, 1000).reshape(-1, 9)
+    small = []
+    for _ in range(500):
+        ax = rng.normal(size=3)
+        ax /= np.linalg.norm(ax)
+        small.append(po.rotation("reference", ax, float(rng.uniform(-0.3, 0.3))))
+    sets["near_z"] = np.array(small)
+    t3 = np.asarray(po.rotation("reference", np.array([1.0, 1.0, 0.0]) / np.sqrt(2.0), 0.9)).reshape(3, 3)
+    sets["tilted"] = np.array([(t3 @ m.reshape(3, 3)).reshape(9) for m in small[:300]])
+    sets["sc_l2"] = np.asarray(systems.sc_l2()[3], dtype=np.float64).reshape(-1, 9)
+    return sets
+
+
+def gen_nematic(rng):
+    """NematicOrder of the reference (core/observables/NematicOrder.cpp:9-28) on the sets above."""
+    out = {}
+    for name, rot in nematic_orientations(rng).items():
+        n = len(rot)
+        pos = np.zeros((n, 3))
+        box = np.eye(3).reshape(9) * 50.0
+        pk = po.CpuPacking("reference", po.SPHEROCYLINDER, np.array([2.0, 0.5]), pos, rot, box)
+        q, p2 = pk.nematic_order()
+        pk.close()
+        out[f"{name}_rot"] = rot
+        out[f"{name}_q"] = q
+        out[f"{name}_p2"] = np.array([p2])
+    np.savez_compressed(os.path.join(HERE, "nematic.npz"), names=np.array(sorted(k[:-4] for k in out if k.endswith("_rot"))),
+                        **out)
+    print("nematic:", len(out) // 3, "orientation sets")
+
+
 def main():
     if not po.reference_available():
         po.build(reference=True)
@@ -423,6 +461,9 @@ def main():
     if sys.argv[1:] == ["box"]:
         gen_box_proposals()
         return
+    if sys.argv[1:] == ["nematic"]:
+        gen_nematic(np.random.default_rng(20261205))
+        return
     rng = np.random.default_rng(20241203)
     gen_pairs(rng)
     gen_geometry(rng)
@@ -440,6 +481,7 @@ def main():
     gen_flips()
     gen_walls()
     gen_correlation()
+    gen_nematic(np.random.default_rng(20261205))
 
 
 if __name__ == "__main__":

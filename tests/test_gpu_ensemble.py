@@ -137,3 +137,23 @@ def test_nematic_order_matches_the_restatement(engine, name):
     qr, p2r = obs.nematic_order(rot)
     np.testing.assert_allclose(q, qr, rtol=0, atol=1e-12)
     assert abs(p2 - p2r) <= 1e-12
+
+
+def test_nematic_order_matches_the_reference_fixture(engine):
+    """rp_nematic_order on the orientation sets whose Q tensor and P2 the reference's own
+    NematicOrder computed (tests/golden/nematic.npz), to 1e-12."""
+    import os
+    from rampack_gb300.packing import GpuPacking
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "nematic.npz"))
+    for name in z["names"]:
+        rot = z[f"{name}_rot"]
+        n = len(rot)
+        # particles on a loose simple-cubic lattice, so that the packing is valid
+        k = int(np.ceil(n ** (1 / 3)))
+        idx = np.arange(n)
+        pos = np.stack([idx % k, (idx // k) % k, idx // (k * k)], axis=1) * 4.0 + 2.0
+        box = np.eye(3) * (4.0 * k)
+        with GpuPacking(po.SPHEROCYLINDER, (2.0, 0.5), pos, rot, box) as g:
+            q, p2 = g.nematic_order()
+        np.testing.assert_allclose(q, z[f"{name}_q"], rtol=0, atol=1e-12, err_msg=str(name))
+        assert abs(p2 - float(z[f"{name}_p2"][0])) <= 1e-12, name

@@ -69,3 +69,41 @@ def test_static_count_rejects_oversize(engine):
     rc = lib.rp_count_overlaps_static(C.byref(desc), 65537, C.c_void_p(d_pos.data_ptr()),
                                       C.c_void_p(d_rot.data_ptr()), _lib.dptr(b), 0, None, C.byref(out))
     assert rc == -7  # RP_ERR_CAPACITY
+
+
+def test_static_count_dilute_packing_gets_larger_cells(engine):
+    """1000 spheres in a box of side 60: range-sized cells would number 216,000, above the
+    scratch's 65,536; the count enlarges its cells and still equals the allocating count."""
+    from rampack_gb300.packing import GpuPacking
+    lib = _lib.load()
+    rng = np.random.default_rng(1234)
+    box = np.eye(3) * 60.0
+    pos = rng.uniform(0.0, 60.0, size=(1000, 3))
+    rot = np.tile(np.eye(3).reshape(9), (1000, 1))
+    cfg = (_lib.SHAPE_SPHERE, (0.5,), pos, rot, box)
+    with GpuPacking(*cfg) as g:
+        want = g.count_total_overlaps(False)
+    assert want > 0  # the random gas has overlapping pairs
+    for _ in range(2):
+        assert static_count(lib, cfg, False) == want
+        assert static_count(lib, cfg, True) == 1
+
+
+def test_static_count_refuses_host_pointers(engine):
+    """Positions in host memory are refused with RP_ERR_ARG before any kernel runs."""
+    import torch
+    lib = _lib.load()
+    desc = _lib.ShapeDesc()
+    desc.kind = _lib.SHAPE_SPHERE
+    desc.radius = 0.5
+    b = np.eye(3).reshape(9) * 10.0
+    h_pos = np.zeros((8, 3))
+    d_rot = torch.zeros(8 * 9, dtype=torch.float64, device="cuda")
+    out = C.c_int64(-1)
+    rc = lib.rp_count_overlaps_static(C.byref(desc), 8, C.c_void_p(h_pos.ctypes.data), C.c_void_p(d_rot.data_ptr()),
+                                      _lib.dptr(b), 0, None, C.byref(out))
+    assert rc == -1  # RP_ERR_ARG
+    assert out.value == -1
+    # the library still works after the refusal
+    cfg = systems.ALL["hs_dense"]()
+    assert static_count(lib, cfg, False) >= 0
