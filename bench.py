@@ -5,9 +5,11 @@ Workload (one "step" = one Monte Carlo cycle): hard spherocylinders l=2, r=0.5 (
 N = 100^3 = 1,000,000 started aligned on an orthorhombic lattice (cell aspect 1:1:3) at
 packing fraction 0.50 in a box that the isotension moves make triclinic; each cycle is
 2N particle moves (translation step 0.2 and rotation step 0.2, half each, in
-checkerboard domains) plus one isotension box move (every box-matrix entry perturbed
-by up to 0.005, p* = 1.5, T = 1) whose overlap check rescales, rebuilds the cell grid
-and recounts all overlaps.  Synthetic seeded input; no dataset.
+checkerboard domains) plus one box move, alternately an isotension move (every box-matrix
+entry perturbed by up to 0.005) and an isotropic volume move (ln V uniform in +-1e-6), at
+p* = 1.5, T = 1, whose overlap check rescales, rebuilds the cell grid and recounts all
+overlaps.  The default line also compares the learned test ordering with the plain scan
+on the same state ("ordering").  Synthetic seeded input; no dataset.
 
   python bench.py [--gpus N] [--steps K] [--warmup W]           GPU engine (this repo)
   python bench.py --impl reference [--steps K] [--warmup W]     CPU implementation of the path
@@ -35,9 +37,13 @@ sys.path.insert(0, ROOT)
 METRIC = "moves/sec at N=1e6"
 UNIT = "moves/s"
 TRANS_STEP, ROT_STEP, BOX_STEP, PRESSURE, TEMPERATURE = 0.2, 0.2, 0.005, 1.5, 1.0
+# isotropic volume move of the headline: ln V uniform in +-VOL_STEP (LogScalingFactorSampler on
+# X & Y & Z, VOL_STEP / 3 per side), the acceptance window at N = 1e6 and p* = 1.5
+VOL_STEP = 1e-6
 WORKLOAD = ("hard spherocylinders l=2 r=0.5 (L/D=2), N={n:,}, aligned orthorhombic start at phi=0.50 "
             "(cell aspect 1:1:3), triclinic box; per cycle 2N moves (translation 0.2, rotation 0.2) "
-            "+ 1 isotension box move (delta 0.005, p*=1.5, T=1)")
+            "+ 1 box move, alternating an isotension move (TriclinicDeltaScaler, delta 0.005) and an "
+            "isotropic volume move (log scaling of X & Y & Z, ln V uniform in +-1e-6); p*=1.5, T=1")
 
 
 def parse():
@@ -51,6 +57,8 @@ def parse():
                     help="sc-1e6: the headline system; the others are further systems of the same path")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-ordering", action="store_true",
+                    help="skip the learned-ordering comparison of the headline line")
     ap.add_argument("--seed", type=int, default=1234)
     ap.add_argument("--tuning", default=None,
                     help="replicas-64: fixed launch shape 'cell_factor,warps_per_block' instead of autotuning")
@@ -197,7 +205,9 @@ def cpu_domains(threads: int):
     return best
 
 
-def cpu_run(cfg, cycles: int, warmup: int, threads: int, seed: int):
+def cpu_run(cfg, cycles: int, warmup: int, threads: int, seed: int, volume_moves: bool = False):
+    """The oracle's cycle loop on all host threads; with ``volume_moves`` the box move of odd
+    cycles is the isotropic log-volume move instead of isotension (the headline's cycle)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as po
     po.build()
@@ -206,12 +216,13 @@ def cpu_run(cfg, cycles: int, warmup: int, threads: int, seed: int):
     dom = cpu_domains(threads)
     kw = dict(translation_step=TRANS_STEP, rotation_step=ROT_STEP, box_kind=1, box_step=BOX_STEP,
               pressure=PRESSURE, temperature=TEMPERATURE, domains=dom, threads=threads, seed=seed)
+    kw_vol = dict(kw, box_kind=2, box_step=VOL_STEP / 3)
     if warmup:
         po.run_cycles(pk, warmup, **kw)
     times = []
     for c in range(cycles):
         t = time.perf_counter()
-        st = po.run_cycles(pk, 1, **dict(kw, seed=seed + 1000 + c))
+        st = po.run_cycles(pk, 1, **dict(kw_vol if volume_moves and c % 2 else kw, seed=seed + 1000 + c))
         times.append(time.perf_counter() - t)
     pk.close()
     moves = 2 * len(pos)
@@ -224,7 +235,8 @@ def main_reference(args):
         return 0
     threads = os.cpu_count() or 1
     cfg = workload(args)
-    moves, times, dom, dom_used = cpu_run(cfg, max(1, args.steps), max(0, args.warmup), threads, args.seed)
+    moves, times, dom, dom_used = cpu_run(cfg, max(1, args.steps), max(0, args.warmup), threads, args.seed,
+                                          volume_moves=args.workload == "sc-1e6")
     total = sum(times)
     value = moves * len(times) / total
     line = {
@@ -329,18 +341,37 @@ def main_gpu(args):
     stream = torch.cuda.ExternalStream(g.stream(), device=local)
     seed = args.seed + 7919 * rank
 
-    # the native cycle loop (rp_sim): one device sweep, then one isotension box move
-    # (TriclinicDeltaScaler, every entry +- 0.005, std::mt19937) pre-checked on the host
+    # the native cycle loop (rp_sim): one device sweep, then one box move pre-checked on the
+    # host: an isotension move (TriclinicDeltaScaler, every entry +- 0.005, std::mt19937) and,
+    # on the headline, on every other cycle an isotropic log-volume move (ln V +- VOL_STEP),
+    # each simulation with its own generator and Philox key
     from rampack_gb300 import simulation as SIM
-    sim = SIM.Simulation(g, TRANS_STEP, ROT_STEP, seed, SIM.delta_triclinic(BOX_STEP, True))
-    sim.set_conditions(TEMPERATURE, PRESSURE)
-    sim.run(max(3, args.warmup))
+    sims = [SIM.Simulation(g, TRANS_STEP, ROT_STEP, seed, SIM.delta_triclinic(BOX_STEP, True))]
+    if args.workload == "sc-1e6":
+        sims.append(SIM.Simulation(g, TRANS_STEP, ROT_STEP, seed + 104729, SIM.log_volume(VOL_STEP / 3)))
+    for sm in sims:
+        sm.set_conditions(TEMPERATURE, PRESSURE)
+    state = {"k": 0}
+
+    def run_cycles(k):
+        for _ in range(k):
+            sims[state["k"] % len(sims)].run(1)
+            state["k"] += 1
+
+    def box_counts():
+        out = []
+        for sm in sims:
+            st = sm.stats()
+            out.append((st["box_moves"], st["accepted_box_moves"]))
+        return out
+
+    run_cycles(max(3, args.warmup))
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
 
     s0 = g.stats()
-    b0 = sim.stats()
+    b0 = box_counts()
     g.set_timing(True)
     clocks = Clocks(local)
     clocks.start()
@@ -349,12 +380,16 @@ def main_gpu(args):
     torch.cuda.synchronize()
     t0 = time.time()
     ev0.record(stream)
-    b1 = sim.run(args.steps)
+    run_cycles(args.steps)
     ev1.record(stream)
     ev1.synchronize()
     torch.cuda.synchronize()
     t1 = time.time()
-    box_acc = b1["accepted_box_moves"] - b0["accepted_box_moves"]
+    b1 = box_counts()
+    box_names = ["isotension", "isotropic_volume"]
+    box_moves = {box_names[i]: {"moves": b1[i][0] - b0[i][0], "accepted": b1[i][1] - b0[i][1]}
+                 for i in range(len(sims))}
+    box_acc = sum(v["accepted"] for v in box_moves.values())
     ms = ev0.elapsed_time(ev1)
     clk = clocks.stop(t0, t1)
     timing = g.timing()
@@ -397,8 +432,12 @@ def main_gpu(args):
     else:
         peak, peak_src = 6800.0, "fallback"
     traffic = read_profile_traffic(args.workload)
-    state_mb = n * (96 + 32 + 64 * kcen) / 1e6
-    l2_note = (f"inputs larger than L2 (FP64 state + FP32 mirror {state_mb:.0f} MB + cell lists)" if state_mb > 129
+    # bytes every cycle touches: the FP64 state (96 B), the FP32 mirror (32 B) and the cell
+    # lists the rebuild writes (slot, particle, cell and rank indices and the by-particle FP32
+    # position: 32 B) per particle, plus the polysphere centres
+    state_mb = n * (96 + 32 + 32 + 64 * kcen) / 1e6
+    l2_note = (f"inputs larger than L2: every cycle touches {state_mb:.0f} MB of device state (FP64 state, "
+               f"FP32 mirror, cell lists; L2 129 MB)" if state_mb > 129
                else f"inputs smaller than L2 ({state_mb:.0f} MB of state; no flush between steps)")
 
     # ---- end to end through the C ABI with host buffers ----
@@ -415,7 +454,7 @@ def main_gpu(args):
         f0.record(stream)
         for _ in range(e_steps):
             g.upload(hpos, hrot, hbox)   # H2D of the step's input state (pinned)
-            sim.run(1)
+            run_cycles(1)
             g.state(out=(hpos, hrot, hbox))  # D2H of the step's result into the same pinned buffers
         f1.record(stream)
         f1.synchronize()
@@ -427,16 +466,23 @@ def main_gpu(args):
                "d2h_bytes_per_step": int(n * 12 * 8),
                "step": "rp_upload_state (pinned host -> device) + one cycle + rp_download_state (device -> pinned host)"}
 
+    # ---- learned test ordering against the plain scan on the same state (rank 0, headline) ----
+    ordering = None
+    if rank == 0 and args.workload == "sc-1e6" and not args.no_ordering:
+        ordering = ordering_compare(g, args, sweeps=max(4, min(args.steps, 8)),
+                                    variants=[("plain", 0, 1), ("distance", 2, 16), ("mlp", 1, 64)])
+
     # ---- CPU baseline (rank 0, N=1 only) ----
     cpu_base = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        cmoves, ctimes, dom, dom_used = cpu_run(cfg, 2, 1, threads, args.seed)
+        cmoves, ctimes, dom, dom_used = cpu_run(cfg, 2, 1, threads, args.seed, volume_moves=args.workload == "sc-1e6")
         cpu_base = {"value": cmoves * len(ctimes) / sum(ctimes), "unit": UNIT, "cores": threads, "kind": "port",
                     "sample": f"2 full cycles of the same N={n:,} system after 1 warm-up cycle, OpenMP domain "
                               f"decomposition {dom_used} (oracle/ restatement of the reference's path)"}
 
-    sim.close()
+    for sm in sims:
+        sm.close()
     g.close()
     if rank == 0:
         line = {
@@ -447,7 +493,8 @@ def main_gpu(args):
                        "variant": "plain (unordered FP32 filter + FP64 guard band)",
                        "l2": l2_note,
                        "parallelism": "replicas" if world > 1 else "single GPU",
-                       "grid_dims": list(info["dims"]), "box_moves_accepted": box_acc},
+                       "grid_dims": list(info["dims"]), "box_moves_accepted": box_acc,
+                       "box_moves": box_moves},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "k_sweep (one launch per checkerboard phase)",
@@ -460,51 +507,44 @@ def main_gpu(args):
             "gpu_launches": launches, "clocks": clk,
             "e2e": e2e, "cpu_baseline": cpu_base,
         }
+        if ordering is not None:
+            line["ordering"] = ordering
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
     return 0
 
 
-def main_ordering(args):
-    """Sweeps of the bench workload with the plain neighbourhood scan, with partners ranked by
-    centre distance, and with partners ranked by the network trained on pair outcomes logged
-    by the sweep itself.  Every ordering must leave the state bit-identical to the plain
-    sweep's; reported: device time of the move sweep and of the ranking per sweep, and the
-    candidate pairs examined per move."""
+def ordering_compare(g, args, sweeps: int, variants, training_sweeps: int = 4, every_move: int = 16,
+                     epochs: int = 4):
+    """Sweeps from the packing's current state with the plain neighbourhood scan, with partners
+    ranked by centre distance and with partners ranked by the network trained (on the device,
+    by the engine's own kernels) on pair outcomes the sweep itself logs.  Every ordering must
+    leave the FP64 state bit-identical to the plain sweep's.  Per variant: device time of the
+    move sweep and of the ranking per sweep (CUDA events), candidate pairs examined per move;
+    ``speedup_vs_plain`` = plain total / variant total, ``speedup_ranking_free`` = plain sweep /
+    variant sweep (the ceiling of the ordering with its ranking made free)."""
     from rampack_gb300 import _lib
-    from rampack_gb300 import build as rb
-    rb.build()
-    from rampack_gb300.packing import GpuPacking
-
-    kind, prm, pos, rot, box = workload(args)
-    g = GpuPacking(kind, prm, pos, rot, box)
-    for c in range(20):
-        g.sweep(TRANS_STEP, ROT_STEP, seed=args.seed, counter=c, stats=False)
     start = g.state()
-    # training data: pairs of every 16th move of 4 sweeps, then 4 epochs of Adam
-    g.pair_log_enable(4_000_000, 16)
-    for c in range(4):
+    # training data: pairs reaching the segment test in every 16th move of 4 sweeps
+    g.pair_log_enable(4_000_000, every_move)
+    for c in range(training_sweeps):
         g.sweep(TRANS_STEP, ROT_STEP, seed=args.seed + 1, counter=c, stats=False)
     feats, labels = g.pair_log()
     _, loss0 = g.mlp_gradient(feats[:200_000], labels[:200_000])
     g.set_timing(True)
     t0 = time.perf_counter()
-    loss = g.mlp_train(epochs=4, batch=1024, lr=2e-3, seed=args.seed)
+    loss = g.mlp_train(epochs=epochs, batch=1024, lr=2e-3, seed=args.seed)
     train_s = time.perf_counter() - t0
     train_ms = g.timing()["mlp"][0]
     g.set_timing(False)
     _, loss1 = g.mlp_gradient(feats[:200_000], labels[:200_000])
     g.pair_log_enable(0)
-
-    sweeps = max(args.steps, 4)
-    rows = []
-    ref_state = None
-    for label, mode, every in [("plain", _lib.ORDER_OFF, 1), ("distance", _lib.ORDER_DISTANCE, 1),
-                               ("distance", _lib.ORDER_DISTANCE, 16), ("mlp", _lib.ORDER_MLP, 1),
-                               ("mlp", _lib.ORDER_MLP, 16), ("mlp", _lib.ORDER_MLP, 64)]:
+    modes = {"plain": _lib.ORDER_OFF, "distance": _lib.ORDER_DISTANCE, "mlp": _lib.ORDER_MLP}
+    rows, ref_state = [], None
+    for label, _, every in variants:
         g.upload(*start)
-        g.set_ordering(mode, every)
+        g.set_ordering(modes[label], every)
         g.set_timing(True)
         pairs = moves = 0
         for c in range(sweeps):
@@ -522,16 +562,42 @@ def main_ordering(args):
         rows.append({"ordering": label, "rerank_every": every, "sweep_ms": round(sweep_ms, 4),
                      "ranking_ms": round(order_ms, 4), "total_ms": round(sweep_ms + order_ms, 4),
                      "pairs_per_move": round(pairs / moves, 2), "state_identical_to_plain": same})
-    base = rows[0]["total_ms"]
+    g.set_ordering(_lib.ORDER_OFF, 1)
+    g.upload(*start)
+    base, base_sweep = rows[0]["total_ms"], rows[0]["sweep_ms"]
     for r in rows:
         r["speedup_vs_plain"] = round(base / r["total_ms"], 3)
-    print(json.dumps({"metric": "learned ordering vs plain scan", "unit": "ms per sweep",
-                      "workload": WORKLOAD.format(n=len(pos)), "sweeps": sweeps,
-                      "training": {"pairs": int(len(feats)), "positive_fraction": round(float(labels.mean()), 4),
-                                   "epochs": 4, "batch": 1024, "loss_before": round(loss0, 4),
-                                   "loss_after": round(loss1, 4), "last_epoch_loss": round(loss, 4),
-                                   "device_ms": round(train_ms, 1), "wall_s": round(train_s, 2)},
-                      "rows": rows}))
+        r["speedup_ranking_free"] = round(base_sweep / r["sweep_ms"], 3)
+    learned = [r for r in rows if r["ordering"] == "mlp"]
+    best = max(learned or rows, key=lambda r: r["speedup_vs_plain"])
+    return {"speedup_vs_plain": best["speedup_vs_plain"], "rerank_every": best["rerank_every"],
+            "speedup_ranking_free": max(r["speedup_ranking_free"] for r in rows),
+            "state_identical_to_plain": all(r["state_identical_to_plain"] for r in rows),
+            "sweeps": sweeps, "unit": "ms per sweep (CUDA events)",
+            "training": {"pairs": int(len(feats)), "positive_fraction": round(float(labels.mean()), 4),
+                         "epochs": epochs, "batch": 1024, "loss_before": round(loss0, 4),
+                         "loss_after": round(loss1, 4), "last_epoch_loss": round(loss, 4),
+                         "device_ms": round(train_ms, 1), "wall_s": round(train_s, 2)},
+            "rows": rows}
+
+
+def main_ordering(args):
+    """The ordering comparison alone, with more variants: sweeps of the bench workload with the
+    plain neighbourhood scan, with partners ranked by centre distance, and with partners ranked
+    by the trained network, each re-ranked every 1, 16 or 64 sweeps."""
+    from rampack_gb300 import build as rb
+    rb.build()
+    from rampack_gb300.packing import GpuPacking
+
+    kind, prm, pos, rot, box = workload(args)
+    g = GpuPacking(kind, prm, pos, rot, box)
+    for c in range(20):
+        g.sweep(TRANS_STEP, ROT_STEP, seed=args.seed, counter=c, stats=False)
+    res = ordering_compare(g, args, sweeps=max(args.steps, 4),
+                           variants=[("plain", 0, 1), ("distance", 0, 1), ("distance", 0, 16), ("mlp", 0, 1),
+                                     ("mlp", 0, 16), ("mlp", 0, 64)])
+    g.close()
+    print(json.dumps(dict({"metric": "learned ordering vs plain scan", "workload": describe(args, len(pos))}, **res)))
     return 0
 
 

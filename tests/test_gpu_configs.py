@@ -1,0 +1,108 @@
+"""The benchmark's small hard-sphere configuration run as stated, on the GPU, against the oracle.
+
+Hard spheres of diameter 1, N = 1000 started on a 10x10x10 simple-cubic lattice in a cubic
+box at packing fraction 0.30, NpT at T = 1 and p* = 10, translation moves of step 0.1
+(uniform in a cube) and isotropic volume moves with ln V uniform in +-0.01 (the reference's
+AnisotropicVolumeScaler over a LogScalingFactorSampler on X & Y & Z, 0.01 / 3 per side),
+10^4 cycles with fixed steps:
+
+* the engine's native cycle loop (Simulation over a GpuPacking: device sweeps, reference
+  box scaler with std::mt19937 draws, host Metropolis pre-check) and the oracle's cycle loop
+  (the reference's Simulation restated, mt19937 proposals) give mean number densities that
+  agree within 3 combined standard errors of block averages;
+* a logged device sweep of the equilibrated GPU state replays move by move on the oracle
+  with identical outcome codes and final FP64 state, and a box move on it decides as the
+  oracle's tryScaling.
+
+The runs are seeded, so the outcome is deterministic.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import pyoracle as po
+from oracle import observables as obs
+from rampack_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+PRESSURE, TRANSLATION, BOX_STEP = 10.0, 0.1, 0.01 / 3
+SKIP, CYCLES, EVERY, BLOCK = 2000, 8000, 10, 40  # 10^4 cycles, 800 samples, 20 blocks
+
+
+def blocked(samples, block=BLOCK):
+    x = np.asarray(samples, dtype=np.float64)
+    n = len(x) // block
+    return x[:n * block].reshape(n, block).mean(1)
+
+
+def gpu_run():
+    from rampack_gb300.packing import GpuPacking
+    from rampack_gb300.simulation import Simulation, box_volume, log_volume
+    kind, prm, pos, rot, box = W.config_hs_1000()
+    rho = []
+    g = GpuPacking(kind, prm, pos, rot, box)
+    sim = Simulation(g, TRANSLATION, 0.0, seed=1234, scaler=log_volume(BOX_STEP))
+    sim.set_conditions(1.0, PRESSURE)
+    sim.run(SKIP)
+    for _ in range(CYCLES // EVERY):
+        st = sim.run(EVERY)
+        rho.append(g.n / box_volume(st["box"]))
+    st = sim.stats()
+    sim.close()
+    return g, rho, st
+
+
+def test_config_hs_1000_density_matches_the_oracle(oracle, engine):
+    g, rho_g, st = gpu_run()
+    try:
+        assert st["cycles"] == SKIP + CYCLES
+        assert st["box_moves"] == SKIP + CYCLES
+        assert 0.05 < st["accepted_box_moves"] / st["box_moves"] < 0.95
+        assert g.count_total_overlaps(False) == 0
+    finally:
+        g.close()
+
+    kind, prm, pos, rot, box = W.config_hs_1000()
+    cpu = po.CpuPacking("oracle", kind, prm, pos, rot, box, threads=1)
+    kw = dict(translation_step=TRANSLATION, box_kind=2, box_step=BOX_STEP, pressure=PRESSURE, temperature=1.0)
+    po.run_cycles(cpu, SKIP, seed=7, **kw)
+    rho_c = []
+    for k in range(CYCLES // EVERY):
+        po.run_cycles(cpu, EVERY, seed=1000 + k, **kw)
+        p, _, b = cpu.state()
+        rho_c.append(obs.number_density(len(p), b))
+    cpu.close()
+
+    mg, eg = obs.sem(blocked(rho_g))
+    mc, ec = obs.sem(blocked(rho_c))
+    # p* = 10 compresses the gas from phi = 0.30 to about phi = 0.47 (rho ~ 0.9)
+    assert 0.85 < mg < 0.95, mg
+    assert abs(mg - mc) <= 3 * math.hypot(eg, ec), (mg, eg, mc, ec)
+
+
+def test_config_hs_1000_logged_sweep_replays_on_the_oracle(oracle, engine):
+    g, _, st = gpu_run()
+    try:
+        p0, r0, b0 = g.state()
+        cpu = po.CpuPacking("oracle", W.SPHERE, np.array([0.5]), p0, r0, b0)
+        for cycle in range(3):
+            g.sweep(TRANSLATION, 0.0, seed=4321, counter=cycle, log=True)
+            moves, codes = g.sweep_log()
+            _, _, bounds = g.grid()
+            want, _ = cpu.replay(moves, bounds)
+            assert np.array_equal(codes, want), np.count_nonzero(codes != want)
+        gp, grot, gb = g.state()
+        cp, cr, _ = cpu.state()
+        assert np.array_equal(gp, cp) and np.array_equal(grot, cr)
+        # a compressing box move on the swept state: the engine's decision is the oracle's
+        for f in (0.999, 0.99):
+            nb = np.asarray(gb, dtype=np.float64).reshape(9) * f
+            de_g = g.try_scaling(nb)
+            de_c = cpu.try_scaling(nb)
+            assert de_g == de_c, (f, de_g, de_c)
+            g.revert_scaling()
+            cpu.revert_scaling()
+    finally:
+        g.close()
