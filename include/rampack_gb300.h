@@ -125,7 +125,8 @@ typedef struct rp_sweep_stats {
 #define RP_KERNEL_ORDER 5         /* partner ranking of the learned ordering */
 #define RP_KERNEL_MLP 6           /* ranking-network training and inference */
 #define RP_KERNEL_FIX 7           /* orientation renormalisation */
-#define RP_NUM_KERNELS 8
+#define RP_KERNEL_SINGLE 8        /* unrestricted single moves (rp_try_move / rp_accept_move) */
+#define RP_NUM_KERNELS 9
 
 /* ---- lifetime ---------------------------------------------------------------------- */
 
@@ -202,6 +203,24 @@ int rp_get_grid(void *handle, rp_grid_info *info, int32_t *cell_of_particle, dou
  * of a phase run concurrently, one warp each, and every move's particle must belong to
  * its cell.  out_codes (n bytes, optional) receives the outcome codes. */
 int rp_run_moves(void *handle, const rp_move *moves, int64_t n, uint8_t *out_codes);
+
+/* One move: Packing::tryTranslation / tryRotation / tryMove (core/Packing.cpp:84-164).
+ * domain6 NULL is std::nullopt, the reference's serial path
+ * (Simulation::performMovesWithoutDomainDivision, core/Simulation.cpp:365-390); otherwise an
+ * ActiveDomain given by its relative bounds lo[3], hi[3] (ActiveDomain::RegionBounds
+ * beg / end, core/ActiveDomain.h:19-31), which a translation or rototranslation must stay
+ * inside (checked before any overlap, as the reference does).  Uses move->particle, type,
+ * translation and rotation (move->domain and uniform are ignored); the tried state stays on
+ * the device, and *dE receives the move's energy: 0 or +inf, in overlap counting -inf, 0 or
+ * +inf (core/Packing.cpp:304-323).  One launch; synchronous.  A tried move is forgotten by
+ * any call that changes the packing. */
+int rp_try_move(void *handle, const rp_move *move, const double *domain6, double *dE);
+
+/* Commits the state the last rp_try_move tried.  Replaces: Packing::acceptTranslation /
+ * acceptRotation / acceptMove (core/Packing.cpp:234-302).  RP_ERR_STATE when no tried
+ * move is pending.  Stream-ordered (no synchronisation); later sweeps, recounts and box
+ * moves rebuild the cell grid first, later single moves do not. */
+int rp_accept_move(void *handle);
 
 /* One device-driven sweep: a random grid shift, then the 8 checkerboard phases in a
  * random order; every active cell performs (number of move types) x (occupancy) moves
@@ -532,7 +551,7 @@ int rp_ramtrj_info(const char *path, int64_t *num_particles, int64_t *snapshots,
                    int32_t *version);
 int rp_ramtrj_read(const char *path, int64_t snapshot, double *pos, double *rot, double *box9);
 
-/* ---- pair correlations (core/observables/correlation/*) ----------------------------- */
+/* ---- pair correlations (core/observables/correlation) ------------------------------- */
 
 /* PairEnumerator implementations: RadialEnumerator (RadialEnumerator.cpp:9-29, distance
  * between focal points), LinearEnumerator (LinearEnumerator.cpp:37-67, separation

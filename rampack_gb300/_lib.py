@@ -116,6 +116,8 @@ SIGNATURES = {
     "rp_set_grid": (C.c_int, [_P, _D, C.POINTER(GridInfo)]),
     "rp_get_grid": (C.c_int, [_P, C.POINTER(GridInfo), C.POINTER(C.c_int32), _D]),
     "rp_run_moves": (C.c_int, [_P, _P, C.c_int64, _P]),
+    "rp_try_move": (C.c_int, [_P, _P, _D, _D]),
+    "rp_accept_move": (C.c_int, [_P]),
     "rp_sweep": (C.c_int, [_P, C.POINTER(SweepParams), C.POINTER(SweepStats)]),
     "rp_sweep_log": (C.c_int, [_P, _P, _P, C.c_int64, C.POINTER(C.c_int64)]),
     "rp_try_scaling": (C.c_int, [_P, _D, _D]),
@@ -197,7 +199,7 @@ SIGNATURES = {
     "rp_correlation_last_error": (C.c_char_p, [_P]),
     "rp_correlation_destroy": (C.c_int, [_P]),
 }
-KERNEL_GROUPS = ["sweep", "rebuild", "count", "rescale", "overflow", "order", "mlp", "fix"]
+KERNEL_GROUPS = ["sweep", "rebuild", "count", "rescale", "overflow", "order", "mlp", "fix", "single"]
 MLP_NPARAM = 5313
 MLP_FEATURES = 16
 ORDER_OFF, ORDER_MLP, ORDER_DISTANCE = 0, 1, 2

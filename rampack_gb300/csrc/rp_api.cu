@@ -58,6 +58,9 @@ cudaError_t launch_score_partners(const DevState &s, const GridDev &g, const flo
                                   int mode, float inv_range, int32_t *partners, cudaStream_t st);
 cudaError_t launch_rot_table(double *out64, float *out32, uint32_t count, uint64_t seed, uint64_t counter, float step,
                              cudaStream_t st);
+cudaError_t launch_try_single(const SingleArgs &a, cudaStream_t st);
+cudaError_t launch_commit_single(const DevState &s, SingleTry *t, uint8_t *disp_flag, int32_t *disp_list, int slot,
+                                 cudaStream_t st);
 
 namespace {
 
@@ -242,6 +245,18 @@ struct Handle {
     unsigned long long *pair_count = nullptr;
     int64_t pair_cap = 0;
     int pair_every = 0;
+    // unrestricted single moves (rp_try_move / rp_accept_move): the tried state on the
+    // device, and the particles moved by single moves since the cell grid was built (the
+    // grid is then current for every other particle: grid_patched)
+    SingleTry *d_try = nullptr;
+    bool try_valid = false;
+    int32_t try_particle = -1;
+    int32_t *d_disp_list = nullptr;
+    uint8_t *d_disp_flag = nullptr;
+    std::vector<int32_t> disp_host;
+    std::vector<uint8_t> disp_flag_host;
+    bool grid_patched = false;
+    static constexpr int DISP_CAP = 4096;  // moved particles before the grid is rebuilt
 };
 
 // One group of kernel launches of a handle or a batch: counted, and bracketed by CUDA events
@@ -594,8 +609,17 @@ int rebuild(Handle *h, int gi, int pi) {
     DevState s = dev_state(h);
     h->gcur = saved_g;
     h->pcur = saved_p;
-    Group grp(h, RP_KERNEL_REBUILD, 6);
-    RP_CUDA(h, launch_rebuild(s, h->grid[gi].d, h->block_sums, h->stream));
+    {
+        Group grp(h, RP_KERNEL_REBUILD, 6);
+        RP_CUDA(h, launch_rebuild(s, h->grid[gi].d, h->block_sums, h->stream));
+    }
+    // a grid built from the current positions lists every particle where it is
+    if (!h->disp_host.empty()) {
+        RP_CUDA(h, cudaMemsetAsync(h->d_disp_flag, 0, static_cast<size_t>(h->n), h->stream));
+        for (int32_t p : h->disp_host) h->disp_flag_host[p] = 0;
+        h->disp_host.clear();
+    }
+    h->grid_patched = false;
     return RP_OK;
 }
 
@@ -1083,6 +1107,9 @@ int rp_destroy(void *handle) {
     cudaFree(h->count_out);
     cudaFree(h->cq_buf);
     cudaFree(h->cq_count);
+    cudaFree(h->d_try);
+    cudaFree(h->d_disp_list);
+    cudaFree(h->d_disp_flag);
     cudaFree(h->flag);
     cudaFree(h->overflow);
     cudaFree(h->overflow_count);
@@ -1112,6 +1139,7 @@ int rp_upload_state(void *handle, const double *pos, const double *rot, const do
     Handle *h = static_cast<Handle *>(handle);
     if (!h || !pos || !rot || !box9) return fail(h, RP_ERR_ARG, "null argument");
     RP_CUDA(h, cudaSetDevice(h->device));
+    h->try_valid = false;
     double inv[9];
     if (det3(box9) == 0) return fail(h, RP_ERR_ARG, "box volume is zero");
     inverse3(box9, inv);
@@ -1293,6 +1321,7 @@ int rp_run_moves(void *handle, const rp_move *moves, int64_t n, uint8_t *out_cod
     if (n <= 0) return RP_OK;
     if (n > (1ll << 31) - 1) return fail(h, RP_ERR_ARG, "too many moves");
     RP_CUDA(h, cudaSetDevice(h->device));
+    h->try_valid = false;
     {
         int rg = ensure_grid(h);  // an upload defers the grid
         if (rg) return rg;
@@ -1391,6 +1420,7 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
         types = SWEEP_ROTOTRANSLATION;
     }
     RP_CUDA(h, cudaSetDevice(h->device));
+    h->try_valid = false;
     // random grid origin and phase order from the Philox stream of this sweep
     u4 r = philox(u4{0x5eedu, 0x9e37u, static_cast<uint32_t>(p->counter), static_cast<uint32_t>(p->counter >> 32)},
                   static_cast<uint32_t>(p->seed), static_cast<uint32_t>(p->seed >> 32));
@@ -1542,6 +1572,7 @@ int rp_try_scaling(void *handle, const double *new_box9, double *dE) {
     if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
     if (det3(new_box9) == 0 || volume_of(new_box9) == 0) return fail(h, RP_ERR_ARG, "box volume is zero");
     RP_CUDA(h, cudaSetDevice(h->device));
+    h->try_valid = false;
     {
         int rg = ensure_grid(h);  // an upload defers the grid
         if (rg) return rg;
@@ -1615,6 +1646,7 @@ int rp_revert_scaling(void *handle) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h) return RP_ERR_ARG;
     if (!h->can_revert) return fail(h, RP_ERR_STATE, "nothing to revert");
+    h->try_valid = false;
     std::memcpy(h->box, h->saved_box, sizeof(h->box));
     std::memcpy(h->inv, h->saved_inv, sizeof(h->inv));
     h->pcur = 1 - h->pcur;
@@ -1626,6 +1658,95 @@ int rp_revert_scaling(void *handle) {
                                    h->stream));
         RP_CUDA(h, cudaStreamSynchronize(h->stream));
     }
+    return RP_OK;
+}
+
+// Packing::tryTranslation / tryRotation / tryMove without an ActiveDomain (core/Packing.cpp:84-164).
+int rp_try_move(void *handle, const rp_move *move, const double *domain6, double *dE) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !move || !dE) return fail(h, RP_ERR_ARG, "null argument");
+    if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
+    if (h->batch_member) return fail(h, RP_ERR_UNSUPPORTED, "single moves on a batch replica");
+    if (move->type < RP_MOVE_TRANSLATION || move->type > RP_MOVE_ROTOTRANSLATION)
+        return fail(h, RP_ERR_ARG, "unknown move type");
+    if (move->particle < 0 || move->particle >= h->n) return fail(h, RP_ERR_ARG, "particle index out of range");
+    RP_CUDA(h, cudaSetDevice(h->device));
+    h->try_valid = false;
+    if (!h->d_try) {
+        RP_CUDA(h, cudaMalloc(&h->d_try, sizeof(SingleTry)));
+        RP_CUDA(h, cudaMalloc(&h->d_disp_list, sizeof(int32_t) * Handle::DISP_CAP));
+        RP_CUDA(h, cudaMalloc(&h->d_disp_flag, static_cast<size_t>(h->n)));
+        RP_CUDA(h, cudaMemsetAsync(h->d_disp_flag, 0, static_cast<size_t>(h->n), h->stream));
+        h->disp_flag_host.assign(static_cast<size_t>(h->n), 0);
+        h->disp_host.clear();
+    }
+    // the grid serves single moves while only particles moved by single moves are out of
+    // place (and few enough of them); otherwise it is rebuilt first
+    if (h->grid_stale && !(h->grid_patched && static_cast<int>(h->disp_host.size()) < Handle::DISP_CAP)) {
+        h->grid_patched = false;
+        int rg = ensure_grid(h);
+        if (rg) return rg;
+    }
+    SingleArgs a{};
+    a.s = dev_state(h);
+    a.g = h->grid[h->gcur].d;
+    a.m = *move;
+    a.out = h->d_try;
+    a.disp_list = h->d_disp_list;
+    a.disp_flag = h->d_disp_flag;
+    a.ndisp = static_cast<int>(h->disp_host.size());
+    // FP32 pre-filter of a separation at one image: the interaction range (body range for
+    // multi-centre bodies) plus a margin far above the FP32 rounding of coordinates of the box's size
+    double pmax = 0;
+    for (int i = 0; i < 3; i++)
+        pmax = std::max(pmax, std::fabs(h->box[3 * i]) + std::fabs(h->box[3 * i + 1]) + std::fabs(h->box[3 * i + 2]));
+    const double reach = h->range * (1.0 + 1e-3) + 1e-4 * (pmax + h->range);
+    a.reach2 = static_cast<float>(reach * reach);
+    for (int i = 0; i < 9; i++) a.box32[i] = static_cast<float>(h->box[i]);
+    if (domain6) {
+        a.has_domain = 1;
+        for (int d = 0; d < 3; d++) {
+            a.dom_lo[d] = domain6[d];
+            a.dom_hi[d] = domain6[3 + d];
+        }
+    }
+    {
+        Group grp(h, RP_KERNEL_SINGLE, 1);
+        RP_CUDA(h, launch_try_single(a, h->stream));
+    }
+    double e = 0;
+    RP_CUDA(h, cudaMemcpyAsync(&e, &h->d_try->dE, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    int rc = check_status(h);  // synchronises
+    if (rc) return rc;
+    *dE = e;
+    h->try_valid = true;
+    h->try_particle = move->particle;
+    return RP_OK;
+}
+
+// Packing::acceptTranslation / acceptRotation / acceptMove (core/Packing.cpp:234-302).
+int rp_accept_move(void *handle) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h) return RP_ERR_ARG;
+    if (!h->try_valid) return fail(h, RP_ERR_STATE, "no tried move to accept");
+    RP_CUDA(h, cudaSetDevice(h->device));
+    const int32_t pid = h->try_particle;
+    int slot = -1;
+    if (!h->disp_flag_host[pid]) {
+        slot = static_cast<int>(h->disp_host.size());
+        h->disp_host.push_back(pid);
+        h->disp_flag_host[pid] = 1;
+    }
+    {
+        Group grp(h, RP_KERNEL_SINGLE, 1);
+        RP_CUDA(h, launch_commit_single(dev_state(h), h->d_try, h->d_disp_flag, h->d_disp_list, slot, h->stream));
+    }
+    h->try_valid = false;
+    // the sweeps, recounts and box moves rebuild the grid (and the FP32 mirror) first
+    h->grid_stale = true;
+    h->grid_patched = true;
+    h->log_valid = false;
+    h->can_revert = false;
     return RP_OK;
 }
 
@@ -1743,6 +1864,7 @@ int rp_set_counting(void *handle, int on) {
     if (!h) return RP_ERR_ARG;
     if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
     RP_CUDA(h, cudaSetDevice(h->device));
+    h->try_valid = false;
     {
         int rg = ensure_grid(h);  // an upload defers the grid
         if (rg) return rg;
@@ -1780,6 +1902,7 @@ int rp_renormalize_orientations(void *handle, int allow_overlaps, int64_t *rejec
     if (!h || !rejected) return fail(h, RP_ERR_ARG, "null argument");
     if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
     RP_CUDA(h, cudaSetDevice(h->device));
+    h->try_valid = false;
     {
         int rg = ensure_grid(h);  // an upload defers the grid
         if (rg) return rg;
@@ -2036,6 +2159,7 @@ int rp_set_walls(void *handle, int32_t mask) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h || mask < 0 || mask > 7) return fail(h, RP_ERR_ARG, "wall mask outside 0..7");
     h->walls = mask;
+    h->try_valid = false;
     return RP_OK;
 }
 

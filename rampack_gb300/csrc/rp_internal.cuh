@@ -229,6 +229,34 @@ struct SweepArgs {
     float inv_range;
 };
 
+// The state a single unrestricted move tried (rp_try_move), kept on the device until the
+// move is accepted (rp_accept_move) or another one is tried: the reference's temp shape
+// slot (core/Packing.cpp:86-93) with its interaction centres (:357-361, :1041-1047).
+struct SingleTry {
+    double pos[3], rot[9];
+    double cen[3 * RP_MAX_CENTRES], abs[3 * RP_MAX_CENTRES];
+    double dE;
+    int32_t particle, type, delta, valid;
+    int32_t outside, pad;   // rejected by the ActiveDomain before any overlap test
+};
+
+// Arguments of one single-move test: the mover's candidates are the particles listed in the
+// 27 grid cells around its position (the grid is current except for the particles moved by
+// single moves since it was built, which are skipped there and tested from `disp_list`).
+struct SingleArgs {
+    DevState s;
+    GridDev g;
+    rp_move m;
+    SingleTry *out;
+    const int32_t *disp_list;
+    const uint8_t *disp_flag;
+    int ndisp;
+    float reach2;       // FP32 pre-filter of a body separation at one image: reach^2
+    float box32[9];     // the box in FP32 (the images' translations in the pre-filter)
+    int has_domain;     // an ActiveDomain: relative bounds lo[3], hi[3] (ActiveDomain::RegionBounds)
+    double dom_lo[3], dom_hi[3];
+};
+
 // One replica of a batched launch (rp_batch_*): its sweep arguments, this sweep's phase
 // order, and its box move when the batch rescales it.  Particles, cells and sweep items of
 // all replicas are numbered consecutively; the prefix offsets live in separate compact

@@ -2,14 +2,20 @@
 // rampack_gb300 (include/rampack_gb300.h), for a C++ caller such as rampack's Simulation.
 //
 // Header-only; link against librampack_gb300.so.  Method names, argument meaning, the
-// energy encoding (0 or +inf; -inf only in overlap counting) and the error behaviour (a
-// failing call throws std::runtime_error, which rampack's callers treat like its own
-// PreconditionException) follow Packing.  Differences, stated where they apply:
-//  * every single move runs with the particle's current grid cell as its ActiveDomain
-//    (the engine has no unrestricted single-move path);
-//  * acceptTranslation/acceptRotation/acceptMove re-run the last tried move with a
-//    Metropolis uniform of 0 (always accepted), which commits the same temp state the
-//    reference's acceptMove commits (core/Packing.cpp:278-302);
+// energy encoding (0 or +inf; -inf only in overlap counting) and the error behaviour follow
+// Packing.  BasicGpuPacking is a template over the caller's types, so that the reference can
+// pass its own objects unchanged:
+//  * Vector: a position or translation with operator[] (Vector<3>, or std::array<double, 3>);
+//  * Matrix: an orientation, rotation or box with operator()(i, j) (Matrix<3, 3>) or a
+//    row-major std::array<double, 9>;
+//  * Domain: an ActiveDomain with getBoundsForCoordinate(i).beg / .end
+//    (core/ActiveDomain.h:19-53), passed as std::optional like Packing::tryTranslation's;
+//  * Raise: how a failing call reports, Raise::raise(message, function, line) (the reference
+//    side throws its PreconditionException; the default throws std::runtime_error).
+// GpuPacking is the instantiation over std::array types.
+//  * tryTranslation / tryRotation / tryMove evaluate one move on the device and keep the
+//    tried state there; acceptTranslation / acceptRotation / acceptMove commit it
+//    (rp_try_move / rp_accept_move, no grid rebuild per move);
 //  * performMoves is the batched entry that replaces Simulation::performMovesWithDomainDivision
 //    (core/Simulation.cpp:396-445): one device sweep of 2N moves.
 #pragma once
@@ -19,8 +25,10 @@
 #include <cstdint>
 #include <limits>
 #include <map>
+#include <optional>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/rampack_gb300.h"
@@ -30,18 +38,63 @@ namespace rampack_gb300 {
 using Vec3 = std::array<double, 3>;
 using Mat3 = std::array<double, 9>;  // row-major Matrix<3, 3>
 
-class GpuPacking {
+namespace detail {
+// element (i, j) of a Matrix<3, 3>-like object or of a row-major array of 9
+template <class M>
+double mat_at(const M &m, int i, int j) {
+    if constexpr (std::is_invocable_v<const M &, std::size_t, std::size_t>)
+        return static_cast<double>(m(static_cast<std::size_t>(i), static_cast<std::size_t>(j)));
+    else
+        return static_cast<double>(m[static_cast<std::size_t>(3 * i + j)]);
+}
+template <class V>
+double vec_at(const V &v, int i) {
+    return static_cast<double>(v[static_cast<std::size_t>(i)]);
+}
+}  // namespace detail
+
+// ActiveDomain stand-in with the reference's accessor (relative bounds per coordinate).
+struct DomainBounds {
+    struct RegionBounds {
+        double beg{}, end{};
+    };
+    std::array<RegionBounds, 3> bounds{};
+    const RegionBounds &getBoundsForCoordinate(std::size_t i) const { return bounds[i]; }
+};
+
+// The default error report: std::runtime_error with the library's message.
+struct ThrowRuntimeError {
+    [[noreturn]] static void raise(const std::string &what, const char *, int) { throw std::runtime_error(what); }
+};
+
+// A particle's state as the engine stores it: position and row-major orientation.
+struct Shape {
+    Vec3 position{};
+    Mat3 orientation{1, 0, 0, 0, 1, 0, 0, 0, 1};
+};
+
+// One sphere or spherocylinder of a multi-centre body: PolysphereTraits::SphereData
+// (position, radius) or PolyspherocylinderTraits::SpherocylinderData (position, half axis,
+// radius), in the body frame.
+struct Centre {
+    Vec3 position{};
+    double radius = 0;
+    Vec3 half_axis{};
+};
+
+template <class Vector = Vec3, class Matrix = Mat3, class Domain = DomainBounds, class Raise = ThrowRuntimeError>
+class BasicGpuPacking {
 public:
     using Vec3 = rampack_gb300::Vec3;
     using Mat3 = rampack_gb300::Mat3;
-    struct Shape {
-        Vec3 position{};
-        Mat3 orientation{1, 0, 0, 0, 1, 0, 0, 0, 1};
-    };
+    using Shape = rampack_gb300::Shape;
+    using Centre = rampack_gb300::Centre;
+    static constexpr double INF = std::numeric_limits<double>::infinity();
 
     // Packing(box, shapes, bc, interaction, moveThreads, scalingThreads) for hard spheres
     // (length < 0) or spherocylinders of the given length.
-    GpuPacking(const Mat3 &box, const std::vector<Shape> &shapes, double radius, double length = -1, int device = 0) {
+    BasicGpuPacking(const Mat3 &box, const std::vector<Shape> &shapes, double radius, double length = -1,
+                    int device = 0) {
         rp_shape_desc d{};
         d.kind = length < 0 ? RP_SHAPE_SPHERE : RP_SHAPE_SPHEROCYLINDER;
         d.radius = radius;
@@ -50,19 +103,10 @@ public:
         n_ = shapes.size();
         reset(shapes, box);
     }
-    // One sphere or spherocylinder of a multi-centre body: PolysphereTraits::SphereData
-    // (position, radius) or PolyspherocylinderTraits::SpherocylinderData (position, half axis,
-    // radius), in the body frame.
-    struct Centre {
-        Vec3 position{};
-        double radius = 0;
-        Vec3 half_axis{};
-    };
-
     // Packing(box, shapes, bc, interaction, ...) for polyspheres (PolysphereTraits) or, with
     // `spherocylinders`, polyspherocylinders (PolyspherocylinderTraits).
-    GpuPacking(const Mat3 &box, const std::vector<Shape> &shapes, const std::vector<Centre> &centres,
-               bool spherocylinders, int device = 0) {
+    BasicGpuPacking(const Mat3 &box, const std::vector<Shape> &shapes, const std::vector<Centre> &centres,
+                    bool spherocylinders, int device = 0) {
         std::vector<double> pos, half, radii;
         for (const auto &c : centres) {
             pos.insert(pos.end(), c.position.begin(), c.position.end());
@@ -79,9 +123,9 @@ public:
         n_ = shapes.size();
         reset(shapes, box);
     }
-    GpuPacking(const GpuPacking &) = delete;
-    GpuPacking &operator=(const GpuPacking &) = delete;
-    ~GpuPacking() {
+    BasicGpuPacking(const BasicGpuPacking &) = delete;
+    BasicGpuPacking &operator=(const BasicGpuPacking &) = delete;
+    ~BasicGpuPacking() {
         if (h_) rp_destroy(h_);
     }
 
@@ -94,7 +138,6 @@ public:
         }
         check(rp_upload_state(h_, pos.data(), rot.data(), box.data()), "rp_upload_state");
         box_ = box;
-        last_ = {};
     }
 
     std::size_t size() const { return n_; }
@@ -112,15 +155,23 @@ public:
         return out;
     }
 
-    // Packing::tryTranslation / tryRotation / tryMove (core/Packing.cpp:84-164)
-    double tryTranslation(std::size_t idx, const Vec3 &t) { return tryAny(RP_MOVE_TRANSLATION, idx, t, identity()); }
-    double tryRotation(std::size_t idx, const Mat3 &r) { return tryAny(RP_MOVE_ROTATION, idx, Vec3{}, r); }
-    double tryMove(std::size_t idx, const Vec3 &t, const Mat3 &r) { return tryAny(RP_MOVE_ROTOTRANSLATION, idx, t, r); }
+    // Packing::tryTranslation / tryRotation / tryMove (core/Packing.cpp:84-164); with no
+    // domain (std::nullopt) the reference's serial path, with one the move must keep the
+    // particle inside it
+    double tryTranslation(std::size_t idx, const Vector &t, const std::optional<Domain> &domain = std::nullopt) {
+        return tryAny(RP_MOVE_TRANSLATION, idx, &t, nullptr, domain);
+    }
+    double tryRotation(std::size_t idx, const Matrix &r) {
+        return tryAny(RP_MOVE_ROTATION, idx, nullptr, &r, std::nullopt);
+    }
+    double tryMove(std::size_t idx, const Vector &t, const Matrix &r, const std::optional<Domain> &domain = std::nullopt) {
+        return tryAny(RP_MOVE_ROTOTRANSLATION, idx, &t, &r, domain);
+    }
 
     // Packing::acceptTranslation / acceptRotation / acceptMove (core/Packing.cpp:234-302)
-    void acceptTranslation() { commit(); }
-    void acceptRotation() { commit(); }
-    void acceptMove() { commit(); }
+    void acceptTranslation() { check(rp_accept_move(h_), "rp_accept_move", __LINE__); }
+    void acceptRotation() { check(rp_accept_move(h_), "rp_accept_move", __LINE__); }
+    void acceptMove() { check(rp_accept_move(h_), "rp_accept_move", __LINE__); }
 
     // Packing::countTotalOverlaps (core/Packing.cpp:519-559)
     std::size_t countTotalOverlaps(bool earlyExit = false) const {
@@ -170,8 +221,8 @@ public:
         rp_ramsnap_info(snap, &n, &naux);
         if (static_cast<std::size_t>(n) != n_) {
             rp_ramsnap_free(snap);
-            throw std::runtime_error("restore: the file holds " + std::to_string(n) + " shapes, the packing " +
-                                     std::to_string(n_));
+            Raise::raise("restore: the file holds " + std::to_string(n) + " shapes, the packing " + std::to_string(n_),
+                         "restore", __LINE__);
         }
         std::vector<double> pos(3 * n_), rot(9 * n_);
         Mat3 box{};
@@ -207,49 +258,36 @@ private:
     void *h_ = nullptr;
     std::size_t n_ = 0;
     Mat3 box_{}, prev_box_{};
-    rp_move last_{};
 
-    static Mat3 identity() { return Mat3{1, 0, 0, 0, 1, 0, 0, 0, 1}; }
-
-    void check(int rc, const char *what) const {
-        if (rc != RP_OK) throw std::runtime_error(std::string(what) + ": " + rp_last_error(h_));
+    void check(int rc, const char *what, int line = 0) const {
+        if (rc != RP_OK) Raise::raise(std::string(what) + ": " + rp_last_error(h_), what, line);
     }
     static void checkIo(int rc, const char *what) {
-        if (rc != RP_OK) throw std::runtime_error(std::string(what) + ": " + rp_io_last_error());
+        if (rc != RP_OK) Raise::raise(std::string(what) + ": " + rp_io_last_error(), what, 0);
     }
 
-    int cellOf(std::size_t idx) const {
-        std::vector<int32_t> cells(n_);
-        check(rp_get_grid(h_, nullptr, cells.data(), nullptr), "rp_get_grid");
-        return cells[idx];
-    }
-
-    double tryAny(int type, std::size_t idx, const Vec3 &t, const Mat3 &r) {
-        if (idx >= n_) throw std::runtime_error("particle index out of range");
+    double tryAny(int type, std::size_t idx, const Vector *t, const Matrix *r, const std::optional<Domain> &domain) {
+        if (idx >= n_) Raise::raise("particle index out of range", "tryMove", __LINE__);
         rp_move m{};
         m.particle = static_cast<int32_t>(idx);
         m.type = type;
-        m.domain = cellOf(idx);
-        for (int k = 0; k < 3; k++) m.translation[k] = t[k];
-        for (int k = 0; k < 9; k++) m.rotation[k] = r[k];
-        m.uniform = 2.0;  // > 1: evaluated, never accepted
-        uint8_t code = 0;
-        check(rp_run_moves(h_, &m, 1, &code), "rp_run_moves");
-        last_ = m;
-        switch (code & 3) {
-            case 0: return 0.0;
-            case 3: return -std::numeric_limits<double>::infinity();
-            default: return std::numeric_limits<double>::infinity();
-        }
-    }
-
-    void commit() {
-        rp_move m = last_;
-        m.uniform = 0.0;  // u <= exp(-dE/T) holds for every dE: the temp state is committed
-        uint8_t code = 0;
-        check(rp_run_moves(h_, &m, 1, &code), "rp_run_moves");
+        m.domain = -1;
+        for (int k = 0; k < 3; k++) m.translation[k] = t ? detail::vec_at(*t, k) : 0.0;
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) m.rotation[3 * i + j] = r ? detail::mat_at(*r, i, j) : (i == j ? 1.0 : 0.0);
+        double bounds[6];
+        if (domain)
+            for (int k = 0; k < 3; k++) {
+                bounds[k] = domain->getBoundsForCoordinate(static_cast<std::size_t>(k)).beg;
+                bounds[3 + k] = domain->getBoundsForCoordinate(static_cast<std::size_t>(k)).end;
+            }
+        double dE = 0;
+        check(rp_try_move(h_, &m, domain ? bounds : nullptr, &dE), "rp_try_move", __LINE__);
+        return dE;
     }
 };
+
+using GpuPacking = BasicGpuPacking<>;
 
 // RamtrjRecorder (core/io/RamtrjRecorder.cpp): a RAMTRJ trajectory; recordSnapshot takes a
 // GpuPacking's state in order with its moves and returns while the file is written.
@@ -265,7 +303,8 @@ public:
     ~RamtrjRecorder() {
         if (r_) rp_ramtrj_close(r_);
     }
-    void recordSnapshot(const GpuPacking &packing, std::size_t cycle) {
+    template <class Packing>
+    void recordSnapshot(const Packing &packing, std::size_t cycle) {
         if (rp_ramtrj_record(r_, packing.handle(), static_cast<int64_t>(cycle)) != RP_OK)
             throw std::runtime_error(std::string("rp_ramtrj_record: ") + rp_io_last_error());
     }

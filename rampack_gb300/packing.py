@@ -181,6 +181,26 @@ class GpuPacking:
                                           codes.ctypes.data_as(C.c_void_p)))
         return codes
 
+    def try_move(self, particle: int, type_: int, translation=(0.0, 0.0, 0.0), rotation=None, domain=None) -> float:
+        """Packing::tryTranslation / tryRotation / tryMove (rp_try_move), with no ActiveDomain or
+        with `domain` = its relative bounds (lo[3], hi[3]): the move's energy (0 or +inf; -inf,
+        0 or +inf in overlap counting); the tried state waits for accept_move."""
+        m = np.zeros(1, dtype=MOVE_DTYPE)
+        m["particle"] = particle
+        m["type"] = type_
+        m["domain"] = -1
+        m["translation"] = np.asarray(translation, dtype=np.float64).reshape(3)
+        m["rotation"] = np.eye(3).reshape(9) if rotation is None else np.asarray(rotation, dtype=np.float64).reshape(9)
+        de = C.c_double()
+        dom = None if domain is None else np.ascontiguousarray(domain, dtype=np.float64).reshape(6)
+        self._check(self.lib.rp_try_move(self.h, m.ctypes.data_as(C.c_void_p), None if dom is None else dptr(dom),
+                                         C.byref(de)))
+        return de.value
+
+    def accept_move(self):
+        """Packing::acceptTranslation / acceptRotation / acceptMove (rp_accept_move)."""
+        self._check(self.lib.rp_accept_move(self.h))
+
     def sweep(self, translation_step: float, rotation_step: float, seed: int, counter: int,
               log: bool = False, fp64_only: bool = False, stats: bool = True, rototranslation: bool = False):
         """One device sweep: 2N moves (translations and rotations), or N rototranslations."""

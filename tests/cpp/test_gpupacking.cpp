@@ -11,6 +11,32 @@
 
 using rampack_gb300::GpuPacking;
 
+// Stand-ins with the reference's accessors: Vector<3> (operator[]), Matrix<3, 3>
+// (operator()(i, j)), ActiveDomain (getBoundsForCoordinate) and an exception type that is not
+// std::runtime_error, as the reference side instantiates BasicGpuPacking.
+struct RefVector {
+    double v[3];
+    double operator[](std::size_t i) const { return v[i]; }
+};
+struct RefMatrix {
+    double m[3][3];
+    double operator()(std::size_t i, std::size_t j) const { return m[i][j]; }
+};
+struct RefDomain {
+    struct RegionBounds {
+        double beg, end;
+    };
+    RegionBounds b[3];
+    const RegionBounds &getBoundsForCoordinate(std::size_t i) const { return b[i]; }
+};
+struct RefPrecondition {
+    std::string what;
+};
+struct RaiseRef {
+    [[noreturn]] static void raise(const std::string &what, const char *, int) { throw RefPrecondition{what}; }
+};
+using RefPacking = rampack_gb300::BasicGpuPacking<RefVector, RefMatrix, RefDomain, RaiseRef>;
+
 static int failures = 0;
 #define CHECK(cond)                                                        \
     do {                                                                   \
@@ -61,6 +87,42 @@ int main(int argc, char **argv) {
         pk.acceptRotation();
         s = pk.getShapes();
         CHECK(s[0].orientation[1] == -1.0 && s[0].position[0] == 0.5);
+    }
+    {
+        // the reference's own types; a translation across a cell face with no ActiveDomain
+        // (the reference's serial path) is evaluated as the reference evaluates it, and the
+        // same translation with a domain it leaves is rejected before any overlap test
+        RefPacking pk(box, three(), 0.25);
+        CHECK(pk.tryTranslation(0, RefVector{{0.0, 0.0, 1.3}}) == 0);
+        pk.acceptTranslation();
+        auto s = pk.getShapes();
+        CHECK(s[0].position[2] == 1.8);
+        RefDomain dom{{{0.0, 0.5}, {0.0, 0.5}, {0.0, 0.5}}};
+        CHECK(pk.tryTranslation(1, RefVector{{0.0, 0.0, 0.1}}, dom) == inf);  // x = 4.5 is outside
+        CHECK(pk.tryMove(0, RefVector{{0.01, 0.0, 0.0}}, RefMatrix{{{0, -1, 0}, {1, 0, 0}, {0, 0, 1}}}, dom) == 0);
+        pk.acceptMove();
+        s = pk.getShapes();
+        CHECK(s[0].position[0] == 0.51 && s[0].orientation[1] == -1.0);
+        // the tried move puts two spheres 0.29 apart (r = 0.25): an overlap
+        CHECK(pk.tryTranslation(2, RefVector{{-1.7, -2.0, -2.2}}) == inf);
+        bool raised = false;
+        try {
+            pk.tryTranslation(3, RefVector{{0, 0, 0}});
+        } catch (const RefPrecondition &e) {
+            raised = e.what.find("out of range") != std::string::npos;
+        }
+        CHECK(raised);
+        CHECK(pk.tryTranslation(2, RefVector{{0.1, 0.0, 0.0}}) == 0);
+        pk.acceptTranslation();
+        raised = false;
+        try {
+            pk.acceptTranslation();  // nothing left to accept
+        } catch (const RefPrecondition &) {
+            raised = true;
+        }
+        CHECK(raised);
+        s = pk.getShapes();
+        CHECK(s[2].position[0] == 2.6 && s[2].position[2] == 4.0);
     }
     {
         // spherocylinders: a device sweep keeps the packing overlap-free

@@ -59,7 +59,8 @@ def test_config_hs_1000_density_matches_the_oracle(oracle, engine):
     try:
         assert st["cycles"] == SKIP + CYCLES
         assert st["box_moves"] == SKIP + CYCLES
-        assert 0.05 < st["accepted_box_moves"] / st["box_moves"] < 0.95
+        # ln V steps of 0.01 at rho ~ 0.9: about 2 % of the box moves are accepted
+        assert 0.005 < st["accepted_box_moves"] / st["box_moves"] < 0.5
         assert g.count_total_overlaps(False) == 0
     finally:
         g.close()
