@@ -2173,8 +2173,6 @@ int rp_set_staging_filter(void *handle, int32_t mode) {
 int rp_set_ordering(void *handle, int32_t mode, int32_t every) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h || mode < RP_ORDER_OFF || mode > RP_ORDER_DISTANCE || every <= 0) return fail(h, RP_ERR_ARG, "bad argument");
-    if (mode != RP_ORDER_OFF && h->shape.kind == RP_SHAPE_POLYSPHERE)
-        return fail(h, RP_ERR_UNSUPPORTED, "test ordering is built for spheres and spherocylinders");
     h->order_mode = mode;
     h->order_every = every;
     h->partners_valid = false;

@@ -358,7 +358,7 @@ cudaError_t launch_sweep(const SweepArgs &a, bool list, int nwarps, cudaStream_t
     const bool count = a.s.counting != 0;
     // rototranslation sweeps have their own plain scan (no learned pre-test, no pair log)
     const bool rt = !list && !count && a.types == SWEEP_ROTOTRANSLATION;
-    const bool learn = !list && !count && !rt && a.s.kind != 2 && (a.partners != nullptr || a.pair_every > 0);
+    const bool learn = !list && !count && !rt && (a.partners != nullptr || a.pair_every > 0);
     size_t smem = sweep_smem_per_warp(a.s.kind, a.cap, learn, a.s.ncen) * wpb;
     unsigned blocks = (unsigned)((nwarps + wpb - 1) / wpb);
     const int th = wpb * 32;
@@ -366,6 +366,7 @@ cudaError_t launch_sweep(const SweepArgs &a, bool list, int nwarps, cudaStream_t
         if (count) return list ? launch_sweep_t<2, true, 2>(a, blocks, th, smem, st)
                                : launch_sweep_t<2, false, 2>(a, blocks, th, smem, st);
         if (list) return launch_sweep_t<2, true, 0>(a, blocks, th, smem, st);
+        if (learn) return launch_sweep_t<2, false, 1>(a, blocks, th, smem, st);
         return rt ? launch_sweep_t<2, false, 3>(a, blocks, th, smem, st)
                   : launch_sweep_t<2, false, 0>(a, blocks, th, smem, st);
     }

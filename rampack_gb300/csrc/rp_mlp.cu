@@ -335,12 +335,17 @@ __global__ void __launch_bounds__(SCORE_WARPS * 32) k_score_partners(DevState S,
         }
     }
     __syncwarp();
-    const float thr = S.kind == 1 ? S.fc.far_hi : S.fc.sphere_hi * 4.0f;
+    // in reach: spherocylinders and multi-centre bodies within their interaction range,
+    // spheres within twice theirs
+    const float thr = S.kind == 0 ? S.fc.sphere_hi * 4.0f : S.fc.far_hi;
     for (int i = 0; i < occ; i++) {
         const float4 pi = spos[wib][i];
         const int pid = __float_as_int(pi.w);
         const float4 ai4 = sax[wib][i];
         const float3 ai = make_float3(ai4.x, ai4.y, ai4.z);
+        float ri[9];
+        if (S.kind == 2)
+            for (int e = 0; e < 9; e++) ri[e] = (float)S.rot64[9 * (size_t)pid + e];
         // in-range candidates
         int nl = 0;
         for (int b = 0; b < total; b += 32) {
@@ -369,9 +374,17 @@ __global__ void __launch_bounds__(SCORE_WARPS * 32) k_score_partners(DevState S,
                     if (li < nl) {
                         int k = slist[wib][li];
                         float4 q = spos[wib][k];
-                        float4 aj = sax[wib][k];
-                        mlp_features(make_float3(q.x - pi.x, q.y - pi.y, q.z - pi.z), ai,
-                                     make_float3(aj.x, aj.y, aj.z), inv_range, f);
+                        if (S.kind == 2) {
+                            // bent bodies: features of the whole orientations
+                            const double *oj = S.rot64 + 9 * (size_t)__float_as_int(q.w);
+                            float rj[9];
+                            for (int e = 0; e < 9; e++) rj[e] = (float)oj[e];
+                            mlp_features_body(make_float3(q.x - pi.x, q.y - pi.y, q.z - pi.z), ri, rj, inv_range, f);
+                        } else {
+                            float4 aj = sax[wib][k];
+                            mlp_features(make_float3(q.x - pi.x, q.y - pi.y, q.z - pi.z), ai,
+                                         make_float3(aj.x, aj.y, aj.z), inv_range, f);
+                        }
                     } else {
                         for (int c = 0; c < MLP_IN; c++) f[c] = 0.f;
                     }

@@ -115,6 +115,29 @@ __device__ __forceinline__ int classify(const FilterConsts &fc, float3 d, float3
     return cls;
 }
 
+// FP32 classification of one candidate body against the mover's moved FP32 centres (the
+// centre-pair stage of multi-centre bodies): dq = candidate body - mover body position,
+// cj its FP32 centres, wx the mover's, thr the centre-pair thresholds (lo block, then hi
+// block).  1 a certain overlap, 2 undecided (FP64), 0 none.
+__device__ __forceinline__ int poly_body_class(int K, const float4 *wx, const float *thr, float3 dq, const float4 *cj) {
+    int cls = 0;
+    for (int j = 0; j < K && cls != 1; j++) {
+        const float4 c = cj[j];
+        const float3 bj = make_float3(dq.x + c.x, dq.y + c.y, dq.z + c.z);
+        for (int a = 0; a < K; a++) {
+            const float4 m = wx[a];
+            const float3 d = make_float3(bj.x - m.x, bj.y - m.y, bj.z - m.z);
+            const float d2 = dot3f(d, d);
+            if (d2 < thr[a * MAX_CEN + j]) {
+                cls = 1;
+                break;
+            }
+            if (d2 <= thr[MAX_CEN * MAX_CEN + a * MAX_CEN + j]) cls = 2;
+        }
+    }
+    return cls;
+}
+
 // Image of candidate j relative to mover i, recovered from the FP32 separation dsep
 // (candidate minus mover, in the right image) and the FP64 positions: the integer box
 // translation m with p_j + box·m - p_i ≈ dsep.  Returns the index into the translation table.
@@ -498,12 +521,19 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                 if (k != 0xffff) {
                     const float4 q = cpos[k];
                     if (__float_as_int(q.w) != pid) {
-                        float3 aj = make_float3(0.f, 0.f, 1.f);
-                        if (KIND == 1) {
-                            const float4 a = cax[k];
-                            aj = make_float3(a.x, a.y, a.z);
+                        const float3 dq = make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z);
+                        if (KIND == 2) {
+                            // the partner body's centre pairs against the mover's moved centres
+                            if (d2_stage<2>(S.fc, dot3f(dq, dq)) == 3)
+                                cls = poly_body_class(S.ncen, wx, wthr, dq, G.mcen + (size_t)cslot[k] * S.ncen);
+                        } else {
+                            float3 aj = make_float3(0.f, 0.f, 1.f);
+                            if (KIND == 1) {
+                                const float4 a = cax[k];
+                                aj = make_float3(a.x, a.y, a.z);
+                            }
+                            cls = classify<KIND>(S.fc, dq, an, aj);
                         }
-                        cls = classify<KIND>(S.fc, make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z), an, aj);
                         tested = true;
                     }
                 }
@@ -562,21 +592,35 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                 if (i < nseg) {
                     k = qseg[i];
                     const float4 q = cpos[k];
-                    const float3 dq = make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z);
-                    const float4 *cj = G.mcen + (size_t)cslot[k] * K;
-                    for (int j = 0; j < K && cls != 1; j++) {
-                        const float4 c = cj[j];
-                        const float3 bj = make_float3(dq.x + c.x, dq.y + c.y, dq.z + c.z);
-                        for (int a = 0; a < K; a++) {
-                            const float4 m = wx[a];
-                            const float3 d = make_float3(bj.x - m.x, bj.y - m.y, bj.z - m.z);
-                            const float d2 = dot3f(d, d);
-                            if (d2 < wthr[a * MAX_CEN + j]) {
-                                cls = 1;
-                                break;
-                            }
-                            if (d2 <= wthr[MAX_CEN * MAX_CEN + a * MAX_CEN + j]) cls = 2;
-                        }
+                    cls = poly_body_class(K, wx, wthr, make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z),
+                                          G.mcen + (size_t)cslot[k] * K);
+                }
+                if (LEARN && A.pair_every > 0 && ((mi + cell) % A.pair_every) == 0) {
+                    // training data of the ranking network: the body pair as it was before
+                    // the move (whole orientations: the bodies are bent), labelled with the
+                    // certain outcome after it
+                    const bool rec = i < nseg && cls != 2;
+                    const unsigned bal = __ballot_sync(FULL, rec);
+                    unsigned long long base_idx = 0;
+                    if (lane == 0 && bal) base_idx = atomicAdd(A.pair_count, (unsigned long long)__popc(bal));
+                    base_idx = __shfl_sync(FULL, base_idx, 0);
+                    const unsigned long long idx = base_idx + __popc(bal & lt);
+                    float ri[9];
+                    for (int e = 0; e < 9; e++) ri[e] = (float)__shfl_sync(FULL, rot_own, e);
+                    if (rec && idx < A.pair_cap) {
+                        const float4 q = cpos[k];
+                        const double *oj = S.rot64 + 9 * (size_t)__float_as_int(q.w);
+                        float rj[9];
+                        for (int e = 0; e < 9; e++) rj[e] = (float)oj[e];
+                        float f[MLP_IN];
+                        mlp_features_body(make_float3(q.x - pcur.x, q.y - pcur.y, q.z - pcur.z), ri, rj, A.inv_range,
+                                          f);
+                        float4 *dst = reinterpret_cast<float4 *>(A.pair_feats + idx * MLP_IN);
+                        dst[0] = make_float4(f[0], f[1], f[2], f[3]);
+                        dst[1] = make_float4(f[4], f[5], f[6], f[7]);
+                        dst[2] = make_float4(f[8], f[9], f[10], f[11]);
+                        dst[3] = make_float4(f[12], f[13], f[14], f[15]);
+                        A.pair_labels[idx] = cls == 1 ? 1 : 0;
                     }
                 }
                 if (__ballot_sync(FULL, cls == 1)) {

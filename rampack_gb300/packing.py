@@ -292,6 +292,12 @@ class GpuPacking:
         self._check(self.lib.rp_pair_log_read(self.h, fptr(f), lab.ctypes.data_as(C.c_void_p), k, C.byref(cnt)))
         return f, lab
 
+    def pair_log_count(self) -> int:
+        """Pair outcomes held by the log (at most its capacity)."""
+        cnt = C.c_int64()
+        self._check(self.lib.rp_pair_log_read(self.h, None, None, 0, C.byref(cnt)))
+        return int(cnt.value)
+
     def pair_log_clear(self):
         self._check(self.lib.rp_pair_log_clear(self.h))
 

@@ -114,3 +114,57 @@ def test_config_hs_1000_logged_sweep_replays_on_the_oracle(oracle, engine):
             cpu.revert_scaling()
     finally:
         g.close()
+
+
+def test_config_bent_chains_learned_ordering(oracle, engine):
+    """The learned-ordering configuration's bent chains as stated: N = 10^5 chains of 5 spheres
+    (diameter 1, bond 0.6, 30 degrees between bonds) at packing fraction 0.45; the ranking
+    network (13 features, 64 x 64 hidden, BF16 weights, FP32 accumulation) trained on the
+    device on 10^7 pair outcomes the sweep itself logged; an ordered sweep leaves the state
+    bit-identical to the plain sweep's, and its log replays on the oracle move by move."""
+    from rampack_gb300 import _lib
+    from rampack_gb300.packing import GpuPacking
+    kind, prm, pos, rot, box = W.config_banana_1e5()
+    assert len(pos) == 100_000
+    with GpuPacking(kind, prm, pos, rot, box) as g:
+        for c in range(4):  # off the lattice
+            g.sweep(0.2, 0.2, seed=1, counter=c, stats=False)
+        start = g.state()
+        g.pair_log_enable(10_000_000, 1)
+        sweeps = 0
+        while g.pair_log_count() < 10_000_000:
+            g.sweep(0.2, 0.2, seed=2, counter=sweeps, stats=False)
+            sweeps += 1
+            assert sweeps <= 40
+        feats, labels = g.pair_log()
+        assert len(feats) == 10_000_000 and 0 < labels.mean() < 1
+        _, l0 = g.mlp_gradient(feats[:200_000], labels[:200_000])
+        g.mlp_train(epochs=2, batch=1024, lr=2e-3, seed=1)
+        _, l1 = g.mlp_gradient(feats[:200_000], labels[:200_000])
+        assert l1 < 0.8 * l0, (l0, l1)
+        g.pair_log_enable(0)
+        results = {}
+        for mode in (_lib.ORDER_OFF, _lib.ORDER_MLP):
+            g.upload(*start)
+            g.set_ordering(mode, every=4)
+            pairs = 0
+            for c in range(3):
+                st = g.sweep(0.2, 0.2, seed=3, counter=c)
+                pairs += st["pair_tests"]
+            results[mode] = (g.state(), pairs)
+        (p0, r0, _), pairs0 = results[_lib.ORDER_OFF]
+        (p1, r1, _), pairs1 = results[_lib.ORDER_MLP]
+        assert np.array_equal(p0, p1) and np.array_equal(r0, r1)
+        assert pairs1 < pairs0
+        # an ordered, logged sweep replays on the oracle
+        g.upload(*start)
+        cpu = po.CpuPacking("oracle", kind, prm, *start, threads=8)
+        g.set_ordering(_lib.ORDER_MLP, every=1)
+        g.sweep(0.2, 0.2, seed=7, counter=0, log=True)
+        moves, codes = g.sweep_log()
+        _, _, bounds = g.grid()
+        want, _ = cpu.replay(moves, bounds)
+        assert np.array_equal(codes, want), np.count_nonzero(codes != want)
+        gp, gr, _ = g.state()
+        cp, cr, _ = cpu.state()
+        assert np.array_equal(gp, cp) and np.array_equal(gr, cr)

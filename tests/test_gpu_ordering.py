@@ -152,3 +152,73 @@ def test_ordered_sweep_log_replays_on_oracle(oracle, engine):
         gp, gr, _ = g.state()
         cp, cr, _ = cpu.state()
         assert np.array_equal(gp, cp) and np.array_equal(gr, cr)
+
+
+# ---- multi-centre bodies (bent chains and bent rods) ----------------------------------
+def test_body_pair_log_and_training(engine):
+    """Pairs of bent chains logged by the sweep carry the body-frame features (unit axes of
+    the other body, |b|^2 and the squared separation across the primary axis consistent with
+    the separation) and both labels; training on them lowers the loss."""
+    cfg = systems.poly_dense()
+    with gpu_packing(cfg) as g:
+        f, lab = collect(g, 4)
+        assert len(f) > 1000
+        assert 0 < lab.mean() < 1
+        assert np.all(np.isfinite(f)) and np.all(f[:, 13:] == 0)
+        np.testing.assert_allclose(np.linalg.norm(f[:, 3:6], axis=1), 1, atol=1e-3)
+        np.testing.assert_allclose(np.linalg.norm(f[:, 6:9], axis=1), 1, atol=1e-3)
+        np.testing.assert_allclose(f[:, 9], (f[:, 0:3] ** 2).sum(1), rtol=1e-4, atol=1e-6)
+        np.testing.assert_allclose(f[:, 12], (f[:, 0:2] ** 2).sum(1), rtol=1e-4, atol=1e-6)
+        assert np.all(f[:, 9] < 1.5)  # within about one body reach before the move
+        _, l0 = g.mlp_gradient(f, lab)
+        g.mlp_train(epochs=10, batch=512, lr=2e-3, seed=1)
+        _, l2 = g.mlp_gradient(f, lab)
+        assert l2 < 0.8 * l0, (l0, l2)
+
+
+@pytest.mark.parametrize("name", ["poly_dense", "psc_bent"])
+def test_ordered_body_sweeps_leave_the_plain_state(engine, name):
+    cfg = systems.ALL[name]()
+    results = {}
+    for mode in (_lib.ORDER_OFF, _lib.ORDER_DISTANCE, _lib.ORDER_MLP):
+        with gpu_packing(cfg) as g:
+            if mode == _lib.ORDER_MLP:
+                collect(g, 3, seed=99)
+                g.mlp_train(epochs=8, batch=512, lr=2e-3, seed=2)
+                g.pair_log_enable(0)
+                g.upload(*cfg[2:])
+            g.set_ordering(mode, every=2)
+            acc = pairs = 0
+            for c in range(5):
+                st = g.sweep(0.2, 0.2, seed=31, counter=c)
+                acc += st["accepted"]
+                pairs += st["pair_tests"]
+            results[mode] = (g.state(), acc, pairs)
+    (p0, r0, b0), acc0, pairs0 = results[_lib.ORDER_OFF]
+    for mode in (_lib.ORDER_DISTANCE, _lib.ORDER_MLP):
+        (p, rr, b), acc, pairs = results[mode]
+        assert np.array_equal(p, p0) and np.array_equal(rr, r0), f"mode {mode}: state differs"
+        assert acc == acc0
+        assert pairs < pairs0, (mode, pairs, pairs0)
+
+
+@pytest.mark.parametrize("name", ["poly_dense", "psc_bent"])
+def test_ordered_body_sweep_log_replays_on_oracle(oracle, engine, name):
+    cfg = systems.ALL[name]()
+    kind, prm, pos, rot, box = cfg
+    cpu = po.CpuPacking("oracle", kind, prm, pos, rot, box, threads=1)
+    with gpu_packing(cfg) as g:
+        collect(g, 2, seed=5)
+        g.mlp_train(epochs=4, batch=512, lr=2e-3, seed=3)
+        g.pair_log_enable(0)
+        g.upload(pos, rot, box)
+        g.set_ordering(_lib.ORDER_MLP, every=1)
+        for cycle in range(2):
+            g.sweep(0.2, 0.2, seed=404, counter=cycle, log=True)
+            moves, codes = g.sweep_log()
+            _, _, bounds = g.grid()
+            want, _ = cpu.replay(moves, bounds)
+            assert np.array_equal(codes, want)
+        gp, gr, _ = g.state()
+        cp, cr, _ = cpu.state()
+        assert np.array_equal(gp, cp) and np.array_equal(gr, cr)
