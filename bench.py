@@ -471,6 +471,12 @@ def main_gpu(args):
     if rank == 0 and args.workload == "sc-1e6" and not args.no_ordering:
         ordering = ordering_compare(g, args, sweeps=max(4, min(args.steps, 8)),
                                     variants=[("plain", 0, 1), ("distance", 2, 16), ("mlp", 1, 64)])
+    if rank == 0 and args.workload == "banana-1e5" and not args.no_ordering:
+        # the bent chains of the learned-ordering configuration: the network trained on 10^7
+        # logged pair outcomes
+        ordering = ordering_compare(g, args, sweeps=max(4, min(args.steps, 8)), pairs=10_000_000, every_move=1,
+                                    epochs=2, variants=[("plain", 0, 1), ("distance", 2, 4), ("mlp", 1, 4),
+                                                        ("mlp", 1, 16)])
 
     # ---- CPU baseline (rank 0, N=1 only) ----
     cpu_base = None
@@ -515,7 +521,7 @@ def main_gpu(args):
     return 0
 
 
-def ordering_compare(g, args, sweeps: int, variants, training_sweeps: int = 4, every_move: int = 16,
+def ordering_compare(g, args, sweeps: int, variants, pairs: int = 4_000_000, every_move: int = 16,
                      epochs: int = 4):
     """Sweeps from the packing's current state with the plain neighbourhood scan, with partners
     ranked by centre distance and with partners ranked by the network trained (on the device,
@@ -526,10 +532,13 @@ def ordering_compare(g, args, sweeps: int, variants, training_sweeps: int = 4, e
     variant sweep (the ceiling of the ordering with its ranking made free)."""
     from rampack_gb300 import _lib
     start = g.state()
-    # training data: pairs reaching the segment test in every 16th move of 4 sweeps
-    g.pair_log_enable(4_000_000, every_move)
-    for c in range(training_sweeps):
-        g.sweep(TRANS_STEP, ROT_STEP, seed=args.seed + 1, counter=c, stats=False)
+    # training data: the pairs reaching the exact pair stage in every `every_move`-th move,
+    # logged over as many sweeps as it takes to collect `pairs` outcomes
+    g.pair_log_enable(pairs, every_move)
+    training_sweeps = 0
+    while g.pair_log_count() < pairs and training_sweeps < 40:
+        g.sweep(TRANS_STEP, ROT_STEP, seed=args.seed + 1, counter=training_sweeps, stats=False)
+        training_sweeps += 1
     feats, labels = g.pair_log()
     _, loss0 = g.mlp_gradient(feats[:200_000], labels[:200_000])
     g.set_timing(True)
@@ -574,7 +583,8 @@ def ordering_compare(g, args, sweeps: int, variants, training_sweeps: int = 4, e
             "speedup_ranking_free": max(r["speedup_ranking_free"] for r in rows),
             "state_identical_to_plain": all(r["state_identical_to_plain"] for r in rows),
             "sweeps": sweeps, "unit": "ms per sweep (CUDA events)",
-            "training": {"pairs": int(len(feats)), "positive_fraction": round(float(labels.mean()), 4),
+            "training": {"pairs": int(len(feats)), "logged_over_sweeps": training_sweeps,
+                         "positive_fraction": round(float(labels.mean()), 4),
                          "epochs": epochs, "batch": 1024, "loss_before": round(loss0, 4),
                          "loss_after": round(loss1, 4), "last_epoch_loss": round(loss, 4),
                          "device_ms": round(train_ms, 1), "wall_s": round(train_s, 2)},
