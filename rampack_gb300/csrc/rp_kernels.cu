@@ -206,7 +206,8 @@ __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(co
     uint16_t *qun = qseg + A.cap;
     uint8_t *nacc = reinterpret_cast<uint8_t *>(qun + A.cap);
     uint16_t *pstage = reinterpret_cast<uint16_t *>(nacc + A.cap);  // LEARN only: MLP_PARTNERS x cap
-    float4 *wx = reinterpret_cast<float4 *>(nacc + A.cap);          // polyspheres (never with LEARN)
+    // polyspheres: after the partner slots when the learned ordering is on
+    float4 *wx = reinterpret_cast<float4 *>(nacc + A.cap) + (LEARN ? A.cap / 4 : 0);
     int nitems = A.work ? *A.work_count : (LIST ? A.num_list : A.num_active);
     WarpStats ws{};
     // persistent launches (next_item set) take cells from a shared counter until none are

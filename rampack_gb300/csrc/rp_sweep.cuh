@@ -26,6 +26,35 @@ __device__ __forceinline__ float3 mat32(const float *m, float x, float y, float 
 
 __device__ __forceinline__ float dot3f(float3 a, float3 b) { return fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)); }
 
+// A group of GW consecutive lanes that sweeps one cell: the whole warp (GW = 32) or either
+// half of it (GW = 16, two cells per warp).  Its votes and shuffles name the group's own lanes
+// (lane = 0..GW-1); ballots return group-relative bits, so a group's code reads the same for
+// both widths.  With GW = 16 the two halves of a warp run their cells independently.
+template <int GW>
+struct Grp {
+    static_assert(GW == 32 || GW == 16, "a group is a warp or half a warp");
+    unsigned mask;  // the group's lanes in the warp
+    int base;       // its first lane
+    int lane;       // this thread's lane in the group
+    __device__ __forceinline__ Grp() {
+        const int wl = threadIdx.x & 31;
+        base = GW == 32 ? 0 : (wl & 16);
+        lane = wl - base;
+        mask = GW == 32 ? 0xffffffffu : (0xffffu << base);
+    }
+    __device__ __forceinline__ unsigned ballot(bool p) const {
+        const unsigned b = __ballot_sync(mask, p);
+        return GW == 32 ? b : ((b & mask) >> base);
+    }
+    template <class T>
+    __device__ __forceinline__ T shfl(T v, int src) const { return __shfl_sync(mask, v, base + src); }
+    template <class T>
+    __device__ __forceinline__ T shfl_up(T v, int d) const { return __shfl_up_sync(mask, v, d, GW); }
+    template <class T>
+    __device__ __forceinline__ T shfl_xor(T v, int d) const { return __shfl_xor_sync(mask, v, d, GW); }
+    __device__ __forceinline__ void sync() const { __syncwarp(mask); }
+};
+
 // ---------------------------------------------------------------------------------
 // FP32 classification of one pair.  0: no overlap, 1: overlap, 2: undecided in FP32
 // (re-decided in FP64).  d = p_j - p_i (candidate minus mover), a_i/a_j unit axes.
@@ -225,7 +254,7 @@ struct WarpStats {
 // MODE 0: plain sweep; 1: learned-ordering pre-test and pair log; 2: overlap counting
 // (Packing::toggleOverlapCounting, core/Packing.cpp:304-323: the move's energy is the sign of
 // the change of the mover's overlap count).
-template <int KIND, bool LIST, int MODE>
+template <int KIND, bool LIST, int MODE, int GW = 32>
 __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, const int cell_direct, const int cap,
                                            int32_t *ovf, int32_t *ovf_count, float4 *cpos, float4 *cax,
                                            uint16_t *qseg, uint16_t *qun, uint8_t *nacc, uint16_t *pstage,
@@ -233,8 +262,8 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
     constexpr bool LEARN = MODE == 1;
     constexpr bool COUNT = MODE == 2;
     constexpr bool RT = MODE == 3;  // every move a rototranslation (the plain scan otherwise)
-    const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
+    const Grp<GW> grp;
+    const int lane = grp.lane;
     const unsigned lt = (1u << lane) - 1u;
     const DevState &S = A.s;
     const GridDev &G = A.g;
@@ -261,42 +290,52 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
     c[1] = (cell / G.dims[0]) % G.dims[1];
     c[2] = cell / (G.dims[0] * G.dims[1]);
 
-    // ---- stage the 3x3x3 neighbourhood (own cell first) ----
-    int cnt = 0, st = 0;
-    float3 off = make_float3(0.f, 0.f, 0.f);
-    if (lane < 27) {
-        int ox, oy, oz;
-        lane_offset(lane, ox, oy, oz);
-        int nb = wrap_cell(c[0] + ox, G.dims[0]) +
-                 G.dims[0] * (wrap_cell(c[1] + oy, G.dims[1]) + G.dims[1] * wrap_cell(c[2] + oz, G.dims[2]));
-        st = G.start[nb];
-        cnt = G.start[nb + 1] - st;
-        off = mat32(G.cellmat, (float)ox, (float)oy, (float)oz);
-    }
+    // ---- stage the 3x3x3 neighbourhood (own cell first): neighbour cell lane + GW r ----
+    constexpr int NR = 32 / GW;  // neighbour cells per lane (27 cells over the group's lanes)
+    int cnt[NR], st[NR], kcnt[NR], pre[NR];
+    float3 off[NR];
     // with the staging filter, a neighbour cell's particles farther than the interaction
     // range from the home cell (whose movers stay inside it: the cell is their ActiveDomain)
-    // are left out; the own cell (lane 0) is always staged whole
+    // are left out; the own cell (neighbour 0) is always staged whole
     const bool filt = G.stage_filter && !LEARN;
-    auto keep = [&](const float4 &p) {
-        const float3 f = mat32(G.cellinv, p.x + off.x, p.y + off.y, p.z + off.z);
+    auto keep = [&](const float4 &p, const float3 &o) {
+        const float3 f = mat32(G.cellinv, p.x + o.x, p.y + o.y, p.z + o.z);
         const float e0 = fmaxf(fmaxf(-f.x, f.x - 1.f), 0.f) * G.stage_h[0];
         const float e1 = fmaxf(fmaxf(-f.y, f.y - 1.f), 0.f) * G.stage_h[1];
         const float e2 = fmaxf(fmaxf(-f.z, f.z - 1.f), 0.f) * G.stage_h[2];
         return fmaxf(e0, fmaxf(e1, e2)) <= G.stage_thr;
     };
-    int kcnt = cnt;
-    if (filt && lane > 0 && lane < 27) {
-        kcnt = 0;
-        for (int k = 0; k < cnt; k++) kcnt += keep(G.mpos[st + k]) ? 1 : 0;
+    int total = 0;
+#pragma unroll
+    for (int r = 0; r < NR; r++) {
+        const int nbl = lane + GW * r;
+        cnt[r] = 0;
+        st[r] = 0;
+        off[r] = make_float3(0.f, 0.f, 0.f);
+        if (nbl < 27) {
+            int ox, oy, oz;
+            lane_offset(nbl, ox, oy, oz);
+            int nb = wrap_cell(c[0] + ox, G.dims[0]) +
+                     G.dims[0] * (wrap_cell(c[1] + oy, G.dims[1]) + G.dims[1] * wrap_cell(c[2] + oz, G.dims[2]));
+            st[r] = G.start[nb];
+            cnt[r] = G.start[nb + 1] - st[r];
+            off[r] = mat32(G.cellmat, (float)ox, (float)oy, (float)oz);
+        }
+        kcnt[r] = cnt[r];
+        if (filt && nbl > 0 && nbl < 27) {
+            kcnt[r] = 0;
+            for (int k = 0; k < cnt[r]; k++) kcnt[r] += keep(G.mpos[st[r] + k], off[r]) ? 1 : 0;
+        }
+        int incl = kcnt[r];
+        for (int d = 1; d < GW; d <<= 1) {
+            int y = grp.shfl_up(incl, d);
+            if (lane >= d) incl += y;
+        }
+        pre[r] = total + incl - kcnt[r];
+        total += grp.shfl(incl, GW - 1);
     }
-    int incl = kcnt;
-    for (int d = 1; d < 32; d <<= 1) {
-        int y = __shfl_up_sync(FULL, incl, d);
-        if (lane >= d) incl += y;
-    }
-    const int total = __shfl_sync(FULL, incl, 31);
-    const int occ = __shfl_sync(FULL, cnt, 0);
-    const int gbase = __shfl_sync(FULL, st, 0);
+    const int occ = grp.shfl(cnt[0], 0);
+    const int gbase = grp.shfl(st[0], 0);
     if (total > cap) {
         if (lane == 0) {
             if (ovf) {
@@ -308,30 +347,34 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
         }
         return;
     }
-    if (!filt) {
-        // every neighbour staged: positions known from the prefix sum (loads pipeline freely)
-        const int base = incl - cnt;
-        for (int k = 0; k < cnt; k++) {
-            float4 p = G.mpos[st + k];
-            p.x += off.x;
-            p.y += off.y;
-            p.z += off.z;
-            cpos[base + k] = p;
-            if (KIND == 1) cax[base + k] = G.maxis[st + k];
-            if (KIND == 2) cslot[base + k] = (uint32_t)(st + k);  // its centres stay in the L2-resident mirror
-        }
-    } else {
-        int j = incl - kcnt;
-        for (int k = 0; k < cnt; k++) {
-            float4 p = G.mpos[st + k];
-            if (lane > 0 && !keep(p)) continue;
-            p.x += off.x;
-            p.y += off.y;
-            p.z += off.z;
-            cpos[j] = p;
-            if (KIND == 1) cax[j] = G.maxis[st + k];
-            if (KIND == 2) cslot[j] = (uint32_t)(st + k);
-            j++;
+#pragma unroll
+    for (int r = 0; r < NR; r++) {
+        const int nbl = lane + GW * r;
+        if (!filt) {
+            // every neighbour staged: positions known from the prefix sum (loads pipeline freely)
+            const int base = pre[r];
+            for (int k = 0; k < cnt[r]; k++) {
+                float4 p = G.mpos[st[r] + k];
+                p.x += off[r].x;
+                p.y += off[r].y;
+                p.z += off[r].z;
+                cpos[base + k] = p;
+                if (KIND == 1) cax[base + k] = G.maxis[st[r] + k];
+                if (KIND == 2) cslot[base + k] = (uint32_t)(st[r] + k);  // its centres stay in the L2-resident mirror
+            }
+        } else {
+            int j = pre[r];
+            for (int k = 0; k < cnt[r]; k++) {
+                float4 p = G.mpos[st[r] + k];
+                if (nbl > 0 && !keep(p, off[r])) continue;
+                p.x += off[r].x;
+                p.y += off[r].y;
+                p.z += off[r].z;
+                cpos[j] = p;
+                if (KIND == 1) cax[j] = G.maxis[st[r] + k];
+                if (KIND == 2) cslot[j] = (uint32_t)(st[r] + k);
+                j++;
+            }
         }
     }
     // polyspheres: the warp's scratch holds the mover's FP32 centres (wx[0..K)), the
@@ -341,15 +384,16 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
     double *wcen = wabs + 3 * MAX_CEN;
     double *whax = wcen + 3 * MAX_CEN;   // polyspherocylinders: the mover's rotated half axes
     if (KIND == 2)
-        for (int t = lane; t < 2 * MAX_CEN * MAX_CEN; t += 32) wthr[t] = G.cthr[t];
+        for (int t = lane; t < 2 * MAX_CEN * MAX_CEN; t += GW) wthr[t] = G.cthr[t];
     const bool self_images = (G.dims[0] == 1) || (G.dims[1] == 1) || (G.dims[2] == 1);
     // per own-cell particle: FP32 roundings accumulated in its mirror position this sweep
-    for (int k = lane; k < occ; k += 32) nacc[k] = 0;
+    for (int k = lane; k < occ; k += GW) nacc[k] = 0;
     if (LEARN && A.partners) {
         // the ranked partners of the cell's particles, as indices into the staged
         // neighbourhood (a partner out of reach of this cell's neighbourhood gets none)
-        const int base_nb = incl - cnt;
-        for (int eb = 0; eb < occ * MLP_PARTNERS; eb += 32) {
+        static_assert(!LEARN || GW == 32, "the partner pre-test stages with whole warps");
+        const int base_nb = pre[0];
+        for (int eb = 0; eb < occ * MLP_PARTNERS; eb += GW) {
             const int e = eb + lane;
             int sj = -1;
             if (e < occ * MLP_PARTNERS) {
@@ -359,14 +403,14 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
             }
             int idx = 0xffff;
             for (int nb = 0; nb < 27; nb++) {
-                const int s0 = __shfl_sync(FULL, st, nb), c0 = __shfl_sync(FULL, cnt, nb),
-                          b0 = __shfl_sync(FULL, base_nb, nb);
+                const int s0 = grp.shfl(st[0], nb), c0 = grp.shfl(cnt[0], nb),
+                          b0 = grp.shfl(base_nb, nb);
                 if (idx == 0xffff && sj >= s0 && sj < s0 + c0) idx = b0 + sj - s0;
             }
             if (e < occ * MLP_PARTNERS) pstage[e] = (uint16_t)idx;
         }
     }
-    __syncwarp();
+    grp.sync();
 
     // this lane's dimension (lanes 0-2): ActiveDomain bounds and cell coordinate
     const int ld = lane < 3 ? lane : 0;
@@ -395,8 +439,9 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
 
     u4 rnd_lane = u4{0u, 0u, 0u, 0u};  // Philox output of move (batch base + lane)
     for (int mi = 0; mi < nmoves; mi++) {
-        if (!LIST && (mi & 31) == 0) {
-            // draw the next 32 moves' random words at once, one move per lane
+        if (!LIST && (mi & (GW - 1)) == 0) {
+            // draw the next GW moves' random words at once, one move per lane (the words
+            // of a move depend only on its index and cell, whatever the group width)
             rnd_lane = philox(u4{(uint32_t)(mi + lane), (uint32_t)cell, (uint32_t)A.counter,
                                  (uint32_t)(A.counter >> 32)},
                               (uint32_t)A.seed, (uint32_t)(A.seed >> 32));
@@ -415,10 +460,10 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
             mrec = A.moves + out_index;
             type = mrec->type;
             int want = mrec->particle;
-            for (int kb = 0; kb < occ; kb += 32) {
+            for (int kb = 0; kb < occ; kb += GW) {
                 int k = kb + lane;
                 bool hit = k < occ && __float_as_int(cpos[k].w) == want;
-                unsigned bal = __ballot_sync(FULL, hit);
+                unsigned bal = grp.ballot(hit);
                 if (bal) {
                     slot = kb + __ffs(bal) - 1;
                     break;
@@ -436,9 +481,9 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
             uni = mrec->uniform;
             for (int q = 0; q < 9; q++) R32[q] = (float)mrec->rotation[q];
         } else {
-            const int src = mi & 31;
-            u4 r = u4{__shfl_sync(FULL, rnd_lane.a, src), __shfl_sync(FULL, rnd_lane.b, src),
-                      __shfl_sync(FULL, rnd_lane.c, src), __shfl_sync(FULL, rnd_lane.d, src)};
+            const int src = mi & (GW - 1);
+            u4 r = u4{grp.shfl(rnd_lane.a, src), grp.shfl(rnd_lane.b, src),
+                      grp.shfl(rnd_lane.c, src), grp.shfl(rnd_lane.d, src)};
             const bool rt = RT || (COUNT && A.types == SWEEP_ROTOTRANSLATION);
             if (rt) type = 2;
             else if (ntypes == 2) type = (r.a >> 31) ? 1 : 0;
@@ -490,7 +535,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                 if (type != 0) cn = mat32(R32, cn.x, cn.y, cn.z);
                 wx[lane] = make_float4(cn.x, cn.y, cn.z, 0.f);
             }
-            __syncwarp();
+            grp.sync();
         }
 
         // ---- FP32 ActiveDomain test (translations): 0 inside, 1 outside, 2 undecided;
@@ -538,18 +583,18 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                     }
                 }
             }
-            const unsigned nt = __popc(__ballot_sync(FULL, tested));
+            const unsigned nt = __popc(grp.ballot(tested));
             if (lane == 0) ws.pairs += nt;
-            if (__ballot_sync(FULL, cls == 1)) overlap = true;
+            if (grp.ballot(cls == 1)) overlap = true;
         }
 
         // ---- FP32 pass 1: centre distances, two candidates per lane per round ----
         int nseg = 0, nun = 0;
         if (!COUNT && dom != 1 && !overlap) {
-            for (int base = 0; base < total; base += 64) {
-                int k0 = base + lane, k1 = base + 32 + lane;
+            for (int base = 0; base < total; base += 2 * GW) {
+                int k0 = base + lane, k1 = base + GW + lane;
                 int c0 = 0, c1 = 0;
-                if (lane == 0) ws.pairs += (unsigned)min(64, total - base);
+                if (lane == 0) ws.pairs += (unsigned)min(2 * GW, total - base);
                 if (k0 < total) {
                     float4 q = cpos[k0];
                     if (__float_as_int(q.w) != pid) {
@@ -564,29 +609,29 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                         c1 = A.fp64_only ? 2 : d2_stage<KIND>(S.fc, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
                     }
                 }
-                if (__ballot_sync(FULL, c0 == 1 || c1 == 1)) {
+                if (grp.ballot(c0 == 1 || c1 == 1)) {
                     overlap = true;
                     break;
                 }
                 if (KIND >= 1) {
-                    unsigned b0 = __ballot_sync(FULL, c0 == 3), b1 = __ballot_sync(FULL, c1 == 3);
+                    unsigned b0 = grp.ballot(c0 == 3), b1 = grp.ballot(c1 == 3);
                     if (c0 == 3) qseg[nseg + __popc(b0 & lt)] = (uint16_t)k0;
                     nseg += __popc(b0);
                     if (c1 == 3) qseg[nseg + __popc(b1 & lt)] = (uint16_t)k1;
                     nseg += __popc(b1);
                 }
-                unsigned u0 = __ballot_sync(FULL, c0 == 2), u1 = __ballot_sync(FULL, c1 == 2);
+                unsigned u0 = grp.ballot(c0 == 2), u1 = grp.ballot(c1 == 2);
                 if (c0 == 2) qun[nun + __popc(u0 & lt)] = (uint16_t)k0;
                 nun += __popc(u0);
                 if (c1 == 2) qun[nun + __popc(u1 & lt)] = (uint16_t)k1;
                 nun += __popc(u1);
             }
         }
-        __syncwarp();
+        grp.sync();
         // ---- FP32 pass 2 (polyspheres): every centre pair of a near body, one body per lane ----
         if (!COUNT && KIND == 2 && !overlap) {
             const int K = S.ncen;
-            for (int base = 0; base < nseg; base += 32) {
+            for (int base = 0; base < nseg; base += GW) {
                 const int i = base + lane;
                 int cls = 0, k = 0;
                 if (i < nseg) {
@@ -600,13 +645,13 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                     // the move (whole orientations: the bodies are bent), labelled with the
                     // certain outcome after it
                     const bool rec = i < nseg && cls != 2;
-                    const unsigned bal = __ballot_sync(FULL, rec);
+                    const unsigned bal = grp.ballot(rec);
                     unsigned long long base_idx = 0;
                     if (lane == 0 && bal) base_idx = atomicAdd(A.pair_count, (unsigned long long)__popc(bal));
-                    base_idx = __shfl_sync(FULL, base_idx, 0);
+                    base_idx = grp.shfl(base_idx, 0);
                     const unsigned long long idx = base_idx + __popc(bal & lt);
                     float ri[9];
-                    for (int e = 0; e < 9; e++) ri[e] = (float)__shfl_sync(FULL, rot_own, e);
+                    for (int e = 0; e < 9; e++) ri[e] = (float)grp.shfl(rot_own, e);
                     if (rec && idx < A.pair_cap) {
                         const float4 q = cpos[k];
                         const double *oj = S.rot64 + 9 * (size_t)__float_as_int(q.w);
@@ -623,19 +668,19 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                         A.pair_labels[idx] = cls == 1 ? 1 : 0;
                     }
                 }
-                if (__ballot_sync(FULL, cls == 1)) {
+                if (grp.ballot(cls == 1)) {
                     overlap = true;
                     break;
                 }
-                unsigned b2 = __ballot_sync(FULL, cls == 2);
+                unsigned b2 = grp.ballot(cls == 2);
                 if (cls == 2) qun[nun + __popc(b2 & lt)] = (uint16_t)k;
                 nun += __popc(b2);
             }
-            __syncwarp();
+            grp.sync();
         }
         // ---- FP32 pass 2 (spherocylinders): segment distances on full warps ----
         if (!COUNT && KIND == 1 && !overlap) {
-            for (int base = 0; base < nseg; base += 32) {
+            for (int base = 0; base < nseg; base += GW) {
                 int i = base + lane;
                 int cls = 0, k = 0;
                 if (i < nseg) {
@@ -649,10 +694,10 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                     // training data of the ranking network: the pair as it was before the
                     // move, labelled with the certain outcome after it
                     const bool rec = i < nseg && cls != 2;
-                    const unsigned bal = __ballot_sync(FULL, rec);
+                    const unsigned bal = grp.ballot(rec);
                     unsigned long long base_idx = 0;
                     if (lane == 0 && bal) base_idx = atomicAdd(A.pair_count, (unsigned long long)__popc(bal));
-                    base_idx = __shfl_sync(FULL, base_idx, 0);
+                    base_idx = grp.shfl(base_idx, 0);
                     const unsigned long long idx = base_idx + __popc(bal & lt);
                     if (rec && idx < A.pair_cap) {
                         float4 q = cpos[k];
@@ -668,15 +713,15 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                         A.pair_labels[idx] = cls == 1 ? 1 : 0;
                     }
                 }
-                if (__ballot_sync(FULL, cls == 1)) {
+                if (grp.ballot(cls == 1)) {
                     overlap = true;
                     break;
                 }
-                unsigned b2 = __ballot_sync(FULL, cls == 2);
+                unsigned b2 = grp.ballot(cls == 2);
                 if (cls == 2) qun[nun + __popc(b2 & lt)] = (uint16_t)k;
                 nun += __popc(b2);
             }
-            __syncwarp();
+            grp.sync();
         }
 
         uint8_t code = dom == 1 ? 2 : (overlap ? 1 : 0);
@@ -729,29 +774,29 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                     // which is box · 0 = +0 exactly
                     pnew_own = dadd(p1, 0.0);
                     if (dom == 2) {
-                        d3 P1{__shfl_sync(FULL, p1, 0), __shfl_sync(FULL, p1, 1), __shfl_sync(FULL, p1, 2)};
+                        d3 P1{grp.shfl(p1, 0), grp.shfl(p1, 1), grp.shfl(p1, 2)};
                         rel_own = mrow(S.inv, ld, P1);
                         exact_rel = true;
                     }
                 } else {
-                    d3 P1{__shfl_sync(FULL, p1, 0), __shfl_sync(FULL, p1, 1), __shfl_sync(FULL, p1, 2)};
+                    d3 P1{grp.shfl(p1, 0), grp.shfl(p1, 1), grp.shfl(p1, 2)};
                     double rel = mrow(S.inv, ld, P1);
                     double cr = 0.0;
                     while (dadd(rel, cr) < 0.0) cr = dadd(cr, 1.0);
                     while (dadd(rel, cr) >= 1.0) cr = dsub(cr, 1.0);
-                    if (__ballot_sync(FULL, lane < 3 && cr != 0.0) == 0u) {
+                    if (grp.ballot(lane < 3 && cr != 0.0) == 0u) {
                         pnew_own = dadd(p1, 0.0);
                         rel_own = rel;
                     } else {
-                        d3 C{__shfl_sync(FULL, cr, 0), __shfl_sync(FULL, cr, 1), __shfl_sync(FULL, cr, 2)};
+                        d3 C{grp.shfl(cr, 0), grp.shfl(cr, 1), grp.shfl(cr, 2)};
                         pnew_own = dadd(p1, mrow(S.box, ld, C));
-                        d3 PN{__shfl_sync(FULL, pnew_own, 0), __shfl_sync(FULL, pnew_own, 1),
-                              __shfl_sync(FULL, pnew_own, 2)};
+                        d3 PN{grp.shfl(pnew_own, 0), grp.shfl(pnew_own, 1),
+                              grp.shfl(pnew_own, 2)};
                         rel_own = mrow(S.inv, ld, PN);
                     }
                     exact_rel = true;
                 }
-                pnew = d3{__shfl_sync(FULL, pnew_own, 0), __shfl_sync(FULL, pnew_own, 1), __shfl_sync(FULL, pnew_own, 2)};
+                pnew = d3{grp.shfl(pnew_own, 0), grp.shfl(pnew_own, 1), grp.shfl(pnew_own, 2)};
                 if (dom == 2) {
                     // ActiveDomain::isInside (core/ActiveDomain.cpp:8-21) on the exact position
                     bool out = false;
@@ -759,24 +804,24 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                         if (hi_d > lo_d) out = rel_own <= lo_d || rel_own >= hi_d;
                         else out = rel_own <= lo_d && rel_own >= hi_d;
                     }
-                    if (__ballot_sync(FULL, out)) code = 2;
+                    if (grp.ballot(out)) code = 2;
                 }
             } else {
-                pnew = d3{__shfl_sync(FULL, pos_own, 0), __shfl_sync(FULL, pos_own, 1), __shfl_sync(FULL, pos_own, 2)};
+                pnew = d3{grp.shfl(pos_own, 0), grp.shfl(pos_own, 1), grp.shfl(pos_own, 2)};
             }
             if (type != 0) {
                 // Shape::rotate: R · O (core/Shape.cpp:14-16, Matrix.tpp:104-113), entry (ei, ej) per lane
                 double oe = rot_own;
-                double o0 = __shfl_sync(FULL, oe, ej), o1 = __shfl_sync(FULL, oe, 3 + ej),
-                       o2 = __shfl_sync(FULL, oe, 6 + ej);
+                double o0 = grp.shfl(oe, ej), o1 = grp.shfl(oe, 3 + ej),
+                       o2 = grp.shfl(oe, 6 + ej);
                 double s = 0.0;
                 s = dadd(s, dmul(rrow[0], o0));
                 s = dadd(s, dmul(rrow[1], o1));
                 s = dadd(s, dmul(rrow[2], o2));
                 onew_own = s;
-                anew = d3{__shfl_sync(FULL, s, 2), __shfl_sync(FULL, s, 5), __shfl_sync(FULL, s, 8)};
+                anew = d3{grp.shfl(s, 2), grp.shfl(s, 5), grp.shfl(s, 8)};
             } else {
-                anew = d3{__shfl_sync(FULL, rot_own, 2), __shfl_sync(FULL, rot_own, 5), __shfl_sync(FULL, rot_own, 8)};
+                anew = d3{grp.shfl(rot_own, 2), grp.shfl(rot_own, 5), grp.shfl(rot_own, 8)};
             }
             if (KIND == 2) {
                 // the mover's centres: rotated by R (Packing::rotateTempInteractionCentres,
@@ -784,9 +829,9 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                 // (core/Packing.cpp:1041-1047); one centre per lane
                 double R[9];
                 for (int d = 0; d < 3; d++) {
-                    R[3 * d] = __shfl_sync(FULL, rrow[0], 3 * d);
-                    R[3 * d + 1] = __shfl_sync(FULL, rrow[1], 3 * d);
-                    R[3 * d + 2] = __shfl_sync(FULL, rrow[2], 3 * d);
+                    R[3 * d] = grp.shfl(rrow[0], 3 * d);
+                    R[3 * d + 1] = grp.shfl(rrow[1], 3 * d);
+                    R[3 * d + 2] = grp.shfl(rrow[2], 3 * d);
                 }
                 if (lane < S.ncen) {
                     d3 c = load_d3(S.cen64 + 3 * ((size_t)pid * S.ncen + lane));
@@ -805,7 +850,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                     // (PolyspherocylinderTraits.cpp:118-119)
                     const double oe = type != 0 ? onew_own : rot_own;
                     double O[9];
-                    for (int e = 0; e < 9; e++) O[e] = __shfl_sync(FULL, oe, e);
+                    for (int e = 0; e < 9; e++) O[e] = grp.shfl(oe, e);
                     if (lane < S.ncen) {
                         d3 h = mv3(O, d3{S.chax[lane][0], S.chax[lane][1], S.chax[lane][2]});
                         whax[3 * lane] = h.x;
@@ -813,7 +858,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                         whax[3 * lane + 2] = h.z;
                     }
                 }
-                __syncwarp();
+                grp.sync();
             }
             // the guard band: queued pairs re-decided in FP64
             if (KIND == 2 && code == 0 && nun > 0) {
@@ -822,7 +867,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                 // keep the lanes busy), else one body per pass
                 const int K = S.ncen;
                 const int KK = K * K;
-                const int per = KK <= 16 ? 32 / KK : 1;
+                const int per = KK <= GW / 2 ? GW / KK : 1;
                 bool ov = false;
                 for (int q0 = 0; q0 < nun && !ov; q0 += per) {
                     const int qi = q0 + (per > 1 ? lane / KK : 0);
@@ -830,7 +875,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                     const float4 q = cpos[k];
                     const float3 dq = make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z);
                     const float4 *cj = G.mcen + (size_t)cslot[k] * K;
-                    for (int tb = 0; tb < (per > 1 ? 1 : KK); tb += 32) {
+                    for (int tb = 0; tb < (per > 1 ? 1 : KK); tb += GW) {
                         const int t = per > 1 ? lane % KK : tb + lane;
                         bool hit = false;
                         if (t < KK && qi < nun && (per == 1 || lane < per * KK)) {
@@ -842,7 +887,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                                                     __float_as_int(q.w), j, d,
                                                     d3{whax[3 * a], whax[3 * a + 1], whax[3 * a + 2]});
                         }
-                        if (__ballot_sync(FULL, hit)) {
+                        if (grp.ballot(hit)) {
                             ov = true;
                             break;
                         }
@@ -853,7 +898,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
             }
             if (KIND != 2 && code == 0 && nun > 0) {
                 bool ov = false;
-                for (int qb = 0; qb < nun; qb += 32) {
+                for (int qb = 0; qb < nun; qb += GW) {
                     int qi = qb + lane;
                     bool hit = false;
                     if (qi < nun) {
@@ -862,7 +907,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                         hit = exact_pair(S, pnew, anew, __float_as_int(q.w),
                                          make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z));
                     }
-                    if (__ballot_sync(FULL, hit)) {
+                    if (grp.ballot(hit)) {
                         ov = true;
                         break;
                     }
@@ -878,7 +923,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                     wov = wall_overlap_count(S.walls, S.wall_vec, S.wall_far, S.wall_half, KIND, S.wall_radius,
                                              S.wall_half_len, pnew, anew, KIND == 2 ? wcen : nullptr,
                                              KIND == 2 ? S.ncen : 0, true, KIND == 2 && S.segs ? whax : nullptr);
-                if (__shfl_sync(FULL, wov, 0)) code = 1;
+                if (grp.shfl(wov, 0)) code = 1;
             }
         }
 
@@ -886,8 +931,8 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
         //      candidate classified (no early exit), undecided pairs in FP64 ----
         int cdelta = 0;
         if (COUNT && code == 0) {
-            const d3 pc64{__shfl_sync(FULL, pos_own, 0), __shfl_sync(FULL, pos_own, 1), __shfl_sync(FULL, pos_own, 2)};
-            const d3 ac64{__shfl_sync(FULL, rot_own, 2), __shfl_sync(FULL, rot_own, 5), __shfl_sync(FULL, rot_own, 8)};
+            const d3 pc64{grp.shfl(pos_own, 0), grp.shfl(pos_own, 1), grp.shfl(pos_own, 2)};
+            const d3 ac64{grp.shfl(rot_own, 2), grp.shfl(rot_own, 5), grp.shfl(rot_own, 8)};
             int before = 0, after = 0;
             if (KIND == 2) {
                 // multi-centre bodies: every centre pair of every candidate body, the mover's
@@ -895,7 +940,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                 const int K = S.ncen;
                 const float4 *mcur = G.mcen + ((size_t)gbase + slot) * K;
                 const bool exact = A.fp64_only || S.pbc_fold == 2;
-                for (int k = lane; k < total; k += 32) {
+                for (int k = lane; k < total; k += GW) {
                     const float4 q = cpos[k];
                     const int pj = __float_as_int(q.w);
                     if (pj == pid) continue;
@@ -943,7 +988,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                                                 pnew, anew, wcen, K, false, S.segs ? whax : nullptr);
                 }
             }
-            for (int k = lane; k < (KIND == 2 ? 0 : total); k += 32) {
+            for (int k = lane; k < (KIND == 2 ? 0 : total); k += GW) {
                 const float4 q = cpos[k];
                 const int pj = __float_as_int(q.w);
                 if (pj == pid) continue;
@@ -967,9 +1012,9 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                 after += wall_overlap_count(S.walls, S.wall_vec, S.wall_far, S.wall_half, KIND, S.wall_radius,
                                             S.wall_half_len, pnew, anew, nullptr, 0, false);
             }
-            for (int d = 16; d > 0; d >>= 1) {
-                before += __shfl_xor_sync(FULL, before, d);
-                after += __shfl_xor_sync(FULL, after, d);
+            for (int d = GW / 2; d > 0; d >>= 1) {
+                before += grp.shfl_xor(before, d);
+                after += grp.shfl_xor(after, d);
             }
             if (lane == 0) ws.pairs += (unsigned)(2 * (total - 1));
             cdelta = after - before;
@@ -984,7 +1029,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
             if (COUNT && lane == 0) atomicAdd(S.overlaps, (unsigned long long)(long long)cdelta);
             float4 np = pcur;
             float4 na = KIND == 1 ? cax[slot] : make_float4(0.f, 0.f, 0.f, 0.f);
-            __syncwarp();
+            grp.sync();
             if (type != 1) {
                 if (lane < 3) S.pos64[3 * (size_t)pid + lane] = pnew_own;
             }
@@ -1004,14 +1049,14 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                 if (fd < -0.5) fd += dims_ld;
                 if (fd > dims_ld - 0.5) fd -= dims_ld;
                 float f = (float)fd;
-                float f0 = __shfl_sync(FULL, f, 0), f1 = __shfl_sync(FULL, f, 1), f2 = __shfl_sync(FULL, f, 2);
+                float f0 = grp.shfl(f, 0), f1 = grp.shfl(f, 1), f2 = grp.shfl(f, 2);
                 float3 loc = mat32(G.cellmat, f0, f1, f2);
                 np = make_float4(loc.x, loc.y, loc.z, pcur.w);
             }
             if (type != 0) {
                 if (lane < 9) S.rot64[9 * (size_t)pid + lane] = onew_own;
                 const float of = (float)onew_own;
-                na = make_float4(__shfl_sync(FULL, of, 2), __shfl_sync(FULL, of, 5), __shfl_sync(FULL, of, 8), 0.f);
+                na = make_float4(grp.shfl(of, 2), grp.shfl(of, 5), grp.shfl(of, 8), 0.f);
             }
             if (lane == 0) {
                 cpos[slot] = np;
@@ -1034,8 +1079,8 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
             }
             if (self_images) {
                 // the own cell is staged several times (periodic images): refresh every copy
-                __syncwarp();
-                for (int k = lane + occ; k < total; k += 32) {
+                grp.sync();
+                for (int k = lane + occ; k < total; k += GW) {
                     float4 q = cpos[k];
                     if (__float_as_int(q.w) == pid) {
                         cpos[k] = make_float4(np.x + (q.x - pcur.x), np.y + (q.y - pcur.y), np.z + (q.z - pcur.z), q.w);
@@ -1043,7 +1088,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                     }
                 }
             }
-            __syncwarp();
+            grp.sync();
         }
 
         const uint8_t full_code = code | (acc ? RP_CODE_ACCEPTED : 0);
