@@ -57,6 +57,8 @@ def parse():
                     help="sc-1e6: the headline system; the others are further systems of the same path")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cells-per-warp", type=int, default=0, choices=[0, 1, 2],
+                    help="plain sweeps: 1 = a warp per cell, 2 = a cell per half-warp (0: the library default)")
     ap.add_argument("--no-ordering", action="store_true",
                     help="skip the learned-ordering comparison of the headline line")
     ap.add_argument("--seed", type=int, default=1234)
@@ -337,6 +339,8 @@ def main_gpu(args):
     kind, prm, pos, rot, box = cfg
     n = len(pos)
     g = GpuPacking(kind, prm, pos, rot, box, device=local)
+    if args.cells_per_warp:
+        g.set_cells_per_warp(args.cells_per_warp)
     g.box = np.array(box, dtype=np.float64)
     stream = torch.cuda.ExternalStream(g.stream(), device=local)
     seed = args.seed + 7919 * rank

@@ -436,6 +436,13 @@ int rp_count_overlaps_static(const rp_shape_desc *shape, int64_t n, const double
 int rp_set_walls(void *handle, int32_t mask);
 int rp_batch_set_walls(void *batch, int32_t mask);
 
+/* Cells a warp sweeps at once in the plain scans of spheres and spherocylinders: 1 (a warp
+ * per cell), or 2 (each half-warp sweeps its own cell with the axes read from the FP32 mirror,
+ * twice the cells in flight per SM).  Decisions and the proposal stream are the same either
+ * way; learned ordering, pair logs, overlap counting, rototranslations, the staging filter,
+ * polyspheres and neighbourhoods above the half-warp capacity keep a warp per cell. */
+int rp_set_cells_per_warp(void *handle, int32_t cells);
+
 /* Staging filter of the sweep: candidates of the 26 neighbour cells farther than the
  * interaction range from every face-slab of the mover's cell (its ActiveDomain) are not
  * staged; decisions are unchanged.  0 off, 1 (default) where cells are well above the range

@@ -58,6 +58,9 @@ cudaError_t launch_score_partners(const DevState &s, const GridDev &g, const flo
                                   int mode, float inv_range, int32_t *partners, cudaStream_t st);
 cudaError_t launch_rot_table(double *out64, float *out32, uint32_t count, uint64_t seed, uint64_t counter, float step,
                              cudaStream_t st);
+cudaError_t launch_sweep_half(const SweepArgs &a, int ncells, cudaStream_t st);
+size_t sweep_smem_per_half(int kind, int cap);
+int sweep_half_blocks_per_sm(int kind, int cap);
 cudaError_t launch_try_single(const SingleArgs &a, cudaStream_t st);
 cudaError_t launch_commit_single(const DevState &s, SingleTry *t, uint8_t *disp_flag, int32_t *disp_list, int slot,
                                  cudaStream_t st);
@@ -72,6 +75,7 @@ struct GridHost {
     int64_t cells_alloc = 0;
     int64_t bounds_alloc = 0;
     int cap = 0;
+    int cap_half = 0;         // staging capacity of a cell with two cells per warp (0: not offered)
     double cellmat64[9]{};
     std::vector<float> cthr;  // host copy of the FP32 centre-pair thresholds (polyspheres)
     std::vector<double> bounds_host;  // batch members: this grid's bounds, packed by the batch
@@ -257,6 +261,10 @@ struct Handle {
     std::vector<uint8_t> disp_flag_host;
     bool grid_patched = false;
     static constexpr int DISP_CAP = 4096;  // moved particles before the grid is rebuilt
+    // plain sweeps of spheres and spherocylinders: cells per warp (1, or 2: two lane groups
+    // of 16 with the axes read from the mirror, twice the cells in flight per SM)
+    int cells_per_warp = 1;
+    int half_cap_cached = -1, half_blocks = 0;  // resident blocks per SM at that capacity
 };
 
 // One group of kernel launches of a handle or a batch: counted, and bracketed by CUDA events
@@ -596,6 +604,14 @@ int setup_grid(Handle *h, GridHost &G, const double *box, const double *shift) {
     cap = (cap + 31) / 32 * 32;
     int maxcap = static_cast<int>(48 * 1024 / (sweep_smem_per_warp(h->shape.kind, 32, false, h->ncen) / 32));
     G.cap = std::min(cap, maxcap / 32 * 32);
+    // two cells per warp: 32 lane groups per SM (4 blocks of 8) in 220 KB of shared memory;
+    // offered when that holds the same capacity (larger neighbourhoods keep a warp per cell)
+    G.cap_half = 0;
+    if (h->shape.kind != RP_SHAPE_POLYSPHERE) {
+        const int half_max = static_cast<int>(220 * 1024 / (SWEEP_WARPS * 2 * 4) /
+                                              (sweep_smem_per_half(h->shape.kind, 32) / 32)) / 32 * 32;
+        if (G.cap <= half_max) G.cap_half = G.cap;
+    }
     int64_t nblocks = (ncell + 4095) / 4096;
     RP_CUDA(h, ensure(h->block_sums, h->block_sums_alloc, nblocks));
     RP_CUDA(h, ensure(h->overflow, h->overflow_alloc, ncell));
@@ -1493,10 +1509,25 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
             a.log = h->d_log;
             a.log_codes = h->d_log_codes;
         }
+        // two cells per warp for the plain scans of spheres and spherocylinders
+        const GridHost &gh = h->grid[h->gcur];
+        const bool half = h->cells_per_warp == 2 && gh.cap_half > 0 && !h->counting && types != SWEEP_ROTOTRANSLATION &&
+                          a.partners == nullptr && a.pair_every == 0 && !g.stage_filter;
+        if (half && h->half_cap_cached != gh.cap_half) {
+            h->half_blocks = sweep_half_blocks_per_sm(h->shape.kind, gh.cap_half);
+            h->half_cap_cached = gh.cap_half;
+        }
         {
             Group grp(h, RP_KERNEL_SWEEP, 1);
-            int resident = h->num_sms * SWEEP_WARPS * SWEEP_MIN_BLOCKS;
-            RP_CUDA(h, launch_sweep(a, false, std::min(a.num_active, resident), h->stream));
+            if (half && h->half_blocks > 0) {
+                a.cap = gh.cap_half;
+                const int resident = h->num_sms * h->half_blocks * SWEEP_WARPS * 2;
+                RP_CUDA(h, launch_sweep_half(a, std::min(a.num_active, resident), h->stream));
+                a.cap = gh.cap;
+            } else {
+                int resident = h->num_sms * SWEEP_WARPS * SWEEP_MIN_BLOCKS;
+                RP_CUDA(h, launch_sweep(a, false, std::min(a.num_active, resident), h->stream));
+            }
         }
         a.next_item = nullptr;
         rc = run_overflow(h, a, false);
@@ -2167,6 +2198,13 @@ int rp_set_staging_filter(void *handle, int32_t mode) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h || mode < 0 || mode > 2) return fail(h, RP_ERR_ARG, "bad argument");
     h->stage_mode = mode;
+    return RP_OK;
+}
+
+int rp_set_cells_per_warp(void *handle, int32_t cells) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || (cells != 1 && cells != 2)) return fail(h, RP_ERR_ARG, "cells per warp must be 1 or 2");
+    h->cells_per_warp = cells;
     return RP_OK;
 }
 

@@ -184,24 +184,26 @@ __global__ void k_count_poly(DevState s, GridDev g, int early, unsigned long lon
 // MODE 1 instantiates the learned-ordering pre-test and the pair-outcome log, MODE 2 the
 // overlap counting, MODE 3 the plain scan of rototranslations (kept out of the plain
 // kernel, whose registers and branches they would crowd)
-template <int KIND, bool LIST, int MODE>
+template <int KIND, bool LIST, int MODE, int GW>
 __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(const SweepArgs A) {
     extern __shared__ float4 smem[];
-    const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const int wib = threadIdx.x >> 5;
-    const int warps_per_block = blockDim.x >> 5;
-    const int warp = blockIdx.x * warps_per_block + wib;
-    // per-warp shared memory (float4 units): staged positions [cap], spherocylinder axes
-    // [cap] or polysphere mirror slots [cap uint32], two uint16 queues and a byte counter
-    // per slot [5 cap bytes], partner slots [LEARN], polysphere scratch [SWEEP_POLY_SCRATCH]
-    const int extra = KIND == 1 ? A.cap : (KIND == 2 ? A.cap / 4 : 0);
+    const Grp<GW> grp;
+    const int lane = grp.lane;
+    const int gib = threadIdx.x / GW;                 // the lane group (one cell at a time) in the block
+    const int groups_per_block = blockDim.x / GW;
+    const int group = blockIdx.x * groups_per_block + gib;
+    // per-group shared memory (float4 units): staged positions [cap], spherocylinder axes
+    // [cap] (with two cells per warp their mirror slots [cap uint32] instead) or polysphere
+    // mirror slots [cap uint32], two uint16 queues and a byte counter per slot [5 cap bytes],
+    // partner slots [LEARN], polysphere scratch [SWEEP_POLY_SCRATCH]
+    constexpr bool AXM = GW == 16 && KIND == 1;
+    const int extra = KIND == 1 ? (AXM ? A.cap / 4 : A.cap) : (KIND == 2 ? A.cap / 4 : 0);
     constexpr bool LEARN = MODE == 1;
-    const int per_warp = A.cap + extra + A.cap / 4 + A.cap / 16 + (LEARN ? A.cap / 4 : 0) +
-                         (KIND == 2 ? SWEEP_POLY_SCRATCH : 0);
-    float4 *cpos = smem + (size_t)wib * per_warp;
+    const int per_group = A.cap + extra + A.cap / 4 + A.cap / 16 + (LEARN ? A.cap / 4 : 0) +
+                          (KIND == 2 ? SWEEP_POLY_SCRATCH : 0);
+    float4 *cpos = smem + (size_t)gib * per_group;
     float4 *cax = cpos + A.cap;                                  // spherocylinders
-    uint32_t *cslot = reinterpret_cast<uint32_t *>(cpos + A.cap); // polyspheres: mirror slot of each candidate
+    uint32_t *cslot = reinterpret_cast<uint32_t *>(cpos + A.cap); // mirror slot of each candidate
     uint16_t *qseg = reinterpret_cast<uint16_t *>(cpos + A.cap + extra);
     uint16_t *qun = qseg + A.cap;
     uint8_t *nacc = reinterpret_cast<uint8_t *>(qun + A.cap);
@@ -211,19 +213,19 @@ __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(co
     int nitems = A.work ? *A.work_count : (LIST ? A.num_list : A.num_active);
     WarpStats ws{};
     // persistent launches (next_item set) take cells from a shared counter until none are
-    // left; otherwise warps stride over the cells
-    const int stride = gridDim.x * warps_per_block;
-    int item = warp;
+    // left; otherwise groups stride over the cells
+    const int stride = gridDim.x * groups_per_block;
+    int item = group;
     for (;;) {
         if (A.next_item) {
             int it = 0;
             if (lane == 0) it = atomicAdd(A.next_item, 1);
-            item = __shfl_sync(FULL, it, 0);
+            item = grp.shfl(it, 0);
         }
         if (item >= nitems) break;
-        sweep_cell<KIND, LIST, MODE>(A, item, -1, A.cap, A.overflow, A.overflow_count, cpos, cax, qseg, qun, nacc,
-                                      pstage, cslot, wx, ws);
-        __syncwarp();
+        sweep_cell<KIND, LIST, MODE, GW>(A, item, -1, A.cap, A.overflow, A.overflow_count, cpos, cax, qseg, qun, nacc,
+                                          pstage, cslot, wx, ws);
+        grp.sync();
         item += stride;
     }
     // ---- statistics ----
@@ -338,19 +340,52 @@ size_t sweep_smem_per_warp(int kind, int cap, bool learn, int ncen) {
            sizeof(float4);
 }
 
+// Shared memory of one cell's lane group when each warp sweeps two cells (spheres and
+// spherocylinders, plain scans): the axes stay in the mirror, a slot index per candidate.
+size_t sweep_smem_per_half(int kind, int cap) {
+    const int extra = kind == 1 ? cap / 4 : 0;
+    return (size_t)(cap + extra + cap / 4 + cap / 16) * sizeof(float4);
+}
+
+// Resident blocks per SM of the two-cells-per-warp sweep at staging capacity `cap`.
+int sweep_half_blocks_per_sm(int kind, int cap) {
+    const size_t smem = sweep_smem_per_half(kind, cap) * (SWEEP_WARPS * 2);
+    int n = 0;
+    cudaError_t e = kind == 0 ? cudaFuncSetAttribute(k_sweep<0, false, 0, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)smem)
+                              : cudaFuncSetAttribute(k_sweep<1, false, 0, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)smem);
+    if (e != cudaSuccess) return 0;
+    e = kind == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep<0, false, 0, 16>, SWEEP_WARPS * 32, smem)
+                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep<1, false, 0, 16>, SWEEP_WARPS * 32, smem);
+    return e == cudaSuccess ? n : 0;
+}
+
 cudaError_t launch_rot_table(double *out64, float *out32, uint32_t count, uint64_t seed, uint64_t counter, float step,
                              cudaStream_t st) {
     k_rot_table<<<(count + 255) / 256, 256, 0, st>>>(out64, out32, count, seed, counter, step);
     return cudaGetLastError();
 }
 
-template <int KIND, bool LIST, int MODE>
+template <int KIND, bool LIST, int MODE, int GW = 32>
 static cudaError_t launch_sweep_t(const SweepArgs &a, unsigned blocks, int threads, size_t smem, cudaStream_t st) {
-    cudaError_t e = cudaFuncSetAttribute(k_sweep<KIND, LIST, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(k_sweep<KIND, LIST, MODE, GW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    k_sweep<KIND, LIST, MODE><<<blocks, threads, smem, st>>>(a);
+    k_sweep<KIND, LIST, MODE, GW><<<blocks, threads, smem, st>>>(a);
     return cudaGetLastError();
+}
+
+// The plain scan of spheres or spherocylinders with two cells per warp: `ncells` lane groups
+// of 16 (a.cap sized for sweep_smem_per_half).
+cudaError_t launch_sweep_half(const SweepArgs &a, int ncells, cudaStream_t st) {
+    if (ncells <= 0) return cudaSuccess;
+    const int groups_per_block = SWEEP_WARPS * 2;
+    const size_t smem = sweep_smem_per_half(a.s.kind, a.cap) * groups_per_block;
+    const unsigned blocks = (unsigned)((ncells + groups_per_block - 1) / groups_per_block);
+    const int th = SWEEP_WARPS * 32;
+    return a.s.kind == 0 ? launch_sweep_t<0, false, 0, 16>(a, blocks, th, smem, st)
+                         : launch_sweep_t<1, false, 0, 16>(a, blocks, th, smem, st);
 }
 
 cudaError_t launch_sweep(const SweepArgs &a, bool list, int nwarps, cudaStream_t st) {

@@ -264,6 +264,10 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
     constexpr bool RT = MODE == 3;  // every move a rototranslation (the plain scan otherwise)
     const Grp<GW> grp;
     const int lane = grp.lane;
+    // two cells per warp (GW = 16): spherocylinder axes are read from the L2-resident FP32
+    // mirror through each candidate's mirror slot instead of being staged, which halves the
+    // shared memory per cell
+    constexpr bool AXM = GW == 16 && KIND == 1;
     const unsigned lt = (1u << lane) - 1u;
     const DevState &S = A.s;
     const GridDev &G = A.g;
@@ -359,8 +363,8 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                 p.y += off[r].y;
                 p.z += off[r].z;
                 cpos[base + k] = p;
-                if (KIND == 1) cax[base + k] = G.maxis[st[r] + k];
-                if (KIND == 2) cslot[base + k] = (uint32_t)(st[r] + k);  // its centres stay in the L2-resident mirror
+                if (KIND == 1 && !AXM) cax[base + k] = G.maxis[st[r] + k];
+                if (KIND == 2 || AXM) cslot[base + k] = (uint32_t)(st[r] + k);  // its centres stay in the L2-resident mirror
             }
         } else {
             int j = pre[r];
@@ -371,8 +375,8 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                 p.y += off[r].y;
                 p.z += off[r].z;
                 cpos[j] = p;
-                if (KIND == 1) cax[j] = G.maxis[st[r] + k];
-                if (KIND == 2) cslot[j] = (uint32_t)(st[r] + k);
+                if (KIND == 1 && !AXM) cax[j] = G.maxis[st[r] + k];
+                if (KIND == 2 || AXM) cslot[j] = (uint32_t)(st[r] + k);
                 j++;
             }
         }
@@ -511,6 +515,22 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                     for (int q = 0; q < 9; q++) R32[q] = rot_inv ? R[3 * (q % 3) + q / 3] : R[q];
                 }
             }
+            if (KIND >= 1) {
+                // the next move's rotation-table entries (its Philox words are in the group
+                // already) into L1 now, off that move's critical path: the FP32 entry the
+                // filter reads and the FP64 one a surviving move reads (48 and 72 bytes,
+                // first and last byte of each)
+                const int nsrc = (mi + 1) & (GW - 1);
+                const uint32_t qa = grp.shfl(rnd_lane.a, nsrc), qb = grp.shfl(rnd_lane.b, nsrc),
+                               qc = grp.shfl(rnd_lane.c, nsrc);
+                const bool qrot = rt || (ntypes == 2 ? (qa >> 31) != 0 : (A.types & 1) == 0);
+                if (nsrc != 0 && mi + 1 < nmoves && qrot && lane < 4) {
+                    const uint32_t qi = rt ? (((qb & 0xffu) | ((qc & 0xffu) << 8)) & A.rtab_mask) : (qb & A.rtab_mask);
+                    const char *pf = lane < 2 ? reinterpret_cast<const char *>(A.rtab32 + 12 * (size_t)qi) + 47 * lane
+                                              : reinterpret_cast<const char *>(A.rtab64 + 9 * (size_t)qi) + 71 * (lane - 2);
+                    asm volatile("prefetch.global.L1 [%0];" ::"l"(pf));
+                }
+            }
         }
         const float4 pcur = cpos[slot];
         const int pid = __float_as_int(pcur.w);
@@ -520,7 +540,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
         const double rot_own = S.rot64[9 * (size_t)pid + (lane < 9 ? lane : 0)];
         float3 ai = make_float3(0.f, 0.f, 1.f);
         if (KIND == 1) {
-            float4 a = cax[slot];
+            float4 a = AXM ? G.maxis[(size_t)gbase + slot] : cax[slot];
             ai = make_float3(a.x, a.y, a.z);
         }
         float3 pn = make_float3(pcur.x, pcur.y, pcur.z);
@@ -686,7 +706,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                 if (i < nseg) {
                     k = qseg[i];
                     float4 q = cpos[k];
-                    float4 a = cax[k];
+                    float4 a = AXM ? G.maxis[cslot[k]] : cax[k];
                     cls = seg_stage(S.fc, make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z), an,
                                     make_float3(a.x, a.y, a.z));
                 }
@@ -701,7 +721,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                     const unsigned long long idx = base_idx + __popc(bal & lt);
                     if (rec && idx < A.pair_cap) {
                         float4 q = cpos[k];
-                        float4 a = cax[k];
+                        float4 a = AXM ? G.maxis[cslot[k]] : cax[k];
                         float f[MLP_IN];
                         mlp_features(make_float3(q.x - pcur.x, q.y - pcur.y, q.z - pcur.z), ai,
                                      make_float3(a.x, a.y, a.z), A.inv_range, f);
@@ -994,7 +1014,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                 if (pj == pid) continue;
                 float3 aj = make_float3(0.f, 0.f, 1.f);
                 if (KIND == 1) {
-                    const float4 a = cax[k];
+                    const float4 a = AXM ? G.maxis[cslot[k]] : cax[k];
                     aj = make_float3(a.x, a.y, a.z);
                 }
                 const float3 db = make_float3(q.x - pcur.x, q.y - pcur.y, q.z - pcur.z);
@@ -1028,7 +1048,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
             // Packing::acceptMove adds the move's overlap delta in counting mode (core/Packing.cpp:298-300)
             if (COUNT && lane == 0) atomicAdd(S.overlaps, (unsigned long long)(long long)cdelta);
             float4 np = pcur;
-            float4 na = KIND == 1 ? cax[slot] : make_float4(0.f, 0.f, 0.f, 0.f);
+            float4 na = (KIND == 1 && !AXM) ? cax[slot] : make_float4(0.f, 0.f, 0.f, 0.f);
             grp.sync();
             if (type != 1) {
                 if (lane < 3) S.pos64[3 * (size_t)pid + lane] = pnew_own;
@@ -1062,7 +1082,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                 cpos[slot] = np;
                 G.mpos[gslot] = np;
                 if (KIND == 1 && type != 0) {
-                    cax[slot] = na;
+                    if (!AXM) cax[slot] = na;
                     G.maxis[gslot] = na;
                 }
             }
@@ -1084,7 +1104,7 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                     float4 q = cpos[k];
                     if (__float_as_int(q.w) == pid) {
                         cpos[k] = make_float4(np.x + (q.x - pcur.x), np.y + (q.y - pcur.y), np.z + (q.z - pcur.z), q.w);
-                        if (KIND == 1 && type != 0) cax[k] = na;
+                        if (KIND == 1 && type != 0 && !AXM) cax[k] = na;
                     }
                 }
             }

@@ -219,6 +219,10 @@ class GpuPacking:
         """Packing::toggleWalls: bit i puts hard walls across box side i (rp_set_walls)."""
         self._check(self.lib.rp_set_walls(self.h, int(mask)))
 
+    def set_cells_per_warp(self, cells: int):
+        """1: a warp sweeps one cell; 2: each half-warp sweeps its own (rp_set_cells_per_warp)."""
+        self._check(self.lib.rp_set_cells_per_warp(self.h, int(cells)))
+
     def set_staging_filter(self, mode: int = 1):
         """0 off, 1 where it pays (default), 2 wherever valid (rp_set_staging_filter)."""
         self._check(self.lib.rp_set_staging_filter(self.h, int(mode)))
