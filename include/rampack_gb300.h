@@ -442,6 +442,8 @@ int rp_batch_set_walls(void *batch, int32_t mask);
  * way; learned ordering, pair logs, overlap counting, rototranslations, the staging filter,
  * polyspheres and neighbourhoods above the half-warp capacity keep a warp per cell. */
 int rp_set_cells_per_warp(void *handle, int32_t cells);
+/* Cells per warp the last sweep used (1 or 2; 0 before the first sweep). */
+int rp_get_cells_per_warp(void *handle, int32_t *last);
 
 /* Staging filter of the sweep: candidates of the 26 neighbour cells farther than the
  * interaction range from every face-slab of the mover's cell (its ActiveDomain) are not

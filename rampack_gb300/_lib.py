@@ -118,6 +118,7 @@ SIGNATURES = {
     "rp_run_moves": (C.c_int, [_P, _P, C.c_int64, _P]),
     "rp_try_move": (C.c_int, [_P, _P, _D, _D]),
     "rp_set_cells_per_warp": (C.c_int, [_P, C.c_int32]),
+    "rp_get_cells_per_warp": (C.c_int, [_P, C.POINTER(C.c_int32)]),
     "rp_accept_move": (C.c_int, [_P]),
     "rp_sweep": (C.c_int, [_P, C.POINTER(SweepParams), C.POINTER(SweepStats)]),
     "rp_sweep_log": (C.c_int, [_P, _P, _P, C.c_int64, C.POINTER(C.c_int64)]),

@@ -265,6 +265,7 @@ struct Handle {
     // of 16 with the axes read from the mirror, twice the cells in flight per SM)
     int cells_per_warp = 1;
     int half_cap_cached = -1, half_blocks = 0;  // resident blocks per SM at that capacity
+    int last_cells_per_warp = 0;                // what the last sweep's phases used
 };
 
 // One group of kernel launches of a handle or a batch: counted, and bracketed by CUDA events
@@ -605,12 +606,13 @@ int setup_grid(Handle *h, GridHost &G, const double *box, const double *shift) {
     int maxcap = static_cast<int>(48 * 1024 / (sweep_smem_per_warp(h->shape.kind, 32, false, h->ncen) / 32));
     G.cap = std::min(cap, maxcap / 32 * 32);
     // two cells per warp: 32 lane groups per SM (4 blocks of 8) in 220 KB of shared memory;
-    // offered when that holds the same capacity (larger neighbourhoods keep a warp per cell)
+    // offered while that capacity holds the mean neighbourhood plus four standard deviations
+    // (the rare larger neighbourhood reruns in the overflow pass; larger cells keep a warp per cell)
     G.cap_half = 0;
     if (h->shape.kind != RP_SHAPE_POLYSPHERE) {
         const int half_max = static_cast<int>(220 * 1024 / (SWEEP_WARPS * 2 * 4) /
                                               (sweep_smem_per_half(h->shape.kind, 32) / 32)) / 32 * 32;
-        if (G.cap <= half_max) G.cap_half = G.cap;
+        if (mean + 4.0 * std::sqrt(mean) + 16.0 <= half_max) G.cap_half = std::min(G.cap, half_max);
     }
     int64_t nblocks = (ncell + 4095) / 4096;
     RP_CUDA(h, ensure(h->block_sums, h->block_sums_alloc, nblocks));
@@ -1519,6 +1521,7 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
         }
         {
             Group grp(h, RP_KERNEL_SWEEP, 1);
+            h->last_cells_per_warp = (half && h->half_blocks > 0) ? 2 : 1;
             if (half && h->half_blocks > 0) {
                 a.cap = gh.cap_half;
                 const int resident = h->num_sms * h->half_blocks * SWEEP_WARPS * 2;
@@ -2205,6 +2208,13 @@ int rp_set_cells_per_warp(void *handle, int32_t cells) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h || (cells != 1 && cells != 2)) return fail(h, RP_ERR_ARG, "cells per warp must be 1 or 2");
     h->cells_per_warp = cells;
+    return RP_OK;
+}
+
+int rp_get_cells_per_warp(void *handle, int32_t *last) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !last) return RP_ERR_ARG;
+    *last = h->last_cells_per_warp;
     return RP_OK;
 }
 

@@ -223,6 +223,12 @@ class GpuPacking:
         """1: a warp sweeps one cell; 2: each half-warp sweeps its own (rp_set_cells_per_warp)."""
         self._check(self.lib.rp_set_cells_per_warp(self.h, int(cells)))
 
+    def cells_per_warp(self) -> int:
+        """Cells per warp the last sweep used (rp_get_cells_per_warp)."""
+        v = C.c_int32()
+        self._check(self.lib.rp_get_cells_per_warp(self.h, C.byref(v)))
+        return int(v.value)
+
     def set_staging_filter(self, mode: int = 1):
         """0 off, 1 where it pays (default), 2 wherever valid (rp_set_staging_filter)."""
         self._check(self.lib.rp_set_staging_filter(self.h, int(mode)))
