@@ -439,8 +439,8 @@ int rp_batch_set_walls(void *batch, int32_t mask);
 /* Cells a warp sweeps at once in the plain scans of spheres and spherocylinders: 1 (a warp
  * per cell), or 2 (each half-warp sweeps its own cell with the axes read from the FP32 mirror,
  * twice the cells in flight per SM).  Decisions and the proposal stream are the same either
- * way; learned ordering, pair logs, overlap counting, rototranslations, the staging filter,
- * polyspheres and neighbourhoods above the half-warp capacity keep a warp per cell. */
+ * way; learned ordering, pair logs, overlap counting, rototranslations, polyspheres and
+ * neighbourhoods above the half-warp capacity keep a warp per cell. */
 int rp_set_cells_per_warp(void *handle, int32_t cells);
 /* Cells per warp the last sweep used (1 or 2; 0 before the first sweep). */
 int rp_get_cells_per_warp(void *handle, int32_t *last);

@@ -22,6 +22,9 @@
 #include "core/Simulation.h"
 #include "core/ObservablesCollector.h"
 #include "core/observables/NematicOrder.h"
+#include "core/interactions/RepulsiveLennardJonesInteraction.h"
+#include "core/interactions/SquareInverseCoreInteraction.h"
+#include "core/shapes/CompoundShapeTraits.h"
 #include "core/observables/correlation/LayerwiseRadialEnumerator.h"
 #include "core/observables/correlation/LinearEnumerator.h"
 #include "core/observables/correlation/PairAveragedCorrelation.h"
@@ -110,6 +113,8 @@ struct Handle {
     std::unique_ptr<Packing> pk;
     int threads = 1;
     bool counting = false;
+    int kind = 0;
+    std::vector<double> prm;
 };
 
 }  // namespace
@@ -132,6 +137,8 @@ void *ref_create(int kind, const double *prm, int np, int64_t n, const double *p
     h->traits = make_traits(kind, prm, np);
     if (!h->traits) return nullptr;
     h->threads = threads;
+    h->kind = kind;
+    h->prm.assign(prm, prm + np);
     std::vector<Shape> shapes;
     for (int64_t i = 0; i < n; i++)
         shapes.emplace_back(Vector<3>{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]}, load_m(rot + 9 * i));
@@ -146,6 +153,49 @@ void *ref_create(int kind, const double *prm, int np, int64_t n, const double *p
 }
 
 void ref_destroy(void *hp) { delete static_cast<Handle *>(hp); }
+
+// The shape joined with a soft helper on its interaction centres, as casino's overlap
+// relaxation joins a helper shape (frontend/modes/CasinoMode.cpp:288-289): CompoundShapeTraits
+// of the shape and SphereTraits / PolysphereTraits carrying a RepulsiveLennardJones (kind 1) or
+// SquareInverseCore (kind 2) interaction; hard = 0 uses the soft traits alone.  The packing is
+// set up for the new interaction (Packing::setupForInteraction).
+int ref_set_soft(void *hp, int kind, double eps, double sigma, int hard) {
+    auto *h = static_cast<Handle *>(hp);
+    try {
+        std::shared_ptr<CentralInteraction> ci;
+        if (kind == 1) ci = std::make_shared<RepulsiveLennardJonesInteraction>(eps, sigma);
+        else if (kind == 2) ci = std::make_shared<SquareInverseCoreInteraction>(eps, sigma);
+        else return -1;
+        std::shared_ptr<ShapeTraits> soft;
+        if (h->kind == 0 || h->kind == 1) {
+            soft = std::make_shared<SphereTraits>(h->kind == 0 ? h->prm[0] : h->prm[1], ci);
+        } else if (h->kind == 2) {
+            int k = static_cast<int>(h->prm[0]);
+            std::vector<PolysphereTraits::SphereData> data;
+            for (int i = 0; i < k; i++)
+                data.emplace_back(Vector<3>{h->prm[1 + 4 * i], h->prm[2 + 4 * i], h->prm[3 + 4 * i]}, h->prm[4 + 4 * i]);
+            PolysphereTraits::PolysphereGeometry geom(std::move(data), std::nullopt, std::nullopt, {0, 0, 0}, 1.0);
+            soft = std::make_shared<PolysphereTraits>(std::move(geom), ci);
+        } else {
+            return -1;
+        }
+        if (hard) {
+            h->traits = std::make_shared<CompoundShapeTraits>(h->traits, soft);
+        } else {
+            if (h->kind == 1) return -1;
+            h->traits = soft;
+        }
+        h->pk->setupForInteraction(h->traits->getInteraction());
+    } catch (const std::exception &) {
+        return -1;
+    }
+    return 0;
+}
+
+double ref_total_energy(void *hp) {
+    auto *h = static_cast<Handle *>(hp);
+    return h->pk->getTotalEnergy(h->traits->getInteraction());
+}
 
 // NematicOrder::calculate (core/observables/NematicOrder.cpp:9-28) of the handle's packing
 // with the Q tensor dumped: out7 = P2, Q_11, Q_12, Q_13, Q_22, Q_23, Q_33.
@@ -183,8 +233,16 @@ int64_t ref_cached_overlaps(void *hp) {
     return static_cast<int64_t>(static_cast<Handle *>(hp)->pk->getCachedNumberOfOverlaps());
 }
 
+int ref_replay_energies(void *hp, const ref_move *mv, int64_t n, const double *domains, double temperature,
+                        uint8_t *out_code, int32_t *out_delta, double *out_energy);
+
 int ref_replay(void *hp, const ref_move *mv, int64_t n, const double *domains, double temperature,
                uint8_t *out_code, int32_t *out_delta) {
+    return ref_replay_energies(hp, mv, n, domains, temperature, out_code, out_delta, nullptr);
+}
+
+int ref_replay_energies(void *hp, const ref_move *mv, int64_t n, const double *domains, double temperature,
+                        uint8_t *out_code, int32_t *out_delta, double *out_energy) {
     auto *h = static_cast<Handle *>(hp);
     Packing &pk = *h->pk;
     const Interaction &inter = h->traits->getInteraction();
@@ -227,6 +285,7 @@ int ref_replay(void *hp, const ref_move *mv, int64_t n, const double *domains, d
                 code |= 0x80;
             }
             out_code[i] = code;
+            if (out_energy) out_energy[i] = dE;
             if (out_delta)
                 out_delta[i] = h->counting
                                    ? (acc ? static_cast<int32_t>(pk.getCachedNumberOfOverlaps() - before) : 0)

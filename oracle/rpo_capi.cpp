@@ -98,6 +98,29 @@ void *rpo_create(int kind, const double *prm, int np, int64_t n, const double *p
 
 void rpo_destroy(void *hp) { delete static_cast<Handle *>(hp); }
 
+// A soft part joined to the shape's hard interaction (CompoundInteraction with a central
+// helper on the same interaction centres): kind 1 RepulsiveLennardJones, 2 SquareInverseCore;
+// hard = 0 keeps the soft part alone (spheres and polyspheres).  The packing is set up
+// again for the compound's range (Packing::setupForInteraction).
+int rpo_set_soft(void *hp, int kind, double eps, double sigma, int hard) {
+    auto *h = static_cast<Handle *>(hp);
+    if (kind < 1 || kind > 2 || !(sigma > 0) || (kind == 1 && !(eps > 0)) || (kind == 2 && eps == 0)) return -1;
+    if (!hard && (h->inter.kind == SPHEROCYLINDER || h->inter.segments())) return -1;
+    h->inter.set_soft(kind, eps, sigma, hard != 0);
+    try {
+        h->pk->setup_for_interaction(h->inter);
+    } catch (const std::exception &) {
+        return -1;
+    }
+    return 0;
+}
+
+// Packing::getTotalEnergy (core/Packing.cpp:689-709)
+double rpo_total_energy(void *hp) {
+    auto *h = static_cast<Handle *>(hp);
+    return h->pk->total_energy(h->inter);
+}
+
 int64_t rpo_size(void *hp) { return static_cast<int64_t>(static_cast<Handle *>(hp)->pk->size()); }
 
 int64_t rpo_count_overlaps(void *hp, int early) {
@@ -126,8 +149,17 @@ int64_t rpo_cached_overlaps(void *hp) { return static_cast<int64_t>(static_cast<
 // low two bits 0 = dE 0, 1 = overlap (+inf), 2 = outside the active domain (+inf),
 // 3 = -inf (fewer overlaps, counting mode); bit 7 = accepted.  out_delta (optional)
 // receives the overlap-count delta in counting mode.
+int rpo_replay_energies(void *hp, const rpo_move *mv_, int64_t n, const double *domains, double temperature,
+                        uint8_t *out_code, int32_t *out_delta, double *out_energy);
+
 int rpo_replay(void *hp, const rpo_move *mv_, int64_t n, const double *domains, double temperature,
                uint8_t *out_code, int32_t *out_delta) {
+    return rpo_replay_energies(hp, mv_, n, domains, temperature, out_code, out_delta, nullptr);
+}
+
+// As rpo_replay, also writing each move's energy (0, +-inf, or the soft energy change).
+int rpo_replay_energies(void *hp, const rpo_move *mv_, int64_t n, const double *domains, double temperature,
+                        uint8_t *out_code, int32_t *out_delta, double *out_energy) {
     auto *h = static_cast<Handle *>(hp);
     Packing &pk = *h->pk;
     try {
@@ -153,6 +185,7 @@ int rpo_replay(void *hp, const rpo_move *mv_, int64_t n, const double *domains, 
                 code |= 0x80;
             }
             out_code[i] = code;
+            if (out_energy) out_energy[i] = dE;
             if (out_delta) out_delta[i] = (pk.counting && acc) ? pk.last_delta[0] : 0;
         }
     } catch (const std::exception &) {

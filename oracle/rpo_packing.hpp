@@ -53,13 +53,53 @@ struct Interaction {
     // this body-frame half axis (SpherocylinderData::halfAxis); empty for polyspheres
     std::vector<V3> half_axes;
 
+    // Soft part: a CentralInteraction helper installed on the same interaction centres and
+    // joined to the hard shape by CompoundInteraction (core/interactions/CompoundInteraction.cpp:9-49):
+    // 0 none, 1 RepulsiveLennardJonesInteraction (RepulsiveLennardJonesInteraction.cpp:9-22),
+    // 2 SquareInverseCoreInteraction (SquareInverseCoreInteraction.cpp:8-15); `hard` false
+    // leaves the soft part alone (SphereTraits(r, centralInteraction), no hard core)
+    int soft = 0;
+    double soft_eps = 0, soft_sigma = 0;
+    double soft_cut = 0;   // RepulsiveLennardJones: sigma * std::pow(2., 1./6)
+    bool hard = true;
+
+    void set_soft(int kind, double eps, double sigma, bool with_hard) {
+        soft = kind;
+        soft_eps = eps;
+        soft_sigma = sigma;
+        soft_cut = sigma * std::pow(2., 1. / 6);
+        hard = with_hard;
+    }
+    // CentralInteraction::getRangeRadius of the potential (RepulsiveLennardJonesInteraction.h:26,
+    // SquareInverseCoreInteraction.h:22)
+    double soft_range() const { return soft == 1 ? soft_cut : (soft == 2 ? soft_sigma : 0.0); }
+    // calculateEnergyForDistance2
+    double energy_for_distance2(double d2) const {
+        if (soft == 1) {
+            if (d2 >= soft_cut * soft_cut) return 0;
+            double x2 = soft_sigma * soft_sigma / d2;
+            double x6 = x2 * x2 * x2;
+            double x12 = x6 * x6;
+            return 4 * soft_eps * (x12 - x6) + soft_eps;
+        }
+        if (soft == 2) return soft_eps * std::max(0.0, std::pow(soft_sigma, 2) / d2 - 1);
+        return 0;
+    }
+    // CentralInteraction::calculateEnergyBetween (core/interactions/CentralInteraction.h:55-63)
+    double energy(const V3 &p1, const V3 &p2, const BC &bc) const { return energy_for_distance2(bc.distance2(p1, p2)); }
+
     bool segments() const { return !half_axes.empty(); }
     // SpherocylinderData::circumsphereRadius = radius + |halfAxis|
     // (PolyspherocylinderTraits.cpp:78-84)
     double circumsphere(std::size_t i) const { return radii[i] + std::sqrt(norm2(half_axes[i])); }
 
-    // SphereTraits.h:34, SpherocylinderTraits.h:81, PolysphereTraits.cpp:115-121
+    // CompoundInteraction: the larger of the hard and the soft range (CompoundInteraction.cpp:33-35)
     double range() const {
+        if (!soft) return hard_range();
+        return hard ? std::max(hard_range(), soft_range()) : soft_range();
+    }
+    // SphereTraits.h:34, SpherocylinderTraits.h:81, PolysphereTraits.cpp:115-121
+    double hard_range() const {
         if (kind == SPHERE) return 2 * radius;
         if (kind == SPHEROCYLINDER) return 2 * radius + length;
         if (segments()) {   // PolyspherocylinderTraits.cpp:140-147
@@ -70,7 +110,8 @@ struct Interaction {
         }
         return 2 * *std::max_element(radii.begin(), radii.end());
     }
-    // Interaction.cpp:55-70
+    // Interaction.cpp:55-70 (both parts share the interaction centres, so the compound's
+    // larger total range is the larger range plus the centres' extent)
     double total_range() const {
         double r = range();
         if (kind != POLYSPHERE) return r;
@@ -83,6 +124,7 @@ struct Interaction {
     // overlapWithWall: SphereTraits.cpp:67-75, SpherocylinderTraits.cpp:56-73 (either cap
     // closer to the wall plane than the radius), PolysphereTraits.cpp:129-136 (centre idx)
     bool overlap_with_wall(const V3 &pos, const M3 &rot, std::size_t idx, const V3 &origin, const V3 &wall) const {
+        if (!hard) return false;   // a soft part has no wall part (CentralInteraction.h:48)
         if (kind == SPHERE) return dot(wall, sub(pos, origin)) < radius;
         if (kind == POLYSPHERE && segments()) {   // PolyspherocylinderTraits.cpp:149-166
             V3 half = mv(rot, half_axes[idx]);
@@ -96,7 +138,8 @@ struct Interaction {
         if (dot(wall, sub(sub(pos, half), origin)) < radius) return true;
         return false;
     }
-    bool convex() const { return kind != POLYSPHERE; }
+    // CompoundInteraction::isConvex (CompoundInteraction.cpp:25-30): the hard part's, none without
+    bool convex() const { return hard && kind != POLYSPHERE; }
 
     // SpherocylinderTraits.cpp:23-25
     V3 cap(int sign, const V3 &pos, const M3 &rot) const {
@@ -105,6 +148,7 @@ struct Interaction {
 
     bool overlap(const V3 &p1, const M3 &o1, std::size_t i1, const V3 &p2, const M3 &o2, std::size_t i2,
                  const BC &bc) const {
+        if (!hard) return false;   // no hard part: nothing overlaps
         if (kind == SPHERE) {
             // SphereTraits.cpp:56-65
             return bc.distance2(p1, p2) < std::pow(2 * radius, 2);
@@ -510,6 +554,106 @@ public:
         return cnt;
     }
 
+    // ----- soft energies: Packing.cpp:649-687 (calculateParticleEnergy), :711-764 -----
+    double particle_energy(std::size_t orig, std::size_t temp, const Interaction &inter) const {
+        if (!inter.soft) return 0;
+        double energy = 0;
+        if (ng.has_value()) {
+            if (num_centres == 0) {
+                const V3 &pos = shapes[temp].pos;
+                std::size_t cell_no = ng->position_to_cell(pos);
+                for (std::size_t off : ng->offsets) {
+                    std::size_t nb = cell_no + off;
+                    BC bc = BC::fixed(ng->translations[ng->trans_idx[nb]]);
+                    for (std::size_t j = ng->heads[ng->reflected[nb]]; j != NeighbourGrid::END; j = ng->succ[j]) {
+                        if (orig == j) continue;
+                        energy += inter.energy(pos, shapes[j].pos, bc);
+                    }
+                }
+            } else {
+                for (std::size_t c1 = 0; c1 < num_centres; c1++) energy += centre_energy_ng(orig, temp, c1, inter);
+            }
+        } else {
+            for (std::size_t j = 0; j < size(); j++) {
+                if (orig == j) continue;
+                energy += pair_energy_no_ng(temp, j, inter);
+            }
+        }
+        return energy;
+    }
+
+    // Packing::calculateInteractionCentreEnergyWithNG (core/Packing.cpp:740-764)
+    double centre_energy_ng(std::size_t orig, std::size_t temp, std::size_t c1, const Interaction &inter) const {
+        double energy = 0;
+        V3 p1 = abs_centres[temp * num_centres + c1];
+        std::size_t cell_no = ng->position_to_cell(p1);
+        for (std::size_t off : ng->offsets) {
+            std::size_t nb = cell_no + off;
+            BC bc = BC::fixed(ng->translations[ng->trans_idx[nb]]);
+            for (std::size_t ci2 = ng->heads[ng->reflected[nb]]; ci2 != NeighbourGrid::END; ci2 = ng->succ[ci2]) {
+                std::size_t j = ci2 / num_centres;
+                if (j == orig) continue;
+                energy += inter.energy(p1, abs_centres[ci2], bc);
+            }
+        }
+        return energy;
+    }
+
+    // Packing::calculateEnergyBetweenParticlesWithoutNG (core/Packing.cpp:711-738)
+    double pair_energy_no_ng(std::size_t temp, std::size_t other, const Interaction &inter) const {
+        BC bc = BC::periodic(box);
+        if (num_centres == 0) return 0.0 + inter.energy(shapes[temp].pos, shapes[other].pos, bc);
+        double energy = 0;
+        for (std::size_t c1 = 0; c1 < num_centres; c1++)
+            for (std::size_t c2 = 0; c2 < num_centres; c2++)
+                energy += inter.energy(abs_centres[temp * num_centres + c1], abs_centres[other * num_centres + c2], bc);
+        return energy;
+    }
+
+    // Packing::getTotalEnergyNGCellHelper (core/Packing.cpp:766-836)
+    double total_energy_cell_helper(const std::array<std::size_t, 3> &coord, const Interaction &inter) const {
+        double energy = 0;
+        std::size_t cell_no = ng->real_coords_to_cell(coord);
+        BC zero = BC::fixed({});
+        for (std::size_t a = ng->heads[cell_no]; a != NeighbourGrid::END; a = ng->succ[a]) {
+            std::size_t pa = num_centres == 0 ? a : a / num_centres;
+            const V3 &p1 = num_centres == 0 ? shapes[pa].pos : abs_centres[a];
+            for (std::size_t b = ng->succ[a]; b != NeighbourGrid::END; b = ng->succ[b]) {
+                std::size_t pb = num_centres == 0 ? b : b / num_centres;
+                if (num_centres != 0 && pa == pb) continue;
+                energy += inter.energy(p1, num_centres == 0 ? shapes[pb].pos : abs_centres[b], zero);
+            }
+            for (std::size_t off : ng->positive_offsets) {
+                std::size_t nb = cell_no + off;
+                BC bc = BC::fixed(ng->translations[ng->trans_idx[nb]]);
+                for (std::size_t b = ng->heads[ng->reflected[nb]]; b != NeighbourGrid::END; b = ng->succ[b]) {
+                    std::size_t pb = num_centres == 0 ? b : b / num_centres;
+                    if (num_centres != 0 && pa == pb) continue;
+                    energy += inter.energy(p1, num_centres == 0 ? shapes[pb].pos : abs_centres[b], bc);
+                }
+            }
+        }
+        return energy;
+    }
+
+    // Packing::getTotalEnergy (core/Packing.cpp:689-709): cells in parallel with an OpenMP sum
+    // (one thread reproduces the reference's serial order)
+    double total_energy(const Interaction &inter) const {
+        if (!inter.soft) return 0;
+        double energy = 0;
+        if (ng.has_value()) {
+            auto d = ng->real_divisions();
+            #pragma omp parallel for collapse(3) reduction(+ : energy) num_threads(scaling_threads)
+            for (std::size_t i = 0; i < d[0]; i++)
+                for (std::size_t j = 0; j < d[1]; j++)
+                    for (std::size_t k = 0; k < d[2]; k++) energy += total_energy_cell_helper({i, j, k}, inter);
+        } else {
+            for (std::size_t i = 0; i < size(); i++)
+                for (std::size_t j = i + 1; j < size(); j++) energy += pair_energy_no_ng(i, j, inter);
+        }
+        return energy;
+    }
+
     // Packing::countWallOverlaps (core/Packing.cpp:561-580)
     std::size_t count_wall_overlaps(const Interaction &inter, bool early) const {
         if (!has_any_walls) return 0;
@@ -636,6 +780,7 @@ public:
 
     // ----- moves: Packing.cpp:84-164, :304-323 -----
     double move_overlap_energy(std::size_t idx, std::size_t temp, const Interaction &inter) {
+        if (!inter.hard) return 0;   // no hard part (core/Packing.cpp:307)
         if (counting) {
             std::size_t before = count_particle_overlaps(idx, idx, inter, false);
             std::size_t after = count_particle_overlaps(idx, temp, inter, false);
@@ -695,7 +840,12 @@ public:
             if (type != 0) rotate_temp_centres(r);
             recalc_abs_centres(temp);
         }
-        return move_overlap_energy(idx, temp, inter);
+        double overlap_energy = move_overlap_energy(idx, temp, inter);
+        if (overlap_energy != 0 || !inter.soft) return overlap_energy;
+        // soft part: the particle's energy after the move minus before (core/Packing.cpp:103-108)
+        double initial = particle_energy(idx, idx, inter);
+        double final_ = particle_energy(idx, temp, inter);
+        return final_ - initial;
     }
 
     // Packing.cpp:234-302 (acceptTranslation / acceptRotation / acceptMove share this
@@ -748,6 +898,7 @@ public:
     double try_scaling(const Box &nb, const Interaction &inter) {
         last_box = box;
         last_shapes = shapes;
+        double initial_energy = total_energy(inter);   // core/Packing.cpp:178
         last_scaling_overlaps = num_overlaps;
         box = nb;
         std::size_t n = size();
@@ -756,16 +907,19 @@ public:
         std::swap(ng, temp_ng);
         if (num_centres != 0) recalc_abs_centres();
         rebuild_ng();
-        if (counting) {
-            num_overlaps = count_total_overlaps(inter, false);
-            int delta = static_cast<int>(num_overlaps) - static_cast<int>(last_scaling_overlaps);
-            if (delta < 0) return -INF;
-            if (delta > 0) return INF;
-        } else {
-            bool cannot = inter.convex() && box_upscaled(last_box, box);
-            if (!cannot && count_total_overlaps(inter, true) > 0) return INF;
+        if (inter.hard) {   // core/Packing.cpp:191-203
+            if (counting) {
+                num_overlaps = count_total_overlaps(inter, false);
+                int delta = static_cast<int>(num_overlaps) - static_cast<int>(last_scaling_overlaps);
+                if (delta < 0) return -INF;
+                if (delta > 0) return INF;
+            } else {
+                bool cannot = inter.convex() && box_upscaled(last_box, box);
+                if (!cannot && count_total_overlaps(inter, true) > 0) return INF;
+            }
         }
-        return 0;
+        double final_energy = total_energy(inter);
+        return final_energy - initial_energy;
     }
 
     void revert_scaling() {

@@ -310,13 +310,21 @@ public:
         return Box(d);
     }
 
-    // Simulation.cpp:493-531 (hard bodies, no overlap counting)
+    // Simulation.cpp:493-531
     bool try_scaling() {
         auto &mt = mts.front();
         Box nb = propose_box(mt);
         double oldV = std::abs(pk.box.volume()), newV = std::abs(nb.volume());
         double dV = newV - oldV, factor = newV / oldV;
         double N = static_cast<double>(pk.size());
+        if (inter.soft || pk.counting) {
+            // a nontrivial energy change (soft part, or counted overlaps): scaling tried first
+            double dE = pk.try_scaling(nb, inter);
+            double exponent = N * std::log(factor) - dE / p.temperature - p.pressure * dV / p.temperature;
+            if (unit(mt) <= std::exp(exponent)) return true;
+            pk.revert_scaling();
+            return false;
+        }
         double expo = N * std::log(factor) - p.pressure * dV / p.temperature;
         if (unit(mt) > std::exp(expo)) return false;
         if (pk.try_scaling(nb, inter) > 0) {

@@ -605,13 +605,14 @@ int setup_grid(Handle *h, GridHost &G, const double *box, const double *shift) {
     cap = (cap + 31) / 32 * 32;
     int maxcap = static_cast<int>(48 * 1024 / (sweep_smem_per_warp(h->shape.kind, 32, false, h->ncen) / 32));
     G.cap = std::min(cap, maxcap / 32 * 32);
-    // two cells per warp: 32 lane groups per SM (4 blocks of 8) in 220 KB of shared memory;
-    // offered while that capacity holds the mean neighbourhood plus four standard deviations
-    // (the rare larger neighbourhood reruns in the overflow pass; larger cells keep a warp per cell)
+    // two cells per warp: 32 lane groups per SM (4 blocks of 8) in 224 KB of shared memory
+    // (capacities in multiples of 16); offered while that capacity holds the mean
+    // neighbourhood plus four standard deviations (the rare larger neighbourhood reruns in the
+    // overflow pass; larger neighbourhoods keep a warp per cell)
     G.cap_half = 0;
     if (h->shape.kind != RP_SHAPE_POLYSPHERE) {
-        const int half_max = static_cast<int>(220 * 1024 / (SWEEP_WARPS * 2 * 4) /
-                                              (sweep_smem_per_half(h->shape.kind, 32) / 32)) / 32 * 32;
+        const int half_max = static_cast<int>(224 * 1024 / (SWEEP_WARPS * 2 * 4) /
+                                              (sweep_smem_per_half(h->shape.kind, 16) / 16)) / 16 * 16;
         if (mean + 4.0 * std::sqrt(mean) + 16.0 <= half_max) G.cap_half = std::min(G.cap, half_max);
     }
     int64_t nblocks = (ncell + 4095) / 4096;
@@ -1514,7 +1515,7 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
         // two cells per warp for the plain scans of spheres and spherocylinders
         const GridHost &gh = h->grid[h->gcur];
         const bool half = h->cells_per_warp == 2 && gh.cap_half > 0 && !h->counting && types != SWEEP_ROTOTRANSLATION &&
-                          a.partners == nullptr && a.pair_every == 0 && !g.stage_filter;
+                          a.partners == nullptr && a.pair_every == 0;
         if (half && h->half_cap_cached != gh.cap_half) {
             h->half_blocks = sweep_half_blocks_per_sm(h->shape.kind, gh.cap_half);
             h->half_cap_cached = gh.cap_half;
