@@ -91,6 +91,9 @@ def _lib(which: str):
         "rotation": (None, [_D, C.c_double, _D]),
         "rng_create": (_P, [C.c_uint64]),
         "rng_destroy": (None, [_P]),
+        "set_soft": (C.c_int, [_P, C.c_int, C.c_double, C.c_double, C.c_int]),
+        "total_energy": (C.c_double, [_P]),
+        "replay_energies": (C.c_int, [_P, _P, C.c_int64, _D, C.c_double, _P, _P, _D]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, pre + name)
@@ -194,17 +197,31 @@ class CpuPacking:
     def cached_overlaps(self) -> int:
         return int(self._f("cached_overlaps")(self.h))
 
-    def replay(self, moves: np.ndarray, domains: np.ndarray | None = None, temperature: float = 1.0):
+    def replay(self, moves: np.ndarray, domains: np.ndarray | None = None, temperature: float = 1.0,
+               energies: bool = False):
+        """Codes and overlap-count deltas of the moves replayed in order; with `energies` also
+        each move's energy (0, +-inf or the soft energy change)."""
         moves = np.ascontiguousarray(moves, dtype=MOVE_DTYPE)
         codes = np.zeros(len(moves), dtype=np.uint8)
         deltas = np.zeros(len(moves), dtype=np.int32)
+        de = np.zeros(len(moves), dtype=np.float64)
         dom = None if domains is None else np.ascontiguousarray(domains, dtype=np.float64)
-        rc = self._f("replay")(self.h, moves.ctypes.data_as(C.c_void_p), len(moves),
-                               None if dom is None else _dp(dom), temperature,
-                               codes.ctypes.data_as(C.c_void_p), deltas.ctypes.data_as(C.c_void_p))
+        rc = self._f("replay_energies")(self.h, moves.ctypes.data_as(C.c_void_p), len(moves),
+                                        None if dom is None else _dp(dom), temperature,
+                                        codes.ctypes.data_as(C.c_void_p), deltas.ctypes.data_as(C.c_void_p), _dp(de))
         if rc != 0:
             raise RuntimeError("replay failed")
-        return codes, deltas
+        return (codes, deltas, de) if energies else (codes, deltas)
+
+    def set_soft(self, kind: int, epsilon: float, sigma: float, hard: bool = True) -> None:
+        """A soft central interaction on the shape's interaction centres: kind 1
+        RepulsiveLennardJones, 2 SquareInverseCore, joined to the hard shape (or alone)."""
+        if self._f("set_soft")(self.h, int(kind), float(epsilon), float(sigma), 1 if hard else 0) != 0:
+            raise ValueError("soft interaction refused")
+
+    def total_energy(self) -> float:
+        """Packing::getTotalEnergy."""
+        return float(self._f("total_energy")(self.h))
 
     def try_scaling(self, box: np.ndarray) -> float:
         b = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
