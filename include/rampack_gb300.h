@@ -436,6 +436,29 @@ int rp_count_overlaps_static(const rp_shape_desc *shape, int64_t n, const double
 int rp_set_walls(void *handle, int32_t mask);
 int rp_batch_set_walls(void *batch, int32_t mask);
 
+/* ---- soft interactions ----------------------------------------------------------- */
+
+#define RP_SOFT_NONE 0
+#define RP_SOFT_REPULSIVE_LJ 1          /* RepulsiveLennardJonesInteraction(epsilon, sigma) (WCA) */
+#define RP_SOFT_SQUARE_INVERSE_CORE 2   /* SquareInverseCoreInteraction(epsilon, sigma) */
+#define RP_SOFT_LENNARD_JONES 3         /* LennardJonesInteraction: refused (no cut-off, see rp_set_soft) */
+
+/* Joins a central potential on the shape's interaction centres (the particle position; the
+ * centres of polyspheres) to its hard interaction, as CompoundShapeTraits /
+ * CompoundInteraction do (core/interactions/CompoundInteraction.cpp:9-49) for casino's
+ * overlap relaxation with a helper shape (frontend/modes/CasinoMode.cpp:288-289); hard = 0
+ * keeps the soft part alone (SphereTraits(r, centralInteraction), PolysphereTraits(geometry,
+ * centralInteraction); spheres and polyspheres).  kind RP_SOFT_NONE removes it.  Moves then
+ * return the energy change (core/Packing.cpp:103-108), box moves the change of the total
+ * energy (:172-207); sweeps decide every move in FP64 at the handle's temperature; move lists
+ * (rp_run_moves) are refused.  Lennard-Jones is refused: it has no cut-off, so the
+ * reference's particle energy sums over whatever its neighbour-grid cells hold. */
+int rp_set_soft(void *handle, int32_t kind, double epsilon, double sigma, int32_t hard);
+/* The Metropolis temperature of sweeps with a soft part (default 1; rp_sim sets it). */
+int rp_set_temperature(void *handle, double temperature);
+/* Packing::getTotalEnergy (core/Packing.cpp:689-764): the soft energy of all pairs. */
+int rp_total_energy(void *handle, double *energy);
+
 /* Cells a warp sweeps at once in the plain scans of spheres and spherocylinders: 1 (a warp
  * per cell), or 2 (each half-warp sweeps its own cell with the axes read from the FP32 mirror,
  * twice the cells in flight per SM).  Decisions and the proposal stream are the same either

@@ -118,6 +118,9 @@ SIGNATURES = {
     "rp_run_moves": (C.c_int, [_P, _P, C.c_int64, _P]),
     "rp_try_move": (C.c_int, [_P, _P, _D, _D]),
     "rp_set_cells_per_warp": (C.c_int, [_P, C.c_int32]),
+    "rp_set_soft": (C.c_int, [_P, C.c_int32, C.c_double, C.c_double, C.c_int32]),
+    "rp_set_temperature": (C.c_int, [_P, C.c_double]),
+    "rp_total_energy": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "rp_get_cells_per_warp": (C.c_int, [_P, C.POINTER(C.c_int32)]),
     "rp_accept_move": (C.c_int, [_P]),
     "rp_sweep": (C.c_int, [_P, C.POINTER(SweepParams), C.POINTER(SweepStats)]),
@@ -205,6 +208,7 @@ KERNEL_GROUPS = ["sweep", "rebuild", "count", "rescale", "overflow", "order", "m
 MLP_NPARAM = 5313
 MLP_FEATURES = 16
 ORDER_OFF, ORDER_MLP, ORDER_DISTANCE = 0, 1, 2
+SOFT_NONE, SOFT_REPULSIVE_LJ, SOFT_SQUARE_INVERSE_CORE, SOFT_LENNARD_JONES = 0, 1, 2, 3
 BATCH_SEED_STRIDE = 0x9E3779B97F4A7C15
 
 _LIB = None

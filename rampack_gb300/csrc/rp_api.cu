@@ -62,6 +62,8 @@ cudaError_t launch_sweep_half(const SweepArgs &a, int ncells, cudaStream_t st);
 size_t sweep_smem_per_half(int kind, int cap);
 int sweep_half_blocks_per_sm(int kind, int cap);
 cudaError_t launch_try_single(const SingleArgs &a, cudaStream_t st);
+cudaError_t launch_soft_sweep(const SoftSweepArgs &a, int nwarps, cudaStream_t st);
+cudaError_t launch_total_energy(const SingleArgs &a, double *scratch, double *out, cudaStream_t st);
 cudaError_t launch_commit_single(const DevState &s, SingleTry *t, uint8_t *disp_flag, int32_t *disp_list, int slot,
                                  cudaStream_t st);
 
@@ -266,6 +268,15 @@ struct Handle {
     int cells_per_warp = 1;
     int half_cap_cached = -1, half_blocks = 0;  // resident blocks per SM at that capacity
     int last_cells_per_warp = 0;                // what the last sweep's phases used
+    // soft part (rp_set_soft): a central potential on the interaction centres joined to the
+    // hard shape (CompoundInteraction), or alone; the shape's own ranges are kept to undo it
+    int soft = 0;
+    bool soft_only = false;
+    double soft_eps = 0, soft_sigma = 0, soft_cut = 0;
+    bool hard_ranges_saved = false;
+    double hard_range = 0, hard_ref_range = 0, hard_total_range = 0;
+    double temperature = 1.0;       // the Metropolis temperature of soft sweeps
+    double *d_energy = nullptr;     // [n] per-particle pair energies, then their sum at [n]
 };
 
 // One group of kernel launches of a handle or a batch: counted, and bracketed by CUDA events
@@ -413,7 +424,12 @@ DevState dev_state(Handle *h) {
     }
     s.counting = h->counting ? 1 : 0;
     s.overlaps = h->d_overlaps;
-    s.walls = h->walls;
+    s.walls = h->soft_only ? 0 : h->walls;   // a soft part alone has no wall part
+    s.soft = h->soft;
+    s.soft_only = h->soft_only ? 1 : 0;
+    s.soft_eps = h->soft_eps;
+    s.soft_sigma = h->soft_sigma;
+    s.soft_cut = h->soft_cut;
     if (h->walls) {
         // Packing::countParticleWallOverlaps (core/Packing.cpp:1089-1101): the box sides
         // (TriclinicBox::getSides: box · e_i, accumulated from zero), the far corner as their
@@ -1127,6 +1143,7 @@ int rp_destroy(void *handle) {
     cudaFree(h->cq_buf);
     cudaFree(h->cq_count);
     cudaFree(h->d_try);
+    cudaFree(h->d_energy);
     cudaFree(h->d_disp_list);
     cudaFree(h->d_disp_flag);
     cudaFree(h->flag);
@@ -1227,6 +1244,10 @@ int rp_count_overlaps(void *handle, int early_exit, int64_t *out_count) {
     if (!h || !out_count) return fail(h, RP_ERR_ARG, "null argument");
     if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
     RP_CUDA(h, cudaSetDevice(h->device));
+    if (h->soft_only) {  // no hard part: nothing overlaps
+        *out_count = 0;
+        return RP_OK;
+    }
     {
         int rg = ensure_grid(h);  // an upload defers the grid
         if (rg) return rg;
@@ -1336,6 +1357,7 @@ int rp_get_grid(void *handle, rp_grid_info *info, int32_t *cell_of_particle, dou
 int rp_run_moves(void *handle, const rp_move *moves, int64_t n, uint8_t *out_codes) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h || (!moves && n > 0)) return fail(h, RP_ERR_ARG, "null argument");
+    if (h->soft) return fail(h, RP_ERR_UNSUPPORTED, "move lists with a soft part (use rp_try_move or rp_sweep)");
     if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
     if (n <= 0) return RP_OK;
     if (n > (1ll << 31) - 1) return fail(h, RP_ERR_ARG, "too many moves");
@@ -1480,8 +1502,48 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
         if (rc2) return rc2;
     }
     h->since_rank++;
+    if (h->soft) {
+        // a soft part: every move decided in FP64 (hard part, then the energy change with the
+        // Metropolis test at the handle's temperature), one warp per active cell
+        if (types == SWEEP_ROTOTRANSLATION) return fail(h, RP_ERR_UNSUPPORTED, "rototranslations with a soft part");
+        SoftSweepArgs sa{};
+        sa.c.s = dev_state(h);
+        sa.c.g = g;
+        sa.c.temperature = h->temperature;
+        double pmax = 0;
+        for (int i = 0; i < 3; i++)
+            pmax = std::max(pmax, std::fabs(h->box[3 * i]) + std::fabs(h->box[3 * i + 1]) + std::fabs(h->box[3 * i + 2]));
+        const double reach = h->range * (1.0 + 1e-3) + 1e-4 * (pmax + h->range);
+        sa.c.reach2 = static_cast<float>(reach * reach);
+        for (int i = 0; i < 9; i++) sa.c.box32[i] = static_cast<float>(h->box[i]);
+        sa.seed = p->seed;
+        sa.counter = p->counter;
+        sa.tstep = static_cast<float>(tstep);
+        sa.types = types;
+        sa.rtab64 = h->rtab64;
+        sa.rtab_mask = ROT_TABLE - 1;
+        if (log) {
+            sa.log = h->d_log;
+            sa.log_codes = h->d_log_codes;
+        }
+        int soft_phase = 0;
+        for (int ph : phases) {
+            int act[3];
+            sa.num_active = phase_cells(g, ph, act);
+            for (int d = 0; d < 3; d++) {
+                sa.phase[d] = phase_digit(ph, d);
+                sa.active[d] = act[d];
+            }
+            sa.next_item = h->item_counters + soft_phase++;
+            Group grp(h, RP_KERNEL_SWEEP, 1);
+            RP_CUDA(h, launch_soft_sweep(sa, std::min(sa.num_active, h->num_sms * 16), h->stream));
+        }
+        // the FP32 mirror no longer follows the moved particles
+        h->grid_stale = true;
+        h->grid_patched = false;
+    }
     int phase_no = 0;
-    for (int ph : phases) {
+    for (int ph : (h->soft ? std::vector<int>{} : phases)) {
         SweepArgs a = base_args(h);
         if (h->order_mode != RP_ORDER_OFF) a.partners = h->partners;
         if (h->pair_cap > 0) {
@@ -1601,6 +1663,40 @@ int rp_sweep_log(void *handle, rp_move *moves, uint8_t *codes, int64_t capacity,
     return RP_OK;
 }
 
+// Packing::getTotalEnergy (core/Packing.cpp:689-764) of the current state on the device
+// (each pair once, a fixed summation order); the grid is rebuilt first if out of date.
+static int soft_total_energy(Handle *h, double *out) {
+    *out = 0.0;
+    if (!h->soft) return RP_OK;
+    int rg = ensure_grid(h);
+    if (rg) return rg;
+    if (!h->d_energy) RP_CUDA(h, cudaMalloc(&h->d_energy, sizeof(double) * (h->n + 1)));
+    SingleArgs a{};
+    a.s = dev_state(h);
+    a.g = h->grid[h->gcur].d;
+    double pmax = 0;
+    for (int i = 0; i < 3; i++)
+        pmax = std::max(pmax, std::fabs(h->box[3 * i]) + std::fabs(h->box[3 * i + 1]) + std::fabs(h->box[3 * i + 2]));
+    const double reach = h->range * (1.0 + 1e-3) + 1e-4 * (pmax + h->range);
+    a.reach2 = static_cast<float>(reach * reach);
+    for (int i = 0; i < 9; i++) a.box32[i] = static_cast<float>(h->box[i]);
+    {
+        Group grp(h, RP_KERNEL_COUNT, 2);
+        RP_CUDA(h, launch_total_energy(a, h->d_energy, h->d_energy + h->n, h->stream));
+    }
+    RP_CUDA(h, cudaMemcpyAsync(out, h->d_energy + h->n, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    return check_status(h);
+}
+
+int rp_total_energy(void *handle, double *energy) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !energy) return fail(h, RP_ERR_ARG, "null argument");
+    if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
+    RP_CUDA(h, cudaSetDevice(h->device));
+    return soft_total_energy(h, energy);
+}
+
 int rp_try_scaling(void *handle, const double *new_box9, double *dE) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h || !new_box9 || !dE) return fail(h, RP_ERR_ARG, "null argument");
@@ -1611,6 +1707,12 @@ int rp_try_scaling(void *handle, const double *new_box9, double *dE) {
     {
         int rg = ensure_grid(h);  // an upload defers the grid
         if (rg) return rg;
+    }
+    // a soft part: the total energy before the rescale (core/Packing.cpp:178)
+    double e0 = 0.0;
+    if (h->soft) {
+        int re = soft_total_energy(h, &e0);
+        if (re) return re;
     }
     int np = 1 - h->pcur, ng = 1 - h->gcur;
     double new_inv[9];
@@ -1648,6 +1750,20 @@ int rp_try_scaling(void *handle, const double *new_box9, double *dE) {
     }
     h->can_revert = true;
     h->log_valid = false;
+    // the soft part's energy change, added where the hard part allows the move
+    // (core/Packing.cpp:205-206)
+    auto soft_change = [&](double *out) -> int {
+        if (!h->soft || std::isinf(*out)) return RP_OK;
+        double e1 = 0.0;
+        int re = soft_total_energy(h, &e1);
+        if (re) return re;
+        *out = e1 - e0;
+        return RP_OK;
+    };
+    if (h->soft_only) {
+        *dE = 0;
+        return soft_change(dE);
+    }
     if (h->counting) {
         // counting mode: the full recount against the count before the move (core/Packing.cpp:189-196)
         RP_CUDA(h, cudaMemcpyAsync(&h->saved_overlaps, h->d_overlaps, sizeof(unsigned long long),
@@ -1661,20 +1777,20 @@ int rp_try_scaling(void *handle, const double *new_box9, double *dE) {
         const long long delta = cnt - static_cast<long long>(h->saved_overlaps);
         *dE = delta < 0 ? -std::numeric_limits<double>::infinity()
                         : (delta > 0 ? std::numeric_limits<double>::infinity() : 0.0);
-        return RP_OK;
+        return soft_change(dE);
     }
     // A convex shape in a box that only grew cannot overlap (core/Packing.cpp:199-200);
     // polyspheres are not convex (PolysphereTraits.h:133).
     if (h->shape.kind != RP_SHAPE_POLYSPHERE && box_upscaled(h->saved_box, h->box)) {
         *dE = 0;
         RP_CUDA(h, cudaStreamSynchronize(h->stream));
-        return RP_OK;
+        return soft_change(dE);
     }
     int64_t cnt = 0;
     rc = rp_count_overlaps(h, 1, &cnt);
     if (rc) return rc;
     *dE = cnt > 0 ? std::numeric_limits<double>::infinity() : 0.0;
-    return RP_OK;
+    return soft_change(dE);
 }
 
 int rp_revert_scaling(void *handle) {
@@ -1936,6 +2052,7 @@ int rp_renormalize_orientations(void *handle, int allow_overlaps, int64_t *rejec
     Handle *h = static_cast<Handle *>(handle);
     if (!h || !rejected) return fail(h, RP_ERR_ARG, "null argument");
     if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
+    if (h->soft) return fail(h, RP_ERR_UNSUPPORTED, "orientation fixes with a soft part");
     RP_CUDA(h, cudaSetDevice(h->device));
     h->try_valid = false;
     {
@@ -2209,6 +2326,80 @@ int rp_set_cells_per_warp(void *handle, int32_t cells) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h || (cells != 1 && cells != 2)) return fail(h, RP_ERR_ARG, "cells per warp must be 1 or 2");
     h->cells_per_warp = cells;
+    return RP_OK;
+}
+
+// CompoundInteraction of the shape's hard interaction and a central potential on the same
+// interaction centres (core/interactions/CompoundInteraction.cpp:9-49), as casino joins a
+// helper shape for overlap relaxation (frontend/modes/CasinoMode.cpp:288-289); or the soft
+// part alone (SphereTraits / PolysphereTraits with a CentralInteraction).
+int rp_set_soft(void *handle, int32_t kind, double epsilon, double sigma, int32_t hard) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h) return RP_ERR_ARG;
+    if (h->batch_member) return fail(h, RP_ERR_UNSUPPORTED, "soft parts on a batch replica");
+    if (kind != RP_SOFT_NONE && kind != RP_SOFT_REPULSIVE_LJ && kind != RP_SOFT_SQUARE_INVERSE_CORE) {
+        if (kind == RP_SOFT_LENNARD_JONES)
+            return fail(h, RP_ERR_UNSUPPORTED,
+                        "Lennard-Jones has no cut-off: the reference's energy then depends on its neighbour-grid cells");
+        return fail(h, RP_ERR_ARG, "unknown soft interaction");
+    }
+    if (kind != RP_SOFT_NONE) {
+        if (!(sigma > 0)) return fail(h, RP_ERR_ARG, "sigma must be positive");
+        if (kind == RP_SOFT_REPULSIVE_LJ && !(epsilon > 0)) return fail(h, RP_ERR_ARG, "epsilon must be positive");
+        if (kind == RP_SOFT_SQUARE_INVERSE_CORE && epsilon == 0) return fail(h, RP_ERR_ARG, "epsilon must be nonzero");
+        if (!hard && (h->shape.kind == RP_SHAPE_SPHEROCYLINDER || h->segs))
+            return fail(h, RP_ERR_UNSUPPORTED, "a soft part alone is built for spheres and polyspheres");
+    }
+    RP_CUDA(h, cudaSetDevice(h->device));
+    if (!h->hard_ranges_saved) {
+        h->hard_range = h->range;
+        h->hard_ref_range = h->ref_range;
+        h->hard_total_range = h->total_range;
+        h->hard_ranges_saved = true;
+    }
+    h->soft = kind;
+    h->soft_only = kind != RP_SOFT_NONE && !hard;
+    h->soft_eps = epsilon;
+    h->soft_sigma = sigma;
+    h->soft_cut = sigma * std::pow(2., 1. / 6);  // RepulsiveLennardJonesInteraction.cpp:19-20
+    h->range = h->hard_range;
+    h->ref_range = h->hard_ref_range;
+    h->total_range = h->hard_total_range;
+    if (kind != RP_SOFT_NONE) {
+        // the compound's range is the larger one (CompoundInteraction.cpp:33-35); the
+        // checkerboard cells hold every body pair with a centre pair within it
+        const double srange = kind == RP_SOFT_REPULSIVE_LJ ? h->soft_cut : sigma;
+        double cmax = 0;
+        for (int b = 0; b < h->ncen; b++)
+            cmax = std::max(cmax, std::sqrt(h->cbody[3 * b] * h->cbody[3 * b] + h->cbody[3 * b + 1] * h->cbody[3 * b + 1] +
+                                            h->cbody[3 * b + 2] * h->cbody[3 * b + 2]));
+        const double body = (h->ncen > 0 ? 2 * cmax + srange : srange) * (1.0 + 1e-12);
+        h->range = h->soft_only ? body : std::max(h->hard_range, body);
+        h->ref_range = h->soft_only ? srange : std::max(h->hard_ref_range, srange);
+        h->total_range = h->ncen > 0 ? 2 * cmax + h->ref_range : h->ref_range;
+    }
+    h->grid_stale = true;
+    h->grid_patched = false;
+    h->partners_valid = false;
+    h->try_valid = false;
+    h->log_valid = false;
+    h->can_revert = false;
+    if (h->counting && h->has_state) {
+        // the cached count follows the new interaction (Packing::setupForInteraction)
+        int64_t cnt = 0;
+        int rc = rp_count_overlaps(h, 0, &cnt);
+        if (rc) return rc;
+        unsigned long long c = static_cast<unsigned long long>(cnt);
+        RP_CUDA(h, cudaMemcpyAsync(h->d_overlaps, &c, sizeof(c), cudaMemcpyHostToDevice, h->stream));
+        RP_CUDA(h, cudaStreamSynchronize(h->stream));
+    }
+    return RP_OK;
+}
+
+int rp_set_temperature(void *handle, double temperature) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !(temperature > 0)) return fail(h, RP_ERR_ARG, "temperature must be positive");
+    h->temperature = temperature;
     return RP_OK;
 }
 
@@ -2840,6 +3031,7 @@ bool handle_box(void *handle, double *box9) {
     return true;
 }
 bool handle_counting(void *handle) { return handle && static_cast<Handle *>(handle)->counting; }
+bool handle_soft(void *handle) { return handle && static_cast<Handle *>(handle)->soft != 0; }
 
 // The current state of a handle for the observables (positions, orientations, box and its
 // reference inverse), after its pending moves (in order on its stream).

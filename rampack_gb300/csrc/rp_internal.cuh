@@ -129,6 +129,11 @@ struct DevState {
     double wall_half;
     double wall_half_len;
     double wall_radius[RP_MAX_CENTRES];
+    // soft part: a central potential on the interaction centres joined to the hard shape
+    // (CompoundInteraction, core/interactions/CompoundInteraction.cpp:9-49): 0 none,
+    // 1 RepulsiveLennardJonesInteraction, 2 SquareInverseCoreInteraction; soft_only: no hard part
+    int soft, soft_only;
+    double soft_eps, soft_sigma, soft_cut;   // soft_cut: sigma * std::pow(2., 1./6) (RepulsiveLennardJones)
 };
 
 constexpr int MAX_CEN = RP_MAX_CENTRES;
@@ -248,6 +253,7 @@ struct SingleArgs {
     GridDev g;
     rp_move m;
     SingleTry *out;
+    double temperature;   // soft sweeps: the Metropolis temperature
     const int32_t *disp_list;
     const uint8_t *disp_flag;
     int ndisp;
@@ -255,6 +261,21 @@ struct SingleArgs {
     float box32[9];     // the box in FP32 (the images' translations in the pre-filter)
     int has_domain;     // an ActiveDomain: relative bounds lo[3], hi[3] (ActiveDomain::RegionBounds)
     double dom_lo[3], dom_hi[3];
+};
+
+// A device sweep with a soft part: every move decided in FP64 (hard part, then the energy
+// change), one warp per active cell of a checkerboard phase.
+struct SoftSweepArgs {
+    SingleArgs c;                  // state, grid, pre-filter reach, temperature (c.m, c.out unused)
+    int phase[3], active[3], num_active;
+    int32_t *next_item;
+    uint64_t seed, counter;
+    float tstep;
+    int types;
+    const double *rtab64;
+    uint32_t rtab_mask;
+    rp_move *log;
+    uint8_t *log_codes;
 };
 
 // One replica of a batched launch (rp_batch_*): its sweep arguments, this sweep's phase

@@ -25,6 +25,7 @@
 
 namespace rp {
 bool handle_box(void *handle, double *box9);
+bool handle_soft(void *handle);
 bool handle_counting(void *handle);
 int64_t handle_size(void *handle);
 }  // namespace rp
@@ -179,8 +180,8 @@ int try_scaling(Sim *s) {
     const double N = static_cast<double>(s->n);
     const double T = s->p.temperature, P = s->p.pressure;
     double dE = 0;
-    if (rp::handle_counting(s->h)) {
-        // overlaps counted: the energy change is needed before the Metropolis test
+    if (rp::handle_counting(s->h) || rp::handle_soft(s->h)) {
+        // overlaps counted or a soft part: the energy change is needed before the Metropolis test
         if (rp_try_scaling(s->h, newb, &dE) != RP_OK) return sim_fail(s, RP_ERR_DEVICE, "rp_try_scaling", s->h);
         const double ex = N * std::log(factor) - dE / T - P * dV / T;
         if (s->unit(s->mt) <= std::exp(ex)) return 1;
@@ -325,6 +326,7 @@ int rp_sim_create(void *handle, const rp_sim_params *p, void **sim) {
     s->last_moves[1] = st.rotations;
     s->last_moves[2] = st.accepted_translations;
     s->last_accepted = st.accepted;
+    rp_set_temperature(handle, p->temperature);
     *sim = s;
     return RP_OK;
 }
@@ -403,7 +405,7 @@ int rp_sim_set_conditions(void *sim, double temperature, double pressure) {
     if (!s || !(temperature > 0)) return RP_ERR_ARG;
     s->p.temperature = temperature;
     s->p.pressure = pressure;
-    return RP_OK;
+    return rp_set_temperature(s->h, temperature);  // the sweeps' Metropolis test of soft energies
 }
 
 const char *rp_sim_last_error(void *sim) {

@@ -1,18 +1,24 @@
-// Unrestricted single moves: Packing::tryTranslation / tryRotation / tryMove with no
-// ActiveDomain (std::nullopt, core/Packing.cpp:84-164) and Packing::accept* (:234-302), the
-// reference's serial path (Simulation::performMovesWithoutDomainDivision,
-// core/Simulation.cpp:365-390).  The per-move entry of the C ABI (rp_try_move /
-// rp_accept_move): one launch tests one move, one launch commits it.
+// Moves decided entirely in FP64, one warp each:
 //
-// A tried move's exact FP64 state is computed as the reference computes its temp shape
+//  * single moves: Packing::tryTranslation / tryRotation / tryMove with or without an
+//    ActiveDomain (core/Packing.cpp:84-164) and Packing::accept* (:234-302), the reference's
+//    serial path (Simulation::performMovesWithoutDomainDivision, core/Simulation.cpp:365-390):
+//    one launch tests one move, one launch commits it (rp_try_move / rp_accept_move);
+//  * sweeps of packings with a soft part (a central potential joined to the hard shape by
+//    CompoundInteraction, core/interactions/CompoundInteraction.cpp:9-49): one warp per active
+//    cell of a checkerboard phase, every move's hard test and energy change in FP64;
+//  * the total soft energy (Packing::getTotalEnergy, core/Packing.cpp:689-764) for box moves.
+//
+// A move's exact FP64 state is computed as the reference computes its temp shape
 // (Shape::translate with the periodic correction, Shape::rotate, the rotated and absolute
 // interaction centres), and every candidate within reach of it is decided in FP64 with the
 // reference's pair test at every periodic image within reach: that is the set of
 // (candidate, translation) pairs the reference's neighbour grid visits that can overlap, so
-// the any-overlap answer and, in overlap counting, the counts are the reference's.
-// Candidates come from the handle's cell grid (cells at least one interaction range high);
-// particles moved by single moves since the grid was built are skipped in their old cells
-// and tested from a short list instead, so a commit never rebuilds the grid.
+// the any-overlap answer and, in overlap counting, the counts are the reference's.  The soft
+// potentials vanish beyond their range, so the energies sum over the same pairs (in another
+// order than the reference's neighbour-grid walk).  Candidates come from the handle's cell
+// grid (cells at least one interaction range high); particles moved by single moves since the
+// grid was built are skipped in their old cells and tested from a short list instead.
 #include <cuda_runtime.h>
 #include <math_constants.h>
 
@@ -22,18 +28,18 @@ namespace rp {
 
 namespace {
 
-constexpr int SINGLE_THREADS = 128;
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int SOFT_WARPS = 4;   // warps per block of the soft sweep
 
-struct SingleShared {
-    double pos[2][3], rot[2][9];        // [0] the tried state, [1] the current one
+// One mover in shared memory: [0] the tried state, [1] the current one.
+struct Mover {
+    double pos[2][3], rot[2][9];
     double abs[2][3 * MAX_CEN];         // absolute interaction centres of both states
     double hax[2][3 * MAX_CEN];         // polyspherocylinders: orientation * half axis
     double cen[3 * MAX_CEN];            // the tried state's rotated centres
     int cells[2][27];                   // distinct grid cells around each state's position
     int ncells[2];
-    int cstart[2][28];                  // prefix of those cells' occupancies, then the list
-    int hit;
-    int count[2];
+    int cstart[2][28];                  // prefix of those cells' occupancies
     int outside;                        // the tried position lies outside the ActiveDomain
 };
 
@@ -69,13 +75,28 @@ __device__ int neighbour_cells(const GridDev &g, const int c[3], int *out) {
     return k;
 }
 
-// Pair test of a sphere or spherocylinder mover state `which` against particle j at
+// CentralInteraction::calculateEnergyForDistance2 of the soft part, in the reference's
+// operation order: RepulsiveLennardJonesInteraction.cpp:9-17, SquareInverseCoreInteraction.cpp:13-15.
+__device__ double soft_energy(const DevState &s, double d2) {
+    if (s.soft == 1) {
+        if (d2 >= dmul(s.soft_cut, s.soft_cut)) return 0.0;
+        const double x2 = ddiv(dmul(s.soft_sigma, s.soft_sigma), d2);
+        const double x6 = dmul(dmul(x2, x2), x2);
+        const double x12 = dmul(x6, x6);
+        return dadd(dmul(dmul(4.0, s.soft_eps), dsub(x12, x6)), s.soft_eps);
+    }
+    if (s.soft == 2) {
+        const double v = dsub(ddiv(dmul(s.soft_sigma, s.soft_sigma), d2), 1.0);
+        return dmul(s.soft_eps, 0.0 < v ? v : 0.0);  // std::max(0.0, v)
+    }
+    return 0.0;
+}
+
+// Pair test of a sphere or spherocylinder mover (position p, axis a) against particle j at
 // translation t (null: no grid in the reference, the periodic boundary conditions' nearest
 // image), SphereTraits.cpp:56-65 / SpherocylinderTraits.cpp:28-46.
 template <int KIND>
-__device__ bool body_overlap(const DevState &s, const SingleShared &sh, int which, int j, const d3 *t) {
-    const d3 p{sh.pos[which][0], sh.pos[which][1], sh.pos[which][2]};
-    const d3 a{sh.rot[which][2], sh.rot[which][5], sh.rot[which][8]};
+__device__ bool body_overlap(const DevState &s, d3 p, d3 a, int j, const d3 *t) {
     const d3 pj = load_d3(s.pos64 + 3 * (size_t)j);
     const double *rj = s.rot64 + 9 * (size_t)j;
     const d3 aj{rj[2], rj[5], rj[8]};
@@ -84,12 +105,11 @@ __device__ bool body_overlap(const DevState &s, const SingleShared &sh, int whic
     return exact_overlap(s.ex, p, a, pj, aj, pbc_translation(s.box, s.inv, p, pj));
 }
 
-// Centre a of a multi-centre mover state `which` against centre b of body j at translation t
-// (null: the nearest image): PolysphereTraits::HardInteraction (core/shapes/PolysphereTraits.cpp:97-106,
-// the cell's translation as core/Packing.cpp:40-42) or PolyspherocylinderTraits::overlapBetween
-// (core/shapes/PolyspherocylinderTraits.cpp:102-124).
-__device__ bool centre_overlap(const DevState &s, const SingleShared &sh, int which, int a, int j, int b, const d3 *t) {
-    const d3 pa{sh.abs[which][3 * a], sh.abs[which][3 * a + 1], sh.abs[which][3 * a + 2]};
+// Centre a of a multi-centre mover (absolute centre pa, half axis ha) against centre b of body
+// j at translation t (null: the nearest image): PolysphereTraits::HardInteraction
+// (core/shapes/PolysphereTraits.cpp:97-106, the cell's translation as core/Packing.cpp:40-42)
+// or PolyspherocylinderTraits::overlapBetween (core/shapes/PolyspherocylinderTraits.cpp:102-124).
+__device__ bool centre_overlap(const DevState &s, d3 pa, d3 ha, int a, int j, int b, const d3 *t) {
     const d3 pb = load_d3(s.abs64 + 3 * ((size_t)j * s.ncen + b));
     const double in2 = s.cthr64[a * MAX_CEN + b];
     if (s.segs) {
@@ -98,7 +118,6 @@ __device__ bool centre_overlap(const DevState &s, const SingleShared &sh, int wh
         const double d2 = norm2(sub3(q, pa));
         if (d2 < in2) return true;
         if (d2 >= s.circ64[a * MAX_CEN + b]) return false;
-        const d3 ha{sh.hax[which][3 * a], sh.hax[which][3 * a + 1], sh.hax[which][3 * a + 2]};
         const d3 hj = mv3(s.rot64 + 9 * (size_t)j, d3{s.chax[b][0], s.chax[b][1], s.chax[b][2]});
         return segment_distance2(add3(pa, ha), sub3(pa, ha), add3(q, hj), sub3(q, hj)) < in2;
     }
@@ -116,191 +135,281 @@ __device__ __forceinline__ bool within_reach(const SingleArgs &A, const double *
     return ex * ex + ey * ey + ez * ez <= A.reach2;
 }
 
-// Overlapping pairs of the mover state `which` with body j over every periodic image within
-// reach (each absolute centre is wrapped into the box on its own, so the images of a body
-// pair are enumerated per centre pair); at most 1 with `early`.
+__device__ __forceinline__ d3 image_translation(const DevState &s, int mx, int my, int mz) {
+    return load_d3(s.trans + 3 * (((mx + 2) * 5 + (my + 2)) * 5 + (mz + 2)));
+}
+
+// Overlapping pairs of a mover state (position p, axis a; multi-centre: absolute centres abs,
+// half axes hax) with body j over every periodic image within reach (each absolute centre is
+// wrapped into the box on its own, so images are enumerated per centre pair); at most 1 with
+// `early`.
 template <int KIND>
-__device__ int candidate_overlaps(const SingleArgs &A, const SingleShared &sh, int which, int j, bool early) {
+__device__ int candidate_overlaps(const SingleArgs &A, const double *p, d3 a, const double *abs, const double *hax,
+                                  int j, bool early) {
     const DevState &s = A.s;
     int cnt = 0;
     if constexpr (KIND != 2) {
-        if (s.pbc_fold) return body_overlap<KIND>(s, sh, which, j, nullptr) ? 1 : 0;
+        const d3 pp{p[0], p[1], p[2]};
+        if (s.pbc_fold) return body_overlap<KIND>(s, pp, a, j, nullptr) ? 1 : 0;
         const double *pj = s.pos64 + 3 * (size_t)j;
         for (int mx = -1; mx <= 1; mx++)
             for (int my = -1; my <= 1; my++)
                 for (int mz = -1; mz <= 1; mz++) {
-                    if (!within_reach(A, pj, sh.pos[which], mx, my, mz)) continue;
-                    const d3 t = load_d3(s.trans + 3 * (((mx + 2) * 5 + (my + 2)) * 5 + (mz + 2)));
-                    if (body_overlap<KIND>(s, sh, which, j, &t)) {
+                    if (!within_reach(A, pj, p, mx, my, mz)) continue;
+                    const d3 t = image_translation(s, mx, my, mz);
+                    if (body_overlap<KIND>(s, pp, a, j, &t)) {
                         if (early) return 1;
                         cnt++;
                     }
                 }
         return cnt;
     } else {
-    for (int a = 0; a < s.ncen; a++)
-        for (int b = 0; b < s.ncen; b++) {
-            if (s.pbc_fold) {
-                if (centre_overlap(s, sh, which, a, j, b, nullptr)) {
-                    if (early) return 1;
-                    cnt++;
+        for (int ca = 0; ca < s.ncen; ca++) {
+            const d3 pa{abs[3 * ca], abs[3 * ca + 1], abs[3 * ca + 2]};
+            const d3 ha = hax ? d3{hax[3 * ca], hax[3 * ca + 1], hax[3 * ca + 2]} : d3{0.0, 0.0, 0.0};
+            for (int b = 0; b < s.ncen; b++) {
+                if (s.pbc_fold) {
+                    if (centre_overlap(s, pa, ha, ca, j, b, nullptr)) {
+                        if (early) return 1;
+                        cnt++;
+                    }
+                    continue;
                 }
+                const double *pb = s.abs64 + 3 * ((size_t)j * s.ncen + b);
+                for (int mx = -1; mx <= 1; mx++)
+                    for (int my = -1; my <= 1; my++)
+                        for (int mz = -1; mz <= 1; mz++) {
+                            if (!within_reach(A, pb, abs + 3 * ca, mx, my, mz)) continue;
+                            const d3 t = image_translation(s, mx, my, mz);
+                            if (centre_overlap(s, pa, ha, ca, j, b, &t)) {
+                                if (early) return 1;
+                                cnt++;
+                            }
+                        }
+            }
+        }
+        return cnt;
+    }
+}
+
+// Soft energy of a mover state with body j: every centre pair at every image within reach
+// (CentralInteraction::calculateEnergyBetween with the cell's translation, or the periodic
+// boundary conditions' distance where the reference keeps no grid).
+template <int KIND>
+__device__ double candidate_energy(const SingleArgs &A, const double *p, const double *abs, int j) {
+    const DevState &s = A.s;
+    double e = 0.0;
+    const int K = KIND == 2 ? s.ncen : 1;
+    for (int ca = 0; ca < K; ca++) {
+        const double *pa = KIND == 2 ? abs + 3 * ca : p;
+        const d3 pa3{pa[0], pa[1], pa[2]};
+        for (int b = 0; b < K; b++) {
+            const double *pb = KIND == 2 ? s.abs64 + 3 * ((size_t)j * s.ncen + b) : s.pos64 + 3 * (size_t)j;
+            const d3 pb3{pb[0], pb[1], pb[2]};
+            if (s.pbc_fold) {
+                e = dadd(e, soft_energy(s, pbc_distance2(s.box, s.inv, pa3, pb3)));
                 continue;
             }
-            const double *pb = s.abs64 + 3 * ((size_t)j * s.ncen + b);
             for (int mx = -1; mx <= 1; mx++)
                 for (int my = -1; my <= 1; my++)
                     for (int mz = -1; mz <= 1; mz++) {
-                        if (!within_reach(A, pb, sh.abs[which] + 3 * a, mx, my, mz)) continue;
-                        const d3 t = load_d3(s.trans + 3 * (((mx + 2) * 5 + (my + 2)) * 5 + (mz + 2)));
-                        if (centre_overlap(s, sh, which, a, j, b, &t)) {
-                            if (early) return 1;
-                            cnt++;
-                        }
+                        if (!within_reach(A, pb, pa, mx, my, mz)) continue;
+                        const d3 t = image_translation(s, mx, my, mz);
+                        e = dadd(e, soft_energy(s, norm2(sub3(add3(pb3, t), pa3))));
                     }
         }
-    return cnt;
     }
+    return e;
 }
 
-// Overlaps of mover state `which` with every candidate (pairs, then walls): the count, or
-// 0 / 1 with `early` (Packing::countParticleOverlaps, core/Packing.cpp:373-429).
+// The candidate behind index k of mover state `which`: particles of its neighbour cells in
+// grid order, then the particles moved since the grid was built; -1 for one to skip.
+__device__ __forceinline__ int candidate_at(const SingleArgs &A, const Mover &mv, int which, int k, int in_cells) {
+    if (k < in_cells) {
+        int c = 0;
+        while (mv.cstart[which][c + 1] <= k) c++;
+        const int cell = mv.cells[which][c];
+        const int j = A.g.slot_pid[A.g.start[cell] + (k - mv.cstart[which][c])];
+        return (A.disp_flag && A.disp_flag[j]) ? -1 : j;  // moved since: tested from the list
+    }
+    return A.disp_list[k - in_cells];
+}
+
+// Overlaps of mover state `which` with every candidate, then the walls (the count, or 0 / 1
+// with `early`: Packing::countParticleOverlaps, core/Packing.cpp:373-429); the whole warp.
 template <int KIND>
-__device__ int state_overlaps(const SingleArgs &A, SingleShared &sh, int which, bool early) {
+__device__ int warp_overlaps(const SingleArgs &A, const Mover &mv, int which, bool early, int pid) {
     const DevState &s = A.s;
-    const GridDev &g = A.g;
-    const int pid = A.m.particle;
-    const int in_cells = sh.cstart[which][sh.ncells[which]];
+    const int lane = threadIdx.x & 31;
+    const int in_cells = mv.cstart[which][mv.ncells[which]];
     const int total = in_cells + A.ndisp;
+    const d3 a{mv.rot[which][2], mv.rot[which][5], mv.rot[which][8]};
+    const double *hax = (KIND == 2 && s.segs) ? mv.hax[which] : nullptr;
     int cnt = 0;
-    for (int k = threadIdx.x; k < total; k += blockDim.x) {
-        if (early && *(volatile int *)&sh.hit) break;
-        int j;
-        if (k < in_cells) {
-            int c = 0;
-            while (sh.cstart[which][c + 1] <= k) c++;
-            const int cell = sh.cells[which][c];
-            j = g.slot_pid[g.start[cell] + (k - sh.cstart[which][c])];
-            if (A.disp_flag[j]) continue;  // moved since the grid was built: tested from the list
-        } else {
-            j = A.disp_list[k - in_cells];
+    for (int base = 0; base < total; base += 32) {
+        const int k = base + lane;
+        int c = 0;
+        if (k < total) {
+            const int j = candidate_at(A, mv, which, k, in_cells);
+            // the self-skip compares particle indices (core/Packing.cpp:633-635)
+            if (j >= 0 && j != pid) c = candidate_overlaps<KIND>(A, mv.pos[which], a, mv.abs[which], hax, j, early);
         }
-        if (j == pid) continue;  // the self-skip compares particle indices (core/Packing.cpp:633-635)
-        const int c = candidate_overlaps<KIND>(A, sh, which, j, early);
-        if (c) {
-            cnt += c;
-            if (early) sh.hit = 1;
-        }
+        if (early && __any_sync(FULL, c != 0)) return 1;
+        cnt += c;
     }
-    for (int d = 16; d > 0; d >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, d);
-    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(&sh.count[which], cnt);
-    __syncthreads();
-    int out = sh.count[which];
-    if (early) out = out > 0 ? 1 : 0;
-    if (s.walls && !(early && out)) {
+    for (int d = 16; d > 0; d >>= 1) cnt += __shfl_xor_sync(FULL, cnt, d);
+    if (s.walls) {
         // hard walls after the pairs (core/Packing.cpp:424-428)
-        const d3 p{sh.pos[which][0], sh.pos[which][1], sh.pos[which][2]};
-        const d3 a{sh.rot[which][2], sh.rot[which][5], sh.rot[which][8]};
-        const double *cen = KIND == 2 ? (which == 0 ? sh.cen : s.cen64 + 3 * (size_t)pid * s.ncen) : nullptr;
-        out += wall_overlap_count(s.walls, s.wall_vec, s.wall_far, s.wall_half, KIND, s.wall_radius, s.wall_half_len,
-                                  p, a, cen, KIND == 2 ? s.ncen : 0, early, KIND == 2 && s.segs ? sh.hax[which] : nullptr);
-        if (early) out = out > 0 ? 1 : 0;
+        int w = 0;
+        if (lane == 0) {
+            const d3 p{mv.pos[which][0], mv.pos[which][1], mv.pos[which][2]};
+            const double *cen = KIND == 2 ? (which == 0 ? mv.cen : s.cen64 + 3 * (size_t)pid * s.ncen) : nullptr;
+            w = wall_overlap_count(s.walls, s.wall_vec, s.wall_far, s.wall_half, KIND, s.wall_radius, s.wall_half_len,
+                                   p, a, cen, KIND == 2 ? s.ncen : 0, early, hax);
+        }
+        cnt += __shfl_sync(FULL, w, 0);
     }
-    return out;
+    return early ? (cnt > 0 ? 1 : 0) : cnt;
+}
+
+// Soft energy of mover state `which` with every candidate (Packing::calculateParticleEnergy,
+// core/Packing.cpp:649-687); the whole warp, a fixed reduction order.
+template <int KIND>
+__device__ double warp_energy(const SingleArgs &A, const Mover &mv, int which, int pid) {
+    const int lane = threadIdx.x & 31;
+    const int in_cells = mv.cstart[which][mv.ncells[which]];
+    const int total = in_cells + A.ndisp;
+    double e = 0.0;
+    for (int k = lane; k < total; k += 32) {
+        const int j = candidate_at(A, mv, which, k, in_cells);
+        if (j >= 0 && j != pid) e = dadd(e, candidate_energy<KIND>(A, mv.pos[which], mv.abs[which], j));
+    }
+    for (int d = 16; d > 0; d >>= 1) e = dadd(e, __shfl_xor_sync(FULL, e, d));
+    return e;
+}
+
+// Lane 0: the current state and the temp shape of move m of particle pid (core/Packing.cpp:86-93,
+// 113-116, 137-146), with their neighbour cells ([1] only when `both`), and the ActiveDomain
+// test of a translation (lo null: none; bounded[d] 0: dimension d unbounded).
+template <int KIND>
+__device__ void build_mover(const SingleArgs &A, Mover &mv, const rp_move &m, int pid, bool both, const double *lo,
+                            const double *hi, const int *bounded) {
+    const DevState &s = A.s;
+    const d3 p0 = load_d3(s.pos64 + 3 * (size_t)pid);
+    const double *o0 = s.rot64 + 9 * (size_t)pid;
+    d3 p1 = p0;
+    if (m.type != RP_MOVE_ROTATION) {
+        // Shape::translate (core/Shape.cpp:9-12) with PeriodicBoundaryConditions::getCorrection
+        const d3 q = add3(p0, d3{m.translation[0], m.translation[1], m.translation[2]});
+        p1 = add3(q, pbc_correction(s.box, s.inv, q, nullptr));
+    }
+    double o1[9];
+    for (int e = 0; e < 9; e++) o1[e] = o0[e];
+    if (m.type != RP_MOVE_TRANSLATION)  // Shape::rotate: R * O (core/Shape.cpp:14-16)
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) o1[3 * i + j] = mm_elem(m.rotation, o0, i, j);
+    mv.pos[0][0] = p1.x, mv.pos[0][1] = p1.y, mv.pos[0][2] = p1.z;
+    mv.pos[1][0] = p0.x, mv.pos[1][1] = p0.y, mv.pos[1][2] = p0.z;
+    for (int e = 0; e < 9; e++) {
+        mv.rot[0][e] = o1[e];
+        mv.rot[1][e] = o0[e];
+    }
+    if (KIND == 2) {
+        for (int a = 0; a < s.ncen; a++) {
+            // the temp centres, rotated by R (core/Packing.cpp:357-361), and the absolute
+            // centres: position + centre with the periodic correction (:1041-1047)
+            d3 c = load_d3(s.cen64 + 3 * ((size_t)pid * s.ncen + a));
+            if (m.type != RP_MOVE_TRANSLATION) c = mv3(m.rotation, c);
+            const d3 q = add3(p1, c);
+            const d3 ab = add3(q, pbc_correction(s.box, s.inv, q, nullptr));
+            mv.cen[3 * a] = c.x, mv.cen[3 * a + 1] = c.y, mv.cen[3 * a + 2] = c.z;
+            mv.abs[0][3 * a] = ab.x, mv.abs[0][3 * a + 1] = ab.y, mv.abs[0][3 * a + 2] = ab.z;
+            for (int d = 0; d < 3; d++) mv.abs[1][3 * a + d] = s.abs64[3 * ((size_t)pid * s.ncen + a) + d];
+            if (s.segs) {
+                // orientation * half axis (PolyspherocylinderTraits.cpp:118-119)
+                const d3 hb{s.chax[a][0], s.chax[a][1], s.chax[a][2]};
+                const d3 h1 = mv3(o1, hb), h0 = mv3(o0, hb);
+                mv.hax[0][3 * a] = h1.x, mv.hax[0][3 * a + 1] = h1.y, mv.hax[0][3 * a + 2] = h1.z;
+                mv.hax[1][3 * a] = h0.x, mv.hax[1][3 * a + 1] = h0.y, mv.hax[1][3 * a + 2] = h0.z;
+            }
+        }
+    }
+    // the ActiveDomain of a translation or rototranslation, tested before any overlap
+    // (core/Packing.cpp:94-96, :141-143; ActiveDomain::isInside, core/ActiveDomain.cpp:8-21)
+    mv.outside = 0;
+    if (lo && m.type != RP_MOVE_ROTATION) {
+        const d3 rel = mv3(s.inv, p1);
+        const double r[3] = {rel.x, rel.y, rel.z};
+        for (int d = 0; d < 3; d++) {
+            if (bounded && !bounded[d]) continue;
+            if (hi[d] > lo[d]) {
+                if (r[d] <= lo[d] || r[d] >= hi[d]) mv.outside = 1;
+            } else if (r[d] <= lo[d] && r[d] >= hi[d]) {
+                mv.outside = 1;
+            }
+        }
+    }
+    for (int w = 0; w < (both ? 2 : 1); w++) {
+        int c[3];
+        cell_of(s, A.g, d3{mv.pos[w][0], mv.pos[w][1], mv.pos[w][2]}, c);
+        mv.ncells[w] = neighbour_cells(A.g, c, mv.cells[w]);
+        int acc = 0;
+        for (int q = 0; q < mv.ncells[w]; q++) {
+            mv.cstart[w][q] = acc;
+            acc += A.g.start[mv.cells[w][q] + 1] - A.g.start[mv.cells[w][q]];
+        }
+        mv.cstart[w][mv.ncells[w]] = acc;
+    }
+}
+
+// The move's energy (the whole warp, after build_mover): the ActiveDomain, then the hard part
+// (any overlap, or in overlap counting the sign of the change of the mover's count:
+// core/Packing.cpp:304-323), then the soft part's energy change (core/Packing.cpp:103-108).
+template <int KIND>
+__device__ double move_energy(const SingleArgs &A, const Mover &mv, int pid, int &delta) {
+    const DevState &s = A.s;
+    delta = 0;
+    if (mv.outside) return CUDART_INF;
+    if (!s.soft_only) {
+        if (s.counting) {
+            const int after = warp_overlaps<KIND>(A, mv, 0, false, pid);
+            const int before = warp_overlaps<KIND>(A, mv, 1, false, pid);
+            delta = after - before;
+            if (delta < 0) return -CUDART_INF;
+            if (delta > 0) return CUDART_INF;
+        } else if (warp_overlaps<KIND>(A, mv, 0, true, pid)) {
+            return CUDART_INF;
+        }
+    }
+    if (!s.soft) return 0.0;
+    const double initial = warp_energy<KIND>(A, mv, 1, pid);
+    const double final_ = warp_energy<KIND>(A, mv, 0, pid);
+    return dsub(final_, initial);
 }
 
 template <int KIND>
-__global__ void __launch_bounds__(SINGLE_THREADS) k_try_single(SingleArgs A) {
-    __shared__ SingleShared sh;
-    const DevState &s = A.s;
-    const rp_move &m = A.m;
-    const int pid = m.particle;
-    const bool counting = s.counting != 0;
-    if (threadIdx.x == 0) {
-        // the current state and the temp shape (core/Packing.cpp:86-93, 113-116, 137-146)
-        const d3 p0 = load_d3(s.pos64 + 3 * (size_t)pid);
-        const double *o0 = s.rot64 + 9 * (size_t)pid;
-        d3 p1 = p0;
-        if (m.type != RP_MOVE_ROTATION) {
-            // Shape::translate (core/Shape.cpp:9-12) with PeriodicBoundaryConditions::getCorrection
-            const d3 q = add3(p0, d3{m.translation[0], m.translation[1], m.translation[2]});
-            p1 = add3(q, pbc_correction(s.box, s.inv, q, nullptr));
-        }
-        double o1[9];
-        for (int e = 0; e < 9; e++) o1[e] = o0[e];
-        if (m.type != RP_MOVE_TRANSLATION)  // Shape::rotate: R * O (core/Shape.cpp:14-16)
-            for (int i = 0; i < 3; i++)
-                for (int j = 0; j < 3; j++) o1[3 * i + j] = mm_elem(m.rotation, o0, i, j);
-        sh.pos[0][0] = p1.x, sh.pos[0][1] = p1.y, sh.pos[0][2] = p1.z;
-        sh.pos[1][0] = p0.x, sh.pos[1][1] = p0.y, sh.pos[1][2] = p0.z;
-        for (int e = 0; e < 9; e++) {
-            sh.rot[0][e] = o1[e];
-            sh.rot[1][e] = o0[e];
-        }
-        if (KIND == 2) {
-            for (int a = 0; a < s.ncen; a++) {
-                // the temp centres, rotated by R (core/Packing.cpp:357-361), and the absolute
-                // centres: position + centre with the periodic correction (:1041-1047)
-                d3 c = load_d3(s.cen64 + 3 * ((size_t)pid * s.ncen + a));
-                if (m.type != RP_MOVE_TRANSLATION) c = mv3(m.rotation, c);
-                const d3 q = add3(p1, c);
-                const d3 ab = add3(q, pbc_correction(s.box, s.inv, q, nullptr));
-                sh.cen[3 * a] = c.x, sh.cen[3 * a + 1] = c.y, sh.cen[3 * a + 2] = c.z;
-                sh.abs[0][3 * a] = ab.x, sh.abs[0][3 * a + 1] = ab.y, sh.abs[0][3 * a + 2] = ab.z;
-                for (int d = 0; d < 3; d++) sh.abs[1][3 * a + d] = s.abs64[3 * ((size_t)pid * s.ncen + a) + d];
-                if (s.segs) {
-                    // orientation * half axis (PolyspherocylinderTraits.cpp:118-119)
-                    const d3 hb{s.chax[a][0], s.chax[a][1], s.chax[a][2]};
-                    const d3 h1 = mv3(o1, hb), h0 = mv3(o0, hb);
-                    sh.hax[0][3 * a] = h1.x, sh.hax[0][3 * a + 1] = h1.y, sh.hax[0][3 * a + 2] = h1.z;
-                    sh.hax[1][3 * a] = h0.x, sh.hax[1][3 * a + 1] = h0.y, sh.hax[1][3 * a + 2] = h0.z;
-                }
-            }
-        }
-        // the ActiveDomain of a translation or rototranslation, tested before any overlap
-        // (core/Packing.cpp:94-96, :141-143; ActiveDomain::isInside, core/ActiveDomain.cpp:8-21)
-        sh.outside = A.has_domain && m.type != RP_MOVE_ROTATION && !inside_domain(s.inv, p1, A.dom_lo, A.dom_hi);
-        for (int w = 0; w < (counting ? 2 : 1); w++) {
-            int c[3];
-            cell_of(s, A.g, d3{sh.pos[w][0], sh.pos[w][1], sh.pos[w][2]}, c);
-            sh.ncells[w] = neighbour_cells(A.g, c, sh.cells[w]);
-            int acc = 0;
-            for (int q = 0; q < sh.ncells[w]; q++) {
-                sh.cstart[w][q] = acc;
-                acc += A.g.start[sh.cells[w][q] + 1] - A.g.start[sh.cells[w][q]];
-            }
-            sh.cstart[w][sh.ncells[w]] = acc;
-        }
-        sh.hit = 0;
-        sh.count[0] = sh.count[1] = 0;
-    }
-    __syncthreads();
-    double dE;
+__global__ void __launch_bounds__(32) k_try_single(SingleArgs A) {
+    __shared__ Mover mv;
+    const int pid = A.m.particle;
+    if (threadIdx.x == 0)
+        build_mover<KIND>(A, mv, A.m, pid, A.s.counting || A.s.soft, A.has_domain ? A.dom_lo : nullptr,
+                          A.has_domain ? A.dom_hi : nullptr, nullptr);
+    __syncwarp();
     int delta = 0;
-    if (sh.outside) {
-        dE = CUDART_INF;
-    } else if (counting) {
-        // Packing::calculateMoveOverlapEnergy in counting mode (core/Packing.cpp:307-317)
-        const int after = state_overlaps<KIND>(A, sh, 0, false);
-        const int before = state_overlaps<KIND>(A, sh, 1, false);
-        delta = after - before;
-        dE = delta < 0 ? -CUDART_INF : (delta > 0 ? CUDART_INF : 0.0);
-    } else {
-        dE = state_overlaps<KIND>(A, sh, 0, true) ? CUDART_INF : 0.0;
-    }
+    const double dE = move_energy<KIND>(A, mv, pid, delta);
     if (threadIdx.x == 0) {
         SingleTry *o = A.out;
-        for (int d = 0; d < 3; d++) o->pos[d] = sh.pos[0][d];
-        for (int e = 0; e < 9; e++) o->rot[e] = sh.rot[0][e];
+        for (int d = 0; d < 3; d++) o->pos[d] = mv.pos[0][d];
+        for (int e = 0; e < 9; e++) o->rot[e] = mv.rot[0][e];
         if (KIND == 2)
-            for (int q = 0; q < 3 * s.ncen; q++) {
-                o->cen[q] = sh.cen[q];
-                o->abs[q] = sh.abs[0][q];
+            for (int q = 0; q < 3 * A.s.ncen; q++) {
+                o->cen[q] = mv.cen[q];
+                o->abs[q] = mv.abs[0][q];
             }
         o->dE = dE;
-        o->outside = sh.outside;
+        o->outside = mv.outside;
         o->particle = pid;
-        o->type = m.type;
+        o->type = A.m.type;
         o->delta = delta;
         o->valid = 1;
     }
@@ -329,18 +438,208 @@ __global__ void k_commit_single(DevState s, SingleTry *t, uint8_t *disp_flag, in
     t->valid = 0;
 }
 
+// ---- soft sweeps ----------------------------------------------------------------------
+
+// The Metropolis uniform of move mi of a cell: 53 bits of a Philox draw apart from the
+// proposal's words.
+__device__ double soft_uniform(const SoftSweepArgs &A, int cell, int mi) {
+    const u4 q = philox(u4{(uint32_t)mi, (uint32_t)cell, (uint32_t)A.counter, (uint32_t)(A.counter >> 32) ^ 0x2545f491u},
+                        (uint32_t)A.seed ^ 0x9e3779b9u, (uint32_t)(A.seed >> 32));
+    return (static_cast<double>(q.a >> 5) * 67108864.0 + static_cast<double>(q.b >> 6)) * (1.0 / 9007199254740992.0);
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(SOFT_WARPS * 32) k_soft_sweep(SoftSweepArgs A) {
+    __shared__ Mover movers[SOFT_WARPS];
+    __shared__ rp_move moves[SOFT_WARPS];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    Mover &mv = movers[wib];
+    rp_move &m = moves[wib];
+    const SingleArgs &C = A.c;
+    const DevState &S = C.s;
+    const GridDev &G = C.g;
+    const int ntypes = sweep_move_types(A.types);
+    unsigned n_moves = 0, n_acc = 0, n_ov = 0, n_dom = 0, n_tr = 0, n_rot = 0, n_acc_tr = 0;
+    for (;;) {
+        int item = 0;
+        if (lane == 0) item = atomicAdd(A.next_item, 1);
+        item = __shfl_sync(FULL, item, 0);
+        if (item >= A.num_active) break;
+        int c[3];
+        {
+            int w = item;
+            const int a0 = w % A.active[0];
+            w /= A.active[0];
+            const int a1 = w % A.active[1];
+            const int a2 = w / A.active[1];
+            const int cc[3] = {a0, a1, a2};
+            for (int d = 0; d < 3; d++) c[d] = ring_cell(G.dims[d], A.phase[d], cc[d]);
+        }
+        const int cell = c[0] + G.dims[0] * (c[1] + G.dims[1] * c[2]);
+        const int gbase = G.start[cell];
+        const int occ = G.start[cell + 1] - gbase;
+        // the cell's ActiveDomain bounds (a dimension of one cell is unbounded)
+        double lo[3], hi[3];
+        int bounded[3];
+        for (int d = 0; d < 3; d++) {
+            lo[d] = G.bounds[G.boundsoff[d] + 2 * c[d]];
+            hi[d] = G.bounds[G.boundsoff[d] + 2 * c[d] + 1];
+            bounded[d] = G.dims[d] > 1;
+        }
+        const int nmoves = ntypes * occ;
+        u4 rnd = u4{0u, 0u, 0u, 0u};
+        for (int mi = 0; mi < nmoves; mi++) {
+            if ((mi & 31) == 0)
+                rnd = philox(u4{(uint32_t)(mi + lane), (uint32_t)cell, (uint32_t)A.counter, (uint32_t)(A.counter >> 32)},
+                             (uint32_t)A.seed, (uint32_t)(A.seed >> 32));
+            const int src = mi & 31;
+            const u4 r = u4{__shfl_sync(FULL, rnd.a, src), __shfl_sync(FULL, rnd.b, src), __shfl_sync(FULL, rnd.c, src),
+                            __shfl_sync(FULL, rnd.d, src)};
+            const int type = ntypes == 2 ? ((r.a >> 31) ? 1 : 0) : ((A.types & 1) ? 0 : 1);
+            const int slot = (int)(((uint64_t)(r.a & 0x7fffffffu) * (uint32_t)occ) >> 31);
+            const int pid = G.slot_pid[gbase + slot];
+            const double uni = soft_uniform(A, cell, mi);
+            if (lane == 0) {
+                // the proposal: a translation uniform in the cube of the step (an FP32 value, exact
+                // as FP64), or a rotation of this sweep's table or its transpose
+                m.particle = pid;
+                m.type = type;
+                m.domain = cell;
+                m.reserved = 0;
+                m.uniform = uni;
+                for (int q = 0; q < 9; q++) m.rotation[q] = (q % 4 == 0) ? 1.0 : 0.0;
+                for (int d = 0; d < 3; d++) m.translation[d] = 0.0;
+                if (type == 0) {
+                    m.translation[0] = (double)(pm1f(r.b) * A.tstep);
+                    m.translation[1] = (double)(pm1f(r.c) * A.tstep);
+                    m.translation[2] = (double)(pm1f(r.d) * A.tstep);
+                } else {
+                    const uint32_t idx = r.b & A.rtab_mask;
+                    const bool inv = (r.c & 1u) != 0;
+                    const double *R = A.rtab64 + 9 * (size_t)idx;
+                    for (int q = 0; q < 9; q++) m.rotation[q] = inv ? R[3 * (q % 3) + q / 3] : R[q];
+                }
+                build_mover<KIND>(C, mv, m, pid, true, lo, hi, bounded);
+            }
+            __syncwarp();
+            int delta = 0;
+            const double dE = move_energy<KIND>(C, mv, pid, delta);
+            // Metropolis (core/Simulation.cpp:483): u <= exp(-dE / T)
+            const bool acc = uni <= exp(-dE / C.temperature);
+            const uint8_t code = mv.outside ? 2 : (dE == CUDART_INF ? 1 : (dE == -CUDART_INF ? 3 : 0));
+            if (acc && lane == 0) {
+                // Packing::acceptMove (core/Packing.cpp:278-302)
+                if (type != RP_MOVE_ROTATION)
+                    for (int d = 0; d < 3; d++) S.pos64[3 * (size_t)pid + d] = mv.pos[0][d];
+                if (type != RP_MOVE_TRANSLATION)
+                    for (int e = 0; e < 9; e++) S.rot64[9 * (size_t)pid + e] = mv.rot[0][e];
+                for (int q = 0; q < 3 * S.ncen; q++) {
+                    S.cen64[3 * (size_t)pid * S.ncen + q] = mv.cen[q];
+                    S.abs64[3 * (size_t)pid * S.ncen + q] = mv.abs[0][q];
+                }
+                if (S.counting) atomicAdd(S.overlaps, (unsigned long long)(long long)delta);
+            }
+            if (lane == 0 && A.log) {
+                A.log[(size_t)ntypes * (size_t)gbase + mi] = m;
+                A.log_codes[(size_t)ntypes * (size_t)gbase + mi] = code | (acc ? RP_CODE_ACCEPTED : 0);
+            }
+            __syncwarp();
+            n_moves++;
+            n_acc += acc ? 1 : 0;
+            n_ov += (code == 1) ? 1 : 0;
+            n_dom += (code == 2) ? 1 : 0;
+            n_tr += type == 0 ? 1 : 0;
+            n_rot += type != 0 ? 1 : 0;
+            n_acc_tr += (type == 0 && acc) ? 1 : 0;
+        }
+    }
+    if (lane == 0 && n_moves) {
+        unsigned long long *Cn = S.counters;
+        atomicAdd(Cn + 0, (unsigned long long)n_moves);
+        atomicAdd(Cn + 1, (unsigned long long)n_acc);
+        atomicAdd(Cn + 2, (unsigned long long)n_ov);
+        atomicAdd(Cn + 3, (unsigned long long)n_dom);
+        atomicAdd(Cn + 6, (unsigned long long)n_tr);
+        atomicAdd(Cn + 7, (unsigned long long)n_rot);
+        atomicAdd(Cn + 8, (unsigned long long)n_acc_tr);
+    }
+}
+
+// ---- total soft energy ----------------------------------------------------------------
+
+// Per particle i: its pairs with every j > i at every image within reach (each unordered pair
+// once, as Packing::getTotalEnergy sums them); the grid current for every particle.
+template <int KIND>
+__global__ void k_pair_energies(SingleArgs A, double *out) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= A.s.n) return;
+    const DevState &s = A.s;
+    const GridDev &g = A.g;
+    const double *p = s.pos64 + 3 * i;
+    const double *abs = KIND == 2 ? s.abs64 + 3 * i * s.ncen : nullptr;
+    const int own = g.pid_cell[i];
+    const int c[3] = {own % g.dims[0], (own / g.dims[0]) % g.dims[1], own / (g.dims[0] * g.dims[1])};
+    int cells[27];
+    const int nc = neighbour_cells(g, c, cells);
+    double e = 0.0;
+    for (int q = 0; q < nc; q++) {
+        const int cell = cells[q];
+        for (int k = g.start[cell]; k < g.start[cell + 1]; k++) {
+            const int j = g.slot_pid[k];
+            if (j > i) e = dadd(e, candidate_energy<KIND>(A, p, abs, j));
+        }
+    }
+    out[i] = e;
+}
+
+// Sum of n values in one block in a fixed order (deterministic): each thread its stride,
+// then a tree.
+__global__ void k_sum_fixed(const double *v, int64_t n, double *out) {
+    __shared__ double part[1024];
+    double e = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) e = dadd(e, v[i]);
+    part[threadIdx.x] = e;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) part[threadIdx.x] = dadd(part[threadIdx.x], part[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = part[0];
+}
+
 }  // namespace
 
 cudaError_t launch_try_single(const SingleArgs &a, cudaStream_t st) {
-    if (a.s.kind == 0) k_try_single<0><<<1, SINGLE_THREADS, 0, st>>>(a);
-    else if (a.s.kind == 1) k_try_single<1><<<1, SINGLE_THREADS, 0, st>>>(a);
-    else k_try_single<2><<<1, SINGLE_THREADS, 0, st>>>(a);
+    if (a.s.kind == 0) k_try_single<0><<<1, 32, 0, st>>>(a);
+    else if (a.s.kind == 1) k_try_single<1><<<1, 32, 0, st>>>(a);
+    else k_try_single<2><<<1, 32, 0, st>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t launch_commit_single(const DevState &s, SingleTry *t, uint8_t *disp_flag, int32_t *disp_list, int slot,
                                  cudaStream_t st) {
     k_commit_single<<<1, 32, 0, st>>>(s, t, disp_flag, disp_list, slot);
+    return cudaGetLastError();
+}
+
+// One phase of a soft sweep: `nwarps` persistent warps over the phase's active cells.
+cudaError_t launch_soft_sweep(const SoftSweepArgs &a, int nwarps, cudaStream_t st) {
+    if (nwarps <= 0) return cudaSuccess;
+    const unsigned blocks = (unsigned)((nwarps + SOFT_WARPS - 1) / SOFT_WARPS);
+    if (a.c.s.kind == 0) k_soft_sweep<0><<<blocks, SOFT_WARPS * 32, 0, st>>>(a);
+    else if (a.c.s.kind == 1) k_soft_sweep<1><<<blocks, SOFT_WARPS * 32, 0, st>>>(a);
+    else k_soft_sweep<2><<<blocks, SOFT_WARPS * 32, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+// Packing::getTotalEnergy into *out (device): per-particle pair sums into scratch[n], then a
+// fixed-order sum.
+cudaError_t launch_total_energy(const SingleArgs &a, double *scratch, double *out, cudaStream_t st) {
+    const unsigned nb = (unsigned)((a.s.n + 127) / 128);
+    if (a.s.kind == 0) k_pair_energies<0><<<nb, 128, 0, st>>>(a, scratch);
+    else if (a.s.kind == 1) k_pair_energies<1><<<nb, 128, 0, st>>>(a, scratch);
+    else k_pair_energies<2><<<nb, 128, 0, st>>>(a, scratch);
+    k_sum_fixed<<<1, 1024, 0, st>>>(scratch, a.s.n, out);
     return cudaGetLastError();
 }
 

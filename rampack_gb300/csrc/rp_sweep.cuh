@@ -515,22 +515,6 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
                     for (int q = 0; q < 9; q++) R32[q] = rot_inv ? R[3 * (q % 3) + q / 3] : R[q];
                 }
             }
-            if (KIND >= 1) {
-                // the next move's rotation-table entries (its Philox words are in the group
-                // already) into L1 now, off that move's critical path: the FP32 entry the
-                // filter reads and the FP64 one a surviving move reads (48 and 72 bytes,
-                // first and last byte of each)
-                const int nsrc = (mi + 1) & (GW - 1);
-                const uint32_t qa = grp.shfl(rnd_lane.a, nsrc), qb = grp.shfl(rnd_lane.b, nsrc),
-                               qc = grp.shfl(rnd_lane.c, nsrc);
-                const bool qrot = rt || (ntypes == 2 ? (qa >> 31) != 0 : (A.types & 1) == 0);
-                if (nsrc != 0 && mi + 1 < nmoves && qrot && lane < 4) {
-                    const uint32_t qi = rt ? (((qb & 0xffu) | ((qc & 0xffu) << 8)) & A.rtab_mask) : (qb & A.rtab_mask);
-                    const char *pf = lane < 2 ? reinterpret_cast<const char *>(A.rtab32 + 12 * (size_t)qi) + 47 * lane
-                                              : reinterpret_cast<const char *>(A.rtab64 + 9 * (size_t)qi) + 71 * (lane - 2);
-                    asm volatile("prefetch.global.L1 [%0];" ::"l"(pf));
-                }
-            }
         }
         const float4 pcur = cpos[slot];
         const int pid = __float_as_int(pcur.w);

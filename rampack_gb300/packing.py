@@ -219,6 +219,20 @@ class GpuPacking:
         """Packing::toggleWalls: bit i puts hard walls across box side i (rp_set_walls)."""
         self._check(self.lib.rp_set_walls(self.h, int(mask)))
 
+    def set_soft(self, kind: int, epsilon: float = 0.0, sigma: float = 1.0, hard: bool = True):
+        """A soft central interaction on the interaction centres joined to the hard shape, or
+        alone (rp_set_soft): _lib.SOFT_REPULSIVE_LJ or _lib.SOFT_SQUARE_INVERSE_CORE."""
+        self._check(self.lib.rp_set_soft(self.h, int(kind), float(epsilon), float(sigma), 1 if hard else 0))
+
+    def set_temperature(self, temperature: float):
+        self._check(self.lib.rp_set_temperature(self.h, float(temperature)))
+
+    def total_energy(self) -> float:
+        """Packing::getTotalEnergy (rp_total_energy)."""
+        e = C.c_double()
+        self._check(self.lib.rp_total_energy(self.h, C.byref(e)))
+        return float(e.value)
+
     def set_cells_per_warp(self, cells: int):
         """1: a warp sweeps one cell; 2: each half-warp sweeps its own (rp_set_cells_per_warp)."""
         self._check(self.lib.rp_set_cells_per_warp(self.h, int(cells)))
