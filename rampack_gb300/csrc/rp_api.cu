@@ -218,6 +218,7 @@ struct Handle {
     double *cen64 = nullptr;
     int stage_mode = 1;  // staging filter: 0 off, 1 where it pays (cells well above the range), 2 wherever valid
     bool grid_stale = false;  // an upload validated the state; the cell grid is built when first needed
+    bool stale_unshifted = false;  // ... and it is built unshifted (not with the last grid's origin)
     // consistent copy of the FP64 state for asynchronous snapshot downloads
     double *snap64 = nullptr;          // [n][3] positions then [n][9] orientations
     cudaEvent_t snap_free = nullptr;   // recorded when the last download out of snap64 ended
@@ -676,15 +677,19 @@ int check_status(Handle *h) {
     return RP_OK;
 }
 
-// The current cell grid, built (unshifted) if an upload left it stale.
+// The current cell grid, rebuilt if it is stale: unshifted after an upload, else with the
+// origin of the grid it replaces (a soft sweep's log is read against that sweep's domains).
 int ensure_grid(Handle *h) {
     if (!h->grid_stale) return RP_OK;
     double shift[3] = {0, 0, 0};
+    if (!h->stale_unshifted)
+        for (int d = 0; d < 3; d++) shift[d] = h->grid[h->gcur].d.shift[d];
     int rc = setup_grid(h, h->grid[h->gcur], h->box, shift);
     if (rc) return rc;
     rc = rebuild(h, h->gcur, h->pcur);
     if (rc) return rc;
     h->grid_stale = false;
+    h->stale_unshifted = false;
     return RP_OK;
 }
 
@@ -1211,6 +1216,7 @@ int rp_upload_state(void *handle, const double *pos, const double *rot, const do
         Group grp(h, RP_KERNEL_REBUILD, 1);
         RP_CUDA(h, launch_validate(dev_state(h), h->stream));
         h->grid_stale = true;
+        h->stale_unshifted = true;
     }
     rc = check_status(h);  // every particle inside the box, orientations rotations
     if (rc) return rc;
@@ -1310,6 +1316,7 @@ int rp_set_grid(void *handle, const double *shift3, rp_grid_info *info) {
     rc = rebuild(h, h->gcur, h->pcur);
     if (rc) return rc;
     h->grid_stale = false;
+    h->stale_unshifted = false;
     h->can_revert = false;
     if (info) {
         rc = fill_info(h, info);
@@ -1472,6 +1479,7 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
     rc = rebuild(h, h->gcur, h->pcur);
     if (rc) return rc;
     h->grid_stale = false;
+    h->stale_unshifted = false;
     const GridDev &g = h->grid[h->gcur].d;
     // translation step limited to half the smallest box height (TranslationSampler.cpp:39-46)
     double hgt[3];
