@@ -160,7 +160,9 @@ int rp_create_polyspherocylinder(int32_t num_centres, const double *centres, con
 /* Releases the handle and all of its device memory. */
 int rp_destroy(void *handle);
 
-/* Text of the last error on this handle (never NULL; empty when none). */
+/* Text of the last error on this handle (never NULL; empty when none).  With a NULL handle:
+ * why the last rp_create* call of this thread failed on the device (no CUDA device, out of
+ * memory, ...), else "null handle". */
 const char *rp_last_error(void *handle);
 
 /* ---- state ------------------------------------------------------------------------- */
@@ -253,7 +255,7 @@ int rp_revert_scaling(void *handle);
  * accepted) when it falls, 1 (+inf) when it grows, 0 when it stays; an accepted move adds its
  * change to the cached total; a box move recounts everything (dE = -inf / 0 / +inf by the
  * change of the total) and rp_revert_scaling restores the count.  Turning counting on counts
- * all overlaps first.  Spheres and spherocylinders. */
+ * all overlaps first.  Every shape. */
 int rp_set_counting(void *handle, int on);
 int rp_cached_overlaps(void *handle, int64_t *count);
 

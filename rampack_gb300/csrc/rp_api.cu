@@ -938,11 +938,16 @@ using namespace rp;
 extern "C" {
 
 // Device allocations and the stream of a new handle whose shape fields are set.
+// why the last rp_create* on this thread failed, for rp_last_error(NULL)
+static thread_local std::string g_create_error;
+
 static int create_common(Handle *h, int64_t n, int device, void **handle) {
     h->device = device;
     h->n = n;
+    g_create_error.clear();
     auto bail = [&](cudaError_t e) {
         h->err = cudaGetErrorString(e);
+        g_create_error = std::string("creating the packing on device ") + std::to_string(device) + ": " + h->err;
         rp_destroy(h);
         return RP_ERR_CUDA;
     };
@@ -1173,7 +1178,8 @@ int rp_destroy(void *handle) {
 
 const char *rp_last_error(void *handle) {
     Handle *h = static_cast<Handle *>(handle);
-    return h ? h->err.c_str() : "null handle";
+    if (h) return h->err.c_str();
+    return g_create_error.empty() ? "null handle" : g_create_error.c_str();
 }
 
 int rp_upload_state(void *handle, const double *pos, const double *rot, const double *box9) {

@@ -239,16 +239,35 @@ public:
         return aux;
     }
 
+    // Packing::toggleOverlapCounting / getCachedNumberOfOverlaps (core/Packing.cpp:1049-1060)
+    void toggleOverlapCounting(bool countOverlaps) {
+        check(rp_set_counting(h_, countOverlaps ? 1 : 0), "rp_set_counting");
+    }
+    std::size_t getCachedNumberOfOverlaps() const {
+        int64_t c = 0;
+        check(rp_cached_overlaps(h_, &c), "rp_cached_overlaps");
+        return static_cast<std::size_t>(c);
+    }
+
+    // Packing::toggleWalls (core/Packing.cpp:1075-1084)
+    void toggleWalls(const std::array<bool, 3> &axisWalls) {
+        const int32_t mask = (axisWalls[0] ? 1 : 0) | (axisWalls[1] ? 2 : 0) | (axisWalls[2] ? 4 : 0);
+        check(rp_set_walls(h_, mask), "rp_set_walls");
+    }
+
     // The handle, for rp_* calls this class does not wrap (e.g. rp_ramtrj_record).
     void *handle() const { return h_; }
 
-    // The batched move entry: one device sweep (2N moves for translation + rotation).
-    rp_sweep_stats performMoves(double translationStep, double rotationStep, uint64_t seed, uint64_t cycle) {
+    // The batched move entry: one device sweep (2N moves for translation + rotation, N for one
+    // of them or, with `rototranslation`, N moves of both at once).
+    rp_sweep_stats performMoves(double translationStep, double rotationStep, uint64_t seed, uint64_t cycle,
+                                bool rototranslation = false) {
         rp_sweep_params p{};
         p.translation_step = translationStep;
         p.rotation_step = rotationStep;
         p.seed = seed;
         p.counter = cycle;
+        p.flags = rototranslation ? RP_SWEEP_ROTOTRANSLATION : 0;
         rp_sweep_stats st{};
         check(rp_sweep(h_, &p, &st), "rp_sweep");
         return st;

@@ -164,6 +164,40 @@ int main(int argc, char **argv) {
         CHECK(np == static_cast<int64_t>(sc.size()) && snaps == 2 && step == 1 && ver == 0x101);
     }
     {
+        // the calls a Simulation backend makes: overlap counting, rototranslation sweeps, walls.
+        // Spherocylinders along x (length 2, radius 0.5) 3.1 apart along x and 0.95 apart
+        // across: every side-by-side neighbour pair overlaps.
+        std::vector<GpuPacking::Shape> sc;
+        for (int i = 0; i < 5; i++)
+            for (int j = 0; j < 5; j++)
+                for (int k = 0; k < 5; k++) {
+                    GpuPacking::Shape s;
+                    s.position = {3.1 * (i + 0.5), 0.95 * (j + 0.5), 0.95 * (k + 0.5)};
+                    sc.push_back(s);
+                }
+        GpuPacking pk({15.5, 0, 0, 0, 4.75, 0, 0, 0, 4.75}, sc, 0.5, 2.0);
+        pk.toggleOverlapCounting(true);
+        const std::size_t n0 = pk.getCachedNumberOfOverlaps();
+        CHECK(n0 > 0 && n0 == pk.countTotalOverlaps());
+        for (uint64_t c = 0; c < 20; c++) {
+            auto st = pk.performMoves(0.1, 0.1, 7, c, true);
+            CHECK(st.moves == sc.size());
+        }
+        const std::size_t n1 = pk.getCachedNumberOfOverlaps();
+        CHECK(n1 < n0 && n1 == pk.countTotalOverlaps());
+        pk.toggleWalls({true, false, false});
+        pk.toggleOverlapCounting(true);
+        CHECK(pk.getCachedNumberOfOverlaps() == pk.countTotalOverlaps());
+        pk.toggleOverlapCounting(false);
+        bool raised = false;
+        try {
+            (void)pk.getCachedNumberOfOverlaps();
+        } catch (const std::runtime_error &) {
+            raised = true;
+        }
+        CHECK(raised);  // Packing::getCachedNumberOfOverlaps throws with counting off
+    }
+    {
         // two bent rods (PolyspherocylinderTraits, two spherocylinders each): an overlap that
         // only the segments find (centres 0.695 apart, inspheres 0.5), and none where only the
         // circumspheres meet (parallel segments 0.56 apart)
