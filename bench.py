@@ -291,17 +291,18 @@ def cycle(g, k, seed, rng, stats=False):
 PROFILES = {"sc-1e6": "k_sweep_sc_n1e6.md", "banana-1e5": "k_sweep_banana_n1e5.md",
             "bent-rods-1e5": "k_sweep_bent_rods_n1e5.md",
             "replicas-64": "k_b_sweep_replicas_64.md"}
+REBUILD_PROFILES = {"sc-1e6": "rebuild_sc_n1e6.md"}
 
 
-def read_profile_traffic(workload):
-    """Per-launch DRAM traffic of the workload's sweep kernel from its committed ncu summary
-    (one --set full capture of a steady-state launch), if any."""
-    name = PROFILES.get(workload)
+def read_profile_traffic(workload, key="traffic_bytes_per_launch", profiles=None):
+    """Per-launch DRAM traffic of the workload's sweep kernel (or, with another key and table,
+    per rebuild of the cell grid) from its committed ncu summary, if any."""
+    name = (profiles or PROFILES).get(workload)
     path = os.path.join(ROOT, "profiles", name) if name else ""
     if not name or not os.path.exists(path):
         return None
     for line in open(path):
-        if line.strip().startswith("traffic_bytes_per_launch:"):
+        if line.strip().startswith(key + ":"):
             try:
                 return float(line.split(":", 1)[1].strip().split()[0])
             except ValueError:
@@ -376,6 +377,7 @@ def main_gpu(args):
 
     s0 = g.stats()
     b0 = box_counts()
+    gc0 = g.grid_counters()
     g.set_timing(True)
     clocks = Clocks(local)
     clocks.start()
@@ -399,6 +401,7 @@ def main_gpu(args):
     timing = g.timing()
     g.set_timing(False)
     s1 = g.stats()
+    gc1 = g.grid_counters()
     if dist:
         ms = reduce_max(ms, dist, device=f"cuda:{local}")
         dist.barrier()
@@ -436,6 +439,22 @@ def main_gpu(args):
     else:
         peak, peak_src = 6800.0, "fallback"
     traffic = read_profile_traffic(args.workload)
+    # the cell-grid rebuild (k_assign, the scan, k_scatter, k_cell_finish): algorithmic bytes
+    # per rebuild N (12 + 12) + 2 (C + 1) 4 -- per particle a position (12 B) in and its cell,
+    # slot and rank indices (12 B) out, plus the cell histogram and offsets -- against its
+    # CUDA-event time per rebuild
+    rebuild_ms, rebuild_groups = timing["rebuild"]
+    rebuilds = gc1["rebuilds"] - gc0["rebuilds"]
+    b_rebuild = n * 24 + 2 * (ncell + 1) * 4
+    rebuild_avg_ms = rebuild_ms / max(1, rebuild_groups)
+    rebuild_achieved = b_rebuild / (rebuild_avg_ms / 1e3) / 1e9 if rebuild_groups else 0.0
+    roofline_rebuild = {"bound": "hbm", "achieved": rebuild_achieved, "peak": peak, "unit": "GB/s",
+                        "frac": rebuild_achieved / peak,
+                        "traffic": read_profile_traffic(args.workload, "traffic_bytes_per_rebuild", REBUILD_PROFILES),
+                        "kernel": "cell-grid rebuild (k_assign, k_scan_blocks, k_scan_sums, k_scan_add, k_scatter, "
+                                  "k_cell_finish)",
+                        "avg_rebuild_ms": rebuild_avg_ms, "bytes_per_rebuild": b_rebuild,
+                        "rebuilds": rebuilds, "box_moves_on_kept_grid": gc1["remaps"] - gc0["remaps"]}
     # bytes every cycle touches: the FP64 state (96 B), the FP32 mirror (32 B) and the cell
     # lists the rebuild writes (slot, particle, cell and rank indices and the by-particle FP32
     # position: 32 B) per particle, plus the polysphere centres
@@ -511,6 +530,7 @@ def main_gpu(args):
                          "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
                          else "fallback 6.8 TB/s",
                          "avg_launch_ms": avg_launch_ms, "bytes_per_launch": b_launch},
+            "roofline_rebuild": roofline_rebuild,
             "kernel_ms": {kname: {"ms": v[0], "groups": v[1]} for kname, v in timing.items()},
             "acceptance": acc_rate, "guard_band": {"pair_tests": pairs, "fp64_pairs": fp64,
                                                    "rate": fp64 / max(1, pairs)},

@@ -39,6 +39,7 @@ extern "C" {
 #define RP_SHAPE_SPHERE 0
 #define RP_SHAPE_SPHEROCYLINDER 1
 #define RP_SHAPE_POLYSPHERE 2     /* created by rp_create_polysphere */
+#define RP_SHAPE_CONVEX 3         /* generic convex body, created by rp_create_convex */
 #define RP_MAX_CENTRES 8          /* spheres per polysphere */
 
 #define RP_MOVE_TRANSLATION 0
@@ -117,10 +118,10 @@ typedef struct rp_sweep_stats {
 } rp_sweep_stats;
 
 /* Kernel groups timed by rp_get_timing. */
-#define RP_KERNEL_SWEEP 0         /* checkerboard move sweep (one launch per phase) */
+#define RP_KERNEL_SWEEP 0         /* checkerboard move sweep (one launch per phase; the sweep's rotation table) */
 #define RP_KERNEL_REBUILD 1       /* cell-grid rebuild (assign, scan, scatter, finish) */
 #define RP_KERNEL_COUNT 2         /* all-pairs overlap recount */
-#define RP_KERNEL_RESCALE 3       /* box rescale */
+#define RP_KERNEL_RESCALE 3       /* box rescale (and the kept-grid remap of a box move) */
 #define RP_KERNEL_OVERFLOW 4      /* large-capacity rerun of oversized neighbourhoods */
 #define RP_KERNEL_ORDER 5         /* partner ranking of the learned ordering */
 #define RP_KERNEL_MLP 6           /* ranking-network training and inference */
@@ -156,6 +157,18 @@ int rp_create_polysphere(int32_t num_centres, const double *centres, const doubl
  * (r_a + r_b), circumspheres (c_a + c_b, c = r + |half axis|), then the segment distance. */
 int rp_create_polyspherocylinder(int32_t num_centres, const double *centres, const double *half_axes,
                                  const double *radii, int64_t n, int device, void **handle);
+
+/* Creates an engine for n generic convex bodies (GenericXenoCollideTraits,
+ * core/shapes/GenericXenoCollideTraits.h) described by an XCBodyBuilder script: the commands
+ * of XCBodyBuilder::processCommand (geometry/xenocollide/XCBodyBuilder.cpp:181-294) -- point,
+ * segment, rectangle, cuboid, disk, sphere, ellipse, ellipsoid, football, saucer, move, rot,
+ * sum [k], diff, wrap [k], dup k, pop, swap -- one per line or separated by ';'.  Pairs are
+ * decided as XenoCollideTraits::overlapBetween (core/shapes/XenoCollideTraits.h:118-140):
+ * circumspheres, inspheres, then XenoCollide's portal refinement with tolerance 1e-12, every
+ * move in FP64.  Sweeps, single moves, overlap counts and counting mode, box moves; not
+ * walls, orientation fixes, move lists, soft parts or the learned ordering (RP_ERR_UNSUPPORTED).
+ * An invalid script fails with RP_ERR_ARG and the builder's message in rp_last_error(NULL). */
+int rp_create_convex(const char *script, int64_t n, int device, void **handle);
 
 /* Releases the handle and all of its device memory. */
 int rp_destroy(void *handle);
@@ -281,6 +294,12 @@ int rp_nematic_order(void *handle, double *q9, double *p2);
 
 /* Cumulative counters of all sweeps and move lists since creation. */
 int rp_get_stats(void *handle, rp_sweep_stats *stats);
+
+/* Packing::getNeighbourGridRebuilds (core/Packing.h:423): full cell-grid rebuilds since
+ * creation; and the box moves whose grid kept the old cells (same divisions and origin,
+ * every particle still in its cell: one pass recomputes the FP32 cell-local positions,
+ * giving the grid a rebuild would build). */
+int rp_get_grid_counters(void *handle, uint64_t *rebuilds, uint64_t *remaps);
 
 /* The cudaStream_t on which all device work of the handle runs (for the caller's own
  * CUDA events); no reference counterpart (the reference is CPU-only). */

@@ -128,6 +128,7 @@ SIGNATURES = {
     "rp_try_scaling": (C.c_int, [_P, _D, _D]),
     "rp_revert_scaling": (C.c_int, [_P]),
     "rp_get_stats": (C.c_int, [_P, C.POINTER(SweepStats)]),
+    "rp_get_grid_counters": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "rp_get_stream": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
     "rp_set_timing": (C.c_int, [_P, C.c_int]),
     "rp_get_timing": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]),

@@ -14,7 +14,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "librampack_gb300.so")
-SOURCES = ["rp_kernels.cu", "rp_api.cu", "rp_static.cu", "rp_mlp.cu", "rp_fix.cu", "rp_observe.cu", "rp_batch.cu", "rp_io.cu", "rp_sim.cu", "rp_correlation.cu", "rp_single.cu"]
+SOURCES = ["rp_kernels.cu", "rp_api.cu", "rp_static.cu", "rp_mlp.cu", "rp_fix.cu", "rp_observe.cu", "rp_batch.cu", "rp_io.cu", "rp_sim.cu", "rp_correlation.cu", "rp_single.cu", "rp_xc.cu"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 

@@ -17,6 +17,7 @@
 namespace rp {
 
 cudaError_t launch_rebuild(const DevState &s, const GridDev &g, int32_t *block_sums, cudaStream_t st);
+cudaError_t launch_remap(const DevState &s, const GridDev &g, const GridDev &old, int *moved, cudaStream_t st);
 cudaError_t launch_validate(const DevState &s, cudaStream_t st);
 cudaError_t launch_rescale(const double *src, double *dst, int64_t n, const double *old_inv, const double *new_box,
                            cudaStream_t st);
@@ -63,6 +64,7 @@ size_t sweep_smem_per_half(int kind, int cap);
 int sweep_half_blocks_per_sm(int kind, int cap);
 cudaError_t launch_try_single(const SingleArgs &a, cudaStream_t st);
 cudaError_t launch_soft_sweep(const SoftSweepArgs &a, int nwarps, cudaStream_t st);
+cudaError_t launch_count_fp64(const SingleArgs &a, int early, unsigned long long *out, int *flag, cudaStream_t st);
 cudaError_t launch_total_energy(const SingleArgs &a, double *scratch, double *out, cudaStream_t st);
 cudaError_t launch_commit_single(const DevState &s, SingleTry *t, uint8_t *disp_flag, int32_t *disp_list, int slot,
                                  cudaStream_t st);
@@ -219,12 +221,15 @@ struct Handle {
     int stage_mode = 1;  // staging filter: 0 off, 1 where it pays (cells well above the range), 2 wherever valid
     bool grid_stale = false;  // an upload validated the state; the cell grid is built when first needed
     bool stale_unshifted = false;  // ... and it is built unshifted (not with the last grid's origin)
+    uint64_t grid_rebuilds = 0;    // full cell-grid rebuilds (Packing::getNeighbourGridRebuilds)
+    uint64_t grid_remaps = 0;      // box moves whose grid kept the old cells (k_remap)
     // consistent copy of the FP64 state for asynchronous snapshot downloads
     double *snap64 = nullptr;          // [n][3] positions then [n][9] orientations
     cudaEvent_t snap_free = nullptr;   // recorded when the last download out of snap64 ended
     double *abs64[2] = {nullptr, nullptr};
     double *cthr64 = nullptr;
     double *cbody_dev = nullptr;    // body-frame centres on the device
+    XcShape *d_xc = nullptr;        // generic convex bodies: the geometry on the device
     // batched replicas: the batch owns the rotation table, counters, status word and the
     // device copy of the ActiveDomain bounds (setup_grid leaves the bounds in bounds_host)
     bool batch_member = false;
@@ -398,6 +403,7 @@ DevState dev_state(Handle *h) {
     DevState s{};
     s.n = h->n;
     s.kind = h->shape.kind;
+    s.xc = h->d_xc;
     std::memcpy(s.box, h->box, sizeof(s.box));
     std::memcpy(s.inv, h->inv, sizeof(s.inv));
     for (int i = 0; i < 9; i++) s.inv32[i] = static_cast<float>(h->inv[i]);
@@ -649,6 +655,7 @@ int rebuild(Handle *h, int gi, int pi) {
         Group grp(h, RP_KERNEL_REBUILD, 6);
         RP_CUDA(h, launch_rebuild(s, h->grid[gi].d, h->block_sums, h->stream));
     }
+    h->grid_rebuilds++;
     // a grid built from the current positions lists every particle where it is
     if (!h->disp_host.empty()) {
         RP_CUDA(h, cudaMemsetAsync(h->d_disp_flag, 0, static_cast<size_t>(h->n), h->stream));
@@ -657,6 +664,32 @@ int rebuild(Handle *h, int gi, int pi) {
     }
     h->grid_patched = false;
     return RP_OK;
+}
+
+// The grid of a rescaled state (rp_try_scaling; h->gcur / h->pcur already name grid `ng` and
+// the rescaled positions): when its divisions and origin are the old grid's and the old grid
+// lists every particle where it is, the old cells are kept and only the FP32 cell-local
+// positions recomputed (k_remap, one pass, the grid a rebuild would build); a particle that
+// changed cell through rounding falls back to the full rebuild.
+int remap_or_rebuild(Handle *h, int old_g, int ng, int np) {
+    const GridDev &o = h->grid[old_g].d, &g = h->grid[ng].d;
+    bool same = !h->grid_patched && !h->grid_stale && h->disp_host.empty() && o.ncell == g.ncell && o.slot_pid;
+    for (int d = 0; d < 3; d++) same = same && o.dims[d] == g.dims[d] && o.shift[d] == g.shift[d];
+    if (same) {
+        RP_CUDA(h, cudaMemsetAsync(h->flag, 0, sizeof(int), h->stream));
+        {
+            Group grp(h, RP_KERNEL_RESCALE, 1);
+            RP_CUDA(h, launch_remap(dev_state(h), g, o, h->flag, h->stream));
+        }
+        int moved = 0;
+        RP_CUDA(h, cudaMemcpyAsync(&moved, h->flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+        RP_CUDA(h, cudaStreamSynchronize(h->stream));
+        if (!moved) {
+            h->grid_remaps++;
+            return RP_OK;
+        }
+    }
+    return rebuild(h, ng, np);
 }
 
 int check_status(Handle *h) {
@@ -1104,6 +1137,57 @@ int rp_create_polyspherocylinder(int32_t num_centres, const double *centres, con
     return create_multi_centre(num_centres, centres, half_axes, radii, n, device, handle);
 }
 
+// Generic convex bodies (GenericXenoCollideTraits): the XCBodyBuilder script's geometry on the
+// device; the range is twice its circumsphere radius (XenoCollideTraits::getRangeRadius,
+// core/shapes/XenoCollideTraits.h:160-172).
+int rp_create_convex(const char *script, int64_t n, int device, void **handle) {
+    if (!script || !handle || n <= 0 || n > (1ll << 31) - 1) return RP_ERR_ARG;
+    XcShape *xs = new (std::nothrow) XcShape();
+    if (!xs) return RP_ERR_ARG;
+    std::string err;
+    if (!xc_build(script, *xs, err)) {
+        g_create_error = "convex body: " + err;
+        delete xs;
+        return RP_ERR_ARG;
+    }
+    if (!(xs->circ > 0)) {
+        g_create_error = "convex body: the body has no extent (circumsphere radius 0)";
+        delete xs;
+        return RP_ERR_ARG;
+    }
+    // the support function's explicit stack lives in each thread's local memory
+    size_t stack = 0;
+    if (cudaSetDevice(device) == cudaSuccess && cudaDeviceGetLimit(&stack, cudaLimitStackSize) == cudaSuccess &&
+        stack < 4096)
+        cudaDeviceSetLimit(cudaLimitStackSize, 4096);
+    Handle *h = new (std::nothrow) Handle();
+    if (!h) {
+        delete xs;
+        return RP_ERR_ARG;
+    }
+    h->shape.kind = RP_SHAPE_CONVEX;
+    h->shape.radius = xs->circ;
+    h->range = 2 * xs->circ;
+    h->ref_range = h->range;
+    h->total_range = h->range;
+    int rc = create_common(h, n, device, handle);
+    if (rc) {
+        delete xs;
+        return rc;
+    }
+    cudaError_t e = cudaMalloc(&h->d_xc, sizeof(XcShape));
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_xc, xs, sizeof(XcShape), cudaMemcpyHostToDevice);
+    delete xs;
+    if (e != cudaSuccess) {
+        g_create_error = std::string("creating the packing on device ") + std::to_string(device) + ": " +
+                         cudaGetErrorString(e);
+        rp_destroy(h);
+        *handle = nullptr;
+        return RP_ERR_CUDA;
+    }
+    return RP_OK;
+}
+
 int rp_destroy(void *handle) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h) return RP_ERR_ARG;
@@ -1114,6 +1198,7 @@ int rp_destroy(void *handle) {
         cudaEventDestroy(h->snap_free);
     }
     cudaFree(h->snap64);
+    cudaFree(h->d_xc);
     for (int i = 0; i < 2; i++) {
         cudaFree(h->pos64[i]);
         cudaFree(h->trans[i]);
@@ -1251,6 +1336,23 @@ int rp_download_state(void *handle, double *pos, double *rot, double *box9) {
     return RP_OK;
 }
 
+// The arguments of the FP64 kernels (single moves, soft and convex sweeps, FP64 recounts) for the
+// current state: the FP32 pre-filter reach of a separation at one image is the interaction
+// range (body range for multi-centre bodies) plus a margin far above the FP32 rounding of
+// coordinates of the box's size.
+SingleArgs single_args(Handle *h) {
+    SingleArgs a{};
+    a.s = dev_state(h);
+    a.g = h->grid[h->gcur].d;
+    double pmax = 0;
+    for (int i = 0; i < 3; i++)
+        pmax = std::max(pmax, std::fabs(h->box[3 * i]) + std::fabs(h->box[3 * i + 1]) + std::fabs(h->box[3 * i + 2]));
+    const double reach = h->range * (1.0 + 1e-3) + 1e-4 * (pmax + h->range);
+    a.reach2 = static_cast<float>(reach * reach);
+    for (int i = 0; i < 9; i++) a.box32[i] = static_cast<float>(h->box[i]);
+    return a;
+}
+
 int rp_count_overlaps(void *handle, int early_exit, int64_t *out_count) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h || !out_count) return fail(h, RP_ERR_ARG, "null argument");
@@ -1282,7 +1384,12 @@ int rp_count_overlaps(void *handle, int early_exit, int64_t *out_count) {
         s.cq_count = h->cq_count;
         s.cq_cap = Handle::CQ_CAP;
     }
-    {
+    if (h->shape.kind == RP_SHAPE_CONVEX) {
+        // generic convex bodies: every pair in FP64 over the images within reach
+        SingleArgs a = single_args(h);
+        Group grp(h, RP_KERNEL_COUNT, 1);
+        RP_CUDA(h, launch_count_fp64(a, early_exit ? 1 : 0, h->count_out, h->flag, h->stream));
+    } else {
         Group grp(h, RP_KERNEL_COUNT, defer ? 2 : 1);
         RP_CUDA(h, launch_count(s, h->grid[h->gcur].d, early_exit ? 1 : 0, h->count_out, h->flag, h->stream));
     }
@@ -1370,7 +1477,8 @@ int rp_get_grid(void *handle, rp_grid_info *info, int32_t *cell_of_particle, dou
 int rp_run_moves(void *handle, const rp_move *moves, int64_t n, uint8_t *out_codes) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h || (!moves && n > 0)) return fail(h, RP_ERR_ARG, "null argument");
-    if (h->soft) return fail(h, RP_ERR_UNSUPPORTED, "move lists with a soft part (use rp_try_move or rp_sweep)");
+    if (h->soft || h->shape.kind == RP_SHAPE_CONVEX)
+        return fail(h, RP_ERR_UNSUPPORTED, "move lists with a soft part or a convex body (use rp_try_move or rp_sweep)");
     if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
     if (n <= 0) return RP_OK;
     if (n > (1ll << 31) - 1) return fail(h, RP_ERR_ARG, "too many moves");
@@ -1507,7 +1615,7 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
     if (stats) RP_CUDA(h, cudaMemsetAsync(h->counters, 0, sizeof(unsigned long long) * NUM_COUNTERS, h->stream));
     RP_CUDA(h, cudaMemsetAsync(h->item_counters, 0, sizeof(int32_t) * 64, h->stream));
     if (types & (2 | SWEEP_ROTOTRANSLATION)) {
-        Group grp(h, RP_KERNEL_REBUILD, 1);
+        Group grp(h, RP_KERNEL_SWEEP, 1);
         RP_CUDA(h, launch_rot_table(h->rtab64, h->rtab32, ROT_TABLE, p->seed, p->counter,
                                     static_cast<float>(p->rotation_step), h->stream));
     }
@@ -1516,10 +1624,13 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
         if (rc2) return rc2;
     }
     h->since_rank++;
-    if (h->soft) {
-        // a soft part: every move decided in FP64 (hard part, then the energy change with the
-        // Metropolis test at the handle's temperature), one warp per active cell
-        if (types == SWEEP_ROTOTRANSLATION) return fail(h, RP_ERR_UNSUPPORTED, "rototranslations with a soft part");
+    const bool fp64_sweep = h->soft || h->shape.kind == RP_SHAPE_CONVEX;
+    if (fp64_sweep) {
+        // a soft part or a generic convex body: every move decided in FP64 (hard part, then the
+        // energy change with the Metropolis test at the handle's temperature), one warp per
+        // active cell
+        if (types == SWEEP_ROTOTRANSLATION)
+            return fail(h, RP_ERR_UNSUPPORTED, "rototranslations with a soft part or a convex body");
         SoftSweepArgs sa{};
         sa.c.s = dev_state(h);
         sa.c.g = g;
@@ -1557,7 +1668,7 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
         h->grid_patched = false;
     }
     int phase_no = 0;
-    for (int ph : (h->soft ? std::vector<int>{} : phases)) {
+    for (int ph : (fp64_sweep ? std::vector<int>{} : phases)) {
         SweepArgs a = base_args(h);
         if (h->order_mode != RP_ORDER_OFF) a.partners = h->partners;
         if (h->pair_cap > 0) {
@@ -1748,7 +1859,7 @@ int rp_try_scaling(void *handle, const double *new_box9, double *dE) {
     h->gcur = ng;
     double shift[3] = {h->grid[old_g].d.shift[0], h->grid[old_g].d.shift[1], h->grid[old_g].d.shift[2]};
     int rc = setup_grid(h, h->grid[ng], h->box, shift);
-    if (rc == RP_OK) rc = rebuild(h, ng, np);
+    if (rc == RP_OK) rc = remap_or_rebuild(h, old_g, ng, np);
     if (rc == RP_OK && h->ncen > 0) {
         // Packing::tryScaling recalculates the absolute centres (core/Packing.cpp:186-187)
         Group grp(h, RP_KERNEL_RESCALE, 1);
@@ -2067,6 +2178,7 @@ int rp_renormalize_orientations(void *handle, int allow_overlaps, int64_t *rejec
     if (!h || !rejected) return fail(h, RP_ERR_ARG, "null argument");
     if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
     if (h->soft) return fail(h, RP_ERR_UNSUPPORTED, "orientation fixes with a soft part");
+    if (h->shape.kind == RP_SHAPE_CONVEX) return fail(h, RP_ERR_UNSUPPORTED, "orientation fixes of convex bodies");
     RP_CUDA(h, cudaSetDevice(h->device));
     h->try_valid = false;
     {
@@ -2220,6 +2332,8 @@ int rp_mlp_gradient(void *handle, const float *feats, const uint8_t *labels, int
 int rp_pair_log_enable(void *handle, int64_t capacity, int32_t every) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h || capacity < 0 || (capacity > 0 && every <= 0)) return fail(h, RP_ERR_ARG, "bad argument");
+    if (capacity > 0 && h->shape.kind == RP_SHAPE_CONVEX)
+        return fail(h, RP_ERR_UNSUPPORTED, "the pair log of convex bodies");
     RP_CUDA(h, cudaSetDevice(h->device));
     RP_CUDA(h, cudaStreamSynchronize(h->stream));
     cudaFree(h->pair_feats);
@@ -2321,9 +2435,18 @@ int rp_mlp_train(void *handle, int32_t epochs, int32_t batch, float lr, uint64_t
     return RP_OK;
 }
 
+int rp_get_grid_counters(void *handle, uint64_t *rebuilds, uint64_t *remaps) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !rebuilds || !remaps) return fail(h, RP_ERR_ARG, "null argument");
+    *rebuilds = h->grid_rebuilds;
+    *remaps = h->grid_remaps;
+    return RP_OK;
+}
+
 int rp_set_walls(void *handle, int32_t mask) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h || mask < 0 || mask > 7) return fail(h, RP_ERR_ARG, "wall mask outside 0..7");
+    if (mask && h->shape.kind == RP_SHAPE_CONVEX) return fail(h, RP_ERR_UNSUPPORTED, "walls with convex bodies");
     h->walls = mask;
     h->try_valid = false;
     return RP_OK;
@@ -2351,6 +2474,7 @@ int rp_set_soft(void *handle, int32_t kind, double epsilon, double sigma, int32_
     Handle *h = static_cast<Handle *>(handle);
     if (!h) return RP_ERR_ARG;
     if (h->batch_member) return fail(h, RP_ERR_UNSUPPORTED, "soft parts on a batch replica");
+    if (h->shape.kind == RP_SHAPE_CONVEX) return fail(h, RP_ERR_UNSUPPORTED, "soft parts of convex bodies");
     if (kind != RP_SOFT_NONE && kind != RP_SOFT_REPULSIVE_LJ && kind != RP_SOFT_SQUARE_INVERSE_CORE) {
         if (kind == RP_SOFT_LENNARD_JONES)
             return fail(h, RP_ERR_UNSUPPORTED,
@@ -2427,6 +2551,8 @@ int rp_get_cells_per_warp(void *handle, int32_t *last) {
 int rp_set_ordering(void *handle, int32_t mode, int32_t every) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h || mode < RP_ORDER_OFF || mode > RP_ORDER_DISTANCE || every <= 0) return fail(h, RP_ERR_ARG, "bad argument");
+    if (mode != RP_ORDER_OFF && h->shape.kind == RP_SHAPE_CONVEX)
+        return fail(h, RP_ERR_UNSUPPORTED, "the learned ordering of convex bodies");
     h->order_mode = mode;
     h->order_every = every;
     h->partners_valid = false;

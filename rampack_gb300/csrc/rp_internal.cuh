@@ -8,6 +8,7 @@
 
 #include "rp_geom.cuh"
 #include "rp_mlp.cuh"
+#include "rp_xc.cuh"
 #include "../../include/rampack_gb300.h"
 
 namespace rp {
@@ -81,6 +82,7 @@ struct DeferredPair {
 struct DevState {
     int64_t n;
     int kind;
+    const XcShape *xc;    // generic convex bodies (kind 3): the body's geometry, device memory
     double box[9], inv[9];
     double *pos64;        // [n][3]
     double *rot64;        // [n][9]

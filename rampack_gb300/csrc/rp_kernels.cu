@@ -95,6 +95,31 @@ __global__ void k_cell_finish(DevState s, GridDev g) {
     if (cell < g.ncell) finish_one(s, g, cell);
 }
 
+// The grid of a rescaled box whose cells are the old grid's cells (same divisions and origin):
+// after a box rescale every particle keeps its relative coordinates up to rounding, so it
+// normally stays in its cell.  The cell lists, the FP32 axes and centres (unchanged by a
+// rescale) are copied from the old grid in its slot order (particle indices ascending in every
+// cell, as a rebuild leaves them) and the FP32 cell-local positions are recomputed from the
+// rescaled FP64 positions with the rebuild's arithmetic, so the result is the grid a full
+// rebuild would build.  A particle whose cell changed raises *moved: the caller then rebuilds.
+// One pass, bound like k_assign by the FP64 relative coordinates.
+__global__ void k_remap(DevState s, GridDev g, GridDev old, int *moved) {
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k <= g.ncell) g.start[k] = old.start[k];
+    if (k == 0) *g.max_occ = *old.max_occ;
+    if (k >= s.n) return;
+    const int pid = old.slot_pid[k];
+    float3 loc;
+    const int cell = locate_one(s, g, pid, loc);
+    if (cell != old.pid_cell[pid]) *moved = 1;
+    g.slot_pid[k] = pid;
+    g.pid_slot[pid] = static_cast<int32_t>(k);
+    g.pid_cell[pid] = cell;
+    g.mpos[k] = make_float4(loc.x, loc.y, loc.z, __int_as_float(pid));
+    g.maxis[k] = old.maxis[k];
+    for (int b = 0; b < s.ncen; b++) g.mcen[k * s.ncen + b] = old.mcen[k * s.ncen + b];
+}
+
 // Absolute centres of every polysphere (Packing::recalculateAbsoluteInteractionCentres,
 // core/Packing.cpp:1041-1047): position + rotated centre, then the PBC correction of
 // that point (core/PeriodicBoundaryConditions.cpp:11-22).  One thread per centre.
@@ -260,6 +285,12 @@ cudaError_t launch_rebuild(const DevState &s, const GridDev &g, int32_t *block_s
     k_scan_add<<<(g.ncell + 255) / 256, 256, 0, st>>>(g.start, block_sums, g.ncell);
     k_scatter<<<nb, tb, 0, st>>>(s, g);
     k_cell_finish<<<(g.ncell + 127) / 128, 128, 0, st>>>(s, g);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_remap(const DevState &s, const GridDev &g, const GridDev &old, int *moved, cudaStream_t st) {
+    const int64_t threads = s.n > static_cast<int64_t>(g.ncell) + 1 ? s.n : static_cast<int64_t>(g.ncell) + 1;
+    k_remap<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(s, g, old, moved);
     return cudaGetLastError();
 }
 

@@ -92,17 +92,27 @@ __device__ double soft_energy(const DevState &s, double d2) {
     return 0.0;
 }
 
-// Pair test of a sphere or spherocylinder mover (position p, axis a) against particle j at
-// translation t (null: no grid in the reference, the periodic boundary conditions' nearest
-// image), SphereTraits.cpp:56-65 / SpherocylinderTraits.cpp:28-46.
+// Pair test of a sphere, spherocylinder or generic convex mover (position p, axis a,
+// orientation rot) against particle j at translation t (null: no grid in the reference, the
+// periodic boundary conditions' nearest image), SphereTraits.cpp:56-65 /
+// SpherocylinderTraits.cpp:28-46 / XenoCollideTraits.h:118-140 (the mover is the first body,
+// as in Packing::countParticleOverlaps).
 template <int KIND>
-__device__ bool body_overlap(const DevState &s, d3 p, d3 a, int j, const d3 *t) {
+__device__ bool body_overlap(const DevState &s, d3 p, d3 a, const double *rot, int j, const d3 *t) {
     const d3 pj = load_d3(s.pos64 + 3 * (size_t)j);
     const double *rj = s.rot64 + 9 * (size_t)j;
-    const d3 aj{rj[2], rj[5], rj[8]};
-    if (t) return exact_overlap(s.ex, p, a, pj, aj, *t);
-    if (KIND == 0) return pbc_distance2(s.box, s.inv, p, pj) < s.ex.sphere_thr;
-    return exact_overlap(s.ex, p, a, pj, aj, pbc_translation(s.box, s.inv, p, pj));
+    if constexpr (KIND == 3) {
+        const d3 q = add3(pj, t ? *t : pbc_translation(s.box, s.inv, p, pj));
+        bool stuck = false;
+        const bool ov = xc_overlap(*s.xc, p, rot, q, rj, stuck);
+        if (stuck) atomicOr(s.status, ST_NUMERIC);
+        return ov;
+    } else {
+        const d3 aj{rj[2], rj[5], rj[8]};
+        if (t) return exact_overlap(s.ex, p, a, pj, aj, *t);
+        if (KIND == 0) return pbc_distance2(s.box, s.inv, p, pj) < s.ex.sphere_thr;
+        return exact_overlap(s.ex, p, a, pj, aj, pbc_translation(s.box, s.inv, p, pj));
+    }
 }
 
 // Centre a of a multi-centre mover (absolute centre pa, half axis ha) against centre b of body
@@ -144,20 +154,20 @@ __device__ __forceinline__ d3 image_translation(const DevState &s, int mx, int m
 // wrapped into the box on its own, so images are enumerated per centre pair); at most 1 with
 // `early`.
 template <int KIND>
-__device__ int candidate_overlaps(const SingleArgs &A, const double *p, d3 a, const double *abs, const double *hax,
-                                  int j, bool early) {
+__device__ int candidate_overlaps(const SingleArgs &A, const double *p, d3 a, const double *rot, const double *abs,
+                                  const double *hax, int j, bool early) {
     const DevState &s = A.s;
     int cnt = 0;
     if constexpr (KIND != 2) {
         const d3 pp{p[0], p[1], p[2]};
-        if (s.pbc_fold) return body_overlap<KIND>(s, pp, a, j, nullptr) ? 1 : 0;
+        if (s.pbc_fold) return body_overlap<KIND>(s, pp, a, rot, j, nullptr) ? 1 : 0;
         const double *pj = s.pos64 + 3 * (size_t)j;
         for (int mx = -1; mx <= 1; mx++)
             for (int my = -1; my <= 1; my++)
                 for (int mz = -1; mz <= 1; mz++) {
                     if (!within_reach(A, pj, p, mx, my, mz)) continue;
                     const d3 t = image_translation(s, mx, my, mz);
-                    if (body_overlap<KIND>(s, pp, a, j, &t)) {
+                    if (body_overlap<KIND>(s, pp, a, rot, j, &t)) {
                         if (early) return 1;
                         cnt++;
                     }
@@ -252,7 +262,8 @@ __device__ int warp_overlaps(const SingleArgs &A, const Mover &mv, int which, bo
         if (k < total) {
             const int j = candidate_at(A, mv, which, k, in_cells);
             // the self-skip compares particle indices (core/Packing.cpp:633-635)
-            if (j >= 0 && j != pid) c = candidate_overlaps<KIND>(A, mv.pos[which], a, mv.abs[which], hax, j, early);
+            if (j >= 0 && j != pid)
+                c = candidate_overlaps<KIND>(A, mv.pos[which], a, mv.rot[which], mv.abs[which], hax, j, early);
         }
         if (early && __any_sync(FULL, c != 0)) return 1;
         cnt += c;
@@ -592,6 +603,42 @@ __global__ void k_pair_energies(SingleArgs A, double *out) {
     out[i] = e;
 }
 
+// Packing::countTotalOverlaps for generic convex bodies (core/Packing.cpp:519-559), every pair
+// decided in FP64: per particle i its pairs with every j > i at every image within reach (the
+// lower index as the first body), with the early-exit flag polled per candidate cell.
+template <int KIND>
+__global__ void k_count_fp64(SingleArgs A, int early, unsigned long long *out, int *flag) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= A.s.n) return;
+    const DevState &s = A.s;
+    const GridDev &g = A.g;
+    const double *p = s.pos64 + 3 * i;
+    const double *rot = s.rot64 + 9 * i;
+    const d3 a{rot[2], rot[5], rot[8]};
+    const int own = g.pid_cell[i];
+    const int c[3] = {own % g.dims[0], (own / g.dims[0]) % g.dims[1], own / (g.dims[0] * g.dims[1])};
+    int cells[27];
+    const int nc = neighbour_cells(g, c, cells);
+    unsigned long long cnt = 0;
+    for (int q = 0; q < nc; q++) {
+        if (early && *(volatile int *)flag) break;
+        const int cell = cells[q];
+        for (int k = g.start[cell]; k < g.start[cell + 1]; k++) {
+            const int j = g.slot_pid[k];
+            if (j <= i) continue;
+            const int o = candidate_overlaps<KIND>(A, p, a, rot, nullptr, nullptr, j, early != 0);
+            if (o) {
+                cnt += (unsigned long long)o;
+                if (early) {
+                    atomicExch(flag, 1);
+                    break;
+                }
+            }
+        }
+    }
+    if (cnt) atomicAdd(out, cnt);
+}
+
 // Sum of n values in one block in a fixed order (deterministic): each thread its stride,
 // then a tree.
 __global__ void k_sum_fixed(const double *v, int64_t n, double *out) {
@@ -612,7 +659,8 @@ __global__ void k_sum_fixed(const double *v, int64_t n, double *out) {
 cudaError_t launch_try_single(const SingleArgs &a, cudaStream_t st) {
     if (a.s.kind == 0) k_try_single<0><<<1, 32, 0, st>>>(a);
     else if (a.s.kind == 1) k_try_single<1><<<1, 32, 0, st>>>(a);
-    else k_try_single<2><<<1, 32, 0, st>>>(a);
+    else if (a.s.kind == 2) k_try_single<2><<<1, 32, 0, st>>>(a);
+    else k_try_single<3><<<1, 32, 0, st>>>(a);
     return cudaGetLastError();
 }
 
@@ -628,7 +676,15 @@ cudaError_t launch_soft_sweep(const SoftSweepArgs &a, int nwarps, cudaStream_t s
     const unsigned blocks = (unsigned)((nwarps + SOFT_WARPS - 1) / SOFT_WARPS);
     if (a.c.s.kind == 0) k_soft_sweep<0><<<blocks, SOFT_WARPS * 32, 0, st>>>(a);
     else if (a.c.s.kind == 1) k_soft_sweep<1><<<blocks, SOFT_WARPS * 32, 0, st>>>(a);
-    else k_soft_sweep<2><<<blocks, SOFT_WARPS * 32, 0, st>>>(a);
+    else if (a.c.s.kind == 2) k_soft_sweep<2><<<blocks, SOFT_WARPS * 32, 0, st>>>(a);
+    else k_soft_sweep<3><<<blocks, SOFT_WARPS * 32, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+// Packing::countTotalOverlaps of generic convex bodies, every pair in FP64.
+cudaError_t launch_count_fp64(const SingleArgs &a, int early, unsigned long long *out, int *flag, cudaStream_t st) {
+    const unsigned nb = (unsigned)((a.s.n + 127) / 128);
+    k_count_fp64<3><<<nb, 128, 0, st>>>(a, early, out, flag);
     return cudaGetLastError();
 }
 

@@ -1151,7 +1151,9 @@ __device__ __forceinline__ void validate_particle(const DevState &s, int64_t i) 
     validate_one(s, i, rr);
 }
 
-__device__ __forceinline__ void assign_one(const DevState &s, const GridDev &g, int64_t i) {
+// Particle i's cell and FP32 cell-local position: relative coordinates box^-1 r in FP64, the
+// cell of each shifted coordinate and the in-cell fraction mapped through the FP32 cell matrix.
+__device__ __forceinline__ int locate_one(const DevState &s, const GridDev &g, int64_t i, float3 &loc) {
     d3 p = load_d3(s.pos64 + 3 * i);
     d3 r = mv3(s.inv, p);
     double rr[3] = {r.x, r.y, r.z};
@@ -1172,8 +1174,13 @@ __device__ __forceinline__ void assign_one(const DevState &s, const GridDev &g, 
         c[d] = cd;
         f[d] = static_cast<float>(un - cd);
     }
-    int cell = c[0] + g.dims[0] * (c[1] + g.dims[1] * c[2]);
-    float3 loc = mat32(g.cellmat, f[0], f[1], f[2]);
+    loc = mat32(g.cellmat, f[0], f[1], f[2]);
+    return c[0] + g.dims[0] * (c[1] + g.dims[1] * c[2]);
+}
+
+__device__ __forceinline__ void assign_one(const DevState &s, const GridDev &g, int64_t i) {
+    float3 loc;
+    const int cell = locate_one(s, g, i, loc);
     g.plocal[i] = make_float4(loc.x, loc.y, loc.z, 0.f);
     g.pid_cell[i] = cell;
     g.rank[i] = atomicAdd(g.count + cell, 1);

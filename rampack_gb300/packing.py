@@ -261,6 +261,13 @@ class GpuPacking:
         self._check(self.lib.rp_get_stats(self.h, C.byref(st)))
         return st.as_dict()
 
+    def grid_counters(self) -> dict:
+        """Full cell-grid rebuilds (Packing::getNeighbourGridRebuilds) and box moves that kept
+        the old cells (remaps) since creation."""
+        rb, rm = C.c_uint64(), C.c_uint64()
+        self._check(self.lib.rp_get_grid_counters(self.h, C.byref(rb), C.byref(rm)))
+        return {"rebuilds": rb.value, "remaps": rm.value}
+
     def stream(self) -> int:
         s = C.c_void_p()
         self._check(self.lib.rp_get_stream(self.h, C.byref(s)))
