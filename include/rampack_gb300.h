@@ -170,6 +170,13 @@ int rp_create_polyspherocylinder(int32_t num_centres, const double *centres, con
  * An invalid script fails with RP_ERR_ARG and the builder's message in rp_last_error(NULL). */
 int rp_create_convex(const char *script, int64_t n, int device, void **handle);
 
+/* XenoCollideTraits::overlapBetween of the handle's convex body on n independent pairs
+ * (positions n x 3, orientations n x 9, the second body at its given position: no periodic
+ * image), decided on the device; out[i] = 1 for an overlap.  For parity checks of the support
+ * functions and the portal refinement. */
+int rp_convex_pair_overlaps(void *handle, int64_t n, const double *pos1, const double *rot1, const double *pos2,
+                            const double *rot2, uint8_t *out);
+
 /* Releases the handle and all of its device memory. */
 int rp_destroy(void *handle);
 

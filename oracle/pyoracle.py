@@ -25,6 +25,8 @@ REF_SO = os.path.join(HERE, "_ref", "librpref.so")
 REFERENCE_DIR = os.environ.get("RAMPACK_REFERENCE_DIR", "/root/reference")
 
 SPHERE, SPHEROCYLINDER, POLYSPHERE = 0, 1, 2
+# generic convex bodies (GenericXenoCollideTraits): `params` is the XCBodyBuilder script
+CONVEX = 4
 
 MOVE_DTYPE = np.dtype([
     ("particle", "<i4"), ("type", "<i4"), ("domain", "<i4"), ("reserved", "<i4"),
@@ -148,13 +150,19 @@ class CpuPacking:
         self.lib, self.pre = _lib("oracle" if which == "oracle" else "reference")
         self.which = which
         self.kind = kind
-        self.params = np.ascontiguousarray(params, dtype=np.float64)
+        self.params = params if kind == CONVEX else np.ascontiguousarray(params, dtype=np.float64)
         pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
         rot = np.ascontiguousarray(rot, dtype=np.float64).reshape(-1, 9)
         box = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
         self.n = pos.shape[0]
-        self.h = self._f("create")(kind, _dp(self.params), len(self.params), self.n, _dp(pos), _dp(rot), _dp(box),
-                                   threads)
+        if kind == CONVEX:
+            f = self._f("create_convex")
+            f.restype, f.argtypes = _P, [C.c_char_p, C.c_int64, _D, _D, _D, C.c_int]
+            self.script = params
+            self.h = f(params.encode(), self.n, _dp(pos), _dp(rot), _dp(box), threads)
+        else:
+            self.h = self._f("create")(kind, _dp(self.params), len(self.params), self.n, _dp(pos), _dp(rot),
+                                       _dp(box), threads)
         if not self.h:
             raise ValueError("packing construction failed")
 
@@ -342,6 +350,26 @@ def pair_overlap(which: str, kind: int, params, p1, r1, p2, r2, c1: int = 0, c2:
                                            c2, bc_kind, None if b is None else _dp(b), None if t is None else _dp(t))
     if r < 0:
         raise ValueError("bad shape")
+    return bool(r)
+
+
+def convex_overlap(which: str, script: str, p1, r1, p2, r2) -> bool:
+    """XenoCollideTraits::overlapBetween of two placed convex bodies (no periodic image)."""
+    lib, pre = _lib("oracle" if which == "oracle" else "reference")
+    a = [np.ascontiguousarray(x, dtype=np.float64).reshape(-1) for x in (p1, r1, p2, r2)]
+    if which == "oracle":
+        f = lib.rpo_convex_overlap
+        f.restype, f.argtypes = C.c_int, [C.c_char_p, _D, _D, _D, _D]
+        r = f(script.encode(), *[_dp(x) for x in a])
+        if r < 0:
+            raise ValueError("invalid convex body script")
+    else:
+        f = lib.ref_convex_overlap
+        f.restype, f.argtypes = C.c_int, [C.c_char_p, _D, _D, _D, _D, C.c_char_p, C.c_int]
+        err = _errbuf()
+        r = f(script.encode(), *[_dp(x) for x in a], err, 512)
+        if r < 0:
+            raise ValueError(err.value.decode())
     return bool(r)
 
 

@@ -44,6 +44,8 @@
 #include "core/shapes/PolyspherocylinderTraits.h"
 #include "core/shapes/SphereTraits.h"
 #include "core/shapes/SpherocylinderTraits.h"
+#include "core/shapes/GenericXenoCollideTraits.h"
+#include "geometry/xenocollide/XCBodyBuilder.h"
 #include "core/volume_scalers/AnisotropicVolumeScaler.h"
 #include "core/volume_scalers/DeltaVolumeScaler.h"
 #include "core/volume_scalers/LinearScalingFactorSampler.h"
@@ -150,6 +152,67 @@ void *ref_create(int kind, const double *prm, int np, int64_t n, const double *p
         return nullptr;
     }
     return h.release();
+}
+
+// GenericXenoCollideTraits from an XCBodyBuilder script (commands one per line or separated by
+// ';', each through XCBodyBuilder::processCommand), as the frontend's generic_convex shape
+// builds it (frontend/matchers/ShapeMatcher.cpp:411-441; volume 1, no axes).
+static std::shared_ptr<ShapeTraits> make_convex_traits(const char *script) {
+    XCBodyBuilder builder;
+    std::string cur;
+    std::string text = std::string(script) + "\n";
+    for (char ch : text) {
+        if (ch == '\n' || ch == ';') {
+            if (cur.find_first_not_of(" \t\r") != std::string::npos) builder.processCommand(cur);
+            cur.clear();
+        } else {
+            cur += ch;
+        }
+    }
+    auto geometry = builder.releaseCollideGeometry();
+    return std::make_shared<GenericXenoCollideTraits>(geometry, std::nullopt, std::nullopt, Vector<3>{0, 0, 0}, 1.0,
+                                                      ShapeGeometry::NamedPoints{});
+}
+
+void *ref_create_convex(const char *script, int64_t n, const double *pos, const double *rot, const double *box9,
+                        int threads) {
+    auto h = std::make_unique<Handle>();
+    try {
+        h->traits = make_convex_traits(script);
+    } catch (const std::exception &) {
+        return nullptr;
+    }
+    h->threads = threads;
+    h->kind = 4;
+    std::vector<Shape> shapes;
+    for (int64_t i = 0; i < n; i++)
+        shapes.emplace_back(Vector<3>{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]}, load_m(rot + 9 * i));
+    try {
+        h->pk = std::make_unique<Packing>(TriclinicBox(load_m(box9)), std::move(shapes),
+                                          std::make_unique<PeriodicBoundaryConditions>(),
+                                          h->traits->getInteraction(), threads, threads);
+    } catch (const std::exception &) {
+        return nullptr;
+    }
+    return h.release();
+}
+
+// The reference's own pair test of two placed bodies (XenoCollideTraits::overlapBetween with
+// free boundary conditions: the second body at pos2 exactly); -1 with the builder's message in
+// err for an invalid script.
+int ref_convex_overlap(const char *script, const double *pos1, const double *rot1, const double *pos2,
+                       const double *rot2, char *err, int errlen) {
+    try {
+        auto traits = make_convex_traits(script);
+        FreeBoundaryConditions fbc;
+        return traits->getInteraction().overlapBetween(Vector<3>{pos1[0], pos1[1], pos1[2]}, load_m(rot1), 0,
+                                                       Vector<3>{pos2[0], pos2[1], pos2[2]}, load_m(rot2), 0, fbc)
+                   ? 1
+                   : 0;
+    } catch (const std::exception &e) {
+        if (err && errlen > 0) std::snprintf(err, static_cast<std::size_t>(errlen), "%s", e.what());
+        return -1;
+    }
 }
 
 void ref_destroy(void *hp) { delete static_cast<Handle *>(hp); }

@@ -96,6 +96,45 @@ void *rpo_create(int kind, const double *prm, int np, int64_t n, const double *p
     return h.release();
 }
 
+// A generic convex body (GenericXenoCollideTraits) from an XCBodyBuilder script: commands one
+// per line or separated by ';'; null for an invalid script.
+void *rpo_create_convex(const char *script, int64_t n, const double *pos, const double *rot, const double *box9,
+                        int threads) {
+    auto h = std::make_unique<Handle>();
+    h->inter.kind = CONVEX;
+    try {
+        h->inter.xc = xc_build_script(script);
+    } catch (const std::exception &) {
+        return nullptr;
+    }
+    std::vector<Shape> shapes(static_cast<std::size_t>(n));
+    for (int64_t i = 0; i < n; i++) {
+        shapes[i].pos = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+        shapes[i].rot = load_m3(rot + 9 * i);
+    }
+    try {
+        h->pk = std::make_unique<Packing>(Box(load_m3(box9)), std::move(shapes), h->inter,
+                                          static_cast<std::size_t>(threads), static_cast<std::size_t>(threads));
+    } catch (const std::exception &) {
+        return nullptr;
+    }
+    return h.release();
+}
+
+// The pair test alone: XenoCollideTraits::overlapBetween of two placed bodies (the second at
+// pos2 exactly, no periodic image); -1 for an invalid script.
+int rpo_convex_overlap(const char *script, const double *pos1, const double *rot1, const double *pos2,
+                       const double *rot2) {
+    XcPtr g;
+    try {
+        g = xc_build_script(script);
+    } catch (const std::exception &) {
+        return -1;
+    }
+    return xc_overlap(*g, {pos1[0], pos1[1], pos1[2]}, load_m3(rot1), {pos2[0], pos2[1], pos2[2]}, load_m3(rot2)) ? 1
+                                                                                                                : 0;
+}
+
 void rpo_destroy(void *hp) { delete static_cast<Handle *>(hp); }
 
 // A soft part joined to the shape's hard interaction (CompoundInteraction with a central

@@ -25,6 +25,7 @@
 #endif
 
 #include "rpo_geometry.hpp"
+#include "rpo_xc.hpp"
 
 namespace rpo {
 
@@ -40,7 +41,7 @@ struct Shape {
     void rotate(const M3 &r) { rot = mm(r, rot); }
 };
 
-enum ShapeKind { SPHERE = 0, SPHEROCYLINDER = 1, POLYSPHERE = 2 };
+enum ShapeKind { SPHERE = 0, SPHEROCYLINDER = 1, POLYSPHERE = 2, CONVEX = 4 };
 
 // The hard interactions of the BASELINE shapes.
 struct Interaction {
@@ -52,6 +53,8 @@ struct Interaction {
     // polyspherocylinders (PolyspherocylinderTraits): each centre is a spherocylinder with
     // this body-frame half axis (SpherocylinderData::halfAxis); empty for polyspheres
     std::vector<V3> half_axes;
+    // generic convex bodies (GenericXenoCollideTraits): the XCBodyBuilder geometry
+    std::shared_ptr<XcGeom> xc;
 
     // Soft part: a CentralInteraction helper installed on the same interaction centres and
     // joined to the hard shape by CompoundInteraction (core/interactions/CompoundInteraction.cpp:9-49):
@@ -102,6 +105,7 @@ struct Interaction {
     double hard_range() const {
         if (kind == SPHERE) return 2 * radius;
         if (kind == SPHEROCYLINDER) return 2 * radius + length;
+        if (kind == CONVEX) return 2 * xc->circ();   // XenoCollideTraits.h:160-172
         if (segments()) {   // PolyspherocylinderTraits.cpp:140-147
             double m = circumsphere(0);
             for (std::size_t i = 1; i < radii.size(); i++)
@@ -152,6 +156,9 @@ struct Interaction {
         if (kind == SPHERE) {
             // SphereTraits.cpp:56-65
             return bc.distance2(p1, p2) < std::pow(2 * radius, 2);
+        } else if (kind == CONVEX) {
+            // XenoCollideTraits.h:118-140
+            return xc_overlap(*xc, p1, o1, add(p2, bc.translation(p1, p2)), o2);
         } else if (kind == SPHEROCYLINDER) {
             // SpherocylinderTraits.cpp:28-46
             V3 p2bc = add(p2, bc.translation(p1, p2));

@@ -22,6 +22,7 @@ ERRORS = {
 SHAPE_SPHERE, SHAPE_SPHEROCYLINDER, SHAPE_POLYSPHERE = 0, 1, 2
 # creation kind of polyspherocylinders (the handle then runs as a multi-centre body)
 SHAPE_POLYSPHEROCYLINDER = 3
+SHAPE_CONVEX = 4      # generic convex body (rp_create_convex): params is the XCBodyBuilder script
 MAX_CENTRES = 8
 MOVE_TRANSLATION, MOVE_ROTATION, MOVE_ROTOTRANSLATION = 0, 1, 2
 CODE_ACCEPTED = 0x80
@@ -108,6 +109,8 @@ SIGNATURES = {
     "rp_create": (C.c_int, [C.POINTER(ShapeDesc), C.c_int64, C.c_int, C.POINTER(C.c_void_p)]),
     "rp_create_polysphere": (C.c_int, [C.c_int32, _D, _D, C.c_int64, C.c_int, C.POINTER(C.c_void_p)]),
     "rp_create_polyspherocylinder": (C.c_int, [C.c_int32, _D, _D, _D, C.c_int64, C.c_int, C.POINTER(C.c_void_p)]),
+    "rp_create_convex": (C.c_int, [C.c_char_p, C.c_int64, C.c_int, C.POINTER(C.c_void_p)]),
+    "rp_convex_pair_overlaps": (C.c_int, [_P, C.c_int64, _D, _D, _D, _D, C.POINTER(C.c_uint8)]),
     "rp_destroy": (C.c_int, [_P]),
     "rp_last_error": (C.c_char_p, [_P]),
     "rp_upload_state": (C.c_int, [_P, _D, _D, _D]),

@@ -65,6 +65,8 @@ int sweep_half_blocks_per_sm(int kind, int cap);
 cudaError_t launch_try_single(const SingleArgs &a, cudaStream_t st);
 cudaError_t launch_soft_sweep(const SoftSweepArgs &a, int nwarps, cudaStream_t st);
 cudaError_t launch_count_fp64(const SingleArgs &a, int early, unsigned long long *out, int *flag, cudaStream_t st);
+cudaError_t launch_convex_pairs(const XcShape *xc, int64_t n, const double *p1, const double *r1, const double *p2,
+                                const double *r2, uint8_t *out, uint32_t *status, cudaStream_t st);
 cudaError_t launch_total_energy(const SingleArgs &a, double *scratch, double *out, cudaStream_t st);
 cudaError_t launch_commit_single(const DevState &s, SingleTry *t, uint8_t *disp_flag, int32_t *disp_list, int slot,
                                  cudaStream_t st);
@@ -1186,6 +1188,35 @@ int rp_create_convex(const char *script, int64_t n, int device, void **handle) {
         return RP_ERR_CUDA;
     }
     return RP_OK;
+}
+
+// The pair test of a convex handle's body on n pairs given in host arrays (parity checks of
+// the device's support functions and portal refinement).
+int rp_convex_pair_overlaps(void *handle, int64_t n, const double *pos1, const double *rot1, const double *pos2,
+                            const double *rot2, uint8_t *out) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || n < 0 || (n > 0 && (!pos1 || !rot1 || !pos2 || !rot2 || !out))) return fail(h, RP_ERR_ARG, "bad argument");
+    if (h->shape.kind != RP_SHAPE_CONVEX) return fail(h, RP_ERR_UNSUPPORTED, "not a convex-body handle");
+    if (n == 0) return RP_OK;
+    RP_CUDA(h, cudaSetDevice(h->device));
+    const size_t nn = static_cast<size_t>(n);
+    double *d = nullptr;
+    uint8_t *o = nullptr;
+    RP_CUDA(h, cudaMalloc(&d, sizeof(double) * 24 * nn));
+    cudaError_t e = cudaMalloc(&o, nn);
+    const size_t off[4] = {0, 3 * nn, 12 * nn, 15 * nn};
+    const double *src[4] = {pos1, rot1, pos2, rot2};
+    const size_t len[4] = {3 * nn, 9 * nn, 3 * nn, 9 * nn};
+    for (int k = 0; k < 4 && e == cudaSuccess; k++)
+        e = cudaMemcpyAsync(d + off[k], src[k], sizeof(double) * len[k], cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess)
+        e = launch_convex_pairs(h->d_xc, n, d + off[0], d + off[1], d + off[2], d + off[3], o, h->status, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, o, nn, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(d);
+    cudaFree(o);
+    if (e != cudaSuccess) return fail(h, RP_ERR_CUDA, cudaGetErrorString(e));
+    return check_status(h);
 }
 
 int rp_destroy(void *handle) {

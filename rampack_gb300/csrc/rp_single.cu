@@ -639,6 +639,18 @@ __global__ void k_count_fp64(SingleArgs A, int early, unsigned long long *out, i
     if (cnt) atomicAdd(out, cnt);
 }
 
+// XenoCollideTraits::overlapBetween of n independent pairs of placed convex bodies (the second
+// body at its given position, no periodic image), one thread each.
+__global__ void k_convex_pairs(const XcShape *xc, int64_t n, const double *p1, const double *r1, const double *p2,
+                               const double *r2, uint8_t *out, uint32_t *status) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    bool stuck = false;
+    const bool ov = xc_overlap(*xc, load_d3(p1 + 3 * i), r1 + 9 * i, load_d3(p2 + 3 * i), r2 + 9 * i, stuck);
+    if (stuck) atomicOr(status, ST_NUMERIC);
+    out[i] = ov ? 1 : 0;
+}
+
 // Sum of n values in one block in a fixed order (deterministic): each thread its stride,
 // then a tree.
 __global__ void k_sum_fixed(const double *v, int64_t n, double *out) {
@@ -678,6 +690,13 @@ cudaError_t launch_soft_sweep(const SoftSweepArgs &a, int nwarps, cudaStream_t s
     else if (a.c.s.kind == 1) k_soft_sweep<1><<<blocks, SOFT_WARPS * 32, 0, st>>>(a);
     else if (a.c.s.kind == 2) k_soft_sweep<2><<<blocks, SOFT_WARPS * 32, 0, st>>>(a);
     else k_soft_sweep<3><<<blocks, SOFT_WARPS * 32, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_convex_pairs(const XcShape *xc, int64_t n, const double *p1, const double *r1, const double *p2,
+                                const double *r2, uint8_t *out, uint32_t *status, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_convex_pairs<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(xc, n, p1, r1, p2, r2, out, status);
     return cudaGetLastError();
 }
 

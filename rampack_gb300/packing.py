@@ -47,7 +47,8 @@ def cell_phase(dims, cell: int) -> int:
 class GpuPacking:
     def __init__(self, kind: int, params, pos, rot, box, device: int = 0):
         self.lib = _lib.load()
-        params = np.asarray(params, dtype=np.float64).reshape(-1)
+        script = params if kind == _lib.SHAPE_CONVEX else None
+        params = np.zeros(0) if script is not None else np.asarray(params, dtype=np.float64).reshape(-1)
         desc = ShapeDesc()
         desc.kind = kind
         pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
@@ -55,7 +56,13 @@ class GpuPacking:
         self.kind = kind
         self.params = params
         h = C.c_void_p()
-        if kind == _lib.SHAPE_POLYSPHERE:
+        if kind == _lib.SHAPE_CONVEX:
+            # a generic convex body: the XCBodyBuilder script
+            self.script = str(script)
+            rc = self.lib.rp_create_convex(self.script.encode(), self.n, device, C.byref(h))
+            if rc != 0:
+                raise EngineError(rc, "rp_create_convex failed: " + self.lib.rp_last_error(None).decode())
+        elif kind == _lib.SHAPE_POLYSPHERE:
             # params as the oracle's: [k, (x, y, z, r) per centre]
             k = int(params[0])
             data = params[1:1 + 4 * k].reshape(k, 4)
@@ -260,6 +267,16 @@ class GpuPacking:
         st = SweepStats()
         self._check(self.lib.rp_get_stats(self.h, C.byref(st)))
         return st.as_dict()
+
+    def convex_pair_overlaps(self, pos1, rot1, pos2, rot2) -> np.ndarray:
+        """XenoCollideTraits::overlapBetween of the handle's convex body on independent pairs
+        (no periodic image), decided on the device."""
+        a = [np.ascontiguousarray(x, dtype=np.float64) for x in (pos1, rot1, pos2, rot2)]
+        n = a[0].reshape(-1, 3).shape[0]
+        out = np.zeros(n, dtype=np.uint8)
+        self._check(self.lib.rp_convex_pair_overlaps(self.h, n, dptr(a[0]), dptr(a[1]), dptr(a[2]), dptr(a[3]),
+                                                     out.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return out.astype(bool)
 
     def grid_counters(self) -> dict:
         """Full cell-grid rebuilds (Packing::getNeighbourGridRebuilds) and box moves that kept

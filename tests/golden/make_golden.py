@@ -443,6 +443,19 @@ def gen_nematic(rng):
     print("nematic:", len(out) // 3, "orientation sets")
 
 
+def gen_convex():
+    """XenoCollideTraits::overlapBetween of the reference's GenericXenoCollideTraits on random
+    pairs around contact for every test body (tests/convex_bodies.py), 400 pairs each."""
+    import convex_bodies as CB
+    out = {}
+    for i, (name, script) in enumerate(sorted(CB.BODIES.items())):
+        p1, r1, p2, r2 = CB.random_pairs(np.random.default_rng(3000 + i), 400)
+        dec = np.array([po.convex_overlap("reference", script, p1[k], r1[k], p2[k], r2[k]) for k in range(len(p1))])
+        out[f"{name}_r1"], out[f"{name}_p2"], out[f"{name}_r2"], out[f"{name}_overlap"] = r1, p2, r2, dec
+    np.savez_compressed(os.path.join(HERE, "convex.npz"), names=np.array(sorted(CB.BODIES)), **out)
+    print("convex:", len(CB.BODIES), "bodies")
+
+
 def main():
     if not po.reference_available():
         po.build(reference=True)
@@ -464,6 +477,9 @@ def main():
     if sys.argv[1:] == ["nematic"]:
         gen_nematic(np.random.default_rng(20261205))
         return
+    if sys.argv[1:] == ["convex"]:
+        gen_convex()
+        return
     rng = np.random.default_rng(20241203)
     gen_pairs(rng)
     gen_geometry(rng)
@@ -482,6 +498,7 @@ def main():
     gen_walls()
     gen_correlation()
     gen_nematic(np.random.default_rng(20261205))
+    gen_convex()
 
 
 if __name__ == "__main__":

@@ -1,0 +1,92 @@
+"""Generic convex bodies (GenericXenoCollideTraits) in the oracle, pinned to the reference.
+
+The oracle restates XCBodyBuilder, the XenoCollide geometries and the portal refinement
+(oracle/rpo_xc.hpp); the reference's own classes are compiled in place (oracle/_ref).  For
+bodies covering every primitive and operation, random pairs around contact (between the
+insphere and circumsphere distances, random orientations) must get identical decisions, and
+packings of them must count overlaps, replay move streams and run the cycle loop identically.
+Skipped where the reference library is not built (the GPU machine); tests/golden/convex.npz
+carries the same pin there.
+"""
+import numpy as np
+import pytest
+
+import pyoracle as po
+
+from convex_bodies import BODIES, lattice, random_pairs
+
+
+@pytest.mark.parametrize("name", sorted(BODIES))
+def test_pair_decisions_match_the_reference(oracle, name):
+    if not po.reference_available():
+        pytest.skip("reference library not built here")
+    script = BODIES[name]
+    p1, r1, p2, r2 = random_pairs(np.random.default_rng(11), 7500)
+    hits = 0
+    for k in range(len(p1)):
+        a = po.convex_overlap("oracle", script, p1[k], r1[k], p2[k], r2[k])
+        b = po.convex_overlap("reference", script, p1[k], r1[k], p2[k], r2[k])
+        assert a == b, (name, k, p2[k], r1[k], r2[k])
+        hits += a
+    assert 0 < hits < len(p1), (name, hits)
+
+
+def test_invalid_scripts_fail_in_both(oracle):
+    if not po.reference_available():
+        pytest.skip("reference library not built here")
+    for bad in ("sphere -1", "cuboid 1 2", "sum", "sphere 1; sphere 1", "blob 1", ""):
+        with pytest.raises(ValueError):
+            po.convex_overlap("oracle", bad, np.zeros(3), np.eye(3), np.ones(3), np.eye(3))
+        with pytest.raises(ValueError):
+            po.convex_overlap("reference", bad, np.zeros(3), np.eye(3), np.ones(3), np.eye(3))
+
+
+# lattice spacings just above twice the circumsphere radius: no overlaps at the start (the cycle
+# loop requires none), contacts after a few moves
+PACKINGS = {"cuboid": 3.76, "cone": 2.02, "capsule_wrap": 2.22, "rotated_sum": 2.76}
+
+
+@pytest.mark.parametrize("name", sorted(PACKINGS))
+def test_packings_match_the_reference(oracle, name):
+    """Counts, a replayed serial move stream and an NpT cycle-loop run: identical codes, counts
+    and final states."""
+    if not po.reference_available():
+        pytest.skip("reference library not built here")
+    script = BODIES[name]
+    pos, rot, box = lattice(6, PACKINGS[name])
+    out = {}
+    for which in ("oracle", "reference"):
+        pk = po.CpuPacking(which, po.CONVEX, script, pos, rot, box, threads=1)
+        c0 = pk.count_overlaps(False)
+        rng = po.CpuPacking("oracle", po.CONVEX, script, pos, rot, box, threads=1)
+        g = rng.rng(3)
+        moves = rng.draw_moves(g, 0.3, 0.3, np.arange(rng.n), rng.n, 2 * rng.n, domain=-1)
+        rng.rng_free(g)
+        rng.close()
+        codes, _ = pk.replay(moves, None)
+        c1 = pk.count_overlaps(False)
+        st = po.run_cycles(pk, 20, translation_step=0.2, rotation_step=0.2, box_kind=1, box_step=0.01,
+                           pressure=2.0, temperature=1.0, seed=9)
+        p, r, b = pk.state()
+        out[which] = (c0, codes, c1, (st.moves[0], st.accepted[0], st.moves[1], st.accepted[1], st.scalings,
+                                      st.scalings_accepted), p, r, b)
+        pk.close()
+    a, b = out["oracle"], out["reference"]
+    assert a[0] == b[0] and a[2] == b[2]
+    assert np.array_equal(a[1], b[1])
+    assert 0 < np.count_nonzero(a[1] & 0x80) < len(a[1])
+    assert a[3] == b[3]
+    for x, y in zip(a[4:], b[4:]):
+        assert np.array_equal(x, y)
+
+
+def test_oracle_matches_the_golden_fixture(oracle):
+    """The restatement against the reference's decisions recorded in tests/golden/convex.npz
+    (runs where the reference is absent too)."""
+    import os
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "convex.npz"))
+    for name in z["names"]:
+        script = BODIES[str(name)]
+        r1, p2, r2, want = z[f"{name}_r1"], z[f"{name}_p2"], z[f"{name}_r2"], z[f"{name}_overlap"]
+        got = [po.convex_overlap("oracle", script, np.zeros(3), r1[k], p2[k], r2[k]) for k in range(len(p2))]
+        assert np.array_equal(np.array(got), want), name
