@@ -75,20 +75,22 @@ def test_counts_and_logged_sweeps_replay_on_the_oracle(oracle, engine, name):
 def test_overlap_counting(oracle, engine, name):
     """A compressed lattice holding overlaps: cached counts, logged counting sweeps and a
     counting box move equal the oracle's."""
-    cpu, g = packing(name, factor=0.8)
+    cpu, g = packing(name, factor=0.75)
     cpu.set_counting(True)
     with g:
         g.set_counting(True)
         assert g.cached_overlaps() == cpu.cached_overlaps() > 0
         assert g.count_total_overlaps(False) == cpu.count_overlaps(False)
-        for cycle in range(2):
+        relieved = 0
+        for cycle in range(3):
             g.sweep(0.3, 0.3, seed=5, counter=cycle, log=True)
             moves, codes = g.sweep_log()
             _, _, bounds = g.grid()
             want, _ = cpu.replay(moves, bounds)
             assert np.array_equal(codes, want)
-            assert np.any((codes & 3) == 3)
+            relieved += np.count_nonzero((codes & 3) == 3)
             assert g.cached_overlaps() == cpu.cached_overlaps()
+        assert relieved > 0  # some moves reduced the overlap count (dE = -inf)
         assert same_state(g, cpu)
         _, _, b = g.state()
         nb = np.asarray(b).reshape(9) * 1.02
