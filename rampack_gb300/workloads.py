@@ -217,3 +217,18 @@ def bent_rods(counts, spacing=(2.0, 0.62, 0.95)):
     box = diag_box(counts[0] * spacing[0], counts[1] * spacing[1], counts[2] * spacing[2])
     return POLYSPHEROCYLINDER, polyspherocylinder_params(BENT_ROD), pos, aligned_rotations(len(pos)), box
 
+
+
+# A generic convex body (GenericXenoCollideTraits): a 1 x 1 x 2 cuboid rounded by a sphere of
+# radius 0.1 (the Minkowski sum), as an XCBodyBuilder script.
+CONVEX = 4
+ROUNDED_BOX = "cuboid 1 1 2; sphere 0.1; sum"
+
+
+def config_convex_32768(spacing=(1.5, 1.5, 2.5)):
+    """32^3 rounded boxes, aligned, on an orthorhombic lattice (contact-free: the bodies span
+    1.2 x 1.2 x 2.2), packing fraction about 0.55."""
+    counts = (32, 32, 32)
+    pos = lattice(counts, spacing)
+    box = diag_box(counts[0] * spacing[0], counts[1] * spacing[1], counts[2] * spacing[2])
+    return CONVEX, ROUNDED_BOX, pos, aligned_rotations(len(pos)), box
