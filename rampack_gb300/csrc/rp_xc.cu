@@ -328,6 +328,9 @@ bool xc_build(const std::string &script, XcShape &out, std::string &error) {
     if (b.depth(out.root) > XC_MAX_DEPTH - 1)
         return b.fail("the body nests more than " + std::to_string(XC_MAX_DEPTH - 1) + " geometries");
     const XcNode &r = out.node[out.root];
+    out.flat = 1;
+    if (r.type >= XC_SUM)
+        for (int i = 0; i < r.nent; i++) out.flat = out.flat && out.node[r.ent[i]].type < XC_SUM;
     out.circ = r.circ;
     out.insph = r.insph;
     for (int k = 0; k < 3; k++) out.centre[k] = r.centre[k];

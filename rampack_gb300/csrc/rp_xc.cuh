@@ -49,6 +49,7 @@ struct XcShape {
     XcNode node[XC_MAX_NODES];
     int32_t nnodes;
     int32_t root;
+    int32_t flat;        // the root is a primitive, or an operation whose entries are all primitives
     double circ, insph;  // the root's radii
     double centre[3];    // the root's centre
 };
@@ -146,6 +147,32 @@ RP_HD d3 xc_primitive_support(const XcNode &g, d3 n) {
     }
 }
 
+// The support point of a flat body (a primitive, or one operation over primitives) without a
+// stack: the same arithmetic as xc_support, entry by entry in registers.
+RP_HD d3 xc_support_flat(const XcShape &s, d3 n) {
+    const XcNode &g = s.node[s.root];
+    if (g.type < XC_SUM) return xc_primitive_support(g, n);
+    d3 acc{0.0, 0.0, 0.0};
+    double best = 0.0;
+    for (int i = 0; i < g.nent; i++) {
+        const d3 dir = (g.type == XC_DIFF && i == 1) ? neg3(n) : n;
+        const d3 r = xc_primitive_support(s.node[g.ent[i]], mtv3(g.erot[i], dir));
+        const d3 w = add3(mv3(g.erot[i], r), ld3(g.epos[i]));
+        if (g.type == XC_SUM) {
+            acc = add3(acc, w);
+        } else if (g.type == XC_MAX) {
+            const double proj = dot3(w, n);
+            if (i == 0 || proj > best) {
+                acc = w;
+                best = proj;
+            }
+        } else {
+            acc = i == 0 ? w : sub3(acc, w);
+        }
+    }
+    return acc;
+}
+
 // AbstractXCGeometry::getSupportPoint of node `root`: sums (XCOperations.cpp:38-43), differences
 // (:82-86) and convex hulls (:102-118) evaluated depth first with an explicit stack.  Returns
 // false if the nesting is deeper than the stack (the builder refuses such bodies).
@@ -203,7 +230,8 @@ RP_HD bool xc_support(const XcShape &s, int root, d3 n, d3 &out) {
 // XenoCollide.h:55-61: the support point of a placed body.
 RP_HD bool xc_transform_support(const XcShape &s, const double *rot, d3 pos, d3 n, d3 &out) {
     d3 local;
-    if (!xc_support(s, s.root, mtv3(rot, n), local)) return false;
+    if (s.flat) local = xc_support_flat(s, mtv3(rot, n));
+    else if (!xc_support(s, s.root, mtv3(rot, n), local)) return false;
     out = add3(mv3(rot, local), pos);
     return true;
 }
