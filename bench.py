@@ -99,9 +99,9 @@ def _sc_64000(args):
     return W.config_sc_64000()
 
 
-def _convex_32768(args):
+def _convex_262144(args):
     from rampack_gb300 import workloads as W
-    return W.config_convex_32768()
+    return W.config_convex(64)
 
 
 # name -> (builder, description, metric)
@@ -120,10 +120,11 @@ WORKLOADS = {
                       "at x=-+0.35: a 60 degree kink), N={n:,} (25x40x100), aligned orthorhombic start at phi~0.33, "
                       "triclinic box; per cycle 2N moves (translation 0.2, rotation 0.2) + 1 isotension box move "
                       "(delta 0.005, p*=1.5, T=1)", "moves/sec, bent spherocylinder rods N=1e5"),
-    "convex-32768": (_convex_32768, "generic convex bodies (XCBodyBuilder 'cuboid 1 1 2; sphere 0.1; sum': "
-                     "rounded 1x1x2 boxes, XenoCollide pair tests, every move in FP64), N={n:,} (32^3), aligned "
-                     "orthorhombic start at phi~0.55, triclinic box; per cycle 2N moves (translation 0.2, rotation "
-                     "0.2) + 1 isotension box move (delta 0.005, p*=1.5, T=1)", "moves/sec, convex bodies N=32768"),
+    "convex-262144": (_convex_262144, "generic convex bodies (XCBodyBuilder 'cuboid 1 1 2; sphere 0.1; sum': "
+                      "rounded 1x1x2 boxes, XenoCollide pair tests: FP32 portal refinement with FP64 certificates, "
+                      "exact FP64 refinement otherwise), N={n:,} (64^3), aligned orthorhombic start at phi~0.55, "
+                      "triclinic box; per cycle 2N moves (translation 0.2, rotation 0.2) + 1 isotension box move "
+                      "(delta 0.005, p*=1.5, T=1)", "moves/sec, convex bodies N=262144"),
     "sc-64000": (_sc_64000, "hard spherocylinders l=5 r=0.5, N={n:,} (40^3), aligned orthorhombic start at "
                  "phi=0.35 (cell aspect 1:1:6), triclinic box; per cycle 2N moves (translation 0.2, rotation "
                  "0.2) + 1 isotension box move (delta 0.005, p*=1.5, T=1)", "moves/sec, spherocylinders N=64000"),

@@ -1143,7 +1143,8 @@ int rp_create_polyspherocylinder(int32_t num_centres, const double *centres, con
 // device; the range is twice its circumsphere radius (XenoCollideTraits::getRangeRadius,
 // core/shapes/XenoCollideTraits.h:160-172).
 int rp_create_convex(const char *script, int64_t n, int device, void **handle) {
-    if (!script || !handle || n <= 0 || n > (1ll << 31) - 1) return RP_ERR_ARG;
+    // (the move kernels queue near pairs as particle * 28 + image in an int)
+    if (!script || !handle || n <= 0 || n > ((1ll << 31) - 1) / 28) return RP_ERR_ARG;
     XcShape *xs = new (std::nothrow) XcShape();
     if (!xs) return RP_ERR_ARG;
     std::string err;

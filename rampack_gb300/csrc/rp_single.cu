@@ -30,6 +30,7 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int SOFT_WARPS = 4;   // warps per block of the soft sweep
+constexpr int XC_QUEUE = 256;   // convex bodies: near (candidate, image) pairs queued per warp
 
 // One mover in shared memory: [0] the tried state, [1] the current one.
 struct Mover {
@@ -41,6 +42,7 @@ struct Mover {
     int ncells[2];
     int cstart[2][28];                  // prefix of those cells' occupancies
     int outside;                        // the tried position lies outside the ActiveDomain
+    mutable int xq[XC_QUEUE];           // convex bodies: candidate * 28 + image of the near pairs
 };
 
 // Grid cell of an FP64 position: the rebuild's own arithmetic (assign_one).
@@ -104,7 +106,7 @@ __device__ bool body_overlap(const DevState &s, d3 p, d3 a, const double *rot, i
     if constexpr (KIND == 3) {
         const d3 q = add3(pj, t ? *t : pbc_translation(s.box, s.inv, p, pj));
         bool stuck = false;
-        const bool ov = xc_overlap(*s.xc, p, rot, q, rj, stuck);
+        const bool ov = xc_overlap_filtered(*s.xc, p, rot, q, rj, stuck);
         if (stuck) atomicOr(s.status, ST_NUMERIC);
         return ov;
     } else {
@@ -135,13 +137,17 @@ __device__ bool centre_overlap(const DevState &s, d3 pa, d3 ha, int a, int j, in
     return pbc_distance2(s.box, s.inv, pa, pb) < in2;
 }
 
-// FP32 separation q - p (FP64 points) at image m, against the pre-filter reach.
-__device__ __forceinline__ bool within_reach(const SingleArgs &A, const double *q, const double *p, int mx, int my,
-                                             int mz) {
+// FP32 separation q - p of two FP64 points (one FP64 subtraction per coordinate, shared by
+// the images tested next).
+__device__ __forceinline__ float3 separation32(const double *q, const double *p) {
+    return make_float3(static_cast<float>(q[0] - p[0]), static_cast<float>(q[1] - p[1]),
+                       static_cast<float>(q[2] - p[2]));
+}
+
+// The FP32 separation at image m against the pre-filter reach.
+__device__ __forceinline__ bool within_reach(const SingleArgs &A, float3 sep, int mx, int my, int mz) {
     const float3 t32 = mat32(A.box32, (float)mx, (float)my, (float)mz);
-    const float ex = static_cast<float>(q[0] - p[0]) + t32.x;
-    const float ey = static_cast<float>(q[1] - p[1]) + t32.y;
-    const float ez = static_cast<float>(q[2] - p[2]) + t32.z;
+    const float ex = sep.x + t32.x, ey = sep.y + t32.y, ez = sep.z + t32.z;
     return ex * ex + ey * ey + ez * ez <= A.reach2;
 }
 
@@ -161,11 +167,11 @@ __device__ int candidate_overlaps(const SingleArgs &A, const double *p, d3 a, co
     if constexpr (KIND != 2) {
         const d3 pp{p[0], p[1], p[2]};
         if (s.pbc_fold) return body_overlap<KIND>(s, pp, a, rot, j, nullptr) ? 1 : 0;
-        const double *pj = s.pos64 + 3 * (size_t)j;
+        const float3 sep = separation32(s.pos64 + 3 * (size_t)j, p);
         for (int mx = -1; mx <= 1; mx++)
             for (int my = -1; my <= 1; my++)
                 for (int mz = -1; mz <= 1; mz++) {
-                    if (!within_reach(A, pj, p, mx, my, mz)) continue;
+                    if (!within_reach(A, sep, mx, my, mz)) continue;
                     const d3 t = image_translation(s, mx, my, mz);
                     if (body_overlap<KIND>(s, pp, a, rot, j, &t)) {
                         if (early) return 1;
@@ -185,11 +191,11 @@ __device__ int candidate_overlaps(const SingleArgs &A, const double *p, d3 a, co
                     }
                     continue;
                 }
-                const double *pb = s.abs64 + 3 * ((size_t)j * s.ncen + b);
+                const float3 sep = separation32(s.abs64 + 3 * ((size_t)j * s.ncen + b), abs + 3 * ca);
                 for (int mx = -1; mx <= 1; mx++)
                     for (int my = -1; my <= 1; my++)
                         for (int mz = -1; mz <= 1; mz++) {
-                            if (!within_reach(A, pb, abs + 3 * ca, mx, my, mz)) continue;
+                            if (!within_reach(A, sep, mx, my, mz)) continue;
                             const d3 t = image_translation(s, mx, my, mz);
                             if (centre_overlap(s, pa, ha, ca, j, b, &t)) {
                                 if (early) return 1;
@@ -220,10 +226,11 @@ __device__ double candidate_energy(const SingleArgs &A, const double *p, const d
                 e = dadd(e, soft_energy(s, pbc_distance2(s.box, s.inv, pa3, pb3)));
                 continue;
             }
+            const float3 sep = separation32(pb, pa);
             for (int mx = -1; mx <= 1; mx++)
                 for (int my = -1; my <= 1; my++)
                     for (int mz = -1; mz <= 1; mz++) {
-                        if (!within_reach(A, pb, pa, mx, my, mz)) continue;
+                        if (!within_reach(A, sep, mx, my, mz)) continue;
                         const d3 t = image_translation(s, mx, my, mz);
                         e = dadd(e, soft_energy(s, norm2(sub3(add3(pb3, t), pa3))));
                     }
@@ -245,10 +252,105 @@ __device__ __forceinline__ int candidate_at(const SingleArgs &A, const Mover &mv
     return A.disp_list[k - in_cells];
 }
 
+// Generic convex bodies: the radii tests of XenoCollideTraits::overlapBetween
+// (core/shapes/XenoCollideTraits.h:124-131) decide most (candidate, image) pairs at once; the
+// pairs between insphere and circumsphere distance are queued and their refinements run packed
+// 32 to a warp pass, so the lanes of a pass all refine (instead of a few lanes per candidate
+// round).  Same pairs and decisions as the per-candidate loop; the count, or 0 / 1 with `early`.
+__device__ int warp_overlaps_convex(const SingleArgs &A, const Mover &mv, int which, bool early, int pid) {
+    const DevState &s = A.s;
+    const int lane = threadIdx.x & 31;
+    const int in_cells = mv.cstart[which][mv.ncells[which]];
+    const int total = in_cells + A.ndisp;
+    const double *rot = mv.rot[which];
+    const d3 p{mv.pos[which][0], mv.pos[which][1], mv.pos[which][2]};
+    const double rc = dadd(s.xc->circ, s.xc->circ), ri = dadd(s.xc->insph, s.xc->insph);
+    const double rc2 = dmul(rc, rc), ri2 = dmul(ri, ri);
+    int cnt = 0, nq = 0;
+    // refine the queued pairs, 32 to a pass; true on an overlap with `early`
+    auto drain = [&]() -> bool {
+        for (int b = 0; b < nq; b += 32) {
+            int c = 0;
+            if (b + lane < nq) {
+                const int e = mv.xq[b + lane];
+                const int j = e / 28, m = e % 28;
+                const d3 pj = load_d3(s.pos64 + 3 * (size_t)j);
+                const d3 t = m == 27 ? pbc_translation(s.box, s.inv, p, pj)
+                                     : image_translation(s, m / 9 - 1, (m / 3) % 3 - 1, m % 3 - 1);
+                bool stuck = false;
+                const int f = xc_filter(*s.xc, p, rot, add3(pj, t), s.rot64 + 9 * (size_t)j);
+                c = f >= 0 ? f : (xc_intersect(*s.xc, rot, p, s.rot64 + 9 * (size_t)j, add3(pj, t), 1.0e-12, stuck) ? 1 : 0);
+                if (stuck) atomicOr(s.status, ST_NUMERIC);
+            }
+            if (early && __any_sync(FULL, c != 0)) return true;
+            cnt += c;
+        }
+        __syncwarp();  // every lane has read its entries before the queue is refilled
+        nq = 0;
+        return false;
+    };
+    for (int base = 0; base < total; base += 32) {
+        const int k = base + lane;
+        int certain = 0;
+        int near_e[4];
+        int nnear = 0;
+        if (k < total) {
+            const int j = candidate_at(A, mv, which, k, in_cells);
+            if (j >= 0 && j != pid) {
+                const double *pjp = s.pos64 + 3 * (size_t)j;
+                const d3 pj = load_d3(pjp);
+                if (s.pbc_fold) {
+                    const d3 q = add3(pj, pbc_translation(s.box, s.inv, p, pj));
+                    const double d2 = norm2(sub3(q, p));
+                    if (d2 < ri2) certain++;
+                    else if (!(d2 > rc2)) near_e[nnear++] = j * 28 + 27;
+                } else {
+                    const float3 sep = separation32(pjp, mv.pos[which]);
+                    for (int m = 0; m < 27; m++) {
+                        const int mx = m / 9 - 1, my = (m / 3) % 3 - 1, mz = m % 3 - 1;
+                        if (!within_reach(A, sep, mx, my, mz)) continue;
+                        const double d2 = norm2(sub3(add3(pj, image_translation(s, mx, my, mz)), p));
+                        if (d2 > rc2) continue;
+                        if (d2 < ri2) {
+                            certain++;
+                        } else if (nnear < 4) {
+                            near_e[nnear++] = j * 28 + m;
+                        } else {
+                            bool stuck = false;  // a fifth near image of one candidate: decided here
+                            const d3 t = image_translation(s, mx, my, mz);
+                            const int f = xc_filter(*s.xc, p, rot, add3(pj, t), s.rot64 + 9 * (size_t)j);
+                            certain += f >= 0 ? f
+                                              : (xc_intersect(*s.xc, rot, p, s.rot64 + 9 * (size_t)j, add3(pj, t),
+                                                              1.0e-12, stuck) ? 1 : 0);
+                            if (stuck) atomicOr(s.status, ST_NUMERIC);
+                        }
+                    }
+                }
+            }
+        }
+        if (early && __any_sync(FULL, certain != 0)) return 1;
+        cnt += certain;
+        // queue this round's near pairs (at most 4 per lane)
+        if (nq + 4 * 32 > XC_QUEUE && drain()) return 1;
+        for (int r = 0; r < 4; r++) {
+            const bool has = r < nnear;
+            const unsigned bal = __ballot_sync(FULL, has);
+            if (!bal) break;
+            if (has) mv.xq[nq + __popc(bal & ((1u << lane) - 1))] = near_e[r];
+            nq += __popc(bal);
+        }
+        __syncwarp();
+    }
+    if (drain()) return 1;
+    for (int d = 16; d > 0; d >>= 1) cnt += __shfl_xor_sync(FULL, cnt, d);
+    return early ? (cnt > 0 ? 1 : 0) : cnt;
+}
+
 // Overlaps of mover state `which` with every candidate, then the walls (the count, or 0 / 1
 // with `early`: Packing::countParticleOverlaps, core/Packing.cpp:373-429); the whole warp.
 template <int KIND>
 __device__ int warp_overlaps(const SingleArgs &A, const Mover &mv, int which, bool early, int pid) {
+    if constexpr (KIND == 3) return warp_overlaps_convex(A, mv, which, early, pid);
     const DevState &s = A.s;
     const int lane = threadIdx.x & 31;
     const int in_cells = mv.cstart[which][mv.ncells[which]];
@@ -646,7 +748,7 @@ __global__ void k_convex_pairs(const XcShape *xc, int64_t n, const double *p1, c
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     bool stuck = false;
-    const bool ov = xc_overlap(*xc, load_d3(p1 + 3 * i), r1 + 9 * i, load_d3(p2 + 3 * i), r2 + 9 * i, stuck);
+    const bool ov = xc_overlap_filtered(*xc, load_d3(p1 + 3 * i), r1 + 9 * i, load_d3(p2 + 3 * i), r2 + 9 * i, stuck);
     if (stuck) atomicOr(status, ST_NUMERIC);
     out[i] = ov ? 1 : 0;
 }

@@ -327,7 +327,21 @@ bool xc_build(const std::string &script, XcShape &out, std::string &error) {
     out.root = b.stack.back().node;
     if (b.depth(out.root) > XC_MAX_DEPTH - 1)
         return b.fail("the body nests more than " + std::to_string(XC_MAX_DEPTH - 1) + " geometries");
+    // the FP32 copy of every node for the device's filter
+    for (int i = 0; i < out.nnodes; i++) {
+        const XcNode &g = out.node[i];
+        XcNodeF &f = out.fnode[i];
+        f.type = g.type;
+        f.nent = g.nent;
+        for (int e = 0; e < XC_MAX_ENTRIES; e++) {
+            f.ent[e] = g.ent[e];
+            for (int k = 0; k < 3; k++) f.epos[e][k] = static_cast<float>(g.epos[e][k]);
+            for (int k = 0; k < 9; k++) f.erot[e][k] = static_cast<float>(g.erot[e][k]);
+        }
+        for (int k = 0; k < 3; k++) f.p[k] = static_cast<float>(g.p[k]);
+    }
     const XcNode &r = out.node[out.root];
+    for (int k = 0; k < 3; k++) out.fcentre[k] = static_cast<float>(r.centre[k]);
     out.flat = 1;
     if (r.type >= XC_SUM)
         for (int i = 0; i < r.nent; i++) out.flat = out.flat && out.node[r.ent[i]].type < XC_SUM;

@@ -19,6 +19,15 @@
 
 #include "rp_geom.cuh"
 
+// The support functions and the refinement loops are called from many places of the move
+// kernels; kept out of line on the device so that the kernels' code stays small enough for the
+// instruction cache (inlined, they made instruction fetch the dominant stall).
+#ifdef __CUDACC__
+#define RP_XC_FN static __host__ __device__ __noinline__
+#else
+#define RP_XC_FN static inline
+#endif
+
 namespace rp {
 
 enum XcType : int32_t {
@@ -45,8 +54,20 @@ struct XcNode {
     double centre[3];    // AbstractXCGeometry::getCenter
 };
 
+// FP32 copy of a node for the device's filter (xc_overlap_filtered).
+struct XcNodeF {
+    int32_t type;
+    int32_t nent;
+    int32_t ent[XC_MAX_ENTRIES];
+    float epos[XC_MAX_ENTRIES][3];
+    float erot[XC_MAX_ENTRIES][9];
+    float p[3];
+};
+
 struct XcShape {
     XcNode node[XC_MAX_NODES];
+    XcNodeF fnode[XC_MAX_NODES];
+    float fcentre[3];
     int32_t nnodes;
     int32_t root;
     int32_t flat;        // the root is a primitive, or an operation whose entries are all primitives
@@ -86,7 +107,7 @@ RP_HD d3 ld3(const double *p) { return {p[0], p[1], p[2]}; }
 
 // Support point of a primitive in its own frame (geometry/xenocollide/XCPrimitives.cpp:36-163,
 // XCPrimitives.h:44, :145).
-RP_HD d3 xc_primitive_support(const XcNode &g, d3 n) {
+RP_XC_FN d3 xc_primitive_support(const XcNode &g, d3 n) {
     switch (g.type) {
         case XC_POINT:
             return ld3(g.p);
@@ -149,7 +170,7 @@ RP_HD d3 xc_primitive_support(const XcNode &g, d3 n) {
 
 // The support point of a flat body (a primitive, or one operation over primitives) without a
 // stack: the same arithmetic as xc_support, entry by entry in registers.
-RP_HD d3 xc_support_flat(const XcShape &s, d3 n) {
+RP_XC_FN d3 xc_support_flat(const XcShape &s, d3 n) {
     const XcNode &g = s.node[s.root];
     if (g.type < XC_SUM) return xc_primitive_support(g, n);
     d3 acc{0.0, 0.0, 0.0};
@@ -176,7 +197,7 @@ RP_HD d3 xc_support_flat(const XcShape &s, d3 n) {
 // AbstractXCGeometry::getSupportPoint of node `root`: sums (XCOperations.cpp:38-43), differences
 // (:82-86) and convex hulls (:102-118) evaluated depth first with an explicit stack.  Returns
 // false if the nesting is deeper than the stack (the builder refuses such bodies).
-RP_HD bool xc_support(const XcShape &s, int root, d3 n, d3 &out) {
+RP_XC_FN bool xc_support(const XcShape &s, int root, d3 n, d3 &out) {
     struct Frame {
         int node, i;
         d3 n, acc;
@@ -228,7 +249,7 @@ RP_HD bool xc_support(const XcShape &s, int root, d3 n, d3 &out) {
 }
 
 // XenoCollide.h:55-61: the support point of a placed body.
-RP_HD bool xc_transform_support(const XcShape &s, const double *rot, d3 pos, d3 n, d3 &out) {
+RP_XC_FN bool xc_transform_support(const XcShape &s, const double *rot, d3 pos, d3 n, d3 &out) {
     d3 local;
     if (s.flat) local = xc_support_flat(s, mtv3(rot, n));
     else if (!xc_support(s, s.root, mtv3(rot, n), local)) return false;
@@ -248,7 +269,7 @@ RP_HD bool xc_diff_support(const XcShape &s, const double *rot1, d3 pos1, const 
 // XenoCollide::Intersect (XenoCollide.h:67-169) for two copies of the body; `stuck` is set when
 // the portal iterations exceed XC_MPR_LIMIT or the geometry is too deep (the pair is then
 // reported as overlapping).
-RP_HD bool xc_intersect(const XcShape &s, const double *rot1, d3 pos1, const double *rot2, d3 pos2, double tol,
+RP_XC_FN bool xc_intersect(const XcShape &s, const double *rot1, d3 pos1, const double *rot2, d3 pos2, double tol,
                         bool &stuck) {
     const d3 c = ld3(s.centre);
     const d3 v0 = sub3(add3(mv3(rot2, c), pos2), add3(mv3(rot1, c), pos1));
@@ -311,6 +332,284 @@ RP_HD bool xc_overlap(const XcShape &s, d3 pos1, const double *rot1, d3 pos2bc, 
     const double d2 = norm2(sub3(pos2bc, pos1));
     if (d2 > dmul(rc, rc)) return false;
     if (d2 < dmul(ri, ri)) return true;
+    return xc_intersect(s, rot1, pos1, rot2, pos2bc, 1.0e-12, stuck);
+}
+
+// ---- FP32 portal refinement with FP64 certificates (device) -----------------------------------
+//
+// The exact test above is the reference's decision, but each portal iteration is hundreds of FP64
+// instructions.  The filter runs the same portal refinement in FP32 and turns its outcome into a
+// certificate checked in FP64 on the real bodies:
+//  * a miss ends with a direction n along which the Minkowski difference's support point has a
+//    non-positive projection (or the portal's tolerance exit): if the FP64 support point along n
+//    projects below -margin, the bodies are separated by at least margin along n;
+//  * a hit ends with a tetrahedron (the centre difference v0 and three support points, each kept
+//    with the direction that produced it) containing the origin: the three support points
+//    recomputed in FP64 span, with v0, a tetrahedron inside the Minkowski difference (a convex
+//    set); if the origin lies inside it farther than margin from every face, the bodies overlap
+//    by at least margin.
+// A body separated or overlapping by margin = 1e-7 (|p2 - p1| + 2 circumsphere radius) + 1e-9 is
+// decided the same way by the reference's FP64 refinement (whose rounding is near 1e-15 relative,
+// whose tolerance is 1e-12 and whose colinearity shortcut acts below 1e-12), so a certified answer
+// is the reference's; everything else — near-touching pairs, degenerate portals, the refinement's
+// special cases — runs the exact test.
+
+struct f3v {
+    float x, y, z;
+};
+RP_HD f3v fadd(f3v a, f3v b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+RP_HD f3v fsub(f3v a, f3v b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+RP_HD f3v fneg(f3v a) { return {-a.x, -a.y, -a.z}; }
+RP_HD f3v fscale(f3v a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+RP_HD float fdot(f3v a, f3v b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+RP_HD f3v fcross(f3v a, f3v b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+RP_HD f3v fnormalized(f3v a) { return fscale(a, 1.0f / sqrtf(fdot(a, a))); }
+RP_HD f3v fmv(const float *m, f3v v) {
+    return {m[0] * v.x + m[1] * v.y + m[2] * v.z, m[3] * v.x + m[4] * v.y + m[5] * v.z,
+            m[6] * v.x + m[7] * v.y + m[8] * v.z};
+}
+RP_HD f3v fmtv(const float *m, f3v v) {
+    return {m[0] * v.x + m[3] * v.y + m[6] * v.z, m[1] * v.x + m[4] * v.y + m[7] * v.z,
+            m[2] * v.x + m[5] * v.y + m[8] * v.z};
+}
+RP_HD bool fzero(f3v v) {
+    const float z = 1e-20f;
+    return fabsf(v.x) < z && fabsf(v.y) < z && fabsf(v.z) < z;
+}
+
+RP_XC_FN f3v xcf_primitive(const XcNodeF &g, f3v n) {
+    const f3v p{g.p[0], g.p[1], g.p[2]};
+    switch (g.type) {
+        case XC_POINT: return p;
+        case XC_SEGMENT: return {0.f, 0.f, n.z < 0 ? -p.x : p.x};
+        case XC_RECTANGLE: return {n.x < 0 ? -p.x : p.x, n.y < 0 ? -p.y : p.y, 0.f};
+        case XC_CUBOID: return {n.x < 0 ? -p.x : p.x, n.y < 0 ? -p.y : p.y, n.z < 0 ? -p.z : p.z};
+        case XC_DISK: {
+            const f3v n2{n.x, n.y, 0.f};
+            if (fzero(n2)) return {0.f, 0.f, 0.f};
+            return fscale(fnormalized(n2), p.x);
+        }
+        case XC_SPHERE: return fscale(fnormalized(n), p.x);
+        case XC_ELLIPSE: {
+            const f3v n2{p.x * n.x, p.y * n.y, 0.f};
+            if (fzero(n2)) return {0.f, 0.f, 0.f};
+            const f3v u = fnormalized(n2);
+            return {u.x * p.x, u.y * p.y, 0.f};
+        }
+        case XC_ELLIPSOID: {
+            const f3v u = fnormalized(f3v{n.x * p.x, n.y * p.y, n.z * p.z});
+            return {u.x * p.x, u.y * p.y, u.z * p.z};
+        }
+        case XC_FOOTBALL: {
+            const float r1 = p.y, h = p.x, r2 = 0.5f * (h * h / r1 + r1);
+            const f3v n3 = fnormalized(n);
+            if (n3.z * r2 < -h) return {0.f, 0.f, -h};
+            if (n3.z * r2 > h) return {0.f, 0.f, h};
+            const f3v n2 = fnormalized(f3v{n.x, n.y, 0.f});
+            return fadd(fscale(n2, -(r2 - r1)), fscale(n3, r2));
+        }
+        case XC_SAUCER: {
+            const float t = p.y, h = p.x, r2 = 0.5f * (h * h / t + t);
+            const f3v n3 = fnormalized(n);
+            const f3v n4{n.x, n.y, 0.f};
+            if (!fzero(n4) && (n3.x * n3.x + n3.y * n3.y) * r2 * r2 > h * h) return fscale(fnormalized(n4), h);
+            const f3v n2{0.f, 0.f, n.z < 0 ? -1.f : 1.f};
+            return fadd(fscale(n2, -(r2 - t)), fscale(n3, r2));
+        }
+        default: return {0.f, 0.f, 0.f};
+    }
+}
+
+// FP32 support point of the body (depth-first with an explicit stack, as xc_support).
+RP_XC_FN bool xcf_support(const XcShape &s, f3v n, f3v &out) {
+    struct Frame {
+        int node, i;
+        f3v n, acc;
+        float best;
+    };
+    Frame st[XC_MAX_DEPTH];
+    int top = 0;
+    st[0] = Frame{s.root, 0, n, {0.f, 0.f, 0.f}, 0.f};
+    f3v r{0.f, 0.f, 0.f};
+    bool have_r = false;
+    for (;;) {
+        Frame &f = st[top];
+        const XcNodeF &g = s.fnode[f.node];
+        if (have_r) {
+            const f3v w = fadd(fmv(g.erot[f.i], r), f3v{g.epos[f.i][0], g.epos[f.i][1], g.epos[f.i][2]});
+            if (g.type == XC_SUM) {
+                f.acc = fadd(f.acc, w);
+            } else if (g.type == XC_MAX) {
+                const float proj = fdot(w, f.n);
+                if (f.i == 0 || proj > f.best) {
+                    f.acc = w;
+                    f.best = proj;
+                }
+            } else {
+                f.acc = f.i == 0 ? w : fsub(f.acc, w);
+            }
+            f.i++;
+            have_r = false;
+        }
+        if (g.type < XC_SUM) {
+            r = xcf_primitive(g, f.n);
+        } else if (f.i < g.nent) {
+            if (top + 1 >= XC_MAX_DEPTH) return false;
+            const f3v dir = (g.type == XC_DIFF && f.i == 1) ? fneg(f.n) : f.n;
+            st[top + 1] = Frame{g.ent[f.i], 0, fmtv(g.erot[f.i], dir), {0.f, 0.f, 0.f}, 0.f};
+            top++;
+            continue;
+        } else {
+            r = f.acc;
+        }
+        if (top == 0) {
+            out = r;
+            return true;
+        }
+        top--;
+        have_r = true;
+    }
+}
+
+// Support point of body2 - body1 along n (FP32); body 1 at the origin.
+RP_HD bool xcf_diff(const XcShape &s, const float *r1, const float *r2, f3v p2, f3v n, f3v &v) {
+    f3v a, b;
+    if (!xcf_support(s, fmtv(r2, n), a)) return false;
+    if (!xcf_support(s, fmtv(r1, fneg(n)), b)) return false;
+    v = fsub(fadd(fmv(r2, a), p2), fmv(r1, b));
+    return true;
+}
+
+// The FP32 refinement: 0 miss (separating direction in n), 1 hit (portal directions d[0..2] of
+// v1, v2, v3), -1 undecided.
+RP_XC_FN int xcf_refine(const XcShape &s, const float *r1, const float *r2, f3v p2, f3v &n, f3v *d) {
+    const f3v c{s.fcentre[0], s.fcentre[1], s.fcentre[2]};
+    const f3v v0 = fsub(fadd(fmv(r2, c), p2), fmv(r1, c));
+    if (fzero(v0)) return -1;
+    f3v v1, v2, v3, v4;
+    n = fneg(v0);
+    if (!xcf_diff(s, r1, r2, p2, n, v1)) return -1;
+    d[0] = n;
+    if (fdot(v1, n) <= 0) return 0;
+    n = fcross(v1, v0);
+    if (fzero(n)) return -1;
+    if (!xcf_diff(s, r1, r2, p2, n, v2)) return -1;
+    d[1] = n;
+    if (fdot(v2, n) <= 0) return 0;
+    n = fcross(fsub(v1, v0), fsub(v2, v0));
+    if (fdot(n, v0) > 0) {
+        const f3v t = v1;
+        v1 = v2;
+        v2 = t;
+        const f3v td = d[0];
+        d[0] = d[1];
+        d[1] = td;
+        n = fneg(n);
+    }
+    for (int it = 0; it < 64; it++) {
+        if (!xcf_diff(s, r1, r2, p2, n, v3)) return -1;
+        const f3v d3 = n;
+        if (fdot(v3, n) <= 0) return 0;
+        if (fdot(fcross(v1, v3), v0) < 0) {
+            v2 = v3;
+            d[1] = d3;
+            n = fcross(fsub(v1, v0), fsub(v3, v0));
+            continue;
+        }
+        if (fdot(fcross(v3, v2), v0) < 0) {
+            v1 = v3;
+            d[0] = d3;
+            n = fcross(fsub(v3, v0), fsub(v2, v0));
+            continue;
+        }
+        d[2] = d3;
+        for (int jt = 0; jt < 64; jt++) {
+            n = fcross(fsub(v2, v1), fsub(v3, v1));
+            if (fdot(n, v1) >= 0) return 1;
+            if (!xcf_diff(s, r1, r2, p2, n, v4)) return -1;
+            const f3v d4 = n;
+            n = fnormalized(n);
+            if (fdot(v4, n) <= 0) return 0;
+            if (fdot(fsub(v4, v3), n) <= 1e-6f * (fabsf(fdot(v4, n)) + 1e-30f)) return 0;  // thin: origin beyond
+            const f3v cr = fcross(v4, v0);
+            if (fdot(v1, cr) > 0) {
+                if (fdot(v2, cr) > 0) {
+                    v1 = v4;
+                    d[0] = d4;
+                } else {
+                    v3 = v4;
+                    d[2] = d4;
+                }
+            } else {
+                if (fdot(v3, cr) > 0) {
+                    v2 = v4;
+                    d[1] = d4;
+                } else {
+                    v1 = v4;
+                    d[0] = d4;
+                }
+            }
+        }
+        return -1;
+    }
+    return -1;
+}
+
+// Signed distance-like value of the origin from the plane of face (a, b, c), positive on the side
+// of vertex e: (m . (0 - a)) * sign(m . (e - a)) / |m|, m = (b - a) x (c - a).
+RP_HD double face_clearance(d3 a, d3 b, d3 c, d3 e) {
+    const d3 m = cross3(sub3(b, a), sub3(c, a));
+    const double se = dot3(m, sub3(e, a));
+    const double so = -dot3(m, a);
+    const double mm = sqrt(norm2(m));
+    if (!(mm > 0) || se == 0) return -1.0;
+    return (se > 0 ? so : -so) / mm;
+}
+
+// The FP32 filter of a pair within the circumspheres and beyond the inspheres: 0 certified
+// separated, 1 certified overlapping, -1 undecided (the exact refinement decides).
+RP_XC_FN int xc_filter(const XcShape &s, d3 pos1, const double *rot1, d3 pos2bc, const double *rot2) {
+    const d3 dp = sub3(pos2bc, pos1);
+    float r1f[9], r2f[9];
+    for (int k = 0; k < 9; k++) {
+        r1f[k] = static_cast<float>(rot1[k]);
+        r2f[k] = static_cast<float>(rot2[k]);
+    }
+    f3v n, dirs[3];
+    const int hint = xcf_refine(s, r1f, r2f, f3v{(float)dp.x, (float)dp.y, (float)dp.z}, n, dirs);
+    const double margin = 1e-7 * (sqrt(norm2(dp)) + dadd(s.circ, s.circ)) + 1e-9;
+    if (hint == 0) {
+        const d3 nd{n.x, n.y, n.z};
+        const double nn = sqrt(norm2(nd));
+        d3 v;
+        if (nn > 0 && xc_diff_support(s, rot1, pos1, rot2, pos2bc, nd, v) && dot3(v, nd) < -margin * nn) return 0;
+    } else if (hint == 1) {
+        const d3 c = ld3(s.centre);
+        const d3 v0 = sub3(add3(mv3(rot2, c), pos2bc), add3(mv3(rot1, c), pos1));
+        d3 w[3];
+        bool ok = true;
+        for (int k = 0; k < 3 && ok; k++)
+            ok = xc_diff_support(s, rot1, pos1, rot2, pos2bc, d3{dirs[k].x, dirs[k].y, dirs[k].z}, w[k]);
+        if (ok && face_clearance(w[0], w[1], w[2], v0) > margin && face_clearance(v0, w[1], w[2], w[0]) > margin &&
+            face_clearance(v0, w[0], w[2], w[1]) > margin && face_clearance(v0, w[0], w[1], w[2]) > margin)
+            return 1;
+    }
+    return -1;
+}
+
+// XenoCollideTraits::overlapBetween with the FP32 filter and its FP64 certificates; the exact
+// refinement decides whatever they leave open.
+RP_HD bool xc_overlap_filtered(const XcShape &s, d3 pos1, const double *rot1, d3 pos2bc, const double *rot2,
+                               bool &stuck) {
+    const double rc = dadd(s.circ, s.circ);
+    const double ri = dadd(s.insph, s.insph);
+    const double d2 = norm2(sub3(pos2bc, pos1));
+    if (d2 > dmul(rc, rc)) return false;
+    if (d2 < dmul(ri, ri)) return true;
+    const int f = xc_filter(s, pos1, rot1, pos2bc, rot2);
+    if (f >= 0) return f == 1;
     return xc_intersect(s, rot1, pos1, rot2, pos2bc, 1.0e-12, stuck);
 }
 

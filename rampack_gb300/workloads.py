@@ -225,10 +225,10 @@ CONVEX = 4
 ROUNDED_BOX = "cuboid 1 1 2; sphere 0.1; sum"
 
 
-def config_convex_32768(spacing=(1.5, 1.5, 2.5)):
-    """32^3 rounded boxes, aligned, on an orthorhombic lattice (contact-free: the bodies span
+def config_convex(n_side=64, spacing=(1.5, 1.5, 2.5)):
+    """n_side^3 rounded boxes, aligned, on an orthorhombic lattice (contact-free: the bodies span
     1.2 x 1.2 x 2.2), packing fraction about 0.55."""
-    counts = (32, 32, 32)
+    counts = (n_side, n_side, n_side)
     pos = lattice(counts, spacing)
     box = diag_box(counts[0] * spacing[0], counts[1] * spacing[1], counts[2] * spacing[2])
     return CONVEX, ROUNDED_BOX, pos, aligned_rotations(len(pos)), box
