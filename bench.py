@@ -99,6 +99,11 @@ def _sc_64000(args):
     return W.config_sc_64000()
 
 
+def _soft_wca(args):
+    from rampack_gb300 import workloads as W
+    return W.hard_spheres(46, 0.40)
+
+
 def _convex_262144(args):
     from rampack_gb300 import workloads as W
     return W.config_convex(64)
@@ -120,6 +125,11 @@ WORKLOADS = {
                       "at x=-+0.35: a 60 degree kink), N={n:,} (25x40x100), aligned orthorhombic start at phi~0.33, "
                       "triclinic box; per cycle 2N moves (translation 0.2, rotation 0.2) + 1 isotension box move "
                       "(delta 0.005, p*=1.5, T=1)", "moves/sec, bent spherocylinder rods N=1e5"),
+    "soft-wca-97336": (_soft_wca, "WCA fluid: spheres of sigma=1 with the repulsive Lennard-Jones "
+                       "(RepulsiveLennardJonesInteraction, eps=1, cut at 2^(1/6) sigma) and no hard core, N={n:,} "
+                       "(46^3), simple-cubic start at phi=0.40, triclinic box; per cycle N translations (0.2) "
+                       "decided in FP64 with the Metropolis test at T=1 + 1 isotension box move (delta 0.005, p*=1.5) "
+                       "with the total-energy change", "moves/sec, WCA fluid N=97336"),
     "convex-262144": (_convex_262144, "generic convex bodies (XCBodyBuilder 'cuboid 1 1 2; sphere 0.1; sum': "
                       "rounded 1x1x2 boxes, XenoCollide pair tests: FP32 portal refinement with FP64 certificates, "
                       "exact FP64 refinement otherwise), N={n:,} (64^3), aligned orthorhombic start at phi~0.55, "
@@ -129,6 +139,15 @@ WORKLOADS = {
                  "phi=0.35 (cell aspect 1:1:6), triclinic box; per cycle 2N moves (translation 0.2, rotation "
                  "0.2) + 1 isotension box move (delta 0.005, p*=1.5, T=1)", "moves/sec, spherocylinders N=64000"),
 }
+
+
+# per-workload overrides: the rotation step (0: translations only) and a soft part
+# (kind, epsilon, sigma, with the hard core) set on the packing before the run
+EXTRA = {"soft-wca-97336": {"rotation_step": 0.0, "soft": (1, 1.0, 1.0, False)}}
+
+
+def rot_step(args) -> float:
+    return EXTRA.get(args.workload, {}).get("rotation_step", ROT_STEP)
 
 
 def workload(args):
@@ -217,7 +236,8 @@ def cpu_domains(threads: int):
     return best
 
 
-def cpu_run(cfg, cycles: int, warmup: int, threads: int, seed: int, volume_moves: bool = False):
+def cpu_run(cfg, cycles: int, warmup: int, threads: int, seed: int, volume_moves: bool = False,
+            rotation_step: float = ROT_STEP, soft=None):
     """The oracle's cycle loop on all host threads; with ``volume_moves`` the box move of odd
     cycles is the isotropic log-volume move instead of isotension (the headline's cycle)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -225,8 +245,10 @@ def cpu_run(cfg, cycles: int, warmup: int, threads: int, seed: int, volume_moves
     po.build()
     kind, prm, pos, rot, box = cfg
     pk = po.CpuPacking("oracle", kind, prm, pos, rot, box, threads=threads)
+    if soft is not None:
+        pk.set_soft(*soft)
     dom = cpu_domains(threads)
-    kw = dict(translation_step=TRANS_STEP, rotation_step=ROT_STEP, box_kind=1, box_step=BOX_STEP,
+    kw = dict(translation_step=TRANS_STEP, rotation_step=rotation_step, box_kind=1, box_step=BOX_STEP,
               pressure=PRESSURE, temperature=TEMPERATURE, domains=dom, threads=threads, seed=seed)
     kw_vol = dict(kw, box_kind=2, box_step=VOL_STEP / 3)
     if warmup:
@@ -237,7 +259,7 @@ def cpu_run(cfg, cycles: int, warmup: int, threads: int, seed: int, volume_moves
         st = po.run_cycles(pk, 1, **dict(kw_vol if volume_moves and c % 2 else kw, seed=seed + 1000 + c))
         times.append(time.perf_counter() - t)
     pk.close()
-    moves = 2 * len(pos)
+    moves = (2 if rotation_step > 0 else 1) * len(pos)
     return moves, times, dom, list(st.domains)
 
 
@@ -248,7 +270,8 @@ def main_reference(args):
     threads = os.cpu_count() or 1
     cfg = workload(args)
     moves, times, dom, dom_used = cpu_run(cfg, max(1, args.steps), max(0, args.warmup), threads, args.seed,
-                                          volume_moves=args.workload == "sc-1e6")
+                                          volume_moves=args.workload == "sc-1e6", rotation_step=rot_step(args),
+                                          soft=EXTRA.get(args.workload, {}).get("soft"))
     total = sum(times)
     value = moves * len(times) / total
     line = {
@@ -350,6 +373,8 @@ def main_gpu(args):
     kind, prm, pos, rot, box = cfg
     n = len(pos)
     g = GpuPacking(kind, prm, pos, rot, box, device=local)
+    if "soft" in EXTRA.get(args.workload, {}):
+        g.set_soft(*EXTRA[args.workload]["soft"])
     if args.cells_per_warp:
         g.set_cells_per_warp(args.cells_per_warp)
     g.box = np.array(box, dtype=np.float64)
@@ -361,7 +386,7 @@ def main_gpu(args):
     # on the headline, on every other cycle an isotropic log-volume move (ln V +- VOL_STEP),
     # each simulation with its own generator and Philox key
     from rampack_gb300 import simulation as SIM
-    sims = [SIM.Simulation(g, TRANS_STEP, ROT_STEP, seed, SIM.delta_triclinic(BOX_STEP, True))]
+    sims = [SIM.Simulation(g, TRANS_STEP, rot_step(args), seed, SIM.delta_triclinic(BOX_STEP, True))]
     if args.workload == "sc-1e6":
         sims.append(SIM.Simulation(g, TRANS_STEP, ROT_STEP, seed + 104729, SIM.log_volume(VOL_STEP / 3)))
     for sm in sims:
@@ -430,7 +455,7 @@ def main_gpu(args):
     for d in info["dims"]:
         phases *= 1 if d == 1 else (3 if d == 3 else 2)  # colours per grid dimension
     ncell = info["num_cells"]
-    moves_per_sweep = 2 * n
+    moves_per_sweep = (2 if rot_step(args) > 0 else 1) * n
     # algorithmic bytes per sweep: each phase streams every particle's FP32 record (28 B) and
     # cell index (4 B) and the cell offsets; every move reads the mover's FP64 state (96 B)
     # and an accepted move writes FP64 (96 B) and FP32 (28 B) state back.  Polyspheres of K
@@ -515,7 +540,8 @@ def main_gpu(args):
     cpu_base = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        cmoves, ctimes, dom, dom_used = cpu_run(cfg, 2, 1, threads, args.seed, volume_moves=args.workload == "sc-1e6")
+        cmoves, ctimes, dom, dom_used = cpu_run(cfg, 2, 1, threads, args.seed, volume_moves=args.workload == "sc-1e6",
+                                                rotation_step=rot_step(args), soft=EXTRA.get(args.workload, {}).get("soft"))
         cpu_base = {"value": cmoves * len(ctimes) / sum(ctimes), "unit": UNIT, "cores": threads, "kind": "port",
                     "sample": f"2 full cycles of the same N={n:,} system after 1 warm-up cycle, OpenMP domain "
                               f"decomposition {dom_used} (oracle/ restatement of the reference's path)"}
@@ -528,7 +554,7 @@ def main_gpu(args):
             "metric": metric(args), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(3, args.warmup), "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": describe(args, n), "n": n, "moves_per_step": 2 * n,
+            "config": {"workload": describe(args, n), "n": n, "moves_per_step": moves_per_sweep,
                        "variant": "plain (unordered FP32 filter + FP64 guard band)",
                        "l2": l2_note,
                        "parallelism": "replicas" if world > 1 else "single GPU",
