@@ -562,7 +562,7 @@ __device__ double soft_uniform(const SoftSweepArgs &A, int cell, int mi) {
 }
 
 template <int KIND>
-__global__ void __launch_bounds__(SOFT_WARPS * 32) k_soft_sweep(SoftSweepArgs A) {
+__global__ void __launch_bounds__(SOFT_WARPS * 32, 4) k_soft_sweep(SoftSweepArgs A) {
     __shared__ Mover movers[SOFT_WARPS];
     __shared__ rp_move moves[SOFT_WARPS];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;

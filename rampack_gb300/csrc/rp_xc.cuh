@@ -568,6 +568,91 @@ RP_HD double face_clearance(d3 a, d3 b, d3 c, d3 e) {
     return (se > 0 ? so : -so) / mm;
 }
 
+// FP64 support points for the certificates of flat bodies: the same geometry in plain double
+// arithmetic (contracted, one division per normalisation) — its rounding, near 1e-15 relative,
+// stays far below the certificates' margin, which is all a certificate needs.
+RP_XC_FN d3 xc_primitive_cert(const XcNode &g, d3 n) {
+    const d3 p{g.p[0], g.p[1], g.p[2]};
+    switch (g.type) {
+        case XC_POINT: return p;
+        case XC_SEGMENT: return {0.0, 0.0, n.z < 0 ? -p.x : p.x};
+        case XC_RECTANGLE: return {n.x < 0 ? -p.x : p.x, n.y < 0 ? -p.y : p.y, 0.0};
+        case XC_CUBOID: return {n.x < 0 ? -p.x : p.x, n.y < 0 ? -p.y : p.y, n.z < 0 ? -p.z : p.z};
+        case XC_DISK: {
+            const double l2 = n.x * n.x + n.y * n.y;
+            if (!(l2 > 0)) return {0.0, 0.0, 0.0};
+            const double k = p.x / sqrt(l2);
+            return {n.x * k, n.y * k, 0.0};
+        }
+        case XC_SPHERE: {
+            const double k = p.x / sqrt(n.x * n.x + n.y * n.y + n.z * n.z);
+            return {n.x * k, n.y * k, n.z * k};
+        }
+        case XC_ELLIPSE: {
+            const double ux = p.x * n.x, uy = p.y * n.y, l2 = ux * ux + uy * uy;
+            if (!(l2 > 0)) return {0.0, 0.0, 0.0};
+            const double k = 1.0 / sqrt(l2);
+            return {ux * k * p.x, uy * k * p.y, 0.0};
+        }
+        case XC_ELLIPSOID: {
+            const double ux = p.x * n.x, uy = p.y * n.y, uz = p.z * n.z;
+            const double k = 1.0 / sqrt(ux * ux + uy * uy + uz * uz);
+            return {ux * k * p.x, uy * k * p.y, uz * k * p.z};
+        }
+        default: {
+            // football, saucer: the exact evaluation (a few instructions more)
+            return xc_primitive_support(g, n);
+        }
+    }
+}
+
+// Support point of body2 - body1 along n for the certificates (flat bodies; others take the
+// exact evaluation).
+RP_XC_FN bool xc_diff_support_cert(const XcShape &s, const double *rot1, d3 pos1, const double *rot2, d3 pos2, d3 n,
+                                   d3 &v) {
+    if (!s.flat) return xc_diff_support(s, rot1, pos1, rot2, pos2, n, v);
+    const XcNode &g = s.node[s.root];
+    d3 side[2];
+    for (int b = 0; b < 2; b++) {
+        const double *rot = b == 0 ? rot2 : rot1;
+        const d3 dir = b == 0 ? n : d3{-n.x, -n.y, -n.z};
+        const d3 ln{rot[0] * dir.x + rot[3] * dir.y + rot[6] * dir.z, rot[1] * dir.x + rot[4] * dir.y + rot[7] * dir.z,
+                    rot[2] * dir.x + rot[5] * dir.y + rot[8] * dir.z};
+        d3 acc{0.0, 0.0, 0.0};
+        if (g.type < XC_SUM) {
+            acc = xc_primitive_cert(g, ln);
+        } else {
+            double best = 0.0;
+            for (int i = 0; i < g.nent; i++) {
+                const double *er = g.erot[i];
+                const d3 d = (g.type == XC_DIFF && i == 1) ? d3{-ln.x, -ln.y, -ln.z} : ln;
+                const d3 cd{er[0] * d.x + er[3] * d.y + er[6] * d.z, er[1] * d.x + er[4] * d.y + er[7] * d.z,
+                            er[2] * d.x + er[5] * d.y + er[8] * d.z};
+                const d3 r = xc_primitive_cert(s.node[g.ent[i]], cd);
+                const d3 w{er[0] * r.x + er[1] * r.y + er[2] * r.z + g.epos[i][0],
+                           er[3] * r.x + er[4] * r.y + er[5] * r.z + g.epos[i][1],
+                           er[6] * r.x + er[7] * r.y + er[8] * r.z + g.epos[i][2]};
+                if (g.type == XC_SUM) {
+                    acc = {acc.x + w.x, acc.y + w.y, acc.z + w.z};
+                } else if (g.type == XC_MAX) {
+                    const double pr = w.x * ln.x + w.y * ln.y + w.z * ln.z;
+                    if (i == 0 || pr > best) {
+                        acc = w;
+                        best = pr;
+                    }
+                } else {
+                    acc = i == 0 ? w : d3{acc.x - w.x, acc.y - w.y, acc.z - w.z};
+                }
+            }
+        }
+        side[b] = {rot[0] * acc.x + rot[1] * acc.y + rot[2] * acc.z, rot[3] * acc.x + rot[4] * acc.y + rot[5] * acc.z,
+                   rot[6] * acc.x + rot[7] * acc.y + rot[8] * acc.z};
+    }
+    v = {side[0].x + pos2.x - side[1].x - pos1.x, side[0].y + pos2.y - side[1].y - pos1.y,
+         side[0].z + pos2.z - side[1].z - pos1.z};
+    return true;
+}
+
 // The FP32 filter of a pair within the circumspheres and beyond the inspheres: 0 certified
 // separated, 1 certified overlapping, -1 undecided (the exact refinement decides).
 RP_XC_FN int xc_filter(const XcShape &s, d3 pos1, const double *rot1, d3 pos2bc, const double *rot2) {
@@ -584,14 +669,15 @@ RP_XC_FN int xc_filter(const XcShape &s, d3 pos1, const double *rot1, d3 pos2bc,
         const d3 nd{n.x, n.y, n.z};
         const double nn = sqrt(norm2(nd));
         d3 v;
-        if (nn > 0 && xc_diff_support(s, rot1, pos1, rot2, pos2bc, nd, v) && dot3(v, nd) < -margin * nn) return 0;
+        if (nn > 0 && xc_diff_support_cert(s, rot1, pos1, rot2, pos2bc, nd, v) && dot3(v, nd) < -margin * nn)
+            return 0;
     } else if (hint == 1) {
         const d3 c = ld3(s.centre);
         const d3 v0 = sub3(add3(mv3(rot2, c), pos2bc), add3(mv3(rot1, c), pos1));
         d3 w[3];
         bool ok = true;
         for (int k = 0; k < 3 && ok; k++)
-            ok = xc_diff_support(s, rot1, pos1, rot2, pos2bc, d3{dirs[k].x, dirs[k].y, dirs[k].z}, w[k]);
+            ok = xc_diff_support_cert(s, rot1, pos1, rot2, pos2bc, d3{dirs[k].x, dirs[k].y, dirs[k].z}, w[k]);
         if (ok && face_clearance(w[0], w[1], w[2], v0) > margin && face_clearance(v0, w[1], w[2], w[0]) > margin &&
             face_clearance(v0, w[0], w[2], w[1]) > margin && face_clearance(v0, w[0], w[1], w[2]) > margin)
             return 1;
