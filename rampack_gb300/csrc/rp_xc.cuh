@@ -482,9 +482,11 @@ RP_HD bool xcf_diff(const XcShape &s, const float *r1, const float *r2, f3v p2, 
     return true;
 }
 
-// The FP32 refinement: 0 miss (separating direction in n), 1 hit (portal directions d[0..2] of
-// v1, v2, v3), -1 undecided.
-RP_XC_FN int xcf_refine(const XcShape &s, const float *r1, const float *r2, f3v p2, f3v &n, f3v *d) {
+// The FP32 refinement: 0 miss (separating direction in n; *h the FP32 support projection along
+// the unit n, or +inf after the tolerance exit), 1 hit (portal directions d[0..2] of v1, v2,
+// v3), -1 undecided.
+RP_XC_FN int xcf_refine(const XcShape &s, const float *r1, const float *r2, f3v p2, f3v &n, f3v *d, float *h) {
+    *h = INFINITY;
     const f3v c{s.fcentre[0], s.fcentre[1], s.fcentre[2]};
     const f3v v0 = fsub(fadd(fmv(r2, c), p2), fmv(r1, c));
     if (fzero(v0)) return -1;
@@ -492,12 +494,18 @@ RP_XC_FN int xcf_refine(const XcShape &s, const float *r1, const float *r2, f3v 
     n = fneg(v0);
     if (!xcf_diff(s, r1, r2, p2, n, v1)) return -1;
     d[0] = n;
-    if (fdot(v1, n) <= 0) return 0;
+    if (fdot(v1, n) <= 0) {
+        *h = fdot(v1, n) / sqrtf(fdot(n, n));
+        return 0;
+    }
     n = fcross(v1, v0);
     if (fzero(n)) return -1;
     if (!xcf_diff(s, r1, r2, p2, n, v2)) return -1;
     d[1] = n;
-    if (fdot(v2, n) <= 0) return 0;
+    if (fdot(v2, n) <= 0) {
+        *h = fdot(v2, n) / sqrtf(fdot(n, n));
+        return 0;
+    }
     n = fcross(fsub(v1, v0), fsub(v2, v0));
     if (fdot(n, v0) > 0) {
         const f3v t = v1;
@@ -511,7 +519,10 @@ RP_XC_FN int xcf_refine(const XcShape &s, const float *r1, const float *r2, f3v 
     for (int it = 0; it < 64; it++) {
         if (!xcf_diff(s, r1, r2, p2, n, v3)) return -1;
         const f3v d3 = n;
-        if (fdot(v3, n) <= 0) return 0;
+        if (fdot(v3, n) <= 0) {
+            *h = fdot(v3, n) / sqrtf(fdot(n, n));
+            return 0;
+        }
         if (fdot(fcross(v1, v3), v0) < 0) {
             v2 = v3;
             d[1] = d3;
@@ -531,7 +542,10 @@ RP_XC_FN int xcf_refine(const XcShape &s, const float *r1, const float *r2, f3v 
             if (!xcf_diff(s, r1, r2, p2, n, v4)) return -1;
             const f3v d4 = n;
             n = fnormalized(n);
-            if (fdot(v4, n) <= 0) return 0;
+            if (fdot(v4, n) <= 0) {
+                *h = fdot(v4, n);  // n is a unit vector here
+                return 0;
+            }
             if (fdot(fsub(v4, v3), n) <= 1e-6f * (fabsf(fdot(v4, n)) + 1e-30f)) return 0;  // thin: origin beyond
             const f3v cr = fcross(v4, v0);
             if (fdot(v1, cr) > 0) {
@@ -663,8 +677,14 @@ RP_XC_FN int xc_filter(const XcShape &s, d3 pos1, const double *rot1, d3 pos2bc,
         r2f[k] = static_cast<float>(rot2[k]);
     }
     f3v n, dirs[3];
-    const int hint = xcf_refine(s, r1f, r2f, f3v{(float)dp.x, (float)dp.y, (float)dp.z}, n, dirs);
-    const double margin = 1e-7 * (sqrt(norm2(dp)) + dadd(s.circ, s.circ)) + 1e-9;
+    float h32;
+    const int hint = xcf_refine(s, r1f, r2f, f3v{(float)dp.x, (float)dp.y, (float)dp.z}, n, dirs, &h32);
+    const double scale = sqrt(norm2(dp)) + dadd(s.circ, s.circ);
+    // a miss certified in FP32 alone: the support projection of the Minkowski difference is a
+    // sum, or a maximum, of the parts' projections, each computed to a few FP32 roundings of
+    // terms no larger than the scale, so an FP32 projection below -1e-4 scale is negative
+    if (hint == 0 && h32 < static_cast<float>(-(1e-4 * scale + 1e-6))) return 0;
+    const double margin = 1e-7 * scale + 1e-9;
     if (hint == 0) {
         const d3 nd{n.x, n.y, n.z};
         const double nn = sqrt(norm2(nd));
