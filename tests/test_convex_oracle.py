@@ -90,3 +90,21 @@ def test_oracle_matches_the_golden_fixture(oracle):
         r1, p2, r2, want = z[f"{name}_r1"], z[f"{name}_p2"], z[f"{name}_r2"], z[f"{name}_overlap"]
         got = [po.convex_overlap("oracle", script, np.zeros(3), r1[k], p2[k], r2[k]) for k in range(len(p2))]
         assert np.array_equal(np.array(got), want), name
+
+
+def test_engine_builder_refuses_as_the_reference(oracle, engine):
+    """The engine's host builder (rp_create_convex) refuses invalid scripts before touching a
+    device, with the reference XCBodyBuilder's own messages."""
+    if not po.reference_available():
+        pytest.skip("reference library not built here")
+    import ctypes as C
+    lib = engine.load()
+    for bad in ("sphere -1", "cuboid 1 2", "sum", "wrap 3", "sphere 1; sphere 1", "blob 1", "", "diff",
+                "football 1 1", "saucer 1 3", "dup 2", "sphere 1; pop; pop", "segment 0", "ellipse 1 -2"):
+        with pytest.raises(ValueError) as ref:
+            po.convex_overlap("reference", bad, np.zeros(3), np.eye(3), np.ones(3), np.eye(3))
+        h = C.c_void_p()
+        rc = lib.rp_create_convex(bad.encode(), 10, 0, C.byref(h))
+        assert rc == -1, (bad, rc)  # RP_ERR_ARG
+        msg = lib.rp_last_error(None).decode()
+        assert msg == "convex body: " + str(ref.value), (bad, msg, str(ref.value))
