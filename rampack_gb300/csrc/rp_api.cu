@@ -700,10 +700,11 @@ int check_status(Handle *h) {
     RP_CUDA(h, cudaStreamSynchronize(h->stream));
     if (st) {
         RP_CUDA(h, cudaMemsetAsync(h->status, 0, sizeof(uint32_t), h->stream));
-        char buf[128];
-        std::snprintf(buf, sizeof(buf), "device status 0x%x%s%s", st,
+        char buf[256];
+        std::snprintf(buf, sizeof(buf), "device status 0x%x%s%s%s", st,
                       (st & ST_PARTICLE_NOT_IN_CELL) ? " (a move's particle is not in its cell)" : "",
-                      (st & ST_CAPACITY) ? " (a cell neighbourhood exceeds the staging capacity)" : "");
+                      (st & ST_CAPACITY) ? " (a cell neighbourhood exceeds the staging capacity)" : "",
+                      (st & ST_PORTAL_STUCK) ? " (a convex pair's portal refinement did not converge)" : "");
         if (st & ST_OUTSIDE) return fail(h, RP_ERR_ARG, "a particle lies outside the box");
         if (st & ST_NOT_ROTATION)
             return fail(h, RP_ERR_ARG, "an orientation is not a rotation matrix (|O^T O - I| >= 1e-6)");

@@ -21,6 +21,7 @@ enum : uint32_t {
     ST_CAPACITY = 1u << 3,              // a neighbourhood exceeded the largest staging capacity
     ST_OUTSIDE = 1u << 4,               // a particle lies outside the box
     ST_NOT_ROTATION = 1u << 5,          // an uploaded orientation is not a rotation (1e-6)
+    ST_PORTAL_STUCK = 1u << 6,          // a convex pair's portal refinement hit its iteration limit
 };
 
 // Constants of the FP32 filter: every comparison of the FP64 reference is decided in

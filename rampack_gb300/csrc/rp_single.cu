@@ -107,7 +107,7 @@ __device__ bool body_overlap(const DevState &s, d3 p, d3 a, const double *rot, i
         const d3 q = add3(pj, t ? *t : pbc_translation(s.box, s.inv, p, pj));
         bool stuck = false;
         const bool ov = xc_overlap_filtered(*s.xc, p, rot, q, rj, stuck);
-        if (stuck) atomicOr(s.status, ST_NUMERIC);
+        if (stuck) atomicOr(s.status, ST_PORTAL_STUCK);
         return ov;
     } else {
         const d3 aj{rj[2], rj[5], rj[8]};
@@ -280,7 +280,7 @@ __device__ int warp_overlaps_convex(const SingleArgs &A, const Mover &mv, int wh
                 bool stuck = false;
                 const int f = xc_filter(*s.xc, p, rot, add3(pj, t), s.rot64 + 9 * (size_t)j);
                 c = f >= 0 ? f : (xc_intersect(*s.xc, rot, p, s.rot64 + 9 * (size_t)j, add3(pj, t), 1.0e-12, stuck) ? 1 : 0);
-                if (stuck) atomicOr(s.status, ST_NUMERIC);
+                if (stuck) atomicOr(s.status, ST_PORTAL_STUCK);
             }
             if (early && __any_sync(FULL, c != 0)) return true;
             cnt += c;
@@ -322,7 +322,7 @@ __device__ int warp_overlaps_convex(const SingleArgs &A, const Mover &mv, int wh
                             certain += f >= 0 ? f
                                               : (xc_intersect(*s.xc, rot, p, s.rot64 + 9 * (size_t)j, add3(pj, t),
                                                               1.0e-12, stuck) ? 1 : 0);
-                            if (stuck) atomicOr(s.status, ST_NUMERIC);
+                            if (stuck) atomicOr(s.status, ST_PORTAL_STUCK);
                         }
                     }
                 }
@@ -749,7 +749,7 @@ __global__ void k_convex_pairs(const XcShape *xc, int64_t n, const double *p1, c
     if (i >= n) return;
     bool stuck = false;
     const bool ov = xc_overlap_filtered(*xc, load_d3(p1 + 3 * i), r1 + 9 * i, load_d3(p2 + 3 * i), r2 + 9 * i, stuck);
-    if (stuck) atomicOr(status, ST_NUMERIC);
+    if (stuck) atomicOr(status, ST_PORTAL_STUCK);
     out[i] = ov ? 1 : 0;
 }
 
