@@ -160,13 +160,15 @@ int rp_create_polyspherocylinder(int32_t num_centres, const double *centres, con
 
 /* Creates an engine for n generic convex bodies (GenericXenoCollideTraits,
  * core/shapes/GenericXenoCollideTraits.h) described by an XCBodyBuilder script: the commands
- * of XCBodyBuilder::processCommand (geometry/xenocollide/XCBodyBuilder.cpp:181-294) -- point,
+ * of XCBodyBuilder::processCommand (geometry/xenocollide/XCBodyBuilder.cpp:194-294) -- point,
  * segment, rectangle, cuboid, disk, sphere, ellipse, ellipsoid, football, saucer, move, rot,
  * sum [k], diff, wrap [k], dup k, pop, swap -- one per line or separated by ';'.  Pairs are
- * decided as XenoCollideTraits::overlapBetween (core/shapes/XenoCollideTraits.h:118-140):
+ * decided as XenoCollideTraits::overlapBetween (core/shapes/XenoCollideTraits.h:147-168):
  * circumspheres, inspheres, then XenoCollide's portal refinement with tolerance 1e-12, every
- * move in FP64.  Sweeps, single moves, overlap counts and counting mode, box moves; not
- * walls, orientation fixes, move lists, soft parts or the learned ordering (RP_ERR_UNSUPPORTED).
+ * move in FP64.  Sweeps, single moves, overlap counts and counting mode, box moves, hard walls
+ * (XenoCollideTraits::overlapWithWall, core/shapes/XenoCollideTraits.h:170-186) and orientation
+ * fixes; not move lists, soft parts, rototranslations or the learned ordering
+ * (RP_ERR_UNSUPPORTED).
  * An invalid script fails with RP_ERR_ARG and the builder's message in rp_last_error(NULL). */
 int rp_create_convex(const char *script, int64_t n, int device, void **handle);
 

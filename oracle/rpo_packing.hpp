@@ -105,7 +105,7 @@ struct Interaction {
     double hard_range() const {
         if (kind == SPHERE) return 2 * radius;
         if (kind == SPHEROCYLINDER) return 2 * radius + length;
-        if (kind == CONVEX) return 2 * xc->circ();   // XenoCollideTraits.h:160-172
+        if (kind == CONVEX) return 2 * xc->circ();   // XenoCollideTraits.h:188-202
         if (segments()) {   // PolyspherocylinderTraits.cpp:140-147
             double m = circumsphere(0);
             for (std::size_t i = 1; i < radii.size(); i++)
@@ -130,6 +130,12 @@ struct Interaction {
     bool overlap_with_wall(const V3 &pos, const M3 &rot, std::size_t idx, const V3 &origin, const V3 &wall) const {
         if (!hard) return false;   // a soft part has no wall part (CentralInteraction.h:48)
         if (kind == SPHERE) return dot(wall, sub(pos, origin)) < radius;
+        if (kind == CONVEX) {   // XenoCollideTraits.h:170-186, in the body frame
+            const V3 nv = mv(transpose(rot), wall);
+            const V3 sp = xc->support(xc_neg(nv));
+            const V3 o = mv(transpose(rot), sub(origin, pos));
+            return !(dot(xc_neg(o), nv) > dot(xc_neg(sp), nv));
+        }
         if (kind == POLYSPHERE && segments()) {   // PolyspherocylinderTraits.cpp:149-166
             V3 half = mv(rot, half_axes[idx]);
             if (dot(wall, sub(sub(pos, half), origin)) < radii[idx]) return true;
@@ -157,7 +163,7 @@ struct Interaction {
             // SphereTraits.cpp:56-65
             return bc.distance2(p1, p2) < std::pow(2 * radius, 2);
         } else if (kind == CONVEX) {
-            // XenoCollideTraits.h:118-140
+            // XenoCollideTraits.h:147-168
             return xc_overlap(*xc, p1, o1, add(p2, bc.translation(p1, p2)), o2);
         } else if (kind == SPHEROCYLINDER) {
             // SpherocylinderTraits.cpp:28-46

@@ -5,8 +5,8 @@
 // Generic convex bodies restated from the reference: the XenoCollide geometries
 // (geometry/xenocollide/XCPrimitives.cpp, XCOperations.cpp), XCBodyBuilder's commands
 // (geometry/xenocollide/XCBodyBuilder.cpp:37-294), Snethen's portal refinement as adapted in
-// geometry/xenocollide/XenoCollide.h:62-170 and the pair test of
-// core/shapes/XenoCollideTraits.h:118-140 — as polymorphic objects, the reference's own
+// geometry/xenocollide/XenoCollide.h:74-168 and the pair test of
+// core/shapes/XenoCollideTraits.h:147-168 — as polymorphic objects, the reference's own
 // structure, in its operation order (compiled with -ffp-contract=off).
 #pragma once
 
@@ -42,7 +42,7 @@ struct XcGeom {
 };
 using XcPtr = std::shared_ptr<XcGeom>;
 
-struct XcPoint : XcGeom {   // XCPrimitives.h:34-52
+struct XcPoint : XcGeom {   // XCPrimitives.h:34-48
     V3 pos;
     explicit XcPoint(const V3 &p) : pos(p) {}
     V3 support(const V3 &) const override { return pos; }
@@ -50,7 +50,7 @@ struct XcPoint : XcGeom {   // XCPrimitives.h:34-52
     double circ() const override { return 0; }
     double insph() const override { return 0; }
 };
-struct XcSegment : XcGeom {   // XCPrimitives.cpp:30-42
+struct XcSegment : XcGeom {   // XCPrimitives.cpp:30-41
     double h;
     explicit XcSegment(double hl) : h(hl) {}
     V3 support(const V3 &n) const override {
@@ -61,7 +61,7 @@ struct XcSegment : XcGeom {   // XCPrimitives.cpp:30-42
     double circ() const override { return h; }
     double insph() const override { return 0; }
 };
-struct XcRectangle : XcGeom {   // XCPrimitives.cpp:44-55
+struct XcRectangle : XcGeom {   // XCPrimitives.cpp:43-54
     V3 half;
     double c;
     XcRectangle(double hx, double hy) : half{hx, hy, 0}, c(std::sqrt(norm2(half))) {}
@@ -74,7 +74,7 @@ struct XcRectangle : XcGeom {   // XCPrimitives.cpp:44-55
     double circ() const override { return c; }
     double insph() const override { return 0; }
 };
-struct XcCuboid : XcGeom {   // XCPrimitives.cpp:57-70
+struct XcCuboid : XcGeom {   // XCPrimitives.cpp:56-69
     V3 half;
     double c, i;
     explicit XcCuboid(const V3 &h) : half(h), c(std::sqrt(norm2(h))), i(*std::min_element(h.begin(), h.end())) {}
@@ -87,7 +87,7 @@ struct XcCuboid : XcGeom {   // XCPrimitives.cpp:57-70
     double circ() const override { return c; }
     double insph() const override { return i; }
 };
-struct XcDisk : XcGeom {   // XCPrimitives.cpp:72-83
+struct XcDisk : XcGeom {   // XCPrimitives.cpp:71-81
     double r;
     explicit XcDisk(double rr) : r(rr) {}
     V3 support(const V3 &n) const override {
@@ -99,14 +99,14 @@ struct XcDisk : XcGeom {   // XCPrimitives.cpp:72-83
     double circ() const override { return r; }
     double insph() const override { return 0; }
 };
-struct XcSphere : XcGeom {   // XCPrimitives.h:135-150
+struct XcSphere : XcGeom {   // XCPrimitives.h:135-148
     double r;
     explicit XcSphere(double rr) : r(rr) {}
     V3 support(const V3 &n) const override { return vscale(xc_normalized(n), r); }
     double circ() const override { return r; }
     double insph() const override { return r; }
 };
-struct XcEllipse : XcGeom {   // XCPrimitives.cpp:89-103
+struct XcEllipse : XcGeom {   // XCPrimitives.cpp:87-100
     V3 axes;
     double c;
     XcEllipse(double a, double b) : axes{a, b, 0}, c(*std::max_element(axes.begin(), axes.end())) {}
@@ -118,7 +118,7 @@ struct XcEllipse : XcGeom {   // XCPrimitives.cpp:89-103
     double circ() const override { return c; }
     double insph() const override { return 0; }
 };
-struct XcEllipsoid : XcGeom {   // XCPrimitives.cpp:105-117
+struct XcEllipsoid : XcGeom {   // XCPrimitives.cpp:102-113
     V3 axes;
     double c, i;
     explicit XcEllipsoid(const V3 &a)
@@ -127,7 +127,7 @@ struct XcEllipsoid : XcGeom {   // XCPrimitives.cpp:105-117
     double circ() const override { return c; }
     double insph() const override { return i; }
 };
-struct XcFootball : XcGeom {   // XCPrimitives.cpp:119-138
+struct XcFootball : XcGeom {   // XCPrimitives.cpp:115-135
     double h, r1;
     XcFootball(double hl, double r) : h(hl), r1(r) {}
     V3 support(const V3 &n) const override {
@@ -141,7 +141,7 @@ struct XcFootball : XcGeom {   // XCPrimitives.cpp:119-138
     double circ() const override { return h; }
     double insph() const override { return r1; }
 };
-struct XcSaucer : XcGeom {   // XCPrimitives.cpp:140-163
+struct XcSaucer : XcGeom {   // XCPrimitives.cpp:137-163
     double h, t;
     XcSaucer(double radius, double half_thickness) : h(radius), t(half_thickness) {}
     V3 support(const V3 &n) const override {
@@ -171,7 +171,7 @@ inline V3 xc_entry_support(const XcEntry &e, const V3 &n) {
 }
 inline V3 xc_entry_centre(const XcEntry &e) { return add(mv(e.rot, e.g->centre()), e.pos); }
 
-struct XcSum : XcGeom {   // XCOperations.cpp:30-70
+struct XcSum : XcGeom {   // XCOperations.cpp:31-70
     std::vector<XcEntry> entries;
     double c = 0, i = 0;
     void add_entry(const XcEntry &e) {
@@ -217,7 +217,7 @@ struct XcDiff : XcGeom {   // XCOperations.cpp:72-97
     double circ() const override { return c; }
     double insph() const override { return i; }
 };
-struct XcMax : XcGeom {   // XCOperations.cpp:99-185
+struct XcMax : XcGeom {   // XCOperations.cpp:97-185
     std::vector<XcEntry> entries;
     double c = 0, i = 0;
     void add_entry(const XcEntry &e) {
@@ -395,7 +395,7 @@ inline XcPtr xc_build_script(const std::string &script) {
     return st.back().g;
 }
 
-// XenoCollide::Intersect (geometry/xenocollide/XenoCollide.h:55-169)
+// XenoCollide::Intersect (geometry/xenocollide/XenoCollide.h:58-168)
 inline V3 xc_tsv(const XcGeom &g, const M3 &rot, const V3 &pos, const V3 &n) {
     return add(mv(rot, g.support(mv(transpose(rot), n))), pos);
 }
@@ -446,7 +446,7 @@ inline bool xc_intersect(const XcGeom &g1, const M3 &r1, const V3 &p1, const XcG
     }
 }
 
-// XenoCollideTraits::overlapBetween (core/shapes/XenoCollideTraits.h:118-140), the second body
+// XenoCollideTraits::overlapBetween (core/shapes/XenoCollideTraits.h:147-168), the second body
 // at p2bc = pos2 + translation.
 inline bool xc_overlap(const XcGeom &g, const V3 &p1, const M3 &o1, const V3 &p2bc, const M3 &o2) {
     double rc = g.circ() + g.circ();

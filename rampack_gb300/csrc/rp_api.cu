@@ -1142,7 +1142,7 @@ int rp_create_polyspherocylinder(int32_t num_centres, const double *centres, con
 
 // Generic convex bodies (GenericXenoCollideTraits): the XCBodyBuilder script's geometry on the
 // device; the range is twice its circumsphere radius (XenoCollideTraits::getRangeRadius,
-// core/shapes/XenoCollideTraits.h:160-172).
+// core/shapes/XenoCollideTraits.h:188-202).
 int rp_create_convex(const char *script, int64_t n, int device, void **handle) {
     // (the move kernels queue near pairs as particle * 28 + image in an int)
     if (!script || !handle || n <= 0 || n > ((1ll << 31) - 1) / 28) return RP_ERR_ARG;
@@ -2211,7 +2211,6 @@ int rp_renormalize_orientations(void *handle, int allow_overlaps, int64_t *rejec
     if (!h || !rejected) return fail(h, RP_ERR_ARG, "null argument");
     if (!h->has_state) return fail(h, RP_ERR_STATE, "no state uploaded");
     if (h->soft) return fail(h, RP_ERR_UNSUPPORTED, "orientation fixes with a soft part");
-    if (h->shape.kind == RP_SHAPE_CONVEX) return fail(h, RP_ERR_UNSUPPORTED, "orientation fixes of convex bodies");
     RP_CUDA(h, cudaSetDevice(h->device));
     h->try_valid = false;
     {
@@ -2479,7 +2478,6 @@ int rp_get_grid_counters(void *handle, uint64_t *rebuilds, uint64_t *remaps) {
 int rp_set_walls(void *handle, int32_t mask) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h || mask < 0 || mask > 7) return fail(h, RP_ERR_ARG, "wall mask outside 0..7");
-    if (mask && h->shape.kind == RP_SHAPE_CONVEX) return fail(h, RP_ERR_UNSUPPORTED, "walls with convex bodies");
     h->walls = mask;
     h->try_valid = false;
     return RP_OK;

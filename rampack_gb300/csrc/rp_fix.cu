@@ -69,6 +69,14 @@ struct Version {
 __device__ __forceinline__ bool overlaps_pair(const DevState &s, d3 pi, const double *ri, const double *ai, int64_t j,
                                               const Version &v) {
     d3 pj = ld3(s.pos64 + 3 * j);
+    if (s.kind == 3) {
+        // generic convex bodies: XenoCollideTraits::overlapBetween (core/shapes/XenoCollideTraits.h:147-168)
+        bool stuck = false;
+        const bool ov = xc_overlap_filtered(*s.xc, pi, ri, add3(pj, pbc_translation(s.box, s.inv, pi, pj)),
+                                            v.rot + 9 * j, stuck);
+        if (stuck) atomicOr(s.status, ST_PORTAL_STUCK);
+        return ov;
+    }
     if (s.ncen == 0 && s.kind == 0 && s.pbc_fold) return pbc_distance2(s.box, s.inv, pi, pj) < s.ex.sphere_thr;
     if (s.ncen == 0) {
         d3 t = pbc_translation(s.box, s.inv, pi, pj);
@@ -107,6 +115,8 @@ __device__ __forceinline__ bool overlaps_pair(const DevState &s, d3 pi, const do
 // rotated centres fixed).
 __device__ __forceinline__ bool overlaps_walls(const DevState &s, d3 pi, const double *ri, const double *ci) {
     if (!s.walls) return false;
+    if (s.kind == 3)   // generic convex bodies: XenoCollideTraits::overlapWithWall
+        return xc_wall_count(*s.xc, s.walls, s.wall_vec, s.wall_far, s.wall_half, pi, ri, true) != 0;
     double hx[3 * MAX_CEN];
     if (s.segs)
         for (int a = 0; a < s.ncen; a++) {

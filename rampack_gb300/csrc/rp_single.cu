@@ -97,7 +97,7 @@ __device__ double soft_energy(const DevState &s, double d2) {
 // Pair test of a sphere, spherocylinder or generic convex mover (position p, axis a,
 // orientation rot) against particle j at translation t (null: no grid in the reference, the
 // periodic boundary conditions' nearest image), SphereTraits.cpp:56-65 /
-// SpherocylinderTraits.cpp:28-46 / XenoCollideTraits.h:118-140 (the mover is the first body,
+// SpherocylinderTraits.cpp:28-46 / XenoCollideTraits.h:147-168 (the mover is the first body,
 // as in Packing::countParticleOverlaps).
 template <int KIND>
 __device__ bool body_overlap(const DevState &s, d3 p, d3 a, const double *rot, int j, const d3 *t) {
@@ -253,7 +253,7 @@ __device__ __forceinline__ int candidate_at(const SingleArgs &A, const Mover &mv
 }
 
 // Generic convex bodies: the radii tests of XenoCollideTraits::overlapBetween
-// (core/shapes/XenoCollideTraits.h:124-131) decide most (candidate, image) pairs at once; the
+// (core/shapes/XenoCollideTraits.h:155-163) decide most (candidate, image) pairs at once; the
 // pairs between insphere and circumsphere distance are queued and their refinements run packed
 // 32 to a warp pass, so the lanes of a pass all refine (instead of a few lanes per candidate
 // round).  Same pairs and decisions as the per-candidate loop; the count, or 0 / 1 with `early`.
@@ -343,6 +343,12 @@ __device__ int warp_overlaps_convex(const SingleArgs &A, const Mover &mv, int wh
     }
     if (drain()) return 1;
     for (int d = 16; d > 0; d >>= 1) cnt += __shfl_xor_sync(FULL, cnt, d);
+    if (s.walls && !(early && cnt)) {
+        // hard walls after the pairs (core/Packing.cpp:424-428)
+        int w = 0;
+        if (lane == 0) w = xc_wall_count(*s.xc, s.walls, s.wall_vec, s.wall_far, s.wall_half, p, rot, early);
+        cnt += __shfl_sync(FULL, w, 0);
+    }
     return early ? (cnt > 0 ? 1 : 0) : cnt;
 }
 
@@ -737,6 +743,12 @@ __global__ void k_count_fp64(SingleArgs A, int early, unsigned long long *out, i
                 }
             }
         }
+    }
+    // Packing::countTotalOverlaps adds every particle's wall overlaps (core/Packing.cpp:558)
+    if (KIND == 3 && s.walls && !(early && (cnt || *(volatile int *)flag))) {
+        const int w = xc_wall_count(*s.xc, s.walls, s.wall_vec, s.wall_far, s.wall_half, load_d3(p), rot, early != 0);
+        if (w && early) atomicExch(flag, 1);
+        cnt += (unsigned long long)w;
     }
     if (cnt) atomicAdd(out, cnt);
 }

@@ -76,7 +76,7 @@ struct Builder {
     }
 
     // XCSum / XCMax: `count` shapes popped from the stack in turn become the entries
-    // (XCBodyBuilder.cpp:151-163, :173-185)
+    // (XCBodyBuilder.cpp:158-170, :180-192)
     bool combine(int type, std::size_t count) {
         if (count > static_cast<std::size_t>(XC_MAX_ENTRIES))
             return fail("more than " + std::to_string(XC_MAX_ENTRIES) + " components in one sum or wrap");
@@ -92,7 +92,7 @@ struct Builder {
             for (int k = 0; k < 9; k++) g.erot[i][k] = s.rot[k];
         }
         if (type == XC_SUM) {
-            // XCSum::recalculateGeometry (XCOperations.cpp:56-70) and getCenter (:45-50)
+            // XCSum::recalculateGeometry (XCOperations.cpp:57-70) and getCenter (:45-50)
             d3 centre_sum{0.0, 0.0, 0.0}, centre{0.0, 0.0, 0.0};
             double circ_sum = 0.0, insph_sum = 0.0;
             for (int i = 0; i < g.nent; i++) {
@@ -106,7 +106,7 @@ struct Builder {
             g.insph = std::max(0., insph_sum - disp);
             g.centre[0] = centre.x, g.centre[1] = centre.y, g.centre[2] = centre.z;
         } else {
-            // XCMax::recalculateGeometry (XCOperations.cpp:142-151), getCenter (:120-125)
+            // XCMax::recalculateGeometry (XCOperations.cpp:143-152), getCenter (:122-127)
             g.circ = norm3(ld3(g.epos[0])) + out.node[g.ent[0]].circ;
             d3 centre{0.0, 0.0, 0.0};
             for (int i = 0; i < g.nent; i++) {
@@ -122,7 +122,7 @@ struct Builder {
         return true;
     }
 
-    // XCMax::calculateInsphereRadius2 (XCOperations.cpp:158-185)
+    // XCMax::calculateInsphereRadius2 (XCOperations.cpp:159-185)
     double hull_insphere2(const XcNode &g) const {
         const double ins1 = out.node[g.ent[0]].insph, ins2 = out.node[g.ent[1]].insph;
         const d3 p1 = ld3(g.epos[0]), p2 = ld3(g.epos[1]);
@@ -171,7 +171,7 @@ struct Builder {
         return in.peek() != std::char_traits<char>::eof();
     }
 
-    // XCBodyBuilder::processCommand (XCBodyBuilder.cpp:181-294)
+    // XCBodyBuilder::processCommand (XCBodyBuilder.cpp:194-294)
     bool command(const std::string &cmd) {
         std::istringstream in(cmd);
         std::string name;

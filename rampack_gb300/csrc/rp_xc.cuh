@@ -1,7 +1,7 @@
 // Generic convex shapes (GenericXenoCollideTraits, core/shapes/GenericXenoCollideTraits.h):
 // a body given by an XCBodyBuilder script (geometry/xenocollide/XCBodyBuilder.cpp), its support
-// function, and the overlap test of core/shapes/XenoCollideTraits.h:118-140 by Minkowski portal
-// refinement (Snethen's XenoCollide, geometry/xenocollide/XenoCollide.h:62-170).
+// function, and the overlap test of core/shapes/XenoCollideTraits.h:147-168 by Minkowski portal
+// refinement (Snethen's XenoCollide, geometry/xenocollide/XenoCollide.h:74-168).
 //
 // The builder runs on the host and flattens the geometry into an array of nodes (primitives and
 // the Minkowski sum / difference / convex hull operations of geometry/xenocollide/
@@ -98,14 +98,14 @@ RP_HD d3 mtv3(const double *m, d3 v) {
     }
     return {r[0], r[1], r[2]};
 }
-// XCUtils.h:31-34
+// XCUtils.h:34-37
 RP_HD bool xc_zero(d3 v) {
     const double z = 9.094947e-13;
     return fabs(v.x) < z && fabs(v.y) < z && fabs(v.z) < z;
 }
 RP_HD d3 ld3(const double *p) { return {p[0], p[1], p[2]}; }
 
-// Support point of a primitive in its own frame (geometry/xenocollide/XCPrimitives.cpp:36-163,
+// Support point of a primitive in its own frame (geometry/xenocollide/XCPrimitives.cpp:30-163,
 // XCPrimitives.h:44, :145).
 RP_XC_FN d3 xc_primitive_support(const XcNode &g, d3 n) {
     switch (g.type) {
@@ -248,7 +248,7 @@ RP_XC_FN bool xc_support(const XcShape &s, int root, d3 n, d3 &out) {
     }
 }
 
-// XenoCollide.h:55-61: the support point of a placed body.
+// XenoCollide.h:58-66: the support point of a placed body.
 RP_XC_FN bool xc_transform_support(const XcShape &s, const double *rot, d3 pos, d3 n, d3 &out) {
     d3 local;
     if (s.flat) local = xc_support_flat(s, mtv3(rot, n));
@@ -266,7 +266,7 @@ RP_HD bool xc_diff_support(const XcShape &s, const double *rot1, d3 pos1, const 
     return true;
 }
 
-// XenoCollide::Intersect (XenoCollide.h:67-169) for two copies of the body; `stuck` is set when
+// XenoCollide::Intersect (XenoCollide.h:74-168) for two copies of the body; `stuck` is set when
 // the portal iterations exceed XC_MPR_LIMIT or the geometry is too deep (the pair is then
 // reported as overlapping).
 RP_XC_FN bool xc_intersect(const XcShape &s, const double *rot1, d3 pos1, const double *rot2, d3 pos2, double tol,
@@ -324,7 +324,7 @@ RP_XC_FN bool xc_intersect(const XcShape &s, const double *rot1, d3 pos1, const 
     return stuck = true;
 }
 
-// XenoCollideTraits::overlapBetween (core/shapes/XenoCollideTraits.h:118-140) with the second
+// XenoCollideTraits::overlapBetween (core/shapes/XenoCollideTraits.h:147-168) with the second
 // body already at its image (pos2bc = pos2 + translation).
 RP_HD bool xc_overlap(const XcShape &s, d3 pos1, const double *rot1, d3 pos2bc, const double *rot2, bool &stuck) {
     const double rc = dadd(s.circ, s.circ);
@@ -717,6 +717,41 @@ RP_HD bool xc_overlap_filtered(const XcShape &s, d3 pos1, const double *rot1, d3
     const int f = xc_filter(s, pos1, rot1, pos2bc, rot2);
     if (f >= 0) return f == 1;
     return xc_intersect(s, rot1, pos1, rot2, pos2bc, 1.0e-12, stuck);
+}
+
+// XenoCollideTraits::overlapWithWall (core/shapes/XenoCollideTraits.h:170-186): the wall normal w
+// taken into the body frame, the body's support point against it, and the wall plane through o.
+RP_XC_FN bool xc_wall_overlap(const XcShape &s, d3 pos, const double *rot, d3 o, d3 w) {
+    const d3 nv = mtv3(rot, w);
+    d3 sp;
+    if (s.flat) sp = xc_support_flat(s, neg3(nv));
+    else if (!xc_support(s, s.root, neg3(nv), sp)) return true;
+    const d3 origin = mtv3(rot, sub3(o, pos));
+    const double dist_support = dot3(neg3(sp), nv);
+    const double dist_wall = dot3(neg3(origin), nv);
+    return !(dist_wall > dist_support);
+}
+
+// Packing::countParticleWallOverlaps (core/Packing.cpp:1086-1139) for a convex body: per walled
+// axis the nearer wall (through the origin, or through the far corner with the normal reversed)
+// when the position lies within half the total range of it.
+RP_HD int xc_wall_count(const XcShape &s, int walls, const double (*wall_vec)[3], const double *wall_far, double half,
+                        d3 pos, const double *rot, bool early) {
+    int cnt = 0;
+    for (int i = 0; i < 3; i++) {
+        if (!((walls >> i) & 1)) continue;
+        const d3 w{wall_vec[i][0], wall_vec[i][1], wall_vec[i][2]};
+        const d3 far{wall_far[0], wall_far[1], wall_far[2]};
+        bool hit;
+        if (dot3(pos, w) < half) hit = xc_wall_overlap(s, pos, rot, d3{0.0, 0.0, 0.0}, w);
+        else if (dot3(sub3(far, pos), w) < half) hit = xc_wall_overlap(s, pos, rot, far, neg3(w));
+        else continue;
+        if (hit) {
+            cnt++;
+            if (early) return 1;
+        }
+    }
+    return cnt;
 }
 
 // ---- the builder (host) ---------------------------------------------------------------------

@@ -1,5 +1,5 @@
 """Generic convex bodies of the tests: XCBodyBuilder scripts covering every primitive and
-operation (geometry/xenocollide/XCBodyBuilder.cpp:181-294), and random rotations."""
+operation (geometry/xenocollide/XCBodyBuilder.cpp:194-294), and random rotations."""
 import numpy as np
 
 BODIES = {

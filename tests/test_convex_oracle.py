@@ -108,3 +108,75 @@ def test_engine_builder_refuses_as_the_reference(oracle, engine):
         assert rc == -1, (bad, rc)  # RP_ERR_ARG
         msg = lib.rp_last_error(None).decode()
         assert msg == "convex body: " + str(ref.value), (bad, msg, str(ref.value))
+
+
+@pytest.mark.parametrize("name,factor", [("cuboid", 1.0), ("cuboid", 0.8), ("cone", 0.8)])
+@pytest.mark.parametrize("allow", [False, True])
+def test_orientation_fixes_match_the_reference(oracle, name, factor, allow):
+    """Packing::renormalizeOrientations on convex bodies with orientations 1e-7 off orthonormal
+    (compressed lattices hold overlaps, so some fixes are rejected)."""
+    if not po.reference_available():
+        pytest.skip("reference library not built here")
+    from convex_bodies import CIRCUMSPHERE
+    pos, rot, box = lattice(5, 2.02 * CIRCUMSPHERE[name])
+    pos, box = pos * factor, np.asarray(box) * factor
+    rot = rot + np.random.default_rng(2).normal(0.0, 1e-7, rot.shape)
+    a = po.CpuPacking("oracle", po.CONVEX, BODIES[name], pos, rot, box)
+    b = po.CpuPacking("reference", po.CONVEX, BODIES[name], pos, rot, box)
+    assert a.renormalize_orientations(allow) == b.renormalize_orientations(allow)
+    sa, sb = a.state(), b.state()
+    assert np.array_equal(sa[0], sb[0]) and np.array_equal(sa[1], sb[1])
+
+
+@pytest.mark.parametrize("name,mask", [("cuboid", 7), ("cone", 5), ("rotated_sum", 2)])
+def test_walls_match_the_reference(oracle, name, mask):
+    """Hard walls (XenoCollideTraits::overlapWithWall, core/shapes/XenoCollideTraits.h:170-186):
+    a lattice pushed against the near walls (some bodies through them), its counts, a replayed
+    move stream, the same stream in overlap-counting mode and a box move; then an NpT cycle-loop
+    run from a lattice clear of the walls.  Identical codes, counts and FP64 states."""
+    if not po.reference_available():
+        pytest.skip("reference library not built here")
+    from convex_bodies import CIRCUMSPHERE
+    spacing = 2.02 * CIRCUMSPHERE[name]
+    pos0, rot, box = lattice(5, spacing)
+    pos = pos0 - 0.3 * spacing
+    g = po.CpuPacking("oracle", po.CONVEX, BODIES[name], pos, rot, box, threads=1)
+    r = g.rng(7)
+    moves = g.draw_moves(r, 0.4, 0.4, np.arange(g.n), g.n, 3 * g.n, domain=-1)
+    g.rng_free(r)
+    g.close()
+    out = {}
+    for which in ("oracle", "reference"):
+        pk = po.CpuPacking(which, po.CONVEX, BODIES[name], pos, rot, box, threads=1)
+        pk.set_walls(mask)
+        counts = (pk.count_overlaps(False), pk.count_overlaps(True))
+        codes, _ = pk.replay(moves, None)
+        st = pk.state()
+        nb = np.asarray(box).reshape(9) * 0.99
+        de = pk.try_scaling(nb)
+        pk.close()
+        c = po.CpuPacking(which, po.CONVEX, BODIES[name], pos, rot, box, threads=1)
+        c.set_walls(mask)
+        c.set_counting(True)
+        c0 = c.cached_overlaps()
+        ccodes, deltas = c.replay(moves, None)
+        cfin = c.cached_overlaps()
+        c.close()
+        s = po.CpuPacking(which, po.CONVEX, BODIES[name], pos0, rot, box, threads=1)
+        s.set_walls(mask)
+        run = po.run_cycles(s, 15, translation_step=0.3, rotation_step=0.3, box_kind=1, box_step=0.01,
+                            pressure=2.0, temperature=1.0, seed=4)
+        out[which] = (counts, codes, st, de, c0, ccodes, deltas, cfin,
+                      (run.moves[0], run.accepted[0], run.scalings, run.scalings_accepted), s.state())
+        s.close()
+    a, b = out["oracle"], out["reference"]
+    assert a[0] == b[0] and a[0][0] > 0, (a[0], b[0])   # the shifted lattice meets the walls
+    assert np.array_equal(a[1], b[1])
+    for x, y in zip(a[2], b[2]):
+        assert np.array_equal(x, y)
+    assert a[3] == b[3]
+    assert a[4] == b[4] and a[7] == b[7] and a[4] != a[7]
+    assert np.array_equal(a[5], b[5]) and np.array_equal(a[6], b[6])
+    assert a[8] == b[8]
+    for x, y in zip(a[9], b[9]):
+        assert np.array_equal(x, y)

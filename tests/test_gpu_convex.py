@@ -121,14 +121,96 @@ def test_single_moves_of_the_serial_path(oracle, engine, name):
     cpu.close()
 
 
+@pytest.mark.parametrize("name,factor", [("cuboid", 1.0), ("cuboid", 0.8), ("cone", 0.8)])
+@pytest.mark.parametrize("allow", [False, True])
+def test_orientation_fixes(oracle, engine, name, factor, allow):
+    """Packing::renormalizeOrientations: rejected counts and FP64 states as the oracle's."""
+    from rampack_gb300 import _lib
+    from rampack_gb300.packing import GpuPacking
+    pos, rot, box = lattice(5, 2.02 * CIRCUMSPHERE[name])
+    pos, box = pos * factor, np.asarray(box) * factor
+    rot = rot + np.random.default_rng(2).normal(0.0, 1e-7, rot.shape)
+    cpu = po.CpuPacking("oracle", po.CONVEX, BODIES[name], pos, rot, box)
+    with GpuPacking(_lib.SHAPE_CONVEX, BODIES[name], pos, rot, box) as g:
+        assert g.renormalize_orientations(allow) == cpu.renormalize_orientations(allow)
+        assert same_state(g, cpu)
+    cpu.close()
+
+
+@pytest.mark.parametrize("name,mask", [("cuboid", 7), ("cone", 5), ("rotated_sum", 2)])
+def test_walls(oracle, engine, name, mask):
+    """Hard walls (XenoCollideTraits::overlapWithWall): a lattice pushed against the near walls,
+    some bodies through them; counts, logged sweeps in counting mode and a box move, then plain
+    sweeps, a single-move stream and orientation fixes, all as the oracle's (pinned to the
+    reference with walls in tests/test_convex_oracle.py)."""
+    from rampack_gb300 import _lib
+    from rampack_gb300.packing import GpuPacking
+    spacing = 2.02 * CIRCUMSPHERE[name]
+    pos, rot, box = lattice(5, spacing)
+    pos = pos - 0.3 * spacing
+    cpu = po.CpuPacking("oracle", po.CONVEX, BODIES[name], pos, rot, box, threads=1)
+    cpu.set_walls(mask)
+    cpu.set_counting(True)
+    with GpuPacking(_lib.SHAPE_CONVEX, BODIES[name], pos, rot, box) as g:
+        g.set_walls(mask)
+        g.set_counting(True)
+        assert g.count_total_overlaps(False) == cpu.count_overlaps(False) > 0
+        assert g.count_total_overlaps(True) == cpu.count_overlaps(True) == 1
+        assert g.cached_overlaps() == cpu.cached_overlaps()
+        for cycle in range(2):
+            g.sweep(0.3, 0.3, seed=13, counter=cycle, log=True)
+            moves, codes = g.sweep_log()
+            _, _, bounds = g.grid()
+            want, _ = cpu.replay(moves, bounds)
+            assert np.array_equal(codes, want), np.count_nonzero(codes != want)
+            assert g.cached_overlaps() == cpu.cached_overlaps()
+        nb = np.asarray(g.state()[2]).reshape(9) * 0.99
+        assert g.try_scaling(nb) == cpu.try_scaling(nb)
+        assert g.cached_overlaps() == cpu.cached_overlaps()
+        assert same_state(g, cpu)
+    cpu.close()
+    # plain mode: sweeps and a single-move stream from the same start, then orientation fixes
+    cpu = po.CpuPacking("oracle", po.CONVEX, BODIES[name], pos, rot, box, threads=1)
+    cpu.set_walls(mask)
+    with GpuPacking(_lib.SHAPE_CONVEX, BODIES[name], pos, rot, box) as g:
+        g.set_walls(mask)
+        for cycle in range(2):
+            st = g.sweep(0.4, 0.4, seed=3, counter=cycle, log=True)
+            moves, codes = g.sweep_log()
+            _, _, bounds = g.grid()
+            want, _ = cpu.replay(moves, bounds)
+            assert np.array_equal(codes, want), np.count_nonzero(codes != want)
+            assert 0 < st["accepted"] < st["moves"]
+        rng = cpu.rng(5)
+        moves = cpu.draw_moves(rng, 0.5, 0.5, np.arange(cpu.n), cpu.n, cpu.n, domain=-1)
+        cpu.rng_free(rng)
+        codes = np.zeros(len(moves), dtype=np.uint8)
+        for i, m in enumerate(moves):
+            de = g.try_move(int(m["particle"]), int(m["type"]), m["translation"], m["rotation"])
+            code = 0 if not np.isinf(de) else 1
+            if m["uniform"] <= np.exp(-de):
+                g.accept_move()
+                code |= 0x80
+            codes[i] = code
+        want, _ = cpu.replay(moves, None)
+        assert np.array_equal(codes, want), np.count_nonzero(codes != want)
+        assert same_state(g, cpu)
+        p, r, b = g.state()
+        r = r + np.random.default_rng(4).normal(0.0, 1e-7, r.shape)
+    cpu.close()
+    cpu = po.CpuPacking("oracle", po.CONVEX, BODIES[name], p, r, b)
+    cpu.set_walls(mask)
+    with GpuPacking(_lib.SHAPE_CONVEX, BODIES[name], p, r, b) as g:
+        g.set_walls(mask)
+        assert g.renormalize_orientations(False) == cpu.renormalize_orientations(False)
+        assert same_state(g, cpu)
+    cpu.close()
+
+
 def test_unsupported_operations_are_refused(engine):
     from rampack_gb300._lib import EngineError
     cpu, g = packing("cuboid", n_side=3)
     with g:
-        with pytest.raises(EngineError):
-            g.set_walls(1)
-        with pytest.raises(EngineError):
-            g.renormalize_orientations(False)
         with pytest.raises(EngineError):
             g.set_soft(2, 1.0, 1.0)
     cpu.close()
