@@ -323,7 +323,8 @@ def cycle(g, k, seed, rng, stats=False):
 
 PROFILES = {"sc-1e6": "k_sweep_sc_n1e6.md", "banana-1e5": "k_sweep_banana_n1e5.md",
             "bent-rods-1e5": "k_sweep_bent_rods_n1e5.md",
-            "replicas-64": "k_b_sweep_replicas_64.md"}
+            "replicas-64": "k_b_sweep_replicas_64.md", "soft-wca-97336": "k_soft_sweep_wca_n97336.md",
+            "convex-262144": "k_soft_sweep_convex_n262144.md"}
 REBUILD_PROFILES = {"sc-1e6": "rebuild_sc_n1e6.md"}
 
 
@@ -340,6 +341,19 @@ def read_profile_traffic(workload, key="traffic_bytes_per_launch", profiles=None
                 return float(line.split(":", 1)[1].strip().split()[0])
             except ValueError:
                 return None
+    return None
+
+
+def read_profile_note(workload, key, profiles=None):
+    """A one-line finding (e.g. the limiter of the sweep kernel) from the workload's committed
+    ncu summary, if any."""
+    name = (profiles or PROFILES).get(workload)
+    path = os.path.join(ROOT, "profiles", name) if name else ""
+    if not name or not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith(key + ":"):
+            return line.split(":", 1)[1].strip()
     return None
 
 
@@ -367,6 +381,7 @@ def main_gpu(args):
 
     from rampack_gb300 import build as rb
     rb.build()
+    from rampack_gb300 import _lib
     from rampack_gb300.packing import GpuPacking
 
     cfg = workload(args)
@@ -464,6 +479,12 @@ def main_gpu(args):
     # K FP32 centres to an accepted move's write.
     kcen = int(prm[0]) if kind == 2 else 0
     rec32, s64, w64 = 28 + 16 * kcen, 96 + 24 * kcen, 96 + 28 + 64 * kcen
+    # soft parts and convex bodies move through the FP64 sweep (k_soft_sweep): each phase reads
+    # every particle's FP64 position (24 B; convex bodies also the orientation, 72 B) and grid
+    # slot (4 B) through the movers' neighbourhoods; an accepted move writes the FP64 state
+    fp64_sweep = kind == _lib.SHAPE_CONVEX or "soft" in EXTRA.get(args.workload, {})
+    if fp64_sweep:
+        rec32, s64, w64 = 24 + (72 if kind == _lib.SHAPE_CONVEX else 0), 96, 96
     b_sweep = phases * n * (rec32 + 4) + phases * (ncell + 1) * 4 + moves_per_sweep * (s64 + acc_rate * w64)
     b_launch = b_sweep / phases
     avg_launch_ms = sweep_ms / max(1, sweep_launches)
@@ -562,7 +583,9 @@ def main_gpu(args):
                        "box_moves": box_moves},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "k_sweep (one launch per checkerboard phase)",
+                         "kernel": ("k_soft_sweep (FP64 moves; one launch per checkerboard phase)" if fp64_sweep
+                                    else "k_sweep (one launch per checkerboard phase)"),
+                         "limiter": read_profile_note(args.workload, "limiter"),
                          "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
                          else "fallback 6.8 TB/s",
                          "avg_launch_ms": avg_launch_ms, "bytes_per_launch": b_launch},

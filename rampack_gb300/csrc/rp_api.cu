@@ -1369,6 +1369,23 @@ int rp_download_state(void *handle, double *pos, double *rot, double *box9) {
     return RP_OK;
 }
 
+// FP32 pre-filter of a separation at one image: the interaction range (body range for
+// multi-centre bodies) plus a margin far above the FP32 rounding of coordinates of the box's
+// size; a single image per pair where that reach stays below 0.45 of every box height (the
+// heights are the reciprocal norms of the inverse box's rows).
+static void set_prefilter(SingleArgs &a, const Handle *h) {
+    double pmax = 0, rowmax = 0;
+    for (int i = 0; i < 3; i++) {
+        pmax = std::max(pmax, std::fabs(h->box[3 * i]) + std::fabs(h->box[3 * i + 1]) + std::fabs(h->box[3 * i + 2]));
+        const double *r = h->inv + 3 * i;
+        rowmax = std::max(rowmax, std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]));
+    }
+    const double reach = h->range * (1.0 + 1e-3) + 1e-4 * (pmax + h->range);
+    a.reach2 = static_cast<float>(reach * reach);
+    for (int i = 0; i < 9; i++) a.box32[i] = static_cast<float>(h->box[i]);
+    a.one_image = reach * rowmax <= 0.45 ? 1 : 0;
+}
+
 // The arguments of the FP64 kernels (single moves, soft and convex sweeps, FP64 recounts) for the
 // current state: the FP32 pre-filter reach of a separation at one image is the interaction
 // range (body range for multi-centre bodies) plus a margin far above the FP32 rounding of
@@ -1377,12 +1394,7 @@ SingleArgs single_args(Handle *h) {
     SingleArgs a{};
     a.s = dev_state(h);
     a.g = h->grid[h->gcur].d;
-    double pmax = 0;
-    for (int i = 0; i < 3; i++)
-        pmax = std::max(pmax, std::fabs(h->box[3 * i]) + std::fabs(h->box[3 * i + 1]) + std::fabs(h->box[3 * i + 2]));
-    const double reach = h->range * (1.0 + 1e-3) + 1e-4 * (pmax + h->range);
-    a.reach2 = static_cast<float>(reach * reach);
-    for (int i = 0; i < 9; i++) a.box32[i] = static_cast<float>(h->box[i]);
+    set_prefilter(a, h);
     return a;
 }
 
@@ -1668,12 +1680,7 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
         sa.c.s = dev_state(h);
         sa.c.g = g;
         sa.c.temperature = h->temperature;
-        double pmax = 0;
-        for (int i = 0; i < 3; i++)
-            pmax = std::max(pmax, std::fabs(h->box[3 * i]) + std::fabs(h->box[3 * i + 1]) + std::fabs(h->box[3 * i + 2]));
-        const double reach = h->range * (1.0 + 1e-3) + 1e-4 * (pmax + h->range);
-        sa.c.reach2 = static_cast<float>(reach * reach);
-        for (int i = 0; i < 9; i++) sa.c.box32[i] = static_cast<float>(h->box[i]);
+        set_prefilter(sa.c, h);
         sa.seed = p->seed;
         sa.counter = p->counter;
         sa.tstep = static_cast<float>(tstep);
@@ -1832,12 +1839,7 @@ static int soft_total_energy(Handle *h, double *out) {
     SingleArgs a{};
     a.s = dev_state(h);
     a.g = h->grid[h->gcur].d;
-    double pmax = 0;
-    for (int i = 0; i < 3; i++)
-        pmax = std::max(pmax, std::fabs(h->box[3 * i]) + std::fabs(h->box[3 * i + 1]) + std::fabs(h->box[3 * i + 2]));
-    const double reach = h->range * (1.0 + 1e-3) + 1e-4 * (pmax + h->range);
-    a.reach2 = static_cast<float>(reach * reach);
-    for (int i = 0; i < 9; i++) a.box32[i] = static_cast<float>(h->box[i]);
+    set_prefilter(a, h);
     {
         Group grp(h, RP_KERNEL_COUNT, 2);
         RP_CUDA(h, launch_total_energy(a, h->d_energy, h->d_energy + h->n, h->stream));
@@ -2004,14 +2006,7 @@ int rp_try_move(void *handle, const rp_move *move, const double *domain6, double
     a.disp_list = h->d_disp_list;
     a.disp_flag = h->d_disp_flag;
     a.ndisp = static_cast<int>(h->disp_host.size());
-    // FP32 pre-filter of a separation at one image: the interaction range (body range for
-    // multi-centre bodies) plus a margin far above the FP32 rounding of coordinates of the box's size
-    double pmax = 0;
-    for (int i = 0; i < 3; i++)
-        pmax = std::max(pmax, std::fabs(h->box[3 * i]) + std::fabs(h->box[3 * i + 1]) + std::fabs(h->box[3 * i + 2]));
-    const double reach = h->range * (1.0 + 1e-3) + 1e-4 * (pmax + h->range);
-    a.reach2 = static_cast<float>(reach * reach);
-    for (int i = 0; i < 9; i++) a.box32[i] = static_cast<float>(h->box[i]);
+    set_prefilter(a, h);
     if (domain6) {
         a.has_domain = 1;
         for (int d = 0; d < 3; d++) {

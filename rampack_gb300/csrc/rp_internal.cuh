@@ -262,6 +262,7 @@ struct SingleArgs {
     int ndisp;
     float reach2;       // FP32 pre-filter of a body separation at one image: reach^2
     float box32[9];     // the box in FP32 (the images' translations in the pre-filter)
+    int one_image;      // the reach is below 0.45 of every box height: one image per pair to test
     int has_domain;     // an ActiveDomain: relative bounds lo[3], hi[3] (ActiveDomain::RegionBounds)
     double dom_lo[3], dom_hi[3];
 };

@@ -65,13 +65,15 @@ __device__ int cell_of(const DevState &s, const GridDev &g, d3 p, int c[3]) {
 // image within reach instead).
 __device__ int neighbour_cells(const GridDev &g, const int c[3], int *out) {
     int k = 0;
+    const bool distinct = g.dims[0] >= 3 && g.dims[1] >= 3 && g.dims[2] >= 3;
     for (int oz = -1; oz <= 1; oz++)
         for (int oy = -1; oy <= 1; oy++)
             for (int ox = -1; ox <= 1; ox++) {
                 int nb = wrap_cell(c[0] + ox, g.dims[0]) +
                          g.dims[0] * (wrap_cell(c[1] + oy, g.dims[1]) + g.dims[1] * wrap_cell(c[2] + oz, g.dims[2]));
                 bool seen = false;
-                for (int q = 0; q < k; q++) seen = seen || out[q] == nb;
+                if (!distinct)
+                    for (int q = 0; q < k; q++) seen = seen || out[q] == nb;
                 if (!seen) out[k++] = nb;
             }
     return k;
@@ -155,6 +157,30 @@ __device__ __forceinline__ d3 image_translation(const DevState &s, int mx, int m
     return load_d3(s.trans + 3 * (((mx + 2) * 5 + (my + 2)) * 5 + (mz + 2)));
 }
 
+// The periodic images m in {-1, 0, 1}^3 of a pair within the pre-filter reach, given its FP32
+// separation q - p, in the order of the 27-image loop; f(mx, my, mz) returns true to stop.
+// Where the reach is below 0.45 of every box height (one_image), an image within reach has
+// every fractional separation component below 0.45 in magnitude and any other image is a
+// whole box height away in some direction, so the only candidate is the image whose
+// fractional separation rounds to zero (FP32 rounding is ~1e-6 against the 0.05 margin): it
+// alone goes through the same pre-filter test, and the images passed are the 27-image loop's.
+template <typename F>
+__device__ __forceinline__ void for_each_image(const SingleArgs &A, float3 sep, F &&f) {
+    if (A.one_image) {
+        const float *iv = A.s.inv32;
+        const int mx = -__float2int_rn(iv[0] * sep.x + iv[1] * sep.y + iv[2] * sep.z);
+        const int my = -__float2int_rn(iv[3] * sep.x + iv[4] * sep.y + iv[5] * sep.z);
+        const int mz = -__float2int_rn(iv[6] * sep.x + iv[7] * sep.y + iv[8] * sep.z);
+        if (mx < -1 || mx > 1 || my < -1 || my > 1 || mz < -1 || mz > 1) return;
+        if (within_reach(A, sep, mx, my, mz)) f(mx, my, mz);
+        return;
+    }
+    for (int mx = -1; mx <= 1; mx++)
+        for (int my = -1; my <= 1; my++)
+            for (int mz = -1; mz <= 1; mz++)
+                if (within_reach(A, sep, mx, my, mz) && f(mx, my, mz)) return;
+}
+
 // Overlapping pairs of a mover state (position p, axis a; multi-centre: absolute centres abs,
 // half axes hax) with body j over every periodic image within reach (each absolute centre is
 // wrapped into the box on its own, so images are enumerated per centre pair); at most 1 with
@@ -168,16 +194,12 @@ __device__ int candidate_overlaps(const SingleArgs &A, const double *p, d3 a, co
         const d3 pp{p[0], p[1], p[2]};
         if (s.pbc_fold) return body_overlap<KIND>(s, pp, a, rot, j, nullptr) ? 1 : 0;
         const float3 sep = separation32(s.pos64 + 3 * (size_t)j, p);
-        for (int mx = -1; mx <= 1; mx++)
-            for (int my = -1; my <= 1; my++)
-                for (int mz = -1; mz <= 1; mz++) {
-                    if (!within_reach(A, sep, mx, my, mz)) continue;
-                    const d3 t = image_translation(s, mx, my, mz);
-                    if (body_overlap<KIND>(s, pp, a, rot, j, &t)) {
-                        if (early) return 1;
-                        cnt++;
-                    }
-                }
+        for_each_image(A, sep, [&](int mx, int my, int mz) {
+            const d3 t = image_translation(s, mx, my, mz);
+            if (!body_overlap<KIND>(s, pp, a, rot, j, &t)) return false;
+            cnt++;
+            return early;
+        });
         return cnt;
     } else {
         for (int ca = 0; ca < s.ncen; ca++) {
@@ -192,16 +214,13 @@ __device__ int candidate_overlaps(const SingleArgs &A, const double *p, d3 a, co
                     continue;
                 }
                 const float3 sep = separation32(s.abs64 + 3 * ((size_t)j * s.ncen + b), abs + 3 * ca);
-                for (int mx = -1; mx <= 1; mx++)
-                    for (int my = -1; my <= 1; my++)
-                        for (int mz = -1; mz <= 1; mz++) {
-                            if (!within_reach(A, sep, mx, my, mz)) continue;
-                            const d3 t = image_translation(s, mx, my, mz);
-                            if (centre_overlap(s, pa, ha, ca, j, b, &t)) {
-                                if (early) return 1;
-                                cnt++;
-                            }
-                        }
+                for_each_image(A, sep, [&](int mx, int my, int mz) {
+                    const d3 t = image_translation(s, mx, my, mz);
+                    if (!centre_overlap(s, pa, ha, ca, j, b, &t)) return false;
+                    cnt++;
+                    return early;
+                });
+                if (early && cnt) return 1;
             }
         }
         return cnt;
@@ -227,13 +246,11 @@ __device__ double candidate_energy(const SingleArgs &A, const double *p, const d
                 continue;
             }
             const float3 sep = separation32(pb, pa);
-            for (int mx = -1; mx <= 1; mx++)
-                for (int my = -1; my <= 1; my++)
-                    for (int mz = -1; mz <= 1; mz++) {
-                        if (!within_reach(A, sep, mx, my, mz)) continue;
-                        const d3 t = image_translation(s, mx, my, mz);
-                        e = dadd(e, soft_energy(s, norm2(sub3(add3(pb3, t), pa3))));
-                    }
+            for_each_image(A, sep, [&](int mx, int my, int mz) {
+                const d3 t = image_translation(s, mx, my, mz);
+                e = dadd(e, soft_energy(s, norm2(sub3(add3(pb3, t), pa3))));
+                return false;
+            });
         }
     }
     return e;
@@ -243,8 +260,13 @@ __device__ double candidate_energy(const SingleArgs &A, const double *p, const d
 // grid order, then the particles moved since the grid was built; -1 for one to skip.
 __device__ __forceinline__ int candidate_at(const SingleArgs &A, const Mover &mv, int which, int k, int in_cells) {
     if (k < in_cells) {
-        int c = 0;
-        while (mv.cstart[which][c + 1] <= k) c++;
+        // the last cell whose prefix is at most k (empty cells share their successor's prefix)
+        int c = 0, hi = mv.ncells[which] - 1;
+        while (c < hi) {
+            const int mid = (c + hi + 1) >> 1;
+            if (mv.cstart[which][mid] <= k) c = mid;
+            else hi = mid - 1;
+        }
         const int cell = mv.cells[which][c];
         const int j = A.g.slot_pid[A.g.start[cell] + (k - mv.cstart[which][c])];
         return (A.disp_flag && A.disp_flag[j]) ? -1 : j;  // moved since: tested from the list
@@ -306,11 +328,10 @@ __device__ int warp_overlaps_convex(const SingleArgs &A, const Mover &mv, int wh
                     else if (!(d2 > rc2)) near_e[nnear++] = j * 28 + 27;
                 } else {
                     const float3 sep = separation32(pjp, mv.pos[which]);
-                    for (int m = 0; m < 27; m++) {
-                        const int mx = m / 9 - 1, my = (m / 3) % 3 - 1, mz = m % 3 - 1;
-                        if (!within_reach(A, sep, mx, my, mz)) continue;
+                    for_each_image(A, sep, [&](int mx, int my, int mz) {
+                        const int m = (mx + 1) * 9 + (my + 1) * 3 + (mz + 1);
                         const double d2 = norm2(sub3(add3(pj, image_translation(s, mx, my, mz)), p));
-                        if (d2 > rc2) continue;
+                        if (d2 > rc2) return false;
                         if (d2 < ri2) {
                             certain++;
                         } else if (nnear < 4) {
@@ -324,7 +345,8 @@ __device__ int warp_overlaps_convex(const SingleArgs &A, const Mover &mv, int wh
                                                               1.0e-12, stuck) ? 1 : 0);
                             if (stuck) atomicOr(s.status, ST_PORTAL_STUCK);
                         }
-                    }
+                        return false;
+                    });
                 }
             }
         }
@@ -408,10 +430,10 @@ __device__ double warp_energy(const SingleArgs &A, const Mover &mv, int which, i
 }
 
 // Lane 0: the current state and the temp shape of move m of particle pid (core/Packing.cpp:86-93,
-// 113-116, 137-146), with their neighbour cells ([1] only when `both`), and the ActiveDomain
-// test of a translation (lo null: none; bounded[d] 0: dimension d unbounded).
+// 113-116, 137-146) and the ActiveDomain test of a translation (lo null: none; bounded[d] 0:
+// dimension d unbounded); mover_cells adds their neighbour cells.
 template <int KIND>
-__device__ void build_mover(const SingleArgs &A, Mover &mv, const rp_move &m, int pid, bool both, const double *lo,
+__device__ void build_mover(const SingleArgs &A, Mover &mv, const rp_move &m, int pid, const double *lo,
                             const double *hi, const int *bounded) {
     const DevState &s = A.s;
     const d3 p0 = load_d3(s.pos64 + 3 * (size_t)pid);
@@ -468,17 +490,48 @@ __device__ void build_mover(const SingleArgs &A, Mover &mv, const rp_move &m, in
             }
         }
     }
+}
+
+// The whole warp, after build_mover: the grid cells of the mover's states ([1] only when
+// `both`; lane w locates state w) and, lane q for neighbour q, their distinct neighbour cells
+// in neighbour_cells' order with the prefix of their occupancies.
+__device__ void mover_cells(const SingleArgs &A, Mover &mv, bool both) {
+    const int lane = threadIdx.x & 31;
+    const GridDev &g = A.g;
+    int cc[3] = {0, 0, 0};
+    if (lane < (both ? 2 : 1)) cell_of(A.s, g, d3{mv.pos[lane][0], mv.pos[lane][1], mv.pos[lane][2]}, cc);
+    const bool distinct = g.dims[0] >= 3 && g.dims[1] >= 3 && g.dims[2] >= 3;
     for (int w = 0; w < (both ? 2 : 1); w++) {
-        int c[3];
-        cell_of(s, A.g, d3{mv.pos[w][0], mv.pos[w][1], mv.pos[w][2]}, c);
-        mv.ncells[w] = neighbour_cells(A.g, c, mv.cells[w]);
-        int acc = 0;
-        for (int q = 0; q < mv.ncells[w]; q++) {
-            mv.cstart[w][q] = acc;
-            acc += A.g.start[mv.cells[w][q] + 1] - A.g.start[mv.cells[w][q]];
+        const int c0 = __shfl_sync(FULL, cc[0], w), c1 = __shfl_sync(FULL, cc[1], w), c2 = __shfl_sync(FULL, cc[2], w);
+        int nb = -1;
+        if (lane < 27)
+            nb = wrap_cell(c0 + lane % 3 - 1, g.dims[0]) +
+                 g.dims[0] * (wrap_cell(c1 + (lane / 3) % 3 - 1, g.dims[1]) +
+                              g.dims[1] * wrap_cell(c2 + lane / 9 - 1, g.dims[2]));
+        bool keep = lane < 27;
+        if (!distinct)  // a dimension of one or two cells: keep the first of equal cells
+            for (int q = 0; q < 27; q++) {
+                const int o = __shfl_sync(FULL, nb, q);
+                if (q < lane && o == nb) keep = false;
+            }
+        const unsigned bal = __ballot_sync(FULL, keep);
+        const int at = __popc(bal & ((1u << lane) - 1));
+        const int occ = keep ? g.start[nb + 1] - g.start[nb] : 0;
+        int incl = occ;
+        for (int d = 1; d < 32; d <<= 1) {
+            const int v = __shfl_up_sync(FULL, incl, d);
+            if (lane >= d) incl += v;
         }
-        mv.cstart[w][mv.ncells[w]] = acc;
+        if (keep) {
+            mv.cells[w][at] = nb;
+            mv.cstart[w][at] = incl - occ;
+        }
+        if (lane == 31) {
+            mv.ncells[w] = __popc(bal);
+            mv.cstart[w][__popc(bal)] = incl;
+        }
     }
+    __syncwarp();
 }
 
 // The move's energy (the whole warp, after build_mover): the ActiveDomain, then the hard part
@@ -511,9 +564,10 @@ __global__ void __launch_bounds__(32) k_try_single(SingleArgs A) {
     __shared__ Mover mv;
     const int pid = A.m.particle;
     if (threadIdx.x == 0)
-        build_mover<KIND>(A, mv, A.m, pid, A.s.counting || A.s.soft, A.has_domain ? A.dom_lo : nullptr,
-                          A.has_domain ? A.dom_hi : nullptr, nullptr);
+        build_mover<KIND>(A, mv, A.m, pid, A.has_domain ? A.dom_lo : nullptr, A.has_domain ? A.dom_hi : nullptr,
+                          nullptr);
     __syncwarp();
+    mover_cells(A, mv, A.s.counting || A.s.soft);
     int delta = 0;
     const double dE = move_energy<KIND>(A, mv, pid, delta);
     if (threadIdx.x == 0) {
@@ -638,9 +692,10 @@ __global__ void __launch_bounds__(SOFT_WARPS * 32, 4) k_soft_sweep(SoftSweepArgs
                     const double *R = A.rtab64 + 9 * (size_t)idx;
                     for (int q = 0; q < 9; q++) m.rotation[q] = inv ? R[3 * (q % 3) + q / 3] : R[q];
                 }
-                build_mover<KIND>(C, mv, m, pid, true, lo, hi, bounded);
+                build_mover<KIND>(C, mv, m, pid, lo, hi, bounded);
             }
             __syncwarp();
+            mover_cells(C, mv, true);
             int delta = 0;
             const double dE = move_energy<KIND>(C, mv, pid, delta);
             // Metropolis (core/Simulation.cpp:483): u <= exp(-dE / T)
