@@ -439,6 +439,9 @@ DevState dev_state(Handle *h) {
     s.soft_eps = h->soft_eps;
     s.soft_sigma = h->soft_sigma;
     s.soft_cut = h->soft_cut;
+    s.soft_cut2 = h->soft_cut * h->soft_cut;
+    s.soft_sigma2 = h->soft_sigma * h->soft_sigma;
+    s.soft_4eps = 4.0 * h->soft_eps;
     if (h->walls) {
         // Packing::countParticleWallOverlaps (core/Packing.cpp:1089-1101): the box sides
         // (TriclinicBox::getSides: box · e_i, accumulated from zero), the far corner as their

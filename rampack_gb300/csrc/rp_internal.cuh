@@ -137,6 +137,7 @@ struct DevState {
     // 1 RepulsiveLennardJonesInteraction, 2 SquareInverseCoreInteraction; soft_only: no hard part
     int soft, soft_only;
     double soft_eps, soft_sigma, soft_cut;   // soft_cut: sigma * std::pow(2., 1./6) (RepulsiveLennardJones)
+    double soft_cut2, soft_sigma2, soft_4eps; // cut * cut, sigma * sigma, 4 * eps (the same roundings)
 };
 
 constexpr int MAX_CEN = RP_MAX_CENTRES;

@@ -45,18 +45,22 @@ struct Mover {
     mutable int xq[XC_QUEUE];           // convex bodies: candidate * 28 + image of the near pairs
 };
 
-// Grid cell of an FP64 position: the rebuild's own arithmetic (assign_one).
+// Grid cell coordinate d of fractional coordinate r: the rebuild's own arithmetic (assign_one).
+__device__ __forceinline__ int cell_coord(const GridDev &g, int d, double r) {
+    double u = r - g.shift[d];
+    if (u < 0.0) u += 1.0;
+    int cd = static_cast<int>(u * g.dims[d]);
+    if (cd >= g.dims[d]) cd = g.dims[d] - 1;
+    if (cd < 0) cd = 0;
+    return cd;
+}
+
+// Grid cell of an FP64 position.
 __device__ int cell_of(const DevState &s, const GridDev &g, d3 p, int c[3]) {
     d3 r = mv3(s.inv, p);
-    double rr[3] = {r.x, r.y, r.z};
-    for (int d = 0; d < 3; d++) {
-        double u = rr[d] - g.shift[d];
-        if (u < 0.0) u += 1.0;
-        int cd = static_cast<int>(u * g.dims[d]);
-        if (cd >= g.dims[d]) cd = g.dims[d] - 1;
-        if (cd < 0) cd = 0;
-        c[d] = cd;
-    }
+    c[0] = cell_coord(g, 0, r.x);
+    c[1] = cell_coord(g, 1, r.y);
+    c[2] = cell_coord(g, 2, r.z);
     return c[0] + g.dims[0] * (c[1] + g.dims[1] * c[2]);
 }
 
@@ -81,16 +85,17 @@ __device__ int neighbour_cells(const GridDev &g, const int c[3], int *out) {
 
 // CentralInteraction::calculateEnergyForDistance2 of the soft part, in the reference's
 // operation order: RepulsiveLennardJonesInteraction.cpp:9-17, SquareInverseCoreInteraction.cpp:13-15.
+// (cut^2, sigma^2 and 4 eps are the host's products of the same operands, identical roundings).
 __device__ double soft_energy(const DevState &s, double d2) {
     if (s.soft == 1) {
-        if (d2 >= dmul(s.soft_cut, s.soft_cut)) return 0.0;
-        const double x2 = ddiv(dmul(s.soft_sigma, s.soft_sigma), d2);
+        if (d2 >= s.soft_cut2) return 0.0;
+        const double x2 = ddiv(s.soft_sigma2, d2);
         const double x6 = dmul(dmul(x2, x2), x2);
         const double x12 = dmul(x6, x6);
-        return dadd(dmul(dmul(4.0, s.soft_eps), dsub(x12, x6)), s.soft_eps);
+        return dadd(dmul(s.soft_4eps, dsub(x12, x6)), s.soft_eps);
     }
     if (s.soft == 2) {
-        const double v = dsub(ddiv(dmul(s.soft_sigma, s.soft_sigma), d2), 1.0);
+        const double v = dsub(ddiv(s.soft_sigma2, d2), 1.0);
         return dmul(s.soft_eps, 0.0 < v ? v : 0.0);  // std::max(0.0, v)
     }
     return 0.0;
@@ -245,10 +250,14 @@ __device__ double candidate_energy(const SingleArgs &A, const double *p, const d
                 e = dadd(e, soft_energy(s, pbc_distance2(s.box, s.inv, pa3, pb3)));
                 continue;
             }
-            const float3 sep = separation32(pb, pa);
+            // q - p in FP64: the pre-filter's separation, and the zero image's difference ((q + 0) - p
+            // is q - p up to the sign of a zero, which the squared norm drops)
+            const d3 dd = sub3(pb3, pa3);
+            const float3 sep = make_float3(static_cast<float>(dd.x), static_cast<float>(dd.y), static_cast<float>(dd.z));
             for_each_image(A, sep, [&](int mx, int my, int mz) {
-                const d3 t = image_translation(s, mx, my, mz);
-                e = dadd(e, soft_energy(s, norm2(sub3(add3(pb3, t), pa3))));
+                const double d2 = (mx | my | mz) ? norm2(sub3(add3(pb3, image_translation(s, mx, my, mz)), pa3))
+                                                 : norm2(dd);
+                e = dadd(e, soft_energy(s, d2));
                 return false;
             });
         }
@@ -429,80 +438,67 @@ __device__ double warp_energy(const SingleArgs &A, const Mover &mv, int which, i
     return e;
 }
 
-// Lane 0: the current state and the temp shape of move m of particle pid (core/Packing.cpp:86-93,
-// 113-116, 137-146) and the ActiveDomain test of a translation (lo null: none; bounded[d] 0:
-// dimension d unbounded); mover_cells adds their neighbour cells.
+// The whole warp: the current state and the temp shape of move m of particle pid
+// (core/Packing.cpp:86-93, 113-116, 137-146), the ActiveDomain test of a translation (lo null:
+// none; bounded[d] 0: dimension d unbounded), and the neighbour cells of the temp state and,
+// with `both`, of the current one.  Each coordinate's arithmetic is the serial restatement's
+// (Shape::translate with pbc_correction, mv3, cell_of, mm_elem), spread over lanes: lane i < 3
+// computes coordinate i of the temp position and its domain test, lane 3w + i coordinate i of
+// state w's cell, lane e < 9 element e of the rotated orientation, lane q < 27 neighbour q;
+// the values meet through shuffles.
 template <int KIND>
-__device__ void build_mover(const SingleArgs &A, Mover &mv, const rp_move &m, int pid, const double *lo,
-                            const double *hi, const int *bounded) {
+__device__ void build_mover(const SingleArgs &A, Mover &mv, const rp_move &m, int pid, bool both,
+                            const double *lo, const double *hi, const int *bounded) {
     const DevState &s = A.s;
-    const d3 p0 = load_d3(s.pos64 + 3 * (size_t)pid);
+    const GridDev &g = A.g;
+    const int lane = threadIdx.x & 31;
+    const int i = lane % 3;
+    const double *p0p = s.pos64 + 3 * (size_t)pid;
     const double *o0 = s.rot64 + 9 * (size_t)pid;
-    d3 p1 = p0;
-    if (m.type != RP_MOVE_ROTATION) {
+    const bool trans = m.type != RP_MOVE_ROTATION;
+    const d3 p0 = load_d3(p0p);
+    const double p0i = p0p[i];
+    double p1i = p0i;
+    if (trans) {
         // Shape::translate (core/Shape.cpp:9-12) with PeriodicBoundaryConditions::getCorrection
-        const d3 q = add3(p0, d3{m.translation[0], m.translation[1], m.translation[2]});
-        p1 = add3(q, pbc_correction(s.box, s.inv, q, nullptr));
+        // (pbc_correction), row i
+        const double qi = dadd(p0i, m.translation[i]);
+        const d3 q{__shfl_sync(FULL, qi, 0), __shfl_sync(FULL, qi, 1), __shfl_sync(FULL, qi, 2)};
+        const double r = mrow(s.inv, i, q);
+        double c = 0.0;
+        while (dadd(r, c) < 0.0) c = dadd(c, 1.0);
+        while (dadd(r, c) >= 1.0) c = dsub(c, 1.0);
+        const d3 cv{__shfl_sync(FULL, c, 0), __shfl_sync(FULL, c, 1), __shfl_sync(FULL, c, 2)};
+        p1i = dadd(qi, mrow(s.box, i, cv));
     }
-    double o1[9];
-    for (int e = 0; e < 9; e++) o1[e] = o0[e];
-    if (m.type != RP_MOVE_TRANSLATION)  // Shape::rotate: R * O (core/Shape.cpp:14-16)
-        for (int i = 0; i < 3; i++)
-            for (int j = 0; j < 3; j++) o1[3 * i + j] = mm_elem(m.rotation, o0, i, j);
-    mv.pos[0][0] = p1.x, mv.pos[0][1] = p1.y, mv.pos[0][2] = p1.z;
-    mv.pos[1][0] = p0.x, mv.pos[1][1] = p0.y, mv.pos[1][2] = p0.z;
-    for (int e = 0; e < 9; e++) {
-        mv.rot[0][e] = o1[e];
-        mv.rot[1][e] = o0[e];
-    }
-    if (KIND == 2) {
-        for (int a = 0; a < s.ncen; a++) {
-            // the temp centres, rotated by R (core/Packing.cpp:357-361), and the absolute
-            // centres: position + centre with the periodic correction (:1041-1047)
-            d3 c = load_d3(s.cen64 + 3 * ((size_t)pid * s.ncen + a));
-            if (m.type != RP_MOVE_TRANSLATION) c = mv3(m.rotation, c);
-            const d3 q = add3(p1, c);
-            const d3 ab = add3(q, pbc_correction(s.box, s.inv, q, nullptr));
-            mv.cen[3 * a] = c.x, mv.cen[3 * a + 1] = c.y, mv.cen[3 * a + 2] = c.z;
-            mv.abs[0][3 * a] = ab.x, mv.abs[0][3 * a + 1] = ab.y, mv.abs[0][3 * a + 2] = ab.z;
-            for (int d = 0; d < 3; d++) mv.abs[1][3 * a + d] = s.abs64[3 * ((size_t)pid * s.ncen + a) + d];
-            if (s.segs) {
-                // orientation * half axis (PolyspherocylinderTraits.cpp:118-119)
-                const d3 hb{s.chax[a][0], s.chax[a][1], s.chax[a][2]};
-                const d3 h1 = mv3(o1, hb), h0 = mv3(o0, hb);
-                mv.hax[0][3 * a] = h1.x, mv.hax[0][3 * a + 1] = h1.y, mv.hax[0][3 * a + 2] = h1.z;
-                mv.hax[1][3 * a] = h0.x, mv.hax[1][3 * a + 1] = h0.y, mv.hax[1][3 * a + 2] = h0.z;
-            }
-        }
-    }
+    const d3 p1{__shfl_sync(FULL, p1i, 0), __shfl_sync(FULL, p1i, 1), __shfl_sync(FULL, p1i, 2)};
+    // fractional coordinate i of the temp position (lanes 0-2) or of the current one (3-5)
+    const double ri = mrow(s.inv, i, lane < 3 ? p1 : p0);
     // the ActiveDomain of a translation or rototranslation, tested before any overlap
     // (core/Packing.cpp:94-96, :141-143; ActiveDomain::isInside, core/ActiveDomain.cpp:8-21)
-    mv.outside = 0;
-    if (lo && m.type != RP_MOVE_ROTATION) {
-        const d3 rel = mv3(s.inv, p1);
-        const double r[3] = {rel.x, rel.y, rel.z};
-        for (int d = 0; d < 3; d++) {
-            if (bounded && !bounded[d]) continue;
-            if (hi[d] > lo[d]) {
-                if (r[d] <= lo[d] || r[d] >= hi[d]) mv.outside = 1;
-            } else if (r[d] <= lo[d] && r[d] >= hi[d]) {
-                mv.outside = 1;
-            }
-        }
+    bool out = false;
+    if (lo && trans && lane < 3 && !(bounded && !bounded[i])) {
+        if (hi[i] > lo[i]) out = ri <= lo[i] || ri >= hi[i];
+        else out = ri <= lo[i] && ri >= hi[i];
     }
-}
-
-// The whole warp, after build_mover: the grid cells of the mover's states ([1] only when
-// `both`; lane w locates state w) and, lane q for neighbour q, their distinct neighbour cells
-// in neighbour_cells' order with the prefix of their occupancies.
-__device__ void mover_cells(const SingleArgs &A, Mover &mv, bool both) {
-    const int lane = threadIdx.x & 31;
-    const GridDev &g = A.g;
-    int cc[3] = {0, 0, 0};
-    if (lane < (both ? 2 : 1)) cell_of(A.s, g, d3{mv.pos[lane][0], mv.pos[lane][1], mv.pos[lane][2]}, cc);
+    const int outside = __any_sync(FULL, out) ? 1 : 0;
+    if (lane < 3) {
+        mv.pos[0][lane] = p1i;
+        mv.pos[1][lane] = p0i;
+    }
+    if (lane < 9) {  // Shape::rotate: R * O (core/Shape.cpp:14-16)
+        const double o0e = o0[lane];
+        mv.rot[0][lane] = m.type != RP_MOVE_TRANSLATION ? mm_elem(m.rotation, o0, lane / 3, lane % 3) : o0e;
+        mv.rot[1][lane] = o0e;
+    }
+    if (lane == 0) mv.outside = outside;
+    const int cdi = cell_coord(g, i, ri);
     const bool distinct = g.dims[0] >= 3 && g.dims[1] >= 3 && g.dims[2] >= 3;
     for (int w = 0; w < (both ? 2 : 1); w++) {
-        const int c0 = __shfl_sync(FULL, cc[0], w), c1 = __shfl_sync(FULL, cc[1], w), c2 = __shfl_sync(FULL, cc[2], w);
+        // the distinct cells among the 27 around state w's cell, in neighbour_cells' order, and
+        // the prefix of their occupancies
+        const int c0 = __shfl_sync(FULL, cdi, 3 * w), c1 = __shfl_sync(FULL, cdi, 3 * w + 1),
+                  c2 = __shfl_sync(FULL, cdi, 3 * w + 2);
         int nb = -1;
         if (lane < 27)
             nb = wrap_cell(c0 + lane % 3 - 1, g.dims[0]) +
@@ -529,6 +525,28 @@ __device__ void mover_cells(const SingleArgs &A, Mover &mv, bool both) {
         if (lane == 31) {
             mv.ncells[w] = __popc(bal);
             mv.cstart[w][__popc(bal)] = incl;
+        }
+    }
+    __syncwarp();
+    if (KIND == 2 && lane == 0) {
+        const double *o1 = mv.rot[0];
+        for (int a = 0; a < s.ncen; a++) {
+            // the temp centres, rotated by R (core/Packing.cpp:357-361), and the absolute
+            // centres: position + centre with the periodic correction (:1041-1047)
+            d3 c = load_d3(s.cen64 + 3 * ((size_t)pid * s.ncen + a));
+            if (m.type != RP_MOVE_TRANSLATION) c = mv3(m.rotation, c);
+            const d3 q = add3(p1, c);
+            const d3 ab = add3(q, pbc_correction(s.box, s.inv, q, nullptr));
+            mv.cen[3 * a] = c.x, mv.cen[3 * a + 1] = c.y, mv.cen[3 * a + 2] = c.z;
+            mv.abs[0][3 * a] = ab.x, mv.abs[0][3 * a + 1] = ab.y, mv.abs[0][3 * a + 2] = ab.z;
+            for (int d = 0; d < 3; d++) mv.abs[1][3 * a + d] = s.abs64[3 * ((size_t)pid * s.ncen + a) + d];
+            if (s.segs) {
+                // orientation * half axis (PolyspherocylinderTraits.cpp:118-119)
+                const d3 hb{s.chax[a][0], s.chax[a][1], s.chax[a][2]};
+                const d3 h1 = mv3(o1, hb), h0 = mv3(o0, hb);
+                mv.hax[0][3 * a] = h1.x, mv.hax[0][3 * a + 1] = h1.y, mv.hax[0][3 * a + 2] = h1.z;
+                mv.hax[1][3 * a] = h0.x, mv.hax[1][3 * a + 1] = h0.y, mv.hax[1][3 * a + 2] = h0.z;
+            }
         }
     }
     __syncwarp();
@@ -563,11 +581,8 @@ template <int KIND>
 __global__ void __launch_bounds__(32) k_try_single(SingleArgs A) {
     __shared__ Mover mv;
     const int pid = A.m.particle;
-    if (threadIdx.x == 0)
-        build_mover<KIND>(A, mv, A.m, pid, A.has_domain ? A.dom_lo : nullptr, A.has_domain ? A.dom_hi : nullptr,
-                          nullptr);
-    __syncwarp();
-    mover_cells(A, mv, A.s.counting || A.s.soft);
+    build_mover<KIND>(A, mv, A.m, pid, A.s.counting || A.s.soft, A.has_domain ? A.dom_lo : nullptr,
+                      A.has_domain ? A.dom_hi : nullptr, nullptr);
     int delta = 0;
     const double dE = move_energy<KIND>(A, mv, pid, delta);
     if (threadIdx.x == 0) {
@@ -612,6 +627,23 @@ __global__ void k_commit_single(DevState s, SingleTry *t, uint8_t *disp_flag, in
 }
 
 // ---- soft sweeps ----------------------------------------------------------------------
+
+// Metropolis acceptance u <= exp(-dE / T) (core/Simulation.cpp:483) for the sweep's own
+// uniforms (multiples of 2^-53 in [0, 1)) and T > 0, without the FP64 exponential where the
+// answer is certain: dE <= 0 accepts (exp >= 1 > u); an exponent below -80 accepts only u = 0
+// (exp < 2e-35 below the smallest positive u); otherwise CUDA's FP32 expf decides wherever u
+// lies more than 1e-4 (relative) away from it, far beyond the FP32 errors of the exponent
+// (< 5e-6 relative at |x| <= 80), of expf (a few ulp) and of u; the band in between, and a NaN,
+// take the FP64 exponential.  The decision is that of the FP64 test in every case.
+__device__ __forceinline__ bool metropolis(double u, double dE, double T) {
+    if (dE <= 0.0) return true;
+    const double x = T == 1.0 ? -dE : -dE / T;   // a division by one is exact
+    if (x < -80.0) return u == 0.0;
+    const float ef = expf(static_cast<float>(x)), uf = static_cast<float>(u);
+    if (uf <= ef * (1.0f - 1e-4f)) return true;
+    if (uf >= ef * (1.0f + 1e-4f)) return false;
+    return u <= exp(x);
+}
 
 // The Metropolis uniform of move mi of a cell: 53 bits of a Philox draw apart from the
 // proposal's words.
@@ -692,14 +724,13 @@ __global__ void __launch_bounds__(SOFT_WARPS * 32, 4) k_soft_sweep(SoftSweepArgs
                     const double *R = A.rtab64 + 9 * (size_t)idx;
                     for (int q = 0; q < 9; q++) m.rotation[q] = inv ? R[3 * (q % 3) + q / 3] : R[q];
                 }
-                build_mover<KIND>(C, mv, m, pid, lo, hi, bounded);
             }
             __syncwarp();
-            mover_cells(C, mv, true);
+            build_mover<KIND>(C, mv, m, pid, true, lo, hi, bounded);
             int delta = 0;
             const double dE = move_energy<KIND>(C, mv, pid, delta);
             // Metropolis (core/Simulation.cpp:483): u <= exp(-dE / T)
-            const bool acc = uni <= exp(-dE / C.temperature);
+            const bool acc = metropolis(uni, dE, C.temperature);
             const uint8_t code = mv.outside ? 2 : (dE == CUDART_INF ? 1 : (dE == -CUDART_INF ? 3 : 0));
             if (acc && lane == 0) {
                 // Packing::acceptMove (core/Packing.cpp:278-302)
