@@ -57,6 +57,9 @@ def parse():
                     help="sc-1e6: the headline system; the others are further systems of the same path")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--bulk-staging", type=int, default=-1, choices=[-1, 0, 1],
+                    help="stage neighbourhoods with bulk asynchronous copies (1) or per-lane loads (0); "
+                         "-1: the engine's default")
     ap.add_argument("--cells-per-warp", type=int, default=0, choices=[0, 1, 2],
                     help="plain sweeps: 1 = a warp per cell, 2 = a cell per half-warp (0: the library default)")
     ap.add_argument("--no-ordering", action="store_true",
@@ -392,6 +395,8 @@ def main_gpu(args):
         g.set_soft(*EXTRA[args.workload]["soft"])
     if args.cells_per_warp:
         g.set_cells_per_warp(args.cells_per_warp)
+    if args.bulk_staging >= 0:
+        g.set_bulk_staging(args.bulk_staging == 1)
     g.box = np.array(box, dtype=np.float64)
     stream = torch.cuda.ExternalStream(g.stream(), device=local)
     seed = args.seed + 7919 * rank

@@ -503,6 +503,12 @@ int rp_get_cells_per_warp(void *handle, int32_t *last);
  * staged; decisions are unchanged.  0 off, 1 (default) where cells are well above the range
  * (keeps < 90 % of the neighbourhood), 2 wherever no grid dimension has a single cell. */
 int rp_set_staging_filter(void *handle, int32_t mode);
+/* How a sweep stages each cell's 3x3x3 neighbourhood into shared memory: 1 with bulk
+ * asynchronous copies (cp.async.bulk, one per neighbour cell and array, completing on an
+ * mbarrier with a bounded wait), 0 with per-lane loads.  Decisions, states and the proposal
+ * stream are the same either way; the two-cells-per-warp path and the staging filter always
+ * use per-lane loads.  A lost copy sets a device status (RP_ERR_DEVICE) instead of waiting. */
+int rp_set_bulk_staging(void *handle, int32_t on);
 
 /* ---- the Monte Carlo cycle loop (Simulation for hard bodies) -----------------------
  *

@@ -221,6 +221,7 @@ struct Handle {
     double ref_range = 0;
     double *cen64 = nullptr;
     int stage_mode = 1;  // staging filter: 0 off, 1 where it pays (cells well above the range), 2 wherever valid
+    int bulk_stage = 0;  // stage neighbourhoods with bulk asynchronous copies
     bool grid_stale = false;  // an upload validated the state; the cell grid is built when first needed
     bool stale_unshifted = false;  // ... and it is built unshifted (not with the last grid's origin)
     uint64_t grid_rebuilds = 0;    // full cell-grid rebuilds (Packing::getNeighbourGridRebuilds)
@@ -704,10 +705,11 @@ int check_status(Handle *h) {
     if (st) {
         RP_CUDA(h, cudaMemsetAsync(h->status, 0, sizeof(uint32_t), h->stream));
         char buf[256];
-        std::snprintf(buf, sizeof(buf), "device status 0x%x%s%s%s", st,
+        std::snprintf(buf, sizeof(buf), "device status 0x%x%s%s%s%s", st,
                       (st & ST_PARTICLE_NOT_IN_CELL) ? " (a move's particle is not in its cell)" : "",
                       (st & ST_CAPACITY) ? " (a cell neighbourhood exceeds the staging capacity)" : "",
-                      (st & ST_PORTAL_STUCK) ? " (a convex pair's portal refinement did not converge)" : "");
+                      (st & ST_PORTAL_STUCK) ? " (a convex pair's portal refinement did not converge)" : "",
+                      (st & ST_STAGE_TIMEOUT) ? " (a staging copy did not complete in time)" : "");
         if (st & ST_OUTSIDE) return fail(h, RP_ERR_ARG, "a particle lies outside the box");
         if (st & ST_NOT_ROTATION)
             return fail(h, RP_ERR_ARG, "an orientation is not a rotation matrix (|O^T O - I| >= 1e-6)");
@@ -761,6 +763,7 @@ SweepArgs base_args(Handle *h) {
     // sphere distances of a sheared box without the reference's grid are not geometric:
     // no FP32 certificate, every pair in FP64
     a.fp64_only = (a.s.pbc_fold == 2 && a.s.kind != 1) ? 1 : 0;
+    a.bulk_stage = h->bulk_stage;
     a.overflow = h->overflow;
     a.overflow_count = h->overflow_count;
     return a;
@@ -2485,6 +2488,13 @@ int rp_set_staging_filter(void *handle, int32_t mode) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h || mode < 0 || mode > 2) return fail(h, RP_ERR_ARG, "bad argument");
     h->stage_mode = mode;
+    return RP_OK;
+}
+
+int rp_set_bulk_staging(void *handle, int32_t on) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || (on != 0 && on != 1)) return fail(h, RP_ERR_ARG, "bulk staging must be 0 or 1");
+    h->bulk_stage = on;
     return RP_OK;
 }
 

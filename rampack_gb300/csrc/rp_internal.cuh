@@ -22,6 +22,7 @@ enum : uint32_t {
     ST_OUTSIDE = 1u << 4,               // a particle lies outside the box
     ST_NOT_ROTATION = 1u << 5,          // an uploaded orientation is not a rotation (1e-6)
     ST_PORTAL_STUCK = 1u << 6,          // a convex pair's portal refinement hit its iteration limit
+    ST_STAGE_TIMEOUT = 1u << 7,         // a bulk staging copy did not complete within its wait limit
 };
 
 // Constants of the FP32 filter: every comparison of the FP64 reference is decided in
@@ -220,6 +221,7 @@ struct SweepArgs {
     rp_move *log;                  // [ntypes * n] indexed by ntypes * start[cell] + k
     uint8_t *log_codes;
     int fp64_only;
+    int bulk_stage;                // stage neighbourhoods with bulk asynchronous copies (one per cell and array)
     // overflow: cells whose neighbourhood exceeds cap are appended here and rerun
     int32_t *overflow;             // [ncell]
     int32_t *overflow_count;

@@ -237,6 +237,18 @@ __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(co
     float4 *wx = reinterpret_cast<float4 *>(nacc + A.cap) + (LEARN ? A.cap / 4 : 0);
     int nitems = A.work ? *A.work_count : (LIST ? A.num_list : A.num_active);
     WarpStats ws{};
+    __shared__ uint64_t stage_bar[SWEEP_WARPS];
+    if (GW == 32 && A.bulk_stage) {
+        // the group's staging barrier: one arrival (lane 0's expected bytes) per phase
+        uint64_t *bar = stage_bar + gib;
+        if (lane == 0) {
+            mbar_init(bar, 1);
+            fence_mbar_init();
+            fence_proxy_async_smem();
+        }
+        grp.sync();
+        ws.bar = bar;
+    }
     // persistent launches (next_item set) take cells from a shared counter until none are
     // left; otherwise groups stride over the cells
     const int stride = gridDim.x * groups_per_block;
@@ -251,6 +263,7 @@ __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(co
         sweep_cell<KIND, LIST, MODE, GW>(A, item, -1, A.cap, A.overflow, A.overflow_count, cpos, cax, qseg, qun, nacc,
                                           pstage, cslot, wx, ws);
         grp.sync();
+        if (ws.abort) break;
         item += stride;
     }
     // ---- statistics ----

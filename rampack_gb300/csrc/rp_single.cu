@@ -55,15 +55,6 @@ __device__ __forceinline__ int cell_coord(const GridDev &g, int d, double r) {
     return cd;
 }
 
-// Grid cell of an FP64 position.
-__device__ int cell_of(const DevState &s, const GridDev &g, d3 p, int c[3]) {
-    d3 r = mv3(s.inv, p);
-    c[0] = cell_coord(g, 0, r.x);
-    c[1] = cell_coord(g, 1, r.y);
-    c[2] = cell_coord(g, 2, r.z);
-    return c[0] + g.dims[0] * (c[1] + g.dims[1] * c[2]);
-}
-
 // The distinct cells among the 27 around cell coordinates c (a grid dimension of one or two
 // cells names the same cell several times; its particles are listed once and tested at every
 // image within reach instead).
@@ -442,7 +433,7 @@ __device__ double warp_energy(const SingleArgs &A, const Mover &mv, int which, i
 // (core/Packing.cpp:86-93, 113-116, 137-146), the ActiveDomain test of a translation (lo null:
 // none; bounded[d] 0: dimension d unbounded), and the neighbour cells of the temp state and,
 // with `both`, of the current one.  Each coordinate's arithmetic is the serial restatement's
-// (Shape::translate with pbc_correction, mv3, cell_of, mm_elem), spread over lanes: lane i < 3
+// (Shape::translate with pbc_correction, mv3, cell_coord, mm_elem), spread over lanes: lane i < 3
 // computes coordinate i of the temp position and its domain test, lane 3w + i coordinate i of
 // state w's cell, lane e < 9 element e of the rotated orientation, lane q < 27 neighbour q;
 // the values meet through shuffles.

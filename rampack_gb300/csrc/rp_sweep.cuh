@@ -5,6 +5,7 @@
 
 #include <cuda_runtime.h>
 
+#include "rp_bulk.cuh"
 #include "rp_internal.cuh"
 
 namespace rp {
@@ -249,7 +250,15 @@ __device__ __forceinline__ bool exact_centre_pair(const DevState &s, d3 pa, int 
 // ---------------------------------------------------------------------------------
 struct WarpStats {
     unsigned moves, accepted, rej_overlap, rej_domain, pairs, fp64, trans, rots, acc_trans;
+    // bulk staging (whole warps): the group's barrier (null: per-lane loads), the parity of
+    // its next phase, and whether a copy timed out (the group then stops)
+    uint64_t *bar;
+    unsigned bphase;
+    int abort;
 };
+
+// Polls of a staging barrier before its copies count as lost (~0.1 s).
+constexpr int STAGE_WAIT_LIMIT = 1 << 21;
 
 // MODE 0: plain sweep; 1: learned-ordering pre-test and pair log; 2: overlap counting
 // (Packing::toggleOverlapCounting, core/Packing.cpp:304-323: the move's energy is the sign of
@@ -351,8 +360,42 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
         }
         return;
     }
+    const bool bulk = GW == 32 && !filt && ws.bar != nullptr;
+    if (bulk) {
+        // bulk staging: one copy per neighbour cell and array (a cell is a contiguous run of
+        // the slot-ordered mirror; float4 records, so addresses and sizes are multiples of
+        // 16 bytes), all in flight at once on the group's barrier; then each lane shifts its
+        // cell's staged positions into the home cell's frame, as the per-lane copy does
+        constexpr bool WITH_AX = KIND == 1 && !AXM;
+        fence_proxy_async_smem();  // this lane's reads and writes of the buffers come first
+        grp.sync();
+        if (lane == 0) mbar_arrive_expect_tx(ws.bar, (uint32_t)total * (WITH_AX ? 32u : 16u));
+        grp.sync();
+        if (lane < 27 && cnt[0] > 0) {
+            bulk_g2s(cpos + pre[0], G.mpos + st[0], (uint32_t)cnt[0] * 16u, ws.bar);
+            if (WITH_AX) bulk_g2s(cax + pre[0], G.maxis + st[0], (uint32_t)cnt[0] * 16u, ws.bar);
+        }
+        if (KIND == 2 || AXM)
+            for (int k = 0; k < cnt[0]; k++) cslot[pre[0] + k] = (uint32_t)(st[0] + k);
+        const bool landed = mbar_wait(ws.bar, ws.bphase, STAGE_WAIT_LIMIT);
+        if (grp.ballot(!landed)) {
+            // lost copies: flag, give those in flight a last bounded wait, stop the group
+            if (lane == 0) atomicOr(S.status, ST_STAGE_TIMEOUT);
+            mbar_wait(ws.bar, ws.bphase, STAGE_WAIT_LIMIT);
+            ws.abort = 1;
+            return;
+        }
+        ws.bphase ^= 1u;
+        if (lane < 27)
+            for (int k = 0; k < cnt[0]; k++) {
+                float4 &p = cpos[pre[0] + k];
+                p.x += off[0].x;
+                p.y += off[0].y;
+                p.z += off[0].z;
+            }
+    }
 #pragma unroll
-    for (int r = 0; r < NR; r++) {
+    for (int r = 0; r < NR && !bulk; r++) {
         const int nbl = lane + GW * r;
         if (!filt) {
             // every neighbour staged: positions known from the prefix sum (loads pipeline freely)

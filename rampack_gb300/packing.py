@@ -240,6 +240,11 @@ class GpuPacking:
         self._check(self.lib.rp_total_energy(self.h, C.byref(e)))
         return float(e.value)
 
+    def set_bulk_staging(self, on: bool):
+        """Stage sweep neighbourhoods with bulk asynchronous copies (1) or per-lane loads (0)
+        (rp_set_bulk_staging)."""
+        self._check(self.lib.rp_set_bulk_staging(self.h, 1 if on else 0))
+
     def set_cells_per_warp(self, cells: int):
         """1: a warp sweeps one cell; 2: each half-warp sweeps its own (rp_set_cells_per_warp)."""
         self._check(self.lib.rp_set_cells_per_warp(self.h, int(cells)))
