@@ -473,11 +473,42 @@ RP_XC_FN bool xcf_support(const XcShape &s, f3v n, f3v &out) {
     }
 }
 
+// FP32 support point of a flat body (a primitive, or one operation over primitives) without a
+// stack, entry by entry as xcf_support.
+RP_XC_FN f3v xcf_support_flat(const XcShape &s, f3v n) {
+    const XcNodeF &g = s.fnode[s.root];
+    if (g.type < XC_SUM) return xcf_primitive(g, n);
+    f3v acc{0.f, 0.f, 0.f};
+    float best = 0.f;
+    for (int i = 0; i < g.nent; i++) {
+        const f3v dir = (g.type == XC_DIFF && i == 1) ? fneg(n) : n;
+        const f3v r = xcf_primitive(s.fnode[g.ent[i]], fmtv(g.erot[i], dir));
+        const f3v w = fadd(fmv(g.erot[i], r), f3v{g.epos[i][0], g.epos[i][1], g.epos[i][2]});
+        if (g.type == XC_SUM) {
+            acc = fadd(acc, w);
+        } else if (g.type == XC_MAX) {
+            const float proj = fdot(w, n);
+            if (i == 0 || proj > best) {
+                acc = w;
+                best = proj;
+            }
+        } else {
+            acc = i == 0 ? w : fsub(acc, w);
+        }
+    }
+    return acc;
+}
+
 // Support point of body2 - body1 along n (FP32); body 1 at the origin.
 RP_HD bool xcf_diff(const XcShape &s, const float *r1, const float *r2, f3v p2, f3v n, f3v &v) {
     f3v a, b;
-    if (!xcf_support(s, fmtv(r2, n), a)) return false;
-    if (!xcf_support(s, fmtv(r1, fneg(n)), b)) return false;
+    if (s.flat) {
+        a = xcf_support_flat(s, fmtv(r2, n));
+        b = xcf_support_flat(s, fmtv(r1, fneg(n)));
+    } else {
+        if (!xcf_support(s, fmtv(r2, n), a)) return false;
+        if (!xcf_support(s, fmtv(r1, fneg(n)), b)) return false;
+    }
     v = fsub(fadd(fmv(r2, a), p2), fmv(r1, b));
     return true;
 }
