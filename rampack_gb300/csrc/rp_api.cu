@@ -409,6 +409,11 @@ DevState dev_state(Handle *h) {
     s.xc = h->d_xc;
     std::memcpy(s.box, h->box, sizeof(s.box));
     std::memcpy(s.inv, h->inv, sizeof(s.inv));
+    for (int i = 0; i < 3; i++) {
+        double z = 0.0;
+        for (int j = 0; j < 3; j++) z = z + h->box[3 * i + j] * 0.0;
+        s.box_zero[i] = z;
+    }
     for (int i = 0; i < 9; i++) s.inv32[i] = static_cast<float>(h->inv[i]);
     s.pos64 = h->pos64[h->pcur];
     s.rot64 = h->rot64;

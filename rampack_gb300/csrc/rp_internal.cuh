@@ -86,6 +86,7 @@ struct DevState {
     int kind;
     const XcShape *xc;    // generic convex bodies (kind 3): the body's geometry, device memory
     double box[9], inv[9];
+    double box_zero[3];   // box * (0, 0, 0) row by row (Matrix * Vector from zero): a no-wrap correction
     double *pos64;        // [n][3]
     double *rot64;        // [n][9]
     double *trans;        // [125][3] box · m for m in {-2..2}^3

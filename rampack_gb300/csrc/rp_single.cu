@@ -449,22 +449,34 @@ __device__ void build_mover(const SingleArgs &A, Mover &mv, const rp_move &m, in
     const bool trans = m.type != RP_MOVE_ROTATION;
     const d3 p0 = load_d3(p0p);
     const double p0i = p0p[i];
-    double p1i = p0i;
+    // Shape::translate (core/Shape.cpp:9-12): q = p0 + t on lanes 0-2 (p0 for a rotation)
+    const double qi = trans ? dadd(p0i, m.translation[i]) : p0i;
+    const d3 q{__shfl_sync(FULL, qi, 0), __shfl_sync(FULL, qi, 1), __shfl_sync(FULL, qi, 2)};
+    // fractional coordinate i of q (lanes 0-2) and of the current position (lanes 3-5)
+    double ri = mrow(s.inv, i, lane < 3 ? q : p0);
+    double p1i = qi;
     if (trans) {
-        // Shape::translate (core/Shape.cpp:9-12) with PeriodicBoundaryConditions::getCorrection
-        // (pbc_correction), row i
-        const double qi = dadd(p0i, m.translation[i]);
-        const d3 q{__shfl_sync(FULL, qi, 0), __shfl_sync(FULL, qi, 1), __shfl_sync(FULL, qi, 2)};
-        const double r = mrow(s.inv, i, q);
+        // PeriodicBoundaryConditions::getCorrection (pbc_correction) row i: the wrap count c
+        // from q's fractional coordinate, then q + box * c
         double c = 0.0;
-        while (dadd(r, c) < 0.0) c = dadd(c, 1.0);
-        while (dadd(r, c) >= 1.0) c = dsub(c, 1.0);
-        const d3 cv{__shfl_sync(FULL, c, 0), __shfl_sync(FULL, c, 1), __shfl_sync(FULL, c, 2)};
-        p1i = dadd(qi, mrow(s.box, i, cv));
+        if (lane < 3) {
+            while (dadd(ri, c) < 0.0) c = dadd(c, 1.0);
+            while (dadd(ri, c) >= 1.0) c = dsub(c, 1.0);
+        }
+        if (__any_sync(FULL, c != 0.0)) {
+            const d3 cv{__shfl_sync(FULL, c, 0), __shfl_sync(FULL, c, 1), __shfl_sync(FULL, c, 2)};
+            p1i = dadd(qi, mrow(s.box, i, cv));
+        } else {
+            p1i = dadd(qi, s.box_zero[i]);  // box * (0, 0, 0), the same products and sums
+        }
+        // the temp position's fractional coordinate is q's unless the correction changed q
+        const bool changed = lane < 3 && __double_as_longlong(p1i) != __double_as_longlong(qi);
+        if (__any_sync(FULL, changed)) {
+            const d3 p1v{__shfl_sync(FULL, p1i, 0), __shfl_sync(FULL, p1i, 1), __shfl_sync(FULL, p1i, 2)};
+            ri = mrow(s.inv, i, lane < 3 ? p1v : p0);
+        }
     }
     const d3 p1{__shfl_sync(FULL, p1i, 0), __shfl_sync(FULL, p1i, 1), __shfl_sync(FULL, p1i, 2)};
-    // fractional coordinate i of the temp position (lanes 0-2) or of the current one (3-5)
-    const double ri = mrow(s.inv, i, lane < 3 ? p1 : p0);
     // the ActiveDomain of a translation or rototranslation, tested before any overlap
     // (core/Packing.cpp:94-96, :141-143; ActiveDomain::isInside, core/ActiveDomain.cpp:8-21)
     bool out = false;
@@ -641,7 +653,9 @@ __device__ __forceinline__ bool metropolis(double u, double dE, double T) {
 __device__ double soft_uniform(const SoftSweepArgs &A, int cell, int mi) {
     const u4 q = philox(u4{(uint32_t)mi, (uint32_t)cell, (uint32_t)A.counter, (uint32_t)(A.counter >> 32) ^ 0x2545f491u},
                         (uint32_t)A.seed ^ 0x9e3779b9u, (uint32_t)(A.seed >> 32));
-    return (static_cast<double>(q.a >> 5) * 67108864.0 + static_cast<double>(q.b >> 6)) * (1.0 / 9007199254740992.0);
+    // (a >> 5) * 2^26 + (b >> 6) is an integer below 2^53: formed exactly as one, then scaled
+    const uint64_t k = (static_cast<uint64_t>(q.a >> 5) << 26) | static_cast<uint64_t>(q.b >> 6);
+    return static_cast<double>(k) * (1.0 / 9007199254740992.0);
 }
 
 template <int KIND>
