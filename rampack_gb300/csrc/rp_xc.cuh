@@ -175,6 +175,7 @@ RP_XC_FN d3 xc_support_flat(const XcShape &s, d3 n) {
     if (g.type < XC_SUM) return xc_primitive_support(g, n);
     d3 acc{0.0, 0.0, 0.0};
     double best = 0.0;
+    #pragma unroll 1
     for (int i = 0; i < g.nent; i++) {
         const d3 dir = (g.type == XC_DIFF && i == 1) ? neg3(n) : n;
         const d3 r = xc_primitive_support(s.node[g.ent[i]], mtv3(g.erot[i], dir));
@@ -480,6 +481,7 @@ RP_XC_FN f3v xcf_support_flat(const XcShape &s, f3v n) {
     if (g.type < XC_SUM) return xcf_primitive(g, n);
     f3v acc{0.f, 0.f, 0.f};
     float best = 0.f;
+    #pragma unroll 1
     for (int i = 0; i < g.nent; i++) {
         const f3v dir = (g.type == XC_DIFF && i == 1) ? fneg(n) : n;
         const f3v r = xcf_primitive(s.fnode[g.ent[i]], fmtv(g.erot[i], dir));
@@ -547,6 +549,7 @@ RP_XC_FN int xcf_refine(const XcShape &s, const float *r1, const float *r2, f3v 
         d[1] = td;
         n = fneg(n);
     }
+    #pragma unroll 1
     for (int it = 0; it < 64; it++) {
         if (!xcf_diff(s, r1, r2, p2, n, v3)) return -1;
         const f3v d3 = n;
@@ -567,6 +570,7 @@ RP_XC_FN int xcf_refine(const XcShape &s, const float *r1, const float *r2, f3v 
             continue;
         }
         d[2] = d3;
+        #pragma unroll 1
         for (int jt = 0; jt < 64; jt++) {
             n = fcross(fsub(v2, v1), fsub(v3, v1));
             if (fdot(n, v1) >= 0) return 1;
@@ -658,6 +662,7 @@ RP_XC_FN bool xc_diff_support_cert(const XcShape &s, const double *rot1, d3 pos1
     if (!s.flat) return xc_diff_support(s, rot1, pos1, rot2, pos2, n, v);
     const XcNode &g = s.node[s.root];
     d3 side[2];
+    #pragma unroll 1
     for (int b = 0; b < 2; b++) {
         const double *rot = b == 0 ? rot2 : rot1;
         const d3 dir = b == 0 ? n : d3{-n.x, -n.y, -n.z};
@@ -668,6 +673,7 @@ RP_XC_FN bool xc_diff_support_cert(const XcShape &s, const double *rot1, d3 pos1
             acc = xc_primitive_cert(g, ln);
         } else {
             double best = 0.0;
+            #pragma unroll 1
             for (int i = 0; i < g.nent; i++) {
                 const double *er = g.erot[i];
                 const d3 d = (g.type == XC_DIFF && i == 1) ? d3{-ln.x, -ln.y, -ln.z} : ln;
@@ -727,6 +733,7 @@ RP_XC_FN int xc_filter(const XcShape &s, d3 pos1, const double *rot1, d3 pos2bc,
         const d3 v0 = sub3(add3(mv3(rot2, c), pos2bc), add3(mv3(rot1, c), pos1));
         d3 w[3];
         bool ok = true;
+        #pragma unroll 1
         for (int k = 0; k < 3 && ok; k++)
             ok = xc_diff_support_cert(s, rot1, pos1, rot2, pos2bc, d3{dirs[k].x, dirs[k].y, dirs[k].z}, w[k]);
         if (ok && face_clearance(w[0], w[1], w[2], v0) > margin && face_clearance(v0, w[1], w[2], w[0]) > margin &&
