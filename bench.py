@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--bulk-staging", type=int, default=-1, choices=[-1, 0, 1],
                     help="stage neighbourhoods with bulk asynchronous copies (1) or per-lane loads (0); "
                          "-1: the engine's default")
+    ap.add_argument("--cell-order", type=int, default=-1, choices=[-1, 0, 1],
+                    help="sweep each phase's cells largest first (1) or in index order (0); -1: the engine's default")
     ap.add_argument("--cells-per-warp", type=int, default=0, choices=[0, 1, 2],
                     help="plain sweeps: 1 = a warp per cell, 2 = a cell per half-warp (0: the library default)")
     ap.add_argument("--no-ordering", action="store_true",
@@ -397,6 +399,8 @@ def main_gpu(args):
         g.set_cells_per_warp(args.cells_per_warp)
     if args.bulk_staging >= 0:
         g.set_bulk_staging(args.bulk_staging == 1)
+    if args.cell_order >= 0:
+        g.set_cell_order(args.cell_order == 1)
     g.box = np.array(box, dtype=np.float64)
     stream = torch.cuda.ExternalStream(g.stream(), device=local)
     seed = args.seed + 7919 * rank

@@ -509,6 +509,11 @@ int rp_set_staging_filter(void *handle, int32_t mode);
  * stream are the same either way; the two-cells-per-warp path and the staging filter always
  * use per-lane loads.  A lost copy sets a device status (RP_ERR_DEVICE) instead of waiting. */
 int rp_set_bulk_staging(void *handle, int32_t on);
+/* The order in which a plain sweep's persistent warps take the cells of a checkerboard phase:
+ * 1 (default) by occupancy, largest first (a counting sort after each grid change, so a phase
+ * ends on short cells), 0 in cell-index order.  Cells of one phase are never neighbours, so
+ * decisions, logs and states are the same either way. */
+int rp_set_cell_order(void *handle, int32_t on);
 
 /* ---- the Monte Carlo cycle loop (Simulation for hard bodies) -----------------------
  *

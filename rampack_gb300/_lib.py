@@ -122,6 +122,7 @@ SIGNATURES = {
     "rp_try_move": (C.c_int, [_P, _P, _D, _D]),
     "rp_set_cells_per_warp": (C.c_int, [_P, C.c_int32]),
     "rp_set_bulk_staging": (C.c_int, [_P, C.c_int32]),
+    "rp_set_cell_order": (C.c_int, [_P, C.c_int32]),
     "rp_set_soft": (C.c_int, [_P, C.c_int32, C.c_double, C.c_double, C.c_int32]),
     "rp_set_temperature": (C.c_int, [_P, C.c_double]),
     "rp_total_energy": (C.c_int, [_P, C.POINTER(C.c_double)]),

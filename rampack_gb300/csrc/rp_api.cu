@@ -222,6 +222,7 @@ struct Handle {
     double *cen64 = nullptr;
     int stage_mode = 1;  // staging filter: 0 off, 1 where it pays (cells well above the range), 2 wherever valid
     int bulk_stage = 0;  // stage neighbourhoods with bulk asynchronous copies
+    int cell_order = 1;  // plain sweeps take each phase's cells by occupancy, largest first
     bool grid_stale = false;  // an upload validated the state; the cell grid is built when first needed
     bool stale_unshifted = false;  // ... and it is built unshifted (not with the last grid's origin)
     uint64_t grid_rebuilds = 0;    // full cell-grid rebuilds (Packing::getNeighbourGridRebuilds)
@@ -548,10 +549,17 @@ int setup_grid(Handle *h, GridHost &G, const double *box, const double *shift) {
     if (ncell > G.cells_alloc) {
         cudaFree(g.count);
         cudaFree(g.start);
-        g.count = g.start = nullptr;
+        cudaFree(g.order);
+        g.count = g.start = g.order = nullptr;
         RP_CUDA(h, cudaMalloc(&g.count, sizeof(int32_t) * ncell));
         RP_CUDA(h, cudaMalloc(&g.start, sizeof(int32_t) * (ncell + 1)));
+        RP_CUDA(h, cudaMalloc(&g.order, sizeof(int32_t) * ncell));
         G.cells_alloc = ncell;
+    }
+    if (!g.order_cnt) {
+        RP_CUDA(h, cudaMalloc(&g.order_cnt, sizeof(int32_t) * 27 * ORDER_BINS));
+        RP_CUDA(h, cudaMalloc(&g.order_off, sizeof(int32_t) * 27 * ORDER_BINS));
+        RP_CUDA(h, cudaMemsetAsync(g.order_cnt, 0, sizeof(int32_t) * 27 * ORDER_BINS, h->stream));
     }
     if (!g.slot_pid) {
         int64_t n = h->n;
@@ -696,6 +704,10 @@ int remap_or_rebuild(Handle *h, int old_g, int ng, int np) {
         RP_CUDA(h, cudaMemcpyAsync(&moved, h->flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
         RP_CUDA(h, cudaStreamSynchronize(h->stream));
         if (!moved) {
+            // the kept cells keep their occupancy order
+            if (g.order && o.order)
+                RP_CUDA(h, cudaMemcpyAsync(g.order, o.order, sizeof(int32_t) * g.ncell, cudaMemcpyDeviceToDevice,
+                                           h->stream));
             h->grid_remaps++;
             return RP_OK;
         }
@@ -772,6 +784,21 @@ SweepArgs base_args(Handle *h) {
     a.overflow = h->overflow;
     a.overflow_count = h->overflow_count;
     return a;
+}
+
+// Where phase ph begins in the grid's occupancy order (phase-major): the cells of the phases
+// before it (a colour digit beyond a dimension's colours names no cells).
+static void order_starts(const GridDev &g, int start[27]) {
+    int acc = 0;
+    for (int ph = 0; ph < 27; ph++) {
+        start[ph] = acc;
+        int cnt = 1;
+        for (int d = 0; d < 3; d++) {
+            const int digit = phase_digit(ph, d);
+            cnt *= digit < ring_ncol(g.dims[d]) ? ring_count(g.dims[d], digit) : 0;
+        }
+        acc += cnt;
+    }
 }
 
 // Re-runs the cells of a phase whose neighbourhood did not fit the normal staging
@@ -1249,6 +1276,9 @@ int rp_destroy(void *handle) {
         GridDev &g = h->grid[i].d;
         cudaFree(g.count);
         cudaFree(g.start);
+        cudaFree(g.order);
+        cudaFree(g.order_cnt);
+        cudaFree(g.order_off);
         cudaFree(g.slot_pid);
         cudaFree(g.pid_slot);
         cudaFree(g.pid_cell);
@@ -1719,6 +1749,9 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
         h->grid_patched = false;
     }
     int phase_no = 0;
+    int order_start[27] = {0};
+    const bool ordered = h->cell_order && !fp64_sweep && g.order;
+    if (ordered) order_starts(g, order_start);
     for (int ph : (fp64_sweep ? std::vector<int>{} : phases)) {
         SweepArgs a = base_args(h);
         if (h->order_mode != RP_ORDER_OFF) a.partners = h->partners;
@@ -1736,6 +1769,11 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
         for (int d = 0; d < 3; d++) {
             a.phase[d] = phase_digit(ph, d);
             a.active[d] = act[d];
+        }
+        if (ordered) {
+            a.work = g.order + order_start[ph];
+            a.work_count = nullptr;
+            a.num_work = a.num_active;
         }
         a.seed = p->seed;
         a.counter = p->counter;
@@ -2493,6 +2531,13 @@ int rp_set_staging_filter(void *handle, int32_t mode) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h || mode < 0 || mode > 2) return fail(h, RP_ERR_ARG, "bad argument");
     h->stage_mode = mode;
+    return RP_OK;
+}
+
+int rp_set_cell_order(void *handle, int32_t on) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || (on != 0 && on != 1)) return fail(h, RP_ERR_ARG, "cell order must be 0 or 1");
+    h->cell_order = on;
     return RP_OK;
 }
 

@@ -63,6 +63,12 @@ struct GridDev {
     double *bounds;       // ActiveDomain bounds: dim d at boundsoff[d], 2 doubles per cell
     int boundsoff[3];
     int32_t *max_occ;     // device scalar
+    // the cells of each checkerboard phase by occupancy, largest first (phase-major), written
+    // by the rebuild's scan; order_cnt [27 x ORDER_BINS] counts (zero between rebuilds),
+    // order_off the ranges' offsets; all null where no order is kept
+    int32_t *order;
+    int32_t *order_cnt;
+    int32_t *order_off;
     // polyspheres
     float4 *mcen;         // [n][ncen] FP32 rotated centre offsets, cell order
     float *cthr;          // [2][MAX_CEN^2] FP32 centre-pair thresholds (r_a + r_b)^2 -/+ margin
@@ -175,6 +181,7 @@ RP_HD int ring_cell(int n, int p, int i) {  // the i-th cell of colour p
     return 3 * i + p;
 }
 RP_HD int phase_digit(int ph, int d) { return d == 0 ? ph % 3 : (d == 1 ? (ph / 3) % 3 : ph / 9); }
+constexpr int ORDER_BINS = 32;  // occupancy bins of the per-phase cell order (the last holds 31 and more)
 RP_HD int cell_phase(const int *dims, int cell) {
     const int cx = cell % dims[0], cy = (cell / dims[0]) % dims[1], cz = cell / (dims[0] * dims[1]);
     return ring_colour(dims[0], cx) + 3 * ring_colour(dims[1], cy) + 9 * ring_colour(dims[2], cz);
@@ -226,8 +233,8 @@ struct SweepArgs {
     // overflow: cells whose neighbourhood exceeds cap are appended here and rerun
     int32_t *overflow;             // [ncell]
     int32_t *overflow_count;
-    const int32_t *work;           // optional explicit list of cells (overflow rerun)
-    const int32_t *work_count;     // device-side length of `work`
+    const int32_t *work;           // optional explicit list of cells (overflow rerun, occupancy order)
+    const int32_t *work_count;     // device-side length of `work` (null: num_work)
     int num_work;
     int32_t *next_item;            // persistent launch: shared cell counter (zeroed per launch)
     // learned ordering: best-ranked partners per particle (pre-tested before the full scan)

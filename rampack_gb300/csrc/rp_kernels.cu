@@ -26,9 +26,22 @@ __global__ void k_validate(DevState s) {
 }
 
 // Two-level exclusive scan of the cell counts (4096 cells per block).
+// Occupancy-order key of a cell: its checkerboard phase, then its occupancy bin (largest
+// first).  Persistent sweep warps take a phase's cells in this order, so the phase ends on
+// short cells; any order of one phase's cells gives the same results (they are never
+// neighbours).
+__device__ __forceinline__ int order_key(const int dims[3], int c, int occ) {
+    return cell_phase(dims, c) * ORDER_BINS + ORDER_BINS - 1 - min(occ, ORDER_BINS - 1);
+}
+
+// Block prefix sums of the cell counts (4096 cells per block); with order_cnt, also the
+// counts of the cells per order key (block-local in shared memory, one global add per key).
 __global__ void k_scan_blocks(const int32_t *count, int32_t *start, int32_t *block_sums, int ncell,
-                              int32_t *max_occ) {
+                              int32_t *max_occ, int3 dims, int32_t *order_cnt) {
     __shared__ int32_t warp_tot[32];
+    __shared__ int32_t okeys[27 * ORDER_BINS];
+    if (order_cnt)
+        for (int i = threadIdx.x; i < 27 * ORDER_BINS; i += blockDim.x) okeys[i] = 0;
     int base = blockIdx.x * 4096 + threadIdx.x * 4;
     int v[4];
     int local_max = 0;
@@ -63,10 +76,20 @@ __global__ void k_scan_blocks(const int32_t *count, int32_t *start, int32_t *blo
         if (base + k < ncell) start[base + k] = run;
         run += v[k];
     }
+    if (order_cnt) {
+        const int d[3] = {dims.x, dims.y, dims.z};
+        for (int k = 0; k < 4; k++)
+            if (base + k < ncell) atomicAdd(&okeys[order_key(d, base + k, v[k])], 1);
+        __syncthreads();
+        for (int i = threadIdx.x; i < 27 * ORDER_BINS; i += blockDim.x)
+            if (okeys[i]) atomicAdd(order_cnt + i, okeys[i]);
+    }
 }
 
-__global__ void k_scan_sums(int32_t *block_sums, int nblocks, int32_t *start, int ncell) {
-    // single block: sequential prefix over the (few) block sums
+// One block: sequential prefix over the (few) block sums; with order_cnt (1024 threads), the
+// exclusive scan of the order keys' counts into order_off, the counts reset to zero.
+__global__ void k_scan_sums(int32_t *block_sums, int nblocks, int32_t *start, int ncell, int32_t *order_cnt,
+                            int32_t *order_off) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         int run = 0;
         for (int b = 0; b < nblocks; b++) {
@@ -76,11 +99,52 @@ __global__ void k_scan_sums(int32_t *block_sums, int nblocks, int32_t *start, in
         }
         start[ncell] = run;
     }
+    if (!order_cnt) return;
+    static_assert(27 * ORDER_BINS <= 1024, "one thread per order key");
+    __shared__ int32_t warp_sum[32];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int v = t < 27 * ORDER_BINS ? order_cnt[t] : 0;
+    int incl = v;
+    for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += y;
+    }
+    if (lane == 31) warp_sum[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        int x = warp_sum[lane];
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, d);
+            if (lane >= d) x += y;
+        }
+        warp_sum[lane] = x;  // inclusive over warps
+    }
+    __syncthreads();
+    if (t < 27 * ORDER_BINS) {
+        order_off[t] = (w > 0 ? warp_sum[w - 1] : 0) + incl - v;
+        order_cnt[t] = 0;
+    }
 }
 
-__global__ void k_scan_add(int32_t *start, const int32_t *block_sums, int ncell) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+// Block offsets added to the cell starts; with order, each cell placed in its key's range
+// (ranks block-local in shared memory, one global reservation per key and block).
+__global__ void __launch_bounds__(256) k_scan_add(int32_t *start, const int32_t *block_sums, int ncell,
+                                                   const int32_t *count, int3 dims, int32_t *order_off,
+                                                   int32_t *order) {
+    __shared__ int32_t okeys[27 * ORDER_BINS], obase[27 * ORDER_BINS];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < ncell) start[i] += block_sums[i / 4096];
+    if (!order) return;
+    for (int k = threadIdx.x; k < 27 * ORDER_BINS; k += blockDim.x) okeys[k] = 0;
+    __syncthreads();
+    const int d[3] = {dims.x, dims.y, dims.z};
+    const int key = i < ncell ? order_key(d, i, count[i]) : -1;
+    const int rank = key >= 0 ? atomicAdd(&okeys[key], 1) : 0;
+    __syncthreads();
+    for (int k = threadIdx.x; k < 27 * ORDER_BINS; k += blockDim.x)
+        if (okeys[k]) obase[k] = atomicAdd(order_off + k, okeys[k]);
+    __syncthreads();
+    if (key >= 0) order[obase[key] + rank] = i;
 }
 
 __global__ void k_scatter(DevState s, GridDev g) {
@@ -235,7 +299,7 @@ __global__ void __launch_bounds__(SWEEP_WARPS * 32, SWEEP_MIN_BLOCKS) k_sweep(co
     uint16_t *pstage = reinterpret_cast<uint16_t *>(nacc + A.cap);  // LEARN only: MLP_PARTNERS x cap
     // polyspheres: after the partner slots when the learned ordering is on
     float4 *wx = reinterpret_cast<float4 *>(nacc + A.cap) + (LEARN ? A.cap / 4 : 0);
-    int nitems = A.work ? *A.work_count : (LIST ? A.num_list : A.num_active);
+    int nitems = A.work ? (A.work_count ? *A.work_count : A.num_work) : (LIST ? A.num_list : A.num_active);
     WarpStats ws{};
     __shared__ uint64_t stage_bar[SWEEP_WARPS];
     if (GW == 32 && A.bulk_stage) {
@@ -293,9 +357,14 @@ cudaError_t launch_rebuild(const DevState &s, const GridDev &g, int32_t *block_s
     cudaMemsetAsync(g.max_occ, 0, sizeof(int32_t), st);
     k_assign<<<nb, tb, 0, st>>>(s, g);
     int nblocks = (g.ncell + 4095) / 4096;
-    k_scan_blocks<<<nblocks, 1024, 0, st>>>(g.count, g.start, block_sums, g.ncell, g.max_occ);
-    k_scan_sums<<<1, 32, 0, st>>>(block_sums, nblocks, g.start, g.ncell);
-    k_scan_add<<<(g.ncell + 255) / 256, 256, 0, st>>>(g.start, block_sums, g.ncell);
+    const int3 dims = make_int3(g.dims[0], g.dims[1], g.dims[2]);
+    const bool ord = g.order && g.order_cnt && g.order_off;
+    k_scan_blocks<<<nblocks, 1024, 0, st>>>(g.count, g.start, block_sums, g.ncell, g.max_occ, dims,
+                                             ord ? g.order_cnt : nullptr);
+    k_scan_sums<<<1, ord ? 1024 : 32, 0, st>>>(block_sums, nblocks, g.start, g.ncell, ord ? g.order_cnt : nullptr,
+                                                ord ? g.order_off : nullptr);
+    k_scan_add<<<(g.ncell + 255) / 256, 256, 0, st>>>(g.start, block_sums, g.ncell, g.count, dims,
+                                                      ord ? g.order_off : nullptr, ord ? g.order : nullptr);
     k_scatter<<<nb, tb, 0, st>>>(s, g);
     k_cell_finish<<<(g.ncell + 127) / 128, 128, 0, st>>>(s, g);
     return cudaGetLastError();
@@ -312,9 +381,10 @@ cudaError_t launch_remap(const DevState &s, const GridDev &g, const GridDev &old
 cudaError_t launch_cell_scan(const int32_t *count, int32_t *start, int32_t *block_sums, int ncell,
                              int32_t *max_occ, cudaStream_t st) {
     int nblocks = (ncell + 4095) / 4096;
-    k_scan_blocks<<<nblocks, 1024, 0, st>>>(count, start, block_sums, ncell, max_occ);
-    k_scan_sums<<<1, 32, 0, st>>>(block_sums, nblocks, start, ncell);
-    k_scan_add<<<(ncell + 255) / 256, 256, 0, st>>>(start, block_sums, ncell);
+    k_scan_blocks<<<nblocks, 1024, 0, st>>>(count, start, block_sums, ncell, max_occ, make_int3(1, 1, 1), nullptr);
+    k_scan_sums<<<1, 32, 0, st>>>(block_sums, nblocks, start, ncell, nullptr, nullptr);
+    k_scan_add<<<(ncell + 255) / 256, 256, 0, st>>>(start, block_sums, ncell, nullptr, make_int3(1, 1, 1), nullptr,
+                                                      nullptr);
     return cudaGetLastError();
 }
 

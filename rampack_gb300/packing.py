@@ -245,6 +245,11 @@ class GpuPacking:
         (rp_set_bulk_staging)."""
         self._check(self.lib.rp_set_bulk_staging(self.h, 1 if on else 0))
 
+    def set_cell_order(self, on: bool):
+        """Sweep each phase's cells by occupancy, largest first (1), or in index order (0)
+        (rp_set_cell_order)."""
+        self._check(self.lib.rp_set_cell_order(self.h, 1 if on else 0))
+
     def set_cells_per_warp(self, cells: int):
         """1: a warp sweeps one cell; 2: each half-warp sweeps its own (rp_set_cells_per_warp)."""
         self._check(self.lib.rp_set_cells_per_warp(self.h, int(cells)))
