@@ -504,7 +504,8 @@ cudaError_t launch_sweep_half(const SweepArgs &a, int ncells, cudaStream_t st) {
 
 cudaError_t launch_sweep(const SweepArgs &a, bool list, int nwarps, cudaStream_t st) {
     if (nwarps <= 0) return cudaSuccess;
-    const int wpb = a.work ? 1 : SWEEP_WARPS;
+    // the overflow rerun (large capacity, device-side count): one warp per block
+    const int wpb = (a.work && a.work_count) ? 1 : SWEEP_WARPS;
     const bool count = a.s.counting != 0;
     // rototranslation sweeps have their own plain scan (no learned pre-test, no pair log)
     const bool rt = !list && !count && a.types == SWEEP_ROTOTRANSLATION;
