@@ -1733,6 +1733,9 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
             sa.log_codes = h->d_log_codes;
         }
         int soft_phase = 0;
+        int soft_start[27] = {0};
+        const bool soft_ordered = h->cell_order && g.order;
+        if (soft_ordered) order_starts(g, soft_start);
         for (int ph : phases) {
             int act[3];
             sa.num_active = phase_cells(g, ph, act);
@@ -1740,6 +1743,7 @@ int rp_sweep(void *handle, const rp_sweep_params *p, rp_sweep_stats *stats) {
                 sa.phase[d] = phase_digit(ph, d);
                 sa.active[d] = act[d];
             }
+            sa.work = soft_ordered ? g.order + soft_start[ph] : nullptr;
             sa.next_item = h->item_counters + soft_phase++;
             Group grp(h, RP_KERNEL_SWEEP, 1);
             RP_CUDA(h, launch_soft_sweep(sa, std::min(sa.num_active, h->num_sms * 16), h->stream));

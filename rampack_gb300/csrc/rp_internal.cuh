@@ -291,6 +291,7 @@ struct SoftSweepArgs {
     uint32_t rtab_mask;
     rp_move *log;
     uint8_t *log_codes;
+    const int32_t *work;           // the phase's cells by occupancy, largest first (null: index order)
 };
 
 // One replica of a batched launch (rp_batch_*): its sweep arguments, this sweep's phase

@@ -676,7 +676,12 @@ __global__ void __launch_bounds__(SOFT_WARPS * 32, 4) k_soft_sweep(SoftSweepArgs
         item = __shfl_sync(FULL, item, 0);
         if (item >= A.num_active) break;
         int c[3];
-        {
+        if (A.work) {  // the phase's cells by occupancy, largest first
+            const int w = A.work[item];
+            c[0] = w % G.dims[0];
+            c[1] = (w / G.dims[0]) % G.dims[1];
+            c[2] = w / (G.dims[0] * G.dims[1]);
+        } else {
             int w = item;
             const int a0 = w % A.active[0];
             w /= A.active[0];
