@@ -506,8 +506,9 @@ int rp_set_staging_filter(void *handle, int32_t mode);
 /* How a sweep stages each cell's 3x3x3 neighbourhood into shared memory: 1 with bulk
  * asynchronous copies (cp.async.bulk, one per neighbour cell and array, completing on an
  * mbarrier with a bounded wait), 0 with per-lane loads.  Decisions, states and the proposal
- * stream are the same either way; the two-cells-per-warp path and the staging filter always
- * use per-lane loads.  A lost copy sets a device status (RP_ERR_DEVICE) instead of waiting. */
+ * stream are the same either way; the two-cells-per-warp path, the staging filter, the FP64
+ * sweeps (soft parts, convex bodies) and batched replicas always use per-lane loads.  A lost
+ * copy sets a device status (RP_ERR_DEVICE) instead of waiting. */
 int rp_set_bulk_staging(void *handle, int32_t on);
 /* The order in which a plain sweep's persistent warps take the cells of a checkerboard phase:
  * 1 (default) by occupancy, largest first (a counting sort after each grid change, so a phase
