@@ -193,6 +193,7 @@ constexpr int SWEEP_POLY_SCRATCH = MAX_CEN + MAX_CEN * MAX_CEN / 2 + 3 * MAX_CEN
 
 constexpr int NUM_COUNTERS = 9;     // sweep statistics words per handle (rp_sweep_stats order)
 constexpr int SWEEP_WARPS = 4;       // warps per block of the sweep kernel
+constexpr int SWEEP_P1 = 4;          // candidates per lane per round of the sweep's FP32 centre pass
 constexpr int SWEEP_MIN_BLOCKS = 4;  // resident blocks per SM the register budget allows
 constexpr int MIRROR_ROUNDINGS = 4;  // FP32 mirror updates per particle and sweep before an exact refresh
 constexpr uint32_t ROT_TABLE = 65536;  // rotations drawn per sweep (plus their inverses); at most 2^16

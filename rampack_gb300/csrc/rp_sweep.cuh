@@ -635,43 +635,44 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
             if (grp.ballot(cls == 1)) overlap = true;
         }
 
-        // ---- FP32 pass 1: centre distances, two candidates per lane per round ----
+        // ---- FP32 pass 1: centre distances, SWEEP_P1 candidates per lane per round (independent
+        //      tests in flight), queued in candidate order ----
         int nseg = 0, nun = 0;
         if (!COUNT && dom != 1 && !overlap) {
-            for (int base = 0; base < total; base += 2 * GW) {
-                int k0 = base + lane, k1 = base + GW + lane;
-                int c0 = 0, c1 = 0;
-                if (lane == 0) ws.pairs += (unsigned)min(2 * GW, total - base);
-                if (k0 < total) {
-                    float4 q = cpos[k0];
-                    if (__float_as_int(q.w) != pid) {
-                        float dx = q.x - pn.x, dy = q.y - pn.y, dz = q.z - pn.z;
-                        c0 = A.fp64_only ? 2 : d2_stage<KIND>(S.fc, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+            for (int base = 0; base < total; base += SWEEP_P1 * GW) {
+                int cl[SWEEP_P1];
+#pragma unroll
+                for (int u = 0; u < SWEEP_P1; u++) {
+                    const int k = base + u * GW + lane;
+                    cl[u] = 0;
+                    if (k < total) {
+                        const float4 q = cpos[k];
+                        if (__float_as_int(q.w) != pid) {
+                            const float dx = q.x - pn.x, dy = q.y - pn.y, dz = q.z - pn.z;
+                            cl[u] = A.fp64_only ? 2 : d2_stage<KIND>(S.fc, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+                        }
                     }
                 }
-                if (k1 < total) {
-                    float4 q = cpos[k1];
-                    if (__float_as_int(q.w) != pid) {
-                        float dx = q.x - pn.x, dy = q.y - pn.y, dz = q.z - pn.z;
-                        c1 = A.fp64_only ? 2 : d2_stage<KIND>(S.fc, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-                    }
-                }
-                if (grp.ballot(c0 == 1 || c1 == 1)) {
+                if (lane == 0) ws.pairs += (unsigned)min(SWEEP_P1 * GW, total - base);
+                bool hit = false;
+#pragma unroll
+                for (int u = 0; u < SWEEP_P1; u++) hit = hit || cl[u] == 1;
+                if (grp.ballot(hit)) {
                     overlap = true;
                     break;
                 }
-                if (KIND >= 1) {
-                    unsigned b0 = grp.ballot(c0 == 3), b1 = grp.ballot(c1 == 3);
-                    if (c0 == 3) qseg[nseg + __popc(b0 & lt)] = (uint16_t)k0;
-                    nseg += __popc(b0);
-                    if (c1 == 3) qseg[nseg + __popc(b1 & lt)] = (uint16_t)k1;
-                    nseg += __popc(b1);
+#pragma unroll
+                for (int u = 0; u < SWEEP_P1; u++) {
+                    const int k = base + u * GW + lane;
+                    if (KIND >= 1) {
+                        const unsigned bs = grp.ballot(cl[u] == 3);
+                        if (cl[u] == 3) qseg[nseg + __popc(bs & lt)] = (uint16_t)k;
+                        nseg += __popc(bs);
+                    }
+                    const unsigned bu = grp.ballot(cl[u] == 2);
+                    if (cl[u] == 2) qun[nun + __popc(bu & lt)] = (uint16_t)k;
+                    nun += __popc(bu);
                 }
-                unsigned u0 = grp.ballot(c0 == 2), u1 = grp.ballot(c1 == 2);
-                if (c0 == 2) qun[nun + __popc(u0 & lt)] = (uint16_t)k0;
-                nun += __popc(u0);
-                if (c1 == 2) qun[nun + __popc(u1 & lt)] = (uint16_t)k1;
-                nun += __popc(u1);
             }
         }
         grp.sync();
