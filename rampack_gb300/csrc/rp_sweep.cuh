@@ -726,8 +726,36 @@ __device__ __forceinline__ void sweep_cell(const SweepArgs &A, const int item, c
             }
             grp.sync();
         }
-        // ---- FP32 pass 2 (spherocylinders): segment distances on full warps ----
-        if (!COUNT && KIND == 1 && !overlap) {
+        // ---- FP32 pass 2 (spherocylinders): segment distances on full warps, two per lane per
+        //      round (the queued order; the learned-ordering log keeps one per lane) ----
+        if (!COUNT && KIND == 1 && !overlap && !LEARN) {
+            for (int base = 0; base < nseg; base += 2 * GW) {
+                int cls[2] = {0, 0}, kk[2] = {0, 0};
+#pragma unroll
+                for (int u = 0; u < 2; u++) {
+                    const int i = base + u * GW + lane;
+                    if (i < nseg) {
+                        kk[u] = qseg[i];
+                        const float4 q = cpos[kk[u]];
+                        const float4 a = AXM ? G.maxis[cslot[kk[u]]] : cax[kk[u]];
+                        cls[u] = seg_stage(S.fc, make_float3(q.x - pn.x, q.y - pn.y, q.z - pn.z), an,
+                                           make_float3(a.x, a.y, a.z));
+                    }
+                }
+                if (grp.ballot(cls[0] == 1 || cls[1] == 1)) {
+                    overlap = true;
+                    break;
+                }
+#pragma unroll
+                for (int u = 0; u < 2; u++) {
+                    const unsigned b2 = grp.ballot(cls[u] == 2);
+                    if (cls[u] == 2) qun[nun + __popc(b2 & lt)] = (uint16_t)kk[u];
+                    nun += __popc(b2);
+                }
+            }
+            grp.sync();
+        }
+        if (!COUNT && KIND == 1 && !overlap && LEARN) {
             for (int base = 0; base < nseg; base += GW) {
                 int i = base + lane;
                 int cls = 0, k = 0;
